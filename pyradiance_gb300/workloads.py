@@ -1,0 +1,197 @@
+"""Seeded synthetic scenes, sensor grids and matrices for the hot path.
+
+Every generator is a pure function of its arguments (numpy ``default_rng``
+seeded explicitly), so the same scene text, sensor file or matrix is produced
+on any machine.  The scene text is plain Radiance scene description (``.rad``)
+that the reference ``oconv`` and this package's own octree builder both read.
+
+Workloads (sizes are the defaults):
+
+* ``daylight_room`` -- 10 x 8 x 3 m closed room of 6 polygons (gray plastic
+  0.5); 200 axis-aligned boxes (1,200 quads) with sizes U[0.2, 1.5] m and
+  reflectance U[0.2, 0.7], standing 2-20 mm above the floor (bottoms that
+  are coplanar with the floor and with each other, where boxes overlap,
+  make oconv subdivide to its resolution limit); one 1 x 1 m ``light`` polygon of
+  radiance 100 at the ceiling centre, coplanar with the ceiling and facing
+  down.  Its modifier is defined last, so under Radiance's tie rule ("later
+  modifier wins", rt/raytrace.c:573) the light, not the ceiling, is the
+  surface hit where the two coincide.
+* ``window_room`` -- the same room shell with a 3 x 2 m glass window
+  (transmissivity 0.6) cut into the south (y = 0) wall, 20,000 random
+  interior triangles (two edges of length U[0.05, 0.5] m from a random
+  vertex, reflectance U[0.1, 0.8], one material each), and the glow sky and
+  ground of the reference's own test fixture (tests/Resources/skyglow.rad).
+* ``sensor_grid`` -- cell-centred n x m grid at z = 0.8 facing +z.
+* ``dc_sky`` -- daylight-coefficient and sky matrices with the value
+  distributions of the annual dctimestep workload.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+ROOM = (10.0, 8.0, 3.0)
+
+
+def _poly(mod: str, name: str, verts) -> str:
+    flat = " ".join(f"{v:.9g}" for p in verts for v in p)
+    return f"{mod} polygon {name}\n0\n0\n{3 * len(verts)} {flat}\n\n"
+
+
+def _mat_plastic(name: str, rho) -> str:
+    r, g, b = rho
+    return f"void plastic {name}\n0\n0\n5 {r:.9g} {g:.9g} {b:.9g} 0 0\n\n"
+
+
+def _room_shell(mod: str, window=None) -> str:
+    """Six inward-facing polygons; with ``window`` = (x0, x1, z0, z1) the
+    south wall is split into four polygons around that opening."""
+    X, Y, Z = ROOM
+    out = []
+    out.append(_poly(mod, "floor", [(0, 0, 0), (X, 0, 0), (X, Y, 0), (0, Y, 0)]))
+    out.append(_poly(mod, "ceiling", [(0, 0, Z), (0, Y, Z), (X, Y, Z), (X, 0, Z)]))
+    out.append(_poly(mod, "north", [(0, Y, 0), (X, Y, 0), (X, Y, Z), (0, Y, Z)]))
+    out.append(_poly(mod, "west", [(0, 0, 0), (0, Y, 0), (0, Y, Z), (0, 0, Z)]))
+    out.append(_poly(mod, "east", [(X, 0, 0), (X, 0, Z), (X, Y, Z), (X, Y, 0)]))
+    if window is None:
+        out.append(_poly(mod, "south", [(0, 0, 0), (0, 0, Z), (X, 0, Z), (X, 0, 0)]))
+    else:
+        x0, x1, z0, z1 = window
+        out.append(_poly(mod, "south_l", [(0, 0, 0), (0, 0, Z), (x0, 0, Z), (x0, 0, 0)]))
+        out.append(_poly(mod, "south_r", [(x1, 0, 0), (x1, 0, Z), (X, 0, Z), (X, 0, 0)]))
+        out.append(_poly(mod, "south_b", [(x0, 0, 0), (x0, 0, z0), (x1, 0, z0), (x1, 0, 0)]))
+        out.append(_poly(mod, "south_t", [(x0, 0, z1), (x0, 0, Z), (x1, 0, Z), (x1, 0, z1)]))
+    return "".join(out)
+
+
+def _box(mod: str, name: str, o, s) -> str:
+    """Axis-aligned box as 6 outward-facing quads."""
+    x0, y0, z0 = o
+    x1, y1, z1 = o[0] + s[0], o[1] + s[1], o[2] + s[2]
+    q = []
+    q.append(_poly(mod, f"{name}.bot", [(x0, y0, z0), (x0, y1, z0), (x1, y1, z0), (x1, y0, z0)]))
+    q.append(_poly(mod, f"{name}.top", [(x0, y0, z1), (x1, y0, z1), (x1, y1, z1), (x0, y1, z1)]))
+    q.append(_poly(mod, f"{name}.s", [(x0, y0, z0), (x1, y0, z0), (x1, y0, z1), (x0, y0, z1)]))
+    q.append(_poly(mod, f"{name}.n", [(x0, y1, z0), (x0, y1, z1), (x1, y1, z1), (x1, y1, z0)]))
+    q.append(_poly(mod, f"{name}.w", [(x0, y0, z0), (x0, y0, z1), (x0, y1, z1), (x0, y1, z0)]))
+    q.append(_poly(mod, f"{name}.e", [(x1, y0, z0), (x1, y1, z0), (x1, y1, z1), (x1, y0, z1)]))
+    return "".join(q)
+
+
+SKY_GLOW = """void glow skyglow
+0
+0
+4 1 1 1 0
+
+void glow groundglow
+0
+0
+4 1 1 1 0
+
+skyglow source sky
+0
+0
+4 0 0 1 180
+
+groundglow source ground
+0
+0
+4 0 0 -1 180
+
+"""
+
+
+def daylight_room(seed: int = 0, nboxes: int = 200, light: bool = True) -> str:
+    """Room + floor-standing boxes + ceiling light (the direct-irradiance
+    workload).  Returns Radiance scene text."""
+    rng = np.random.default_rng(seed)
+    X, Y, Z = ROOM
+    out = [_mat_plastic("room_mat", (0.5, 0.5, 0.5)), _room_shell("room_mat")]
+    sizes = rng.uniform(0.2, 1.5, size=(nboxes, 3))
+    fx = rng.uniform(0.0, 1.0, size=nboxes)
+    fy = rng.uniform(0.0, 1.0, size=nboxes)
+    rho = rng.uniform(0.2, 0.7, size=nboxes)
+    lift = rng.uniform(0.002, 0.02, size=nboxes)
+    for i in range(nboxes):
+        s = sizes[i]
+        o = (fx[i] * (X - s[0]), fy[i] * (Y - s[1]), lift[i])
+        out.append(_mat_plastic(f"box_mat{i}", (rho[i],) * 3))
+        out.append(_box(f"box_mat{i}", f"box{i}", o, s))
+    if light:
+        out.append("void light light_mat\n0\n0\n3 100 100 100\n\n")
+        cx, cy = X / 2, Y / 2
+        out.append(_poly("light_mat", "light", [(cx - .5, cy - .5, Z), (cx - .5, cy + .5, Z),
+                                                (cx + .5, cy + .5, Z), (cx + .5, cy - .5, Z)]))
+    return "".join(out)
+
+
+WINDOW = (3.5, 6.5, 0.5, 2.5)
+
+
+def window_room(seed: int = 0, ntri: int = 20000, nmat: int | None = None) -> str:
+    """Room shell with a glass window in the south wall, random interior
+    triangles and the glow sky/ground.  ``nmat`` groups the triangles into
+    that many materials (default: one material per triangle)."""
+    rng = np.random.default_rng(seed)
+    X, Y, Z = ROOM
+    out = [_mat_plastic("room_mat", (0.5, 0.5, 0.5)), _room_shell("room_mat", WINDOW)]
+    out.append("void glass window_glass\n0\n0\n3 .6 .6 .6\n\n")
+    x0, x1, z0, z1 = WINDOW
+    out.append(_poly("window_glass", "window", [(x0, 0, z0), (x0, 0, z1), (x1, 0, z1), (x1, 0, z0)]))
+    margin = 0.05
+    v0 = rng.uniform((margin, margin, margin), (X - margin, Y - margin, Z - margin), size=(ntri, 3))
+    lens = rng.uniform(0.05, 0.5, size=(ntri, 2))
+    dirs = rng.normal(size=(ntri, 2, 3))
+    dirs /= np.linalg.norm(dirs, axis=2, keepdims=True)
+    v1 = v0 + lens[:, 0:1] * dirs[:, 0]
+    v2 = v0 + lens[:, 1:2] * dirs[:, 1]
+    lo, hi = np.array([1e-3] * 3), np.array([X - 1e-3, Y - 1e-3, Z - 1e-3])
+    v1 = np.clip(v1, lo, hi)
+    v2 = np.clip(v2, lo, hi)
+    nm = ntri if nmat is None else nmat
+    rho = rng.uniform(0.1, 0.8, size=nm)
+    for m in range(nm):
+        out.append(_mat_plastic(f"tri_mat{m}", (rho[m],) * 3))
+    for i in range(ntri):
+        out.append(_poly(f"tri_mat{i % nm}", f"tri{i}", [v0[i], v1[i], v2[i]]))
+    out.append(SKY_GLOW)
+    return "".join(out)
+
+
+def sensor_grid(nx: int, ny: int, z: float = 0.8) -> np.ndarray:
+    """(nx*ny, 6) float64 array of ``ox oy oz dx dy dz``, cell-centred over
+    the room floor plan, facing +z, row-major in y then x."""
+    X, Y, _ = ROOM
+    xs = (np.arange(nx) + 0.5) * (X / nx)
+    ys = (np.arange(ny) + 0.5) * (Y / ny)
+    gx, gy = np.meshgrid(xs, ys)
+    n = nx * ny
+    out = np.zeros((n, 6))
+    out[:, 0] = gx.ravel()
+    out[:, 1] = gy.ravel()
+    out[:, 2] = z
+    out[:, 5] = 1.0
+    return out
+
+
+def rays_ascii(rays: np.ndarray) -> bytes:
+    return "".join(" ".join(f"{v:.17g}" for v in r) + "\n" for r in rays).encode()
+
+
+def dc_sky(M: int, K: int, N: int, seed: int = 0):
+    """Daylight-coefficient matrix (M, K, 3) and sky matrix (K, N, 3), float32.
+
+    DC: lognormal(mu=-6, sigma=2) with 30% of the (row, patch) entries exactly
+    zero in all three channels.  Sky: for each hour column, a diffuse
+    lognormal(mu=2, sigma=1) background plus a sun spike log-uniform in
+    [1e4, 1e6] on one random patch; about half the columns (night) all zero.
+    """
+    rng = np.random.default_rng(seed)
+    dc = rng.lognormal(-6.0, 2.0, size=(M, K, 3)).astype(np.float32)
+    dc[rng.random((M, K)) < 0.3] = 0.0
+    sky = rng.lognormal(2.0, 1.0, size=(K, N, 3)).astype(np.float32)
+    sun = rng.integers(0, K, size=N)
+    spike = np.exp(rng.uniform(np.log(1e4), np.log(1e6), size=N)).astype(np.float32)
+    sky[sun, np.arange(N), :] += spike[:, None]
+    night = rng.random(N) < 0.5
+    sky[:, night, :] = 0.0
+    return dc, sky
