@@ -1,0 +1,136 @@
+/*
+ * gbrad.h -- C ABI of the GB300 ray-tracing library (libgbrad.so).
+ *
+ * Plain pointers and sizes only.  Every function returns 0 on success or a
+ * negative GB_E* code; gb_last_error() gives the message of the last failure
+ * on the calling thread.  The caller owns every host buffer; a gb_scene owns
+ * its device copy of the scene and its work buffers until gb_scene_free().
+ * Calls on one scene are serialised by the caller (one CUDA stream each).
+ *
+ * The entry points stand in for the programs pyradiance runs as
+ * subprocesses (src/pyradiance/rt.py:278-362 rtrace, rt.py:165-235
+ * Rcontrib, src/pyradiance/util.py:140-192 dctimestep); see each entry.
+ */
+#ifndef GBRAD_H
+#define GBRAD_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GB_OK            0
+#define GB_EINVAL       -1   /* bad argument or option */
+#define GB_EIO          -2   /* cannot read a file, malformed octree or scene */
+#define GB_EUNSUPPORTED -3   /* valid input the GPU path does not implement */
+#define GB_ECUDA        -4   /* CUDA runtime failure */
+#define GB_ENOMEM       -5   /* device or host allocation failed */
+#define GB_EOVERFLOW    -6   /* a work queue or a limit overflowed */
+
+#define GB_PROG_RTRACE   0
+#define GB_PROG_RCONTRIB 1
+
+/* Options shared by rtrace and rcontrib.  Field meanings and defaults follow
+ * the reference: rt/raycalls.c:121-150 (rtrace defaults), rt/rcontrib.c:24-58
+ * and rt/rcmain.c:164-172 (rcontrib defaults and overrides), option letters
+ * as parsed by rt/renderopts.c:123-340, rt/rtmain.c:144-330 and
+ * rt/rcmain.c:207-320. */
+typedef struct {
+    int    prog;            /* GB_PROG_* the defaults came from */
+    int    ab, ad, as, ar, aw;
+    double aa;
+    double av[3];
+    int    lr;              /* maxdepth */
+    double lw;              /* minweight */
+    double dj, ds, dt, dc;  /* dstrsrc, srcsizerat, shadthresh, shadcert */
+    int    dr, dp, dv;
+    double st, ss;          /* specthresh, specjitter */
+    int    bv;              /* back face visibility */
+    int    I;               /* -I: irradiance at the sensor point */
+    int    i;               /* -i: irradiance at the hit surface */
+    int    u;               /* -u: uncorrelated (time-seeded) sampling */
+    int    h;               /* header output */
+    int    n;               /* processes requested (informational) */
+    int    c;               /* rcontrib -c: rays accumulated per record */
+    int    V;               /* rcontrib -V: contributions, not coefficients */
+    char   fin, fout;       /* -f{a,f,d}{a,f,d,c} */
+    char   outspec[32];     /* rtrace -o spec */
+    int    x, y;            /* flush interval / resolution */
+    double ld;              /* unused: -ld (limit distance) flag */
+    uint64_t seed;          /* random stream key; set from -u */
+    uint32_t replica;       /* independent replica index of the stream */
+} gb_opts;
+
+/* One rcontrib modifier (rt/rcontrib.c:92-159 addmodifier, argument order of
+ * rt.py:190-228: -f calfile -e expr -bn nbins -b binv -p params -m mod). */
+typedef struct {
+    const char *modifier;   /* modifier name to track */
+    const char *binv;       /* bin expression, NULL = "0" */
+    const char *nbins;      /* bin count expression (-bn), NULL = from a constant binv */
+    const char *params;     /* -p settings "MF=1,rNz=-1,..." or NULL */
+    const char *calfile;    /* -f file (reinhartb.cal is built in) or NULL */
+    const char *expr;       /* -e definitions or NULL */
+} gb_modspec;
+
+typedef struct gb_scene gb_scene;
+
+/* Load a Radiance octree, frozen or not (common/readoct.c:29, the readoct()
+ * call of rt/rtmain.c and rt/rcmain.c:352). */
+int  gb_scene_load(const char *oct_path, gb_scene **out);
+/* Build the octree from scene text files as oconv does (ot/oconv.c:42-180),
+ * then load it.  objlim <= 0 and resolu <= 0 select oconv's 6 and 16384. */
+int  gb_scene_load_rad(const char *const *paths, int npaths, int objlim, int resolu, gb_scene **out);
+void gb_scene_free(gb_scene *scene);
+/* Number of objects; name, modifier name and material name of an object
+ * (the -os/-om/-oM outputs of rt/rtrace.c:824-860). */
+int64_t     gb_scene_nobjects(const gb_scene *scene);
+const char *gb_scene_object_name(const gb_scene *scene, int64_t obj);
+const char *gb_scene_modifier_name(const gb_scene *scene, int64_t obj);
+const char *gb_scene_material_name(const gb_scene *scene, int64_t obj);
+
+/* Parse options; consumed arguments are counted in *nused, the first
+ * non-option (the octree) stops parsing.  prog selects the defaults. */
+int  gb_opts_default(int prog, gb_opts *out);
+int  gb_opts_parse(int argc, const char *const *argv, int prog, gb_opts *out, int *nused);
+
+/* rtrace over n rays (org_dir: n x 6 doubles, ox oy oz dx dy dz): the -ov
+ * value (n x 3 doubles) and the first-hit object of each ray cast forward
+ * (hit_id, -1 for none; hit_t distance).  Any output pointer may be NULL.
+ * Replaces rt/rtrace.c:146-236 (rtrace) and :436-468 (rtcompute). */
+int  gb_rtrace(gb_scene *scene, const gb_opts *opts, const double *org_dir, int64_t n,
+               double *out_rgb, int32_t *hit_id, double *hit_t);
+
+/* rcontrib: out has (n / opts->c) records x (sum of nbins) x 3 doubles,
+ * modifiers in the given order (rt/rcontrib.c:379-427, rt/rc2.c:294-357).
+ * ray_count (optional) receives the number of rays traced. */
+int  gb_rcontrib(gb_scene *scene, const gb_opts *opts, const gb_modspec *mods, int nmods,
+                 const double *org_dir, int64_t n, double *out, int64_t *ray_count);
+/* Total bins of a modifier list (validates the bin expressions). */
+int  gb_rcontrib_nbins(const gb_modspec *mods, int nmods, int *nbins_total);
+
+/* dctimestep's two-matrix product R[m,n,c] = sum_k DC[m,k,c] * S[k,n,c]
+ * (util/dctimestep.c:324-393, util/cmatrix.c:421-474); all matrices are
+ * interleaved RGB float32 (row-major, 3 floats per element).  mode selects
+ * the arithmetic: GB_DCT_FP32 (FP32 FMA), GB_DCT_BF16X3 (bf16 split,
+ * 3 tensor-core products, FP32 accumulate), GB_DCT_FP64 (FP64 FMA). */
+#define GB_DCT_FP32  0
+#define GB_DCT_BF16X3 1
+#define GB_DCT_FP64  2
+int  gb_dctimestep(const float *dc, const float *sky, int64_t M, int64_t K, int64_t N, int mode,
+                   float *out);
+/* Same on device pointers already resident in HBM (no copies). */
+int  gb_dctimestep_device(const float *d_dc, const float *d_sky, int64_t M, int64_t K, int64_t N,
+                          int mode, float *d_out, void *stream);
+
+/* Counters of the last call on this thread: rays traced, cube steps,
+ * contributions binned, kernel launches. */
+int  gb_last_stats(int64_t *rays, int64_t *steps, int64_t *contribs, int64_t *launches);
+
+const char *gb_last_error(void);
+const char *gb_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,420 @@
+"""GB300 drop-in for pyradiance's ray-tracing hot path.
+
+``rtrace``, ``Rcontrib`` and ``dctimestep`` keep the call signatures, option
+semantics and byte formats of ``pyradiance.rtrace``
+(src/pyradiance/rt.py:278-362), ``pyradiance.Rcontrib`` (rt.py:165-235) and
+``pyradiance.dctimestep`` (src/pyradiance/util.py:140-192), but run in
+process on the GPU through ``libgbrad.so`` instead of spawning the Radiance
+programs.  Errors raise ``RuntimeError`` as the reference's
+``handle_called_process_error`` does (src/pyradiance/anci.py:13-29).
+"""
+from __future__ import annotations
+
+import os
+import time
+from pathlib import Path
+from typing import Sequence
+
+import numpy as np
+
+from . import _lib
+from ._lib import GbError, GbModspec, Scene, check, last_stats, lib, parse_opts, ptr
+
+__all__ = ["rtrace", "Rcontrib", "dctimestep", "Scene", "load_scene", "read_rays", "GbError", "last_stats"]
+
+_SCENES: dict = {}
+
+
+def load_scene(octree) -> Scene:
+    """Scene for an octree path (cached per path and modification time) or
+    for a list of scene text files (octree built on the host)."""
+    if isinstance(octree, Scene):
+        return octree
+    if isinstance(octree, (list, tuple)):
+        return Scene(rad_files=octree)
+    p = str(octree)
+    key = (os.path.abspath(p), os.path.getmtime(p) if os.path.exists(p) else 0)
+    sc = _SCENES.get(key)
+    if sc is None:
+        if p.endswith(".rad"):
+            sc = Scene(rad_files=[p])
+        else:
+            sc = Scene(p)
+        _SCENES[key] = sc
+    return sc
+
+
+def _wrap(fn):
+    def inner(*a, **k):
+        try:
+            return fn(*a, **k)
+        except GbError as e:
+            raise RuntimeError(f"An error occurred with exit code {-e.code}: {e}") from None
+    inner.__name__ = fn.__name__
+    inner.__doc__ = fn.__doc__
+    inner.__wrapped__ = fn
+    return inner
+
+
+# ---------------------------------------------------------------- formats
+
+def read_rays(data: bytes, fmt: str) -> np.ndarray:
+    """Ray records (n, 6) float64 from rtrace/rcontrib input bytes
+    (rt/rtrace.c:505-548 getvec; rt/rc2.c:259-290)."""
+    if fmt == "a":
+        vals = np.array(data.split(), dtype=np.float64) if data.strip() else np.zeros(0)
+        n = len(vals) // 6
+        return vals[: 6 * n].reshape(n, 6)
+    if fmt == "f":
+        a = np.frombuffer(data, dtype=np.float32)
+        n = len(a) // 6
+        return a[: 6 * n].reshape(n, 6).astype(np.float64)
+    if fmt == "d":
+        a = np.frombuffer(data, dtype=np.float64)
+        n = len(a) // 6
+        return a[: 6 * n].reshape(n, 6).copy()
+    raise RuntimeError(f"Illegal i/o format: {fmt}")
+
+
+def _header(prog: str, args: list[str], octree, fmt: str, ncomp: int | None) -> bytes:
+    lines = ["#?RADIANCE"]
+    if octree is not None and not isinstance(octree, (Scene, list, tuple)):
+        try:
+            with open(octree, "rb") as f:
+                head = f.read(4096)
+            for ln in head.split(b"\n\n")[0].split(b"\n")[1:]:
+                s = ln.decode(errors="replace")
+                if s and not s.startswith("FORMAT="):
+                    lines.append(s)
+        except OSError:
+            pass
+    lines.append(" ".join([prog, *map(str, args)]))
+    lines.append("SOFTWARE= " + lib().gb_version().decode())
+    now = time.time()
+    lines.append(time.strftime("CAPDATE= %Y:%m:%d %H:%M:%S", time.localtime(now)))
+    lines.append(time.strftime("GMT= %Y:%m:%d %H:%M:%S", time.gmtime(now)))
+    if ncomp:
+        lines.append(f"NCOMP={ncomp}")
+    if fmt in ("f", "d"):
+        lines.append("BigEndian=0")
+    name = {"a": "ascii", "f": "float", "d": "double", "c": "32-bit_rle_rgbe"}[fmt]
+    text = "\n".join(lines) + "\n" + "FORMAT=" + name
+    align = {"f": 4, "d": 8}.get(fmt, 0)
+    if align:                       # common/header.c:190-222 padding
+        pos = (len(text.encode()) + 2) % align
+        text += " " * ((align - pos) if pos else 0)
+    return (text + "\n\n").encode()
+
+
+def _fmt_values(vals: np.ndarray, fmt: str) -> bytes:
+    if fmt == "a":
+        return "".join("".join(f"{x:e}\t" for x in row) + "\n" for row in vals).encode()
+    if fmt == "f":
+        return np.ascontiguousarray(vals, dtype=np.float32).tobytes()
+    if fmt == "d":
+        return np.ascontiguousarray(vals, dtype=np.float64).tobytes()
+    raise RuntimeError("color (-fc) output is not supported")
+
+
+# ------------------------------------------------------------------ rtrace
+
+_CAST_ONLY = set("odLpNsmMw~")
+
+
+def _rtrace(rays: bytes, octree, header: bool = True, inform: str = "a", outform: str = "a",
+            irradiance: bool = False, irradiance_lambertian: bool = False, outspec: str | None = None,
+            trace_exclude: str = "", trace_include: str = "", trace_exclude_file=None,
+            trace_include_file=None, uncorrelated: bool = False, xres: int | None = None,
+            yres: int | None = None, nproc: int | None = None, params: Sequence[str] | None = None,
+            report: bool = False, version: bool = False) -> bytes:
+    """Run rtrace on the GPU (same signature as pyradiance.rtrace)."""
+    if version:
+        return (lib().gb_version().decode() + "\n").encode()
+    if not isinstance(rays, bytes):
+        raise TypeError("Rays must be bytes")
+    args: list[str] = []
+    if not header:
+        args.append("-h")
+    if irradiance:
+        args.append("-I")
+    elif irradiance_lambertian:
+        args.append("-i")
+    args.append(f"-f{inform}{outform}")
+    if outspec:
+        args.append(f"-o{outspec}")
+    if trace_exclude or trace_include or trace_exclude_file or trace_include_file:
+        raise GbError(-3, "trace include/exclude lists are not supported")
+    if uncorrelated:
+        args.append("-u+")
+    if xres is not None:
+        args += ["-x", str(xres)]
+    if yres is not None:
+        args += ["-y", str(yres)]
+    if nproc:
+        args += ["-n", str(nproc)]
+    if params is not None:
+        args += list(params)
+    opts, used = parse_opts(args, _lib.GB_PROG_RTRACE)
+    if used != len(args):
+        raise GbError(-1, f"command line error at '{args[used]}'")
+    spec = opts.outspec.decode() or "v"
+    fin, fout = opts.fin.decode(), opts.fout.decode()
+    sc = load_scene(octree)
+    r = read_rays(rays, fin)
+    n = len(r)
+    dirlen = np.sqrt((r[:, 3:6] ** 2).sum(axis=1)) if n else np.zeros(0)
+    need_val = any(ch not in _CAST_ONLY for ch in spec)
+    vals = np.zeros((n, 3)) if need_val else None
+    hit = np.full(n, -1, dtype=np.int32)
+    hitt = np.zeros(n)
+    good = dirlen > 0
+    rr = np.ascontiguousarray(r[good]) if n else r
+    ng = len(rr)
+    gv = np.zeros((ng, 3)) if need_val else None
+    gh = np.zeros(ng, dtype=np.int32)
+    gt = np.zeros(ng)
+    if ng:
+        check(lib().gb_rtrace(sc.handle, opts, ptr(rr), ng, ptr(gv), ptr(gh), ptr(gt)))
+    if need_val:
+        vals[good] = gv
+    hit[good] = gh
+    hitt[good] = gt
+    out = []
+    ncomp = 0
+    for ch in spec:
+        ncomp += {"v": 3, "o": 3, "d": 3, "p": 3, "N": 3, "n": 3, "L": 1, "l": 1, "w": 1}.get(ch, 0)
+    if opts.h:
+        out.append(_header("rtrace", args, octree, fout, ncomp or None))
+    unit = np.where(good[:, None], r[:, 3:6] / np.where(dirlen > 0, dirlen, 1)[:, None], 0.0) if n else r[:, 3:6]
+    for i in range(n):
+        cols = []
+        text = []
+        for ch in spec:
+            if ch == "v":
+                cols.append(vals[i])
+            elif ch == "o":
+                cols.append(r[i, 0:3])
+            elif ch == "d":
+                cols.append(unit[i])
+            elif ch == "L":
+                cols.append(np.array([hitt[i] if hit[i] >= 0 else 1e10]))
+            elif ch == "p":
+                cols.append(r[i, 0:3] + unit[i] * (hitt[i] if hit[i] >= 0 else 0.0) if hit[i] >= 0 else np.zeros(3))
+            elif ch in "smM":
+                if cols:
+                    text.append(_fmt_values(np.concatenate(cols)[None, :], "a").decode().rstrip("\n")
+                                if fout == "a" else None)
+                    cols = []
+                name = "*"
+                if hit[i] >= 0:
+                    name = {"s": sc.object_name, "m": sc.modifier_name, "M": sc.material_name}[ch](int(hit[i]))
+                text.append(name + "\t")
+            elif ch == "w":
+                cols.append(np.array([1.0]))
+            else:
+                raise GbError(-3, f"output option -o{ch} is not supported")
+        if fout == "a":
+            if cols:
+                text.append("".join(f"{x:e}\t" for x in np.concatenate(cols)))
+            out.append(("".join(t for t in text if t is not None) + "\n").encode())
+        else:
+            if any(ch in "smM" for ch in spec):
+                raise GbError(-1, "names need ascii output")
+            if cols:
+                out.append(_fmt_values(np.concatenate(cols)[None, :], fout))
+    return b"".join(out)
+
+
+rtrace = _wrap(_rtrace)
+
+
+# ---------------------------------------------------------------- rcontrib
+
+class Rcontrib:
+    """rcontrib on the GPU (same constructor and methods as pyradiance.Rcontrib)."""
+
+    def __init__(self, inp: bytes, octree, nproc: int = 1, yres: int | None = None, inform: str | None = None,
+                 outform: str | None = None, report: int = 0, params: Sequence[str] | None = None):
+        self.octree = octree
+        self.inp = inp
+        self.args: list[str] = ["-n", str(nproc)]
+        if params is not None:
+            self.args.extend(params)
+        if None not in (inform, outform):
+            self.args.append(f"-f{inform}{outform}")
+        if yres is not None:
+            self.args.extend(["-y", str(yres)])
+        if report:
+            self.args.extend(["-t", str(report)])
+        self.mods: list[dict] = []
+        self.seed = None
+        self.replica = 0
+        self.last_rays = 0
+
+    def add_modifier(self, modifier: str | None = None, modifier_path: str | None = None,
+                     calfile: str | None = None, expression: str | None = None, nbins: str | None = None,
+                     binv: str | None = None, param: str | None = None, xres: int | None = None,
+                     yres: int | None = None, output: str | None = None):
+        if modifier is None and modifier_path is None:
+            raise ValueError("Modifier or modifier path must be provided.")
+        names = [modifier] if modifier is not None else [
+            w for w in Path(modifier_path).read_text().split() if w]
+        if output is not None:
+            raise RuntimeError("An error occurred with exit code 3: per-modifier output files (-o) "
+                               "are not supported; results are returned as bytes")
+        for nm in names:
+            self.mods.append(dict(modifier=nm, calfile=calfile, expr=expression, nbins=nbins, binv=binv,
+                                  params=param))
+        return self
+
+    def _specs(self):
+        keep = []
+        arr = (GbModspec * len(self.mods))()
+        for i, m in enumerate(self.mods):
+            vals = {k: (str(v).encode() if v is not None else None) for k, v in m.items()}
+            keep.append(vals)
+            arr[i] = GbModspec(vals["modifier"], vals["binv"], vals["nbins"], vals["params"], vals["calfile"],
+                               vals["expr"])
+        return arr, keep
+
+    def run_array(self, rays: np.ndarray | None = None) -> np.ndarray:
+        """Contributions as a (records, total bins, 3) float64 array."""
+        opts, used = parse_opts(self.args, _lib.GB_PROG_RCONTRIB)
+        if used != len(self.args):
+            raise GbError(-1, f"command line error at '{self.args[used]}'")
+        if self.seed is not None:
+            opts.seed = int(self.seed)
+        opts.replica = int(self.replica)
+        if rays is None:
+            r = _rc_rays(self.inp, opts.fin.decode())
+        else:
+            r = np.ascontiguousarray(rays, dtype=np.float64).reshape(-1, 6)
+        specs, keep = self._specs()
+        nb = _lib.C.c_int(0)
+        check(lib().gb_rcontrib_nbins(specs, len(self.mods), _lib.C.byref(nb)))
+        accum = max(1, opts.c)
+        nrec = len(r) // accum
+        out = np.zeros((max(nrec, 0), nb.value, 3))
+        if len(r):
+            cnt = _lib.C.c_int64(0)
+            sc = load_scene(self.octree)
+            check(lib().gb_rcontrib(sc.handle, opts, specs, len(self.mods), ptr(r), len(r), ptr(out),
+                                    _lib.C.byref(cnt)))
+            self.last_rays = cnt.value
+        self._opts = opts
+        return out
+
+    def _call(self) -> bytes:
+        arr = self.run_array()
+        opts = self._opts
+        fout = opts.fout.decode()
+        parts = []
+        if opts.h:
+            parts.append(_header("rcontrib", self.args + [a for m in self.mods for a in ("-m", m["modifier"])],
+                                 self.octree, fout, 3))
+        if fout == "a":
+            flat = arr.reshape(arr.shape[0], -1)
+            parts.append("".join("".join(f"{x:.6e}\t" for x in row) + "\n" for row in flat).encode())
+        else:
+            parts.append(_fmt_values(arr.reshape(-1, 3), fout))
+        return b"".join(parts)
+
+    def __call__(self) -> bytes:
+        return _wrap(self._call)()
+
+
+def _rc_rays(data: bytes, fmt: str) -> np.ndarray:
+    r = read_rays(data, fmt)
+    d = np.sqrt((r[:, 3:6] ** 2).sum(axis=1)) if len(r) else np.zeros(0)
+    if len(r) and (d == 0).any():
+        raise GbError(-3, "zero-direction (flush) records are not supported")
+    return r
+
+
+# -------------------------------------------------------------- dctimestep
+
+def _read_matrix(src, fmt_hint: str | None = None):
+    """Radiance matrix file or bytes -> (rows, cols, 3) float32 array
+    (util/cmatrix.c:82-122 header, :191 cm_load)."""
+    data = Path(src).read_bytes() if not isinstance(src, bytes) else src
+    nrows = ncols = 0
+    fmt = fmt_hint
+    big = None
+    body = data
+    if data.startswith(b"#?"):
+        end = data.find(b"\n\n")
+        head, body = data[:end], data[end + 2:]
+        for ln in head.split(b"\n"):
+            s = ln.decode(errors="replace").strip()
+            if s.startswith("NROWS="):
+                nrows = int(s[6:])
+            elif s.startswith("NCOLS="):
+                ncols = int(s[6:])
+            elif s.startswith("NCOMP=") and int(s[6:]) != 3:
+                raise GbError(-1, "unexpected # components (must be 3)")
+            elif s.startswith("FORMAT="):
+                fmt = {"ascii": "a", "float": "f", "double": "d"}.get(s[7:].strip(), s[7:].strip())
+            elif s.startswith("BigEndian="):
+                big = s[10:] == "1"
+    if fmt == "a" or fmt is None:
+        vals = np.array(body.split(), dtype=np.float64)
+    elif fmt == "f":
+        vals = np.frombuffer(body, dtype=">f4" if big else "<f4").astype(np.float64)
+    elif fmt == "d":
+        vals = np.frombuffer(body, dtype=">f8" if big else "<f8")
+    else:
+        raise GbError(-3, f"matrix format '{fmt}' is not supported")
+    if nrows <= 0 and ncols > 0:
+        nrows = len(vals) // (3 * ncols)
+    if ncols <= 0 and nrows > 0:
+        ncols = len(vals) // (3 * nrows)
+    if nrows <= 0 or ncols <= 0:
+        raise GbError(-1, "missing matrix dimensions")
+    return np.ascontiguousarray(vals[: nrows * ncols * 3].reshape(nrows, ncols, 3), dtype=np.float32)
+
+
+def dctimestep_array(dc: np.ndarray, sky: np.ndarray, mode: str = "fp32") -> np.ndarray:
+    """R = DC x sky per channel on the GPU; (M,K,3) x (K,N,3) -> (M,N,3) float32."""
+    dc = np.ascontiguousarray(dc, dtype=np.float32)
+    sky = np.ascontiguousarray(sky, dtype=np.float32)
+    M, K, _ = dc.shape
+    K2, N, _ = sky.shape
+    if K != K2:
+        raise GbError(-1, "matrix dimension mismatch")
+    out = np.empty((M, N, 3), dtype=np.float32)
+    m = {"fp32": _lib.GB_DCT_FP32, "bf16x3": _lib.GB_DCT_BF16X3, "fp64": _lib.GB_DCT_FP64}[mode]
+    check(lib().gb_dctimestep(ptr(dc), ptr(sky), M, K, N, m, ptr(out)))
+    return out
+
+
+def _dctimestep(*mtx, nstep: int | None = None, header: bool = True, xres: int | None = None,
+                yres: int | None = None, inform: str | None = None, outform: str | None = None,
+                ospec: str | None = None) -> bytes | None:
+    """dctimestep on the GPU (same signature as pyradiance.dctimestep);
+    the two-matrix form DC x sky."""
+    if len(mtx) not in (2, 4):
+        raise ValueError("mtx must be a list of 2 or 4 items")
+    if len(mtx) == 4:
+        raise GbError(-3, "the four-matrix (view/BSDF/daylight) form is not supported")
+    if ospec:
+        raise GbError(-3, "output specification files are not supported")
+    dc = _read_matrix(mtx[0])
+    sky = _read_matrix(mtx[1], inform)
+    R = dctimestep_array(dc, sky)
+    fout = outform or "a"
+    parts = []
+    if header:
+        lines = ["#?RADIANCE", "dctimestep", "SOFTWARE= " + lib().gb_version().decode(),
+                 f"NROWS={R.shape[0]}", f"NCOLS={R.shape[1]}", "NCOMP=3"]
+        if fout in ("f", "d"):
+            lines.append("BigEndian=0")
+        lines.append("FORMAT=" + {"a": "ascii", "f": "float", "d": "double"}[fout])
+        parts.append(("\n".join(lines) + "\n\n").encode())
+    if fout == "a":
+        parts.append("".join("\t".join(f"{v:.6e}" for v in row.ravel()) + "\n" for row in R).encode())
+    else:
+        parts.append(_fmt_values(R.reshape(-1, 3), fout))
+    return b"".join(parts)
+
+
+dctimestep = _wrap(_dctimestep)

@@ -1,0 +1,85 @@
+/*
+ * devscene.h -- the scene as the kernels see it, in HBM.
+ *
+ * Layout (structure of arrays, all read-only during a run):
+ *   kids      int32[8 * nnodes]   octree children codes (>= 0 node, -1 empty,
+ *                                 <= -2 leaf set), 32 B per node
+ *   set_off   int32[nsets]        start of each leaf set in set_data
+ *   set_data  int32[...]          [count, members in DESCENDING object order]
+ *                                 (the order rt/raytrace.c:585 tests them)
+ *   obj       int4[nobjs]         x: kind | flags << 8 | nv << 16,
+ *                                 y: material slot (-1 none), z: modifier
+ *                                 object index, w: vertex / cone offset
+ *   geo       float4[nobjs]       faces: unit normal + plane offset;
+ *                                 spheres: centre + radius
+ *   fvert     float2[...]         polygon vertices projected on the two
+ *                                 axes other than the dominant normal axis
+ *   cone      float[16 * ncones]  3x4 world->canonical transform, axis,
+ *                                 length terms and radii
+ *   mat       float4[2 * nmats]   material kind and parameters
+ *   src       gb_dsrc[nsrc]       light sources (rt/source.h SRCREC subset)
+ *   trk       int32[nobjs]        tracked-modifier slot of each object's
+ *                                 direct modifier (-1 untracked)
+ */
+#ifndef GB_DEVSCENE_H
+#define GB_DEVSCENE_H
+
+#include <stdint.h>
+
+/* object kinds on the device */
+enum { DK_NONE = 0, DK_FACE, DK_SPHERE, DK_BUBBLE, DK_CONE, DK_CUP, DK_CYL, DK_TUBE, DK_RING, DK_SOURCE };
+/* object flags */
+#define DF_HASMAT  0x01   /* has a material (findmaterial != NULL) */
+#define DF_TRANSP  0x02   /* material is nominally transparent */
+#define DF_AXSHIFT 2      /* bits 2-3: dominant normal axis of a face */
+
+/* material kinds on the device */
+enum { DM_NONE = 0, DM_PLASTIC, DM_METAL, DM_GLASS, DM_LIGHT, DM_GLOW, DM_TRANS };
+
+/* source flags (rt/source.h:24-37) */
+#define DS_DISTANT 0x01
+#define DS_SKIP    0x02
+#define DS_FLAT    0x04
+#define DS_PROX    0x08
+#define DS_FOLLOW  0x10
+
+typedef struct {
+    float sloc[3];      /* centre (local) or direction (distant) */
+    float snorm[3];     /* flat source normal */
+    float ss[3][3];     /* SU, SV, SW size vectors */
+    float ss2;          /* area (flat) or solid angle (distant) */
+    float srad;         /* radius */
+    float prox;         /* glow proximity radius */
+    int   flags;
+    int   so;           /* source object index */
+    int   mat;          /* material slot of the source */
+    int   pad;
+} gb_dsrc;
+
+typedef struct {
+    /* octree */
+    float cuorg[3];
+    float cusize;
+    float grid_scale;          /* 2^24 / cusize */
+    float cell;                /* cusize / 2^24 */
+    int   root;
+    int   nnodes;
+    const int   *kids;
+    const int   *set_off;
+    const int   *set_data;
+    /* objects */
+    int   nobjs;
+    const int4  *obj;
+    const float4 *geo;
+    const float2 *fvert;
+    const float *cone;
+    /* materials */
+    const float4 *mat;
+    /* sources */
+    int   nsrc;
+    const gb_dsrc *src;
+    /* tracked modifiers (per object) */
+    const int *trk;
+} gb_dscene;
+
+#endif

@@ -1,0 +1,1061 @@
+/*
+ * host.cu -- the C ABI (include/gbrad.h): scene loading and upload, option
+ * parsing, and the orchestration of the wavefront kernels of trace.cu.
+ */
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <ctime>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/gbrad.h"
+#include "binexpr.h"
+#include "dct.h"
+#include "scene.h"
+#include "tracehost.h"
+
+static thread_local std::string g_error;
+static thread_local int64_t g_stats[4];
+
+static int set_err(int code, const char *fmt, ...)
+{
+    char buf[1024];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    g_error = buf;
+    return code;
+}
+
+#define CK(call)                                                                              \
+    do {                                                                                      \
+        cudaError_t e_ = (call);                                                              \
+        if (e_ != cudaSuccess)                                                                \
+            return set_err(GB_ECUDA, "CUDA error %s at %s:%d", cudaGetErrorString(e_), __FILE__, __LINE__); \
+    } while (0)
+
+extern "C" const char *gb_last_error(void) { return g_error.c_str(); }
+extern "C" const char *gb_version(void) { return "gbrad 0.1 (sm_103a)"; }
+
+extern "C" int gb_last_stats(int64_t *rays, int64_t *steps, int64_t *contribs, int64_t *launches)
+{
+    if (rays) *rays = g_stats[0];
+    if (steps) *steps = g_stats[1];
+    if (contribs) *contribs = g_stats[2];
+    if (launches) *launches = g_stats[3];
+    return GB_OK;
+}
+
+/* ------------------------------------------------------------------ scene */
+
+struct DevBuf {
+    void *p = nullptr;
+    size_t n = 0;
+    int ensure(size_t bytes)
+    {
+        if (bytes <= n)
+            return 0;
+        if (p)
+            cudaFree(p);
+        p = nullptr;
+        n = 0;
+        if (cudaMalloc(&p, bytes) != cudaSuccess)
+            return -1;
+        n = bytes;
+        return 0;
+    }
+    void release()
+    {
+        if (p)
+            cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+};
+
+struct gb_scene {
+    gb_scene_host H;
+    std::vector<int> matslot;          /* per object: material slot or -1 */
+    std::vector<int> matobj;           /* per slot: material object index */
+    std::vector<float4> mat;           /* 2 per slot */
+    std::vector<int> unsupported;      /* material objects the shader lacks */
+    std::vector<gb_dsrc> src;
+    std::string src_error;             /* non-empty if a source is unsupported */
+    std::vector<std::string> modname, matname;
+    /* device scene */
+    DevBuf kids, setoff, setdata, obj, geo, fvert, cone, matd, srcd, trk;
+    gb_dscene ds;
+    /* work buffers */
+    DevBuf sensors, value, bins, stats, roots, rootspt, qa, qb, qcount, binprog, modinfo, hits, hitt, trkrun;
+    cudaStream_t stream = nullptr;
+    int sms = 0;
+};
+
+static int material_kind(const gb_object *m, float4 *m0, float4 *m1, std::string &why)
+{
+    const double *f = m->farg;
+    *m0 = make_float4(0, 0, 0, 0);
+    *m1 = make_float4(0, 0, 0, 0);
+    switch (m->otype) {
+    case GT_PLASTIC:
+    case GT_METAL:
+        if (m->nfargs != 5) { why = "bad number of arguments"; return -1; }
+        *m0 = make_float4(m->otype == GT_PLASTIC ? DM_PLASTIC : DM_METAL, f[0], f[1], f[2]);
+        *m1 = make_float4(f[3], f[4], 0, 0);
+        return 0;
+    case GT_GLASS:
+        if (m->nfargs != 3 && m->nfargs != 4) { why = "bad arguments"; return -1; }
+        *m0 = make_float4(DM_GLASS, f[0], f[1], f[2]);
+        *m1 = make_float4(m->nfargs == 4 ? f[3] : 1.52, 0, 0, 0);
+        return 0;
+    case GT_LIGHT:
+        if (m->nfargs != 3) { why = "bad # arguments"; return -1; }
+        *m0 = make_float4(DM_LIGHT, f[0], f[1], f[2]);
+        return 0;
+    case GT_GLOW:
+        if (m->nfargs != 4) { why = "bad # arguments"; return -1; }
+        *m0 = make_float4(DM_GLOW, f[0], f[1], f[2]);
+        *m1 = make_float4(f[3], 0, 0, 0);
+        return 0;
+    default:
+        why = std::string("material type '") + gb_otype_name(m->otype) + "' is not implemented on the GPU path";
+        return -1;
+    }
+}
+
+/* getperpendicular without randomisation (common/fvect.c:159-196) */
+static void perp(double vp[3], const double v[3])
+{
+    double v1[3] = {0, 0, 0};
+    int i;
+    for (i = 3; i--;)
+        if (-0.6 < v[i] && v[i] < 0.6)
+            break;
+    if (i < 0) i = 0;
+    v1[i] = 1.0;
+    vp[0] = v1[1] * v[2] - v1[2] * v[1];
+    vp[1] = v1[2] * v[0] - v1[0] * v[2];
+    vp[2] = v1[0] * v[1] - v1[1] * v[0];
+    double l = sqrt(vp[0] * vp[0] + vp[1] * vp[1] + vp[2] * vp[2]);
+    for (i = 0; i < 3; i++) vp[i] /= l;
+}
+
+static double dist2line(const double p[3], const double a[3], const double b[3])
+{
+    double d[3], v[3], l2 = 0, t = 0, r = 0;
+    for (int i = 0; i < 3; i++) { d[i] = b[i] - a[i]; v[i] = p[i] - a[i]; l2 += d[i] * d[i]; t += d[i] * v[i]; }
+    for (int i = 0; i < 3; i++) r += v[i] * v[i];
+    return r - t * t / l2;
+}
+
+/* rt/source.c:47-142 (marksources) with rt/srcsupp.c:88-180 (fsetsrc,
+ * ssetsrc) */
+static int mark_sources(gb_scene *G)
+{
+    gb_scene_host &H = G->H;
+    for (int32_t i = 0; i < H.nobjs; i++) {
+        const gb_object *o = &H.objs[i];
+        if (!gb_is_surface(o->otype) || o->omod < 0)
+            continue;
+        int32_t m = gb_find_material(&H, i);
+        if (m < 0)
+            continue;
+        const gb_object *mo = &H.objs[m];
+        if (!gb_is_light(mo->otype))
+            continue;
+        int need = mo->otype == GT_GLOW ? 4 : mo->otype == GT_SPOT ? 7 : 3;
+        if (mo->nfargs != need)
+            return set_err(GB_EIO, "%s: bad # arguments", mo->name);
+        if (mo->farg[0] <= GB_FTINY && mo->farg[1] <= GB_FTINY && mo->farg[2] <= GB_FTINY)
+            continue;
+        if (mo->otype == GT_GLOW && o->otype != GT_SOURCE && mo->farg[3] <= GB_FTINY)
+            continue;                                /* indirect glow */
+        gb_dsrc s;
+        memset(&s, 0, sizeof s);
+        s.so = i;
+        s.mat = G->matslot[i];
+        if (o->otype == GT_POLYGON) {
+            const gb_face *f = &H.faces[i];
+            const double *va = o->farg;
+            double c[3] = {0, 0, 0}, su[3] = {0, 0, 0}, sv[3] = {0, 0, 0}, srad = 0;
+            if (!f->ok)
+                return set_err(GB_EIO, "%s: zero source area", o->name);
+            for (int j = 0; j < 3; j++) {
+                for (int k = 0; k < f->nv; k++) c[j] += va[3 * k + j];
+                c[j] /= f->nv;
+            }
+            for (int k = 0; k < f->nv; k++) {
+                double d = 0;
+                for (int j = 0; j < 3; j++) d += (va[3 * k + j] - c[j]) * (va[3 * k + j] - c[j]);
+                if (d > srad) srad = d;
+            }
+            if (f->nv == 4) {
+                for (int j = 0; j < 3; j++) {
+                    su[j] = .5 * (va[3 + j] - va[j]);
+                    sv[j] = .5 * (va[9 + j] - va[j]);
+                }
+            } else if (f->nv == 3) {
+                int near0 = 2;
+                double dmin = dist2line(c, va + 6, va);
+                for (int k = 0; k < 2; k++) {
+                    double d2 = dist2line(c, va + 3 * k, va + 3 * (k + 1));
+                    if (d2 >= dmin) continue;
+                    near0 = k;
+                    dmin = d2;
+                }
+                int k = (near0 + 1) % 3;
+                double l = 0;
+                for (int j = 0; j < 3; j++) { su[j] = va[3 * k + j] - va[3 * near0 + j]; l += su[j] * su[j]; }
+                l = sqrt(dmin) / sqrt(l);
+                for (int j = 0; j < 3; j++) su[j] *= l;
+                sv[0] = f->norm[1] * su[2] - f->norm[2] * su[1];
+                sv[1] = f->norm[2] * su[0] - f->norm[0] * su[2];
+                sv[2] = f->norm[0] * su[1] - f->norm[1] * su[0];
+            } else {
+                perp(su, f->norm);
+                double mult = .5 * sqrt(f->area);
+                for (int j = 0; j < 3; j++) su[j] *= mult;
+                sv[0] = f->norm[1] * su[2] - f->norm[2] * su[1];
+                sv[1] = f->norm[2] * su[0] - f->norm[0] * su[2];
+                sv[2] = f->norm[0] * su[1] - f->norm[1] * su[0];
+            }
+            s.flags = DS_FLAT;
+            for (int j = 0; j < 3; j++) {
+                s.sloc[j] = (float)c[j];
+                s.snorm[j] = (float)f->norm[j];
+                s.ss[0][j] = (float)su[j];
+                s.ss[1][j] = (float)sv[j];
+            }
+            s.ss2 = (float)f->area;
+            s.srad = (float)sqrt(srad);
+        } else if (o->otype == GT_SOURCE) {
+            double d[3] = {o->farg[0], o->farg[1], o->farg[2]};
+            double l = sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+            if (l == 0.0)
+                return set_err(GB_EIO, "%s: zero direction", o->name);
+            for (int j = 0; j < 3; j++) d[j] /= l;
+            double theta = M_PI / 180.0 / 2.0 * o->farg[3];
+            if (theta <= GB_FTINY)
+                return set_err(GB_EIO, "%s: zero size", o->name);
+            double ss2 = 2.0 * M_PI * (1.0 - cos(theta));
+            double su[3], sv[3];
+            perp(su, d);
+            double mult = .5 * sqrt(ss2);
+            for (int j = 0; j < 3; j++) su[j] *= mult;
+            sv[0] = d[1] * su[2] - d[2] * su[1];
+            sv[1] = d[2] * su[0] - d[0] * su[2];
+            sv[2] = d[0] * su[1] - d[1] * su[0];
+            s.flags = DS_DISTANT;
+            for (int j = 0; j < 3; j++) {
+                s.sloc[j] = (float)d[j];
+                s.snorm[j] = (float)d[j];
+                s.ss[0][j] = (float)su[j];
+                s.ss[1][j] = (float)sv[j];
+            }
+            s.ss2 = (float)ss2;
+            s.srad = (float)sqrt(ss2 / M_PI);
+        } else {
+            if (G->src_error.empty())
+                G->src_error = std::string("light source geometry '") + gb_otype_name(o->otype) + "' (" +
+                               o->name + ") is not implemented on the GPU path";
+            continue;
+        }
+        if (mo->otype == GT_GLOW) {
+            s.flags |= DS_PROX;
+            s.prox = (float)mo->farg[3];
+            if (s.flags & DS_DISTANT)
+                s.flags |= DS_SKIP;
+        } else if (mo->otype == GT_SPOT || mo->otype == GT_ILLUM) {
+            if (G->src_error.empty())
+                G->src_error = std::string("light material '") + gb_otype_name(mo->otype) + "' (" + mo->name +
+                               ") is not implemented on the GPU path";
+        }
+        G->src.push_back(s);
+    }
+    return GB_OK;
+}
+
+template <typename T>
+static int upload(DevBuf &b, const std::vector<T> &v)
+{
+    size_t bytes = v.size() * sizeof(T);
+    if (b.ensure(bytes ? bytes : 16) < 0)
+        return -1;
+    if (bytes && cudaMemcpy(b.p, v.data(), bytes, cudaMemcpyHostToDevice) != cudaSuccess)
+        return -1;
+    return 0;
+}
+
+static int prepare_device(gb_scene *G)
+{
+    gb_scene_host &H = G->H;
+    if (gb_scene_prepare(&H) < 0)
+        return set_err(GB_EIO, "%s", gb_scene_error());
+    int dev = 0;
+    CK(cudaGetDevice(&dev));
+    CK(cudaDeviceGetAttribute(&G->sms, cudaDevAttrMultiProcessorCount, dev));
+    CK(cudaStreamCreateWithFlags(&G->stream, cudaStreamNonBlocking));
+    /* materials */
+    G->matslot.assign(H.nobjs, -1);
+    std::vector<int> slot_of_mat(H.nobjs, -1);
+    for (int32_t i = 0; i < H.nobjs; i++) {
+        if (!gb_is_surface(H.objs[i].otype))
+            continue;
+        int32_t m = gb_find_material(&H, i);
+        if (m < 0)
+            continue;
+        if (slot_of_mat[m] < 0) {
+            float4 a, b;
+            std::string why;
+            if (material_kind(&H.objs[m], &a, &b, why) < 0) {
+                a = make_float4(-1.f, 0, 0, 0);
+                G->unsupported.push_back(m);
+            }
+            slot_of_mat[m] = (int)G->matobj.size();
+            G->matobj.push_back(m);
+            G->mat.push_back(a);
+            G->mat.push_back(b);
+        }
+        G->matslot[i] = slot_of_mat[m];
+    }
+    if (G->mat.empty()) {
+        G->mat.push_back(make_float4(0, 0, 0, 0));
+        G->mat.push_back(make_float4(0, 0, 0, 0));
+    }
+    /* objects */
+    std::vector<int4> obj(H.nobjs);
+    std::vector<float4> geo(H.nobjs);
+    std::vector<float2> fvert;
+    std::vector<float> cone;
+    for (int32_t i = 0; i < H.nobjs; i++) {
+        const gb_object *o = &H.objs[i];
+        int kind = DK_NONE, flags = 0, nv = 0, aux = 0;
+        int32_t m = gb_is_surface(o->otype) ? gb_find_material(&H, i) : -1;
+        if (m >= 0) {
+            flags |= DF_HASMAT;
+            if (gb_is_transp(H.objs[m].otype))
+                flags |= DF_TRANSP;
+        }
+        geo[i] = make_float4(0, 0, 0, 0);
+        switch (o->otype) {
+        case GT_POLYGON: {
+            const gb_face *f = &H.faces[i];
+            if (!f->ok)
+                break;
+            kind = DK_FACE;
+            nv = f->nv;
+            flags |= f->ax << DF_AXSHIFT;
+            geo[i] = make_float4((float)f->norm[0], (float)f->norm[1], (float)f->norm[2], (float)f->offset);
+            aux = (int)fvert.size();
+            int xi = (f->ax + 1) % 3, yi = (xi + 1) % 3;
+            for (int k = 0; k < nv; k++)
+                fvert.push_back(make_float2((float)o->farg[3 * k + xi], (float)o->farg[3 * k + yi]));
+            break;
+        }
+        case GT_SPHERE:
+        case GT_BUBBLE:
+            kind = o->otype == GT_SPHERE ? DK_SPHERE : DK_BUBBLE;
+            geo[i] = make_float4((float)o->farg[0], (float)o->farg[1], (float)o->farg[2], (float)o->farg[3]);
+            break;
+        case GT_CONE: case GT_CUP: case GT_CYLINDER: case GT_TUBE: case GT_RING: {
+            const gb_cone *c = &H.cones[i];
+            if (!c->ok)
+                break;
+            kind = o->otype == GT_CONE ? DK_CONE : o->otype == GT_CUP ? DK_CUP :
+                   o->otype == GT_CYLINDER ? DK_CYL : o->otype == GT_TUBE ? DK_TUBE : DK_RING;
+            aux = (int)(cone.size() / 24);
+            const double *ca = o->farg;
+            double ad[3];
+            if (o->otype == GT_RING) {
+                for (int j = 0; j < 3; j++) ad[j] = ca[3 + j];
+            } else {
+                for (int j = 0; j < 3; j++) ad[j] = ca[c->p1 + j] - ca[c->p0 + j];
+            }
+            double l = sqrt(ad[0] * ad[0] + ad[1] * ad[1] + ad[2] * ad[2]);
+            for (int j = 0; j < 3; j++) ad[j] /= l;
+            float rec[24] = {0};
+            for (int a = 0; a < 4; a++)
+                for (int b = 0; b < 3; b++)
+                    rec[3 * a + b] = (float)c->tm[a][b];
+            for (int j = 0; j < 3; j++) {
+                rec[12 + j] = (float)ad[j];
+                rec[15 + j] = (float)ca[c->p0 + j];
+            }
+            rec[18] = (float)c->al;
+            rec[19] = (float)c->sl;
+            rec[20] = (float)ca[c->r0];
+            rec[21] = (float)ca[c->r1];
+            cone.insert(cone.end(), rec, rec + 24);
+            break;
+        }
+        case GT_SOURCE:
+            kind = DK_SOURCE;
+            break;
+        default:
+            break;
+        }
+        if (nv > 0xffff)
+            return set_err(GB_EUNSUPPORTED, "%s: polygon with more than 65535 vertices", o->name);
+        obj[i] = make_int4(kind | (flags << 8) | (nv << 16), G->matslot[i], o->omod, aux);
+    }
+    if (fvert.empty()) fvert.push_back(make_float2(0, 0));
+    if (cone.empty()) cone.assign(24, 0.f);
+    int rc = mark_sources(G);
+    if (rc < 0)
+        return rc;
+    /* octree: sets in descending member order (rt/raytrace.c:585) */
+    std::vector<int> kids(H.kids, H.kids + 8 * (size_t)H.nnodes);
+    if (kids.empty()) kids.assign(8, -1);
+    std::vector<int> setoff(H.nsets), setdata((size_t)H.set_len);
+    for (int32_t s = 0; s < H.nsets; s++) {
+        const int32_t *st = H.set_data + H.set_off[s];
+        setoff[s] = (int)H.set_off[s];
+        setdata[H.set_off[s]] = st[0];
+        for (int k = 1; k <= st[0]; k++)
+            setdata[H.set_off[s] + k] = st[st[0] + 1 - k];
+    }
+    if (setoff.empty()) setoff.push_back(0);
+    if (setdata.empty()) setdata.push_back(0);
+    std::vector<gb_dsrc> src = G->src;
+    if (src.empty()) src.resize(1);
+    if (upload(G->kids, kids) < 0 || upload(G->setoff, setoff) < 0 || upload(G->setdata, setdata) < 0 ||
+        upload(G->obj, obj) < 0 || upload(G->geo, geo) < 0 || upload(G->fvert, fvert) < 0 ||
+        upload(G->cone, cone) < 0 || upload(G->matd, G->mat) < 0 || upload(G->srcd, src) < 0)
+        return set_err(GB_ENOMEM, "device upload of the scene failed");
+    gb_dscene &d = G->ds;
+    memset(&d, 0, sizeof d);
+    for (int j = 0; j < 3; j++) d.cuorg[j] = (float)H.cuorg[j];
+    d.cusize = (float)H.cusize;
+    d.grid_scale = (float)((double)(1 << GRID_BITS_HOST) / H.cusize);
+    d.cell = (float)(H.cusize / (double)(1 << GRID_BITS_HOST));
+    d.root = H.root;
+    d.nnodes = H.nnodes;
+    d.kids = (const int *)G->kids.p;
+    d.set_off = (const int *)G->setoff.p;
+    d.set_data = (const int *)G->setdata.p;
+    d.nobjs = H.nobjs;
+    d.obj = (const int4 *)G->obj.p;
+    d.geo = (const float4 *)G->geo.p;
+    d.fvert = (const float2 *)G->fvert.p;
+    d.cone = (const float *)G->cone.p;
+    d.mat = (const float4 *)G->matd.p;
+    d.nsrc = (int)G->src.size();
+    d.src = (const gb_dsrc *)G->srcd.p;
+    /* names for output */
+    G->modname.resize(H.nobjs);
+    G->matname.resize(H.nobjs);
+    for (int32_t i = 0; i < H.nobjs; i++) {
+        int32_t m = H.objs[i].omod;
+        G->modname[i] = m >= 0 ? H.objs[m].name : "void";
+        int32_t mm = gb_find_material(&H, i);
+        G->matname[i] = mm >= 0 ? H.objs[mm].name : "void";
+    }
+    return GB_OK;
+}
+
+static int finish_load(gb_scene *G, gb_scene **out)
+{
+    int rc = prepare_device(G);
+    if (rc < 0) {
+        gb_scene_free(G);
+        return rc;
+    }
+    *out = G;
+    return GB_OK;
+}
+
+extern "C" int gb_scene_load(const char *oct_path, gb_scene **out)
+{
+    if (!oct_path || !out)
+        return set_err(GB_EINVAL, "null argument");
+    gb_scene *G = new gb_scene();
+    gb_scene_init(&G->H);
+    if (gb_scene_read_oct(&G->H, oct_path) < 0) {
+        int rc = set_err(GB_EIO, "%s", gb_scene_error());
+        gb_scene_free(G);
+        return rc;
+    }
+    return finish_load(G, out);
+}
+
+extern "C" int gb_scene_load_rad(const char *const *paths, int npaths, int objlim, int resolu, gb_scene **out)
+{
+    if (!paths || npaths <= 0 || !out)
+        return set_err(GB_EINVAL, "no scene files");
+    gb_scene *G = new gb_scene();
+    gb_scene_init(&G->H);
+    for (int i = 0; i < npaths; i++)
+        if (gb_scene_read_rad_file(&G->H, paths[i]) < 0) {
+            int rc = set_err(GB_EIO, "%s", gb_scene_error());
+            gb_scene_free(G);
+            return rc;
+        }
+    if (gb_scene_build_octree(&G->H, objlim, resolu) < 0) {
+        int rc = set_err(GB_EIO, "octree build failed: %s", gb_scene_error());
+        gb_scene_free(G);
+        return rc;
+    }
+    return finish_load(G, out);
+}
+
+extern "C" void gb_scene_free(gb_scene *G)
+{
+    if (!G)
+        return;
+    DevBuf *bufs[] = {&G->kids, &G->setoff, &G->setdata, &G->obj, &G->geo, &G->fvert, &G->cone, &G->matd,
+                      &G->srcd, &G->trk, &G->sensors, &G->value, &G->bins, &G->stats, &G->roots, &G->rootspt, &G->qa,
+                      &G->qb, &G->qcount, &G->binprog, &G->modinfo, &G->hits, &G->hitt, &G->trkrun};
+    for (DevBuf *b : bufs)
+        b->release();
+    if (G->stream)
+        cudaStreamDestroy(G->stream);
+    gb_scene_clear(&G->H);
+    delete G;
+}
+
+extern "C" int64_t gb_scene_nobjects(const gb_scene *G) { return G ? G->H.nobjs : 0; }
+extern "C" const char *gb_scene_object_name(const gb_scene *G, int64_t i)
+{
+    return (G && i >= 0 && i < G->H.nobjs) ? G->H.objs[i].name : "*";
+}
+extern "C" const char *gb_scene_modifier_name(const gb_scene *G, int64_t i)
+{
+    return (G && i >= 0 && i < G->H.nobjs) ? G->modname[i].c_str() : "*";
+}
+extern "C" const char *gb_scene_material_name(const gb_scene *G, int64_t i)
+{
+    return (G && i >= 0 && i < G->H.nobjs) ? G->matname[i].c_str() : "*";
+}
+
+/* ---------------------------------------------------------------- options */
+
+extern "C" int gb_opts_default(int prog, gb_opts *o)
+{
+    if (!o)
+        return set_err(GB_EINVAL, "null options");
+    memset(o, 0, sizeof *o);
+    o->prog = prog;
+    o->fin = o->fout = 'a';
+    o->h = 1;
+    o->n = 1;
+    o->u = 1;
+    o->bv = 1;
+    o->dv = 1;
+    o->lr = -10;
+    o->ar = 256;
+    o->dc = .75;
+    o->dp = 512;
+    o->ss = 1.0;
+    o->c = 1;
+    strcpy(o->outspec, "v");
+    if (prog == GB_PROG_RCONTRIB) {   /* rt/rcontrib.c:24-58 + rcmain.c:164-172 */
+        o->dj = .9; o->ds = .2; o->dt = 0.; o->dr = 3; o->st = .02; o->lw = 2e-3;
+        o->ab = 1; o->aa = 0.; o->ad = 350; o->as = 0;
+    } else {                          /* rt/raycalls.c:121-150 */
+        o->dj = 0.; o->ds = .2; o->dt = .03; o->dr = 2; o->st = .15; o->lw = 1e-4;
+        o->ab = 0; o->aa = .1; o->ad = 1024; o->as = 512;
+    }
+    return GB_OK;
+}
+
+static int boolopt(const char *a, int olen, int *var)
+{
+    switch (a[olen]) {
+    case '\0': *var = !*var; return 0;
+    case '+': case '1': *var = 1; return 0;
+    case '-': case '0': *var = 0; return 0;
+    default: return -1;
+    }
+}
+
+extern "C" int gb_opts_parse(int argc, const char *const *argv, int prog, gb_opts *o, int *nused)
+{
+    int i;
+    for (i = 0; i < argc; i++) {
+        const char *a = argv[i];
+        if (!a || a[0] != '-' || !a[1])
+            break;
+        auto need = [&](int k) { return i + k < argc; };
+#define NEED(k) do { if (!need(k)) return set_err(GB_EINVAL, "missing argument for %s", a); } while (0)
+#define FARG(k) atof(argv[i + (k)])
+#define IARG(k) atoi(argv[i + (k)])
+        bool ok = true;
+        switch (a[1]) {
+        case 'u': ok = boolopt(a, 2, &o->u) == 0; break;
+        case 'w': break;                              /* warnings */
+        case 'b':
+            if (a[2] == 'v') ok = boolopt(a, 3, &o->bv) == 0;
+            else ok = false;
+            break;
+        case 'd':
+            switch (a[2]) {
+            case 't': NEED(1); o->dt = FARG(1); i++; break;
+            case 'c': NEED(1); o->dc = FARG(1); i++; break;
+            case 'j': NEED(1); o->dj = FARG(1); i++; break;
+            case 'r': NEED(1); o->dr = IARG(1); i++; break;
+            case 'p': NEED(1); o->dp = IARG(1); i++; break;
+            case 'v': ok = boolopt(a, 3, &o->dv) == 0; break;
+            case 's': NEED(1); o->ds = FARG(1); i++; break;
+            default: ok = false;
+            }
+            break;
+        case 's':
+            if (a[2] == 't') { NEED(1); o->st = FARG(1); i++; }
+            else if (a[2] == 's') { NEED(1); o->ss = FARG(1); i++; }
+            else ok = false;
+            break;
+        case 'l':
+            if (a[2] == 'r' && !a[3]) { NEED(1); o->lr = IARG(1); i++; }
+            else if (a[2] == 'w' && !a[3]) { NEED(1); o->lw = FARG(1); i++; }
+            else if (a[2] == 'd') { int v = o->ld != 0; ok = boolopt(a, 3, &v) == 0; o->ld = v; }
+            else ok = false;
+            break;
+        case 'i': ok = boolopt(a, 2, &o->i) == 0; break;
+        case 'I': ok = boolopt(a, 2, &o->I) == 0; break;
+        case 'a':
+            switch (a[2]) {
+            case 'v': NEED(3); o->av[0] = FARG(1); o->av[1] = FARG(2); o->av[2] = FARG(3); i += 3; break;
+            case 'w': NEED(1); o->aw = IARG(1); i++; break;
+            case 'a': NEED(1); o->aa = FARG(1); i++; break;
+            case 'r': NEED(1); o->ar = IARG(1); i++; break;
+            case 'd': NEED(1); o->ad = IARG(1); i++; break;
+            case 's': NEED(1); o->as = IARG(1); i++; break;
+            case 'b': NEED(1); o->ab = IARG(1); i++; break;
+            case 'i': case 'I': case 'e': case 'E': case 'f':
+                return set_err(GB_EUNSUPPORTED, "option %s (ambient lists/files) is not supported", a);
+            default: ok = false;
+            }
+            break;
+        case 'm':
+            if (prog == GB_PROG_RCONTRIB && !a[2]) { ok = false; break; }
+            return set_err(GB_EUNSUPPORTED, "participating media (%s) are not supported", a);
+        case 'h': ok = boolopt(a, 2, &o->h) == 0; break;
+        case 'n': NEED(1); o->n = IARG(1); i++; break;
+        case 'x': NEED(1); o->x = IARG(1); i++; break;
+        case 'y': NEED(1); o->y = IARG(1); i++; break;
+        case 'c':
+            if (prog == GB_PROG_RCONTRIB && !a[2]) { NEED(1); o->c = IARG(1); i++; }
+            else return set_err(GB_EUNSUPPORTED, "option %s is not supported", a);
+            break;
+        case 'V': ok = prog == GB_PROG_RCONTRIB && boolopt(a, 2, &o->V) == 0; break;
+        case 'f':
+            if (!a[2]) { ok = false; break; }     /* -f calfile: modifier option */
+            if (a[2] == 'o') break;               /* -fo force open */
+            if (!strchr("afd", a[2])) { ok = false; break; }
+            o->fin = a[2];
+            o->fout = a[3] ? a[3] : a[2];
+            if (!strchr("afdc", o->fout)) ok = false;
+            break;
+        case 'o':
+            if (prog == GB_PROG_RTRACE && a[2]) {
+                snprintf(o->outspec, sizeof o->outspec, "%s", a + 2);
+                break;
+            }
+            ok = false;
+            break;
+        case 'e': case 'p': case 'b' + 256: case 'M':
+            ok = false;
+            break;
+        case 't': NEED(1); i++; break;            /* report interval */
+        default: ok = false;
+        }
+        if (!ok) {
+            if (prog == GB_PROG_RCONTRIB && strchr("fepbmMo", a[1]))
+                break;                             /* modifier options: caller */
+            return set_err(GB_EINVAL, "command line error at '%s'", a);
+        }
+#undef NEED
+#undef FARG
+#undef IARG
+    }
+    if (nused)
+        *nused = i;
+    return GB_OK;
+}
+
+/* -------------------------------------------------------- run machinery */
+
+static int check_shading(gb_scene *G, const gb_opts *o)
+{
+    if (!G->unsupported.empty()) {
+        const gb_object *m = &G->H.objs[G->unsupported[0]];
+        std::string why;
+        float4 a, b;
+        material_kind(m, &a, &b, why);
+        return set_err(GB_EUNSUPPORTED, "%s (\"%s\")", why.c_str(), m->name);
+    }
+    if (!G->src_error.empty())
+        return set_err(GB_EUNSUPPORTED, "%s", G->src_error.c_str());
+    if (o->ab > 0 && o->aa > GB_FTINY)
+        return set_err(GB_EUNSUPPORTED, "the ambient cache (-aa %g) is not implemented; use -aa 0", o->aa);
+    if (o->as > 0 && o->ab > 0 && o->aa > GB_FTINY)
+        return set_err(GB_EUNSUPPORTED, "ambient super-sampling (-as) is not implemented");
+    if (o->i)
+        return set_err(GB_EUNSUPPORTED, "-i (irradiance at the hit surface) is not implemented");
+    if (!o->bv)
+        return set_err(GB_EUNSUPPORTED, "-bv- is not implemented");
+    if (!o->dv)
+        return set_err(GB_EUNSUPPORTED, "-dv- is not implemented");
+    if (o->ld != 0)
+        return set_err(GB_EUNSUPPORTED, "-ld is not implemented");
+    if (o->ds > GB_FTINY) {
+        for (const gb_dsrc &s : G->src)
+            if (!(s.flags & (DS_SKIP | DS_DISTANT)))
+                return set_err(GB_EUNSUPPORTED,
+                               "source subdivision (-ds %g) of local sources is not implemented; use -ds 0", o->ds);
+    }
+    /* rough specular needing sampling (rt/normal.c:364 gaussamp) */
+    for (size_t sl = 0; sl < G->matobj.size(); sl++) {
+        float4 a = G->mat[2 * sl], b = G->mat[2 * sl + 1];
+        int k = (int)a.x;
+        if ((k == DM_PLASTIC || k == DM_METAL) && b.y * b.y > GB_FTINY) {
+            double rspec = b.x;
+            if (rspec > GB_FTINY && !(o->st >= rspec - GB_FTINY))
+                return set_err(GB_EUNSUPPORTED,
+                               "rough specular sampling of \"%s\" (specularity %g above -st %g) is not implemented",
+                               G->H.objs[G->matobj[sl]].name, rspec, o->st);
+        }
+    }
+    return GB_OK;
+}
+
+static uint64_t seed_of(const gb_opts *o)
+{
+    if (o->seed)
+        return o->seed;
+    if (!o->u)
+        return 0;
+    return (uint64_t)time(nullptr) * 0x9E3779B97F4A7C15ull;
+}
+
+static int root_divisions(const gb_opts *o)
+{
+    /* samp_hemi for the Lambertian (rho = pi) at weight 1 (rt/ambcomp.c:366-374) */
+    double d = M_PI, wt = 1.0;
+    d *= 0.8 * 1.0 / (o->ad * o->lw + 1e-20);
+    if (wt > d) wt = d;
+    int n = (int)(sqrt(o->ad * wt) + 0.5);
+    return n < 1 ? 1 : n;
+}
+
+struct RunOut {
+    double *value;          /* host n x 3 or null */
+    double *bins;           /* host records x nbins x 3 or null */
+    int32_t *hit_id;
+    double *hit_t;
+};
+
+static int run(gb_scene *G, const gb_opts *o, int follow, const double *org_dir, int64_t n,
+               const std::vector<gb_binins> *prog, const std::vector<int4> *modinfo, int nbins_total,
+               const std::vector<int> *trk, RunOut out)
+{
+    cudaStream_t st = G->stream;
+    g_stats[0] = g_stats[1] = g_stats[2] = g_stats[3] = 0;
+    if (n <= 0)
+        return GB_OK;
+    size_t sbytes = (size_t)n * 6 * sizeof(double);
+    if (G->sensors.ensure(sbytes) < 0 || G->stats.ensure(GB_ST_N * sizeof(unsigned long long)) < 0 ||
+        G->qcount.ensure(4 * sizeof(unsigned long long)) < 0)
+        return set_err(GB_ENOMEM, "device allocation failed");
+    CK(cudaMemcpyAsync(G->sensors.p, org_dir, sbytes, cudaMemcpyHostToDevice, st));
+    CK(cudaMemsetAsync(G->stats.p, 0, GB_ST_N * sizeof(unsigned long long), st));
+
+    gb_run P;
+    memset(&P, 0, sizeof P);
+    P.S = G->ds;
+    P.ab = o->ab;
+    P.ad = o->ad;
+    P.minweight = (float)o->lw;
+    P.maxdepth = o->lr;
+    for (int j = 0; j < 3; j++) P.av[j] = (float)o->av[j];
+    P.dstrsrc = (float)o->dj;
+    P.specthresh = (float)o->st;
+    P.follow = follow;
+    P.contrib_mode = o->V;
+    uint64_t seed = seed_of(o);
+    P.k0 = (uint32_t)seed;
+    P.k1 = (uint32_t)(seed >> 32);
+    P.replica = o->replica;
+    P.nsensors = n;
+    P.sensors = (const double *)G->sensors.p;
+    P.stats = (unsigned long long *)G->stats.p;
+    P.accum = o->c > 0 ? o->c : 1;
+    P.nbins_total = nbins_total;
+
+    /* cast-only outputs */
+    if (out.hit_id) {
+        if (G->hits.ensure((size_t)n * sizeof(int)) < 0 || G->hitt.ensure((size_t)n * sizeof(float)) < 0)
+            return set_err(GB_ENOMEM, "device allocation failed");
+        P.S.trk = nullptr;
+        if (gb_launch_cast(&P, (int *)G->hits.p, (float *)G->hitt.p, nullptr, st, G->sms) < 0)
+            return set_err(GB_ECUDA, "cast launch failed: %s", cudaGetErrorString(cudaGetLastError()));
+        g_stats[3]++;
+        std::vector<int> h(n);
+        std::vector<float> t(n);
+        CK(cudaMemcpyAsync(h.data(), G->hits.p, (size_t)n * sizeof(int), cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpyAsync(t.data(), G->hitt.p, (size_t)n * sizeof(float), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        for (int64_t i = 0; i < n; i++) {
+            out.hit_id[i] = h[i];
+            if (out.hit_t)
+                out.hit_t[i] = t[i];
+        }
+        if (!out.value && !out.bins) {
+            g_stats[0] = n;
+            return GB_OK;
+        }
+    }
+
+    if (out.value) {
+        if (G->value.ensure((size_t)n * 3 * sizeof(double)) < 0)
+            return set_err(GB_ENOMEM, "device allocation failed");
+        CK(cudaMemsetAsync(G->value.p, 0, (size_t)n * 3 * sizeof(double), st));
+        P.value = (double *)G->value.p;
+    }
+    int64_t nrec = n / P.accum;
+    if (out.bins) {
+        size_t bb = (size_t)(nrec > 0 ? nrec : 1) * nbins_total * 3 * sizeof(double);
+        if (G->bins.ensure(bb) < 0 || upload(G->binprog, *prog) < 0 || upload(G->modinfo, *modinfo) < 0 ||
+            upload(G->trkrun, *trk) < 0)
+            return set_err(GB_ENOMEM, "device allocation failed");
+        CK(cudaMemsetAsync(G->bins.p, 0, bb, st));
+        P.bins = (double *)G->bins.p;
+        P.binprog = (const gb_binins *)G->binprog.p;
+        P.modinfo = (const int4 *)G->modinfo.p;
+        P.S.trk = (const int *)G->trkrun.p;
+    } else {
+        std::vector<int> none(G->H.nobjs > 0 ? G->H.nobjs : 1, -1);
+        if (upload(G->trkrun, none) < 0)
+            return set_err(GB_ENOMEM, "device allocation failed");
+        P.S.trk = (const int *)G->trkrun.p;
+    }
+
+    /* queues: sized for the expected fan-out, bounded by memory */
+    int n0 = (o->I && o->ab > 0 && o->ad > 0) ? root_divisions(o) : 0;
+    long long est = (long long)n * (n0 > 0 ? (long long)n0 * n0 * 4 : (o->ab > 0 ? (long long)o->ad * 2 : 8));
+    long long qcap = est < (1ll << 20) ? (1ll << 20) : est;
+    size_t freeb = 0, totalb = 0;
+    cudaMemGetInfo(&freeb, &totalb);
+    long long qmax = (long long)(freeb / 4 / sizeof(gb_qray));
+    if (qmax > (1ll << 28)) qmax = 1ll << 28;
+    if (qcap > qmax) qcap = qmax;
+    if (G->qa.ensure((size_t)qcap * sizeof(gb_qray)) < 0 || G->qb.ensure((size_t)qcap * sizeof(gb_qray)) < 0)
+        return set_err(GB_ENOMEM, "cannot allocate %lld-ray work queues", qcap);
+    P.qcap = qcap;
+    unsigned long long *cnt = (unsigned long long *)G->qcount.p;   /* [0] A, [1] B */
+    CK(cudaMemsetAsync(cnt, 0, 2 * sizeof(unsigned long long), st));
+    gb_qray *qa = (gb_qray *)G->qa.p, *qb = (gb_qray *)G->qb.p;
+
+    if (o->I) {
+        if (n0 > 0) {
+            if (G->roots.ensure((size_t)n * sizeof(gb_rootrec)) < 0 ||
+                G->rootspt.ensure((size_t)n * n0 * n0 * sizeof(float2)) < 0)
+                return set_err(GB_ENOMEM, "device allocation failed");
+            P.roots = (gb_rootrec *)G->roots.p;
+            P.root_spt = (float2 *)G->rootspt.p;
+        }
+        P.root_n = n0;
+        if (gb_launch_root(&P, st, G->sms) < 0)
+            return set_err(GB_ECUDA, "launch failed: %s", cudaGetErrorString(cudaGetLastError()));
+        g_stats[3]++;
+        if (n0 > 0) {
+            P.qout = qa;
+            P.qout_count = cnt;
+            if (gb_launch_gen_root(&P, st, G->sms) < 0)
+                return set_err(GB_ECUDA, "launch failed: %s", cudaGetErrorString(cudaGetLastError()));
+            g_stats[3]++;
+        }
+    } else {
+        P.qout = qa;
+        P.qout_count = cnt;
+        if (gb_launch_primary(&P, st, G->sms) < 0)
+            return set_err(GB_ECUDA, "launch failed: %s", cudaGetErrorString(cudaGetLastError()));
+        g_stats[3]++;
+    }
+    /* later generations until the queue drains */
+    int in = 0;
+    for (int gen = 0; gen < 64; gen++) {
+        unsigned long long c = 0;
+        CK(cudaMemcpyAsync(&c, cnt + in, sizeof c, cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        if (c == 0)
+            break;
+        if ((long long)c > qcap)
+            return set_err(GB_EOVERFLOW, "ray queue overflow (%llu rays for %lld slots)", c, qcap);
+        P.qin = in ? qb : qa;
+        P.qin_count = cnt + in;
+        P.qout = in ? qa : qb;
+        P.qout_count = cnt + (1 - in);
+        CK(cudaMemsetAsync(cnt + (1 - in), 0, sizeof(unsigned long long), st));
+        if (gb_launch_gen(&P, st, G->sms) < 0)
+            return set_err(GB_ECUDA, "launch failed: %s", cudaGetErrorString(cudaGetLastError()));
+        g_stats[3]++;
+        CK(cudaMemsetAsync(cnt + in, 0, sizeof(unsigned long long), st));
+        in = 1 - in;
+    }
+    unsigned long long stats[GB_ST_N];
+    CK(cudaMemcpyAsync(stats, G->stats.p, sizeof stats, cudaMemcpyDeviceToHost, st));
+    if (out.value)
+        CK(cudaMemcpyAsync(out.value, G->value.p, (size_t)n * 3 * sizeof(double), cudaMemcpyDeviceToHost, st));
+    if (out.bins && nrec > 0)
+        CK(cudaMemcpyAsync(out.bins, G->bins.p, (size_t)nrec * nbins_total * 3 * sizeof(double),
+                           cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    g_stats[0] = (int64_t)stats[GB_ST_RAYS];
+    g_stats[1] = (int64_t)stats[GB_ST_STEPS];
+    g_stats[2] = (int64_t)stats[GB_ST_CONTRIB];
+    if (stats[GB_ST_OVERFLOW])
+        return set_err(GB_EOVERFLOW, "ray queue overflow (%llu records dropped)", stats[GB_ST_OVERFLOW]);
+    return GB_OK;
+}
+
+extern "C" int gb_rtrace(gb_scene *G, const gb_opts *o, const double *org_dir, int64_t n, double *out_rgb,
+                         int32_t *hit_id, double *hit_t)
+{
+    if (!G || !o || (!org_dir && n > 0))
+        return set_err(GB_EINVAL, "null argument");
+    if (out_rgb) {
+        int rc = check_shading(G, o);
+        if (rc < 0)
+            return rc;
+    }
+    RunOut out = {out_rgb, nullptr, hit_id, hit_t};
+    return run(G, o, 0, org_dir, n, nullptr, nullptr, 0, nullptr, out);
+}
+
+static int compile_mods(gb_scene *G, const gb_modspec *mods, int nmods, std::vector<gb_binins> &prog,
+                        std::vector<int4> &info, std::vector<int> *trk, int *nbins_total)
+{
+    int total = 0;
+    prog.clear();
+    info.clear();
+    if (trk)
+        trk->assign(G ? (G->H.nobjs > 0 ? G->H.nobjs : 1) : 0, -1);
+    for (int m = 0; m < nmods; m++) {
+        std::vector<gb_binins> p;
+        std::string err;
+        int nb = 0;
+        if (!mods[m].modifier)
+            return set_err(GB_EINVAL, "modifier %d has no name", m);
+        if (gb_compile_bin(mods[m].binv, mods[m].params, mods[m].calfile, mods[m].expr, mods[m].nbins, p, &nb,
+                           err) < 0)
+            return set_err(GB_EUNSUPPORTED, "modifier '%s': %s", mods[m].modifier, err.c_str());
+        for (int k = 0; k < m; k++)
+            if (!strcmp(mods[k].modifier, mods[m].modifier))
+                return set_err(GB_EINVAL, "duplicate modifier '%s'", mods[m].modifier);
+        if (!strcmp(mods[m].modifier, "void"))
+            return set_err(GB_EINVAL, "cannot track 'void' modifier");
+        info.push_back(make_int4((int)prog.size(), nb, total, 0));
+        prog.insert(prog.end(), p.begin(), p.end());
+        total += nb;
+        if (trk && G) {
+            for (int32_t i = 0; i < G->H.nobjs; i++) {
+                int32_t mo = G->H.objs[i].omod;
+                if (mo >= 0 && !strcmp(G->H.objs[mo].name, mods[m].modifier))
+                    (*trk)[i] = m;
+            }
+        }
+    }
+    *nbins_total = total;
+    return GB_OK;
+}
+
+extern "C" int gb_rcontrib_nbins(const gb_modspec *mods, int nmods, int *nbins_total)
+{
+    std::vector<gb_binins> prog;
+    std::vector<int4> info;
+    return compile_mods(nullptr, mods, nmods, prog, info, nullptr, nbins_total);
+}
+
+extern "C" int gb_rcontrib(gb_scene *G, const gb_opts *o, const gb_modspec *mods, int nmods,
+                           const double *org_dir, int64_t n, double *out, int64_t *ray_count)
+{
+    if (!G || !o || !mods || nmods <= 0 || (!org_dir && n > 0) || !out)
+        return set_err(GB_EINVAL, "null argument or no modifiers");
+    gb_opts oo = *o;
+    /* rt/rcmain.c:164-172 override_options */
+    oo.dt = 0;
+    oo.as = 0;
+    oo.aa = 0;
+    int rc = check_shading(G, &oo);
+    if (rc < 0)
+        return rc;
+    std::vector<gb_binins> prog;
+    std::vector<int4> info;
+    std::vector<int> trk;
+    int nbt = 0;
+    rc = compile_mods(G, mods, nmods, prog, info, &trk, &nbt);
+    if (rc < 0)
+        return rc;
+    if (oo.V) {
+        /* contributions need the radiance of the tracked surface, which is
+         * local only for light sources */
+        for (int32_t i = 0; i < G->H.nobjs; i++) {
+            if (trk[i] < 0) continue;
+            int ms = G->matslot[i];
+            int k = ms >= 0 ? (int)G->mat[2 * ms].x : DM_NONE;
+            if (k != DM_LIGHT && k != DM_GLOW)
+                return set_err(GB_EUNSUPPORTED, "-V with a non-emitting tracked modifier is not implemented");
+        }
+    }
+    RunOut ro = {nullptr, out, nullptr, nullptr};
+    rc = run(G, &oo, 1, org_dir, n, &prog, &info, nbt, &trk, ro);
+    if (ray_count)
+        *ray_count = g_stats[0];
+    if (rc == GB_OK && oo.c > 1) {
+        int64_t nrec = n / oo.c;
+        double sf = 1.0 / oo.c;
+        for (int64_t i = 0; i < nrec * nbt * 3; i++)
+            out[i] *= sf;
+    }
+    return rc;
+}
+
+/* ------------------------------------------------------------- dctimestep */
+
+extern "C" int gb_dctimestep_device(const float *d_dc, const float *d_sky, int64_t M, int64_t K, int64_t N,
+                                    int mode, float *d_out, void *stream)
+{
+    std::string err;
+    int rc = gb_dct_device(d_dc, d_sky, M, K, N, mode, d_out, (cudaStream_t)stream, err);
+    if (rc < 0)
+        return set_err(rc, "%s", err.c_str());
+    return GB_OK;
+}
+
+extern "C" int gb_dctimestep(const float *dc, const float *sky, int64_t M, int64_t K, int64_t N, int mode,
+                             float *out)
+{
+    if (!dc || !sky || !out || M <= 0 || K <= 0 || N <= 0)
+        return set_err(GB_EINVAL, "bad matrix arguments");
+    float *a = nullptr, *b = nullptr, *c = nullptr;
+    size_t na = (size_t)M * K * 3, nb = (size_t)K * N * 3, nc = (size_t)M * N * 3;
+    cudaStream_t st;
+    CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    int rc = GB_OK;
+    if (cudaMalloc(&a, na * 4) != cudaSuccess || cudaMalloc(&b, nb * 4) != cudaSuccess ||
+        cudaMalloc(&c, nc * 4) != cudaSuccess) {
+        rc = set_err(GB_ENOMEM, "cannot allocate matrices on the device");
+    } else {
+        cudaMemcpyAsync(a, dc, na * 4, cudaMemcpyHostToDevice, st);
+        cudaMemcpyAsync(b, sky, nb * 4, cudaMemcpyHostToDevice, st);
+        rc = gb_dctimestep_device(a, b, M, K, N, mode, c, st);
+        if (rc == GB_OK) {
+            cudaMemcpyAsync(out, c, nc * 4, cudaMemcpyDeviceToHost, st);
+            cudaError_t e = cudaStreamSynchronize(st);
+            if (e != cudaSuccess)
+                rc = set_err(GB_ECUDA, "dctimestep: %s", cudaGetErrorString(e));
+        }
+    }
+    cudaFree(a);
+    cudaFree(b);
+    cudaFree(c);
+    cudaStreamDestroy(st);
+    return rc;
+}

@@ -12,7 +12,7 @@
  *   - face/cube overlap by vertex location, Cohen-Sutherland edge clipping
  *     and the plane test (ot/o_face.c:40-99, common/clip.c:19-72,
  *     common/plocate.c); sphere/cube by ot/sphere.c:50-109; cones, cups,
- *     cylinders, tubes and rings conservatively by their bounding boxes;
+ *     cylinders, tubes and rings by the strict test of ot/o_cone.c:41-126;
  *   - identical sibling leaves merged (common/octree.c:73-90).
  */
 #include "scene.h"
@@ -281,6 +281,8 @@ static void cone_bbox(const gb_object *o, const gb_cone *co, double mn[3], doubl
     }
 }
 
+static int cone_cube(const gb_object *o, const gb_cone *co, const double org[3], double size, double mincusize);
+
 static int object_cube(builder *B, int32_t obj, const double org[3], double size)
 {
     const gb_scene_host *S = B->S;
@@ -296,19 +298,72 @@ static int object_cube(builder *B, int32_t obj, const double org[3], double size
     case GT_CYLINDER:
     case GT_TUBE:
     case GT_RING: {
-        double mn[3], mx[3];
-        int i;
         if (!S->cones[obj].ok)
             return O_MISS;
-        cone_bbox(o, &S->cones[obj], mn, mx);
-        for (i = 0; i < 3; i++)
-            if (mx[i] < org[i] - GB_FTINY || mn[i] > org[i] + size + GB_FTINY)
-                return O_MISS;
-        return O_HIT;
+        return cone_cube(o, &S->cones[obj], org, size, B->mincusize);
     }
     default:
         return O_MISS;
     }
+}
+
+/* ot/o_cone.c:41-105 with STRICT (as it is compiled): the cone segment
+ * nearest the cube centre against the cube's bounding sphere, then clipped
+ * to the cube, else the eight sub-cubes down to the minimum cube size */
+static int cone_cube(const gb_object *o, const gb_cone *co, const double org[3], double size, double mincusize)
+{
+    const double *ca = o->farg;
+    double ad[3], p[3], v[3], ep0[3], ep1[3], r, d, l, ks;
+    int i, j;
+    if (o->otype == GT_RING)
+        for (i = 0; i < 3; i++) ad[i] = ca[3 + i];
+    else
+        for (i = 0; i < 3; i++) ad[i] = ca[co->p1 + i] - ca[co->p0 + i];
+    l = sqrt(ad[0] * ad[0] + ad[1] * ad[1] + ad[2] * ad[2]);
+    for (i = 0; i < 3; i++) ad[i] /= l;
+    r = size * 0.5;
+    for (i = 0; i < 3; i++) p[i] = org[i] + r;
+    r *= 1.732050808;
+    /* findcseg: segment of the cone surface nearest p */
+    for (i = 0; i < 3; i++) v[i] = p[i] - ca[co->p0 + i];
+    d = v[0] * ad[0] + v[1] * ad[1] + v[2] * ad[2];
+    for (i = 0; i < 3; i++) v[i] -= d * ad[i];
+    l = sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+    if (l != 0.0) {
+        double dd = 0, d1 = 0, d2 = 0, q, cumin[3], cumax[3];
+        for (i = 0; i < 3; i++) {
+            v[i] /= l;
+            ep0[i] = ca[co->r0] * v[i] + ca[co->p0 + i];
+            ep1[i] = ca[co->r1] * v[i] + ca[co->p1 + i];
+        }
+        /* common/fvect.c:77-99 dist2lseg */
+        for (i = 0; i < 3; i++) {
+            dd += (ep1[i] - ep0[i]) * (ep1[i] - ep0[i]);
+            d1 += (p[i] - ep0[i]) * (p[i] - ep0[i]);
+            d2 += (p[i] - ep1[i]) * (p[i] - ep1[i]);
+        }
+        if (d2 > d1 && d2 - d1 > dd) q = d1;
+        else if (d2 <= d1 && d1 - d2 > dd) q = d2;
+        else { double e = dd + d1 - d2; q = d1 - 0.25 * e * e / dd; }
+        if (q > (r + GB_FTINY) * (r + GB_FTINY))
+            return O_MISS;
+        for (i = 0; i < 3; i++) {
+            cumin[i] = org[i];
+            cumax[i] = org[i] + size;
+        }
+        if (clip_seg(ep0, ep1, cumin, cumax))
+            return O_HIT;
+    }
+    ks = size * 0.5;                    /* check sub-cubes */
+    if (ks < mincusize)
+        return O_HIT;
+    for (j = 0; j < 8; j++) {
+        double ko[3];
+        for (i = 0; i < 3; i++) ko[i] = org[i] + (((1 << i) & j) ? ks : 0.0);
+        if (cone_cube(o, co, ko, ks, mincusize))
+            return O_HIT;
+    }
+    return O_MISS;
 }
 
 static void addobject(builder *B, int32_t nd, const double org[3], double size, int32_t obj);

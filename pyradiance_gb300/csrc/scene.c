@@ -88,8 +88,7 @@ int gb_is_transp(int t)
 }
 int gb_is_volume(int t)
 {
-    return t == GT_SPHERE || t == GT_BUBBLE || t == GT_CONE || t == GT_CUP ||
-           t == GT_CYLINDER || t == GT_TUBE;
+    return t == GT_INSTANCE || t == GT_MESH;     /* T_V in common/otypes.h:126-137 */
 }
 
 /* ---------------------------------------------------------------- storage */

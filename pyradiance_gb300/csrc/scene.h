@@ -44,7 +44,7 @@ int gb_is_surface(int t);
 int gb_is_material(int t);
 int gb_is_light(int t);          /* light, illum, glow, spotlight */
 int gb_is_transp(int t);         /* rt/otspecial.h:14 (trans, glass, dielectric, interface) */
-int gb_is_volume(int t);         /* sphere, bubble, cone, cup, cylinder, tube */
+int gb_is_volume(int t);         /* instance, mesh (octree volumes) */
 
 typedef struct {
     int      otype;              /* enum gb_otype */

@@ -1,0 +1,1038 @@
+/*
+ * trace.cu -- the GB300 wavefront path engine behind rtrace and rcontrib.
+ *
+ * Work is organised by ray generation instead of by recursion:
+ *   k_root      one thread per sensor: the -I "pretend hit" Lambertian at the
+ *               sensor (rt/rtrace.c:416-433, rt/rcontrib.c:321-338), its
+ *               direct component, and the frame of its ambient hemisphere;
+ *   k_gen_root  the first hemisphere, expanded lazily: ray index ->
+ *               (sensor, stratum), so the 1,024 strata of every sensor are
+ *               traced in parallel without being written to memory;
+ *   k_primary   radiance mode: the sensor rays themselves as generation 0;
+ *   k_gen       any later generation, from a queue of 64-byte ray records.
+ * Each ray is traced, shaded, and continues in the same thread with one of
+ * its children; the other children are appended to the next generation's
+ * queue with one atomic per coalesced group.  Contributions are added to
+ * FP64 per-sensor values and per-record bins with warp-aggregated atomics.
+ *
+ * Shading follows the reference: m_normal for plastic/metal with pure
+ * specular reflection (rt/normal.c:177-360, dirnorm :72-173), m_glass
+ * (rt/glass.c:45-165), m_light (rt/source.c:749-793), direct()
+ * (rt/source.c:398-556, srcray :219, nextssamp rt/srcsamp.c:37-145 with a
+ * single partition), the -aa 0 hemisphere (rt/ambient.c:269-297,
+ * rt/ambcomp.c:177-250, 351-421) and rayorigin's weights and Russian
+ * roulette (rt/raytrace.c:39-135).  rcontrib's trace callback
+ * (rt/rcontrib.c:272-316) is applied to every traced ray.
+ */
+#include <cooperative_groups.h>
+#include <cooperative_groups/scan.h>
+#include "trace.cuh"
+#include "tracehost.h"
+
+namespace cg = cooperative_groups;
+
+#define FRESTHRESH 0.017999f
+__device__ __forceinline__ float fresne(float ci) { return expf(-5.85f * ci) - 0.00202943064f; }
+
+/* stats slots */
+/* stats slots: see tracehost.h (GB_ST_*) */
+#define ST_RAYS GB_ST_RAYS
+#define ST_STEPS GB_ST_STEPS
+#define ST_CONTRIB GB_ST_CONTRIB
+#define ST_OVERFLOW GB_ST_OVERFLOW
+#define ST_BADBIN GB_ST_BADBIN
+
+struct Ray {
+    float3 org, dir, coef;
+    float weight, lcoef;
+    int origin, rsrc;
+    uint32_t crtype;
+    int rlvl, adepth;
+    uint64_t path;
+    uint32_t sensor;
+};
+
+struct Counters {
+    unsigned long long rays, steps, contrib;
+};
+
+/* -------------------------------------------------------------- records */
+
+__device__ __forceinline__ void store_ray(gb_qray *q, const Ray &r)
+{
+    float4 a = make_float4(r.org.x, r.org.y, r.org.z, r.weight);
+    float4 b = make_float4(r.dir.x, r.dir.y, r.dir.z, r.lcoef);
+    float4 c = make_float4(r.coef.x, r.coef.y, r.coef.z, __int_as_float(r.origin));
+    uint4 d = make_uint4((uint32_t)r.path, (uint32_t)(r.path >> 32), r.sensor,
+                         (r.crtype & 0xffff) | ((uint32_t)r.rlvl << 16) | ((uint32_t)r.adepth << 24));
+    float4 *p = reinterpret_cast<float4 *>(q);
+    p[0] = a;
+    p[1] = b;
+    p[2] = c;
+    reinterpret_cast<uint4 *>(q)[3] = d;
+}
+
+__device__ __forceinline__ Ray load_ray(const gb_qray *q)
+{
+    const float4 *p = reinterpret_cast<const float4 *>(q);
+    float4 a = p[0], b = p[1], c = p[2];
+    uint4 d = reinterpret_cast<const uint4 *>(q)[3];
+    Ray r;
+    r.org = f3(a.x, a.y, a.z);
+    r.weight = a.w;
+    r.dir = f3(b.x, b.y, b.z);
+    r.lcoef = b.w;
+    r.coef = f3(c.x, c.y, c.z);
+    r.origin = __float_as_int(c.w);
+    r.path = (uint64_t)d.x | ((uint64_t)d.y << 32);
+    r.sensor = d.z;
+    r.crtype = d.w & 0xffff;
+    r.rlvl = (d.w >> 16) & 0xff;
+    r.adepth = (d.w >> 24) & 0xff;
+    r.rsrc = -1;
+    return r;
+}
+
+__device__ __forceinline__ void push_ray(const gb_run &P, const Ray &r)
+{
+    cg::coalesced_group g = cg::coalesced_threads();
+    unsigned long long base = 0;
+    if (g.thread_rank() == 0)
+        base = atomicAdd(P.qout_count, (unsigned long long)g.size());
+    base = g.shfl(base, 0) + g.thread_rank();
+    if (base < (unsigned long long)P.qcap)
+        store_ray(P.qout + base, r);
+    else if (g.thread_rank() == 0)
+        atomicAdd(P.stats + ST_OVERFLOW, 1ull);
+}
+
+/* ------------------------------------------------------- contributions */
+
+__device__ __forceinline__ void add_value(const gb_run &P, uint32_t sensor, float3 v)
+{
+    if (!P.value)
+        return;
+    if (v.x == 0.f && v.y == 0.f && v.z == 0.f)
+        return;
+    double *d = P.value + 3ull * sensor;
+    atomicAdd(d, (double)v.x);
+    atomicAdd(d + 1, (double)v.y);
+    atomicAdd(d + 2, (double)v.z);
+}
+
+/* rt/rcontrib.c:272-316: bin the chain coefficient of a ray that hit a
+ * tracked modifier; lanes adding to the same (record, bin) are merged first */
+__device__ __forceinline__ void add_bin(const gb_run &P, uint32_t sensor, int slot, float3 dir, float3 c,
+                                        Counters &cnt)
+{
+    int4 mi = P.modinfo[slot];           /* x: program offset, y: nbins, z: bin0 */
+    float bval = eval_bin(P.binprog + mi.x, dir);
+    if (bval <= -.5f)
+        return;
+    int bn = (int)(bval + .5f);
+    if (bn >= mi.y) {
+        atomicAdd(P.stats + ST_BADBIN, 1ull);   /* rt/rcontrib.c:305-309 warning */
+        return;
+    }
+    uint32_t rec = sensor / (uint32_t)P.accum;
+    unsigned long long key = (unsigned long long)rec * (unsigned long long)P.nbins_total + (unsigned long long)(mi.z + bn);
+    cnt.contrib++;
+    /* warp aggregation: lanes with the same key sum through shuffles */
+    unsigned int act = __activemask();
+    unsigned int grp = __match_any_sync(act, key);
+    float sx = 0.f, sy = 0.f, sz = 0.f;
+    for (int l = 0; l < 32; l++) {
+        if (grp & (1u << l)) {
+            sx += __shfl_sync(grp, c.x, l);
+            sy += __shfl_sync(grp, c.y, l);
+            sz += __shfl_sync(grp, c.z, l);
+        }
+    }
+    int leader = __ffs(grp) - 1;
+    if ((int)(threadIdx.x & 31) == leader) {
+        double *d = P.bins + 3ull * key;
+        atomicAdd(d, (double)sx);
+        atomicAdd(d + 1, (double)sy);
+        atomicAdd(d + 2, (double)sz);
+    }
+}
+
+/* rt/source.c:749-793 (m_light) for a ray r that hit light object obj;
+ * returns the radiance it carries (rcol) and applies rcontrib's callback */
+__device__ __forceinline__ void light_hit(const gb_run &P, const Ray &r, int obj, int ms, float t, float rod,
+                                          Counters &cnt, float3 *rcol_out)
+{
+    const gb_dscene &S = P.S;
+    float4 m0 = S.mat[2 * ms], m1 = S.mat[2 * ms + 1];
+    int mk = (int)m0.x;
+    float3 col = f3(m0.y, m0.z, m0.w);
+    float3 rcol = f3(0.f, 0.f, 0.f);
+    float3 rc = r.coef;
+    bool glow = mk == DM_GLOW;
+    bool distglow = glow && (m1.x >= -D_FTINY) && (t > m1.x);
+    bool bad = (r.crtype & (GB_AMBIENT | GB_SPECULAR)) && !((r.crtype & GB_SHADOW) || rod < 0.f || distglow);
+    bool wrong = r.rsrc >= 0 && S.src[r.rsrc].so != obj;
+    if (bad || wrong)
+        rc = f3(0.f, 0.f, 0.f);
+    else if (rod >= 0.f)
+        rcol = col;
+    if (rcol_out)
+        *rcol_out = rcol;
+    if (!(bad || wrong)) {
+        if (r.rsrc < 0)                  /* shadow values are added by direct() */
+            add_value(P, r.sensor, rc * rcol);
+        if (P.binprog) {
+            int slot = S.trk[obj];
+            if (slot >= 0 && (r.rsrc < 0 || S.src[r.rsrc].so == obj) && r.lcoef > D_FTINY) {
+                float3 c = P.contrib_mode ? rc * rcol : rc;
+                add_bin(P, r.sensor, slot, r.dir, c, cnt);
+            }
+        }
+    }
+}
+
+/* rcontrib callback for a ray that hit a non-light surface */
+__device__ __forceinline__ void surface_contrib(const gb_run &P, const Ray &r, int obj, Counters &cnt)
+{
+    if (!P.binprog || P.contrib_mode)
+        return;
+    int slot = P.S.trk[obj];
+    if (slot < 0 || r.lcoef <= D_FTINY)
+        return;
+    if (r.rsrc >= 0 && P.S.src[r.rsrc].so != obj)
+        return;
+    add_bin(P, r.sensor, slot, r.dir, r.coef, cnt);
+}
+
+/* ----------------------------------------------------------- rayorigin */
+
+/* rt/raytrace.c:39-135 for a child of `parent` of type rt with local
+ * coefficient rc (has_rc = 0 for the reference's NULL); decides Russian
+ * roulette with the child's own draw.  Returns false if the child dies. */
+__device__ __forceinline__ bool ray_origin(const gb_run &P, const Ray &parent, uint32_t rt, float3 rc,
+                                           bool has_rc, uint32_t code, Ray &c, float4 *u_out)
+{
+    float rw = 1.f;
+    if (has_rc) {
+        rw = maxc(rc);
+        if (rw > 1.f)
+            rw = 1.f;
+    } else
+        rc = f3(1.f, 1.f, 1.f);
+    c.path = gb_child(parent.path, code);
+    c.sensor = parent.sensor;
+    c.rsrc = parent.rsrc;
+    c.rlvl = parent.rlvl + ((rt & GB_RAYREFL) ? 1 : 0);
+    if ((rt & GB_RAYREFL) && c.rsrc >= 0)
+        c.rsrc = -1;
+    c.crtype = parent.crtype | rt;
+    c.adepth = parent.adepth;
+    c.weight = parent.weight * rw;
+    c.coef = parent.coef * rc;
+    c.lcoef = maxc(rc);
+    gb_u4 u = gb_draw(c.path, c.sensor, GB_G_CREATE, P.k0, P.k1);
+    if (u_out)
+        *u_out = make_float4(gb_u01(u.v[0]), gb_u01(u.v[1]), gb_u01(u.v[2]), gb_u01(u.v[3]));
+    if (c.weight <= 0.f)
+        return false;
+    if (c.crtype & GB_SHADOW)
+        return true;
+    if ((P.maxdepth <= 0) & has_rc) {
+        if ((P.maxdepth < 0) & (c.rlvl > -P.maxdepth))
+            return false;
+        if (c.weight >= P.minweight)
+            return true;
+        if (gb_u01(u.v[0]) > c.weight / P.minweight)
+            return false;
+        float s = P.minweight / c.weight;
+        c.coef = c.coef * s;
+        c.lcoef *= s;
+        c.weight = P.minweight;
+        return true;
+    }
+    return (c.weight >= P.minweight) & (c.rlvl <= abs(P.maxdepth));
+}
+
+/* common/fvect.c getperpendicular with randomized orientation */
+__device__ __forceinline__ float3 perpendicular(float3 v, float4 u, uint32_t ord_draw)
+{
+    float v1[3] = {0.5f - u.x, 0.5f - u.y, 0.5f - u.z};
+    int ord[3];
+    switch (gb_irand(ord_draw, 6u)) {
+    case 0: ord[0] = 0; ord[1] = 1; ord[2] = 2; break;
+    case 1: ord[0] = 0; ord[1] = 2; ord[2] = 1; break;
+    case 2: ord[0] = 1; ord[1] = 0; ord[2] = 2; break;
+    case 3: ord[0] = 1; ord[1] = 2; ord[2] = 0; break;
+    case 4: ord[0] = 2; ord[1] = 0; ord[2] = 1; break;
+    default: ord[0] = 2; ord[1] = 1; ord[2] = 0; break;
+    }
+    int i;
+    for (i = 3; i--;)
+        if ((-0.6f < comp(v, ord[i])) & (comp(v, ord[i]) < 0.6f))
+            break;
+    if (i < 0)
+        i = 0;
+    v1[ord[i]] = 1.f;
+    return normalize3(cross3(f3(v1[0], v1[1], v1[2]), v));
+}
+
+/* hemisphere frame of a hit, drawn from the hit ray's frame group */
+struct Hemi {
+    float3 onrm, ux, uy;
+    float3 acoef;       /* aval / n^2 */
+    int n;
+    uint32_t atyp;
+};
+
+__device__ __forceinline__ bool make_hemi(const gb_run &P, const Ray &r, float3 aval, float3 ron, Hemi &h)
+{
+    /* rt/ambcomp.c:351-421 (samp_hemi) for the ambacc <= FTINY case */
+    float d = maxc(aval);
+    if (d <= D_FTINY)
+        return false;
+    float wt = r.weight;
+    d *= 0.8f * r.weight / ((float)P.ad * P.minweight + 1e-20f);
+    if (wt > d)
+        wt = d;
+    int n = (int)(sqrtf((float)P.ad * wt) + 0.5f);
+    if (n < 1)
+        n = 1;
+    h.n = n;
+    h.atyp = GB_RAMBIENT;
+    h.onrm = ron;
+    h.acoef = aval * (1.f / (float)(n * n));
+    gb_u4 u = gb_draw(r.path, r.sensor, GB_G_FRAME, P.k0, P.k1);
+    h.ux = perpendicular(ron, make_float4(gb_u01(u.v[0]), gb_u01(u.v[1]), gb_u01(u.v[2]), 0.f), u.v[3]);
+    h.uy = cross3(h.onrm, h.ux);
+    return true;
+}
+
+/* child k of a hemisphere (rt/ambcomp.c:177-250 ambsample).  With
+ * spt == nullptr the disk position is the plain jitter of the child's own
+ * draw (hemispheres below 4 x 4 strata, where the reference makes no
+ * collision test); otherwise spt is the position placed by
+ * gb_place_sample. */
+__device__ __forceinline__ bool hemi_child(const gb_run &P, const Ray &parent, const Hemi &h, float3 hp,
+                                           int origin, int k, const float *spt, Ray &c)
+{
+    float4 u;
+    if (!ray_origin(P, parent, h.atyp, h.acoef, true, GB_C_STRATUM(k), c, &u))
+        return false;
+    float s[2];
+    if (spt) {
+        s[0] = spt[0];
+        s[1] = spt[1];
+    } else {
+        int i = k / h.n, j = k - i * h.n;
+        gb_square2disk(s, ((float)j + u.z) / (float)h.n, ((float)i + u.y) / (float)h.n);
+    }
+    float zd = sqrtf(fmaxf(0.f, 1.f - s[0] * s[0] - s[1] * s[1]));
+    c.dir = normalize3(h.ux * s[0] + h.uy * s[1] + h.onrm * zd);
+    c.org = hp;
+    c.origin = origin;
+    c.adepth = parent.adepth + 1;
+    return true;
+}
+
+#define MAX_HEMI_N 128
+
+/* Place every stratum of an n x n (n >= 4) hemisphere in the reference's
+ * order with collision avoidance; positions go to out (n*n float2, dead
+ * strata get x = 2).  Runs sequentially in one thread. */
+__device__ __noinline__ void place_hemi(const gb_run &P, const Ray &parent, const Hemi &h, float2 *out)
+{
+    gb_lot L;
+    float rows[2][MAX_HEMI_N][2];
+    float (*prev)[2] = rows[0], (*cur)[2] = rows[1];
+    gb_lot_init(&L, parent.path, parent.sensor, P.k0, P.k1);
+    const int n = h.n;
+    for (int k = 0; k < n; k++) {
+        rows[0][k][0] = rows[0][k][1] = 2.f;
+        rows[1][k][0] = rows[1][k][1] = 2.f;
+    }
+    for (int i = n - 1; i >= 0; i--) {
+        for (int j = n - 1; j >= 0; j--) {
+            Ray c;
+            float4 u;
+            int k = i * n + j;
+            float s[2] = {2.f, 2.f};
+            if (ray_origin(P, parent, h.atyp, h.acoef, true, GB_C_STRATUM(k), c, &u))
+                gb_place_sample(&L, n, i, j, u.y, u.z, i + 1 < n ? (const float(*)[2])prev : nullptr,
+                                (const float(*)[2])cur, s);
+            cur[j][0] = s[0];
+            cur[j][1] = s[1];
+            out[k] = make_float2(s[0], s[1]);
+        }
+        float(*t)[2] = prev;
+        prev = cur;
+        cur = t;
+        for (int k = 0; k < n; k++)
+            cur[k][0] = cur[k][1] = 2.f;
+    }
+}
+
+/* Spawn all children of a hemisphere of 4 x 4 strata or more met after the
+ * first generation: placed sequentially with collision avoidance and
+ * queued as they are placed (only two rows of positions are kept). */
+__device__ __noinline__ void spawn_hemi_big(const gb_run &P, const Ray &parent, const Hemi &h, float3 hp, int origin)
+{
+    gb_lot L;
+    float rows[2][MAX_HEMI_N][2];
+    float (*prev)[2] = rows[0], (*cur)[2] = rows[1];
+    const int n = h.n;
+    if (n > MAX_HEMI_N) {
+        atomicAdd(P.stats + GB_ST_OVERFLOW, 1ull);
+        return;
+    }
+    gb_lot_init(&L, parent.path, parent.sensor, P.k0, P.k1);
+    for (int k = 0; k < n; k++) {
+        rows[0][k][0] = rows[0][k][1] = 2.f;
+        rows[1][k][0] = rows[1][k][1] = 2.f;
+    }
+    for (int i = n - 1; i >= 0; i--) {
+        for (int j = n - 1; j >= 0; j--) {
+            Ray c;
+            float4 u;
+            int k = i * n + j;
+            float sp[2] = {2.f, 2.f};
+            if (ray_origin(P, parent, h.atyp, h.acoef, true, GB_C_STRATUM(k), c, &u)) {
+                gb_place_sample(&L, n, i, j, u.y, u.z, i + 1 < n ? (const float(*)[2])prev : nullptr,
+                                (const float(*)[2])cur, sp);
+                float zd = sqrtf(fmaxf(0.f, 1.f - sp[0] * sp[0] - sp[1] * sp[1]));
+                c.dir = normalize3(h.ux * sp[0] + h.uy * sp[1] + h.onrm * zd);
+                c.org = hp;
+                c.origin = origin;
+                c.adepth = parent.adepth + 1;
+                push_ray(P, c);
+            }
+            cur[j][0] = sp[0];
+            cur[j][1] = sp[1];
+        }
+        float(*t)[2] = prev;
+        prev = cur;
+        cur = t;
+        for (int k = 0; k < n; k++)
+            cur[k][0] = cur[k][1] = 2.f;
+    }
+}
+
+/* ------------------------------------------------------------- shading */
+
+struct Surf {                 /* rt/normal.c NORMDAT */
+    float3 mcolor, scolor, pnorm;
+    float rdiff, rspec, alpha2, pdot;
+    bool pure, refl, rblt, flat;
+};
+
+/* rt/normal.c:72-173 dirnorm (opaque materials: trans = 0) */
+__device__ __forceinline__ float3 dirnorm(const gb_run &P, const Surf &s, float3 rdir, float3 ldir, float omega)
+{
+    float3 v = f3(0.f, 0.f, 0.f);
+    float ldot = dot3(s.pnorm, ldir);
+    if (ldot < 0.f)
+        return v;
+    float lrdiff = s.rdiff;
+    if (s.pure && s.rspec >= FRESTHRESH && lrdiff > D_FTINY)
+        lrdiff *= 1.f - fresne(fabsf(ldot));
+    if ((ldot > D_FTINY) & (lrdiff > D_FTINY))
+        v = v + s.mcolor * (ldot * omega * lrdiff * (1.f / D_PI));
+    if ((ldot > D_FTINY) & s.refl & !s.pure) {
+        float dt = s.alpha2;
+        if (s.flat)
+            dt += (1.f - P.dstrsrc) * omega * (0.25f / D_PI);
+        float3 vt = ldir - rdir;
+        float d2 = dot3(vt, s.pnorm);
+        d2 *= d2;
+        float d3 = dot3(vt, vt);
+        float d4 = (d3 - d2) / d2;
+        dt = expf(-d4 / dt) * d3 / (D_PI * d2 * d2 * dt);
+        if (dt > D_FTINY)
+            v = v + s.scolor * (dt * ldot * omega);
+    }
+    return v;
+}
+
+/* Follow a shadow ray and its transmitted continuations (rt/source.c:497-545
+ * and the raycont() chain it starts).  Returns the value the sample adds
+ * to the ray's colour (scp->val): the potential when the first ray reaches
+ * the source or nothing, else coefficient x transmission x source radiance;
+ * applies the rcontrib callback to every ray of the chain. */
+__device__ float3 shadow_chain(const gb_run &P, Ray sr, int s, Counters &cnt, float3 coef, float3 potential)
+{
+    const gb_dscene &S = P.S;
+    const gb_dsrc &src = S.src[s];
+    float3 T = f3(1.f, 1.f, 1.f);           /* product of transmissions so far */
+    const float3 zero = f3(0.f, 0.f, 0.f);
+    for (int guard = 0; guard < 32; guard++) {
+        Hit h;
+        uint32_t st = 0;
+        cnt.rays++;
+        int okind = sr.origin >= 0 ? (S.obj[sr.origin].x & 0xff) : DK_NONE;
+        bool planar = okind == DK_FACE || okind == DK_RING;
+        bool hit = local_hit(S, sr.org, sr.dir, planar ? sr.origin : -1, D_FTINY, D_FHUGE, h, &st);
+        cnt.steps += st;
+        if (!hit) {
+            if (guard == 0) {
+                if (P.follow && (src.flags & DS_DISTANT)) {
+                    if (source_hit(S, sr.dir, s, sr.crtype) >= 0)
+                        light_hit(P, sr, src.so, src.mat, D_FHUGE, 1.f, cnt, nullptr);
+                }
+                return potential;
+            }
+            if (source_hit(S, sr.dir, s, sr.crtype) < 0)
+                return zero;
+            float3 rc;
+            light_hit(P, sr, src.so, src.mat, D_FHUGE, 1.f, cnt, &rc);
+            return coef * T * rc;
+        }
+        int ms = S.obj[h.obj].y;
+        int mk = ms >= 0 ? (int)S.mat[2 * ms].x : DM_NONE;
+        if (h.obj == src.so && guard == 0 && !P.follow)
+            return potential;                 /* aimed and reached */
+        float3 hp = sr.org + sr.dir * h.t;
+        if (mk == DM_LIGHT || mk == DM_GLOW) {
+            float3 rc;
+            light_hit(P, sr, h.obj, ms, h.t, h.rod, cnt, &rc);
+            return coef * T * rc;
+        }
+        if (mk == DM_NONE) {
+            surface_contrib(P, sr, h.obj, cnt);
+            Ray c;
+            ray_origin(P, sr, GB_TRANS, f3(1.f, 1.f, 1.f), false, GB_C_PASS, c, nullptr);
+            c.org = hp;
+            c.dir = sr.dir;
+            c.origin = h.obj;
+            sr = c;
+            continue;
+        }
+        if (mk == DM_GLASS) {
+            /* rt/glass.c:45-120, transmission only for shadow rays */
+            float4 m0 = S.mat[2 * ms], m1 = S.mat[2 * ms + 1];
+            float3 mc = f3(m0.y, m0.z, m0.w);
+            float rindex = m1.x;
+            if (!(maxc(mc) > 1e-15f))
+                return zero;
+            mc = f3(fmaxf(mc.x, 1e-15f), fmaxf(mc.y, 1e-15f), fmaxf(mc.z, 1e-15f));
+            float pdot = fabsf(h.rod);
+            float cos2 = sqrtf((1.f - 1.f / (rindex * rindex)) + pdot * pdot / (rindex * rindex));
+            mc = f3(powf(mc.x, 1.f / cos2), powf(mc.y, 1.f / cos2), powf(mc.z, 1.f / cos2));
+            float r1e = (pdot - rindex * cos2) / (pdot + rindex * cos2);
+            r1e *= r1e;
+            float r1m = (1.f / pdot - rindex / cos2) / (1.f / pdot + rindex / cos2);
+            r1m *= r1m;
+            float tc[3], mm[3] = {mc.x, mc.y, mc.z};
+            for (int i = 0; i < 3; i++) {
+                float d = mm[i];
+                tc[i] = .5f * (1.f - r1e) * (1.f - r1e) * d / (1.f - r1e * r1e * d * d) +
+                        .5f * (1.f - r1m) * (1.f - r1m) * d / (1.f - r1m * r1m * d * d);
+            }
+            surface_contrib(P, sr, h.obj, cnt);
+            Ray c;
+            float3 tcv = f3(tc[0], tc[1], tc[2]);
+            if (!ray_origin(P, sr, GB_TRANS, tcv, true, GB_C_TRANS, c, nullptr))
+                return zero;
+            c.org = hp;
+            c.dir = sr.dir;
+            c.origin = h.obj;
+            T = T * tcv;
+            sr = c;
+            continue;
+        }
+        /* opaque: blocked (rt/normal.c:190, m_normal's shadow test) */
+        surface_contrib(P, sr, h.obj, cnt);
+        return zero;
+    }
+    return zero;
+}
+
+/* rt/source.c:398-556 (direct) with single-partition sources
+ * (nextssamp/nopart) and every shadow tested */
+__device__ void direct(const gb_run &P, const Ray &r, float3 hp, const Surf &s, int origin, Counters &cnt)
+{
+    const gb_dscene &S = P.S;
+    for (int sn = 0; sn < S.nsrc; sn++) {
+        const gb_dsrc &src = S.src[sn];
+        if (src.flags & DS_SKIP)
+            continue;
+        float3 sloc = f3(src.sloc[0], src.sloc[1], src.sloc[2]);
+        if ((src.flags & (DS_PROX | DS_DISTANT)) == DS_PROX) {
+            float3 dv = hp - sloc;
+            float rr = src.prox + src.srad;
+            if (dot3(dv, dv) > rr * rr)
+                continue;
+        }
+        float vpos[3] = {0.f, 0.f, 0.f};
+        if (P.dstrsrc > D_FTINY) {
+            gb_u4 u = gb_draw(gb_child(r.path, GB_C_SHADOW(sn)), r.sensor, GB_G_SRC, P.k0, P.k1);
+            vpos[0] = P.dstrsrc * (1.f - 2.f * gb_u01(u.v[0]));
+            vpos[1] = P.dstrsrc * (1.f - 2.f * gb_u01(u.v[1]));
+            vpos[2] = (src.flags & DS_FLAT) ? 0.f : P.dstrsrc * (1.f - 2.f * gb_u01(u.v[2]));
+            if ((src.flags & DS_DISTANT) && P.dstrsrc > 0.7f) {
+                /* circular source trim (rt/srcsamp.c:85-96) */
+                float d = 1.12837917f;
+                float t0 = d * sqrtf(1.f - 0.5f * vpos[1] * vpos[1]);
+                float t1 = d * sqrtf(1.f - 0.5f * vpos[0] * vpos[0]);
+                vpos[0] *= t0;
+                vpos[1] *= t1;
+                vpos[2] = 0.f;
+            }
+        }
+        float3 dir = sloc + f3(src.ss[0][0], src.ss[0][1], src.ss[0][2]) * vpos[0] +
+                     f3(src.ss[1][0], src.ss[1][1], src.ss[1][2]) * vpos[1] +
+                     f3(src.ss[2][0], src.ss[2][1], src.ss[2][2]) * vpos[2];
+        if (!(src.flags & DS_DISTANT))
+            dir = dir - hp;
+        float dist = sqrtf(dot3(dir, dir));
+        if (dist == 0.f)
+            continue;
+        dir = dir * (1.f / dist);
+        float dom;
+        if (src.flags & DS_FLAT)
+            dom = -(src.snorm[0] * dir.x + src.snorm[1] * dir.y + src.snorm[2] * dir.z);
+        else
+            dom = 1.f;
+        if (src.flags & DS_DISTANT) {
+            dom *= src.ss2;
+        } else {
+            if (dom <= 1e-4f)
+                continue;
+            dom *= src.ss2 / (dist * dist);
+            if ((src.flags & DS_PROX) && dist > src.prox)
+                continue;
+        }
+        float3 coef = dirnorm(P, s, r.dir, dir, dom);
+        if (maxc(coef) <= 0.f)
+            continue;
+        /* potential (srcvalue): the source alone */
+        float4 m0 = S.mat[2 * src.mat];
+        float3 L = f3(m0.y, m0.z, m0.w);
+        if (src.flags & DS_DISTANT) {
+            float dt = dot3(sloc, dir);
+            if (2.f * D_PI * (1.f - dt) > src.ss2)
+                continue;
+        } else {
+            Hit hs;
+            hs.obj = -1;
+            hs.t = D_FHUGE;
+            hs.rod = 1.f;
+            hit_object(S, src.so, hp, dir, hs, D_FTINY);
+            if (hs.obj != src.so)
+                continue;                      /* aiming failure */
+            if (hs.rod < 0.f)
+                continue;                      /* behind the source: black */
+        }
+        float3 pot = coef * L;
+        if (0.2126f * pot.x + 0.7152f * pot.y + 0.0722f * pot.z <= 0.f)
+            continue;
+        /* shadow ray (rt/source.c:497-510) */
+        Ray sr;
+        bool thru = !(dot3(dir, s.pnorm) > 0.f);      /* thrudir, rt/ray.h:87 */
+        ray_origin(P, r, thru ? GB_TSHADOW : GB_RSHADOW, f3(1.f, 1.f, 1.f), false, GB_C_SHADOW(sn), sr, nullptr);
+        sr.coef = r.coef * coef;
+        sr.lcoef = maxc(coef);
+        sr.rsrc = sn;
+        sr.org = hp;
+        sr.dir = dir;
+        sr.origin = origin;
+        float3 v = shadow_chain(P, sr, sn, cnt, coef, pot);
+        add_value(P, r.sensor, r.coef * v);
+    }
+}
+
+/* Shade a hit on plastic or metal: returns false if unsupported */
+__device__ __forceinline__ void setup_surf(const gb_run &P, int mk, float4 m0, float4 m1, float3 n, float rod,
+                                           bool flat, Surf &s)
+{
+    s.mcolor = f3(m0.y, m0.z, m0.w);
+    s.alpha2 = m1.y * m1.y;
+    s.pure = s.alpha2 <= D_FTINY;
+    s.pnorm = n;
+    s.pdot = rod < .001f ? .001f : rod;
+    s.flat = flat;
+    s.rspec = m1.x;
+    float fest = 0.f;
+    if (s.pure && s.rspec >= FRESTHRESH) {
+        fest = fresne(s.pdot);
+        s.rspec += fest * (1.f - s.rspec);
+    }
+    s.rdiff = 1.f - s.rspec;
+    s.refl = s.rspec > D_FTINY;
+    if (s.refl) {
+        if (mk != DM_METAL)
+            s.scolor = f3(s.rspec, s.rspec, s.rspec);
+        else if (fest > D_FTINY) {
+            float d = m1.x * (1.f - fest);
+            s.scolor = f3(fest + s.mcolor.x * d, fest + s.mcolor.y * d, fest + s.mcolor.z * d);
+        } else
+            s.scolor = s.mcolor * s.rspec;
+    } else
+        s.scolor = f3(0.f, 0.f, 0.f);
+    s.rblt = !s.pure && P.specthresh >= s.rspec - D_FTINY;
+}
+
+#define MAXKIDS 2
+
+/* Trace ray r and its single-child continuations; other children go to the
+ * next generation.  `hemi_push` decides whether hemispheres are expanded
+ * here (deferred generations) or written out. */
+__device__ void run_ray(const gb_run &P, Ray r, Counters &cnt)
+{
+    const gb_dscene &S = P.S;
+    for (int guard = 0; guard < 256; guard++) {
+        Hit h;
+        cnt.rays++;
+        int okind = r.origin >= 0 ? (S.obj[r.origin].x & 0xff) : DK_NONE;
+        bool planar = okind == DK_FACE || okind == DK_RING;
+        unsigned long long steps = 0;
+        uint32_t st32 = 0;
+        bool hit = local_hit(S, r.org, r.dir, planar ? r.origin : -1, D_FTINY, D_FHUGE, h, &st32);
+        steps += st32;
+        cnt.steps += steps;
+        if (!hit) {
+            int sidx = source_hit(S, r.dir, r.rsrc, r.crtype);
+            if (sidx < 0)
+                return;
+            light_hit(P, r, S.src[sidx].so, S.src[sidx].mat, D_FHUGE, 1.f, cnt, nullptr);
+            return;
+        }
+        int ms = S.obj[h.obj].y;
+        int mk = ms >= 0 ? (int)S.mat[2 * ms].x : DM_NONE;
+        float3 hp = r.org + r.dir * h.t;
+        if (mk == DM_LIGHT || mk == DM_GLOW) {
+            light_hit(P, r, h.obj, ms, h.t, h.rod, cnt, nullptr);
+            return;
+        }
+        if (mk == DM_NONE) {
+            surface_contrib(P, r, h.obj, cnt);
+            Ray c;
+            ray_origin(P, r, GB_TRANS, f3(1.f, 1.f, 1.f), false, GB_C_PASS, c, nullptr);
+            c.org = hp;
+            c.dir = r.dir;
+            c.origin = h.obj;
+            r = c;
+            continue;
+        }
+        Ray kids[MAXKIDS];
+        int nk = 0;
+        float4 m0 = S.mat[2 * ms], m1 = S.mat[2 * ms + 1];
+        float3 n = h.n;
+        float rod = h.rod;
+        if (rod < 0.f) {                        /* flipsurface (backvis on) */
+            rod = -rod;
+            n = -n;
+        }
+        surface_contrib(P, r, h.obj, cnt);
+        if (mk == DM_GLASS) {
+            float3 mc = f3(m0.y, m0.z, m0.w);
+            float rindex = m1.x;
+            bool hastrans = maxc(mc) > 1e-15f;
+            mc = f3(fmaxf(mc.x, 1e-15f), fmaxf(mc.y, 1e-15f), fmaxf(mc.z, 1e-15f));
+            float pdot = rod;
+            float cos2 = sqrtf((1.f - 1.f / (rindex * rindex)) + pdot * pdot / (rindex * rindex));
+            if (hastrans)
+                mc = f3(powf(mc.x, 1.f / cos2), powf(mc.y, 1.f / cos2), powf(mc.z, 1.f / cos2));
+            float r1e = (pdot - rindex * cos2) / (pdot + rindex * cos2);
+            r1e *= r1e;
+            float r1m = (1.f / pdot - rindex / cos2) / (1.f / pdot + rindex / cos2);
+            r1m *= r1m;
+            float mm[3] = {mc.x, mc.y, mc.z}, tc[3], rc[3];
+            for (int i = 0; i < 3; i++) {
+                float d = mm[i];
+                tc[i] = .5f * (1.f - r1e) * (1.f - r1e) * d / (1.f - r1e * r1e * d * d) +
+                        .5f * (1.f - r1m) * (1.f - r1m) * d / (1.f - r1m * r1m * d * d);
+                float d2 = d * d;
+                rc[i] = .5f * r1e * (1.f + (1.f - 2.f * r1e) * d2) / (1.f - r1e * r1e * d2) +
+                        .5f * r1m * (1.f + (1.f - 2.f * r1m) * d2) / (1.f - r1m * r1m * d2);
+            }
+            if (hastrans) {
+                Ray c;
+                if (ray_origin(P, r, GB_TRANS, f3(tc[0], tc[1], tc[2]), true, GB_C_TRANS, c, nullptr)) {
+                    c.org = hp;
+                    c.dir = r.dir;
+                    c.origin = h.obj;
+                    kids[nk++] = c;
+                }
+            }
+            Ray c;
+            if (ray_origin(P, r, GB_REFLECTED, f3(rc[0], rc[1], rc[2]), true, GB_C_REFL, c, nullptr)) {
+                c.org = hp;
+                c.dir = normalize3(r.dir + n * (2.f * pdot));
+                c.origin = h.obj;
+                kids[nk++] = c;
+            }
+        } else {                                /* plastic / metal */
+            int okd = S.obj[h.obj].x & 0xff;
+            Surf s;
+            setup_surf(P, mk, m0, m1, n, rod, okd == DK_FACE || okd == DK_RING, s);
+            if (s.refl && s.pure) {
+                Ray c;
+                if (ray_origin(P, r, GB_REFLECTED, s.scolor, true, GB_C_REFL, c, nullptr)) {
+                    c.org = hp;
+                    c.dir = normalize3(r.dir + s.pnorm * (2.f * s.pdot));
+                    c.origin = h.obj;
+                    kids[nk++] = c;
+                }
+            }
+            if (!(s.pure && s.rdiff <= D_FTINY)) {
+                if (s.rdiff > D_FTINY) {
+                    float3 aval = s.mcolor * s.rdiff;
+                    if (s.rblt)
+                        aval = aval + s.scolor;
+                    if (P.ad > 0 && r.adepth < P.ab) {
+                        Hemi hm;
+                        if (make_hemi(P, r, aval, n, hm) && hm.n >= 4) {
+                            spawn_hemi_big(P, r, hm, hp, h.obj);
+                        } else if (hm.n > 0) {
+                            int nn = hm.n * hm.n;
+                            for (int k = 0; k < nn; k++) {
+                                Ray c;
+                                if (!hemi_child(P, r, hm, hp, h.obj, k, nullptr, c))
+                                    continue;
+                                if (nk < MAXKIDS)
+                                    kids[nk++] = c;
+                                else
+                                    push_ray(P, c);
+                            }
+                        }
+                    } else if (P.av[0] != 0.f || P.av[1] != 0.f || P.av[2] != 0.f) {
+                        add_value(P, r.sensor, r.coef * aval * f3(P.av[0], P.av[1], P.av[2]));
+                    }
+                }
+                if (S.nsrc > 0)
+                    direct(P, r, hp, s, h.obj, cnt);
+            }
+        }
+        if (nk == 0)
+            return;
+        for (int k = 1; k < nk; k++)
+            push_ray(P, kids[k]);
+        r = kids[0];
+    }
+}
+
+/* -------------------------------------------------------------- kernels */
+
+/* -I sensor: the Lambertian pretend-hit, its direct part and its frame */
+__global__ void k_root(gb_run P)
+{
+    Counters cnt = {0, 0, 0};
+    for (long long s = blockIdx.x * (long long)blockDim.x + threadIdx.x; s < P.nsensors;
+         s += (long long)gridDim.x * blockDim.x) {
+        const double *sv = P.sensors + 6 * s;
+        float3 org = f3((float)sv[0], (float)sv[1], (float)sv[2]);
+        float3 dir = normalize3(f3((float)sv[3], (float)sv[4], (float)sv[5]));
+        Ray r;
+        r.org = f3((float)(sv[0] + 1.1e-4 * sv[3]), (float)(sv[1] + 1.1e-4 * sv[4]), (float)(sv[2] + 1.1e-4 * sv[5]));
+        r.dir = -dir;
+        r.coef = f3(1.f, 1.f, 1.f);
+        r.weight = 1.f;
+        r.lcoef = 1.f;
+        r.origin = -1;
+        r.rsrc = -1;
+        r.crtype = GB_PRIMARY;
+        r.rlvl = 0;
+        r.adepth = 0;
+        r.path = GB_ROOT_PATH(P.replica);
+        r.sensor = (uint32_t)s;
+        float3 hp = f3((float)(sv[0] + 1e-4 * sv[3]), (float)(sv[1] + 1e-4 * sv[4]), (float)(sv[2] + 1e-4 * sv[5]));
+        Surf su;
+        su.mcolor = f3(D_PI, D_PI, D_PI);
+        su.scolor = f3(0.f, 0.f, 0.f);
+        su.pnorm = dir;
+        su.rdiff = 1.f;
+        su.rspec = 0.f;
+        su.alpha2 = 0.f;
+        su.pdot = 1.f;
+        su.pure = true;
+        su.refl = false;
+        su.rblt = false;
+        su.flat = false;
+        if (P.S.nsrc > 0)
+            direct(P, r, hp, su, -1, cnt);
+        if (P.root_n > 0) {
+            Hemi hm;
+            make_hemi(P, r, su.mcolor, dir, hm);
+            gb_rootrec *rr = P.roots + s;
+            rr->hp[0] = hp.x; rr->hp[1] = hp.y; rr->hp[2] = hp.z;
+            rr->nrm[0] = dir.x; rr->nrm[1] = dir.y; rr->nrm[2] = dir.z;
+            rr->ux[0] = hm.ux.x; rr->ux[1] = hm.ux.y; rr->ux[2] = hm.ux.z;
+            rr->n = hm.n;
+            if (hm.n >= 4)
+                place_hemi(P, r, hm, P.root_spt + s * (long long)hm.n * hm.n);
+        } else if (P.av[0] != 0.f || P.av[1] != 0.f || P.av[2] != 0.f) {
+            add_value(P, r.sensor, su.mcolor * f3(P.av[0], P.av[1], P.av[2]));
+        }
+    }
+    atomicAdd(P.stats + ST_RAYS, cnt.rays);
+    atomicAdd(P.stats + ST_CONTRIB, cnt.contrib);
+}
+
+/* first hemisphere of every -I sensor, expanded from (sensor, stratum) */
+__global__ void __launch_bounds__(256) k_gen_root(gb_run P)
+{
+    Counters cnt = {0, 0, 0};
+    const long long nn = (long long)P.root_n * P.root_n;
+    const long long total = nn * P.nsensors;
+    for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < total;
+         g += (long long)gridDim.x * blockDim.x) {
+        long long s = g / nn;
+        int k = (int)(g - s * nn);
+        const gb_rootrec *rr = P.roots + s;
+        Ray parent;
+        parent.org = f3(rr->hp[0], rr->hp[1], rr->hp[2]);
+        parent.coef = f3(1.f, 1.f, 1.f);
+        parent.weight = 1.f;
+        parent.lcoef = 1.f;
+        parent.origin = -1;
+        parent.rsrc = -1;
+        parent.crtype = GB_PRIMARY;
+        parent.rlvl = 0;
+        parent.adepth = 0;
+        parent.path = GB_ROOT_PATH(P.replica);
+        parent.sensor = (uint32_t)s;
+        Hemi hm;
+        hm.n = rr->n;
+        hm.atyp = GB_RAMBIENT;
+        hm.onrm = f3(rr->nrm[0], rr->nrm[1], rr->nrm[2]);
+        hm.ux = f3(rr->ux[0], rr->ux[1], rr->ux[2]);
+        hm.uy = cross3(hm.onrm, hm.ux);
+        float a = D_PI / (float)(hm.n * hm.n);
+        hm.acoef = f3(a, a, a);
+        Ray c;
+        const float *sp = nullptr;
+        float2 pk;
+        if (hm.n >= 4) {
+            pk = P.root_spt[g];
+            if (pk.x > 1.5f)
+                continue;                     /* stratum died in Russian roulette */
+            sp = &pk.x;
+        }
+        if (!hemi_child(P, parent, hm, parent.org, -1, k, sp, c))
+            continue;
+        run_ray(P, c, cnt);
+    }
+    atomicAdd(P.stats + ST_RAYS, cnt.rays);
+    atomicAdd(P.stats + ST_STEPS, cnt.steps);
+    atomicAdd(P.stats + ST_CONTRIB, cnt.contrib);
+}
+
+/* radiance-mode primaries (rt/rtrace.c:436-468, rt/rcontrib.c:343-353) */
+__global__ void k_primary(gb_run P)
+{
+    Counters cnt = {0, 0, 0};
+    for (long long s = blockIdx.x * (long long)blockDim.x + threadIdx.x; s < P.nsensors;
+         s += (long long)gridDim.x * blockDim.x) {
+        const double *sv = P.sensors + 6 * s;
+        Ray r;
+        r.org = f3((float)sv[0], (float)sv[1], (float)sv[2]);
+        r.dir = normalize3(f3((float)sv[3], (float)sv[4], (float)sv[5]));
+        r.coef = f3(1.f, 1.f, 1.f);
+        r.weight = 1.f;
+        r.lcoef = 1.f;
+        r.origin = -1;
+        r.rsrc = -1;
+        r.crtype = GB_PRIMARY;
+        r.rlvl = 0;
+        r.adepth = 0;
+        r.path = GB_ROOT_PATH(P.replica);
+        r.sensor = (uint32_t)s;
+        run_ray(P, r, cnt);
+    }
+    atomicAdd(P.stats + ST_RAYS, cnt.rays);
+    atomicAdd(P.stats + ST_STEPS, cnt.steps);
+    atomicAdd(P.stats + ST_CONTRIB, cnt.contrib);
+}
+
+__global__ void __launch_bounds__(256) k_gen(gb_run P)
+{
+    Counters cnt = {0, 0, 0};
+    unsigned long long n = *P.qin_count;
+    if (n > (unsigned long long)P.qcap)
+        n = P.qcap;
+    for (unsigned long long g = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; g < n;
+         g += (unsigned long long)gridDim.x * blockDim.x) {
+        Ray r = load_ray(P.qin + g);
+        run_ray(P, r, cnt);
+    }
+    atomicAdd(P.stats + ST_RAYS, cnt.rays);
+    atomicAdd(P.stats + ST_STEPS, cnt.steps);
+    atomicAdd(P.stats + ST_CONTRIB, cnt.contrib);
+}
+
+/* castonly rtrace (rt/rtrace.c:398-411 raycast): first intersection only */
+__global__ void k_cast(gb_run P, int *hit_obj, float *hit_t, float *hit_pn)
+{
+    for (long long s = blockIdx.x * (long long)blockDim.x + threadIdx.x; s < P.nsensors;
+         s += (long long)gridDim.x * blockDim.x) {
+        const double *sv = P.sensors + 6 * s;
+        float3 org = f3((float)sv[0], (float)sv[1], (float)sv[2]);
+        float3 dir = normalize3(f3((float)sv[3], (float)sv[4], (float)sv[5]));
+        Hit h;
+        uint32_t st = 0;
+        int obj = -1;
+        float t = D_FHUGE;
+        float3 n = f3(0.f, 0.f, 0.f);
+        if (local_hit(P.S, org, dir, -1, D_FTINY, D_FHUGE, h, &st)) {
+            obj = h.obj;
+            t = h.t;
+            n = h.n;
+        } else {
+            int sidx = source_hit(P.S, dir, -1, GB_PRIMARY);
+            if (sidx >= 0)
+                obj = P.S.src[sidx].so;
+        }
+        hit_obj[s] = obj;
+        if (hit_t)
+            hit_t[s] = t;
+        if (hit_pn) {
+            float3 p = org + dir * t;
+            float *o = hit_pn + 6 * s;
+            o[0] = p.x; o[1] = p.y; o[2] = p.z;
+            o[3] = n.x; o[4] = n.y; o[5] = n.z;
+        }
+    }
+}
+
+/* ------------------------------------------------------ host launchers */
+
+static int grid_for(long long n, int block, int sms)
+{
+    long long g = (n + block - 1) / block;
+    long long cap = (long long)sms * 8;
+    if (g > cap)
+        g = cap;
+    if (g < 1)
+        g = 1;
+    return (int)g;
+}
+
+int gb_launch_cast(const gb_run *P, int *hit_obj, float *hit_t, float *hit_pn, cudaStream_t st, int sms)
+{
+    k_cast<<<grid_for(P->nsensors, 128, sms), 128, 0, st>>>(*P, hit_obj, hit_t, hit_pn);
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+int gb_launch_root(const gb_run *P, cudaStream_t st, int sms)
+{
+    k_root<<<grid_for(P->nsensors, 128, sms), 128, 0, st>>>(*P);
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+int gb_launch_gen_root(const gb_run *P, cudaStream_t st, int sms)
+{
+    long long total = (long long)P->root_n * P->root_n * P->nsensors;
+    k_gen_root<<<grid_for(total, 256, sms), 256, 0, st>>>(*P);
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+int gb_launch_primary(const gb_run *P, cudaStream_t st, int sms)
+{
+    k_primary<<<grid_for(P->nsensors, 128, sms), 128, 0, st>>>(*P);
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+int gb_launch_gen(const gb_run *P, cudaStream_t st, int sms)
+{
+    k_gen<<<sms * 8, 256, 0, st>>>(*P);
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}

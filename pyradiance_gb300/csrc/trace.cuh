@@ -1,0 +1,513 @@
+/*
+ * trace.cuh -- device-side ray tracing core: octree traversal, primitive
+ * intersection with the reference's hit arbitration, source hits and the
+ * bin programs.  FP32 throughout; see trace.cu for the wavefront kernels.
+ */
+#ifndef GB_TRACE_CUH
+#define GB_TRACE_CUH
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include "devscene.h"
+#include "gbcommon.h"
+
+#define D_FTINY 1e-6f
+#define D_FHUGE 1e10f
+#define D_PI 3.14159265358979323846f
+#define GRID_BITS 24
+#define GRID_N (1 << GRID_BITS)
+#define MAX_CUBE_STEPS 65536
+
+struct Hit {
+    int   obj;      /* -1 none */
+    float t;
+    float rod;      /* -dot(dir, normal) */
+    float3 n;       /* unflipped surface normal */
+};
+
+__device__ __forceinline__ float3 f3(float x, float y, float z) { return make_float3(x, y, z); }
+__device__ __forceinline__ float3 operator+(float3 a, float3 b) { return f3(a.x + b.x, a.y + b.y, a.z + b.z); }
+__device__ __forceinline__ float3 operator-(float3 a, float3 b) { return f3(a.x - b.x, a.y - b.y, a.z - b.z); }
+__device__ __forceinline__ float3 operator*(float3 a, float s) { return f3(a.x * s, a.y * s, a.z * s); }
+__device__ __forceinline__ float3 operator*(float3 a, float3 b) { return f3(a.x * b.x, a.y * b.y, a.z * b.z); }
+__device__ __forceinline__ float3 operator-(float3 a) { return f3(-a.x, -a.y, -a.z); }
+__device__ __forceinline__ float dot3(float3 a, float3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ float3 cross3(float3 a, float3 b)
+{
+    return f3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+}
+__device__ __forceinline__ float comp(float3 v, int i) { return i == 0 ? v.x : (i == 1 ? v.y : v.z); }
+__device__ __forceinline__ float maxc(float3 v) { return fmaxf(v.x, fmaxf(v.y, v.z)); }
+__device__ __forceinline__ float3 normalize3(float3 v)
+{
+    float l = sqrtf(dot3(v, v));
+    return l > 0.f ? v * (1.f / l) : v;
+}
+
+/* ------------------------------------------------------------------------
+ * Hit arbitration: rt/raytrace.c:536-575 (rayreject).  Returns true when the
+ * candidate (obj, t, rod) is worse than the current best.
+ */
+__device__ __forceinline__ bool ray_reject(const gb_dscene &S, int obj, float t, float rod,
+                                           const Hit &best, float tmin)
+{
+    if ((t <= tmin) | (t > best.t + D_FTINY))
+        return true;
+    if (t < best.t - D_FTINY)
+        return false;
+    if (obj == best.obj)
+        return true;
+    if (best.obj < 0)
+        return false;
+    int fn = (S.obj[obj].x >> 8) & 0xff, fb = (S.obj[best.obj].x >> 8) & 0xff;
+    if (!(fn & DF_HASMAT)) {
+        if (fb & DF_HASMAT)
+            return true;
+    } else if (!(fb & DF_HASMAT)) {
+        return false;
+    } else if (fn & DF_TRANSP) {
+        if (!(fb & DF_TRANSP))
+            return true;
+    } else if (fb & DF_TRANSP) {
+        return false;
+    }
+    if (rod <= 0.f) {
+        if (best.rod > 0.f)
+            return true;
+    } else if (best.rod <= 0.f) {
+        return false;
+    }
+    return S.obj[best.obj].z >= S.obj[obj].z;   /* later modifier wins */
+}
+
+/* point in polygon on the dominant projection: common/face.c:121-161 */
+__device__ __forceinline__ bool in_face(const float2 *__restrict__ v, int nv, float x, float y)
+{
+    int ncross = 0;
+    float2 p0 = v[nv - 1];
+    for (int k = 0; k < nv; k++) {
+        float2 p1 = v[k];
+        if ((fabsf(p0.y - y) <= D_FTINY) & (fabsf(p1.y - y) <= D_FTINY) & ((p0.x > x) ^ (p1.x > x)))
+            return true;                                           /* edge case #1 */
+        if ((p0.y > y) ^ (p1.y > y)) {
+            int tst = (p0.x > x) + (p1.x > x);
+            if (tst == 2)
+                ncross++;
+            else if (tst) {
+                float prodA = (p0.y - y) * (p1.x - x);
+                float prodB = (p0.x - x) * (p1.y - y);
+                if (fabsf(prodA - prodB) <= D_FTINY)
+                    return true;                                   /* edge case #2 */
+                ncross += (p1.y > p0.y) ^ (prodA > prodB);
+            } else if ((fabsf(p0.x - x) <= D_FTINY) & (fabsf(p1.x - x) <= D_FTINY))
+                return true;                                       /* edge case #3 */
+        }
+        p0 = p1;
+    }
+    return ncross & 1;
+}
+
+/* rt/o_face.c:15-62 */
+__device__ __forceinline__ void hit_face(const gb_dscene &S, int obj, int4 od, float3 org, float3 dir,
+                                         Hit &best, float tmin)
+{
+    float4 pl = S.geo[obj];
+    float3 n = f3(pl.x, pl.y, pl.z);
+    float rdot = -dot3(dir, n);
+    if ((rdot <= D_FTINY) & (rdot >= -D_FTINY))
+        return;
+    float t = (dot3(org, n) - pl.w) / rdot;
+    if (ray_reject(S, obj, t, rdot, best, tmin))
+        return;
+    float3 p = org + dir * t;
+    int ax = ((od.x >> 8) >> DF_AXSHIFT) & 3;
+    int xi = ax + 1 >= 3 ? ax - 2 : ax + 1;
+    int yi = xi + 1 >= 3 ? xi - 2 : xi + 1;
+    if (!in_face(S.fvert + od.w, (od.x >> 16) & 0xffff, comp(p, xi), comp(p, yi)))
+        return;
+    best.obj = obj;
+    best.t = t;
+    best.rod = rdot;
+    best.n = n;
+}
+
+/* common/zeroes.c:19-53 */
+__device__ __forceinline__ int quadratic(float r[2], float a, float b, float c)
+{
+    int first;
+    if (a < -D_FTINY)
+        first = 1;
+    else if (a > D_FTINY)
+        first = 0;
+    else if (fabsf(b) > D_FTINY) {
+        r[0] = -c / b;
+        return 1;
+    } else
+        return 0;
+    b *= 0.5f;
+    float disc = b * b - a * c;
+    if (disc < -D_FTINY * D_FTINY)
+        return 0;
+    if (disc <= D_FTINY * D_FTINY) {
+        r[0] = -b / a;
+        return 1;
+    }
+    disc = sqrtf(disc);
+    r[first] = (-b - disc) / a;
+    r[1 - first] = (-b + disc) / a;
+    return 2;
+}
+
+/* rt/sphere.c:15-83 */
+__device__ __forceinline__ void hit_sphere(const gb_dscene &S, int obj, bool bubble, float3 org,
+                                           float3 dir, Hit &best, float tmin)
+{
+    float4 sp = S.geo[obj];
+    float3 d = org - f3(sp.x, sp.y, sp.z);
+    float a = dot3(dir, dir), b = 2.f * dot3(dir, d), c = dot3(d, d) - sp.w * sp.w;
+    float root[2];
+    int nr = quadratic(root, a, b, c), i;
+    float t = 0.f;
+    for (i = 0; i < nr; i++)
+        if ((t = root[i]) > D_FTINY)
+            break;
+    if (i >= nr)
+        return;
+    if (ray_reject(S, obj, t, (float)(1 - 2 * ((i > 0) ^ bubble)), best, tmin))
+        return;
+    float rad = bubble ? -sp.w : sp.w;
+    float3 p = org + dir * t;
+    float3 n = (p - f3(sp.x, sp.y, sp.z)) * (1.f / rad);
+    best.obj = obj;
+    best.t = t;
+    best.n = n;
+    best.rod = -dot3(dir, n);
+}
+
+/* rt/o_cone.c:16-146; cone record: tm (12: 3x3 rows then translation),
+ * ad (3), p0 (3), al, sl, r0, r1 */
+__device__ __forceinline__ void hit_cone(const gb_dscene &S, int obj, int kind, int ci, float3 org,
+                                         float3 dir, Hit &best, float tmin)
+{
+    const float *c = S.cone + 24 * ci;
+    float3 rox = f3(org.x * c[0] + org.y * c[3] + org.z * c[6] + c[9],
+                    org.x * c[1] + org.y * c[4] + org.z * c[7] + c[10],
+                    org.x * c[2] + org.y * c[5] + org.z * c[8] + c[11]);
+    float3 rdx = f3(dir.x * c[0] + dir.y * c[3] + dir.z * c[6],
+                    dir.x * c[1] + dir.y * c[4] + dir.z * c[7],
+                    dir.x * c[2] + dir.y * c[5] + dir.z * c[8]);
+    float3 ad = f3(c[12], c[13], c[14]);
+    float3 p0 = f3(c[15], c[16], c[17]);
+    float al = c[18], sl = c[19], r0 = c[20], r1 = c[21];
+    float a, b, cc, root[2];
+    if (kind == DK_RING) {
+        if ((rdx.z <= D_FTINY) & (rdx.z >= -D_FTINY))
+            return;
+        root[0] = -rox.z / rdx.z;
+        if (ray_reject(S, obj, root[0], -rdx.z, best, tmin))
+            return;
+        b = root[0] * rdx.x + rox.x;
+        cc = root[0] * rdx.y + rox.y;
+        a = b * b + cc * cc;
+        if (a > r1 * r1 || a < r0 * r0)
+            return;
+        best.obj = obj;
+        best.t = root[0];
+        best.n = ad;
+        best.rod = -rdx.z;
+        return;
+    }
+    if ((kind == DK_CONE) | (kind == DK_CUP)) {
+        a = rdx.x * rdx.x + rdx.y * rdx.y - rdx.z * rdx.z;
+        b = 2.f * (rdx.x * rox.x + rdx.y * rox.y - rdx.z * rox.z);
+        cc = rox.x * rox.x + rox.y * rox.y - rox.z * rox.z;
+    } else {
+        a = rdx.x * rdx.x + rdx.y * rdx.y;
+        b = 2.f * (rdx.x * rox.x + rdx.y * rox.y);
+        cc = rox.x * rox.x + rox.y * rox.y - r0 * r0;
+    }
+    int nr = quadratic(root, a, b, cc);
+    for (int rn = 0; rn < nr; rn++) {
+        if (root[rn] <= D_FTINY)
+            continue;
+        if (root[rn] > best.t + D_FTINY)
+            break;
+        float3 p = org + dir * root[rn];
+        float3 v = p - p0;
+        float bb = dot3(v, ad);
+        if (bb < 0.f || bb > al)
+            continue;
+        bool inv = (kind == DK_CUP) | (kind == DK_TUBE);
+        if (ray_reject(S, obj, root[rn], (float)(1 - 2 * ((rn > 0) ^ inv)), best, tmin))
+            break;
+        float aa, c2 = 0.f;
+        if (kind == DK_CYL)
+            aa = r0;
+        else if (kind == DK_TUBE)
+            aa = -r0;
+        else {
+            c2 = r1 - r0;
+            aa = r0 + bb * c2 / al;
+            if (kind == DK_CUP) {
+                c2 = -c2;
+                aa = -aa;
+            }
+        }
+        float3 n = (v - ad * bb) * (1.f / aa);
+        if ((kind == DK_CONE) | (kind == DK_CUP))
+            n = (n * al - ad * c2) * (1.f / sl);
+        float nn = dot3(n, n);
+        if ((nn > 1.f + D_FTINY) | (nn < 1.f - D_FTINY))
+            n = n * (1.f / (.5f + .5f * nn));
+        best.obj = obj;
+        best.t = root[rn];
+        best.n = n;
+        best.rod = -dot3(dir, n);
+        return;
+    }
+}
+
+__device__ __forceinline__ void hit_object(const gb_dscene &S, int obj, float3 org, float3 dir, Hit &best,
+                                           float tmin)
+{
+    int4 od = S.obj[obj];
+    int kind = od.x & 0xff;
+    switch (kind) {
+    case DK_FACE:
+        hit_face(S, obj, od, org, dir, best, tmin);
+        break;
+    case DK_SPHERE:
+    case DK_BUBBLE:
+        hit_sphere(S, obj, kind == DK_BUBBLE, org, dir, best, tmin);
+        break;
+    case DK_CONE:
+    case DK_CUP:
+    case DK_CYL:
+    case DK_TUBE:
+    case DK_RING:
+        hit_cone(S, obj, kind, od.w, org, dir, best, tmin);
+        break;
+    default:
+        break;
+    }
+}
+
+/* ------------------------------------------------------------------------
+ * Octree traversal (rt/raytrace.c:595-793 localhit/raymove/checkhit).
+ *
+ * Cube positions are kept as integer coordinates on a 2^24 grid over the
+ * scene cube, so descending from the root is bit selection and stepping to
+ * the neighbour cube is an exact integer increment; only the ray parameter
+ * at each cube exit is floating point.  Leaf sets are tested in the
+ * reference's order, a hit inside the current cube ends the walk (checkhit),
+ * and a hit recorded earlier but never confirmed is still returned when the
+ * ray leaves the scene, as localhit does.
+ */
+__device__ __forceinline__ bool local_hit(const gb_dscene &S, float3 org, float3 dir, int skip,
+                                          float tmin, float tmax, Hit &best, uint32_t *steps_out)
+{
+    best.obj = -1;
+    best.t = D_FHUGE;
+    best.rod = 1.f;
+    best.n = f3(0.f, 0.f, 0.f);
+    const float cs = S.cusize;
+    float3 rel = org - f3(S.cuorg[0], S.cuorg[1], S.cuorg[2]);
+    int sg[3];
+    float dd[3] = {dir.x, dir.y, dir.z}, rr[3] = {rel.x, rel.y, rel.z}, inv[3];
+    int anyd = 0;
+    for (int i = 0; i < 3; i++) {
+        sg[i] = dd[i] > 1e-7f ? 1 : (dd[i] < -1e-7f ? -1 : 0);
+        inv[i] = sg[i] ? 1.f / dd[i] : 0.f;
+        anyd |= sg[i];
+    }
+    if (!anyd)
+        return false;
+    float t = 0.f;
+    bool inside = (rr[0] >= 0.f) & (rr[0] < cs) & (rr[1] >= 0.f) & (rr[1] < cs) & (rr[2] >= 0.f) & (rr[2] < cs);
+    if (!inside) {
+        for (int i = 0; i < 3; i++) {
+            if (!sg[i])
+                continue;
+            float pl = sg[i] > 0 ? 0.f : cs;
+            float dt = (pl - rr[i]) * inv[i];
+            if (dt > t)
+                t = dt;
+        }
+        t += D_FTINY;
+        if (t >= tmax)
+            return false;
+        for (int i = 0; i < 3; i++) {
+            float p = rr[i] + dd[i] * t;
+            if (!(p >= 0.f && p < cs))
+                return false;
+        }
+    }
+    const float gs = S.grid_scale, cell = S.cell;
+    int q[3];
+    for (int i = 0; i < 3; i++) {
+        int v = __float2int_rd((rr[i] + dd[i] * t) * gs);
+        q[i] = min(max(v, 0), GRID_N - 1);
+    }
+    uint32_t steps = 0;
+    for (;;) {
+        /* descend to the leaf containing q */
+        int node = S.root, level = 0;
+        while (node >= 0) {
+            int sh = GRID_BITS - 1 - level;
+            int br = ((q[0] >> sh) & 1) | (((q[1] >> sh) & 1) << 1) | (((q[2] >> sh) & 1) << 2);
+            node = __ldg(S.kids + 8 * node + br);
+            level++;
+        }
+        int span = 1 << (GRID_BITS - level);
+        int lo[3] = {q[0] & ~(span - 1), q[1] & ~(span - 1), q[2] & ~(span - 1)};
+        /* exit distance of this cube */
+        float texit = D_FHUGE;
+        int ax = 0;
+        for (int i = 0; i < 3; i++) {
+            if (!sg[i])
+                continue;
+            float pl = (float)(sg[i] > 0 ? lo[i] + span : lo[i]) * cell;
+            float dt = (pl - rr[i]) * inv[i];
+            if (dt < texit) {
+                texit = dt;
+                ax = i;
+            }
+        }
+        if (node <= -2) {                       /* full leaf: test its set */
+            const int *set = S.set_data + __ldg(S.set_off + (-node - 2));
+            int cnt = __ldg(set);
+            for (int k = 1; k <= cnt; k++) {
+                int o = __ldg(set + k);
+                if (o != skip)
+                    hit_object(S, o, org, dir, best, tmin);
+            }
+            if (best.obj >= 0 && best.t <= texit)
+                break;                          /* hit inside this cube */
+        }
+        steps++;
+        if (texit >= tmax || steps >= MAX_CUBE_STEPS)
+            break;
+        /* step to the face neighbour along the exit axis; the exit point lies
+         * on that face, so the other coordinates stay inside this cube's
+         * slab (an edge or corner exit takes a second, zero-length step) */
+        for (int i = 0; i < 3; i++) {
+            if (i == ax)
+                continue;
+            int v = __float2int_rd((rr[i] + dd[i] * texit) * gs);
+            q[i] = min(max(v, lo[i]), lo[i] + span - 1);
+        }
+        q[ax] = sg[ax] > 0 ? lo[ax] + span : lo[ax] - 1;
+        if (q[ax] < 0 || q[ax] >= GRID_N)
+            break;                              /* left the scene */
+    }
+    if (steps_out)
+        *steps_out += steps + 1;
+    return best.obj >= 0;
+}
+
+/* ------------------------------------------------------------------------
+ * Distant source test for rays that leave the scene: rt/source.c:317-377.
+ * Returns the source index or -1.
+ */
+__device__ __forceinline__ int source_hit(const gb_dscene &S, float3 dir, int rsrc, uint32_t crtype)
+{
+    int glowsrc = -1;
+    int first = 0, last = S.nsrc - 1;
+    if (rsrc >= 0)
+        first = last = rsrc;
+    for (int i = first; i <= last; i++) {
+        const gb_dsrc &s = S.src[i];
+        if (!(s.flags & DS_DISTANT))
+            continue;
+        float dt = s.sloc[0] * dir.x + s.sloc[1] * dir.y + s.sloc[2] * dir.z;
+        if (2.f * D_PI * (1.f - dt) > s.ss2)
+            continue;
+        if (i == rsrc)
+            return i;
+        if (s.flags & DS_SKIP) {
+            if (glowsrc < 0)
+                glowsrc = i;
+            continue;
+        }
+        return i;
+    }
+    return glowsrc;
+}
+
+/* ------------------------------------------------------------------------
+ * Bin programs (rcontrib -b expressions; Reinhart bins as in
+ * src/radiance/util/reinhartb.cal:17-47).
+ */
+__device__ __forceinline__ float reinhart_bin(float Dx, float Dy, float Dz, const gb_binins *p)
+{
+    float MF = p[0].op, RHS = p[0].a, rNx = p[0].b, rNy = p[0].c;
+    float rNz = p[1].op, Ux = p[1].a, Uy = p[1].b, Uz = p[1].c;
+    const float DEG = D_PI / 180.f;
+    float inc_dz = -Dx * rNx - Dy * rNy - Dz * rNz;
+    float inc_rx = -RHS * (Dx * (Uy * rNz - Uz * rNy) + Dy * (Uz * rNx - Ux * rNz) + Dz * (Ux * rNy - Uy * rNx));
+    float inc_ry = Dx * Ux + Dy * Uy + Dz * Uz + inc_dz * (rNx * Ux + rNy * Uy + rNz * Uz);
+    float r_alt = (inc_dz - 1.f > 0.f ? D_PI / 2 : (-1.f - inc_dz > 0.f ? -D_PI / 2 : asinf(inc_dz))) / DEG;
+    if (!(r_alt > 0.f))
+        return -1.f;
+    float a = atan2f(inc_rx, inc_ry);
+    float r_azi = (-a > 0.f ? a + 2.f * D_PI : a) / DEG;
+    float alpha = 90.f / (MF * 7.f + .5f);
+    int row = (int)floorf(r_alt / alpha);
+    const float tnaz[7] = {30.f, 30.f, 24.f, 24.f, 18.f, 12.f, 6.f};
+    /* raccum(row) and rnaz(row) */
+    float acc = 0.f;
+    float lim = 7.f * MF - .5f;
+    float rn = 1.f;
+    for (int r = 0; r <= row; r++) {
+        float nz;
+        if ((float)r - lim > 0.f)
+            nz = 1.f;
+        else {
+            int k = (int)floorf(((float)r + .5f) / MF);
+            nz = MF * tnaz[min(max(k, 0), 6)];
+        }
+        if (r < row)
+            acc += nz;
+        else
+            rn = nz;
+    }
+    float r_inc = 360.f / rn;
+    float azn = (359.9999f - .5f * r_inc - r_azi > 0.f) ? floorf((r_azi + .5f * r_inc) / r_inc) : 0.f;
+    return acc + azn;
+}
+
+__device__ __forceinline__ float eval_bin(const gb_binins *prog, float3 d)
+{
+    float st[16];
+    int sp = 0;
+    for (int pc = 0; pc < GB_BINPROG_MAX; pc++) {
+        gb_binins in = prog[pc];
+        int op = (int)in.op;
+        switch (op) {
+        case GB_OP_END:
+            return sp > 0 ? st[sp - 1] : -1.f;
+        case GB_OP_CONST: st[sp++] = in.a; break;
+        case GB_OP_DX: st[sp++] = d.x; break;
+        case GB_OP_DY: st[sp++] = d.y; break;
+        case GB_OP_DZ: st[sp++] = d.z; break;
+        case GB_OP_ADD: sp--; st[sp - 1] += st[sp]; break;
+        case GB_OP_SUB: sp--; st[sp - 1] -= st[sp]; break;
+        case GB_OP_MUL: sp--; st[sp - 1] *= st[sp]; break;
+        case GB_OP_DIV: sp--; st[sp - 1] /= st[sp]; break;
+        case GB_OP_NEG: st[sp - 1] = -st[sp - 1]; break;
+        case GB_OP_IF: sp -= 2; st[sp - 1] = st[sp - 1] > 0.f ? st[sp] : st[sp + 1]; break;
+        case GB_OP_FLOOR: st[sp - 1] = floorf(st[sp - 1]); break;
+        case GB_OP_RBIN:
+            st[sp++] = reinhart_bin(d.x, d.y, d.z, prog + pc + 1);
+            pc += 2;
+            break;
+        default:
+            return -1.f;
+        }
+        if (sp >= 15)
+            return -1.f;
+    }
+    return -1.f;
+}
+
+#endif

@@ -1,0 +1,74 @@
+/*
+ * tracehost.h -- the launch record shared by trace.cu (device) and host.cu.
+ */
+#ifndef GB_TRACEHOST_H
+#define GB_TRACEHOST_H
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include "devscene.h"
+#include "gbcommon.h"
+
+/* stats slots */
+#define GB_ST_RAYS     0   /* rays traced (octree walks) */
+#define GB_ST_STEPS    1   /* cube visits */
+#define GB_ST_CONTRIB  2   /* contributions binned */
+#define GB_ST_OVERFLOW 3   /* queue records dropped */
+#define GB_ST_BADBIN   4   /* bin numbers beyond nbins */
+#define GB_ST_N        8
+
+#define GRID_BITS_HOST 24      /* must equal GRID_BITS of trace.cuh */
+
+/* one queued ray: 64 bytes, four float4 lanes */
+typedef struct __align__(16) {
+    float v[16];
+} gb_qray;
+
+/* first hemisphere of a -I sensor */
+typedef struct {
+    float hp[3], nrm[3], ux[3];
+    int n;
+} gb_rootrec;
+
+typedef struct {
+    gb_dscene S;
+    /* options */
+    int   ab, ad;
+    float minweight;
+    int   maxdepth;
+    float av[3];
+    float dstrsrc;
+    float specthresh;
+    int   follow;              /* rcontrib: every source is followed (SFOLLOW) */
+    int   contrib_mode;        /* rcontrib -V */
+    uint32_t k0, k1;           /* random stream key */
+    uint32_t replica;
+    /* sensors */
+    long long nsensors;
+    const double *sensors;     /* n x 6 */
+    /* outputs */
+    double *value;             /* n x 3 or NULL */
+    double *bins;              /* records x nbins_total x 3 or NULL */
+    int   accum;
+    int   nbins_total;
+    const gb_binins *binprog;
+    const int4 *modinfo;       /* per tracked slot: program offset, nbins, bin0 */
+    unsigned long long *stats;
+    /* work */
+    gb_rootrec *roots;
+    float2 *root_spt;          /* n x root_n^2 placed disk positions (root_n >= 4) */
+    int   root_n;
+    const gb_qray *qin;
+    const unsigned long long *qin_count;
+    gb_qray *qout;
+    unsigned long long *qout_count;
+    long long qcap;
+} gb_run;
+
+int gb_launch_cast(const gb_run *P, int *hit_obj, float *hit_t, float *hit_pn, cudaStream_t st, int sms);
+int gb_launch_root(const gb_run *P, cudaStream_t st, int sms);
+int gb_launch_gen_root(const gb_run *P, cudaStream_t st, int sms);
+int gb_launch_primary(const gb_run *P, cudaStream_t st, int sms);
+int gb_launch_gen(const gb_run *P, cudaStream_t st, int sms);
+
+#endif

@@ -157,6 +157,58 @@ def window_room(seed: int = 0, ntri: int = 20000, nmat: int | None = None) -> st
     return "".join(out)
 
 
+def shape_zoo(seed: int = 0, n: int = 40) -> str:
+    """Room with every primitive type the intersectors handle: spheres,
+    bubbles, cones, cups, cylinders, tubes, rings and polygons, gray plastic
+    and metal, and the ceiling light of ``daylight_room``."""
+    rng = np.random.default_rng(seed)
+    X, Y, Z = ROOM
+    out = [_mat_plastic("room_mat", (0.5, 0.5, 0.5)), _room_shell("room_mat")]
+    out.append("void metal shiny\n0\n0\n5 .6 .6 .6 .8 0\n\n")
+    for i in range(n):
+        rho = rng.uniform(0.2, 0.7)
+        out.append(_mat_plastic(f"zoo_mat{i}", (rho, rho * 0.9, rho * 0.8)))
+        mod = "shiny" if i % 7 == 3 else f"zoo_mat{i}"
+        c = rng.uniform((1, 1, 0.3), (X - 1, Y - 1, Z - 0.6))
+        r = rng.uniform(0.1, 0.4)
+        kind = i % 7
+        if kind == 0:
+            out.append(f"{mod} sphere sph{i}\n0\n0\n4 {c[0]:.9g} {c[1]:.9g} {c[2]:.9g} {r:.9g}\n\n")
+        elif kind == 1:
+            out.append(f"{mod} bubble bub{i}\n0\n0\n4 {c[0]:.9g} {c[1]:.9g} {c[2]:.9g} {r:.9g}\n\n")
+        elif kind in (2, 3, 4, 5):
+            d = rng.normal(size=3)
+            d /= np.linalg.norm(d)
+            p1 = c + d * rng.uniform(0.2, 0.6)
+            name = {2: "cone", 3: "cup", 4: "cylinder", 5: "tube"}[kind]
+            if kind in (2, 3):
+                r2 = rng.uniform(0.0, 0.3)
+                args = f"8 {c[0]:.9g} {c[1]:.9g} {c[2]:.9g} {p1[0]:.9g} {p1[1]:.9g} {p1[2]:.9g} {r:.9g} {r2:.9g}"
+            else:
+                args = f"7 {c[0]:.9g} {c[1]:.9g} {c[2]:.9g} {p1[0]:.9g} {p1[1]:.9g} {p1[2]:.9g} {r:.9g}"
+            out.append(f"{mod} {name} {name}{i}\n0\n0\n{args}\n\n")
+        else:
+            d = rng.normal(size=3)
+            d /= np.linalg.norm(d)
+            out.append(f"{mod} ring ring{i}\n0\n0\n8 {c[0]:.9g} {c[1]:.9g} {c[2]:.9g} {d[0]:.9g} {d[1]:.9g} "
+                       f"{d[2]:.9g} {r * 0.3:.9g} {r:.9g}\n\n")
+    out.append("void light light_mat\n0\n0\n3 100 100 100\n\n")
+    cx, cy = X / 2, Y / 2
+    out.append(_poly("light_mat", "light", [(cx - .5, cy - .5, Z - 0.01), (cx - .5, cy + .5, Z - 0.01),
+                                            (cx + .5, cy + .5, Z - 0.01), (cx + .5, cy - .5, Z - 0.01)]))
+    return "".join(out)
+
+
+def random_rays(n: int, seed: int = 1) -> np.ndarray:
+    """(n, 6) rays from random interior points in uniformly random directions."""
+    rng = np.random.default_rng(seed)
+    X, Y, Z = ROOM
+    o = rng.uniform((0.2, 0.2, 0.2), (X - 0.2, Y - 0.2, Z - 0.2), size=(n, 3))
+    d = rng.normal(size=(n, 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    return np.hstack([o, d])
+
+
 def sensor_grid(nx: int, ny: int, z: float = 0.8) -> np.ndarray:
     """(nx*ny, 6) float64 array of ``ox oy oz dx dy dz``, cell-centred over
     the room floor plan, facing +z, row-major in y then x."""

@@ -1,0 +1,181 @@
+"""Generates the golden vectors in tests/golden from the reference programs.
+
+Runs the reference rtrace, rcontrib, oconv and dctimestep compiled from the
+reference sources by oracle/build_ref.mk (into oracle/_ref/) on the seeded
+scenes of pyradiance_gb300.workloads, and stores their outputs as small .npz
+fixtures.  Only this script runs the reference; the tests read the fixtures.
+
+    make -f oracle/build_ref.mk REF=/root/reference -j8
+    python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import os
+import subprocess
+import sys
+import tempfile
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parents[2]
+sys.path.insert(0, str(ROOT))
+from pyradiance_gb300 import workloads as w  # noqa: E402
+
+REF = ROOT / "oracle" / "_ref"
+BIN = REF / "bin"
+OUT = Path(__file__).resolve().parent
+REFERENCE_TREE = Path(os.environ.get("GB_REFERENCE", "/root/reference"))
+
+
+def run(args, inp: bytes | None = None, cwd=None) -> bytes:
+    env = dict(os.environ, RAYPATH=f".:{REF / 'lib'}")
+    p = subprocess.run([str(BIN / args[0]), *map(str, args[1:])], input=inp, capture_output=True, env=env,
+                       cwd=cwd)
+    if p.returncode != 0:
+        raise RuntimeError(f"{args[0]} failed: {p.stderr.decode()}")
+    return p.stdout
+
+
+def oconv(rad_text: str, tmp: Path, name: str) -> Path:
+    rad = tmp / f"{name}.rad"
+    rad.write_text(rad_text)
+    oct_path = tmp / f"{name}.oct"
+    oct_path.write_bytes(run(["oconv", "-f", rad]))
+    return oct_path
+
+
+def names(out: bytes) -> np.ndarray:
+    return np.array([ln.split("\t")[0] for ln in out.decode().splitlines()])
+
+
+def c1_direct(tmp: Path) -> None:
+    """Deterministic direct irradiance (rtrace -I -ab 0 -dj 0 -ds 0 -dr 0)
+    and first-hit surfaces on the 100 x 100 sensor grid."""
+    octp = oconv(w.daylight_room(), tmp, "c1")
+    rays = w.sensor_grid(100, 100)
+    inp = rays.astype("<f8").tobytes()
+    irr = np.frombuffer(run(["rtrace", "-h", "-u-", "-I", "-ab", "0", "-dj", "0", "-ds", "0", "-dr", "0",
+                             "-fdd", "-ov", octp], inp), dtype="<f8").reshape(-1, 3)
+    hit = names(run(["rtrace", "-h", "-u-", "-ab", "0", "-fda", "-os", octp], inp))
+    dist = np.frombuffer(run(["rtrace", "-h", "-u-", "-ab", "0", "-fdd", "-oL", octp], inp), dtype="<f8")
+    np.savez_compressed(OUT / "c1_direct.npz", rays=rays, irradiance=irr, hit_name=hit, hit_dist=dist,
+                        cmd="rtrace -h -u- -I -ab 0 -dj 0 -ds 0 -dr 0 -fdd -ov | -ab 0 -os | -ab 0 -oL")
+    print("c1_direct: lit fraction %.4f" % (irr[:, 0] > 0).mean())
+
+
+def zoo(tmp: Path) -> None:
+    """Every primitive type: first-hit surface and distance of random rays,
+    and deterministic -ab 0 radiance (direct + mirror reflections)."""
+    octp = oconv(w.shape_zoo(), tmp, "zoo")
+    rays = w.random_rays(4000, seed=3)
+    inp = rays.astype("<f8").tobytes()
+    hit = names(run(["rtrace", "-h", "-u-", "-ab", "0", "-fda", "-os", octp], inp))
+    dist = np.frombuffer(run(["rtrace", "-h", "-u-", "-ab", "0", "-fdd", "-oL", octp], inp), dtype="<f8")
+    val = np.frombuffer(run(["rtrace", "-h", "-u-", "-ab", "0", "-dj", "0", "-ds", "0", "-dr", "0", "-dt", "0",
+                             "-fdd", "-ov", octp], inp), dtype="<f8").reshape(-1, 3)
+    irr = np.frombuffer(run(["rtrace", "-h", "-u-", "-I", "-ab", "0", "-dj", "0", "-ds", "0", "-dr", "0",
+                             "-dt", "0", "-fdd", "-ov", octp], inp), dtype="<f8").reshape(-1, 3)
+    np.savez_compressed(OUT / "zoo.npz", rays=rays, hit_name=hit, hit_dist=dist, radiance=val, irradiance=irr,
+                        cmd="rtrace -h -u- -ab 0 [-I] -dj 0 -ds 0 -dr 0 -dt 0")
+    print("zoo: %d hits on curved surfaces" % sum(not n.startswith(("floor", "ceiling", "north", "south", "east",
+                                                                   "west", "light")) for n in hit))
+
+
+# bin groups of the 146 columns: ground, then the 8 Reinhart MF:1 altitude rows
+ROW_EDGES = [0, 1, 31, 61, 85, 109, 127, 139, 145, 146]
+
+MODS = ["-m", "groundglow", "-f", "reinhartb.cal", "-p", "MF=1", "-b", "rbin", "-bn", "Nrbins", "-m", "skyglow"]
+
+
+def c2_stats(tmp: Path, nsens: int = 32, K: int = 256, ab: int = 3) -> None:
+    """rcontrib daylight coefficients on a subset of the 64 x 64 grid, each
+    sensor replicated K times with uncorrelated sampling (-u+, the
+    reference's default): per-sensor, per-bin sample mean and standard
+    error of channel 0 (the scene is gray)."""
+    octp = oconv(w.window_room(), tmp, "c2")
+    grid = w.sensor_grid(64, 64)
+    idx = np.linspace(0, len(grid) - 1, nsens).astype(int)
+    rays = grid[idx]
+    rep = np.repeat(rays, K, axis=0)
+    out = run(["rcontrib", "-h", "-u+", "-n", str(os.cpu_count() or 1), "-I+", "-ab", str(ab), "-ad", "1024",
+               "-lw", "1e-4", "-c", "1", "-fdd", *MODS, octp], rep.astype("<f8").tobytes())
+    a = np.frombuffer(out, dtype="<f8").reshape(nsens, K, 146, 3)[..., 0]
+    grp = np.stack([a[:, :, e0:e1].sum(2) for e0, e1 in zip(ROW_EDGES[:-1], ROW_EDGES[1:])], 2)
+    np.savez_compressed(OUT / f"c2_stats_ab{ab}.npz", sensor_index=idx, rays=rays, K=K,
+                        mean=a.mean(1), se=a.std(1, ddof=1) / np.sqrt(K), nnz=(a > 0).sum(1),
+                        group_mean=grp.mean(1), group_se=grp.std(1, ddof=1) / np.sqrt(K),
+                        total_mean=a.sum(2).mean(1), total_se=a.sum(2).std(1, ddof=1) / np.sqrt(K),
+                        cmd="rcontrib -h -u+ -I+ -ab %d -ad 1024 -lw 1e-4 -c 1 " % ab + " ".join(MODS))
+    print("c2_stats ab%d: mean total %.4g" % (ab, a.sum(2).mean()))
+
+
+def dct_small() -> None:
+    """dctimestep on small matrices with the annual workload's value
+    distributions (DC lognormal with zeros, sky spikes and night columns)."""
+    dc, sky = w.dc_sky(48, 145, 40, seed=5)
+    with tempfile.TemporaryDirectory() as td:
+        td = Path(td)
+        for name, m in (("dc", dc), ("sky", sky)):
+            hdr = (f"#?RADIANCE\nNROWS={m.shape[0]}\nNCOLS={m.shape[1]}\nNCOMP=3\nBigEndian=0\n"
+                   "FORMAT=float\n\n").encode()
+            (td / f"{name}.mtx").write_bytes(hdr + m.astype("<f4").tobytes())
+        out = run(["dctimestep", "-h", "-of", td / "dc.mtx", td / "sky.mtx"])
+    res = np.frombuffer(out, dtype="<f4").reshape(48, 40, 3)
+    np.savez_compressed(OUT / "dct_small.npz", dc=dc, sky=sky, out=res, cmd="dctimestep -h -of dc.mtx sky.mtx")
+    print("dct_small: max %.4g" % res.max())
+
+
+def octree_digests(tmp: Path) -> None:
+    """Digest (node count, set count, pre-order hash of the tree and its
+    leaf sets) of the reference oconv octree of each workload, read with the
+    oracle's loader; the octree builder test rebuilds them from scene text."""
+    sys.path.insert(0, str(ROOT))
+    from oracle import pyoracle as po
+    rows = {}
+    for name, text in (("c1", w.daylight_room()), ("c2", w.window_room()), ("zoo", w.shape_zoo())):
+        octp = oconv(text, tmp, name + "_d")
+        rows[name] = np.array(po.octree_digest(octp), dtype=np.uint64)
+    np.savez_compressed(OUT / "octree_ref.npz", **rows)
+    print("octree digests:", {k: v.tolist() for k, v in rows.items()})
+
+
+def ref_fixture_trace() -> None:
+    """The reference's own test scene (tests/Resources/trace.oct, polygons,
+    a cone and a sphere): first hits and distances of the two rays of its
+    rtrace test (tests/test_rtrace.py:52-59) and of a fan of rays."""
+    octp = REFERENCE_TREE / "tests" / "Resources" / "trace.oct"
+    if not octp.exists():
+        print("reference tree not found; skipping trace.oct vectors")
+        return
+    base = np.array([[1.0, 2.0, 3.0, 0.0, 0.0, 1.0], [4.0, 5.0, 6.0, 0.0, 1.0, 0.0]])
+    rng = np.random.default_rng(11)
+    o = rng.uniform((-2, 1, -15), (40, 4, 3), size=(2000, 3))
+    d = rng.normal(size=(2000, 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    rays = np.vstack([base, np.hstack([o, d])])
+    inp = rays.astype("<f8").tobytes()
+    hit = names(run(["rtrace", "-h", "-u-", "-ab", "0", "-fda", "-os", octp], inp, cwd=octp.parent))
+    dist = np.frombuffer(run(["rtrace", "-h", "-u-", "-ab", "0", "-fdd", "-oL", octp], inp, cwd=octp.parent),
+                         dtype="<f8")
+    np.savez_compressed(OUT / "ref_trace_oct.npz", rays=rays, hit_name=hit, hit_dist=dist,
+                        cmd="rtrace -h -u- -ab 0 -os | -oL  tests/Resources/trace.oct")
+    print("ref_trace_oct: %d of %d rays hit" % ((hit != "*").sum(), len(hit)))
+
+
+def main() -> None:
+    if not (BIN / "rtrace").exists():
+        sys.exit("reference programs missing: make -f oracle/build_ref.mk REF=/root/reference -j8")
+    with tempfile.TemporaryDirectory() as td:
+        tmp = Path(td)
+        octree_digests(tmp)
+        c1_direct(tmp)
+        zoo(tmp)
+        dct_small()
+        ref_fixture_trace()
+        c2_stats(tmp, ab=1, K=256)
+        c2_stats(tmp, ab=3, K=256)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,110 @@
+"""The CPU oracle against the golden vectors of the reference programs.
+
+These pin the oracle (and the host scene loader and octree builder it
+shares with the library) before it is used to check the GPU.  CPU only.
+"""
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from conftest import MODS_C2, golden, zscores
+from oracle import pyoracle as po
+
+REF_TRACE = Path("/root/reference/tests/Resources/trace.oct")
+
+
+@pytest.fixture(scope="module")
+def oscenes(scene_dir):
+    return {k: po.Scene(scene_dir / f"{k}.rad") for k in ("c1", "c2", "zoo")}
+
+
+def test_octree_builder_matches_reference(scene_dir):
+    g = golden("octree_ref.npz")
+    for name in ("c1", "c2", "zoo"):
+        assert po.octree_digest(scene_dir / f"{name}.rad") == [int(x) for x in g[name]], name
+
+
+def test_c1_direct_irradiance_and_hits(oscenes):
+    g = golden("c1_direct.npz")
+    sc = oscenes["c1"]
+    o = po.default_opts("rtrace", I=1, ab=0, dj=0, ds=0, dr=0, u=0)
+    rgb, hid, ht, _ = po.rtrace(sc, o, g["rays"])
+    ref = g["irradiance"]
+    lit = ref[:, 0] > 0
+    assert lit.mean() > 0.05
+    np.testing.assert_array_equal(rgb[~lit], 0.0)
+    rel = np.abs(rgb[lit] - ref[lit]) / ref[lit]
+    assert rel.max() < 1e-6, rel.max()
+    names = np.array([sc.object_name(i) if i >= 0 else "*" for i in hid])
+    assert (names == g["hit_name"]).all()
+    np.testing.assert_allclose(ht, g["hit_dist"], rtol=1e-7)  # frozen-octree float precision
+
+
+def test_zoo_cast_and_direct(oscenes):
+    g = golden("zoo.npz")
+    sc = oscenes["zoo"]
+    o = po.default_opts("rtrace", ab=0, dj=0, ds=0, dr=0, dt=0, u=0)
+    rgb, hid, ht, _ = po.rtrace(sc, o, g["rays"])
+    names = np.array([sc.object_name(i) if i >= 0 else "*" for i in hid])
+    assert (names == g["hit_name"]).mean() == 1.0
+    # the reference read a frozen octree (31-bit mantissas); near-tangent
+    # hits on curved surfaces amplify that to a few 1e-6
+    np.testing.assert_allclose(ht, g["hit_dist"], rtol=1e-5, atol=1e-9)
+    np.testing.assert_allclose(rgb, g["radiance"], rtol=1e-5, atol=1e-9)
+    o.I = 1
+    irr, _, _, _ = po.rtrace(sc, o, g["rays"], hits=False)
+    np.testing.assert_allclose(irr, g["irradiance"], rtol=1e-6, atol=1e-9)
+
+
+@pytest.mark.skipif(not REF_TRACE.exists(), reason="reference test fixture not present")
+def test_reference_fixture_trace_oct():
+    g = golden("ref_trace_oct.npz")
+    sc = po.Scene(REF_TRACE)
+    o = po.default_opts("rtrace", ab=0, u=0)
+    _, hid, ht, _ = po.rtrace(sc, o, g["rays"], values=False)
+    names = np.array([sc.object_name(i) if i >= 0 else "*" for i in hid])
+    assert (names == g["hit_name"]).all()
+    np.testing.assert_allclose(ht, g["hit_dist"], rtol=1e-8)
+
+
+def test_dctimestep_oracle():
+    g = golden("dct_small.npz")
+    out = po.dctimestep(g["dc"], g["sky"])
+    np.testing.assert_array_equal(out, g["out"])
+
+
+def check_c2_statistics(a, g, K):
+    """a: (sensors, K, 146) samples of channel 0.  Compares with the golden
+    reference statistics: per-sensor totals, per-sensor altitude-row groups
+    and the individual bins that both sides sample often enough for a
+    normal approximation (z-scores of the difference of means)."""
+    from conftest import ROW_EDGES
+    zt = zscores(a.sum(2).mean(1), a.sum(2).std(1, ddof=1) / np.sqrt(K), g["total_mean"], g["total_se"])
+    assert np.abs(zt).max() < 4.5, zt
+    assert abs(zt.mean()) < 1.0, zt
+    grp = np.stack([a[:, :, e0:e1].sum(2) for e0, e1 in zip(ROW_EDGES[:-1], ROW_EDGES[1:])], 2)
+    gm, gs = grp.mean(1), grp.std(1, ddof=1) / np.sqrt(K)
+    gn = (grp > 0).sum(1)
+    ok = (gn >= 10) & (g["group_se"] > 0)
+    zg = (gm - g["group_mean"])[ok] / np.sqrt(gs ** 2 + g["group_se"] ** 2)[ok]
+    assert len(zg) >= 20
+    assert abs(zg.mean()) < 0.5 and zg.std() < 1.5 and np.abs(zg).max() < 5, (zg.mean(), zg.std())
+    nz = (a > 0).sum(1)
+    okb = (nz >= 10) & (g["nnz"] >= 10 * g["K"] // K)
+    zb = (a.mean(1) - g["mean"])[okb] / np.sqrt((a.std(1, ddof=1) / np.sqrt(K)) ** 2 + g["se"] ** 2)[okb]
+    if len(zb) >= 20:
+        assert abs(zb.mean()) < 0.5 and zb.std() < 1.5 and (np.abs(zb) > 4).mean() < 0.01, (zb.mean(), zb.std())
+    return zt, zg, zb
+
+
+@pytest.mark.parametrize("ab,K", [(1, 128), (3, 48)])
+def test_c2_rcontrib_statistics(oscenes, ab, K):
+    """Sample means of the oracle agree with the reference's -u+ runs within
+    their standard errors."""
+    g = golden(f"c2_stats_ab{ab}.npz")
+    sc = oscenes["c2"]
+    rays = np.repeat(g["rays"], K, axis=0)
+    o = po.default_opts("rcontrib", I=1, ab=ab, ad=1024, lw=1e-4, c=1, u=0, seed=12345)
+    out, nr = po.rcontrib(sc, o, MODS_C2, rays, threads=8)
+    check_c2_statistics(out[..., 0].reshape(len(g["rays"]), K, 146), g, K)
