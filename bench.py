@@ -1,0 +1,330 @@
+"""Benchmark of the GPU rcontrib path (the daylight-coefficient workload).
+
+Workload: 4,096 sensors (64 x 64 grid at z = 0.8, facing up) in the 10 x 8 x 3 m
+room with a 3 x 2 m glass window and 20,000 random triangles, glow sky and
+ground binned into Reinhart MF:1 (145 patches) + ground = 146 bins, run as
+rcontrib -I+ -ab 3 -ad 1024 -lw 1e-4 -c 1.  A step is one full pass over the
+4,096 sensors.  The metric is rays traced per second (every octree walk:
+ambient, transmitted, reflected and shadow rays), in Mrays/s.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+value   device throughput: rays / (CUDA-event time of the kernel region on the
+        library's stream), inputs and outputs resident in HBM;
+e2e     the same through the C ABI with host buffers (sensor upload and
+        bin download inside the timed region), wall clock per call;
+L2 is flushed (256 MB write) before every timed step.  Multi-GPU runs shard
+independent sensor replicas across ranks (weak scaling, no data collective).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "rcontrib Mrays/s (1 GB300)"
+PARAMS = ["-I+", "-ab", "3", "-ad", "1024", "-lw", "1e-4", "-c", "1", "-u-"]
+MODS = [dict(modifier="groundglow"),
+        dict(modifier="skyglow", calfile="reinhartb.cal", param="MF=1", binv="rbin", nbins="Nrbins")]
+WORKLOAD = ("rcontrib daylight coefficients: 4096 sensors (64x64 grid, z=0.8, +z), -I+ -ab 3 -ad 1024 "
+            "-lw 1e-4 -c 1; room 10x8x3 m + 2x3 m glass window (transmissivity 0.6) + 20,000 random "
+            "triangles; glow sky + ground, Reinhart MF:1 + ground = 146 bins")
+# algorithmic bytes per unit of traversal work
+B_NODE, B_STEP, B_TEST, B_QRAY = 4, 8, 60, 128
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.out = tempfile.NamedTemporaryFile(mode="w+", delete=False, suffix=".csv")
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.out, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.out.flush()
+        rows = [ln.split(",") for ln in Path(self.out.name).read_text().splitlines() if ln.strip()]
+        os.unlink(self.out.name)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            try:
+                sm.append(float(r[1]))
+                mx.append(float(r[2]))
+                for k, nm in enumerate(names):
+                    if r[5 + k].strip().lower() in ("active", "1"):
+                        reasons.add(nm)
+            except (ValueError, IndexError):
+                continue
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def make_scene(tmp: Path):
+    from pyradiance_gb300 import workloads as w
+    rad = tmp / "window_room.rad"
+    rad.write_text(w.window_room())
+    return rad, w.sensor_grid(64, 64)
+
+
+# ------------------------------------------------------------ CPU baseline
+
+def cpu_baseline(rad: Path, rays: np.ndarray, seconds: float = 15.0):
+    """The oracle (a scalar FP64 port of the reference algorithm) on the host
+    cores, on a bounded sample: sensors of the same grid, OpenMP threads over
+    sensors.  Returns (Mrays/s, threads, sample description)."""
+    from oracle import pyoracle as po
+    threads = os.cpu_count() or 1
+    sc = po.Scene(rad)
+    o = po.default_opts("rcontrib", I=1, ab=3, ad=1024, lw=1e-4, c=1, u=0, seed=1)
+    mods = [dict(modifier="groundglow"),
+            dict(modifier="skyglow", calfile="reinhartb.cal", params="MF=1", binv="rbin", nbins="Nrbins")]
+    n = threads * 2
+    total_rays, total_t, used = 0, 0.0, 0
+    idx = np.linspace(0, len(rays) - 1, len(rays)).astype(int)
+    rng = np.random.default_rng(0)
+    rng.shuffle(idx)
+    while total_t < seconds and used < len(rays):
+        sel = rays[idx[used:used + n]]
+        t0 = time.perf_counter()
+        _, nr = po.rcontrib(sc, o, mods, sel, threads=threads)
+        total_t += time.perf_counter() - t0
+        total_rays += nr
+        used += len(sel)
+    return total_rays / total_t / 1e6, threads, f"{used} of the 4096 sensors (random subset), full -ab 3 -ad 1024 paths"
+
+
+def reference_arm(args):
+    """--impl reference: the reference's CPU implementation of the path on
+    the host cores: the reference rcontrib compiled from its sources where it
+    is present (oracle/_ref), else the oracle port of it."""
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    with tempfile.TemporaryDirectory() as td:
+        rad, rays = make_scene(Path(td))
+        ref_bin = ROOT / "oracle" / "_ref" / "bin"
+        threads = os.cpu_count() or 1
+        if (ref_bin / "rcontrib").exists() and (ref_bin / "oconv").exists():
+            from oracle import pyoracle as po
+            from pyradiance_gb300 import workloads as w
+            env = dict(os.environ, RAYPATH=f".:{ROOT / 'oracle' / '_ref' / 'lib'}")
+            octp = Path(td) / "scene.oct"
+            octp.write_bytes(subprocess.run([str(ref_bin / "oconv"), str(rad)], capture_output=True,
+                                            check=True, env=env).stdout)
+            n = threads * 32
+            sel = rays[np.linspace(0, len(rays) - 1, n).astype(int)]
+            # ray count of this sample from the oracle's counters (same definition as the GPU's)
+            sc = po.Scene(rad)
+            o = po.default_opts("rcontrib", I=1, ab=3, ad=1024, lw=1e-4, c=1, u=0, seed=3)
+            mods = [dict(modifier="groundglow"),
+                    dict(modifier="skyglow", calfile="reinhartb.cal", params="MF=1", binv="rbin",
+                         nbins="Nrbins")]
+            _, nrays = po.rcontrib(sc, o, mods, sel, threads=threads)
+            times = []
+            for _ in range(max(1, args.steps)):
+                t0 = time.perf_counter()
+                subprocess.run([str(ref_bin / "rcontrib"), "-h", "-n", str(threads), "-I+", "-ab", "3", "-ad",
+                                "1024", "-lw", "1e-4", "-c", "1", "-fad", "-m", "groundglow", "-f",
+                                "reinhartb.cal", "-p", "MF=1", "-b", "rbin", "-bn", "Nrbins", "-m", "skyglow",
+                                str(octp)], input=w.rays_ascii(sel), capture_output=True, check=True, env=env,
+                               cwd=td)
+                times.append(time.perf_counter() - t0)
+            v = nrays / statistics.median(times) / 1e6
+            kind, sample = "reference", f"{n} sensors of the grid, rcontrib -n {threads}"
+        else:
+            v, threads, sample = cpu_baseline(rad, rays, seconds=max(10.0, 5.0 * args.steps))
+            kind = "port"
+    line = {"metric": METRIC, "value": round(v, 4), "unit": "Mrays/s", "impl": "reference", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+            "config": {"workload": WORKLOAD},
+            "cpu_baseline": {"value": round(v, 4), "unit": "Mrays/s", "cores": threads, "kind": kind,
+                             "sample": sample},
+            "e2e": {"value": round(v, 4), "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------- GPU arm
+
+def traffic_from_profiles():
+    """Per-launch DRAM bytes of the dominant kernel from the committed ncu
+    summary, if one exists."""
+    p = ROOT / "profiles" / "k_gen_root_rcontrib_window_room_traffic.txt"
+    if not p.exists():
+        return None
+    for ln in p.read_text().splitlines():
+        if ln.startswith("dram_bytes_per_launch_full_size="):
+            return float(ln.split("=", 1)[1])
+    return None
+
+
+def gpu_arm(args):
+    import torch
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    import pyradiance_gb300 as gb
+    from pyradiance_gb300 import _lib
+
+    dev = torch.device("cuda", local)
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)   # 256 MB > L2
+
+    with tempfile.TemporaryDirectory() as td:
+        rad, rays = make_scene(Path(td))
+        sc = gb.Scene(rad_files=[rad])
+        rc = gb.Rcontrib(b"", sc, params=PARAMS)
+        for m in MODS:
+            rc.add_modifier(**m)
+        rc.replica = rank                        # independent samples per rank
+        rc.seed = 20261203
+        rays = np.ascontiguousarray(rays)
+
+        def step():
+            flush.fill_(float(np.random.rand()))
+            torch.cuda.synchronize(dev)
+            t0 = time.perf_counter()
+            out = rc.run_array(rays)
+            wall = time.perf_counter() - t0
+            prof = _lib.last_profile()
+            st = _lib.last_stats()
+            return out, wall, prof, st
+
+        for _ in range(max(3, args.warmup)):
+            step()
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+        torch.cuda.synchronize(dev)
+        clocks = ClockSampler(local)
+        clocks.start()
+        walls, regions, rays_tot, launches, profs = [], [], 0, 0, []
+        for _ in range(args.steps):
+            out, wall, prof, st = step()
+            walls.append(wall)
+            regions.append(prof["region_ms"])
+            rays_tot += st["rays"]
+            launches += st["launches"]
+            profs.append(prof)
+        torch.cuda.synchronize(dev)
+        ck = clocks.stop()
+        dev_s = sum(regions) / 1e3
+        wall_s = sum(walls)
+        if world > 1:
+            import torch.distributed as dist
+            t = torch.tensor([dev_s, wall_s, float(rays_tot)], dtype=torch.float64, device=dev)
+            mx = t.clone()
+            dist.all_reduce(mx, op=dist.ReduceOp.MAX)
+            sm = t.clone()
+            dist.all_reduce(sm, op=dist.ReduceOp.SUM)
+            dev_s, wall_s, rays_all = float(mx[0]), float(mx[1]), float(sm[2])
+        else:
+            rays_all = float(rays_tot)
+        if rank != 0:
+            return
+        # dominant kernel and its roofline
+        agg = {}
+        for p in profs:
+            for k, v in p.items():
+                if k == "region_ms":
+                    continue
+                a = agg.setdefault(k, {"ms": 0.0, "launches": 0, "rays": 0, "steps": 0, "nodes": 0, "tests": 0})
+                for f in a:
+                    a[f] += v[f]
+        dom = max(agg, key=lambda k: agg[k]["ms"])
+        d = agg[dom]
+        bytes_per_launch = (d["nodes"] * B_NODE + d["steps"] * B_STEP + d["tests"] * B_TEST) / d["launches"]
+        ms_per_launch = d["ms"] / d["launches"]
+        achieved = bytes_per_launch / (ms_per_launch / 1e3) / 1e9
+        peak, peak_kind = peaks()
+        traffic = traffic_from_profiles()
+        cpu_v, cores, sample = cpu_baseline(rad, rays, seconds=12.0) if not args.no_cpu else (None, 0, "skipped")
+        value = rays_all / dev_s / 1e6
+        e2e = rays_all / wall_s / 1e6
+        line = {
+            "metric": METRIC, "value": round(value, 3), "unit": "Mrays/s", "n_gpus": world,
+            "steps": args.steps, "warmup": max(3, args.warmup), "ms_per_step": round(dev_s * 1e3 / args.steps, 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded scene and sensor grid)",
+            "config": {"workload": WORKLOAD, "sensors_per_gpu": int(len(rays)), "l2": "flushed before each step",
+                       "rays_per_step_per_gpu": int(rays_tot / args.steps), "kernels": {k: {
+                           "ms_per_step": round(v["ms"] / args.steps, 3), "launches": v["launches"]}
+                           for k, v in agg.items()}},
+            "e2e": {"value": round(e2e, 3), "unit": "Mrays/s", "h2d_bytes_per_step": int(rays.nbytes),
+                    "d2h_bytes_per_step": int(len(rays) * 146 * 3 * 8)},
+            "gpu_launches": int(launches),
+            "roofline": {"bound": "hbm", "kernel": "k_" + dom, "achieved": round(achieved, 1), "peak": peak,
+                         "unit": "GB/s", "frac": round(achieved / peak, 4),
+                         "traffic": traffic, "peak_source": peak_kind,
+                         "note": "algorithmic bytes = node descents*4 + cube visits*8 + object tests*60"},
+            "cpu_baseline": {"value": None if cpu_v is None else round(cpu_v, 4), "unit": "Mrays/s",
+                             "cores": cores, "kind": "port", "sample": sample},
+            "clocks": ck,
+        }
+        print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        reference_arm(args)
+    else:
+        gpu_arm(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -69,6 +69,8 @@ _SIGS = {
     "gb_dctimestep_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_int64, C.c_int64, C.c_int,
                                        C.c_void_p, C.c_void_p]),
     "gb_last_stats": (C.c_int, [C.POINTER(C.c_int64)] * 4),
+    "gb_last_profile": (C.c_int, [C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_int64), C.POINTER(C.c_int64),
+                                  C.c_int, C.POINTER(C.c_double)]),
     "gb_last_error": (C.c_char_p, []),
     "gb_version": (C.c_char_p, []),
 }
@@ -100,6 +102,25 @@ def last_stats() -> dict:
     v = [C.c_int64() for _ in range(4)]
     lib().gb_last_stats(*[C.byref(x) for x in v])
     return {"rays": v[0].value, "steps": v[1].value, "contribs": v[2].value, "launches": v[3].value}
+
+
+KERNELS = ["cast", "root", "gen_root", "primary", "gen"]
+COUNTERS = ["rays", "steps", "contribs", "overflow", "badbin", "nodes", "tests", "spare"]
+
+
+def last_profile() -> dict:
+    """Per-kernel device time (ms), launches and counters of the last call."""
+    out = {}
+    region = C.c_double(0)
+    for k, name in enumerate(KERNELS):
+        ms = C.c_double(0)
+        nl = C.c_int64(0)
+        cnt = (C.c_int64 * 8)()
+        lib().gb_last_profile(k, C.byref(ms), C.byref(nl), cnt, 8, C.byref(region))
+        if nl.value:
+            out[name] = {"ms": ms.value, "launches": nl.value, **{c: int(cnt[i]) for i, c in enumerate(COUNTERS)}}
+    out["region_ms"] = region.value
+    return out
 
 
 def ptr(a: np.ndarray | None):

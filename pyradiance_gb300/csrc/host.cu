@@ -95,7 +95,31 @@ struct gb_scene {
     DevBuf sensors, value, bins, stats, roots, rootspt, qa, qb, qcount, binprog, modinfo, hits, hitt, trkrun;
     cudaStream_t stream = nullptr;
     int sms = 0;
+    cudaEvent_t ev[2 * 96 + 2];
+    int nev = 0;
 };
+
+/* per-kernel profile of the last run on this thread */
+struct KProf {
+    double ms[GB_K_N];
+    int64_t launches[GB_K_N];
+    unsigned long long st[GB_K_N][GB_ST_N];
+    double region_ms;
+};
+static thread_local KProf g_prof;
+
+extern "C" int gb_last_profile(int kernel, double *ms, int64_t *launches, int64_t *counters, int ncounters,
+                               double *region_ms)
+{
+    if (kernel < 0 || kernel >= GB_K_N)
+        return set_err(GB_EINVAL, "bad kernel index");
+    if (ms) *ms = g_prof.ms[kernel];
+    if (launches) *launches = g_prof.launches[kernel];
+    for (int i = 0; counters && i < ncounters && i < GB_ST_N; i++)
+        counters[i] = (int64_t)g_prof.st[kernel][i];
+    if (region_ms) *region_ms = g_prof.region_ms;
+    return GB_OK;
+}
 
 static int material_kind(const gb_object *m, float4 *m0, float4 *m1, std::string &why)
 {
@@ -301,6 +325,11 @@ static int prepare_device(gb_scene *G)
     CK(cudaGetDevice(&dev));
     CK(cudaDeviceGetAttribute(&G->sms, cudaDevAttrMultiProcessorCount, dev));
     CK(cudaStreamCreateWithFlags(&G->stream, cudaStreamNonBlocking));
+    /* the sequential hemisphere placement keeps a 4 KB lot per thread */
+    size_t stack = 0;
+    cudaDeviceGetLimit(&stack, cudaLimitStackSize);
+    if (stack < 16384)
+        CK(cudaDeviceSetLimit(cudaLimitStackSize, 16384));
     /* materials */
     G->matslot.assign(H.nobjs, -1);
     std::vector<int> slot_of_mat(H.nobjs, -1);
@@ -757,14 +786,41 @@ static int run(gb_scene *G, const gb_opts *o, int follow, const double *org_dir,
 {
     cudaStream_t st = G->stream;
     g_stats[0] = g_stats[1] = g_stats[2] = g_stats[3] = 0;
+    memset(&g_prof, 0, sizeof g_prof);
     if (n <= 0)
         return GB_OK;
+    const size_t stat_bytes = GB_K_N * GB_ST_N * sizeof(unsigned long long);
     size_t sbytes = (size_t)n * 6 * sizeof(double);
-    if (G->sensors.ensure(sbytes) < 0 || G->stats.ensure(GB_ST_N * sizeof(unsigned long long)) < 0 ||
+    if (G->sensors.ensure(sbytes) < 0 || G->stats.ensure(stat_bytes) < 0 ||
         G->qcount.ensure(4 * sizeof(unsigned long long)) < 0)
         return set_err(GB_ENOMEM, "device allocation failed");
+    if (!G->nev) {
+        for (int k = 0; k < (int)(sizeof G->ev / sizeof G->ev[0]); k++)
+            CK(cudaEventCreate(&G->ev[k]));
+        G->nev = (int)(sizeof G->ev / sizeof G->ev[0]);
+    }
+    int evused = 2;                                /* ev[0], ev[1]: the kernel region */
+    int evkid[96];
+    /* one launch, bracketed by events, counting into its kernel's block */
+    auto launch = [&](int kid, gb_run &PR, auto fn) -> int {
+        PR.stats = (unsigned long long *)G->stats.p + kid * GB_ST_N;
+        int slot = (evused - 2) / 2;
+        bool timed = slot < 96;
+        if (timed)
+            cudaEventRecord(G->ev[evused], st);
+        if (fn(PR) < 0)
+            return set_err(GB_ECUDA, "launch failed: %s", cudaGetErrorString(cudaGetLastError()));
+        if (timed) {
+            cudaEventRecord(G->ev[evused + 1], st);
+            evkid[slot] = kid;
+            evused += 2;
+        }
+        g_stats[3]++;
+        g_prof.launches[kid]++;
+        return GB_OK;
+    };
     CK(cudaMemcpyAsync(G->sensors.p, org_dir, sbytes, cudaMemcpyHostToDevice, st));
-    CK(cudaMemsetAsync(G->stats.p, 0, GB_ST_N * sizeof(unsigned long long), st));
+    CK(cudaMemsetAsync(G->stats.p, 0, stat_bytes, st));
 
     gb_run P;
     memset(&P, 0, sizeof P);
@@ -793,9 +849,10 @@ static int run(gb_scene *G, const gb_opts *o, int follow, const double *org_dir,
         if (G->hits.ensure((size_t)n * sizeof(int)) < 0 || G->hitt.ensure((size_t)n * sizeof(float)) < 0)
             return set_err(GB_ENOMEM, "device allocation failed");
         P.S.trk = nullptr;
-        if (gb_launch_cast(&P, (int *)G->hits.p, (float *)G->hitt.p, nullptr, st, G->sms) < 0)
-            return set_err(GB_ECUDA, "cast launch failed: %s", cudaGetErrorString(cudaGetLastError()));
-        g_stats[3]++;
+        int rc = launch(GB_K_CAST, P, [&](gb_run &R) {
+            return gb_launch_cast(&R, (int *)G->hits.p, (float *)G->hitt.p, nullptr, st, G->sms); });
+        if (rc < 0)
+            return rc;
         std::vector<int> h(n);
         std::vector<float> t(n);
         CK(cudaMemcpyAsync(h.data(), G->hits.p, (size_t)n * sizeof(int), cudaMemcpyDeviceToHost, st));
@@ -820,7 +877,8 @@ static int run(gb_scene *G, const gb_opts *o, int follow, const double *org_dir,
     }
     int64_t nrec = n / P.accum;
     if (out.bins) {
-        size_t bb = (size_t)(nrec > 0 ? nrec : 1) * nbins_total * 3 * sizeof(double);
+        /* room for a trailing partial record, which is not returned */
+        size_t bb = (size_t)((n + P.accum - 1) / P.accum + 1) * nbins_total * 3 * sizeof(double);
         if (G->bins.ensure(bb) < 0 || upload(G->binprog, *prog) < 0 || upload(G->modinfo, *modinfo) < 0 ||
             upload(G->trkrun, *trk) < 0)
             return set_err(GB_ENOMEM, "device allocation failed");
@@ -838,6 +896,9 @@ static int run(gb_scene *G, const gb_opts *o, int follow, const double *org_dir,
 
     /* queues: sized for the expected fan-out, bounded by memory */
     int n0 = (o->I && o->ab > 0 && o->ad > 0) ? root_divisions(o) : 0;
+    if (n0 > 128)
+        return set_err(GB_EUNSUPPORTED, "-ad %d gives %d x %d hemisphere divisions; at most 128 x 128 are "
+                       "supported", o->ad, n0, n0);
     long long est = (long long)n * (n0 > 0 ? (long long)n0 * n0 * 4 : (o->ab > 0 ? (long long)o->ad * 2 : 8));
     long long qcap = est < (1ll << 20) ? (1ll << 20) : est;
     size_t freeb = 0, totalb = 0;
@@ -861,22 +922,24 @@ static int run(gb_scene *G, const gb_opts *o, int follow, const double *org_dir,
             P.root_spt = (float2 *)G->rootspt.p;
         }
         P.root_n = n0;
-        if (gb_launch_root(&P, st, G->sms) < 0)
-            return set_err(GB_ECUDA, "launch failed: %s", cudaGetErrorString(cudaGetLastError()));
-        g_stats[3]++;
+        CK(cudaEventRecord(G->ev[0], st));
+        int rc = launch(GB_K_ROOT, P, [&](gb_run &R) { return gb_launch_root(&R, st, G->sms); });
+        if (rc < 0)
+            return rc;
         if (n0 > 0) {
             P.qout = qa;
             P.qout_count = cnt;
-            if (gb_launch_gen_root(&P, st, G->sms) < 0)
-                return set_err(GB_ECUDA, "launch failed: %s", cudaGetErrorString(cudaGetLastError()));
-            g_stats[3]++;
+            rc = launch(GB_K_GENROOT, P, [&](gb_run &R) { return gb_launch_gen_root(&R, st, G->sms); });
+            if (rc < 0)
+                return rc;
         }
     } else {
         P.qout = qa;
         P.qout_count = cnt;
-        if (gb_launch_primary(&P, st, G->sms) < 0)
-            return set_err(GB_ECUDA, "launch failed: %s", cudaGetErrorString(cudaGetLastError()));
-        g_stats[3]++;
+        CK(cudaEventRecord(G->ev[0], st));
+        int rc = launch(GB_K_PRIMARY, P, [&](gb_run &R) { return gb_launch_primary(&R, st, G->sms); });
+        if (rc < 0)
+            return rc;
     }
     /* later generations until the queue drains */
     int in = 0;
@@ -893,13 +956,14 @@ static int run(gb_scene *G, const gb_opts *o, int follow, const double *org_dir,
         P.qout = in ? qa : qb;
         P.qout_count = cnt + (1 - in);
         CK(cudaMemsetAsync(cnt + (1 - in), 0, sizeof(unsigned long long), st));
-        if (gb_launch_gen(&P, st, G->sms) < 0)
-            return set_err(GB_ECUDA, "launch failed: %s", cudaGetErrorString(cudaGetLastError()));
-        g_stats[3]++;
+        int rc = launch(GB_K_GEN, P, [&](gb_run &R) { return gb_launch_gen(&R, st, G->sms); });
+        if (rc < 0)
+            return rc;
         CK(cudaMemsetAsync(cnt + in, 0, sizeof(unsigned long long), st));
         in = 1 - in;
     }
-    unsigned long long stats[GB_ST_N];
+    CK(cudaEventRecord(G->ev[1], st));
+    unsigned long long stats[GB_K_N][GB_ST_N];
     CK(cudaMemcpyAsync(stats, G->stats.p, sizeof stats, cudaMemcpyDeviceToHost, st));
     if (out.value)
         CK(cudaMemcpyAsync(out.value, G->value.p, (size_t)n * 3 * sizeof(double), cudaMemcpyDeviceToHost, st));
@@ -907,11 +971,26 @@ static int run(gb_scene *G, const gb_opts *o, int follow, const double *org_dir,
         CK(cudaMemcpyAsync(out.bins, G->bins.p, (size_t)nrec * nbins_total * 3 * sizeof(double),
                            cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
-    g_stats[0] = (int64_t)stats[GB_ST_RAYS];
-    g_stats[1] = (int64_t)stats[GB_ST_STEPS];
-    g_stats[2] = (int64_t)stats[GB_ST_CONTRIB];
-    if (stats[GB_ST_OVERFLOW])
-        return set_err(GB_EOVERFLOW, "ray queue overflow (%llu records dropped)", stats[GB_ST_OVERFLOW]);
+    unsigned long long overflow = 0;
+    for (int k = 0; k < GB_K_N; k++) {
+        g_stats[0] += (int64_t)stats[k][GB_ST_RAYS];
+        g_stats[1] += (int64_t)stats[k][GB_ST_STEPS];
+        g_stats[2] += (int64_t)stats[k][GB_ST_CONTRIB];
+        overflow += stats[k][GB_ST_OVERFLOW];
+        memcpy(g_prof.st[k], stats[k], sizeof stats[k]);
+    }
+    for (int s = 0; 2 + 2 * s + 1 < evused; s++) {
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, G->ev[2 + 2 * s], G->ev[3 + 2 * s]);
+        g_prof.ms[evkid[s]] += ms;
+    }
+    {
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, G->ev[0], G->ev[1]);
+        g_prof.region_ms = ms;
+    }
+    if (overflow)
+        return set_err(GB_EOVERFLOW, "ray queue overflow (%llu records dropped)", overflow);
     return GB_OK;
 }
 

@@ -53,8 +53,24 @@ struct Ray {
 };
 
 struct Counters {
-    unsigned long long rays, steps, contrib;
+    unsigned long long rays, steps, nodes, tests, contrib;
+    __device__ void add(const uint32_t t[3])
+    {
+        steps += t[0];
+        nodes += t[1];
+        tests += t[2];
+    }
 };
+
+/* one atomic per thread and counter at the end of a kernel */
+__device__ __forceinline__ void flush_counters(const gb_run &P, const Counters &c)
+{
+    if (c.rays) atomicAdd(P.stats + GB_ST_RAYS, c.rays);
+    if (c.steps) atomicAdd(P.stats + GB_ST_STEPS, c.steps);
+    if (c.nodes) atomicAdd(P.stats + GB_ST_NODES, c.nodes);
+    if (c.tests) atomicAdd(P.stats + GB_ST_TESTS, c.tests);
+    if (c.contrib) atomicAdd(P.stats + GB_ST_CONTRIB, c.contrib);
+}
 
 /* -------------------------------------------------------------- records */
 
@@ -465,12 +481,12 @@ __device__ float3 shadow_chain(const gb_run &P, Ray sr, int s, Counters &cnt, fl
     const float3 zero = f3(0.f, 0.f, 0.f);
     for (int guard = 0; guard < 32; guard++) {
         Hit h;
-        uint32_t st = 0;
+        uint32_t st[3] = {0, 0, 0};
         cnt.rays++;
         int okind = sr.origin >= 0 ? (S.obj[sr.origin].x & 0xff) : DK_NONE;
         bool planar = okind == DK_FACE || okind == DK_RING;
-        bool hit = local_hit(S, sr.org, sr.dir, planar ? sr.origin : -1, D_FTINY, D_FHUGE, h, &st);
-        cnt.steps += st;
+        bool hit = local_hit(S, sr.org, sr.dir, planar ? sr.origin : -1, D_FTINY, D_FHUGE, h, st);
+        cnt.add(st);
         if (!hit) {
             if (guard == 0) {
                 if (P.follow && (src.flags & DS_DISTANT)) {
@@ -683,11 +699,9 @@ __device__ void run_ray(const gb_run &P, Ray r, Counters &cnt)
         cnt.rays++;
         int okind = r.origin >= 0 ? (S.obj[r.origin].x & 0xff) : DK_NONE;
         bool planar = okind == DK_FACE || okind == DK_RING;
-        unsigned long long steps = 0;
-        uint32_t st32 = 0;
-        bool hit = local_hit(S, r.org, r.dir, planar ? r.origin : -1, D_FTINY, D_FHUGE, h, &st32);
-        steps += st32;
-        cnt.steps += steps;
+        uint32_t st[3] = {0, 0, 0};
+        bool hit = local_hit(S, r.org, r.dir, planar ? r.origin : -1, D_FTINY, D_FHUGE, h, st);
+        cnt.add(st);
         if (!hit) {
             int sidx = source_hit(S, r.dir, r.rsrc, r.crtype);
             if (sidx < 0)
@@ -815,7 +829,7 @@ __device__ void run_ray(const gb_run &P, Ray r, Counters &cnt)
 /* -I sensor: the Lambertian pretend-hit, its direct part and its frame */
 __global__ void k_root(gb_run P)
 {
-    Counters cnt = {0, 0, 0};
+    Counters cnt = {0, 0, 0, 0, 0};
     for (long long s = blockIdx.x * (long long)blockDim.x + threadIdx.x; s < P.nsensors;
          s += (long long)gridDim.x * blockDim.x) {
         const double *sv = P.sensors + 6 * s;
@@ -863,14 +877,13 @@ __global__ void k_root(gb_run P)
             add_value(P, r.sensor, su.mcolor * f3(P.av[0], P.av[1], P.av[2]));
         }
     }
-    atomicAdd(P.stats + ST_RAYS, cnt.rays);
-    atomicAdd(P.stats + ST_CONTRIB, cnt.contrib);
+    flush_counters(P, cnt);
 }
 
 /* first hemisphere of every -I sensor, expanded from (sensor, stratum) */
 __global__ void __launch_bounds__(256) k_gen_root(gb_run P)
 {
-    Counters cnt = {0, 0, 0};
+    Counters cnt = {0, 0, 0, 0, 0};
     const long long nn = (long long)P.root_n * P.root_n;
     const long long total = nn * P.nsensors;
     for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < total;
@@ -911,15 +924,13 @@ __global__ void __launch_bounds__(256) k_gen_root(gb_run P)
             continue;
         run_ray(P, c, cnt);
     }
-    atomicAdd(P.stats + ST_RAYS, cnt.rays);
-    atomicAdd(P.stats + ST_STEPS, cnt.steps);
-    atomicAdd(P.stats + ST_CONTRIB, cnt.contrib);
+    flush_counters(P, cnt);
 }
 
 /* radiance-mode primaries (rt/rtrace.c:436-468, rt/rcontrib.c:343-353) */
 __global__ void k_primary(gb_run P)
 {
-    Counters cnt = {0, 0, 0};
+    Counters cnt = {0, 0, 0, 0, 0};
     for (long long s = blockIdx.x * (long long)blockDim.x + threadIdx.x; s < P.nsensors;
          s += (long long)gridDim.x * blockDim.x) {
         const double *sv = P.sensors + 6 * s;
@@ -938,14 +949,12 @@ __global__ void k_primary(gb_run P)
         r.sensor = (uint32_t)s;
         run_ray(P, r, cnt);
     }
-    atomicAdd(P.stats + ST_RAYS, cnt.rays);
-    atomicAdd(P.stats + ST_STEPS, cnt.steps);
-    atomicAdd(P.stats + ST_CONTRIB, cnt.contrib);
+    flush_counters(P, cnt);
 }
 
 __global__ void __launch_bounds__(256) k_gen(gb_run P)
 {
-    Counters cnt = {0, 0, 0};
+    Counters cnt = {0, 0, 0, 0, 0};
     unsigned long long n = *P.qin_count;
     if (n > (unsigned long long)P.qcap)
         n = P.qcap;
@@ -954,9 +963,7 @@ __global__ void __launch_bounds__(256) k_gen(gb_run P)
         Ray r = load_ray(P.qin + g);
         run_ray(P, r, cnt);
     }
-    atomicAdd(P.stats + ST_RAYS, cnt.rays);
-    atomicAdd(P.stats + ST_STEPS, cnt.steps);
-    atomicAdd(P.stats + ST_CONTRIB, cnt.contrib);
+    flush_counters(P, cnt);
 }
 
 /* castonly rtrace (rt/rtrace.c:398-411 raycast): first intersection only */
@@ -968,11 +975,11 @@ __global__ void k_cast(gb_run P, int *hit_obj, float *hit_t, float *hit_pn)
         float3 org = f3((float)sv[0], (float)sv[1], (float)sv[2]);
         float3 dir = normalize3(f3((float)sv[3], (float)sv[4], (float)sv[5]));
         Hit h;
-        uint32_t st = 0;
+        uint32_t st[3] = {0, 0, 0};
         int obj = -1;
         float t = D_FHUGE;
         float3 n = f3(0.f, 0.f, 0.f);
-        if (local_hit(P.S, org, dir, -1, D_FTINY, D_FHUGE, h, &st)) {
+        if (local_hit(P.S, org, dir, -1, D_FTINY, D_FHUGE, h, st)) {
             obj = h.obj;
             t = h.t;
             n = h.n;

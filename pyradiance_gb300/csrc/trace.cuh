@@ -304,7 +304,7 @@ __device__ __forceinline__ void hit_object(const gb_dscene &S, int obj, float3 o
  * ray leaves the scene, as localhit does.
  */
 __device__ __forceinline__ bool local_hit(const gb_dscene &S, float3 org, float3 dir, int skip,
-                                          float tmin, float tmax, Hit &best, uint32_t *steps_out)
+                                          float tmin, float tmax, Hit &best, uint32_t *tally)
 {
     best.obj = -1;
     best.t = D_FHUGE;
@@ -348,7 +348,7 @@ __device__ __forceinline__ bool local_hit(const gb_dscene &S, float3 org, float3
         int v = __float2int_rd((rr[i] + dd[i] * t) * gs);
         q[i] = min(max(v, 0), GRID_N - 1);
     }
-    uint32_t steps = 0;
+    uint32_t steps = 0, nodes = 0, tests = 0;
     for (;;) {
         /* descend to the leaf containing q */
         int node = S.root, level = 0;
@@ -358,6 +358,7 @@ __device__ __forceinline__ bool local_hit(const gb_dscene &S, float3 org, float3
             node = __ldg(S.kids + 8 * node + br);
             level++;
         }
+        nodes += level;
         int span = 1 << (GRID_BITS - level);
         int lo[3] = {q[0] & ~(span - 1), q[1] & ~(span - 1), q[2] & ~(span - 1)};
         /* exit distance of this cube */
@@ -376,6 +377,7 @@ __device__ __forceinline__ bool local_hit(const gb_dscene &S, float3 org, float3
         if (node <= -2) {                       /* full leaf: test its set */
             const int *set = S.set_data + __ldg(S.set_off + (-node - 2));
             int cnt = __ldg(set);
+            tests += cnt;
             for (int k = 1; k <= cnt; k++) {
                 int o = __ldg(set + k);
                 if (o != skip)
@@ -400,8 +402,11 @@ __device__ __forceinline__ bool local_hit(const gb_dscene &S, float3 org, float3
         if (q[ax] < 0 || q[ax] >= GRID_N)
             break;                              /* left the scene */
     }
-    if (steps_out)
-        *steps_out += steps + 1;
+    if (tally) {
+        tally[0] += steps + 1;
+        tally[1] += nodes;
+        tally[2] += tests;
+    }
     return best.obj >= 0;
 }
 

@@ -15,7 +15,16 @@
 #define GB_ST_CONTRIB  2   /* contributions binned */
 #define GB_ST_OVERFLOW 3   /* queue records dropped */
 #define GB_ST_BADBIN   4   /* bin numbers beyond nbins */
+#define GB_ST_NODES    5   /* octree node descents */
+#define GB_ST_TESTS    6   /* ray-object intersection tests */
 #define GB_ST_N        8
+/* kernels with their own block of GB_ST_N counters */
+#define GB_K_CAST      0
+#define GB_K_ROOT      1
+#define GB_K_GENROOT   2
+#define GB_K_PRIMARY   3
+#define GB_K_GEN       4
+#define GB_K_N         5
 
 #define GRID_BITS_HOST 24      /* must equal GRID_BITS of trace.cuh */
 

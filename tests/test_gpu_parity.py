@@ -1,0 +1,173 @@
+"""GPU path against the golden vectors and the CPU oracle (needs a GB300).
+
+Every call goes through the C ABI of libgbrad.so (ctypes).
+Tolerances: bit-exact first-hit objects; FP32 traversal and shading give
+values within 1e-5 relative of the reference for the deterministic direct
+cases (the bar of the deterministic rtrace workload), 1e-4 for distances
+and for radiance chains through mirrors; Monte Carlo results are compared
+with the oracle sample for sample (same random streams) and with the
+reference statistically.
+"""
+import numpy as np
+import pytest
+
+from conftest import MODS_C2, golden
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def gb():
+    import pyradiance_gb300 as gb
+    from pyradiance_gb300 import _lib
+    _lib.lib()
+    return gb
+
+
+@pytest.fixture(scope="module")
+def scenes(gb, scene_dir):
+    return {k: gb.Scene(rad_files=[scene_dir / f"{k}.rad"]) for k in ("c1", "c2", "zoo", "c2e")}
+
+
+def opts(prog, **kw):
+    from pyradiance_gb300 import _lib
+    o, _ = _lib.parse_opts([], _lib.GB_PROG_RCONTRIB if prog == "rcontrib" else _lib.GB_PROG_RTRACE)
+    for k, v in kw.items():
+        setattr(o, "as_" if k == "as" else k, v)
+    return o
+
+
+def rtrace_c(gb, sc, o, rays, values=True):
+    from pyradiance_gb300 import _lib
+    rays = np.ascontiguousarray(rays, dtype=np.float64)
+    n = len(rays)
+    rgb = np.zeros((n, 3)) if values else None
+    hid = np.zeros(n, dtype=np.int32)
+    ht = np.zeros(n)
+    _lib.check(_lib.lib().gb_rtrace(sc.handle, o, _lib.ptr(rays), n, _lib.ptr(rgb), _lib.ptr(hid), _lib.ptr(ht)))
+    return rgb, hid, ht
+
+
+def rcontrib_c(gb, sc, o, rays, mods=MODS_C2):
+    rc = gb.Rcontrib(b"", sc)
+    for m in mods:
+        rc.add_modifier(**{("expression" if k == "expr" else k): v for k, v in m.items()})
+    rc.args = []
+    rc.seed = int(o.seed)
+    from pyradiance_gb300 import _lib
+    out_opts = o
+
+    # run through the C ABI with exactly these options
+    specs, keep = rc._specs()
+    nb = _lib.C.c_int(0)
+    _lib.check(_lib.lib().gb_rcontrib_nbins(specs, len(rc.mods), _lib.C.byref(nb)))
+    rays = np.ascontiguousarray(rays, dtype=np.float64)
+    out = np.zeros((len(rays) // max(1, out_opts.c), nb.value, 3))
+    cnt = _lib.C.c_int64(0)
+    _lib.check(_lib.lib().gb_rcontrib(sc.handle, out_opts, specs, len(rc.mods), _lib.ptr(rays), len(rays),
+                                      _lib.ptr(out), _lib.C.byref(cnt)))
+    return out, cnt.value
+
+
+def names_of(sc, hid):
+    return np.array([sc.object_name(int(i)) if i >= 0 else "*" for i in hid])
+
+
+def test_c1_hit_ids_bit_exact(gb, scenes):
+    g = golden("c1_direct.npz")
+    sc = scenes["c1"]
+    _, hid, ht = rtrace_c(gb, sc, opts("rtrace", ab=0, u=0), g["rays"], values=False)
+    assert (names_of(sc, hid) == g["hit_name"]).all()
+    np.testing.assert_allclose(ht, g["hit_dist"], rtol=1e-5)
+
+
+def test_c1_direct_irradiance(gb, scenes):
+    g = golden("c1_direct.npz")
+    sc = scenes["c1"]
+    rgb, _, _ = rtrace_c(gb, sc, opts("rtrace", I=1, ab=0, dj=0, ds=0, dr=0, u=0), g["rays"])
+    ref = g["irradiance"]
+    lit = ref[:, 0] > 0
+    np.testing.assert_array_equal(rgb[~lit], 0.0)
+    rel = np.abs(rgb[lit] - ref[lit]) / ref[lit]
+    assert rel.max() < 1e-5, rel.max()
+
+
+def test_zoo_all_primitives(gb, scenes):
+    g = golden("zoo.npz")
+    sc = scenes["zoo"]
+    o = opts("rtrace", ab=0, dj=0, ds=0, dr=0, dt=0, u=0)
+    rgb, hid, ht = rtrace_c(gb, sc, o, g["rays"])
+    names = names_of(sc, hid)
+    match = names == g["hit_name"]
+    assert match.mean() >= 0.999, np.nonzero(~match)
+    ok = match & (g["hit_dist"] < 1e9)
+    np.testing.assert_allclose(ht[ok], g["hit_dist"][ok], rtol=1e-4)
+    np.testing.assert_allclose(rgb[match], g["radiance"][match], rtol=1e-4, atol=1e-6)
+    o.I = 1
+    irr, _, _ = rtrace_c(gb, sc, o, g["rays"])
+    np.testing.assert_allclose(irr, g["irradiance"], rtol=1e-4, atol=1e-6)
+
+
+def test_c2_matches_oracle_sample_for_sample(gb, scenes, scene_dir):
+    """Same random streams on the GPU (FP32) and in the oracle (FP64):
+    per-record sums agree closely; a path that diverges near an edge moves
+    at most one sample's coefficient."""
+    from oracle import pyoracle as po
+    rays = np.repeat(golden("c2_stats_ab3.npz")["rays"][:8], 4, axis=0)
+    o = opts("rcontrib", I=1, ab=3, ad=1024, lw=1e-4, c=1, u=0, seed=777)
+    out, nr = rcontrib_c(gb, scenes["c2"], o, rays)
+    osc = po.Scene(scene_dir / "c2.rad")
+    oo = po.default_opts("rcontrib", I=1, ab=3, ad=1024, lw=1e-4, c=1, u=0, seed=777)
+    ref, onr = po.rcontrib(osc, oo, MODS_C2, rays, threads=8)
+    ta, tb = out.sum((1, 2)), ref.sum((1, 2))
+    rel = np.abs(ta - tb) / np.maximum(tb, 1e-12)
+    assert np.median(rel) < 1e-4, rel
+    assert (rel < 2e-2).all(), rel
+    assert abs(nr - onr) / onr < 1e-3, (nr, onr)
+    assert abs(out.sum() - ref.sum()) / ref.sum() < 2e-3
+
+
+@pytest.mark.parametrize("ab,K", [(1, 256), (3, 256)])
+def test_c2_statistics_vs_reference(gb, scenes, ab, K):
+    from test_oracle_golden import check_c2_statistics
+    g = golden(f"c2_stats_ab{ab}.npz")
+    rays = np.repeat(g["rays"], K, axis=0)
+    o = opts("rcontrib", I=1, ab=ab, ad=1024, lw=1e-4, c=1, u=0, seed=4242)
+    out, _ = rcontrib_c(gb, scenes["c2"], o, rays)
+    check_c2_statistics(out[..., 0].reshape(len(g["rays"]), K, 146), g, K)
+
+
+def test_c2_full_grid_bins_equal_irradiance(gb, scenes):
+    """Size-independent property at the full 64 x 64 grid: the sky and
+    ground glows have radiance 1, so each sensor's coefficients summed over
+    all 146 bins equal its rtrace -I irradiance from the same random
+    streams."""
+    from pyradiance_gb300 import workloads as w
+    rays = w.sensor_grid(64, 64)
+    o = opts("rcontrib", I=1, ab=3, ad=1024, lw=1e-4, c=1, u=0, seed=99)
+    out, nr = rcontrib_c(gb, scenes["c2"], o, rays)
+    ort = opts("rtrace", I=1, ab=3, ad=1024, lw=1e-4, aa=0, u=0, seed=99, dj=0.9, ds=0.2, st=0.02, dt=0)
+    rgb, _, _ = rtrace_c(gb, scenes["c2"], ort, rays)
+    np.testing.assert_allclose(out.sum(1)[:, 0], rgb[:, 0], rtol=1e-5, atol=1e-12)
+    assert nr > 4096 * 5000
+
+
+def test_dctimestep_fp32_fp64(gb):
+    g = golden("dct_small.npz")
+    r64 = gb.dctimestep_array(g["dc"], g["sky"], mode="fp64")
+    np.testing.assert_allclose(r64, g["out"], rtol=1e-6, atol=1e-30)
+    r32 = gb.dctimestep_array(g["dc"], g["sky"], mode="fp32")
+    np.testing.assert_allclose(r32, g["out"], rtol=1e-4, atol=1e-6 * np.abs(g["out"]).max())
+
+
+def test_errors_are_reported(gb, scenes):
+    from pyradiance_gb300 import _lib
+    with pytest.raises(_lib.GbError) as e:
+        _lib.parse_opts(["-ab", "1", "-zz"], _lib.GB_PROG_RTRACE)
+    assert e.value.code == -1
+    o = opts("rtrace", ab=1, aa=0.1)
+    with pytest.raises(_lib.GbError) as e:
+        rtrace_c(gb, scenes["c1"], o, np.array([[1, 1, 1, 0, 0, 1.0]]))
+    assert e.value.code == -3
+    with pytest.raises(RuntimeError):
+        gb.rtrace(b"1 1 1 0 0 1\n", "/nonexistent.oct")

@@ -1,0 +1,96 @@
+"""Host-side logic of the library (CPU only): the C ABI loads and exports
+every declared symbol, option defaults and parsing follow the reference,
+bin expressions compile, and the workloads are deterministic."""
+import hashlib
+import re
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+ROOT = Path(__file__).resolve().parents[1]
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from pyradiance_gb300 import _lib
+    return _lib
+
+
+def test_c_abi_exports_every_declared_symbol(lib):
+    import ctypes
+    hdr = (ROOT / "include" / "gbrad.h").read_text()
+    names = re.findall(r"^[a-z][^(\n]*?\b(gb_[a-z_0-9]+)\s*\(", hdr, re.M)
+    assert len(names) >= 15
+    L = ctypes.CDLL(str(lib._LIBPATH))
+    missing = [n for n in names if not hasattr(L, n)]
+    assert not missing, missing
+
+
+def test_option_defaults(lib):
+    o, used = lib.parse_opts([], lib.GB_PROG_RTRACE)
+    assert (o.ab, o.ad, o.lr, o.aa, o.lw, o.dj, o.ds, o.dt, o.st, o.u) == (0, 1024, -10, 0.1, 1e-4, 0.0, 0.2, 0.03,
+                                                                            0.15, 1)
+    o, used = lib.parse_opts([], lib.GB_PROG_RCONTRIB)
+    assert (o.ab, o.ad, o.lw, o.dj, o.dt, o.st, o.c, o.V) == (1, 350, 2e-3, 0.9, 0.0, 0.02, 1, 0)
+
+
+def test_option_parsing(lib):
+    o, used = lib.parse_opts(["-I+", "-ab", "3", "-ad", "1024", "-lw", "1e-4", "-c", "4", "-u-", "-faf",
+                              "-av", "1", "2", "3", "-m", "sky"], lib.GB_PROG_RCONTRIB)
+    assert used == 15 and o.I == 1 and o.ab == 3 and o.ad == 1024 and o.lw == 1e-4 and o.c == 4 and o.u == 0
+    assert (o.fin, o.fout) == (b"a", b"f") and list(o.av) == [1, 2, 3]
+    o, used = lib.parse_opts(["-h", "-ovs", "-I", "-dj", ".5"], lib.GB_PROG_RTRACE)
+    assert o.h == 0 and o.outspec == b"vs" and o.I == 1 and o.dj == 0.5
+    with pytest.raises(lib.GbError):
+        lib.parse_opts(["-qq"], lib.GB_PROG_RTRACE)
+    with pytest.raises(lib.GbError):
+        lib.parse_opts(["-me", "1", "1", "1"], lib.GB_PROG_RTRACE)
+
+
+def nbins(lib, mods):
+    arr = (lib.GbModspec * len(mods))()
+    keep = []
+    for i, m in enumerate(mods):
+        v = {k: (m[k].encode() if m.get(k) else None) for k in ("modifier", "binv", "nbins", "params", "calfile",
+                                                                 "expr")}
+        keep.append(v)
+        arr[i] = lib.GbModspec(v["modifier"], v["binv"], v["nbins"], v["params"], v["calfile"], v["expr"])
+    n = lib.C.c_int(0)
+    lib.check(lib.lib().gb_rcontrib_nbins(arr, len(mods), lib.C.byref(n)))
+    return n.value
+
+
+def test_bin_expressions(lib):
+    assert nbins(lib, [dict(modifier="g")]) == 1
+    assert nbins(lib, [dict(modifier="s", calfile="reinhartb.cal", params="MF=1", binv="rbin",
+                            nbins="Nrbins")]) == 145
+    assert nbins(lib, [dict(modifier="s", calfile="reinhartb.cal", params="MF=2", binv="rbin",
+                            nbins="Nrbins")]) == 577
+    assert nbins(lib, [dict(modifier="s", binv="if(-Dx*0-Dy*0-Dz*-1,0,-1)", nbins="1")]) == 1
+    assert nbins(lib, [dict(modifier="s", expr="b=floor(Dz*10)", binv="b", nbins="10")]) == 10
+    with pytest.raises(lib.GbError):
+        nbins(lib, [dict(modifier="s", binv="sin(Dx)", nbins="4")])
+    with pytest.raises(lib.GbError):
+        nbins(lib, [dict(modifier="s", binv="3")])          # non-zero constant bin
+    with pytest.raises(lib.GbError):
+        nbins(lib, [dict(modifier="s", binv="Dz")])         # no bin count
+
+
+def test_workloads_are_deterministic():
+    from pyradiance_gb300 import workloads as w
+    h = hashlib.sha256(w.window_room(ntri=500).encode()).hexdigest()
+    assert h == hashlib.sha256(w.window_room(ntri=500).encode()).hexdigest()
+    g = w.sensor_grid(64, 64)
+    assert g.shape == (4096, 6) and np.allclose(g[:, 5], 1.0) and np.allclose(g[:, 2], 0.8)
+    dc, sky = w.dc_sky(64, 100, 200)
+    assert dc.dtype == np.float32 and (dc == 0).all(axis=2).mean() > 0.2
+    assert (sky == 0).all(axis=(0, 2)).mean() > 0.3
+
+
+def test_read_rays_formats():
+    import pyradiance_gb300 as gb
+    r = np.arange(12, dtype=np.float64).reshape(2, 6)
+    np.testing.assert_array_equal(gb.read_rays(b"0 1 2 3 4 5\n6 7 8 9 10 11\n", "a"), r)
+    np.testing.assert_array_equal(gb.read_rays(r.astype(np.float32).tobytes(), "f"), r)
+    np.testing.assert_array_equal(gb.read_rays(r.tobytes(), "d"), r)
