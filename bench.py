@@ -220,6 +220,8 @@ def gpu_arm(args):
 
     with tempfile.TemporaryDirectory() as td:
         rad, rays = make_scene(Path(td))
+        if args.sensors:
+            rays = rays[np.linspace(0, len(rays) - 1, args.sensors).astype(int)]
         sc = gb.Scene(rad_files=[rad])
         rc = gb.Rcontrib(b"", sc, params=PARAMS)
         for m in MODS:
@@ -319,6 +321,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--sensors", type=int, default=0,
+                    help="profile a smaller case: this many sensors of the grid (the metric is not reported)")
     args = ap.parse_args()
     if args.impl == "reference":
         reference_arm(args)

@@ -483,9 +483,7 @@ __device__ float3 shadow_chain(const gb_run &P, Ray sr, int s, Counters &cnt, fl
         Hit h;
         uint32_t st[3] = {0, 0, 0};
         cnt.rays++;
-        int okind = sr.origin >= 0 ? (S.obj[sr.origin].x & 0xff) : DK_NONE;
-        bool planar = okind == DK_FACE || okind == DK_RING;
-        bool hit = local_hit(S, sr.org, sr.dir, planar ? sr.origin : -1, D_FTINY, D_FHUGE, h, st);
+        bool hit = local_hit(S, sr.org, sr.dir, sr.origin, D_FTINY, D_FHUGE, h, st);
         cnt.add(st);
         if (!hit) {
             if (guard == 0) {
@@ -697,10 +695,8 @@ __device__ void run_ray(const gb_run &P, Ray r, Counters &cnt)
     for (int guard = 0; guard < 256; guard++) {
         Hit h;
         cnt.rays++;
-        int okind = r.origin >= 0 ? (S.obj[r.origin].x & 0xff) : DK_NONE;
-        bool planar = okind == DK_FACE || okind == DK_RING;
         uint32_t st[3] = {0, 0, 0};
-        bool hit = local_hit(S, r.org, r.dir, planar ? r.origin : -1, D_FTINY, D_FHUGE, h, st);
+        bool hit = local_hit(S, r.org, r.dir, r.origin, D_FTINY, D_FHUGE, h, st);
         cnt.add(st);
         if (!hit) {
             int sidx = source_hit(S, r.dir, r.rsrc, r.crtype);

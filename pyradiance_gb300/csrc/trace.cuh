@@ -311,6 +311,18 @@ __device__ __forceinline__ bool local_hit(const gb_dscene &S, float3 org, float3
     best.rod = 1.f;
     best.n = f3(0.f, 0.f, 0.f);
     const float cs = S.cusize;
+    /* Self-intersection: a ray leaving a planar surface cannot meet it
+     * again, so that surface is skipped.  A curved origin surface is still
+     * tested (its far side is a legitimate hit) but roots closer than a few
+     * FP32 position ulps of the scene (4e-6 of its size, the rounding of the
+     * hit point this ray starts from) are taken as the origin itself, where
+     * the reference's FP64 arithmetic gives a root below 1e-6. */
+    float self_tmin = 0.f;
+    if (skip >= 0) {
+        int k = S.obj[skip].x & 0xff;
+        if (k != DK_FACE && k != DK_RING)
+            self_tmin = fmaxf(tmin, 4e-6f * cs);
+    }
     float3 rel = org - f3(S.cuorg[0], S.cuorg[1], S.cuorg[2]);
     int sg[3];
     float dd[3] = {dir.x, dir.y, dir.z}, rr[3] = {rel.x, rel.y, rel.z}, inv[3];
@@ -382,6 +394,8 @@ __device__ __forceinline__ bool local_hit(const gb_dscene &S, float3 org, float3
                 int o = __ldg(set + k);
                 if (o != skip)
                     hit_object(S, o, org, dir, best, tmin);
+                else if (self_tmin > 0.f)      /* curved origin surface */
+                    hit_object(S, o, org, dir, best, self_tmin);
             }
             if (best.obj >= 0 && best.t <= texit)
                 break;                          /* hit inside this cube */
