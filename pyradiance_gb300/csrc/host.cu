@@ -88,6 +88,13 @@ struct gb_scene {
     std::vector<gb_dsrc> src;
     std::string src_error;             /* non-empty if a source is unsupported */
     std::vector<std::string> modname, matname;
+    /* host arrays of the device scene */
+    std::vector<int> hkids, hsetoff, hsetdata;
+    std::vector<int4> hobj;
+    std::vector<float4> hgeo;
+    std::vector<float2> hfvert;
+    std::vector<float> hcone;
+    std::vector<gb_dsrc> hsrc;
     /* device scene */
     DevBuf kids, setoff, setdata, obj, geo, fvert, cone, matd, srcd, trk;
     gb_dscene ds;
@@ -316,11 +323,14 @@ static int upload(DevBuf &b, const std::vector<T> &v)
     return 0;
 }
 
+static int build_arrays(gb_scene *G);
+
 static int prepare_device(gb_scene *G)
 {
+    int rc = build_arrays(G);
+    if (rc < 0)
+        return rc;
     gb_scene_host &H = G->H;
-    if (gb_scene_prepare(&H) < 0)
-        return set_err(GB_EIO, "%s", gb_scene_error());
     int dev = 0;
     CK(cudaGetDevice(&dev));
     CK(cudaDeviceGetAttribute(&G->sms, cudaDevAttrMultiProcessorCount, dev));
@@ -330,6 +340,31 @@ static int prepare_device(gb_scene *G)
     cudaDeviceGetLimit(&stack, cudaLimitStackSize);
     if (stack < 16384)
         CK(cudaDeviceSetLimit(cudaLimitStackSize, 16384));
+    if (upload(G->kids, G->hkids) < 0 || upload(G->setoff, G->hsetoff) < 0 || upload(G->setdata, G->hsetdata) < 0 ||
+        upload(G->obj, G->hobj) < 0 || upload(G->geo, G->hgeo) < 0 || upload(G->fvert, G->hfvert) < 0 ||
+        upload(G->cone, G->hcone) < 0 || upload(G->matd, G->mat) < 0 || upload(G->srcd, G->hsrc) < 0)
+        return set_err(GB_ENOMEM, "device upload of the scene failed");
+    gb_dscene &d = G->ds;
+    d.kids = (const int *)G->kids.p;
+    d.set_off = (const int *)G->setoff.p;
+    d.set_data = (const int *)G->setdata.p;
+    d.obj = (const int4 *)G->obj.p;
+    d.geo = (const float4 *)G->geo.p;
+    d.fvert = (const float2 *)G->fvert.p;
+    d.cone = (const float *)G->cone.p;
+    d.mat = (const float4 *)G->matd.p;
+    d.src = (const gb_dsrc *)G->srcd.p;
+    (void)H;
+    return GB_OK;
+}
+
+/* Host-side arrays of the device scene (and the gb_dscene header with
+ * host pointers); no CUDA calls. */
+static int build_arrays(gb_scene *G)
+{
+    gb_scene_host &H = G->H;
+    if (gb_scene_prepare(&H) < 0)
+        return set_err(GB_EIO, "%s", gb_scene_error());
     /* materials */
     G->matslot.assign(H.nobjs, -1);
     std::vector<int> slot_of_mat(H.nobjs, -1);
@@ -453,10 +488,14 @@ static int prepare_device(gb_scene *G)
     if (setdata.empty()) setdata.push_back(0);
     std::vector<gb_dsrc> src = G->src;
     if (src.empty()) src.resize(1);
-    if (upload(G->kids, kids) < 0 || upload(G->setoff, setoff) < 0 || upload(G->setdata, setdata) < 0 ||
-        upload(G->obj, obj) < 0 || upload(G->geo, geo) < 0 || upload(G->fvert, fvert) < 0 ||
-        upload(G->cone, cone) < 0 || upload(G->matd, G->mat) < 0 || upload(G->srcd, src) < 0)
-        return set_err(GB_ENOMEM, "device upload of the scene failed");
+    G->hkids.swap(kids);
+    G->hsetoff.swap(setoff);
+    G->hsetdata.swap(setdata);
+    G->hobj.swap(obj);
+    G->hgeo.swap(geo);
+    G->hfvert.swap(fvert);
+    G->hcone.swap(cone);
+    G->hsrc.swap(src);
     gb_dscene &d = G->ds;
     memset(&d, 0, sizeof d);
     for (int j = 0; j < 3; j++) d.cuorg[j] = (float)H.cuorg[j];
@@ -465,17 +504,17 @@ static int prepare_device(gb_scene *G)
     d.cell = (float)(H.cusize / (double)(1 << GRID_BITS_HOST));
     d.root = H.root;
     d.nnodes = H.nnodes;
-    d.kids = (const int *)G->kids.p;
-    d.set_off = (const int *)G->setoff.p;
-    d.set_data = (const int *)G->setdata.p;
+    d.kids = G->hkids.data();
+    d.set_off = G->hsetoff.data();
+    d.set_data = G->hsetdata.data();
     d.nobjs = H.nobjs;
-    d.obj = (const int4 *)G->obj.p;
-    d.geo = (const float4 *)G->geo.p;
-    d.fvert = (const float2 *)G->fvert.p;
-    d.cone = (const float *)G->cone.p;
-    d.mat = (const float4 *)G->matd.p;
+    d.obj = G->hobj.data();
+    d.geo = G->hgeo.data();
+    d.fvert = G->hfvert.data();
+    d.cone = G->hcone.data();
+    d.mat = G->mat.data();
     d.nsrc = (int)G->src.size();
-    d.src = (const gb_dsrc *)G->srcd.p;
+    d.src = G->hsrc.data();
     /* names for output */
     G->modname.resize(H.nobjs);
     G->matname.resize(H.nobjs);
@@ -688,7 +727,7 @@ extern "C" int gb_opts_parse(int argc, const char *const *argv, int prog, gb_opt
             }
             ok = false;
             break;
-        case 'e': case 'p': case 'b' + 256: case 'M':
+        case 'e': case 'p': case 'M':
             ok = false;
             break;
         case 't': NEED(1); i++; break;            /* report interval */
@@ -909,8 +948,9 @@ static int run(gb_scene *G, const gb_opts *o, int follow, const double *org_dir,
     if (G->qa.ensure((size_t)qcap * sizeof(gb_qray)) < 0 || G->qb.ensure((size_t)qcap * sizeof(gb_qray)) < 0)
         return set_err(GB_ENOMEM, "cannot allocate %lld-ray work queues", qcap);
     P.qcap = qcap;
-    unsigned long long *cnt = (unsigned long long *)G->qcount.p;   /* [0] A, [1] B */
-    CK(cudaMemsetAsync(cnt, 0, 2 * sizeof(unsigned long long), st));
+    unsigned long long *cnt = (unsigned long long *)G->qcount.p;   /* [0] A, [1] B, [2] work items */
+    CK(cudaMemsetAsync(cnt, 0, 3 * sizeof(unsigned long long), st));
+    P.work = cnt + 2;
     gb_qray *qa = (gb_qray *)G->qa.p, *qb = (gb_qray *)G->qb.p;
 
     if (o->I) {
@@ -929,6 +969,7 @@ static int run(gb_scene *G, const gb_opts *o, int follow, const double *org_dir,
         if (n0 > 0) {
             P.qout = qa;
             P.qout_count = cnt;
+            CK(cudaMemsetAsync(P.work, 0, sizeof(unsigned long long), st));
             rc = launch(GB_K_GENROOT, P, [&](gb_run &R) { return gb_launch_gen_root(&R, st, G->sms); });
             if (rc < 0)
                 return rc;
@@ -956,6 +997,7 @@ static int run(gb_scene *G, const gb_opts *o, int follow, const double *org_dir,
         P.qout = in ? qa : qb;
         P.qout_count = cnt + (1 - in);
         CK(cudaMemsetAsync(cnt + (1 - in), 0, sizeof(unsigned long long), st));
+        CK(cudaMemsetAsync(P.work, 0, sizeof(unsigned long long), st));
         int rc = launch(GB_K_GEN, P, [&](gb_run &R) { return gb_launch_gen(&R, st, G->sms); });
         if (rc < 0)
             return rc;

@@ -689,10 +689,13 @@ __device__ __forceinline__ void setup_surf(const gb_run &P, int mk, float4 m0, f
 /* Trace ray r and its single-child continuations; other children go to the
  * next generation.  `hemi_push` decides whether hemispheres are expanded
  * here (deferred generations) or written out. */
-__device__ void run_ray(const gb_run &P, Ray r, Counters &cnt)
+/* Trace ray r once and shade its hit.  Children beyond the first go to the
+ * next generation's queue; the first replaces r and true is returned, or
+ * false when the path ends here. */
+__device__ bool step_ray(const gb_run &P, Ray &r, Counters &cnt)
 {
     const gb_dscene &S = P.S;
-    for (int guard = 0; guard < 256; guard++) {
+    {
         Hit h;
         cnt.rays++;
         uint32_t st[3] = {0, 0, 0};
@@ -700,17 +703,16 @@ __device__ void run_ray(const gb_run &P, Ray r, Counters &cnt)
         cnt.add(st);
         if (!hit) {
             int sidx = source_hit(S, r.dir, r.rsrc, r.crtype);
-            if (sidx < 0)
-                return;
-            light_hit(P, r, S.src[sidx].so, S.src[sidx].mat, D_FHUGE, 1.f, cnt, nullptr);
-            return;
+            if (sidx >= 0)
+                light_hit(P, r, S.src[sidx].so, S.src[sidx].mat, D_FHUGE, 1.f, cnt, nullptr);
+            return false;
         }
         int ms = S.obj[h.obj].y;
         int mk = ms >= 0 ? (int)S.mat[2 * ms].x : DM_NONE;
         float3 hp = r.org + r.dir * h.t;
         if (mk == DM_LIGHT || mk == DM_GLOW) {
             light_hit(P, r, h.obj, ms, h.t, h.rod, cnt, nullptr);
-            return;
+            return false;
         }
         if (mk == DM_NONE) {
             surface_contrib(P, r, h.obj, cnt);
@@ -720,7 +722,7 @@ __device__ void run_ray(const gb_run &P, Ray r, Counters &cnt)
             c.dir = r.dir;
             c.origin = h.obj;
             r = c;
-            continue;
+            return true;
         }
         Ray kids[MAXKIDS];
         int nk = 0;
@@ -813,11 +815,65 @@ __device__ void run_ray(const gb_run &P, Ray r, Counters &cnt)
             }
         }
         if (nk == 0)
-            return;
+            return false;
         for (int k = 1; k < nk; k++)
             push_ray(P, kids[k]);
         r = kids[0];
+        return true;
     }
+}
+
+#define MAX_CHAIN 256   /* rays one path may continue through in one thread */
+
+/* Persistent work loop: every lane without a ray fetches the next work item
+ * (one atomic per warp), so lanes whose paths end early are refilled at
+ * once instead of idling until the longest path of the warp ends.
+ * make(i, r) turns work item i into a ray (false if it dies at birth). */
+template <typename Make>
+__device__ __forceinline__ void persistent_loop(const gb_run &P, unsigned long long *work,
+                                                unsigned long long total, Counters &cnt, Make make)
+{
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    Ray r;
+    bool active = false, exhausted = false;
+    int chain = 0;
+    for (;;) {
+        unsigned need = __ballot_sync(FULL, !active);
+        if (need && !exhausted) {
+            unsigned long long base = 0;
+            int leader = __ffs(need) - 1;
+            if (lane == leader)
+                base = atomicAdd(work, (unsigned long long)__popc(need));
+            base = __shfl_sync(FULL, base, leader);
+            if (base >= total)
+                exhausted = true;
+            if (!active) {
+                unsigned long long i = base + __popc(need & ((1u << lane) - 1u));
+                if (i < total) {
+                    active = make(i, r);
+                    chain = 0;
+                }
+            }
+        }
+        if (!__any_sync(FULL, active)) {
+            if (exhausted)
+                break;
+            continue;
+        }
+        if (active) {
+            active = step_ray(P, r, cnt);
+            if (++chain >= MAX_CHAIN)
+                active = false;
+        }
+    }
+}
+
+__device__ void run_ray(const gb_run &P, Ray r, Counters &cnt)
+{
+    for (int guard = 0; guard < MAX_CHAIN; guard++)
+        if (!step_ray(P, r, cnt))
+            return;
 }
 
 /* -------------------------------------------------------------- kernels */
@@ -881,11 +937,10 @@ __global__ void __launch_bounds__(256) k_gen_root(gb_run P)
 {
     Counters cnt = {0, 0, 0, 0, 0};
     const long long nn = (long long)P.root_n * P.root_n;
-    const long long total = nn * P.nsensors;
-    for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < total;
-         g += (long long)gridDim.x * blockDim.x) {
-        long long s = g / nn;
-        int k = (int)(g - s * nn);
+    const unsigned long long total = (unsigned long long)(nn * P.nsensors);
+    persistent_loop(P, P.work, total, cnt, [&](unsigned long long g, Ray &c) -> bool {
+        long long s = (long long)(g / (unsigned long long)nn);
+        int k = (int)(g - (unsigned long long)s * nn);
         const gb_rootrec *rr = P.roots + s;
         Ray parent;
         parent.org = f3(rr->hp[0], rr->hp[1], rr->hp[2]);
@@ -907,19 +962,16 @@ __global__ void __launch_bounds__(256) k_gen_root(gb_run P)
         hm.uy = cross3(hm.onrm, hm.ux);
         float a = D_PI / (float)(hm.n * hm.n);
         hm.acoef = f3(a, a, a);
-        Ray c;
         const float *sp = nullptr;
         float2 pk;
         if (hm.n >= 4) {
             pk = P.root_spt[g];
             if (pk.x > 1.5f)
-                continue;                     /* stratum died in Russian roulette */
+                return false;                 /* stratum died in Russian roulette */
             sp = &pk.x;
         }
-        if (!hemi_child(P, parent, hm, parent.org, -1, k, sp, c))
-            continue;
-        run_ray(P, c, cnt);
-    }
+        return hemi_child(P, parent, hm, parent.org, -1, k, sp, c);
+    });
     flush_counters(P, cnt);
 }
 
@@ -954,11 +1006,10 @@ __global__ void __launch_bounds__(256) k_gen(gb_run P)
     unsigned long long n = *P.qin_count;
     if (n > (unsigned long long)P.qcap)
         n = P.qcap;
-    for (unsigned long long g = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; g < n;
-         g += (unsigned long long)gridDim.x * blockDim.x) {
-        Ray r = load_ray(P.qin + g);
-        run_ray(P, r, cnt);
-    }
+    persistent_loop(P, P.work, n, cnt, [&](unsigned long long g, Ray &r) -> bool {
+        r = load_ray(P.qin + g);
+        return true;
+    });
     flush_counters(P, cnt);
 }
 
@@ -1021,10 +1072,22 @@ int gb_launch_root(const gb_run *P, cudaStream_t st, int sms)
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
+/* persistent kernels: exactly the blocks that fit at once */
+template <typename K>
+static int resident_grid(K kernel, int block, int sms)
+{
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, block, 0) != cudaSuccess || per_sm < 1)
+        per_sm = 1;
+    return per_sm * sms;
+}
+
 int gb_launch_gen_root(const gb_run *P, cudaStream_t st, int sms)
 {
-    long long total = (long long)P->root_n * P->root_n * P->nsensors;
-    k_gen_root<<<grid_for(total, 256, sms), 256, 0, st>>>(*P);
+    static int grid = 0;
+    if (!grid)
+        grid = resident_grid(k_gen_root, 256, sms);
+    k_gen_root<<<grid, 256, 0, st>>>(*P);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
@@ -1036,6 +1099,9 @@ int gb_launch_primary(const gb_run *P, cudaStream_t st, int sms)
 
 int gb_launch_gen(const gb_run *P, cudaStream_t st, int sms)
 {
-    k_gen<<<sms * 8, 256, 0, st>>>(*P);
+    static int grid = 0;
+    if (!grid)
+        grid = resident_grid(k_gen, 256, sms);
+    k_gen<<<grid, 256, 0, st>>>(*P);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }

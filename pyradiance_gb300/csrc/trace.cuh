@@ -11,6 +11,19 @@
 #include "devscene.h"
 #include "gbcommon.h"
 
+/* The traversal and intersection code is written once for the device; it
+ * also compiles for the host so that it can be exercised without a GPU. */
+#define GB_DFN __host__ __device__ __forceinline__
+#ifdef __CUDA_ARCH__
+#define GB_LDG(p) __ldg(p)
+#define GB_F2I_RD(x) __float2int_rd(x)
+#define GB_CLZ(x) __clz(x)
+#else
+#define GB_LDG(p) (*(p))
+#define GB_F2I_RD(x) ((int)floorf(x))
+#define GB_CLZ(x) __builtin_clz(x)
+#endif
+
 #define D_FTINY 1e-6f
 #define D_FHUGE 1e10f
 #define D_PI 3.14159265358979323846f
@@ -25,20 +38,20 @@ struct Hit {
     float3 n;       /* unflipped surface normal */
 };
 
-__device__ __forceinline__ float3 f3(float x, float y, float z) { return make_float3(x, y, z); }
-__device__ __forceinline__ float3 operator+(float3 a, float3 b) { return f3(a.x + b.x, a.y + b.y, a.z + b.z); }
-__device__ __forceinline__ float3 operator-(float3 a, float3 b) { return f3(a.x - b.x, a.y - b.y, a.z - b.z); }
-__device__ __forceinline__ float3 operator*(float3 a, float s) { return f3(a.x * s, a.y * s, a.z * s); }
-__device__ __forceinline__ float3 operator*(float3 a, float3 b) { return f3(a.x * b.x, a.y * b.y, a.z * b.z); }
-__device__ __forceinline__ float3 operator-(float3 a) { return f3(-a.x, -a.y, -a.z); }
-__device__ __forceinline__ float dot3(float3 a, float3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
-__device__ __forceinline__ float3 cross3(float3 a, float3 b)
+GB_DFN float3 f3(float x, float y, float z) { return make_float3(x, y, z); }
+GB_DFN float3 operator+(float3 a, float3 b) { return f3(a.x + b.x, a.y + b.y, a.z + b.z); }
+GB_DFN float3 operator-(float3 a, float3 b) { return f3(a.x - b.x, a.y - b.y, a.z - b.z); }
+GB_DFN float3 operator*(float3 a, float s) { return f3(a.x * s, a.y * s, a.z * s); }
+GB_DFN float3 operator*(float3 a, float3 b) { return f3(a.x * b.x, a.y * b.y, a.z * b.z); }
+GB_DFN float3 operator-(float3 a) { return f3(-a.x, -a.y, -a.z); }
+GB_DFN float dot3(float3 a, float3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+GB_DFN float3 cross3(float3 a, float3 b)
 {
     return f3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
 }
-__device__ __forceinline__ float comp(float3 v, int i) { return i == 0 ? v.x : (i == 1 ? v.y : v.z); }
-__device__ __forceinline__ float maxc(float3 v) { return fmaxf(v.x, fmaxf(v.y, v.z)); }
-__device__ __forceinline__ float3 normalize3(float3 v)
+GB_DFN float comp(float3 v, int i) { return i == 0 ? v.x : (i == 1 ? v.y : v.z); }
+GB_DFN float maxc(float3 v) { return fmaxf(v.x, fmaxf(v.y, v.z)); }
+GB_DFN float3 normalize3(float3 v)
 {
     float l = sqrtf(dot3(v, v));
     return l > 0.f ? v * (1.f / l) : v;
@@ -48,7 +61,7 @@ __device__ __forceinline__ float3 normalize3(float3 v)
  * Hit arbitration: rt/raytrace.c:536-575 (rayreject).  Returns true when the
  * candidate (obj, t, rod) is worse than the current best.
  */
-__device__ __forceinline__ bool ray_reject(const gb_dscene &S, int obj, float t, float rod,
+GB_DFN bool ray_reject(const gb_dscene &S, int obj, float t, float rod,
                                            const Hit &best, float tmin)
 {
     if ((t <= tmin) | (t > best.t + D_FTINY))
@@ -81,7 +94,7 @@ __device__ __forceinline__ bool ray_reject(const gb_dscene &S, int obj, float t,
 }
 
 /* point in polygon on the dominant projection: common/face.c:121-161 */
-__device__ __forceinline__ bool in_face(const float2 *__restrict__ v, int nv, float x, float y)
+GB_DFN bool in_face(const float2 *__restrict__ v, int nv, float x, float y)
 {
     int ncross = 0;
     float2 p0 = v[nv - 1];
@@ -108,7 +121,7 @@ __device__ __forceinline__ bool in_face(const float2 *__restrict__ v, int nv, fl
 }
 
 /* rt/o_face.c:15-62 */
-__device__ __forceinline__ void hit_face(const gb_dscene &S, int obj, int4 od, float3 org, float3 dir,
+GB_DFN void hit_face(const gb_dscene &S, int obj, int4 od, float3 org, float3 dir,
                                          Hit &best, float tmin)
 {
     float4 pl = S.geo[obj];
@@ -132,7 +145,7 @@ __device__ __forceinline__ void hit_face(const gb_dscene &S, int obj, int4 od, f
 }
 
 /* common/zeroes.c:19-53 */
-__device__ __forceinline__ int quadratic(float r[2], float a, float b, float c)
+GB_DFN int quadratic(float r[2], float a, float b, float c)
 {
     int first;
     if (a < -D_FTINY)
@@ -159,7 +172,7 @@ __device__ __forceinline__ int quadratic(float r[2], float a, float b, float c)
 }
 
 /* rt/sphere.c:15-83 */
-__device__ __forceinline__ void hit_sphere(const gb_dscene &S, int obj, bool bubble, float3 org,
+GB_DFN void hit_sphere(const gb_dscene &S, int obj, bool bubble, float3 org,
                                            float3 dir, Hit &best, float tmin)
 {
     float4 sp = S.geo[obj];
@@ -186,7 +199,7 @@ __device__ __forceinline__ void hit_sphere(const gb_dscene &S, int obj, bool bub
 
 /* rt/o_cone.c:16-146; cone record: tm (12: 3x3 rows then translation),
  * ad (3), p0 (3), al, sl, r0, r1 */
-__device__ __forceinline__ void hit_cone(const gb_dscene &S, int obj, int kind, int ci, float3 org,
+GB_DFN void hit_cone(const gb_dscene &S, int obj, int kind, int ci, float3 org,
                                          float3 dir, Hit &best, float tmin)
 {
     const float *c = S.cone + 24 * ci;
@@ -267,7 +280,7 @@ __device__ __forceinline__ void hit_cone(const gb_dscene &S, int obj, int kind, 
     }
 }
 
-__device__ __forceinline__ void hit_object(const gb_dscene &S, int obj, float3 org, float3 dir, Hit &best,
+GB_DFN void hit_object(const gb_dscene &S, int obj, float3 org, float3 dir, Hit &best,
                                            float tmin)
 {
     int4 od = S.obj[obj];
@@ -303,7 +316,7 @@ __device__ __forceinline__ void hit_object(const gb_dscene &S, int obj, float3 o
  * and a hit recorded earlier but never confirmed is still returned when the
  * ray leaves the scene, as localhit does.
  */
-__device__ __forceinline__ bool local_hit(const gb_dscene &S, float3 org, float3 dir, int skip,
+GB_DFN bool local_hit(const gb_dscene &S, float3 org, float3 dir, int skip,
                                           float tmin, float tmax, Hit &best, uint32_t *tally)
 {
     best.obj = -1;
@@ -357,25 +370,70 @@ __device__ __forceinline__ bool local_hit(const gb_dscene &S, float3 org, float3
     const float gs = S.grid_scale, cell = S.cell;
     int q[3];
     for (int i = 0; i < 3; i++) {
-        int v = __float2int_rd((rr[i] + dd[i] * t) * gs);
+        int v = GB_F2I_RD((rr[i] + dd[i] * t) * gs);
         q[i] = min(max(v, 0), GRID_N - 1);
     }
     uint32_t steps = 0, nodes = 0, tests = 0;
+    /* One flat loop whose iterations either test one object of the current
+     * leaf or move to the next leaf, so that the lanes of a warp stay in step
+     * whatever the set sizes of the leaves they cross.  stk[l] is the node
+     * chosen at level l on the way to the current leaf; a step to the
+     * neighbouring cube restarts the descent at the deepest level the two
+     * cubes share (from the highest coordinate bit that changed). */
+    int stk[GRID_BITS + 1];
+    stk[0] = S.root;
+    int rl = 0, k = 1, cnt = 0, span = 0, ax = 0;
+    int lo[3] = {0, 0, 0};
+    const int *set = nullptr;
+    float texit = 0.f;
+    bool leaf = false;
     for (;;) {
-        /* descend to the leaf containing q */
-        int node = S.root, level = 0;
+        if (k <= cnt) {                          /* next object of this leaf */
+            int o = GB_LDG(set + k);
+            k++;
+            if (o != skip)
+                hit_object(S, o, org, dir, best, tmin);
+            else if (self_tmin > 0.f)           /* curved origin surface */
+                hit_object(S, o, org, dir, best, self_tmin);
+            continue;
+        }
+        if (leaf) {
+            if (best.obj >= 0 && best.t <= texit)
+                break;                          /* hit inside this cube */
+            steps++;
+            if (texit >= tmax || steps >= MAX_CUBE_STEPS)
+                break;
+            /* step to the face neighbour along the exit axis; the exit point
+             * lies on that face, so the other coordinates stay inside this
+             * cube's slab (an edge or corner exit takes a second, zero-length
+             * step) */
+            int oq0 = q[0], oq1 = q[1], oq2 = q[2];
+            for (int i = 0; i < 3; i++) {
+                if (i == ax)
+                    continue;
+                int v = GB_F2I_RD((rr[i] + dd[i] * texit) * gs);
+                q[i] = min(max(v, lo[i]), lo[i] + span - 1);
+            }
+            q[ax] = sg[ax] > 0 ? lo[ax] + span : lo[ax] - 1;
+            if (q[ax] < 0 || q[ax] >= GRID_N)
+                break;                          /* left the scene */
+            unsigned diff = (unsigned)((oq0 ^ q[0]) | (oq1 ^ q[1]) | (oq2 ^ q[2]));
+            rl = GRID_BITS - 1 - (31 - GB_CLZ(diff));
+        }
+        /* descend from the shared ancestor to the leaf containing q */
+        int node = stk[rl], level = rl;
         while (node >= 0) {
             int sh = GRID_BITS - 1 - level;
             int br = ((q[0] >> sh) & 1) | (((q[1] >> sh) & 1) << 1) | (((q[2] >> sh) & 1) << 2);
-            node = __ldg(S.kids + 8 * node + br);
-            level++;
+            node = GB_LDG(S.kids + 8 * node + br);
+            stk[++level] = node;
+            nodes++;
         }
-        nodes += level;
-        int span = 1 << (GRID_BITS - level);
-        int lo[3] = {q[0] & ~(span - 1), q[1] & ~(span - 1), q[2] & ~(span - 1)};
-        /* exit distance of this cube */
-        float texit = D_FHUGE;
-        int ax = 0;
+        span = 1 << (GRID_BITS - level);
+        lo[0] = q[0] & ~(span - 1);
+        lo[1] = q[1] & ~(span - 1);
+        lo[2] = q[2] & ~(span - 1);
+        texit = D_FHUGE;                         /* exit distance of this cube */
         for (int i = 0; i < 3; i++) {
             if (!sg[i])
                 continue;
@@ -386,35 +444,14 @@ __device__ __forceinline__ bool local_hit(const gb_dscene &S, float3 org, float3
                 ax = i;
             }
         }
-        if (node <= -2) {                       /* full leaf: test its set */
-            const int *set = S.set_data + __ldg(S.set_off + (-node - 2));
-            int cnt = __ldg(set);
+        leaf = true;
+        k = 1;
+        cnt = 0;
+        if (node <= -2) {                       /* full leaf: its set to test */
+            set = S.set_data + GB_LDG(S.set_off + (-node - 2));
+            cnt = GB_LDG(set);
             tests += cnt;
-            for (int k = 1; k <= cnt; k++) {
-                int o = __ldg(set + k);
-                if (o != skip)
-                    hit_object(S, o, org, dir, best, tmin);
-                else if (self_tmin > 0.f)      /* curved origin surface */
-                    hit_object(S, o, org, dir, best, self_tmin);
-            }
-            if (best.obj >= 0 && best.t <= texit)
-                break;                          /* hit inside this cube */
         }
-        steps++;
-        if (texit >= tmax || steps >= MAX_CUBE_STEPS)
-            break;
-        /* step to the face neighbour along the exit axis; the exit point lies
-         * on that face, so the other coordinates stay inside this cube's
-         * slab (an edge or corner exit takes a second, zero-length step) */
-        for (int i = 0; i < 3; i++) {
-            if (i == ax)
-                continue;
-            int v = __float2int_rd((rr[i] + dd[i] * texit) * gs);
-            q[i] = min(max(v, lo[i]), lo[i] + span - 1);
-        }
-        q[ax] = sg[ax] > 0 ? lo[ax] + span : lo[ax] - 1;
-        if (q[ax] < 0 || q[ax] >= GRID_N)
-            break;                              /* left the scene */
     }
     if (tally) {
         tally[0] += steps + 1;
@@ -428,7 +465,7 @@ __device__ __forceinline__ bool local_hit(const gb_dscene &S, float3 org, float3
  * Distant source test for rays that leave the scene: rt/source.c:317-377.
  * Returns the source index or -1.
  */
-__device__ __forceinline__ int source_hit(const gb_dscene &S, float3 dir, int rsrc, uint32_t crtype)
+GB_DFN int source_hit(const gb_dscene &S, float3 dir, int rsrc, uint32_t crtype)
 {
     int glowsrc = -1;
     int first = 0, last = S.nsrc - 1;
@@ -457,7 +494,7 @@ __device__ __forceinline__ int source_hit(const gb_dscene &S, float3 dir, int rs
  * Bin programs (rcontrib -b expressions; Reinhart bins as in
  * src/radiance/util/reinhartb.cal:17-47).
  */
-__device__ __forceinline__ float reinhart_bin(float Dx, float Dy, float Dz, const gb_binins *p)
+GB_DFN float reinhart_bin(float Dx, float Dy, float Dz, const gb_binins *p)
 {
     float MF = p[0].op, RHS = p[0].a, rNx = p[0].b, rNy = p[0].c;
     float rNz = p[1].op, Ux = p[1].a, Uy = p[1].b, Uz = p[1].c;
@@ -495,7 +532,7 @@ __device__ __forceinline__ float reinhart_bin(float Dx, float Dy, float Dz, cons
     return acc + azn;
 }
 
-__device__ __forceinline__ float eval_bin(const gb_binins *prog, float3 d)
+GB_DFN float eval_bin(const gb_binins *prog, float3 d)
 {
     float st[16];
     int sp = 0;

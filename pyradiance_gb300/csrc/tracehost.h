@@ -72,6 +72,7 @@ typedef struct {
     gb_qray *qout;
     unsigned long long *qout_count;
     long long qcap;
+    unsigned long long *work;  /* work-item counter of the persistent kernels (zeroed per launch) */
 } gb_run;
 
 int gb_launch_cast(const gb_run *P, int *hit_obj, float *hit_t, float *hit_pn, cudaStream_t st, int sms);
