@@ -144,53 +144,87 @@ GB_DFN void hit_face(const gb_dscene &S, int obj, int4 od, float3 org, float3 di
     best.n = n;
 }
 
-/* common/zeroes.c:19-53 */
-GB_DFN int quadratic(float r[2], float a, float b, float c)
+/* Roots of a*tau^2 + 2*bh*tau + c in ascending order, with the degenerate
+ * cases of common/zeroes.c:19-53 (|a| <= FTINY: linear; a discriminant
+ * within FTINY^2 of zero: one root).  The root of smaller magnitude is
+ * formed as c/q so that it carries no cancellation (the stable form of
+ * Numerical Recipes, section 5.6). */
+GB_DFN int quadratic_half(float r[2], float a, float bh, float c)
 {
-    int first;
-    if (a < -D_FTINY)
-        first = 1;
-    else if (a > D_FTINY)
-        first = 0;
-    else if (fabsf(b) > D_FTINY) {
-        r[0] = -c / b;
-        return 1;
-    } else
+    if ((a <= D_FTINY) & (a >= -D_FTINY)) {
+        if (fabsf(bh) > 0.5f * D_FTINY) {
+            r[0] = -c / (2.f * bh);
+            return 1;
+        }
         return 0;
-    b *= 0.5f;
-    float disc = b * b - a * c;
+    }
+    float disc = bh * bh - a * c;
     if (disc < -D_FTINY * D_FTINY)
         return 0;
     if (disc <= D_FTINY * D_FTINY) {
-        r[0] = -b / a;
+        r[0] = -bh / a;
         return 1;
     }
-    disc = sqrtf(disc);
-    r[first] = (-b - disc) / a;
-    r[1 - first] = (-b + disc) / a;
+    float q = -(bh + copysignf(sqrtf(disc), bh));
+    float x0 = q / a, x1 = c / q;
+    r[0] = fminf(x0, x1);
+    r[1] = fmaxf(x0, x1);
     return 2;
+}
+
+/* Quadrics in FP32 from a far ray origin.  The reference solves its
+ * quadratics in FP64 from the ray origin; in FP32 the constant term
+ * |org - centre|^2 - r^2 of a small object seen from a few metres loses
+ * most of its digits, and so do the discriminant and the near root.  The
+ * ray parameter is therefore split as t = ts + tau, ts the point of closest
+ * approach to the centre (sphere) or axis (cone family), and the quadratic
+ * is solved in tau with coefficients formed from the closest-approach
+ * vector (the method of Haines, Guenther and Akenine-Moeller, "Precision
+ * Improvements for Ray/Sphere Intersection", Ray Tracing Gems, 2019,
+ * extended to the axial radius of a cone).  The roots are the reference's;
+ * only their rounding differs, to a few ulps of the hit position.
+ *
+ * `self` marks the surface the ray leaves.  One root of its quadratic is
+ * the ray origin; in FP64 the reference finds it below FTINY and passes
+ * over it.  In FP32 the rounding of the origin, divided by the sine of the
+ * angle at which the ray leaves, can put that root well above FTINY for a
+ * grazing departure, so it is identified instead: of the two roots, the
+ * one nearer zero is the origin and only the other is a candidate.  The
+ * first index a test may take is returned. */
+GB_DFN int first_root(const float *t, int nr, bool self)
+{
+    if (!self)
+        return 0;
+    if (nr < 2)
+        return 2;                       /* the only root is the origin */
+    return fabsf(t[0]) <= fabsf(t[1]) ? 1 : 2;   /* else the far root is behind */
 }
 
 /* rt/sphere.c:15-83 */
 GB_DFN void hit_sphere(const gb_dscene &S, int obj, bool bubble, float3 org,
-                                           float3 dir, Hit &best, float tmin)
+                                           float3 dir, Hit &best, float tmin, bool self)
 {
     float4 sp = S.geo[obj];
-    float3 d = org - f3(sp.x, sp.y, sp.z);
-    float a = dot3(dir, dir), b = 2.f * dot3(dir, d), c = dot3(d, d) - sp.w * sp.w;
-    float root[2];
-    int nr = quadratic(root, a, b, c), i;
-    float t = 0.f;
-    for (i = 0; i < nr; i++)
-        if ((t = root[i]) > D_FTINY)
+    float3 f = org - f3(sp.x, sp.y, sp.z);
+    float a = dot3(dir, dir);
+    float ts = -dot3(f, dir) / a;
+    float3 ws = f + dir * ts;           /* centre to closest approach */
+    float root[2], tr[2];
+    int nr = quadratic_half(root, a, dot3(ws, dir), dot3(ws, ws) - sp.w * sp.w), i;
+    tr[0] = ts + root[0];
+    tr[1] = ts + root[1];
+    float t = 0.f, tau = 0.f;
+    for (i = first_root(tr, nr, self); i < nr; i++) {
+        tau = root[i];
+        if ((t = tr[i]) > tmin)
             break;
+    }
     if (i >= nr)
         return;
     if (ray_reject(S, obj, t, (float)(1 - 2 * ((i > 0) ^ bubble)), best, tmin))
         return;
     float rad = bubble ? -sp.w : sp.w;
-    float3 p = org + dir * t;
-    float3 n = (p - f3(sp.x, sp.y, sp.z)) * (1.f / rad);
+    float3 n = (ws + dir * tau) * (1.f / rad);
     best.obj = obj;
     best.t = t;
     best.n = n;
@@ -200,20 +234,20 @@ GB_DFN void hit_sphere(const gb_dscene &S, int obj, bool bubble, float3 org,
 /* rt/o_cone.c:16-146; cone record: tm (12: 3x3 rows then translation),
  * ad (3), p0 (3), al, sl, r0, r1 */
 GB_DFN void hit_cone(const gb_dscene &S, int obj, int kind, int ci, float3 org,
-                                         float3 dir, Hit &best, float tmin)
+                                         float3 dir, Hit &best, float tmin, bool self)
 {
     const float *c = S.cone + 24 * ci;
-    float3 rox = f3(org.x * c[0] + org.y * c[3] + org.z * c[6] + c[9],
-                    org.x * c[1] + org.y * c[4] + org.z * c[7] + c[10],
-                    org.x * c[2] + org.y * c[5] + org.z * c[8] + c[11]);
-    float3 rdx = f3(dir.x * c[0] + dir.y * c[3] + dir.z * c[6],
-                    dir.x * c[1] + dir.y * c[4] + dir.z * c[7],
-                    dir.x * c[2] + dir.y * c[5] + dir.z * c[8]);
     float3 ad = f3(c[12], c[13], c[14]);
     float3 p0 = f3(c[15], c[16], c[17]);
     float al = c[18], sl = c[19], r0 = c[20], r1 = c[21];
     float a, b, cc, root[2];
-    if (kind == DK_RING) {
+    if (kind == DK_RING) {              /* in the ring's own frame */
+        float3 rox = f3(org.x * c[0] + org.y * c[3] + org.z * c[6] + c[9],
+                        org.x * c[1] + org.y * c[4] + org.z * c[7] + c[10],
+                        org.x * c[2] + org.y * c[5] + org.z * c[8] + c[11]);
+        float3 rdx = f3(dir.x * c[0] + dir.y * c[3] + dir.z * c[6],
+                        dir.x * c[1] + dir.y * c[4] + dir.z * c[7],
+                        dir.x * c[2] + dir.y * c[5] + dir.z * c[8]);
         if ((rdx.z <= D_FTINY) & (rdx.z >= -D_FTINY))
             return;
         root[0] = -rox.z / rdx.z;
@@ -230,28 +264,33 @@ GB_DFN void hit_cone(const gb_dscene &S, int obj, int kind, int ci, float3 org,
         best.rod = -rdx.z;
         return;
     }
-    if ((kind == DK_CONE) | (kind == DK_CUP)) {
-        a = rdx.x * rdx.x + rdx.y * rdx.y - rdx.z * rdx.z;
-        b = 2.f * (rdx.x * rox.x + rdx.y * rox.y - rdx.z * rox.z);
-        cc = rox.x * rox.x + rox.y * rox.y - rox.z * rox.z;
-    } else {
-        a = rdx.x * rdx.x + rdx.y * rdx.y;
-        b = 2.f * (rdx.x * rox.x + rdx.y * rox.y);
-        cc = rox.x * rox.x + rox.y * rox.y - r0 * r0;
-    }
-    int nr = quadratic(root, a, b, cc);
-    for (int rn = 0; rn < nr; rn++) {
-        if (root[rn] <= D_FTINY)
+    /* surface |w(t)| = r0 + k*s(t): s the axial and w the radial part of
+     * the ray point relative to p0, k the radius slope (0 for cylinders) */
+    const bool cyl = (kind == DK_CYL) | (kind == DK_TUBE);
+    const float k = cyl ? 0.f : (r1 - r0) / al;
+    float3 v0 = org - p0;
+    float s0 = dot3(v0, ad), ds = dot3(dir, ad);
+    float3 w0 = v0 - ad * s0, wd = dir - ad * ds;
+    float wdd = dot3(wd, wd);
+    float ts = wdd > 1e-12f ? -dot3(w0, wd) / wdd : 0.f;   /* closest to the axis */
+    float3 ws = w0 + wd * ts;
+    float rs = r0 + k * (s0 + ts * ds), kd = k * ds;
+    a = wdd - kd * kd;
+    b = dot3(ws, wd) - rs * kd;
+    cc = dot3(ws, ws) - rs * rs;
+    int nr = quadratic_half(root, a, b, cc);
+    float tr[2] = {ts + root[0], ts + root[1]};
+    for (int rn = first_root(tr, nr, self); rn < nr; rn++) {
+        float t = tr[rn];
+        if (t <= tmin)
             continue;
-        if (root[rn] > best.t + D_FTINY)
+        if (t > best.t + D_FTINY)
             break;
-        float3 p = org + dir * root[rn];
-        float3 v = p - p0;
-        float bb = dot3(v, ad);
+        float bb = s0 + t * ds;
         if (bb < 0.f || bb > al)
             continue;
         bool inv = (kind == DK_CUP) | (kind == DK_TUBE);
-        if (ray_reject(S, obj, root[rn], (float)(1 - 2 * ((rn > 0) ^ inv)), best, tmin))
+        if (ray_reject(S, obj, t, (float)(1 - 2 * ((rn > 0) ^ inv)), best, tmin))
             break;
         float aa, c2 = 0.f;
         if (kind == DK_CYL)
@@ -266,14 +305,14 @@ GB_DFN void hit_cone(const gb_dscene &S, int obj, int kind, int ci, float3 org,
                 aa = -aa;
             }
         }
-        float3 n = (v - ad * bb) * (1.f / aa);
+        float3 n = (ws + wd * root[rn]) * (1.f / aa);   /* radial part at the hit */
         if ((kind == DK_CONE) | (kind == DK_CUP))
             n = (n * al - ad * c2) * (1.f / sl);
         float nn = dot3(n, n);
         if ((nn > 1.f + D_FTINY) | (nn < 1.f - D_FTINY))
             n = n * (1.f / (.5f + .5f * nn));
         best.obj = obj;
-        best.t = root[rn];
+        best.t = t;
         best.n = n;
         best.rod = -dot3(dir, n);
         return;
@@ -281,7 +320,7 @@ GB_DFN void hit_cone(const gb_dscene &S, int obj, int kind, int ci, float3 org,
 }
 
 GB_DFN void hit_object(const gb_dscene &S, int obj, float3 org, float3 dir, Hit &best,
-                                           float tmin)
+                                           float tmin, bool self = false)
 {
     int4 od = S.obj[obj];
     int kind = od.x & 0xff;
@@ -291,14 +330,14 @@ GB_DFN void hit_object(const gb_dscene &S, int obj, float3 org, float3 dir, Hit 
         break;
     case DK_SPHERE:
     case DK_BUBBLE:
-        hit_sphere(S, obj, kind == DK_BUBBLE, org, dir, best, tmin);
+        hit_sphere(S, obj, kind == DK_BUBBLE, org, dir, best, tmin, self);
         break;
     case DK_CONE:
     case DK_CUP:
     case DK_CYL:
     case DK_TUBE:
     case DK_RING:
-        hit_cone(S, obj, kind, od.w, org, dir, best, tmin);
+        hit_cone(S, obj, kind, od.w, org, dir, best, tmin, self);
         break;
     default:
         break;
@@ -326,15 +365,12 @@ GB_DFN bool local_hit(const gb_dscene &S, float3 org, float3 dir, int skip,
     const float cs = S.cusize;
     /* Self-intersection: a ray leaving a planar surface cannot meet it
      * again, so that surface is skipped.  A curved origin surface is still
-     * tested (its far side is a legitimate hit) but roots closer than a few
-     * FP32 position ulps of the scene (4e-6 of its size, the rounding of the
-     * hit point this ray starts from) are taken as the origin itself, where
-     * the reference's FP64 arithmetic gives a root below 1e-6. */
-    float self_tmin = 0.f;
+     * tested, since its far side is a legitimate hit, with the root at the
+     * origin itself excluded (first_root). */
+    bool curved_skip = false;
     if (skip >= 0) {
         int k = S.obj[skip].x & 0xff;
-        if (k != DK_FACE && k != DK_RING)
-            self_tmin = fmaxf(tmin, 4e-6f * cs);
+        curved_skip = k != DK_FACE && k != DK_RING;
     }
     float3 rel = org - f3(S.cuorg[0], S.cuorg[1], S.cuorg[2]);
     int sg[3];
@@ -393,8 +429,8 @@ GB_DFN bool local_hit(const gb_dscene &S, float3 org, float3 dir, int skip,
             k++;
             if (o != skip)
                 hit_object(S, o, org, dir, best, tmin);
-            else if (self_tmin > 0.f)           /* curved origin surface */
-                hit_object(S, o, org, dir, best, self_tmin);
+            else if (curved_skip)               /* curved origin surface */
+                hit_object(S, o, org, dir, best, tmin, true);
             continue;
         }
         if (leaf) {

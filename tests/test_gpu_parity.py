@@ -105,7 +105,20 @@ def test_zoo_all_primitives(gb, scenes):
     np.testing.assert_allclose(rgb[match], g["radiance"][match], rtol=1e-4, atol=1e-6)
     o.I = 1
     irr, _, _ = rtrace_c(gb, sc, o, g["rays"])
-    np.testing.assert_allclose(irr, g["irradiance"], rtol=1e-4, atol=1e-6)
+    # -I at the ray origin: the value is proportional to the cosine between
+    # the sensor direction and the direction to the light's centre (the one
+    # sample of -ds 0).  That direction is formed in FP32 from positions of
+    # a few metres, an angular error of about 1e-6 rad, so the relative
+    # error is bounded by 1e-5 + 1e-6 / cosine: grazing sensors amplify it.
+    rays = g["rays"]
+    to_light = np.array([5.0, 4.0, 2.99]) - rays[:, :3]
+    to_light /= np.linalg.norm(to_light, axis=1, keepdims=True)
+    cosine = np.abs((rays[:, 3:] / np.linalg.norm(rays[:, 3:], axis=1, keepdims=True) * to_light).sum(1))
+    bound = (1e-5 + 1e-6 / np.maximum(cosine, 1e-3))[:, None] * np.abs(g["irradiance"]) + 1e-6
+    err = np.abs(irr - g["irradiance"])
+    assert (err <= bound).all(), (np.nonzero((err > bound).any(1))[0], err.max())
+    # isotropic directions: about 5% of the rays are within 0.05 of grazing
+    assert (cosine < 0.05).mean() < 0.08
 
 
 def test_c2_matches_oracle_sample_for_sample(gb, scenes, scene_dir):
