@@ -205,6 +205,22 @@ def traffic_from_profiles():
     return None
 
 
+def combine_ranks(dev_s: float, wall_s: float, rays: float, world: int, device=None):
+    """Whole-job figures of a multi-rank run: the slowest rank's device and
+    wall seconds, and the rays of all ranks (the ranks trace independent
+    samples, so there is no other exchange)."""
+    if world <= 1:
+        return dev_s, wall_s, rays
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([dev_s, wall_s, rays], dtype=torch.float64, device=device)
+    mx = t.clone()
+    dist.all_reduce(mx, op=dist.ReduceOp.MAX)
+    sm = t.clone()
+    dist.all_reduce(sm, op=dist.ReduceOp.SUM)
+    return float(mx[0]), float(mx[1]), float(sm[2])
+
+
 def gpu_arm(args):
     import torch
     rank, world, local = dist_env()
@@ -260,16 +276,7 @@ def gpu_arm(args):
         ck = clocks.stop()
         dev_s = sum(regions) / 1e3
         wall_s = sum(walls)
-        if world > 1:
-            import torch.distributed as dist
-            t = torch.tensor([dev_s, wall_s, float(rays_tot)], dtype=torch.float64, device=dev)
-            mx = t.clone()
-            dist.all_reduce(mx, op=dist.ReduceOp.MAX)
-            sm = t.clone()
-            dist.all_reduce(sm, op=dist.ReduceOp.SUM)
-            dev_s, wall_s, rays_all = float(mx[0]), float(mx[1]), float(sm[2])
-        else:
-            rays_all = float(rays_tot)
+        dev_s, wall_s, rays_all = combine_ranks(dev_s, wall_s, float(rays_tot), world, dev)
         if rank != 0:
             return
         # dominant kernel and its roofline

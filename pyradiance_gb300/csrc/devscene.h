@@ -14,8 +14,8 @@
  *                                 spheres: centre + radius
  *   fvert     float2[...]         polygon vertices projected on the two
  *                                 axes other than the dominant normal axis
- *   cone      float[16 * ncones]  3x4 world->canonical transform, axis,
- *                                 length terms and radii
+ *   cone      float[24 * ncones]  3x4 world->canonical transform (rings),
+ *                                 axis, base point, length, slant, radii
  *   mat       float4[2 * nmats]   material kind and parameters
  *   src       gb_dsrc[nsrc]       light sources (rt/source.h SRCREC subset)
  *   trk       int32[nobjs]        tracked-modifier slot of each object's
