@@ -101,6 +101,26 @@ int  gb_opts_parse(int argc, const char *const *argv, int prog, gb_opts *out, in
 int  gb_rtrace(gb_scene *scene, const gb_opts *opts, const double *org_dir, int64_t n,
                double *out_rgb, int32_t *hit_id, double *hit_t);
 
+/* The values of gb_rtrace for rays already in device memory (d_org_dir:
+ * n x 6 doubles; d_rgb: n x 3 doubles, overwritten), allocating no device
+ * memory.  For callers that cannot allocate while they run: a service that
+ * reserved the GPU's memory for its own pool at start-up, or a loop beside
+ * latency-bound streams that cudaMalloc/cudaFree would stall by
+ * synchronising the device.  Working memory comes from one static 64 MiB
+ * device array per device; a call whose rays would not fit (roughly 1 KiB
+ * per ray without ambient bounces, 256 queue records of 64 bytes per
+ * hemisphere sample with -I and -ab > 0) is rejected with GB_EINVAL and a
+ * message giving the need.  The scene must have been loaded on the current
+ * device.  The first call on a device looks the array up there (and may
+ * load this library's device code); make that first call before capturing
+ * work on any stream.  Calls on the same device share the array: calls that
+ * overlap in time, from several threads or scenes, race and corrupt each
+ * other's results; serialise them.  The call returns when the output is
+ * complete.  No counterpart in the reference (its rtrace reads rays from a
+ * pipe, rt/rtrace.c:146-236). */
+int  gb_rtrace_device_noalloc(gb_scene *scene, const gb_opts *opts, const double *d_org_dir, int64_t n,
+                              double *d_rgb);
+
 /* rcontrib: out has (n / opts->c) records x (sum of nbins) x 3 doubles,
  * modifiers in the given order (rt/rcontrib.c:379-427, rt/rc2.c:294-357).
  * ray_count (optional) receives the number of rays traced. */

@@ -8,6 +8,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <ctime>
+#include <atomic>
 #include <string>
 #include <vector>
 
@@ -1179,4 +1180,201 @@ extern "C" int gb_dctimestep(const float *dc, const float *sky, int64_t M, int64
     cudaFree(c);
     cudaStreamDestroy(st);
     return rc;
+}
+
+/* ------------------------------------------- rtrace without device allocation
+ *
+ * gb_rtrace_device_noalloc: the values of gb_rtrace for rays that are
+ * already on the device, written to a device buffer, for callers that must
+ * not allocate device memory while they run -- a service that reserved the
+ * GPU's memory for its own pool when it started (a caching allocator holds
+ * the rest, so an allocation inside a request fails or forces an eviction),
+ * or a loop that shares the GPU with latency-bound streams, which
+ * cudaMalloc and cudaFree stall because they synchronise the device.
+ *
+ * All working memory of a call -- the per-kernel counters, the queue
+ * counters, the table of tracked modifiers (none for rtrace), the sensor
+ * hemisphere records of -I and the two ray queues -- is carved from the one
+ * static device array below; the rays and the output are the caller's.  The
+ * kernels are those of gb_rtrace, so results agree with it up to the order
+ * of the FP64 atomic additions.
+ */
+#define GB_NOALLOC_SCRATCH_BYTES (64u << 20)   /* 64 MiB per device */
+#define GB_NOALLOC_MAX_DEVICES 64
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[GB_NOALLOC_SCRATCH_BYTES];
+static std::atomic<void *> g_noalloc_addr[GB_NOALLOC_MAX_DEVICES];
+
+/* Device address of the scratch on the current device.  The first call on a
+ * device looks it up (which loads this module there if it is not loaded
+ * yet); later calls reuse the address. */
+static int noalloc_scratch(int dev, unsigned char **p)
+{
+    if (dev < 0 || dev >= GB_NOALLOC_MAX_DEVICES)
+        return set_err(GB_EUNSUPPORTED, "device %d: at most %d devices", dev, GB_NOALLOC_MAX_DEVICES);
+    void *a = g_noalloc_addr[dev].load();
+    if (!a) {
+        cudaError_t e = cudaGetSymbolAddress(&a, g_noalloc_scratch);
+        if (e != cudaSuccess || !a)
+            return set_err(GB_ECUDA, "scratch lookup on device %d failed: %s", dev, cudaGetErrorString(e));
+        g_noalloc_addr[dev].store(a);
+    }
+    *p = (unsigned char *)a;
+    return GB_OK;
+}
+
+static int on_device(const void *p, int dev)
+{
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return (at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged) && at.device == dev;
+}
+
+extern "C" int gb_rtrace_device_noalloc(gb_scene *G, const gb_opts *o, const double *d_org_dir, int64_t n,
+                                        double *d_rgb)
+{
+    if (!G || !o || (n > 0 && (!d_org_dir || !d_rgb)) || n < 0)
+        return set_err(GB_EINVAL, "null argument or negative ray count");
+    g_stats[0] = g_stats[1] = g_stats[2] = g_stats[3] = 0;
+    memset(&g_prof, 0, sizeof g_prof);
+    int rc = check_shading(G, o);
+    if (rc < 0)
+        return rc;
+    if (n == 0)
+        return GB_OK;
+    int dev = 0;
+    CK(cudaGetDevice(&dev));
+    if (!on_device(G->ds.obj, dev))
+        return set_err(GB_EINVAL, "the scene was loaded on another device than the current one (%d)", dev);
+    if (!on_device(d_org_dir, dev) || !on_device(d_rgb, dev))
+        return set_err(GB_EINVAL, "rays and output must be device memory of the current device (%d)", dev);
+    unsigned char *base = nullptr;
+    rc = noalloc_scratch(dev, &base);
+    if (rc < 0)
+        return rc;
+
+    /* scratch layout, each part on a 256-byte boundary */
+    auto up = [](size_t b) { return (b + 255) & ~(size_t)255; };
+    const size_t stat_bytes = GB_K_N * GB_ST_N * sizeof(unsigned long long);
+    const int n0 = (o->I && o->ab > 0 && o->ad > 0) ? root_divisions(o) : 0;
+    if (n0 > 128)
+        return set_err(GB_EUNSUPPORTED, "-ad %d gives %d x %d hemisphere divisions; at most 128 x 128 are "
+                       "supported", o->ad, n0, n0);
+    const size_t nobj = G->H.nobjs > 0 ? (size_t)G->H.nobjs : 1;
+    size_t off_stats = 0, off_cnt = up(stat_bytes), off_trk = off_cnt + up(4 * sizeof(unsigned long long));
+    size_t off_roots = off_trk + up(nobj * sizeof(int));
+    size_t off_spt = off_roots + (n0 > 0 ? up((size_t)n * sizeof(gb_rootrec)) : 0);
+    size_t off_q = off_spt + (n0 > 0 ? up((size_t)n * n0 * n0 * sizeof(float2)) : 0);
+    /* the queue need gb_rtrace sizes for, without its 1M-ray minimum */
+    long long est = (long long)n * (n0 > 0 ? (long long)n0 * n0 * 4 : (o->ab > 0 ? (long long)o->ad * 2 : 8));
+    long long qcap = off_q < GB_NOALLOC_SCRATCH_BYTES
+                         ? (long long)((GB_NOALLOC_SCRATCH_BYTES - off_q) / 2 / sizeof(gb_qray)) : 0;
+    if (est > qcap)
+        return set_err(GB_EINVAL, "%lld rays with these options need %.1f MiB of scratch; the static scratch "
+                       "is %u MiB (trace fewer rays per call)", (long long)n,
+                       (off_q + 2.0 * est * sizeof(gb_qray)) / 1048576.0, GB_NOALLOC_SCRATCH_BYTES >> 20);
+    qcap = (qcap / 4) * 4;
+
+    cudaStream_t st = G->stream;
+    unsigned long long *stats = (unsigned long long *)(base + off_stats);
+    unsigned long long *cnt = (unsigned long long *)(base + off_cnt);   /* [0] A, [1] B, [2] work items */
+    int *trk = (int *)(base + off_trk);
+    gb_qray *qa = (gb_qray *)(base + off_q);
+    gb_qray *qb = qa + qcap;
+    /* what must start at zero: the counters and the output, which the
+     * kernels accumulate into; the table of tracked modifiers is all -1
+     * (no modifier is tracked); queues and hemisphere records are written
+     * before they are read */
+    CK(cudaMemsetAsync(stats, 0, stat_bytes, st));
+    CK(cudaMemsetAsync(cnt, 0, 4 * sizeof(unsigned long long), st));
+    CK(cudaMemsetAsync(trk, 0xff, nobj * sizeof(int), st));
+    CK(cudaMemsetAsync(d_rgb, 0, (size_t)n * 3 * sizeof(double), st));
+
+    gb_run P;
+    memset(&P, 0, sizeof P);
+    P.S = G->ds;
+    P.S.trk = trk;
+    P.ab = o->ab;
+    P.ad = o->ad;
+    P.minweight = (float)o->lw;
+    P.maxdepth = o->lr;
+    for (int j = 0; j < 3; j++) P.av[j] = (float)o->av[j];
+    P.dstrsrc = (float)o->dj;
+    P.specthresh = (float)o->st;
+    P.contrib_mode = o->V;
+    uint64_t seed = seed_of(o);
+    P.k0 = (uint32_t)seed;
+    P.k1 = (uint32_t)(seed >> 32);
+    P.replica = o->replica;
+    P.nsensors = n;
+    P.sensors = d_org_dir;
+    P.value = d_rgb;
+    P.accum = 1;
+    P.qcap = qcap;
+    P.work = cnt + 2;
+    auto go = [&](int kid, int (*fn)(const gb_run *, cudaStream_t, int)) -> int {
+        P.stats = stats + kid * GB_ST_N;
+        if (fn(&P, st, G->sms) < 0)
+            return set_err(GB_ECUDA, "launch failed: %s", cudaGetErrorString(cudaGetLastError()));
+        g_stats[3]++;
+        g_prof.launches[kid]++;
+        return GB_OK;
+    };
+    if (o->I) {
+        if (n0 > 0) {
+            P.roots = (gb_rootrec *)(base + off_roots);
+            P.root_spt = (float2 *)(base + off_spt);
+        }
+        P.root_n = n0;
+        if ((rc = go(GB_K_ROOT, gb_launch_root)) < 0)
+            return rc;
+        if (n0 > 0) {
+            P.qout = qa;
+            P.qout_count = cnt;
+            if ((rc = go(GB_K_GENROOT, gb_launch_gen_root)) < 0)
+                return rc;
+        }
+    } else {
+        P.qout = qa;
+        P.qout_count = cnt;
+        if ((rc = go(GB_K_PRIMARY, gb_launch_primary)) < 0)
+            return rc;
+    }
+    int in = 0;
+    for (int gen = 0; gen < 64; gen++) {
+        unsigned long long c = 0;
+        CK(cudaMemcpyAsync(&c, cnt + in, sizeof c, cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        if (c == 0)
+            break;
+        if ((long long)c > qcap)
+            return set_err(GB_EOVERFLOW, "ray queue overflow (%llu rays for %lld slots)", c, qcap);
+        P.qin = in ? qb : qa;
+        P.qin_count = cnt + in;
+        P.qout = in ? qa : qb;
+        P.qout_count = cnt + (1 - in);
+        CK(cudaMemsetAsync(cnt + (1 - in), 0, sizeof(unsigned long long), st));
+        CK(cudaMemsetAsync(P.work, 0, sizeof(unsigned long long), st));
+        if ((rc = go(GB_K_GEN, gb_launch_gen)) < 0)
+            return rc;
+        CK(cudaMemsetAsync(cnt + in, 0, sizeof(unsigned long long), st));
+        in = 1 - in;
+    }
+    unsigned long long hs[GB_K_N][GB_ST_N];
+    CK(cudaMemcpyAsync(hs, stats, sizeof hs, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    unsigned long long overflow = 0;
+    for (int k = 0; k < GB_K_N; k++) {
+        g_stats[0] += (int64_t)hs[k][GB_ST_RAYS];
+        g_stats[1] += (int64_t)hs[k][GB_ST_STEPS];
+        g_stats[2] += (int64_t)hs[k][GB_ST_CONTRIB];
+        overflow += hs[k][GB_ST_OVERFLOW];
+        memcpy(g_prof.st[k], hs[k], sizeof hs[k]);
+    }
+    if (overflow)
+        return set_err(GB_EOVERFLOW, "ray queue overflow (%llu records dropped)", overflow);
+    return GB_OK;
 }
