@@ -173,6 +173,34 @@ def test_dctimestep_fp32_fp64(gb):
     np.testing.assert_allclose(r32, g["out"], rtol=1e-4, atol=1e-6 * np.abs(g["out"]).max())
 
 
+def _dc_pair(rng, M, K, N):
+    """Daylight-coefficient-like operands: lognormal DC with 30% zeros,
+    lognormal sky with half of the columns (night hours) zero."""
+    dc = rng.lognormal(-6, 2, (M, K, 3)).astype(np.float32)
+    dc[rng.random((M, K)) < 0.3] = 0
+    sky = rng.lognormal(2, 1, (K, N, 3)).astype(np.float32)
+    sky[:, rng.random(N) < 0.5] = 0
+    ref = np.stack([dc[..., c].astype(np.float64) @ sky[..., c].astype(np.float64) for c in range(3)], -1)
+    return dc, sky, ref
+
+
+@pytest.mark.parametrize("M,K,N", [(300, 333, 700), (2100, 700, 2100)])
+def test_dctimestep_bf16x3_error_vs_fp64(gb, M, K, N):
+    """BF16x3 on the tensor cores against an FP64 product.  Sizes that are
+    not multiples of the 128 x 256 x 64 tiles; the second has more tiles
+    than SMs and a partial row-tile group.  Bound: the split leaves 2^-18
+    of each operand, FP32 accumulation adds about sqrt(K) * 2^-24."""
+    dc, sky, ref = _dc_pair(np.random.default_rng(M), M, K, N)
+    out = gb.dctimestep_array(dc, sky, mode="bf16x3")
+    nz = ref > 0
+    np.testing.assert_array_equal(out[~nz], 0.0)
+    rel = np.abs(out[nz] - ref[nz]) / ref[nz]
+    assert rel.max() < 3e-5 and rel.mean() < 3e-6, (rel.max(), rel.mean())
+    g = golden("dct_small.npz")
+    r = gb.dctimestep_array(g["dc"], g["sky"], mode="bf16x3")
+    np.testing.assert_allclose(r, g["out"], rtol=1e-4, atol=1e-6 * np.abs(g["out"]).max())
+
+
 def test_errors_are_reported(gb, scenes):
     from pyradiance_gb300 import _lib
     with pytest.raises(_lib.GbError) as e:
