@@ -41,8 +41,10 @@ MODS = [dict(modifier="groundglow"),
 WORKLOAD = ("rcontrib daylight coefficients: 4096 sensors (64x64 grid, z=0.8, +z), -I+ -ab 3 -ad 1024 "
             "-lw 1e-4 -c 1; room 10x8x3 m + 2x3 m glass window (transmissivity 0.6) + 20,000 random "
             "triangles; glow sky + ground, Reinhart MF:1 + ground = 146 bins")
-# algorithmic bytes per unit of traversal work
-B_NODE, B_STEP, B_TEST, B_QRAY = 4, 8, 60, 128
+# algorithmic bytes per unit of traversal work: one child code per node descent,
+# set offset + count per cube visit, object record + vertices per test
+B_NODE, B_STEP, B_TEST = 4, 8, 60
+B_RAYIO = 48 + 32          # the walk kernel reads origin, direction, origin object; writes a 32-byte result
 
 
 def dist_env():
@@ -52,12 +54,13 @@ def dist_env():
     return rank, world, local
 
 
-def peaks():
+def peaks(kind: str = "hbm"):
+    """Roofline denominator: HBM copy GB/s, or dense bf16 TFLOP/s (burst)."""
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
         d = json.loads(p.read_text())
-        return float(d["hbm_gbs"]), "measured"
-    return 6800.0, "fallback"
+        return float(d["hbm_gbs"] if kind == "hbm" else d["bf16_tflops"]), "measured"
+    return (6800.0 if kind == "hbm" else 1900.0), "fallback"
 
 
 class ClockSampler:
@@ -205,6 +208,57 @@ def traffic_from_profiles():
     return None
 
 
+DCT_SHAPE = (1024, 2306, 8760)     # 1/16 of the rows of a 16,384-sensor x 2,306-patch x 8,760-hour run
+
+
+def dct_measure(dev, steps: int):
+    """DC x sky (dctimestep) on the device: BF16x3 on the tensor cores and
+    the FP32 CUDA-core kernel on the same resident operands (lognormal DC
+    with 30% zeros, half of the sky's hours dark), each timed with CUDA
+    events on the calling stream (best of `steps`), and the error of both
+    against an FP64 product of the same operands."""
+    import ctypes as C
+    import torch
+    from pyradiance_gb300 import _lib
+    L = _lib.lib()
+    M, K, N = DCT_SHAPE
+    g = torch.Generator(device=dev).manual_seed(0)
+    dc = torch.exp(torch.randn(M, K, 3, device=dev, generator=g) * 2 - 6)
+    dc[torch.rand(M, K, device=dev, generator=g) < 0.3] = 0
+    sky = torch.exp(torch.randn(K, N, 3, device=dev, generator=g) + 2)
+    sky[:, torch.rand(N, device=dev, generator=g) < 0.5] = 0
+    st = torch.cuda.current_stream(dev)
+    outs, ms = {}, {}
+    for mode, name, reps in ((_lib.GB_DCT_FP64, "fp64", 1), (_lib.GB_DCT_FP32, "fp32", max(3, steps)),
+                             (_lib.GB_DCT_BF16X3, "bf16x3", max(3, steps))):
+        out = torch.empty(M, N, 3, device=dev)
+        ts = []
+        for _ in range(reps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(st)
+            _lib.check(L.gb_dctimestep_device(C.c_void_p(dc.data_ptr()), C.c_void_p(sky.data_ptr()), M, K, N,
+                                              mode, C.c_void_p(out.data_ptr()), C.c_void_p(st.cuda_stream)))
+            e1.record(st)
+            torch.cuda.synchronize(dev)
+            ts.append(e0.elapsed_time(e1))
+        outs[name], ms[name] = out, min(ts)
+    ref = outs["fp64"].double()
+    nz = ref > 0
+    flops = 2.0 * M * K * N * 3
+    res = {"shape": {"M": M, "K": K, "N": N}, "flops": flops}
+    for name in ("fp32", "bf16x3"):
+        rel = (outs[name].double() - ref).abs()[nz] / ref[nz]
+        res[name] = {"ms": round(ms[name], 3), "tflops": round(flops / ms[name] / 1e9, 1),
+                     "err_vs_fp64": {"mean_rel": float(rel.mean()), "max_rel": float(rel.max())}}
+    res["speedup_bf16x3_vs_fp32"] = round(ms["fp32"] / ms["bf16x3"], 2)
+    peak, kind = peaks("bf16")
+    res["tensor_frac"] = {"achieved_tflops": round(3 * flops / ms["bf16x3"] / 1e9, 1), "peak": peak,
+                          "frac": round(3 * flops / ms["bf16x3"] / 1e9 / peak, 4), "peak_source": kind,
+                          "note": "three bf16 products per useful product (hi*hi + hi*lo + lo*hi); the time "
+                                  "includes the hi/lo split of both operands"}
+    return res
+
+
 def combine_ranks(dev_s: float, wall_s: float, rays: float, world: int, device=None):
     """Whole-job figures of a multi-rank run: the slowest rank's device and
     wall seconds, and the rays of all ranks (the ranks trace independent
@@ -290,7 +344,8 @@ def gpu_arm(args):
                     a[f] += v[f]
         dom = max(agg, key=lambda k: agg[k]["ms"])
         d = agg[dom]
-        bytes_per_launch = (d["nodes"] * B_NODE + d["steps"] * B_STEP + d["tests"] * B_TEST) / d["launches"]
+        io = B_RAYIO * d["rays"] if dom == "trace" else 0      # ray record in, walk result out
+        bytes_per_launch = (d["nodes"] * B_NODE + d["steps"] * B_STEP + d["tests"] * B_TEST + io) / d["launches"]
         ms_per_launch = d["ms"] / d["launches"]
         achieved = bytes_per_launch / (ms_per_launch / 1e3) / 1e9
         peak, peak_kind = peaks()
@@ -313,10 +368,12 @@ def gpu_arm(args):
             "roofline": {"bound": "hbm", "kernel": "k_" + dom, "achieved": round(achieved, 1), "peak": peak,
                          "unit": "GB/s", "frac": round(achieved / peak, 4),
                          "traffic": traffic, "peak_source": peak_kind,
-                         "note": "algorithmic bytes = node descents*4 + cube visits*8 + object tests*60"},
+                         "note": "algorithmic bytes = node descents*4 + cube visits*8 + object tests*60 (+ rays*80 for "
+                                 "the walk kernel's ray record and result)"},
             "cpu_baseline": {"value": None if cpu_v is None else round(cpu_v, 4), "unit": "Mrays/s",
                              "cores": cores, "kind": "port", "sample": sample},
             "clocks": ck,
+            "dctimestep": dct_measure(dev, args.steps),
         }
         print(json.dumps(line), flush=True)
 

@@ -107,10 +107,10 @@ int  gb_rtrace(gb_scene *scene, const gb_opts *opts, const double *org_dir, int6
  * reserved the GPU's memory for its own pool at start-up, or a loop beside
  * latency-bound streams that cudaMalloc/cudaFree would stall by
  * synchronising the device.  Working memory comes from one static 64 MiB
- * device array per device; a call whose rays would not fit (roughly 1 KiB
- * per ray without ambient bounces, 256 queue records of 64 bytes per
- * hemisphere sample with -I and -ab > 0) is rejected with GB_EINVAL and a
- * message giving the need.  The scene must have been loaded on the current
+ * device array per device; a call whose rays would not fit (1.25 KiB per
+ * ray without ambient bounces, 640 bytes per first-hemisphere sample with
+ * -I and -ab > 0) is rejected with GB_EINVAL and a message giving the
+ * need.  The scene must have been loaded on the current
  * device.  The first call on a device looks the array up there (and may
  * load this library's device code); make that first call before capturing
  * work on any stream.  Calls on the same device share the array: calls that
@@ -147,8 +147,8 @@ int  gb_dctimestep_device(const float *d_dc, const float *d_sky, int64_t M, int6
  * contributions binned, kernel launches. */
 int  gb_last_stats(int64_t *rays, int64_t *steps, int64_t *contribs, int64_t *launches);
 /* Per-kernel profile of the last rtrace/rcontrib call on this thread:
- * kernel 0 cast, 1 sensor roots, 2 first hemisphere, 3 primaries, 4 later
- * generations; device milliseconds (CUDA events on the library's stream),
+ * kernel 0 cast, 1 sensor roots, 2 first-hemisphere rays, 3 primaries, 4 octree
+ * walks, 5 shading (one launch of 4 and 5 per generation); device milliseconds (CUDA events on the library's stream),
  * launches, counters (rays, cube steps, contributions, queue overflows,
  * bad bins, node descents, object tests, spare) and the milliseconds of the
  * whole kernel region.  No counterpart in the reference (its -t progress

@@ -105,7 +105,7 @@ def last_stats() -> dict:
     return {"rays": v[0].value, "steps": v[1].value, "contribs": v[2].value, "launches": v[3].value}
 
 
-KERNELS = ["cast", "root", "gen_root", "primary", "gen"]
+KERNELS = ["cast", "root", "expand", "primary", "trace", "shade"]
 COUNTERS = ["rays", "steps", "contribs", "overflow", "badbin", "nodes", "tests", "spare"]
 
 

@@ -45,6 +45,8 @@
 #include <cudaTypedefs.h>
 #include <stdint.h>
 
+#include <mutex>
+
 #include "dct.h"
 #include "../../include/gbrad.h"
 
@@ -384,28 +386,30 @@ k_dct_tc(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUten
                      : "memory");
 }
 
-/* A[m][k][c] (interleaved RGB) -> As[c][h][Mp][Kp] bf16 hi/lo; padding is
- * zeroed beforehand */
+/* A[m][k][c] (interleaved RGB) -> As[c][h][Mp][Kp] bf16 hi/lo, one thread
+ * per element of the padded plane (zeros in the padding) */
 __global__ void k_split_a(const float *__restrict__ A, __nv_bfloat16 *__restrict__ As, int M, int K, int Mp,
                           int Kp)
 {
     long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= (long long)M * K)
+    if (i >= (long long)Mp * Kp)
         return;
-    const int m = (int)(i / K), k = (int)(i % K);
-    const size_t plane = (size_t)Mp * Kp, at = (size_t)m * Kp + k;
+    const int m = (int)(i / Kp), k = (int)(i % Kp);
+    const bool in = m < M && k < K;
+    const size_t plane = (size_t)Mp * Kp;
+    const float *a = in ? A + 3 * ((long long)m * K + k) : A;
 #pragma unroll
     for (int c = 0; c < 3; c++) {
-        const float x = A[3 * i + c];
+        const float x = in ? a[c] : 0.f;
         const __nv_bfloat16 hi = __float2bfloat16_rn(x);
         const __nv_bfloat16 lo = __float2bfloat16_rn(x - __bfloat162float(hi));
-        As[(2 * c) * plane + at] = hi;
-        As[(2 * c + 1) * plane + at] = lo;
+        As[(2 * c) * plane + i] = hi;
+        As[(2 * c + 1) * plane + i] = lo;
     }
 }
 
 /* B[k][n][c] -> Bs[c][h][Np][Kp] (transposed, K contiguous) through a 32x32
- * shared tile per channel */
+ * shared tile per channel; the grid covers the padded plane */
 __global__ void k_split_b(const float *__restrict__ B, __nv_bfloat16 *__restrict__ Bs, int K, int N, int Np,
                           int Kp)
 {
@@ -421,10 +425,8 @@ __global__ void k_split_b(const float *__restrict__ B, __nv_bfloat16 *__restrict
     }
     __syncthreads();
     const size_t plane = (size_t)Np * Kp;
-    for (int r = ty; r < 32; r += 8) {
+    for (int r = ty; r < 32; r += 8) {            /* padded plane: zeros beyond K, N */
         const int n = n0 + r, k = k0 + tx;
-        if (n >= N || k >= K)
-            continue;
 #pragma unroll
         for (int c = 0; c < 3; c++) {
             const float x = tile[c][tx][r];
@@ -471,7 +473,7 @@ int gb_dct_bf16x3(const float *A, const float *B, int64_t M, int64_t K, int64_t 
                   std::string &err)
 {
     auto rnd = [](int64_t x, int64_t q) { return (x + q - 1) / q * q; };
-    if (M > (1 << 24) || K > (1 << 24) || N > (1 << 24) || M * K > (1ll << 40) || K * N > (1ll << 40)) {
+    if (M > (1 << 24) || K > (1 << 20) || N > (1 << 24) || M * K > (1ll << 37) || K * N > (1ll << 37)) {
         err = "matrix too large for the BF16x3 path";
         return GB_EINVAL;
     }
@@ -487,29 +489,49 @@ int gb_dct_bf16x3(const float *A, const float *B, int64_t M, int64_t K, int64_t 
     s.kb = s.Kp / TK;
     s.tiles = (long long)s.mt * s.nt * 3;
     const size_t a_elems = (size_t)6 * s.Mp * s.Kp, b_elems = (size_t)6 * s.Np * s.Kp;
-    /* workspace: error flag, split A, split B */
-    unsigned char *ws = nullptr;
+    /* workspace (error flag, split A, split B), kept per device between
+     * calls and grown on demand; calls are serialised on it */
     const size_t a_off = 256, b_off = a_off + ((a_elems * 2 + 255) & ~(size_t)255);
     const size_t total = b_off + b_elems * 2;
-    if (cudaMalloc(&ws, total) != cudaSuccess) {
-        cudaGetLastError();
-        err = "cannot allocate the BF16x3 operand planes";
-        return GB_ENOMEM;
+    static std::mutex lock;
+    static unsigned char *ws_dev[64];
+    static size_t ws_size[64];
+    std::lock_guard<std::mutex> guard(lock);
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) {
+        err = "no usable CUDA device";
+        return GB_ECUDA;
     }
+    if (ws_size[dev] < total) {
+        if (ws_dev[dev]) {
+            cudaStreamSynchronize(st);
+            cudaFree(ws_dev[dev]);
+        }
+        ws_dev[dev] = nullptr;
+        ws_size[dev] = 0;
+        if (cudaMalloc(&ws_dev[dev], total) != cudaSuccess) {
+            cudaGetLastError();
+            ws_dev[dev] = nullptr;
+            err = "cannot allocate the BF16x3 operand planes";
+            return GB_ENOMEM;
+        }
+        ws_size[dev] = total;
+    }
+    unsigned char *ws = ws_dev[dev];
     int *d_err = (int *)ws;
     __nv_bfloat16 *As = (__nv_bfloat16 *)(ws + a_off), *Bs = (__nv_bfloat16 *)(ws + b_off);
     int rc = GB_OK;
     CUtensorMap ma, mb;
     do {
-        if (cudaMemsetAsync(ws, 0, total, st) != cudaSuccess) {
+        if (cudaMemsetAsync(d_err, 0, sizeof(int), st) != cudaSuccess) {
             err = "memset failed";
             rc = GB_ECUDA;
             break;
         }
-        const long long na = M * K;
+        const long long na = (long long)s.Mp * s.Kp;
         k_split_a<<<(unsigned)((na + 255) / 256), 256, 0, st>>>(A, As, s.M, s.K, s.Mp, s.Kp);
-        k_split_b<<<dim3((unsigned)((N + 31) / 32), (unsigned)((K + 31) / 32)), dim3(32, 8), 0, st>>>(
-            B, Bs, s.K, s.N, s.Np, s.Kp);
+        k_split_b<<<dim3((unsigned)(s.Np / 32), (unsigned)(s.Kp / 32)), dim3(32, 8), 0, st>>>(B, Bs, s.K, s.N,
+                                                                                           s.Np, s.Kp);
         if (!make_map(&ma, As, (uint64_t)6 * s.Mp, (uint64_t)s.Kp, TM) ||
             !make_map(&mb, Bs, (uint64_t)6 * s.Np, (uint64_t)s.Kp, TN)) {
             err = "cannot encode the TMA tensor maps";
@@ -549,6 +571,5 @@ int gb_dct_bf16x3(const float *A, const float *B, int64_t M, int64_t K, int64_t 
             rc = GB_ECUDA;
         }
     } while (0);
-    cudaFree(ws);
     return rc;
 }

@@ -20,6 +20,9 @@
 #include "scene.h"
 #include "tracehost.h"
 
+#define GB_MAX_GENERATIONS 256    /* walk/shade rounds of one run (path length) */
+#define GB_TIMED_LAUNCHES 256     /* launches timed with events in one run */
+
 static thread_local std::string g_error;
 static thread_local int64_t g_stats[4];
 
@@ -100,10 +103,11 @@ struct gb_scene {
     DevBuf kids, setoff, setdata, obj, geo, fvert, cone, matd, srcd, trk;
     gb_dscene ds;
     /* work buffers */
-    DevBuf sensors, value, bins, stats, roots, rootspt, qa, qb, qcount, binprog, modinfo, hits, hitt, trkrun;
+    DevBuf sensors, value, bins, stats, roots, rootspt, qa, qb, qcount, binprog, modinfo, hits, hitt, trkrun,
+        hitrec;
     cudaStream_t stream = nullptr;
     int sms = 0;
-    cudaEvent_t ev[2 * 96 + 2];
+    cudaEvent_t ev[2 * GB_TIMED_LAUNCHES + 2];
     int nev = 0;
 };
 
@@ -579,7 +583,7 @@ extern "C" void gb_scene_free(gb_scene *G)
         return;
     DevBuf *bufs[] = {&G->kids, &G->setoff, &G->setdata, &G->obj, &G->geo, &G->fvert, &G->cone, &G->matd,
                       &G->srcd, &G->trk, &G->sensors, &G->value, &G->bins, &G->stats, &G->roots, &G->rootspt, &G->qa,
-                      &G->qb, &G->qcount, &G->binprog, &G->modinfo, &G->hits, &G->hitt, &G->trkrun};
+                      &G->qb, &G->qcount, &G->binprog, &G->modinfo, &G->hits, &G->hitt, &G->trkrun, &G->hitrec};
     for (DevBuf *b : bufs)
         b->release();
     if (G->stream)
@@ -840,12 +844,12 @@ static int run(gb_scene *G, const gb_opts *o, int follow, const double *org_dir,
         G->nev = (int)(sizeof G->ev / sizeof G->ev[0]);
     }
     int evused = 2;                                /* ev[0], ev[1]: the kernel region */
-    int evkid[96];
+    int evkid[GB_TIMED_LAUNCHES];
     /* one launch, bracketed by events, counting into its kernel's block */
     auto launch = [&](int kid, gb_run &PR, auto fn) -> int {
         PR.stats = (unsigned long long *)G->stats.p + kid * GB_ST_N;
         int slot = (evused - 2) / 2;
-        bool timed = slot < 96;
+        bool timed = slot < GB_TIMED_LAUNCHES;
         if (timed)
             cudaEventRecord(G->ev[evused], st);
         if (fn(PR) < 0)
@@ -943,17 +947,24 @@ static int run(gb_scene *G, const gb_opts *o, int follow, const double *org_dir,
     long long qcap = est < (1ll << 20) ? (1ll << 20) : est;
     size_t freeb = 0, totalb = 0;
     cudaMemGetInfo(&freeb, &totalb);
-    long long qmax = (long long)(freeb / 4 / sizeof(gb_qray));
+    const size_t slot = 2 * sizeof(gb_qray) + sizeof(gb_qhit);   /* two queues and the walk results */
+    long long qmax = (long long)(freeb / 3 / slot);
     if (qmax > (1ll << 28)) qmax = 1ll << 28;
     if (qcap > qmax) qcap = qmax;
-    if (G->qa.ensure((size_t)qcap * sizeof(gb_qray)) < 0 || G->qb.ensure((size_t)qcap * sizeof(gb_qray)) < 0)
+    if (G->qa.ensure((size_t)qcap * sizeof(gb_qray)) < 0 || G->qb.ensure((size_t)qcap * sizeof(gb_qray)) < 0 ||
+        G->hitrec.ensure((size_t)qcap * sizeof(gb_qhit)) < 0)
         return set_err(GB_ENOMEM, "cannot allocate %lld-ray work queues", qcap);
     P.qcap = qcap;
+    P.hits = (gb_qhit *)G->hitrec.p;
     unsigned long long *cnt = (unsigned long long *)G->qcount.p;   /* [0] A, [1] B, [2] work items */
     CK(cudaMemsetAsync(cnt, 0, 3 * sizeof(unsigned long long), st));
     P.work = cnt + 2;
     gb_qray *qa = (gb_qray *)G->qa.p, *qb = (gb_qray *)G->qb.p;
 
+    /* the first generation's queue: -I hemisphere rays or primaries */
+    P.qout = qa;
+    P.qout_count = cnt;
+    CK(cudaEventRecord(G->ev[0], st));
     if (o->I) {
         if (n0 > 0) {
             if (G->roots.ensure((size_t)n * sizeof(gb_rootrec)) < 0 ||
@@ -963,29 +974,22 @@ static int run(gb_scene *G, const gb_opts *o, int follow, const double *org_dir,
             P.root_spt = (float2 *)G->rootspt.p;
         }
         P.root_n = n0;
-        CK(cudaEventRecord(G->ev[0], st));
         int rc = launch(GB_K_ROOT, P, [&](gb_run &R) { return gb_launch_root(&R, st, G->sms); });
         if (rc < 0)
             return rc;
         if (n0 > 0) {
-            P.qout = qa;
-            P.qout_count = cnt;
-            CK(cudaMemsetAsync(P.work, 0, sizeof(unsigned long long), st));
-            rc = launch(GB_K_GENROOT, P, [&](gb_run &R) { return gb_launch_gen_root(&R, st, G->sms); });
+            rc = launch(GB_K_EXPAND, P, [&](gb_run &R) { return gb_launch_expand_root(&R, st, G->sms); });
             if (rc < 0)
                 return rc;
         }
     } else {
-        P.qout = qa;
-        P.qout_count = cnt;
-        CK(cudaEventRecord(G->ev[0], st));
         int rc = launch(GB_K_PRIMARY, P, [&](gb_run &R) { return gb_launch_primary(&R, st, G->sms); });
         if (rc < 0)
             return rc;
     }
-    /* later generations until the queue drains */
+    /* generations until the queue drains: walk, then shade into the other queue */
     int in = 0;
-    for (int gen = 0; gen < 64; gen++) {
+    for (int gen = 0; gen < GB_MAX_GENERATIONS; gen++) {
         unsigned long long c = 0;
         CK(cudaMemcpyAsync(&c, cnt + in, sizeof c, cudaMemcpyDeviceToHost, st));
         CK(cudaStreamSynchronize(st));
@@ -999,7 +1003,11 @@ static int run(gb_scene *G, const gb_opts *o, int follow, const double *org_dir,
         P.qout_count = cnt + (1 - in);
         CK(cudaMemsetAsync(cnt + (1 - in), 0, sizeof(unsigned long long), st));
         CK(cudaMemsetAsync(P.work, 0, sizeof(unsigned long long), st));
-        int rc = launch(GB_K_GEN, P, [&](gb_run &R) { return gb_launch_gen(&R, st, G->sms); });
+        int rc = launch(GB_K_TRACE, P, [&](gb_run &R) { return gb_launch_trace(&R, st, G->sms); });
+        if (rc < 0)
+            return rc;
+        CK(cudaMemsetAsync(P.work, 0, sizeof(unsigned long long), st));
+        rc = launch(GB_K_SHADE, P, [&](gb_run &R) { return gb_launch_shade(&R, st, G->sms); });
         if (rc < 0)
             return rc;
         CK(cudaMemsetAsync(cnt + in, 0, sizeof(unsigned long long), st));
@@ -1194,7 +1202,8 @@ extern "C" int gb_dctimestep(const float *dc, const float *sky, int64_t M, int64
  *
  * All working memory of a call -- the per-kernel counters, the queue
  * counters, the table of tracked modifiers (none for rtrace), the sensor
- * hemisphere records of -I and the two ray queues -- is carved from the one
+ * hemisphere records of -I, the two ray queues and the walk results -- is
+ * carved from the one
  * static device array below; the rays and the output are the caller's.  The
  * kernels are those of gb_rtrace, so results agree with it up to the order
  * of the FP64 atomic additions.
@@ -1270,12 +1279,12 @@ extern "C" int gb_rtrace_device_noalloc(gb_scene *G, const gb_opts *o, const dou
     size_t off_q = off_spt + (n0 > 0 ? up((size_t)n * n0 * n0 * sizeof(float2)) : 0);
     /* the queue need gb_rtrace sizes for, without its 1M-ray minimum */
     long long est = (long long)n * (n0 > 0 ? (long long)n0 * n0 * 4 : (o->ab > 0 ? (long long)o->ad * 2 : 8));
-    long long qcap = off_q < GB_NOALLOC_SCRATCH_BYTES
-                         ? (long long)((GB_NOALLOC_SCRATCH_BYTES - off_q) / 2 / sizeof(gb_qray)) : 0;
+    const size_t slot = 2 * sizeof(gb_qray) + sizeof(gb_qhit);   /* two queues and the walk results */
+    long long qcap = off_q < GB_NOALLOC_SCRATCH_BYTES ? (long long)((GB_NOALLOC_SCRATCH_BYTES - off_q) / slot) : 0;
     if (est > qcap)
         return set_err(GB_EINVAL, "%lld rays with these options need %.1f MiB of scratch; the static scratch "
                        "is %u MiB (trace fewer rays per call)", (long long)n,
-                       (off_q + 2.0 * est * sizeof(gb_qray)) / 1048576.0, GB_NOALLOC_SCRATCH_BYTES >> 20);
+                       (off_q + (double)est * slot) / 1048576.0, GB_NOALLOC_SCRATCH_BYTES >> 20);
     qcap = (qcap / 4) * 4;
 
     cudaStream_t st = G->stream;
@@ -1284,6 +1293,7 @@ extern "C" int gb_rtrace_device_noalloc(gb_scene *G, const gb_opts *o, const dou
     int *trk = (int *)(base + off_trk);
     gb_qray *qa = (gb_qray *)(base + off_q);
     gb_qray *qb = qa + qcap;
+    gb_qhit *hits = (gb_qhit *)(qb + qcap);
     /* what must start at zero: the counters and the output, which the
      * kernels accumulate into; the table of tracked modifiers is all -1
      * (no modifier is tracked); queues and hemisphere records are written
@@ -1314,6 +1324,7 @@ extern "C" int gb_rtrace_device_noalloc(gb_scene *G, const gb_opts *o, const dou
     P.value = d_rgb;
     P.accum = 1;
     P.qcap = qcap;
+    P.hits = hits;
     P.work = cnt + 2;
     auto go = [&](int kid, int (*fn)(const gb_run *, cudaStream_t, int)) -> int {
         P.stats = stats + kid * GB_ST_N;
@@ -1334,7 +1345,7 @@ extern "C" int gb_rtrace_device_noalloc(gb_scene *G, const gb_opts *o, const dou
         if (n0 > 0) {
             P.qout = qa;
             P.qout_count = cnt;
-            if ((rc = go(GB_K_GENROOT, gb_launch_gen_root)) < 0)
+            if ((rc = go(GB_K_EXPAND, gb_launch_expand_root)) < 0)
                 return rc;
         }
     } else {
@@ -1344,7 +1355,7 @@ extern "C" int gb_rtrace_device_noalloc(gb_scene *G, const gb_opts *o, const dou
             return rc;
     }
     int in = 0;
-    for (int gen = 0; gen < 64; gen++) {
+    for (int gen = 0; gen < GB_MAX_GENERATIONS; gen++) {
         unsigned long long c = 0;
         CK(cudaMemcpyAsync(&c, cnt + in, sizeof c, cudaMemcpyDeviceToHost, st));
         CK(cudaStreamSynchronize(st));
@@ -1358,7 +1369,10 @@ extern "C" int gb_rtrace_device_noalloc(gb_scene *G, const gb_opts *o, const dou
         P.qout_count = cnt + (1 - in);
         CK(cudaMemsetAsync(cnt + (1 - in), 0, sizeof(unsigned long long), st));
         CK(cudaMemsetAsync(P.work, 0, sizeof(unsigned long long), st));
-        if ((rc = go(GB_K_GEN, gb_launch_gen)) < 0)
+        if ((rc = go(GB_K_TRACE, gb_launch_trace)) < 0)
+            return rc;
+        CK(cudaMemsetAsync(P.work, 0, sizeof(unsigned long long), st));
+        if ((rc = go(GB_K_SHADE, gb_launch_shade)) < 0)
             return rc;
         CK(cudaMemsetAsync(cnt + in, 0, sizeof(unsigned long long), st));
         in = 1 - in;

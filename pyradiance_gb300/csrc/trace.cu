@@ -483,7 +483,7 @@ __device__ float3 shadow_chain(const gb_run &P, Ray sr, int s, Counters &cnt, fl
         Hit h;
         uint32_t st[3] = {0, 0, 0};
         cnt.rays++;
-        bool hit = local_hit(S, sr.org, sr.dir, sr.origin, D_FTINY, D_FHUGE, h, st);
+        bool hit = local_hit(S, sr.org, sr.dir, sr.origin, h, st);
         cnt.add(st);
         if (!hit) {
             if (guard == 0) {
@@ -684,196 +684,161 @@ __device__ __forceinline__ void setup_surf(const gb_run &P, int mk, float4 m0, f
     s.rblt = !s.pure && P.specthresh >= s.rspec - D_FTINY;
 }
 
-#define MAXKIDS 2
-
-/* Trace ray r and its single-child continuations; other children go to the
- * next generation.  `hemi_push` decides whether hemispheres are expanded
- * here (deferred generations) or written out. */
-/* Trace ray r once and shade its hit.  Children beyond the first go to the
- * next generation's queue; the first replaces r and true is returned, or
- * false when the path ends here. */
-__device__ bool step_ray(const gb_run &P, Ray &r, Counters &cnt)
+/* Shade ray r given its trace result (h.obj < 0: the ray left the scene)
+ * and push every child ray to the next generation's queue
+ * (rt/raytrace.c:163-256 raytrace / rayshade, the material routines). */
+__device__ void shade_ray(const gb_run &P, const Ray &r, const Hit &h, Counters &cnt)
 {
     const gb_dscene &S = P.S;
-    {
-        Hit h;
-        cnt.rays++;
-        uint32_t st[3] = {0, 0, 0};
-        bool hit = local_hit(S, r.org, r.dir, r.origin, D_FTINY, D_FHUGE, h, st);
-        cnt.add(st);
-        if (!hit) {
-            int sidx = source_hit(S, r.dir, r.rsrc, r.crtype);
-            if (sidx >= 0)
-                light_hit(P, r, S.src[sidx].so, S.src[sidx].mat, D_FHUGE, 1.f, cnt, nullptr);
-            return false;
-        }
-        int ms = S.obj[h.obj].y;
-        int mk = ms >= 0 ? (int)S.mat[2 * ms].x : DM_NONE;
-        float3 hp = r.org + r.dir * h.t;
-        if (mk == DM_LIGHT || mk == DM_GLOW) {
-            light_hit(P, r, h.obj, ms, h.t, h.rod, cnt, nullptr);
-            return false;
-        }
-        if (mk == DM_NONE) {
-            surface_contrib(P, r, h.obj, cnt);
-            Ray c;
-            ray_origin(P, r, GB_TRANS, f3(1.f, 1.f, 1.f), false, GB_C_PASS, c, nullptr);
-            c.org = hp;
-            c.dir = r.dir;
-            c.origin = h.obj;
-            r = c;
-            return true;
-        }
-        Ray kids[MAXKIDS];
-        int nk = 0;
-        float4 m0 = S.mat[2 * ms], m1 = S.mat[2 * ms + 1];
-        float3 n = h.n;
-        float rod = h.rod;
-        if (rod < 0.f) {                        /* flipsurface (backvis on) */
-            rod = -rod;
-            n = -n;
-        }
-        surface_contrib(P, r, h.obj, cnt);
-        if (mk == DM_GLASS) {
-            float3 mc = f3(m0.y, m0.z, m0.w);
-            float rindex = m1.x;
-            bool hastrans = maxc(mc) > 1e-15f;
-            mc = f3(fmaxf(mc.x, 1e-15f), fmaxf(mc.y, 1e-15f), fmaxf(mc.z, 1e-15f));
-            float pdot = rod;
-            float cos2 = sqrtf((1.f - 1.f / (rindex * rindex)) + pdot * pdot / (rindex * rindex));
-            if (hastrans)
-                mc = f3(powf(mc.x, 1.f / cos2), powf(mc.y, 1.f / cos2), powf(mc.z, 1.f / cos2));
-            float r1e = (pdot - rindex * cos2) / (pdot + rindex * cos2);
-            r1e *= r1e;
-            float r1m = (1.f / pdot - rindex / cos2) / (1.f / pdot + rindex / cos2);
-            r1m *= r1m;
-            float mm[3] = {mc.x, mc.y, mc.z}, tc[3], rc[3];
-            for (int i = 0; i < 3; i++) {
-                float d = mm[i];
-                tc[i] = .5f * (1.f - r1e) * (1.f - r1e) * d / (1.f - r1e * r1e * d * d) +
-                        .5f * (1.f - r1m) * (1.f - r1m) * d / (1.f - r1m * r1m * d * d);
-                float d2 = d * d;
-                rc[i] = .5f * r1e * (1.f + (1.f - 2.f * r1e) * d2) / (1.f - r1e * r1e * d2) +
-                        .5f * r1m * (1.f + (1.f - 2.f * r1m) * d2) / (1.f - r1m * r1m * d2);
-            }
-            if (hastrans) {
-                Ray c;
-                if (ray_origin(P, r, GB_TRANS, f3(tc[0], tc[1], tc[2]), true, GB_C_TRANS, c, nullptr)) {
-                    c.org = hp;
-                    c.dir = r.dir;
-                    c.origin = h.obj;
-                    kids[nk++] = c;
-                }
-            }
-            Ray c;
-            if (ray_origin(P, r, GB_REFLECTED, f3(rc[0], rc[1], rc[2]), true, GB_C_REFL, c, nullptr)) {
-                c.org = hp;
-                c.dir = normalize3(r.dir + n * (2.f * pdot));
-                c.origin = h.obj;
-                kids[nk++] = c;
-            }
-        } else {                                /* plastic / metal */
-            int okd = S.obj[h.obj].x & 0xff;
-            Surf s;
-            setup_surf(P, mk, m0, m1, n, rod, okd == DK_FACE || okd == DK_RING, s);
-            if (s.refl && s.pure) {
-                Ray c;
-                if (ray_origin(P, r, GB_REFLECTED, s.scolor, true, GB_C_REFL, c, nullptr)) {
-                    c.org = hp;
-                    c.dir = normalize3(r.dir + s.pnorm * (2.f * s.pdot));
-                    c.origin = h.obj;
-                    kids[nk++] = c;
-                }
-            }
-            if (!(s.pure && s.rdiff <= D_FTINY)) {
-                if (s.rdiff > D_FTINY) {
-                    float3 aval = s.mcolor * s.rdiff;
-                    if (s.rblt)
-                        aval = aval + s.scolor;
-                    if (P.ad > 0 && r.adepth < P.ab) {
-                        Hemi hm;
-                        if (make_hemi(P, r, aval, n, hm) && hm.n >= 4) {
-                            spawn_hemi_big(P, r, hm, hp, h.obj);
-                        } else if (hm.n > 0) {
-                            int nn = hm.n * hm.n;
-                            for (int k = 0; k < nn; k++) {
-                                Ray c;
-                                if (!hemi_child(P, r, hm, hp, h.obj, k, nullptr, c))
-                                    continue;
-                                if (nk < MAXKIDS)
-                                    kids[nk++] = c;
-                                else
-                                    push_ray(P, c);
-                            }
-                        }
-                    } else if (P.av[0] != 0.f || P.av[1] != 0.f || P.av[2] != 0.f) {
-                        add_value(P, r.sensor, r.coef * aval * f3(P.av[0], P.av[1], P.av[2]));
-                    }
-                }
-                if (S.nsrc > 0)
-                    direct(P, r, hp, s, h.obj, cnt);
-            }
-        }
-        if (nk == 0)
-            return false;
-        for (int k = 1; k < nk; k++)
-            push_ray(P, kids[k]);
-        r = kids[0];
-        return true;
+    if (h.obj < 0) {
+        int sidx = source_hit(S, r.dir, r.rsrc, r.crtype);
+        if (sidx >= 0)
+            light_hit(P, r, S.src[sidx].so, S.src[sidx].mat, D_FHUGE, 1.f, cnt, nullptr);
+        return;
     }
+    int ms = S.obj[h.obj].y;
+    int mk = ms >= 0 ? (int)S.mat[2 * ms].x : DM_NONE;
+    float3 hp = r.org + r.dir * h.t;
+    if (mk == DM_LIGHT || mk == DM_GLOW) {
+        light_hit(P, r, h.obj, ms, h.t, h.rod, cnt, nullptr);
+        return;
+    }
+    if (mk == DM_NONE) {
+        surface_contrib(P, r, h.obj, cnt);
+        Ray c;
+        ray_origin(P, r, GB_TRANS, f3(1.f, 1.f, 1.f), false, GB_C_PASS, c, nullptr);
+        c.org = hp;
+        c.dir = r.dir;
+        c.origin = h.obj;
+        push_ray(P, c);
+        return;
+    }
+    float4 m0 = S.mat[2 * ms], m1 = S.mat[2 * ms + 1];
+    float3 n = h.n;
+    float rod = h.rod;
+    if (rod < 0.f) {                            /* flipsurface (backvis on) */
+        rod = -rod;
+        n = -n;
+    }
+    surface_contrib(P, r, h.obj, cnt);
+    if (mk == DM_GLASS) {
+        float3 mc = f3(m0.y, m0.z, m0.w);
+        float rindex = m1.x;
+        bool hastrans = maxc(mc) > 1e-15f;
+        mc = f3(fmaxf(mc.x, 1e-15f), fmaxf(mc.y, 1e-15f), fmaxf(mc.z, 1e-15f));
+        float pdot = rod;
+        float cos2 = sqrtf((1.f - 1.f / (rindex * rindex)) + pdot * pdot / (rindex * rindex));
+        if (hastrans)
+            mc = f3(powf(mc.x, 1.f / cos2), powf(mc.y, 1.f / cos2), powf(mc.z, 1.f / cos2));
+        float r1e = (pdot - rindex * cos2) / (pdot + rindex * cos2);
+        r1e *= r1e;
+        float r1m = (1.f / pdot - rindex / cos2) / (1.f / pdot + rindex / cos2);
+        r1m *= r1m;
+        float mm[3] = {mc.x, mc.y, mc.z}, tc[3], rc[3];
+        for (int i = 0; i < 3; i++) {
+            float d = mm[i];
+            tc[i] = .5f * (1.f - r1e) * (1.f - r1e) * d / (1.f - r1e * r1e * d * d) +
+                    .5f * (1.f - r1m) * (1.f - r1m) * d / (1.f - r1m * r1m * d * d);
+            float d2 = d * d;
+            rc[i] = .5f * r1e * (1.f + (1.f - 2.f * r1e) * d2) / (1.f - r1e * r1e * d2) +
+                    .5f * r1m * (1.f + (1.f - 2.f * r1m) * d2) / (1.f - r1m * r1m * d2);
+        }
+        if (hastrans) {
+            Ray c;
+            if (ray_origin(P, r, GB_TRANS, f3(tc[0], tc[1], tc[2]), true, GB_C_TRANS, c, nullptr)) {
+                c.org = hp;
+                c.dir = r.dir;
+                c.origin = h.obj;
+                push_ray(P, c);
+            }
+        }
+        Ray c;
+        if (ray_origin(P, r, GB_REFLECTED, f3(rc[0], rc[1], rc[2]), true, GB_C_REFL, c, nullptr)) {
+            c.org = hp;
+            c.dir = normalize3(r.dir + n * (2.f * pdot));
+            c.origin = h.obj;
+            push_ray(P, c);
+        }
+        return;
+    }
+    /* plastic / metal */
+    int okd = S.obj[h.obj].x & 0xff;
+    Surf su;
+    setup_surf(P, mk, m0, m1, n, rod, okd == DK_FACE || okd == DK_RING, su);
+    if (su.refl && su.pure) {
+        Ray c;
+        if (ray_origin(P, r, GB_REFLECTED, su.scolor, true, GB_C_REFL, c, nullptr)) {
+            c.org = hp;
+            c.dir = normalize3(r.dir + su.pnorm * (2.f * su.pdot));
+            c.origin = h.obj;
+            push_ray(P, c);
+        }
+    }
+    if (su.pure && su.rdiff <= D_FTINY)
+        return;
+    if (su.rdiff > D_FTINY) {
+        float3 aval = su.mcolor * su.rdiff;
+        if (su.rblt)
+            aval = aval + su.scolor;
+        if (P.ad > 0 && r.adepth < P.ab) {
+            Hemi hm;
+            if (make_hemi(P, r, aval, n, hm) && hm.n >= 4) {
+                spawn_hemi_big(P, r, hm, hp, h.obj);
+            } else if (hm.n > 0) {
+                int nn = hm.n * hm.n;
+                for (int k = 0; k < nn; k++) {
+                    Ray c;
+                    if (hemi_child(P, r, hm, hp, h.obj, k, nullptr, c))
+                        push_ray(P, c);
+                }
+            }
+        } else if (P.av[0] != 0.f || P.av[1] != 0.f || P.av[2] != 0.f) {
+            add_value(P, r.sensor, r.coef * aval * f3(P.av[0], P.av[1], P.av[2]));
+        }
+    }
+    if (S.nsrc > 0)
+        direct(P, r, hp, su, h.obj, cnt);
 }
 
-#define MAX_CHAIN 256   /* rays one path may continue through in one thread */
-
-/* Persistent work loop: every lane without a ray fetches the next work item
- * (one atomic per warp), so lanes whose paths end early are refilled at
- * once instead of idling until the longest path of the warp ends.
- * make(i, r) turns work item i into a ray (false if it dies at birth). */
-template <typename Make>
-__device__ __forceinline__ void persistent_loop(const gb_run &P, unsigned long long *work,
-                                                unsigned long long total, Counters &cnt, Make make)
+/* Persistent work loop: each warp takes work items 32 at a time with one
+ * atomic, so warps that finish early take more instead of idling.  body(i)
+ * processes item i. */
+template <typename Body>
+__device__ __forceinline__ void persistent_items(unsigned long long *work, unsigned long long total, Body body)
 {
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
-    Ray r;
-    bool active = false, exhausted = false;
-    int chain = 0;
     for (;;) {
-        unsigned need = __ballot_sync(FULL, !active);
-        if (need && !exhausted) {
-            unsigned long long base = 0;
-            int leader = __ffs(need) - 1;
-            if (lane == leader)
-                base = atomicAdd(work, (unsigned long long)__popc(need));
-            base = __shfl_sync(FULL, base, leader);
-            if (base >= total)
-                exhausted = true;
-            if (!active) {
-                unsigned long long i = base + __popc(need & ((1u << lane) - 1u));
-                if (i < total) {
-                    active = make(i, r);
-                    chain = 0;
-                }
-            }
-        }
-        if (!__any_sync(FULL, active)) {
-            if (exhausted)
-                break;
-            continue;
-        }
-        if (active) {
-            active = step_ray(P, r, cnt);
-            if (++chain >= MAX_CHAIN)
-                active = false;
-        }
+        unsigned long long base = 0;
+        if (lane == 0)
+            base = atomicAdd(work, 32ull);
+        base = __shfl_sync(FULL, base, 0);
+        if (base >= total)
+            break;
+        unsigned long long i = base + lane;
+        if (i < total)
+            body(i);
     }
 }
 
-__device__ void run_ray(const gb_run &P, Ray r, Counters &cnt)
+/* hit record of the trace kernels: 32 bytes, two float4 */
+__device__ __forceinline__ void store_hit(gb_qhit *q, const Hit &h)
 {
-    for (int guard = 0; guard < MAX_CHAIN; guard++)
-        if (!step_ray(P, r, cnt))
-            return;
+    float4 *p = reinterpret_cast<float4 *>(q);
+    p[0] = make_float4(__int_as_float(h.obj), h.t, h.rod, h.n.x);
+    p[1] = make_float4(h.n.y, h.n.z, 0.f, 0.f);
+}
+
+__device__ __forceinline__ Hit load_hit(const gb_qhit *q)
+{
+    const float4 *p = reinterpret_cast<const float4 *>(q);
+    float4 a = p[0], b = p[1];
+    Hit h;
+    h.obj = __float_as_int(a.x);
+    h.t = a.y;
+    h.rod = a.z;
+    h.n = f3(a.w, b.x, b.y);
+    return h;
 }
 
 /* -------------------------------------------------------------- kernels */
@@ -932,13 +897,13 @@ __global__ void k_root(gb_run P)
     flush_counters(P, cnt);
 }
 
-/* first hemisphere of every -I sensor, expanded from (sensor, stratum) */
-__global__ void __launch_bounds__(256) k_gen_root(gb_run P)
+/* first hemisphere of every -I sensor: one ray per (sensor, stratum) into
+ * the queue of the first generation */
+__global__ void __launch_bounds__(256) k_expand_root(gb_run P)
 {
-    Counters cnt = {0, 0, 0, 0, 0};
     const long long nn = (long long)P.root_n * P.root_n;
     const unsigned long long total = (unsigned long long)(nn * P.nsensors);
-    persistent_loop(P, P.work, total, cnt, [&](unsigned long long g, Ray &c) -> bool {
+    persistent_items(P.work, total, [&](unsigned long long g) {
         long long s = (long long)(g / (unsigned long long)nn);
         int k = (int)(g - (unsigned long long)s * nn);
         const gb_rootrec *rr = P.roots + s;
@@ -967,18 +932,19 @@ __global__ void __launch_bounds__(256) k_gen_root(gb_run P)
         if (hm.n >= 4) {
             pk = P.root_spt[g];
             if (pk.x > 1.5f)
-                return false;                 /* stratum died in Russian roulette */
+                return;                       /* stratum died in Russian roulette */
             sp = &pk.x;
         }
-        return hemi_child(P, parent, hm, parent.org, -1, k, sp, c);
+        Ray c;
+        if (hemi_child(P, parent, hm, parent.org, -1, k, sp, c))
+            push_ray(P, c);
     });
-    flush_counters(P, cnt);
 }
 
-/* radiance-mode primaries (rt/rtrace.c:436-468, rt/rcontrib.c:343-353) */
+/* radiance-mode primaries (rt/rtrace.c:436-468, rt/rcontrib.c:343-353)
+ * into the queue of the first generation */
 __global__ void k_primary(gb_run P)
 {
-    Counters cnt = {0, 0, 0, 0, 0};
     for (long long s = blockIdx.x * (long long)blockDim.x + threadIdx.x; s < P.nsensors;
          s += (long long)gridDim.x * blockDim.x) {
         const double *sv = P.sensors + 6 * s;
@@ -995,20 +961,93 @@ __global__ void k_primary(gb_run P)
         r.adepth = 0;
         r.path = GB_ROOT_PATH(P.replica);
         r.sensor = (uint32_t)s;
-        run_ray(P, r, cnt);
+        push_ray(P, r);
+    }
+}
+
+/* One generation, first half: the octree walk of every queued ray
+ * (rt/raytrace.c:595-793), its result written beside it.  Only the walk
+ * runs here, so the lanes of a warp execute one loop body, one iteration
+ * (an object test or a step to the next leaf) at a time.  Walks differ in
+ * length by an order of magnitude, so a lane whose walk ends takes the next
+ * queued ray at once (the warp fetches for all its idle lanes with one
+ * atomic once a quarter of them wait, or when none is busy) instead of
+ * idling until the longest walk of the warp ends.  The walk is latency
+ * bound: four blocks of 256 threads per SM (64 registers) hide more of it
+ * than two blocks at 102 registers; the descent stacks of a block sit in
+ * shared memory (25.6 KB), one column per thread. */
+#define TRACE_BLOCK 256
+/* descent stack of one thread: a column of a block-wide shared array */
+struct ColumnStack {
+    int *p;
+    __device__ __forceinline__ int &operator[](int i) { return p[i * TRACE_BLOCK]; }
+};
+
+__global__ void __launch_bounds__(TRACE_BLOCK, 4) k_trace(gb_run P)
+{
+    __shared__ int stack_cols[(GRID_BITS + 1) * TRACE_BLOCK];
+    ColumnStack stk{stack_cols + threadIdx.x};
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    Counters cnt = {0, 0, 0, 0, 0};
+    unsigned long long total = *P.qin_count;
+    if (total > (unsigned long long)P.qcap)
+        total = P.qcap;
+    Walk W;
+    unsigned long long cur = 0;
+    bool active = false, exhausted = false;
+    for (;;) {
+        const unsigned idle = __ballot_sync(FULL, !active);
+        if (!exhausted && (__popc(idle) >= 8 || idle == FULL)) {
+            unsigned long long base = 0;
+            const int leader = __ffs(idle) - 1;
+            if (lane == leader)
+                base = atomicAdd(P.work, (unsigned long long)__popc(idle));
+            base = __shfl_sync(FULL, base, leader);
+            if (base + __popc(idle) >= total)
+                exhausted = true;
+            if (!active) {
+                const unsigned long long i = base + __popc(idle & ((1u << lane) - 1u));
+                if (i < total) {
+                    const float4 *q = reinterpret_cast<const float4 *>(P.qin + i);
+                    const float4 a = q[0], b = q[1], c = q[2];
+                    cur = i;
+                    cnt.rays++;
+                    active = walk_begin(P.S, f3(a.x, a.y, a.z), f3(b.x, b.y, b.z), __float_as_int(c.w), W,
+                                        stk);
+                    if (!active)
+                        store_hit(P.hits + i, W.best);     /* missed the scene cube */
+                }
+            }
+        }
+        if (!__any_sync(FULL, active)) {
+            if (exhausted)
+                break;
+            continue;
+        }
+        if (active && walk_iter(P.S, W, stk)) {
+            uint32_t st[3] = {0, 0, 0};
+            walk_tally(W, st);
+            cnt.add(st);
+            store_hit(P.hits + cur, W.best);
+            active = false;
+        }
     }
     flush_counters(P, cnt);
 }
 
-__global__ void __launch_bounds__(256) k_gen(gb_run P)
+/* One generation, second half: shade every traced ray and queue its
+ * children for the next generation. */
+__global__ void __launch_bounds__(256) k_shade(gb_run P)
 {
     Counters cnt = {0, 0, 0, 0, 0};
     unsigned long long n = *P.qin_count;
     if (n > (unsigned long long)P.qcap)
         n = P.qcap;
-    persistent_loop(P, P.work, n, cnt, [&](unsigned long long g, Ray &r) -> bool {
-        r = load_ray(P.qin + g);
-        return true;
+    persistent_items(P.work, n, [&](unsigned long long g) {
+        const Ray r = load_ray(P.qin + g);
+        const Hit h = load_hit(P.hits + g);
+        shade_ray(P, r, h, cnt);
     });
     flush_counters(P, cnt);
 }
@@ -1026,7 +1065,7 @@ __global__ void k_cast(gb_run P, int *hit_obj, float *hit_t, float *hit_pn)
         int obj = -1;
         float t = D_FHUGE;
         float3 n = f3(0.f, 0.f, 0.f);
-        if (local_hit(P.S, org, dir, -1, D_FTINY, D_FHUGE, h, st)) {
+        if (local_hit(P.S, org, dir, -1, h, st)) {
             obj = h.obj;
             t = h.t;
             n = h.n;
@@ -1082,12 +1121,12 @@ static int resident_grid(K kernel, int block, int sms)
     return per_sm * sms;
 }
 
-int gb_launch_gen_root(const gb_run *P, cudaStream_t st, int sms)
+int gb_launch_expand_root(const gb_run *P, cudaStream_t st, int sms)
 {
     static int grid = 0;
     if (!grid)
-        grid = resident_grid(k_gen_root, 256, sms);
-    k_gen_root<<<grid, 256, 0, st>>>(*P);
+        grid = resident_grid(k_expand_root, 256, sms);
+    k_expand_root<<<grid, 256, 0, st>>>(*P);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
@@ -1097,11 +1136,20 @@ int gb_launch_primary(const gb_run *P, cudaStream_t st, int sms)
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
-int gb_launch_gen(const gb_run *P, cudaStream_t st, int sms)
+int gb_launch_trace(const gb_run *P, cudaStream_t st, int sms)
 {
     static int grid = 0;
     if (!grid)
-        grid = resident_grid(k_gen, 256, sms);
-    k_gen<<<grid, 256, 0, st>>>(*P);
+        grid = resident_grid(k_trace, TRACE_BLOCK, sms);
+    k_trace<<<grid, TRACE_BLOCK, 0, st>>>(*P);
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+int gb_launch_shade(const gb_run *P, cudaStream_t st, int sms)
+{
+    static int grid = 0;
+    if (!grid)
+        grid = resident_grid(k_shade, 256, sms);
+    k_shade<<<grid, 256, 0, st>>>(*P);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }

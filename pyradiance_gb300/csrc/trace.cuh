@@ -14,6 +14,9 @@
 /* The traversal and intersection code is written once for the device; it
  * also compiles for the host so that it can be exercised without a GPU. */
 #define GB_DFN __host__ __device__ __forceinline__
+/* rarely taken paths kept out of line, so that their registers do not
+ * count against the walk loop's */
+#define GB_DNI static __host__ __device__ __noinline__
 #ifdef __CUDA_ARCH__
 #define GB_LDG(p) __ldg(p)
 #define GB_F2I_RD(x) __float2int_rd(x)
@@ -201,7 +204,7 @@ GB_DFN int first_root(const float *t, int nr, bool self)
 }
 
 /* rt/sphere.c:15-83 */
-GB_DFN void hit_sphere(const gb_dscene &S, int obj, bool bubble, float3 org,
+GB_DNI void hit_sphere(const gb_dscene &S, int obj, bool bubble, float3 org,
                                            float3 dir, Hit &best, float tmin, bool self)
 {
     float4 sp = S.geo[obj];
@@ -233,7 +236,7 @@ GB_DFN void hit_sphere(const gb_dscene &S, int obj, bool bubble, float3 org,
 
 /* rt/o_cone.c:16-146; cone record: tm (12: 3x3 rows then translation),
  * ad (3), p0 (3), al, sl, r0, r1 */
-GB_DFN void hit_cone(const gb_dscene &S, int obj, int kind, int ci, float3 org,
+GB_DNI void hit_cone(const gb_dscene &S, int obj, int kind, int ci, float3 org,
                                          float3 dir, Hit &best, float tmin, bool self)
 {
     const float *c = S.cone + 24 * ci;
@@ -329,16 +332,22 @@ GB_DFN void hit_object(const gb_dscene &S, int obj, float3 org, float3 dir, Hit 
         hit_face(S, obj, od, org, dir, best, tmin);
         break;
     case DK_SPHERE:
-    case DK_BUBBLE:
-        hit_sphere(S, obj, kind == DK_BUBBLE, org, dir, best, tmin, self);
+    case DK_BUBBLE: {                   /* out of line: a copy, so that the */
+        Hit b = best;                   /* caller's record stays in registers */
+        hit_sphere(S, obj, kind == DK_BUBBLE, org, dir, b, tmin, self);
+        best = b;
         break;
+    }
     case DK_CONE:
     case DK_CUP:
     case DK_CYL:
     case DK_TUBE:
-    case DK_RING:
-        hit_cone(S, obj, kind, od.w, org, dir, best, tmin, self);
+    case DK_RING: {
+        Hit b = best;
+        hit_cone(S, obj, kind, od.w, org, dir, b, tmin, self);
+        best = b;
         break;
+    }
     default:
         break;
     }
@@ -355,145 +364,216 @@ GB_DFN void hit_object(const gb_dscene &S, int obj, float3 org, float3 dir, Hit 
  * and a hit recorded earlier but never confirmed is still returned when the
  * ray leaves the scene, as localhit does.
  */
-GB_DFN bool local_hit(const gb_dscene &S, float3 org, float3 dir, int skip,
-                                          float tmin, float tmax, Hit &best, uint32_t *tally)
+/* State of one ray's walk, so that a walk can be advanced one iteration at
+ * a time and a lane whose walk ends can start another ray at once.  Every
+ * field is indexed with constants only, so that it can live in registers,
+ * and it is kept small (the origin relative to the scene cube, the
+ * direction signs and the current cube's corner are recomputed where they
+ * are used); the descent stack (the node chosen at each level, indexed by
+ * level) is kept apart: a WalkStack in local memory, or a column of shared
+ * memory.  Every walk runs from FTINY to FHUGE, as every localhit call of
+ * the reference on this path does. */
+struct Walk {
+    float3 org, dir;
+    float inv[3];                 /* 1/dir, 0 where the direction is ~0 */
+    int skip;                     /* the object the ray leaves */
+    bool curved_skip, leaf;
+    int q[3];                     /* integer position on the 2^24 grid */
+    int rl, k, cnt, span, ax;     /* restart level; leaf set cursor; cube size; exit axis */
+    int set;                      /* current leaf set: offset into set_data */
+    float texit;
+    Hit best;
+    uint32_t steps, nodes, tests;
+};
+
+struct WalkStack {
+    int v[GRID_BITS + 1];
+    GB_DFN int &operator[](int i) { return v[i]; }
+};
+
+GB_DFN float walk_rel(const gb_dscene &S, const Walk &W, int i)   /* origin - cube origin */
 {
-    best.obj = -1;
-    best.t = D_FHUGE;
-    best.rod = 1.f;
-    best.n = f3(0.f, 0.f, 0.f);
+    return comp(W.org, i) - S.cuorg[i];
+}
+
+/* Set up the walk of a ray; false when the ray misses the scene cube (no
+ * hit, nothing to iterate). */
+template <typename Stack>
+GB_DFN bool walk_begin(const gb_dscene &S, float3 org, float3 dir, int skip, Walk &W, Stack &stk)
+{
+    W.best.obj = -1;
+    W.best.t = D_FHUGE;
+    W.best.rod = 1.f;
+    W.best.n = f3(0.f, 0.f, 0.f);
+    W.steps = W.nodes = W.tests = 0;
     const float cs = S.cusize;
     /* Self-intersection: a ray leaving a planar surface cannot meet it
      * again, so that surface is skipped.  A curved origin surface is still
      * tested, since its far side is a legitimate hit, with the root at the
      * origin itself excluded (first_root). */
-    bool curved_skip = false;
+    W.skip = skip;
+    W.curved_skip = false;
     if (skip >= 0) {
-        int k = S.obj[skip].x & 0xff;
-        curved_skip = k != DK_FACE && k != DK_RING;
+        int kd = S.obj[skip].x & 0xff;
+        W.curved_skip = kd != DK_FACE && kd != DK_RING;
     }
-    float3 rel = org - f3(S.cuorg[0], S.cuorg[1], S.cuorg[2]);
-    int sg[3];
-    float dd[3] = {dir.x, dir.y, dir.z}, rr[3] = {rel.x, rel.y, rel.z}, inv[3];
+    W.org = org;
+    W.dir = dir;
+    const float dd[3] = {dir.x, dir.y, dir.z};
+    float rr[3];
     int anyd = 0;
+#pragma unroll
     for (int i = 0; i < 3; i++) {
-        sg[i] = dd[i] > 1e-7f ? 1 : (dd[i] < -1e-7f ? -1 : 0);
-        inv[i] = sg[i] ? 1.f / dd[i] : 0.f;
-        anyd |= sg[i];
+        rr[i] = walk_rel(S, W, i);
+        const bool pos = dd[i] > 1e-7f, neg = dd[i] < -1e-7f;
+        W.inv[i] = (pos | neg) ? 1.f / dd[i] : 0.f;
+        anyd |= pos | neg;
     }
     if (!anyd)
         return false;
     float t = 0.f;
     bool inside = (rr[0] >= 0.f) & (rr[0] < cs) & (rr[1] >= 0.f) & (rr[1] < cs) & (rr[2] >= 0.f) & (rr[2] < cs);
     if (!inside) {
+#pragma unroll
         for (int i = 0; i < 3; i++) {
-            if (!sg[i])
+            if (W.inv[i] == 0.f)
                 continue;
-            float pl = sg[i] > 0 ? 0.f : cs;
-            float dt = (pl - rr[i]) * inv[i];
+            float pl = W.inv[i] > 0.f ? 0.f : cs;
+            float dt = (pl - rr[i]) * W.inv[i];
             if (dt > t)
                 t = dt;
         }
         t += D_FTINY;
-        if (t >= tmax)
+        if (t >= D_FHUGE)
             return false;
+        bool in = true;
+#pragma unroll
         for (int i = 0; i < 3; i++) {
             float p = rr[i] + dd[i] * t;
-            if (!(p >= 0.f && p < cs))
-                return false;
+            in &= p >= 0.f && p < cs;
         }
+        if (!in)
+            return false;
     }
-    const float gs = S.grid_scale, cell = S.cell;
-    int q[3];
+#pragma unroll
     for (int i = 0; i < 3; i++) {
-        int v = GB_F2I_RD((rr[i] + dd[i] * t) * gs);
-        q[i] = min(max(v, 0), GRID_N - 1);
+        int v = GB_F2I_RD((rr[i] + dd[i] * t) * S.grid_scale);
+        W.q[i] = min(max(v, 0), GRID_N - 1);
     }
-    uint32_t steps = 0, nodes = 0, tests = 0;
-    /* One flat loop whose iterations either test one object of the current
-     * leaf or move to the next leaf, so that the lanes of a warp stay in step
-     * whatever the set sizes of the leaves they cross.  stk[l] is the node
-     * chosen at level l on the way to the current leaf; a step to the
-     * neighbouring cube restarts the descent at the deepest level the two
-     * cubes share (from the highest coordinate bit that changed). */
-    int stk[GRID_BITS + 1];
     stk[0] = S.root;
-    int rl = 0, k = 1, cnt = 0, span = 0, ax = 0;
-    int lo[3] = {0, 0, 0};
-    const int *set = nullptr;
-    float texit = 0.f;
-    bool leaf = false;
-    for (;;) {
-        if (k <= cnt) {                          /* next object of this leaf */
-            int o = GB_LDG(set + k);
-            k++;
-            if (o != skip)
-                hit_object(S, o, org, dir, best, tmin);
-            else if (curved_skip)               /* curved origin surface */
-                hit_object(S, o, org, dir, best, tmin, true);
-            continue;
-        }
-        if (leaf) {
-            if (best.obj >= 0 && best.t <= texit)
-                break;                          /* hit inside this cube */
-            steps++;
-            if (texit >= tmax || steps >= MAX_CUBE_STEPS)
-                break;
-            /* step to the face neighbour along the exit axis; the exit point
-             * lies on that face, so the other coordinates stay inside this
-             * cube's slab (an edge or corner exit takes a second, zero-length
-             * step) */
-            int oq0 = q[0], oq1 = q[1], oq2 = q[2];
-            for (int i = 0; i < 3; i++) {
-                if (i == ax)
-                    continue;
-                int v = GB_F2I_RD((rr[i] + dd[i] * texit) * gs);
-                q[i] = min(max(v, lo[i]), lo[i] + span - 1);
-            }
-            q[ax] = sg[ax] > 0 ? lo[ax] + span : lo[ax] - 1;
-            if (q[ax] < 0 || q[ax] >= GRID_N)
-                break;                          /* left the scene */
-            unsigned diff = (unsigned)((oq0 ^ q[0]) | (oq1 ^ q[1]) | (oq2 ^ q[2]));
-            rl = GRID_BITS - 1 - (31 - GB_CLZ(diff));
-        }
-        /* descend from the shared ancestor to the leaf containing q */
-        int node = stk[rl], level = rl;
-        while (node >= 0) {
-            int sh = GRID_BITS - 1 - level;
-            int br = ((q[0] >> sh) & 1) | (((q[1] >> sh) & 1) << 1) | (((q[2] >> sh) & 1) << 2);
-            node = GB_LDG(S.kids + 8 * node + br);
-            stk[++level] = node;
-            nodes++;
-        }
-        span = 1 << (GRID_BITS - level);
-        lo[0] = q[0] & ~(span - 1);
-        lo[1] = q[1] & ~(span - 1);
-        lo[2] = q[2] & ~(span - 1);
-        texit = D_FHUGE;                         /* exit distance of this cube */
+    W.rl = 0;
+    W.k = 1;
+    W.cnt = 0;
+    W.span = 0;
+    W.ax = 0;
+    W.set = 0;
+    W.texit = 0.f;
+    W.leaf = false;
+    return true;
+}
+
+/* One iteration of the walk: test one object of the current leaf, or move
+ * to the next leaf (descending from the deepest ancestor it shares with the
+ * last one, from the highest coordinate bit that changed).  Returns true
+ * when the walk has ended. */
+template <typename Stack>
+GB_DFN bool walk_iter(const gb_dscene &S, Walk &W, Stack &stk)
+{
+    if (W.k <= W.cnt) {                          /* next object of this leaf */
+        int o = GB_LDG(S.set_data + W.set + W.k);
+        W.k++;
+        if (o != W.skip)
+            hit_object(S, o, W.org, W.dir, W.best, D_FTINY);
+        else if (W.curved_skip)                  /* curved origin surface */
+            hit_object(S, o, W.org, W.dir, W.best, D_FTINY, true);
+        return false;
+    }
+    const float dd[3] = {W.dir.x, W.dir.y, W.dir.z};
+    if (W.leaf) {
+        if (W.best.obj >= 0 && W.best.t <= W.texit)
+            return true;                         /* hit inside this cube */
+        W.steps++;
+        if (W.texit >= D_FHUGE || W.steps >= MAX_CUBE_STEPS)
+            return true;
+        /* step to the face neighbour along the exit axis; the exit point
+         * lies on that face, so the other coordinates stay inside this
+         * cube's slab (an edge or corner exit takes a second, zero-length
+         * step) */
+        const int mask = ~(W.span - 1);
+        int oq0 = W.q[0], oq1 = W.q[1], oq2 = W.q[2];
+#pragma unroll
         for (int i = 0; i < 3; i++) {
-            if (!sg[i])
-                continue;
-            float pl = (float)(sg[i] > 0 ? lo[i] + span : lo[i]) * cell;
-            float dt = (pl - rr[i]) * inv[i];
-            if (dt < texit) {
-                texit = dt;
-                ax = i;
+            const int lo = W.q[i] & mask;        /* this cube's corner */
+            if (i == W.ax) {
+                W.q[i] = W.inv[i] > 0.f ? lo + W.span : lo - 1;
+            } else {
+                int v = GB_F2I_RD((walk_rel(S, W, i) + dd[i] * W.texit) * S.grid_scale);
+                W.q[i] = min(max(v, lo), lo + W.span - 1);
             }
         }
-        leaf = true;
-        k = 1;
-        cnt = 0;
-        if (node <= -2) {                       /* full leaf: its set to test */
-            set = S.set_data + GB_LDG(S.set_off + (-node - 2));
-            cnt = GB_LDG(set);
-            tests += cnt;
+        if ((unsigned)(W.q[0] | W.q[1] | W.q[2]) >= (unsigned)GRID_N)
+            return true;                         /* left the scene */
+        unsigned diff = (unsigned)((oq0 ^ W.q[0]) | (oq1 ^ W.q[1]) | (oq2 ^ W.q[2]));
+        W.rl = GRID_BITS - 1 - (31 - GB_CLZ(diff));
+    }
+    /* descend from the shared ancestor to the leaf containing q */
+    int node = stk[W.rl], level = W.rl;
+    while (node >= 0) {
+        int sh = GRID_BITS - 1 - level;
+        int br = ((W.q[0] >> sh) & 1) | (((W.q[1] >> sh) & 1) << 1) | (((W.q[2] >> sh) & 1) << 2);
+        node = GB_LDG(S.kids + 8 * node + br);
+        stk[++level] = node;
+        W.nodes++;
+    }
+    W.span = 1 << (GRID_BITS - level);
+    const int mask = ~(W.span - 1);
+    W.texit = D_FHUGE;                           /* exit distance of this cube */
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+        if (W.inv[i] == 0.f)
+            continue;
+        const int lo = W.q[i] & mask;
+        float pl = (float)(W.inv[i] > 0.f ? lo + W.span : lo) * S.cell;
+        float dt = (pl - walk_rel(S, W, i)) * W.inv[i];
+        if (dt < W.texit) {
+            W.texit = dt;
+            W.ax = i;
         }
     }
-    if (tally) {
-        tally[0] += steps + 1;
-        tally[1] += nodes;
-        tally[2] += tests;
+    W.leaf = true;
+    W.k = 1;
+    W.cnt = 0;
+    if (node <= -2) {                            /* full leaf: its set to test */
+        W.set = GB_LDG(S.set_off + (-node - 2));
+        W.cnt = GB_LDG(S.set_data + W.set);
+        W.tests += W.cnt;
     }
+    return false;
+}
+
+/* counters of a finished walk: cube visits, node descents, object tests */
+GB_DFN void walk_tally(const Walk &W, uint32_t *tally)
+{
+    if (tally) {
+        tally[0] += W.steps + 1;
+        tally[1] += W.nodes;
+        tally[2] += W.tests;
+    }
+}
+
+/* The whole walk of one ray: best hit in `best`, true if there is one. */
+GB_DFN bool local_hit(const gb_dscene &S, float3 org, float3 dir, int skip, Hit &best, uint32_t *tally)
+{
+    Walk W;
+    WalkStack stk;
+    if (!walk_begin(S, org, dir, skip, W, stk)) {
+        best = W.best;
+        return false;
+    }
+    while (!walk_iter(S, W, stk))
+        ;
+    walk_tally(W, tally);
+    best = W.best;
     return best.obj >= 0;
 }
 

@@ -19,12 +19,13 @@
 #define GB_ST_TESTS    6   /* ray-object intersection tests */
 #define GB_ST_N        8
 /* kernels with their own block of GB_ST_N counters */
-#define GB_K_CAST      0
-#define GB_K_ROOT      1
-#define GB_K_GENROOT   2
-#define GB_K_PRIMARY   3
-#define GB_K_GEN       4
-#define GB_K_N         5
+#define GB_K_CAST      0   /* first hit only */
+#define GB_K_ROOT      1   /* -I sensor roots */
+#define GB_K_EXPAND    2   /* first hemisphere of the -I sensors into the queue */
+#define GB_K_PRIMARY   3   /* primaries into the queue */
+#define GB_K_TRACE     4   /* octree walk of one generation */
+#define GB_K_SHADE     5   /* shading of one generation, children queued */
+#define GB_K_N         6
 
 #define GRID_BITS_HOST 24      /* must equal GRID_BITS of trace.cuh */
 
@@ -32,6 +33,12 @@
 typedef struct __align__(16) {
     float v[16];
 } gb_qray;
+
+/* the walk result of a queued ray: 32 bytes (object, distance, -dir.n,
+ * normal) */
+typedef struct __align__(16) {
+    float v[8];
+} gb_qhit;
 
 /* first hemisphere of a -I sensor */
 typedef struct {
@@ -71,14 +78,16 @@ typedef struct {
     const unsigned long long *qin_count;
     gb_qray *qout;
     unsigned long long *qout_count;
+    gb_qhit *hits;             /* walk results of qin, same indices */
     long long qcap;
     unsigned long long *work;  /* work-item counter of the persistent kernels (zeroed per launch) */
 } gb_run;
 
 int gb_launch_cast(const gb_run *P, int *hit_obj, float *hit_t, float *hit_pn, cudaStream_t st, int sms);
 int gb_launch_root(const gb_run *P, cudaStream_t st, int sms);
-int gb_launch_gen_root(const gb_run *P, cudaStream_t st, int sms);
+int gb_launch_expand_root(const gb_run *P, cudaStream_t st, int sms);
 int gb_launch_primary(const gb_run *P, cudaStream_t st, int sms);
-int gb_launch_gen(const gb_run *P, cudaStream_t st, int sms);
+int gb_launch_trace(const gb_run *P, cudaStream_t st, int sms);
+int gb_launch_shade(const gb_run *P, cudaStream_t st, int sms);
 
 #endif
