@@ -14,6 +14,10 @@
  *                                 spheres: centre + radius
  *   fvert     float2[...]         polygon vertices projected on the two
  *                                 axes other than the dominant normal axis
+ *   fv4       float4[2 * nobjs]   the same for faces of at most four
+ *                                 vertices, packed at a fixed place per
+ *                                 object (v0 v1 | v2 v3), so that a face
+ *                                 test needs no second indirection
  *   cone      float[24 * ncones]  3x4 world->canonical transform (rings),
  *                                 axis, base point, length, slant, radii
  *   mat       float4[2 * nmats]   material kind and parameters
@@ -72,6 +76,7 @@ typedef struct {
     const int4  *obj;
     const float4 *geo;
     const float2 *fvert;
+    const float4 *fv4;
     const float *cone;
     /* materials */
     const float4 *mat;

@@ -97,10 +97,11 @@ struct gb_scene {
     std::vector<int4> hobj;
     std::vector<float4> hgeo;
     std::vector<float2> hfvert;
+    std::vector<float4> hfv4;
     std::vector<float> hcone;
     std::vector<gb_dsrc> hsrc;
     /* device scene */
-    DevBuf kids, setoff, setdata, obj, geo, fvert, cone, matd, srcd, trk;
+    DevBuf kids, setoff, setdata, obj, geo, fvert, fv4, cone, matd, srcd, trk;
     gb_dscene ds;
     /* work buffers */
     DevBuf sensors, value, bins, stats, roots, rootspt, qa, qb, qcount, binprog, modinfo, hits, hitt, trkrun,
@@ -347,7 +348,8 @@ static int prepare_device(gb_scene *G)
         CK(cudaDeviceSetLimit(cudaLimitStackSize, 16384));
     if (upload(G->kids, G->hkids) < 0 || upload(G->setoff, G->hsetoff) < 0 || upload(G->setdata, G->hsetdata) < 0 ||
         upload(G->obj, G->hobj) < 0 || upload(G->geo, G->hgeo) < 0 || upload(G->fvert, G->hfvert) < 0 ||
-        upload(G->cone, G->hcone) < 0 || upload(G->matd, G->mat) < 0 || upload(G->srcd, G->hsrc) < 0)
+        upload(G->fv4, G->hfv4) < 0 || upload(G->cone, G->hcone) < 0 || upload(G->matd, G->mat) < 0 ||
+        upload(G->srcd, G->hsrc) < 0)
         return set_err(GB_ENOMEM, "device upload of the scene failed");
     gb_dscene &d = G->ds;
     d.kids = (const int *)G->kids.p;
@@ -356,6 +358,7 @@ static int prepare_device(gb_scene *G)
     d.obj = (const int4 *)G->obj.p;
     d.geo = (const float4 *)G->geo.p;
     d.fvert = (const float2 *)G->fvert.p;
+    d.fv4 = (const float4 *)G->fv4.p;
     d.cone = (const float *)G->cone.p;
     d.mat = (const float4 *)G->matd.p;
     d.src = (const gb_dsrc *)G->srcd.p;
@@ -401,6 +404,7 @@ static int build_arrays(gb_scene *G)
     std::vector<int4> obj(H.nobjs);
     std::vector<float4> geo(H.nobjs);
     std::vector<float2> fvert;
+    std::vector<float4> fv4(2 * (size_t)(H.nobjs > 0 ? H.nobjs : 1), make_float4(0, 0, 0, 0));
     std::vector<float> cone;
     for (int32_t i = 0; i < H.nobjs; i++) {
         const gb_object *o = &H.objs[i];
@@ -425,6 +429,15 @@ static int build_arrays(gb_scene *G)
             int xi = (f->ax + 1) % 3, yi = (xi + 1) % 3;
             for (int k = 0; k < nv; k++)
                 fvert.push_back(make_float2((float)o->farg[3 * k + xi], (float)o->farg[3 * k + yi]));
+            if (nv <= 4) {
+                float v[8] = {0};
+                for (int k = 0; k < nv; k++) {
+                    v[2 * k] = fvert[aux + k].x;
+                    v[2 * k + 1] = fvert[aux + k].y;
+                }
+                fv4[2 * i] = make_float4(v[0], v[1], v[2], v[3]);
+                fv4[2 * i + 1] = make_float4(v[4], v[5], v[6], v[7]);
+            }
             break;
         }
         case GT_SPHERE:
@@ -499,6 +512,7 @@ static int build_arrays(gb_scene *G)
     G->hobj.swap(obj);
     G->hgeo.swap(geo);
     G->hfvert.swap(fvert);
+    G->hfv4.swap(fv4);
     G->hcone.swap(cone);
     G->hsrc.swap(src);
     gb_dscene &d = G->ds;
@@ -516,6 +530,7 @@ static int build_arrays(gb_scene *G)
     d.obj = G->hobj.data();
     d.geo = G->hgeo.data();
     d.fvert = G->hfvert.data();
+    d.fv4 = G->hfv4.data();
     d.cone = G->hcone.data();
     d.mat = G->mat.data();
     d.nsrc = (int)G->src.size();
@@ -581,7 +596,7 @@ extern "C" void gb_scene_free(gb_scene *G)
 {
     if (!G)
         return;
-    DevBuf *bufs[] = {&G->kids, &G->setoff, &G->setdata, &G->obj, &G->geo, &G->fvert, &G->cone, &G->matd,
+    DevBuf *bufs[] = {&G->kids, &G->setoff, &G->setdata, &G->obj, &G->geo, &G->fvert, &G->fv4, &G->cone, &G->matd,
                       &G->srcd, &G->trk, &G->sensors, &G->value, &G->bins, &G->stats, &G->roots, &G->rootspt, &G->qa,
                       &G->qb, &G->qcount, &G->binprog, &G->modinfo, &G->hits, &G->hitt, &G->trkrun, &G->hitrec};
     for (DevBuf *b : bufs)

@@ -123,11 +123,44 @@ GB_DFN bool in_face(const float2 *__restrict__ v, int nv, float x, float y)
     return ncross & 1;
 }
 
-/* rt/o_face.c:15-62 */
-GB_DFN void hit_face(const gb_dscene &S, int obj, int4 od, float3 org, float3 dir,
-                                         Hit &best, float tmin)
+/* in_face for a triangle or quadrilateral whose projected vertices are in
+ * registers (va: v0 v1, vb: v2 v3); the same arithmetic in the same order */
+GB_DFN bool in_face4(float4 va, float4 vb, int nv, float x, float y)
 {
-    float4 pl = S.geo[obj];
+    const float2 v[4] = {make_float2(va.x, va.y), make_float2(va.z, va.w), make_float2(vb.x, vb.y),
+                         make_float2(vb.z, vb.w)};
+    int ncross = 0;
+    float2 p0 = nv == 3 ? v[2] : v[3];
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        if (k >= nv)
+            break;
+        float2 p1 = v[k];
+        if ((fabsf(p0.y - y) <= D_FTINY) & (fabsf(p1.y - y) <= D_FTINY) & ((p0.x > x) ^ (p1.x > x)))
+            return true;                                           /* edge case #1 */
+        if ((p0.y > y) ^ (p1.y > y)) {
+            int tst = (p0.x > x) + (p1.x > x);
+            if (tst == 2)
+                ncross++;
+            else if (tst) {
+                float prodA = (p0.y - y) * (p1.x - x);
+                float prodB = (p0.x - x) * (p1.y - y);
+                if (fabsf(prodA - prodB) <= D_FTINY)
+                    return true;                                   /* edge case #2 */
+                ncross += (p1.y > p0.y) ^ (prodA > prodB);
+            } else if ((fabsf(p0.x - x) <= D_FTINY) & (fabsf(p1.x - x) <= D_FTINY))
+                return true;                                       /* edge case #3 */
+        }
+        p0 = p1;
+    }
+    return ncross & 1;
+}
+
+/* rt/o_face.c:15-62; pl is the face's plane, va/vb its first four projected
+ * vertices (used when it has at most four) */
+GB_DFN void hit_face(const gb_dscene &S, int obj, int4 od, float4 pl, float4 va, float4 vb, float3 org,
+                     float3 dir, Hit &best, float tmin)
+{
     float3 n = f3(pl.x, pl.y, pl.z);
     float rdot = -dot3(dir, n);
     if ((rdot <= D_FTINY) & (rdot >= -D_FTINY))
@@ -139,7 +172,10 @@ GB_DFN void hit_face(const gb_dscene &S, int obj, int4 od, float3 org, float3 di
     int ax = ((od.x >> 8) >> DF_AXSHIFT) & 3;
     int xi = ax + 1 >= 3 ? ax - 2 : ax + 1;
     int yi = xi + 1 >= 3 ? xi - 2 : xi + 1;
-    if (!in_face(S.fvert + od.w, (od.x >> 16) & 0xffff, comp(p, xi), comp(p, yi)))
+    const int nv = (od.x >> 16) & 0xffff;
+    const bool in = nv <= 4 ? in_face4(va, vb, nv, comp(p, xi), comp(p, yi))
+                            : in_face(S.fvert + od.w, nv, comp(p, xi), comp(p, yi));
+    if (!in)
         return;
     best.obj = obj;
     best.t = t;
@@ -325,11 +361,15 @@ GB_DNI void hit_cone(const gb_dscene &S, int obj, int kind, int ci, float3 org,
 GB_DFN void hit_object(const gb_dscene &S, int obj, float3 org, float3 dir, Hit &best,
                                            float tmin, bool self = false)
 {
-    int4 od = S.obj[obj];
+    /* the object record, plane and packed vertices depend on obj alone, so
+     * all four loads are issued together */
+    const int4 od = GB_LDG(S.obj + obj);
+    const float4 pl = GB_LDG(S.geo + obj);
+    const float4 va = GB_LDG(S.fv4 + 2 * obj), vb = GB_LDG(S.fv4 + 2 * obj + 1);
     int kind = od.x & 0xff;
     switch (kind) {
     case DK_FACE:
-        hit_face(S, obj, od, org, dir, best, tmin);
+        hit_face(S, obj, od, pl, va, vb, org, dir, best, tmin);
         break;
     case DK_SPHERE:
     case DK_BUBBLE: {                   /* out of line: a copy, so that the */
