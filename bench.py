@@ -196,10 +196,10 @@ def reference_arm(args):
 
 # ---------------------------------------------------------------- GPU arm
 
-def traffic_from_profiles():
+def traffic_from_profiles(kernel: str):
     """Per-launch DRAM bytes of the dominant kernel from the committed ncu
     summary, if one exists."""
-    p = ROOT / "profiles" / "k_gen_root_rcontrib_window_room_traffic.txt"
+    p = ROOT / "profiles" / f"k_{kernel}_rcontrib_window_room_traffic.txt"
     if not p.exists():
         return None
     for ln in p.read_text().splitlines():
@@ -349,7 +349,7 @@ def gpu_arm(args):
         ms_per_launch = d["ms"] / d["launches"]
         achieved = bytes_per_launch / (ms_per_launch / 1e3) / 1e9
         peak, peak_kind = peaks()
-        traffic = traffic_from_profiles()
+        traffic = traffic_from_profiles(dom)
         cpu_v, cores, sample = cpu_baseline(rad, rays, seconds=12.0) if not args.no_cpu else (None, 0, "skipped")
         value = rays_all / dev_s / 1e6
         e2e = rays_all / wall_s / 1e6
