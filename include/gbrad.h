@@ -121,6 +121,28 @@ int  gb_rtrace(gb_scene *scene, const gb_opts *opts, const double *org_dir, int6
 int  gb_rtrace_device_noalloc(gb_scene *scene, const gb_opts *opts, const double *d_org_dir, int64_t n,
                               double *d_rgb);
 
+/* Material parameters.  Every material the scene's surfaces use has a
+ * slot; gb_scene_material_rgb reads (get_rgb) and/or replaces (set_rgb) its
+ * colour: the reflectance of plastic and metal, the transmissivity of
+ * glass, the radiance of light and glow.  A new colour takes effect in the
+ * next call on the scene.  No counterpart in the reference (its materials
+ * are fixed when the octree is read). */
+int64_t gb_scene_material_slots(const gb_scene *scene);
+int  gb_scene_material_slot(const gb_scene *scene, const char *name, int *slot);
+int  gb_scene_material_rgb(gb_scene *scene, int slot, double *get_rgb, const double *set_rgb);
+
+/* Gradient of sum_i dl_dvalue[i] . value[i] -- value being gb_rtrace's -ov
+ * output for the same rays and options (with -I, the sensor irradiance) --
+ * with respect to the colour of every material slot (grad: nslots x 3,
+ * nslots = gb_scene_material_slots): plastic and metal reflectance through
+ * their diffuse terms, glass transmissivity through rt/glass.c's
+ * transmission and reflection coefficients.  The paths are replayed from the
+ * same random streams as the forward call (options, seed and replica must be
+ * the same), sampling decisions held fixed.  No counterpart in the
+ * reference. */
+int  gb_rtrace_grad(gb_scene *scene, const gb_opts *opts, const double *org_dir, int64_t n,
+                    const double *dl_dvalue, double *grad, int64_t nslots);
+
 /* rcontrib: out has (n / opts->c) records x (sum of nbins) x 3 doubles,
  * modifiers in the given order (rt/rcontrib.c:379-427, rt/rc2.c:294-357).
  * ray_count (optional) receives the number of rays traced. */

@@ -63,6 +63,11 @@ _SIGS = {
     "gb_rtrace": (C.c_int, [C.c_void_p, C.POINTER(GbOpts), C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p,
                             C.c_void_p]),
     "gb_rtrace_device_noalloc": (C.c_int, [C.c_void_p, C.POINTER(GbOpts), C.c_void_p, C.c_int64, C.c_void_p]),
+    "gb_rtrace_grad": (C.c_int, [C.c_void_p, C.POINTER(GbOpts), C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p,
+                                 C.c_int64]),
+    "gb_scene_material_slots": (C.c_int64, [C.c_void_p]),
+    "gb_scene_material_slot": (C.c_int, [C.c_void_p, C.c_char_p, C.POINTER(C.c_int)]),
+    "gb_scene_material_rgb": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]),
     "gb_rcontrib": (C.c_int, [C.c_void_p, C.POINTER(GbOpts), C.POINTER(GbModspec), C.c_int, C.c_void_p,
                               C.c_int64, C.c_void_p, C.POINTER(C.c_int64)]),
     "gb_rcontrib_nbins": (C.c_int, [C.POINTER(GbModspec), C.c_int, C.POINTER(C.c_int)]),
@@ -166,6 +171,18 @@ class Scene:
 
     def material_name(self, i: int) -> str:
         return lib().gb_scene_material_name(self._h, i).decode()
+
+    def material_slot(self, name: str) -> int:
+        sl = C.c_int(-1)
+        check(lib().gb_scene_material_slot(self._h, name.encode(), C.byref(sl)))
+        return sl.value
+
+    def material_rgb(self, slot: int, rgb=None) -> np.ndarray:
+        """The colour of a material slot; replaced by rgb when given."""
+        old = np.zeros(3)
+        new = None if rgb is None else np.ascontiguousarray(rgb, dtype=np.float64)
+        check(lib().gb_scene_material_rgb(self._h, slot, ptr(old), ptr(new)))
+        return old
 
     def close(self) -> None:
         if self._h:

@@ -105,7 +105,7 @@ struct gb_scene {
     gb_dscene ds;
     /* work buffers */
     DevBuf sensors, value, bins, stats, roots, rootspt, qa, qb, qcount, binprog, modinfo, hits, hitt, trkrun,
-        hitrec;
+        hitrec, adja, adjb, dlde, gradd;
     cudaStream_t stream = nullptr;
     int sms = 0;
     cudaEvent_t ev[2 * GB_TIMED_LAUNCHES + 2];
@@ -598,7 +598,8 @@ extern "C" void gb_scene_free(gb_scene *G)
         return;
     DevBuf *bufs[] = {&G->kids, &G->setoff, &G->setdata, &G->obj, &G->geo, &G->fvert, &G->fv4, &G->cone, &G->matd,
                       &G->srcd, &G->trk, &G->sensors, &G->value, &G->bins, &G->stats, &G->roots, &G->rootspt, &G->qa,
-                      &G->qb, &G->qcount, &G->binprog, &G->modinfo, &G->hits, &G->hitt, &G->trkrun, &G->hitrec};
+                      &G->qb, &G->qcount, &G->binprog, &G->modinfo, &G->hits, &G->hitt, &G->trkrun, &G->hitrec,
+                      &G->adja, &G->adjb, &G->dlde, &G->gradd};
     for (DevBuf *b : bufs)
         b->release();
     if (G->stream)
@@ -837,6 +838,8 @@ struct RunOut {
     double *bins;           /* host records x nbins x 3 or null */
     int32_t *hit_id;
     double *hit_t;
+    const double *dlde;     /* gradient runs: host n x 3 d(loss)/d(value) */
+    double *grad;           /* gradient runs: host nslots x 3 */
 };
 
 static int run(gb_scene *G, const gb_opts *o, int follow, const double *org_dir, int64_t n,
@@ -962,7 +965,9 @@ static int run(gb_scene *G, const gb_opts *o, int follow, const double *org_dir,
     long long qcap = est < (1ll << 20) ? (1ll << 20) : est;
     size_t freeb = 0, totalb = 0;
     cudaMemGetInfo(&freeb, &totalb);
-    const size_t slot = 2 * sizeof(gb_qray) + sizeof(gb_qhit);   /* two queues and the walk results */
+    const bool grad = out.grad != nullptr;
+    /* two queues, the walk results, and in gradient runs the factor lists */
+    const size_t slot = 2 * sizeof(gb_qray) + sizeof(gb_qhit) + (grad ? 2 * sizeof(gb_qadj) : 0);
     long long qmax = (long long)(freeb / 3 / slot);
     if (qmax > (1ll << 28)) qmax = 1ll << 28;
     if (qcap > qmax) qcap = qmax;
@@ -971,6 +976,18 @@ static int run(gb_scene *G, const gb_opts *o, int follow, const double *org_dir,
         return set_err(GB_ENOMEM, "cannot allocate %lld-ray work queues", qcap);
     P.qcap = qcap;
     P.hits = (gb_qhit *)G->hitrec.p;
+    const int nslots = (int)(G->mat.size() / 2);
+    if (grad) {
+        if (G->adja.ensure((size_t)qcap * sizeof(gb_qadj)) < 0 || G->adjb.ensure((size_t)qcap * sizeof(gb_qadj)) < 0 ||
+            G->dlde.ensure((size_t)n * 3 * sizeof(double)) < 0 || G->gradd.ensure((size_t)nslots * 3 * sizeof(double)) < 0)
+            return set_err(GB_ENOMEM, "cannot allocate the gradient buffers");
+        CK(cudaMemcpyAsync(G->dlde.p, out.dlde, (size_t)n * 3 * sizeof(double), cudaMemcpyHostToDevice, st));
+        CK(cudaMemsetAsync(G->gradd.p, 0, (size_t)nslots * 3 * sizeof(double), st));
+        P.dlde = (const double *)G->dlde.p;
+        P.grad = (double *)G->gradd.p;
+        P.nslots = nslots;
+    }
+    gb_qadj *adja = (gb_qadj *)G->adja.p, *adjb = (gb_qadj *)G->adjb.p;
     unsigned long long *cnt = (unsigned long long *)G->qcount.p;   /* [0] A, [1] B, [2] work items */
     CK(cudaMemsetAsync(cnt, 0, 3 * sizeof(unsigned long long), st));
     P.work = cnt + 2;
@@ -979,6 +996,7 @@ static int run(gb_scene *G, const gb_opts *o, int follow, const double *org_dir,
     /* the first generation's queue: -I hemisphere rays or primaries */
     P.qout = qa;
     P.qout_count = cnt;
+    P.adj_out = adja;
     CK(cudaEventRecord(G->ev[0], st));
     if (o->I) {
         if (n0 > 0) {
@@ -989,16 +1007,19 @@ static int run(gb_scene *G, const gb_opts *o, int follow, const double *org_dir,
             P.root_spt = (float2 *)G->rootspt.p;
         }
         P.root_n = n0;
-        int rc = launch(GB_K_ROOT, P, [&](gb_run &R) { return gb_launch_root(&R, st, G->sms); });
+        int rc = launch(GB_K_ROOT, P, [&](gb_run &R) {
+            return grad ? gb_launch_root_grad(&R, st, G->sms) : gb_launch_root(&R, st, G->sms); });
         if (rc < 0)
             return rc;
         if (n0 > 0) {
-            rc = launch(GB_K_EXPAND, P, [&](gb_run &R) { return gb_launch_expand_root(&R, st, G->sms); });
+            rc = launch(GB_K_EXPAND, P, [&](gb_run &R) {
+                return grad ? gb_launch_expand_root_grad(&R, st, G->sms) : gb_launch_expand_root(&R, st, G->sms); });
             if (rc < 0)
                 return rc;
         }
     } else {
-        int rc = launch(GB_K_PRIMARY, P, [&](gb_run &R) { return gb_launch_primary(&R, st, G->sms); });
+        int rc = launch(GB_K_PRIMARY, P, [&](gb_run &R) {
+            return grad ? gb_launch_primary_grad(&R, st, G->sms) : gb_launch_primary(&R, st, G->sms); });
         if (rc < 0)
             return rc;
     }
@@ -1016,13 +1037,16 @@ static int run(gb_scene *G, const gb_opts *o, int follow, const double *org_dir,
         P.qin_count = cnt + in;
         P.qout = in ? qa : qb;
         P.qout_count = cnt + (1 - in);
+        P.adj_in = in ? adjb : adja;
+        P.adj_out = in ? adja : adjb;
         CK(cudaMemsetAsync(cnt + (1 - in), 0, sizeof(unsigned long long), st));
         CK(cudaMemsetAsync(P.work, 0, sizeof(unsigned long long), st));
         int rc = launch(GB_K_TRACE, P, [&](gb_run &R) { return gb_launch_trace(&R, st, G->sms); });
         if (rc < 0)
             return rc;
         CK(cudaMemsetAsync(P.work, 0, sizeof(unsigned long long), st));
-        rc = launch(GB_K_SHADE, P, [&](gb_run &R) { return gb_launch_shade(&R, st, G->sms); });
+        rc = launch(GB_K_SHADE, P, [&](gb_run &R) {
+            return grad ? gb_launch_shade_grad(&R, st, G->sms) : gb_launch_shade(&R, st, G->sms); });
         if (rc < 0)
             return rc;
         CK(cudaMemsetAsync(cnt + in, 0, sizeof(unsigned long long), st));
@@ -1036,6 +1060,8 @@ static int run(gb_scene *G, const gb_opts *o, int follow, const double *org_dir,
     if (out.bins && nrec > 0)
         CK(cudaMemcpyAsync(out.bins, G->bins.p, (size_t)nrec * nbins_total * 3 * sizeof(double),
                            cudaMemcpyDeviceToHost, st));
+    if (grad)
+        CK(cudaMemcpyAsync(out.grad, G->gradd.p, (size_t)nslots * 3 * sizeof(double), cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
     unsigned long long overflow = 0;
     for (int k = 0; k < GB_K_N; k++) {
@@ -1070,8 +1096,60 @@ extern "C" int gb_rtrace(gb_scene *G, const gb_opts *o, const double *org_dir, i
         if (rc < 0)
             return rc;
     }
-    RunOut out = {out_rgb, nullptr, hit_id, hit_t};
+    RunOut out = {out_rgb, nullptr, hit_id, hit_t, nullptr, nullptr};
     return run(G, o, 0, org_dir, n, nullptr, nullptr, 0, nullptr, out);
+}
+
+extern "C" int gb_rtrace_grad(gb_scene *G, const gb_opts *o, const double *org_dir, int64_t n,
+                              const double *dl_dvalue, double *grad, int64_t nslots)
+{
+    if (!G || !o || (n > 0 && (!org_dir || !dl_dvalue)) || !grad)
+        return set_err(GB_EINVAL, "null argument");
+    if (nslots != (int64_t)G->matobj.size())
+        return set_err(GB_EINVAL, "the gradient has %lld material slots, the scene %lld", (long long)nslots,
+                       (long long)G->matobj.size());
+    int rc = check_shading(G, o);
+    if (rc < 0)
+        return rc;
+    memset(grad, 0, (size_t)nslots * 3 * sizeof(double));
+    if (nslots == 0)
+        return GB_OK;
+    RunOut out = {nullptr, nullptr, nullptr, nullptr, dl_dvalue, grad};
+    return run(G, o, 0, org_dir, n, nullptr, nullptr, 0, nullptr, out);
+}
+
+extern "C" int64_t gb_scene_material_slots(const gb_scene *G) { return G ? (int64_t)G->matobj.size() : 0; }
+
+extern "C" int gb_scene_material_slot(const gb_scene *G, const char *name, int *slot)
+{
+    if (!G || !name || !slot)
+        return set_err(GB_EINVAL, "null argument");
+    for (size_t sl = 0; sl < G->matobj.size(); sl++)
+        if (!strcmp(G->H.objs[G->matobj[sl]].name, name)) {
+            *slot = (int)sl;
+            return GB_OK;
+        }
+    return set_err(GB_EINVAL, "no material '%s' in the scene", name);
+}
+
+extern "C" int gb_scene_material_rgb(gb_scene *G, int slot, double *get_rgb, const double *set_rgb)
+{
+    if (!G || slot < 0 || slot >= (int)G->matobj.size())
+        return set_err(GB_EINVAL, "bad material slot %d", slot);
+    float4 &m0 = G->mat[2 * (size_t)slot];
+    if (get_rgb) {
+        get_rgb[0] = m0.y;
+        get_rgb[1] = m0.z;
+        get_rgb[2] = m0.w;
+    }
+    if (set_rgb) {
+        m0.y = (float)set_rgb[0];
+        m0.z = (float)set_rgb[1];
+        m0.w = (float)set_rgb[2];
+        if (G->matd.p)
+            CK(cudaMemcpy((float4 *)G->matd.p + 2 * (size_t)slot, &m0, sizeof(float4), cudaMemcpyHostToDevice));
+    }
+    return GB_OK;
 }
 
 static int compile_mods(gb_scene *G, const gb_modspec *mods, int nmods, std::vector<gb_binins> &prog,
@@ -1149,7 +1227,7 @@ extern "C" int gb_rcontrib(gb_scene *G, const gb_opts *o, const gb_modspec *mods
                 return set_err(GB_EUNSUPPORTED, "-V with a non-emitting tracked modifier is not implemented");
         }
     }
-    RunOut ro = {nullptr, out, nullptr, nullptr};
+    RunOut ro = {nullptr, out, nullptr, nullptr, nullptr, nullptr};
     rc = run(G, &oo, 1, org_dir, n, &prog, &info, nbt, &trk, ro);
     if (ray_count)
         *ray_count = g_stats[0];

@@ -50,6 +50,7 @@ struct Ray {
     int rlvl, adepth;
     uint64_t path;
     uint32_t sensor;
+    gb_qadj adj;            /* gradient runs only: parameter factors of the path */
 };
 
 struct Counters {
@@ -109,6 +110,7 @@ __device__ __forceinline__ Ray load_ray(const gb_qray *q)
     return r;
 }
 
+template <bool G = false>
 __device__ __forceinline__ void push_ray(const gb_run &P, const Ray &r)
 {
     cg::coalesced_group g = cg::coalesced_threads();
@@ -116,10 +118,114 @@ __device__ __forceinline__ void push_ray(const gb_run &P, const Ray &r)
     if (g.thread_rank() == 0)
         base = atomicAdd(P.qout_count, (unsigned long long)g.size());
     base = g.shfl(base, 0) + g.thread_rank();
-    if (base < (unsigned long long)P.qcap)
+    if (base < (unsigned long long)P.qcap) {
         store_ray(P.qout + base, r);
-    else if (g.thread_rank() == 0)
+        if (G)
+            P.adj_out[base] = r.adj;
+    } else if (g.thread_rank() == 0)
         atomicAdd(P.stats + ST_OVERFLOW, 1ull);
+}
+
+/* ------------------------------------------------------------ gradients
+ *
+ * A gradient run replays the forward run (same random streams, so the same
+ * rays) and, wherever the forward adds a contribution v to a sensor's value,
+ * adds w * v * d(ln f)/d(theta) for every parameter-dependent factor f on
+ * the contribution's path, w being d(loss)/d(value) of that sensor: the
+ * diffuse reflectance of each plastic or metal bounce (f = rho, so
+ * d ln f / d rho = 1 / rho) and each transmission through or reflection off
+ * glass (f = the rt/glass.c:45-165 coefficient as a function of the
+ * transmissivity).  Sampling decisions (Russian roulette, hemisphere sizes)
+ * are held fixed.  Accumulators: per block in shared memory when the slots
+ * fit, flushed once per block. */
+extern __shared__ double grad_smem[];
+
+__device__ __forceinline__ void adj_append(gb_qadj &a, int slot, uint32_t kind, float pd)
+{
+    if (a.n < GB_ADJ_MAX) {
+        a.e[a.n] = ((uint32_t)slot << 2) | kind;
+        a.pd[a.n] = pd;
+        a.n++;
+    } else {
+        a.n = GB_ADJ_MAX + 1;                /* too long: contributes no gradient */
+    }
+}
+
+/* d ln(coefficient) / d(parameter) of one factor, per channel */
+__device__ float3 adj_dlog(const gb_run &P, uint32_t e, float pd)
+{
+    const int slot = (int)(e >> 2);
+    const uint32_t kind = e & 3u;
+    const float4 m0 = P.S.mat[2 * slot], m1 = P.S.mat[2 * slot + 1];
+    const float c[3] = {m0.y, m0.z, m0.w};
+    float out[3];
+    if (kind == GB_ADJ_REFL) {
+        for (int i = 0; i < 3; i++)
+            out[i] = c[i] > 0.f ? 1.f / c[i] : 0.f;
+        return f3(out[0], out[1], out[2]);
+    }
+    const float rindex = m1.x, pdot = pd;
+    const float cos2 = sqrtf((1.f - 1.f / (rindex * rindex)) + pdot * pdot / (rindex * rindex));
+    float r1e = (pdot - rindex * cos2) / (pdot + rindex * cos2);
+    r1e *= r1e;
+    float r1m = (1.f / pdot - rindex / cos2) / (1.f / pdot + rindex / cos2);
+    r1m *= r1m;
+    for (int i = 0; i < 3; i++) {
+        const float tau = fmaxf(c[i], 1e-15f);
+        const float d = powf(tau, 1.f / cos2), dd = d / (cos2 * tau);
+        const float qe = 1.f - r1e * r1e * d * d, qm = 1.f - r1m * r1m * d * d;
+        float f, df;
+        if (kind == GB_ADJ_GLASST) {
+            f = .5f * (1.f - r1e) * (1.f - r1e) * d / qe + .5f * (1.f - r1m) * (1.f - r1m) * d / qm;
+            df = .5f * (1.f - r1e) * (1.f - r1e) * (1.f + r1e * r1e * d * d) / (qe * qe) +
+                 .5f * (1.f - r1m) * (1.f - r1m) * (1.f + r1m * r1m * d * d) / (qm * qm);
+        } else {
+            f = .5f * r1e * (1.f + (1.f - 2.f * r1e) * d * d) / qe + .5f * r1m * (1.f + (1.f - 2.f * r1m) * d * d) / qm;
+            df = r1e * d * (1.f - r1e) * (1.f - r1e) / (qe * qe) + r1m * d * (1.f - r1m) * (1.f - r1m) / (qm * qm);
+        }
+        out[i] = f > 0.f ? df * dd / f : 0.f;
+    }
+    return f3(out[0], out[1], out[2]);
+}
+
+__device__ __forceinline__ void grad_slot_add(const gb_run &P, int slot, float3 g)
+{
+    double *acc = P.grad_shared ? grad_smem : P.grad;
+    if (g.x != 0.f) atomicAdd(acc + 3 * slot, (double)g.x);
+    if (g.y != 0.f) atomicAdd(acc + 3 * slot + 1, (double)g.y);
+    if (g.z != 0.f) atomicAdd(acc + 3 * slot + 2, (double)g.z);
+}
+
+/* the gradient of a contribution v to sensor `sensor` along factor list a */
+__device__ void grad_add(const gb_run &P, uint32_t sensor, float3 v, const gb_qadj &a)
+{
+    if (a.n == 0 || a.n > GB_ADJ_MAX)
+        return;
+    const double *w = P.dlde + 3ull * sensor;
+    const float3 wv = f3((float)w[0] * v.x, (float)w[1] * v.y, (float)w[2] * v.z);
+    if (wv.x == 0.f && wv.y == 0.f && wv.z == 0.f)
+        return;
+    for (uint32_t i = 0; i < a.n; i++)
+        grad_slot_add(P, (int)(a.e[i] >> 2), wv * adj_dlog(P, a.e[i], a.pd[i]));
+}
+
+__device__ __forceinline__ void grad_begin(const gb_run &P)
+{
+    if (!P.grad_shared)
+        return;
+    for (int i = threadIdx.x; i < 3 * P.nslots; i += blockDim.x)
+        grad_smem[i] = 0.0;
+    __syncthreads();
+}
+
+__device__ __forceinline__ void grad_end(const gb_run &P)
+{
+    if (!P.grad_shared)
+        return;
+    __syncthreads();
+    for (int i = threadIdx.x; i < 3 * P.nslots; i += blockDim.x)
+        if (grad_smem[i] != 0.0)
+            atomicAdd(P.grad + i, grad_smem[i]);
 }
 
 /* ------------------------------------------------------- contributions */
@@ -175,6 +281,7 @@ __device__ __forceinline__ void add_bin(const gb_run &P, uint32_t sensor, int sl
 
 /* rt/source.c:749-793 (m_light) for a ray r that hit light object obj;
  * returns the radiance it carries (rcol) and applies rcontrib's callback */
+template <bool G = false>
 __device__ __forceinline__ void light_hit(const gb_run &P, const Ray &r, int obj, int ms, float t, float rod,
                                           Counters &cnt, float3 *rcol_out)
 {
@@ -195,8 +302,12 @@ __device__ __forceinline__ void light_hit(const gb_run &P, const Ray &r, int obj
     if (rcol_out)
         *rcol_out = rcol;
     if (!(bad || wrong)) {
-        if (r.rsrc < 0)                  /* shadow values are added by direct() */
-            add_value(P, r.sensor, rc * rcol);
+        if (r.rsrc < 0) {                /* shadow values are added by direct() */
+            if (G)
+                grad_add(P, r.sensor, rc * rcol, r.adj);
+            else
+                add_value(P, r.sensor, rc * rcol);
+        }
         if (P.binprog) {
             int slot = S.trk[obj];
             if (slot >= 0 && (r.rsrc < 0 || S.src[r.rsrc].so == obj) && r.lcoef > D_FTINY) {
@@ -390,7 +501,9 @@ __device__ __noinline__ void place_hemi(const gb_run &P, const Ray &parent, cons
 /* Spawn all children of a hemisphere of 4 x 4 strata or more met after the
  * first generation: placed sequentially with collision avoidance and
  * queued as they are placed (only two rows of positions are kept). */
-__device__ __noinline__ void spawn_hemi_big(const gb_run &P, const Ray &parent, const Hemi &h, float3 hp, int origin)
+template <bool G = false>
+__device__ __noinline__ void spawn_hemi_big(const gb_run &P, const Ray &parent, const Hemi &h, float3 hp, int origin,
+                                            int slot)
 {
     gb_lot L;
     float rows[2][MAX_HEMI_N][2];
@@ -419,7 +532,11 @@ __device__ __noinline__ void spawn_hemi_big(const gb_run &P, const Ray &parent, 
                 c.org = hp;
                 c.origin = origin;
                 c.adepth = parent.adepth + 1;
-                push_ray(P, c);
+                if (G) {
+                    c.adj = parent.adj;
+                    adj_append(c.adj, slot, GB_ADJ_REFL, 0.f);
+                }
+                push_ray<G>(P, c);
             }
             cur[j][0] = sp[0];
             cur[j][1] = sp[1];
@@ -441,7 +558,8 @@ struct Surf {                 /* rt/normal.c NORMDAT */
 };
 
 /* rt/normal.c:72-173 dirnorm (opaque materials: trans = 0) */
-__device__ __forceinline__ float3 dirnorm(const gb_run &P, const Surf &s, float3 rdir, float3 ldir, float omega)
+__device__ __forceinline__ float3 dirnorm(const gb_run &P, const Surf &s, float3 rdir, float3 ldir, float omega,
+                                          float3 *diffuse = nullptr)
 {
     float3 v = f3(0.f, 0.f, 0.f);
     float ldot = dot3(s.pnorm, ldir);
@@ -452,6 +570,8 @@ __device__ __forceinline__ float3 dirnorm(const gb_run &P, const Surf &s, float3
         lrdiff *= 1.f - fresne(fabsf(ldot));
     if ((ldot > D_FTINY) & (lrdiff > D_FTINY))
         v = v + s.mcolor * (ldot * omega * lrdiff * (1.f / D_PI));
+    if (diffuse)
+        *diffuse = v;
     if ((ldot > D_FTINY) & s.refl & !s.pure) {
         float dt = s.alpha2;
         if (s.flat)
@@ -473,7 +593,9 @@ __device__ __forceinline__ float3 dirnorm(const gb_run &P, const Surf &s, float3
  * to the ray's colour (scp->val): the potential when the first ray reaches
  * the source or nothing, else coefficient x transmission x source radiance;
  * applies the rcontrib callback to every ray of the chain. */
-__device__ float3 shadow_chain(const gb_run &P, Ray sr, int s, Counters &cnt, float3 coef, float3 potential)
+template <bool G = false>
+__device__ float3 shadow_chain(const gb_run &P, Ray sr, int s, Counters &cnt, float3 coef, float3 potential,
+                               gb_qadj *factors)
 {
     const gb_dscene &S = P.S;
     const gb_dsrc &src = S.src[s];
@@ -549,6 +671,8 @@ __device__ float3 shadow_chain(const gb_run &P, Ray sr, int s, Counters &cnt, fl
             c.dir = sr.dir;
             c.origin = h.obj;
             T = T * tcv;
+            if (G)
+                adj_append(*factors, ms, GB_ADJ_GLASST, pdot);
             sr = c;
             continue;
         }
@@ -561,7 +685,9 @@ __device__ float3 shadow_chain(const gb_run &P, Ray sr, int s, Counters &cnt, fl
 
 /* rt/source.c:398-556 (direct) with single-partition sources
  * (nextssamp/nopart) and every shadow tested */
-__device__ void direct(const gb_run &P, const Ray &r, float3 hp, const Surf &s, int origin, Counters &cnt)
+template <bool G = false>
+__device__ void direct(const gb_run &P, const Ray &r, float3 hp, const Surf &s, int origin, Counters &cnt,
+                       int slot)
 {
     const gb_dscene &S = P.S;
     for (int sn = 0; sn < S.nsrc; sn++) {
@@ -614,7 +740,8 @@ __device__ void direct(const gb_run &P, const Ray &r, float3 hp, const Surf &s, 
             if ((src.flags & DS_PROX) && dist > src.prox)
                 continue;
         }
-        float3 coef = dirnorm(P, s, r.dir, dir, dom);
+        float3 coefd;
+        float3 coef = dirnorm(P, s, r.dir, dir, dom, G ? &coefd : nullptr);
         if (maxc(coef) <= 0.f)
             continue;
         /* potential (srcvalue): the source alone */
@@ -648,8 +775,22 @@ __device__ void direct(const gb_run &P, const Ray &r, float3 hp, const Surf &s, 
         sr.org = hp;
         sr.dir = dir;
         sr.origin = origin;
-        float3 v = shadow_chain(P, sr, sn, cnt, coef, pot);
-        add_value(P, r.sensor, r.coef * v);
+        if (!G) {
+            float3 v = shadow_chain(P, sr, sn, cnt, coef, pot, nullptr);
+            add_value(P, r.sensor, r.coef * v);
+            continue;
+        }
+        gb_qadj fac = r.adj;                   /* the path's factors and the shadow's glass */
+        const float3 c = r.coef * shadow_chain<true>(P, sr, sn, cnt, coef, pot, &fac);
+        grad_add(P, r.sensor, c, fac);
+        if (slot >= 0 && fac.n <= GB_ADJ_MAX) {  /* this surface's own reflectance: */
+            const double *w = P.dlde + 3ull * r.sensor;     /* the diffuse part of dirnorm */
+            float g[3], cc[3] = {c.x, c.y, c.z}, cd[3] = {coefd.x, coefd.y, coefd.z}, ct[3] = {coef.x, coef.y, coef.z};
+            float mc[3] = {s.mcolor.x, s.mcolor.y, s.mcolor.z};
+            for (int i = 0; i < 3; i++)
+                g[i] = (ct[i] > 0.f && mc[i] > 0.f) ? (float)w[i] * cc[i] * (cd[i] / ct[i]) / mc[i] : 0.f;
+            grad_slot_add(P, slot, f3(g[0], g[1], g[2]));
+        }
     }
 }
 
@@ -687,20 +828,21 @@ __device__ __forceinline__ void setup_surf(const gb_run &P, int mk, float4 m0, f
 /* Shade ray r given its trace result (h.obj < 0: the ray left the scene)
  * and push every child ray to the next generation's queue
  * (rt/raytrace.c:163-256 raytrace / rayshade, the material routines). */
+template <bool G>
 __device__ void shade_ray(const gb_run &P, const Ray &r, const Hit &h, Counters &cnt)
 {
     const gb_dscene &S = P.S;
     if (h.obj < 0) {
         int sidx = source_hit(S, r.dir, r.rsrc, r.crtype);
         if (sidx >= 0)
-            light_hit(P, r, S.src[sidx].so, S.src[sidx].mat, D_FHUGE, 1.f, cnt, nullptr);
+            light_hit<G>(P, r, S.src[sidx].so, S.src[sidx].mat, D_FHUGE, 1.f, cnt, nullptr);
         return;
     }
     int ms = S.obj[h.obj].y;
     int mk = ms >= 0 ? (int)S.mat[2 * ms].x : DM_NONE;
     float3 hp = r.org + r.dir * h.t;
     if (mk == DM_LIGHT || mk == DM_GLOW) {
-        light_hit(P, r, h.obj, ms, h.t, h.rod, cnt, nullptr);
+        light_hit<G>(P, r, h.obj, ms, h.t, h.rod, cnt, nullptr);
         return;
     }
     if (mk == DM_NONE) {
@@ -710,7 +852,9 @@ __device__ void shade_ray(const gb_run &P, const Ray &r, const Hit &h, Counters 
         c.org = hp;
         c.dir = r.dir;
         c.origin = h.obj;
-        push_ray(P, c);
+        if (G)
+            c.adj = r.adj;
+        push_ray<G>(P, c);
         return;
     }
     float4 m0 = S.mat[2 * ms], m1 = S.mat[2 * ms + 1];
@@ -749,7 +893,11 @@ __device__ void shade_ray(const gb_run &P, const Ray &r, const Hit &h, Counters 
                 c.org = hp;
                 c.dir = r.dir;
                 c.origin = h.obj;
-                push_ray(P, c);
+                if (G) {
+                    c.adj = r.adj;
+                    adj_append(c.adj, ms, GB_ADJ_GLASST, pdot);
+                }
+                push_ray<G>(P, c);
             }
         }
         Ray c;
@@ -757,7 +905,11 @@ __device__ void shade_ray(const gb_run &P, const Ray &r, const Hit &h, Counters 
             c.org = hp;
             c.dir = normalize3(r.dir + n * (2.f * pdot));
             c.origin = h.obj;
-            push_ray(P, c);
+            if (G) {
+                c.adj = r.adj;
+                adj_append(c.adj, ms, GB_ADJ_GLASSR, pdot);
+            }
+            push_ray<G>(P, c);
         }
         return;
     }
@@ -771,7 +923,9 @@ __device__ void shade_ray(const gb_run &P, const Ray &r, const Hit &h, Counters 
             c.org = hp;
             c.dir = normalize3(r.dir + su.pnorm * (2.f * su.pdot));
             c.origin = h.obj;
-            push_ray(P, c);
+            if (G)                               /* specular color: not a parameter */
+                c.adj = r.adj;
+            push_ray<G>(P, c);
         }
     }
     if (su.pure && su.rdiff <= D_FTINY)
@@ -783,13 +937,18 @@ __device__ void shade_ray(const gb_run &P, const Ray &r, const Hit &h, Counters 
         if (P.ad > 0 && r.adepth < P.ab) {
             Hemi hm;
             if (make_hemi(P, r, aval, n, hm) && hm.n >= 4) {
-                spawn_hemi_big(P, r, hm, hp, h.obj);
+                spawn_hemi_big<G>(P, r, hm, hp, h.obj, ms);
             } else if (hm.n > 0) {
                 int nn = hm.n * hm.n;
                 for (int k = 0; k < nn; k++) {
                     Ray c;
-                    if (hemi_child(P, r, hm, hp, h.obj, k, nullptr, c))
-                        push_ray(P, c);
+                    if (hemi_child(P, r, hm, hp, h.obj, k, nullptr, c)) {
+                        if (G) {
+                            c.adj = r.adj;
+                            adj_append(c.adj, ms, GB_ADJ_REFL, 0.f);
+                        }
+                        push_ray<G>(P, c);
+                    }
                 }
             }
         } else if (P.av[0] != 0.f || P.av[1] != 0.f || P.av[2] != 0.f) {
@@ -797,7 +956,7 @@ __device__ void shade_ray(const gb_run &P, const Ray &r, const Hit &h, Counters 
         }
     }
     if (S.nsrc > 0)
-        direct(P, r, hp, su, h.obj, cnt);
+        direct<G>(P, r, hp, su, h.obj, cnt, ms);
 }
 
 /* Persistent work loop: each warp takes work items 32 at a time with one
@@ -844,8 +1003,11 @@ __device__ __forceinline__ Hit load_hit(const gb_qhit *q)
 /* -------------------------------------------------------------- kernels */
 
 /* -I sensor: the Lambertian pretend-hit, its direct part and its frame */
+template <bool G>
 __global__ void k_root(gb_run P)
 {
+    if (G)
+        grad_begin(P);
     Counters cnt = {0, 0, 0, 0, 0};
     for (long long s = blockIdx.x * (long long)blockDim.x + threadIdx.x; s < P.nsensors;
          s += (long long)gridDim.x * blockDim.x) {
@@ -865,6 +1027,7 @@ __global__ void k_root(gb_run P)
         r.adepth = 0;
         r.path = GB_ROOT_PATH(P.replica);
         r.sensor = (uint32_t)s;
+        r.adj.n = 0;
         float3 hp = f3((float)(sv[0] + 1e-4 * sv[3]), (float)(sv[1] + 1e-4 * sv[4]), (float)(sv[2] + 1e-4 * sv[5]));
         Surf su;
         su.mcolor = f3(D_PI, D_PI, D_PI);
@@ -879,7 +1042,7 @@ __global__ void k_root(gb_run P)
         su.rblt = false;
         su.flat = false;
         if (P.S.nsrc > 0)
-            direct(P, r, hp, su, -1, cnt);
+            direct<G>(P, r, hp, su, -1, cnt, -1);
         if (P.root_n > 0) {
             Hemi hm;
             make_hemi(P, r, su.mcolor, dir, hm);
@@ -895,10 +1058,13 @@ __global__ void k_root(gb_run P)
         }
     }
     flush_counters(P, cnt);
+    if (G)
+        grad_end(P);
 }
 
 /* first hemisphere of every -I sensor: one ray per (sensor, stratum) into
  * the queue of the first generation */
+template <bool G>
 __global__ void __launch_bounds__(256) k_expand_root(gb_run P)
 {
     const long long nn = (long long)P.root_n * P.root_n;
@@ -936,13 +1102,16 @@ __global__ void __launch_bounds__(256) k_expand_root(gb_run P)
             sp = &pk.x;
         }
         Ray c;
-        if (hemi_child(P, parent, hm, parent.org, -1, k, sp, c))
-            push_ray(P, c);
+        if (hemi_child(P, parent, hm, parent.org, -1, k, sp, c)) {
+            c.adj.n = 0;                       /* the -I sensor is not a parameter */
+            push_ray<G>(P, c);
+        }
     });
 }
 
 /* radiance-mode primaries (rt/rtrace.c:436-468, rt/rcontrib.c:343-353)
  * into the queue of the first generation */
+template <bool G>
 __global__ void k_primary(gb_run P)
 {
     for (long long s = blockIdx.x * (long long)blockDim.x + threadIdx.x; s < P.nsensors;
@@ -961,7 +1130,8 @@ __global__ void k_primary(gb_run P)
         r.adepth = 0;
         r.path = GB_ROOT_PATH(P.replica);
         r.sensor = (uint32_t)s;
-        push_ray(P, r);
+        r.adj.n = 0;
+        push_ray<G>(P, r);
     }
 }
 
@@ -1038,18 +1208,25 @@ __global__ void __launch_bounds__(TRACE_BLOCK, 4) k_trace(gb_run P)
 
 /* One generation, second half: shade every traced ray and queue its
  * children for the next generation. */
+template <bool G>
 __global__ void __launch_bounds__(256) k_shade(gb_run P)
 {
+    if (G)
+        grad_begin(P);
     Counters cnt = {0, 0, 0, 0, 0};
     unsigned long long n = *P.qin_count;
     if (n > (unsigned long long)P.qcap)
         n = P.qcap;
     persistent_items(P.work, n, [&](unsigned long long g) {
-        const Ray r = load_ray(P.qin + g);
+        Ray r = load_ray(P.qin + g);
+        if (G)
+            r.adj = P.adj_in[g];
         const Hit h = load_hit(P.hits + g);
-        shade_ray(P, r, h, cnt);
+        shade_ray<G>(P, r, h, cnt);
     });
     flush_counters(P, cnt);
+    if (G)
+        grad_end(P);
 }
 
 /* castonly rtrace (rt/rtrace.c:398-411 raycast): first intersection only */
@@ -1105,9 +1282,27 @@ int gb_launch_cast(const gb_run *P, int *hit_obj, float *hit_t, float *hit_pn, c
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
+/* dynamic shared memory of a gradient launch: the per-block accumulators
+ * when the material slots fit in 32 KB, else none (global accumulation) */
+static size_t grad_smem_bytes(const gb_run *P, gb_run &R)
+{
+    R = *P;
+    size_t b = (size_t)P->nslots * 3 * sizeof(double);
+    R.grad_shared = b <= 32768;
+    return R.grad_shared ? b : 0;
+}
+
 int gb_launch_root(const gb_run *P, cudaStream_t st, int sms)
 {
-    k_root<<<grid_for(P->nsensors, 128, sms), 128, 0, st>>>(*P);
+    k_root<false><<<grid_for(P->nsensors, 128, sms), 128, 0, st>>>(*P);
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+int gb_launch_root_grad(const gb_run *P, cudaStream_t st, int sms)
+{
+    gb_run R;
+    size_t sm = grad_smem_bytes(P, R);
+    k_root<true><<<grid_for(P->nsensors, 128, sms), 128, sm, st>>>(R);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
@@ -1125,14 +1320,29 @@ int gb_launch_expand_root(const gb_run *P, cudaStream_t st, int sms)
 {
     static int grid = 0;
     if (!grid)
-        grid = resident_grid(k_expand_root, 256, sms);
-    k_expand_root<<<grid, 256, 0, st>>>(*P);
+        grid = resident_grid(k_expand_root<false>, 256, sms);
+    k_expand_root<false><<<grid, 256, 0, st>>>(*P);
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+int gb_launch_expand_root_grad(const gb_run *P, cudaStream_t st, int sms)
+{
+    static int grid = 0;
+    if (!grid)
+        grid = resident_grid(k_expand_root<true>, 256, sms);
+    k_expand_root<true><<<grid, 256, 0, st>>>(*P);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
 int gb_launch_primary(const gb_run *P, cudaStream_t st, int sms)
 {
-    k_primary<<<grid_for(P->nsensors, 128, sms), 128, 0, st>>>(*P);
+    k_primary<false><<<grid_for(P->nsensors, 128, sms), 128, 0, st>>>(*P);
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+int gb_launch_primary_grad(const gb_run *P, cudaStream_t st, int sms)
+{
+    k_primary<true><<<grid_for(P->nsensors, 128, sms), 128, 0, st>>>(*P);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
@@ -1149,7 +1359,18 @@ int gb_launch_shade(const gb_run *P, cudaStream_t st, int sms)
 {
     static int grid = 0;
     if (!grid)
-        grid = resident_grid(k_shade, 256, sms);
-    k_shade<<<grid, 256, 0, st>>>(*P);
+        grid = resident_grid(k_shade<false>, 256, sms);
+    k_shade<false><<<grid, 256, 0, st>>>(*P);
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+int gb_launch_shade_grad(const gb_run *P, cudaStream_t st, int sms)
+{
+    gb_run R;
+    size_t sm = grad_smem_bytes(P, R);
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_shade<true>, 256, sm) != cudaSuccess || per_sm < 1)
+        per_sm = 1;
+    k_shade<true><<<per_sm * sms, 256, sm, st>>>(R);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }

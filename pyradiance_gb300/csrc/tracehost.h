@@ -40,6 +40,20 @@ typedef struct __align__(16) {
     float v[8];
 } gb_qhit;
 
+/* the parameter-dependent factors along a queued ray's path (gradient
+ * runs): up to GB_ADJ_MAX entries (material slot << 2 | kind) and the
+ * cosine at each glass vertex */
+#define GB_ADJ_MAX 6
+#define GB_ADJ_REFL   0    /* diffuse reflectance of a plastic or metal */
+#define GB_ADJ_GLASST 1    /* transmission through glass */
+#define GB_ADJ_GLASSR 2    /* reflection off glass */
+typedef struct __align__(16) {
+    uint32_t n;
+    uint32_t e[GB_ADJ_MAX];
+    float pd[GB_ADJ_MAX];
+    uint32_t pad[3];
+} gb_qadj;
+
 /* first hemisphere of a -I sensor */
 typedef struct {
     float hp[3], nrm[3], ux[3];
@@ -79,6 +93,14 @@ typedef struct {
     gb_qray *qout;
     unsigned long long *qout_count;
     gb_qhit *hits;             /* walk results of qin, same indices */
+    /* gradient runs: d(loss)/d(value) per sensor, the gradient per material
+     * slot (RGB), and the factor lists beside the two queues */
+    const double *dlde;
+    double *grad;
+    int nslots;
+    int grad_shared;           /* set per launch: accumulators in shared memory */
+    const gb_qadj *adj_in;
+    gb_qadj *adj_out;
     long long qcap;
     unsigned long long *work;  /* work-item counter of the persistent kernels (zeroed per launch) */
 } gb_run;
@@ -89,5 +111,10 @@ int gb_launch_expand_root(const gb_run *P, cudaStream_t st, int sms);
 int gb_launch_primary(const gb_run *P, cudaStream_t st, int sms);
 int gb_launch_trace(const gb_run *P, cudaStream_t st, int sms);
 int gb_launch_shade(const gb_run *P, cudaStream_t st, int sms);
+/* gradient runs: the same kernels, shading with the factor lists */
+int gb_launch_root_grad(const gb_run *P, cudaStream_t st, int sms);
+int gb_launch_expand_root_grad(const gb_run *P, cudaStream_t st, int sms);
+int gb_launch_primary_grad(const gb_run *P, cudaStream_t st, int sms);
+int gb_launch_shade_grad(const gb_run *P, cudaStream_t st, int sms);
 
 #endif
