@@ -259,6 +259,51 @@ def dct_measure(dev, steps: int):
     return res
 
 
+GRAD_ARGS = ["-I+", "-ab", "2", "-ad", "1024", "-aa", "0", "-lw", "1e-4", "-u-"]
+
+
+def grad_measure(steps: int):
+    """Gradient of an irradiance loss with respect to 64 material RGB
+    reflectances and the glazing transmissivity (the window room with its
+    20,000 triangles in 64 materials, 4,096 sensors, -ab 2, 1,024 hemisphere
+    samples per sensor): the forward call and the path-replay gradient call,
+    each timed with CUDA events around the kernels (best of `steps`)."""
+    import ctypes as C
+    from pyradiance_gb300 import _lib
+    from pyradiance_gb300 import workloads as w
+    L = _lib.lib()
+    with tempfile.TemporaryDirectory() as td:
+        rad = Path(td) / "room64.rad"
+        rad.write_text(w.window_room(seed=0, ntri=20000, nmat=64))
+        import pyradiance_gb300 as gb
+        sc = gb.Scene(rad_files=[rad])
+    rays = np.ascontiguousarray(w.sensor_grid(64, 64))
+    rng = np.random.default_rng(5)
+    for m in range(64):
+        sc.material_rgb(sc.material_slot(f"tri_mat{m}"), rng.uniform(0.2, 0.8, 3))
+    o, _ = _lib.parse_opts(GRAD_ARGS, _lib.GB_PROG_RTRACE)
+    n = len(rays)
+    e = np.zeros((n, 3))
+    ns = int(L.gb_scene_material_slots(sc.handle))
+    g = np.zeros((ns, 3))
+    dl = np.full((n, 3), 1.0 / (3 * n))
+    fwd, bwd, rays_f = [], [], 0
+    for _ in range(max(3, steps)):
+        _lib.check(L.gb_rtrace(sc.handle, o, _lib.ptr(rays), n, _lib.ptr(e), None, None))
+        fwd.append(_lib.last_profile()["region_ms"])
+        rays_f = _lib.last_stats()["rays"]
+        _lib.check(L.gb_rtrace_grad(sc.handle, o, _lib.ptr(rays), n, _lib.ptr(dl), _lib.ptr(g), ns))
+        bwd.append(_lib.last_profile()["region_ms"])
+    f, b = min(fwd), min(bwd)
+    return {"workload": "window room, 20,000 triangles in 64 plastic materials + glass window, 4096 sensors, "
+                        "rtrace " + " ".join(GRAD_ARGS) + "; d(mean irradiance)/d(64 x RGB reflectance, "
+                        "glass transmissivity)",
+            "forward_ms": round(f, 3), "gradient_ms": round(b, 3), "rays_per_forward": int(rays_f),
+            "cost_ratio_forward_plus_gradient_vs_forward": round((f + b) / f, 3),
+            "note": "the gradient call replays the forward's paths; timed regions are the kernel regions "
+                    "(CUDA events); finite-difference agreement is checked in the GPU tests"}
+
+
 def combine_ranks(dev_s: float, wall_s: float, rays: float, world: int, device=None):
     """Whole-job figures of a multi-rank run: the slowest rank's device and
     wall seconds, and the rays of all ranks (the ranks trace independent
@@ -374,6 +419,7 @@ def gpu_arm(args):
                              "cores": cores, "kind": "port", "sample": sample},
             "clocks": ck,
             "dctimestep": dct_measure(dev, args.steps),
+            "gradient": grad_measure(args.steps),
         }
         print(json.dumps(line), flush=True)
 
