@@ -304,6 +304,63 @@ def grad_measure(steps: int):
                     "(CUDA events); finite-difference agreement is checked in the GPU tests"}
 
 
+BATCH_ARGS = ["-I+", "-ab", "2", "-ad", "512", "-lw", "1e-4", "-c", "1", "-u-"]
+
+
+def batch_measure(steps: int):
+    """Batched grids: 256 sensor grids of lognormal sizes (median 1,024,
+    clipped to 64..16,384) over 16 window rooms with log-uniform triangle
+    counts, rcontrib -ab 2 -ad 512 into Reinhart MF:1 + ground, all in one
+    gb_rcontrib_batch call; against one 16,384-sensor grid on the median
+    scene with the same options.  Wall-clock rays/s of whole calls (host
+    buffers in and out), best of `steps`."""
+    import concurrent.futures as cf
+    import pyradiance_gb300 as gb
+    from pyradiance_gb300 import workloads as w
+    rng = np.random.default_rng(2026)
+    ntri = np.exp(rng.uniform(np.log(2e4), np.log(1.6e5), 16)).astype(int)
+    sizes = np.clip(np.exp(rng.normal(np.log(1024), 1.0, 256)), 64, 16384).astype(int)
+    owner = rng.integers(0, 16, 256)
+    with tempfile.TemporaryDirectory() as td:
+        def build(k):
+            p = Path(td) / f"room{k}.rad"
+            p.write_text(w.window_room(seed=100 + k, ntri=int(ntri[k]), nmat=64))
+            return gb.Scene(rad_files=[p])
+        with cf.ThreadPoolExecutor(max_workers=min(16, os.cpu_count() or 1)) as ex:
+            scenes = list(ex.map(build, range(16)))
+    def sensors(n, seed):
+        r = np.random.default_rng(seed)
+        xy = r.uniform((0.3, 0.3), (9.7, 7.7), size=(n, 2))
+        return np.column_stack([xy, np.full(n, 0.8), np.zeros(n), np.zeros(n), np.ones(n)])
+    jobs = [(scenes[owner[j]], sensors(int(sizes[j]), j)) for j in range(256)]
+    rc = gb.Rcontrib(b"", None, params=BATCH_ARGS)
+    for m in MODS:
+        rc.add_modifier(**m)
+    rc.seed = 7
+    median = int(np.argsort(ntri)[8])
+    single = sensors(16384, 99)
+    rc.run_batch(jobs)                                   # warm-up (and queue-size pilots)
+    rc.octree = scenes[median]
+    rc.run_array(single)
+    tb, tsg, rays_b, rays_s = [], [], 0, 0
+    for _ in range(max(1, steps)):
+        t0 = time.perf_counter()
+        rc.run_batch(jobs)
+        tb.append(time.perf_counter() - t0)
+        rays_b = rc.last_rays
+        t0 = time.perf_counter()
+        rc.run_array(single)
+        tsg.append(time.perf_counter() - t0)
+        rays_s = rc.last_rays
+    vb, vs = rays_b / min(tb) / 1e6, rays_s / min(tsg) / 1e6
+    return {"workload": f"256 grids (sizes lognormal median 1024, 64..16384; {int(sizes.sum())} sensors) over 16 "
+                        f"window rooms of {int(ntri.min())}..{int(ntri.max())} triangles, rcontrib "
+                        + " ".join(BATCH_ARGS) + ", Reinhart MF:1 + ground",
+            "batch_mrays_s": round(vb, 1), "single_grid_mrays_s": round(vs, 1),
+            "batch_vs_single": round(vb / vs, 3), "batch_s": round(min(tb), 3), "rays_batch": int(rays_b),
+            "single_grid": "16384 sensors on the median scene"}
+
+
 def combine_ranks(dev_s: float, wall_s: float, rays: float, world: int, device=None):
     """Whole-job figures of a multi-rank run: the slowest rank's device and
     wall seconds, and the rays of all ranks (the ranks trace independent
@@ -420,6 +477,7 @@ def gpu_arm(args):
             "clocks": ck,
             "dctimestep": dct_measure(dev, args.steps),
             "gradient": grad_measure(args.steps),
+            "batching": batch_measure(min(args.steps, 3)),
         }
         print(json.dumps(line), flush=True)
 

@@ -148,6 +148,21 @@ int  gb_rtrace_grad(gb_scene *scene, const gb_opts *opts, const double *org_dir,
  * ray_count (optional) receives the number of rays traced. */
 int  gb_rcontrib(gb_scene *scene, const gb_opts *opts, const gb_modspec *mods, int nmods,
                  const double *org_dir, int64_t n, double *out, int64_t *ray_count);
+/* Many rcontrib grids at once: job j traces n[j] rays (org_dir[j]) in
+ * scenes[j] into out[j] (n[j] / opts->c records, as gb_rcontrib), all with
+ * the same options and modifiers.  The jobs of one scene run as a single
+ * wavefront over their concatenated sensors, with the queue capacity taken
+ * from a pilot run over a sample of them (remembered per scene and option
+ * set); different scenes run concurrently on their own streams.  n[j] must
+ * be a multiple of opts->c.  ray_count (optional) receives the rays traced
+ * by all jobs.  A sensor draws the random streams of its position in its
+ * scene's concatenated sensors: a job alone on its scene reproduces its
+ * separate gb_rcontrib call up to rounding (the order in which a warp's
+ * lanes are summed and bins accumulated), jobs sharing a scene are
+ * statistically equivalent to separate calls.  No
+ * counterpart in the reference (one rcontrib process per grid). */
+int  gb_rcontrib_batch(int njobs, gb_scene *const *scenes, const gb_opts *opts, const gb_modspec *mods, int nmods,
+                       const double *const *org_dir, const int64_t *n, double *const *out, int64_t *ray_count);
 /* Total bins of a modifier list (validates the bin expressions). */
 int  gb_rcontrib_nbins(const gb_modspec *mods, int nmods, int *nbins_total);
 

@@ -304,6 +304,39 @@ class Rcontrib:
         self._opts = opts
         return out
 
+    def run_batch(self, jobs) -> list[np.ndarray]:
+        """Many sensor grids at once: jobs is a sequence of (octree or Scene,
+        rays n x 6); each grid's contributions come back as run_array's.
+        The grids of one scene are traced as one wavefront and different
+        scenes concurrently (gb_rcontrib_batch)."""
+        opts, used = parse_opts(self.args, _lib.GB_PROG_RCONTRIB)
+        if used != len(self.args):
+            raise GbError(-1, f"command line error at '{self.args[used]}'")
+        if self.seed is not None:
+            opts.seed = int(self.seed)
+        opts.replica = int(self.replica)
+        specs, keep = self._specs()
+        nb = _lib.C.c_int(0)
+        check(lib().gb_rcontrib_nbins(specs, len(self.mods), _lib.C.byref(nb)))
+        accum = max(1, opts.c)
+        scenes, rays, outs = [], [], []
+        for scene, r in jobs:
+            sc = scene if isinstance(scene, Scene) else load_scene(scene)
+            r = np.ascontiguousarray(r, dtype=np.float64).reshape(-1, 6)
+            scenes.append(sc)
+            rays.append(r)
+            outs.append(np.zeros((len(r) // accum, nb.value, 3)))
+        k = len(scenes)
+        vp = _lib.C.c_void_p
+        c_sc = (vp * max(1, k))(*[s.handle.value for s in scenes])
+        c_in = (vp * max(1, k))(*[r.ctypes.data for r in rays])
+        c_out = (vp * max(1, k))(*[o.ctypes.data for o in outs])
+        c_n = (_lib.C.c_int64 * max(1, k))(*[len(r) for r in rays])
+        cnt = _lib.C.c_int64(0)
+        check(lib().gb_rcontrib_batch(k, c_sc, opts, specs, len(self.mods), c_in, c_n, c_out, _lib.C.byref(cnt)))
+        self.last_rays = cnt.value
+        return outs
+
     def _call(self) -> bytes:
         arr = self.run_array()
         opts = self._opts

@@ -71,6 +71,9 @@ _SIGS = {
     "gb_rcontrib": (C.c_int, [C.c_void_p, C.POINTER(GbOpts), C.POINTER(GbModspec), C.c_int, C.c_void_p,
                               C.c_int64, C.c_void_p, C.POINTER(C.c_int64)]),
     "gb_rcontrib_nbins": (C.c_int, [C.POINTER(GbModspec), C.c_int, C.POINTER(C.c_int)]),
+    "gb_rcontrib_batch": (C.c_int, [C.c_int, C.POINTER(C.c_void_p), C.POINTER(GbOpts), C.POINTER(GbModspec), C.c_int,
+                                    C.POINTER(C.c_void_p), C.POINTER(C.c_int64), C.POINTER(C.c_void_p),
+                                    C.POINTER(C.c_int64)]),
     "gb_dctimestep": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_int64, C.c_int64, C.c_int, C.c_void_p]),
     "gb_dctimestep_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_int64, C.c_int64, C.c_int,
                                        C.c_void_p, C.c_void_p]),

@@ -10,6 +10,7 @@
 #include <ctime>
 #include <atomic>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include <cuda_runtime.h>
@@ -110,6 +111,8 @@ struct gb_scene {
     int sms = 0;
     cudaEvent_t ev[2 * GB_TIMED_LAUNCHES + 2];
     int nev = 0;
+    std::string tuned_key;             /* options of the queue-size pilot */
+    double tuned_per_sensor = 0.0;     /* its queue slots per sensor */
 };
 
 /* per-kernel profile of the last run on this thread */
@@ -842,13 +845,20 @@ struct RunOut {
     double *grad;           /* gradient runs: host nslots x 3 */
 };
 
+/* largest generation and queue capacity of the last run on this thread */
+static thread_local long long g_maxgen, g_qcap;
+
 static int run(gb_scene *G, const gb_opts *o, int follow, const double *org_dir, int64_t n,
                const std::vector<gb_binins> *prog, const std::vector<int4> *modinfo, int nbins_total,
-               const std::vector<int> *trk, RunOut out)
+               const std::vector<int> *trk, RunOut out, long long qcap_req = 0, int64_t sensor_base = 0)
 {
     cudaStream_t st = G->stream;
-    g_stats[0] = g_stats[1] = g_stats[2] = g_stats[3] = 0;
-    memset(&g_prof, 0, sizeof g_prof);
+    if (sensor_base == 0) {                      /* first slice: counters start over */
+        g_maxgen = 0;
+        g_qcap = 0;
+        g_stats[0] = g_stats[1] = g_stats[2] = g_stats[3] = 0;
+        memset(&g_prof, 0, sizeof g_prof);
+    }
     if (n <= 0)
         return GB_OK;
     const size_t stat_bytes = GB_K_N * GB_ST_N * sizeof(unsigned long long);
@@ -901,6 +911,7 @@ static int run(gb_scene *G, const gb_opts *o, int follow, const double *org_dir,
     P.k1 = (uint32_t)(seed >> 32);
     P.replica = o->replica;
     P.nsensors = n;
+    P.sensor_base = (uint32_t)sensor_base;
     P.sensors = (const double *)G->sensors.p;
     P.stats = (unsigned long long *)G->stats.p;
     P.accum = o->c > 0 ? o->c : 1;
@@ -963,6 +974,8 @@ static int run(gb_scene *G, const gb_opts *o, int follow, const double *org_dir,
                        "supported", o->ad, n0, n0);
     long long est = (long long)n * (n0 > 0 ? (long long)n0 * n0 * 4 : (o->ab > 0 ? (long long)o->ad * 2 : 8));
     long long qcap = est < (1ll << 20) ? (1ll << 20) : est;
+    if (qcap_req > 0)
+        qcap = qcap_req;                         /* measured by a pilot run, or a retry */
     size_t freeb = 0, totalb = 0;
     cudaMemGetInfo(&freeb, &totalb);
     const bool grad = out.grad != nullptr;
@@ -975,6 +988,7 @@ static int run(gb_scene *G, const gb_opts *o, int follow, const double *org_dir,
         G->hitrec.ensure((size_t)qcap * sizeof(gb_qhit)) < 0)
         return set_err(GB_ENOMEM, "cannot allocate %lld-ray work queues", qcap);
     P.qcap = qcap;
+    g_qcap = qcap;
     P.hits = (gb_qhit *)G->hitrec.p;
     const int nslots = (int)(G->mat.size() / 2);
     if (grad) {
@@ -1031,6 +1045,8 @@ static int run(gb_scene *G, const gb_opts *o, int follow, const double *org_dir,
         CK(cudaStreamSynchronize(st));
         if (c == 0)
             break;
+        if ((long long)c > g_maxgen)
+            g_maxgen = (long long)c;
         if ((long long)c > qcap)
             return set_err(GB_EOVERFLOW, "ray queue overflow (%llu rays for %lld slots)", c, qcap);
         P.qin = in ? qb : qa;
@@ -1069,7 +1085,8 @@ static int run(gb_scene *G, const gb_opts *o, int follow, const double *org_dir,
         g_stats[1] += (int64_t)stats[k][GB_ST_STEPS];
         g_stats[2] += (int64_t)stats[k][GB_ST_CONTRIB];
         overflow += stats[k][GB_ST_OVERFLOW];
-        memcpy(g_prof.st[k], stats[k], sizeof stats[k]);
+        for (int c = 0; c < GB_ST_N; c++)
+            g_prof.st[k][c] += stats[k][c];
     }
     for (int s = 0; 2 + 2 * s + 1 < evused; s++) {
         float ms = 0.f;
@@ -1079,10 +1096,69 @@ static int run(gb_scene *G, const gb_opts *o, int follow, const double *org_dir,
     {
         float ms = 0.f;
         cudaEventElapsedTime(&ms, G->ev[0], G->ev[1]);
-        g_prof.region_ms = ms;
+        g_prof.region_ms += ms;
     }
     if (overflow)
         return set_err(GB_EOVERFLOW, "ray queue overflow (%llu records dropped)", overflow);
+    return GB_OK;
+}
+
+/* Queue slots per sensor that run() sizes for (the first generation's
+ * fan-out times four), or the pilot's measurement. */
+static double slots_per_sensor(const gb_scene *G, const gb_opts *o)
+{
+    int n0 = (o->I && o->ab > 0 && o->ad > 0) ? root_divisions(o) : 0;
+    return n0 > 0 ? (double)n0 * n0 * 4 : (o->ab > 0 ? (double)o->ad * 2 : 8.0);
+}
+
+/* run() over slices of at most as many sensors as keep the work buffers
+ * within a quarter of free device memory (and 8 GB): the random streams are
+ * keyed by the index in the whole set, so the result is that of one run.
+ * Slices of -c records stay whole.  per_sensor: queue slots per sensor
+ * (0: run()'s estimate). */
+static int run_sliced(gb_scene *G, const gb_opts *o, int follow, const double *org_dir, int64_t n,
+                      const std::vector<gb_binins> *prog, const std::vector<int4> *modinfo, int nbins_total,
+                      const std::vector<int> *trk, RunOut out, double per_sensor)
+{
+    const int64_t acc = o->c > 0 ? o->c : 1;
+    const bool grad = out.grad != nullptr;
+    const size_t slot = 2 * sizeof(gb_qray) + sizeof(gb_qhit) + (grad ? 2 * sizeof(gb_qadj) : 0);
+    if (per_sensor <= 0)
+        per_sensor = slots_per_sensor(G, o);
+    size_t freeb = 0, totalb = 0;
+    cudaMemGetInfo(&freeb, &totalb);
+    double budget = fmin((double)freeb / 4.0, 8e9);
+    int64_t chunk = (int64_t)(budget / (per_sensor * (double)slot));
+    chunk = chunk / acc * acc;
+    if (chunk < acc)
+        chunk = acc;
+    if (chunk >= n)
+        return run(G, o, follow, org_dir, n, prog, modinfo, nbins_total, trk, out,
+                   (long long)(per_sensor * (double)n) + (1ll << 16), 0);
+    const int nslots = (int)G->matobj.size();
+    std::vector<double> gsum(grad ? (size_t)nslots * 3 : 0), gpart(gsum.size());
+    long long maxgen = 0;
+    for (int64_t b = 0; b < n; b += chunk) {
+        const int64_t m = n - b < chunk ? n - b : chunk;
+        RunOut so = out;
+        if (out.value) so.value = out.value + 3 * b;
+        if (out.bins) so.bins = out.bins + (size_t)(b / acc) * nbins_total * 3;
+        if (out.hit_id) so.hit_id = out.hit_id + b;
+        if (out.hit_t) so.hit_t = out.hit_t + b;
+        if (grad) {
+            so.dlde = out.dlde + 3 * b;
+            so.grad = gpart.data();
+        }
+        int rc = run(G, o, follow, org_dir + 6 * b, m, prog, modinfo, nbins_total, trk, so,
+                     (long long)(per_sensor * (double)m) + (1ll << 16), b);
+        if (rc < 0)
+            return rc;
+        if (g_maxgen > maxgen) maxgen = g_maxgen;
+        for (size_t i = 0; i < gsum.size(); i++) gsum[i] += gpart[i];
+    }
+    g_maxgen = maxgen;
+    if (grad)
+        memcpy(out.grad, gsum.data(), gsum.size() * sizeof(double));
     return GB_OK;
 }
 
@@ -1097,7 +1173,7 @@ extern "C" int gb_rtrace(gb_scene *G, const gb_opts *o, const double *org_dir, i
             return rc;
     }
     RunOut out = {out_rgb, nullptr, hit_id, hit_t, nullptr, nullptr};
-    return run(G, o, 0, org_dir, n, nullptr, nullptr, 0, nullptr, out);
+    return run_sliced(G, o, 0, org_dir, n, nullptr, nullptr, 0, nullptr, out, 0.0);
 }
 
 extern "C" int gb_rtrace_grad(gb_scene *G, const gb_opts *o, const double *org_dir, int64_t n,
@@ -1115,7 +1191,7 @@ extern "C" int gb_rtrace_grad(gb_scene *G, const gb_opts *o, const double *org_d
     if (nslots == 0)
         return GB_OK;
     RunOut out = {nullptr, nullptr, nullptr, nullptr, dl_dvalue, grad};
-    return run(G, o, 0, org_dir, n, nullptr, nullptr, 0, nullptr, out);
+    return run_sliced(G, o, 0, org_dir, n, nullptr, nullptr, 0, nullptr, out, 0.0);
 }
 
 extern "C" int64_t gb_scene_material_slots(const gb_scene *G) { return G ? (int64_t)G->matobj.size() : 0; }
@@ -1196,11 +1272,12 @@ extern "C" int gb_rcontrib_nbins(const gb_modspec *mods, int nmods, int *nbins_t
     return compile_mods(nullptr, mods, nmods, prog, info, nullptr, nbins_total);
 }
 
-extern "C" int gb_rcontrib(gb_scene *G, const gb_opts *o, const gb_modspec *mods, int nmods,
-                           const double *org_dir, int64_t n, double *out, int64_t *ray_count)
+/* one rcontrib run on one scene: options overridden as rcmain does, bin
+ * programs compiled for the scene's modifiers; a queue that overflows is
+ * enlarged and the run repeated (the random streams make it identical) */
+static int rcontrib_run(gb_scene *G, const gb_opts *o, const gb_modspec *mods, int nmods, const double *org_dir,
+                        int64_t n, double *out, int64_t *ray_count, double per_sensor)
 {
-    if (!G || !o || !mods || nmods <= 0 || (!org_dir && n > 0) || !out)
-        return set_err(GB_EINVAL, "null argument or no modifiers");
     gb_opts oo = *o;
     /* rt/rcmain.c:164-172 override_options */
     oo.dt = 0;
@@ -1228,7 +1305,13 @@ extern "C" int gb_rcontrib(gb_scene *G, const gb_opts *o, const gb_modspec *mods
         }
     }
     RunOut ro = {nullptr, out, nullptr, nullptr, nullptr, nullptr};
-    rc = run(G, &oo, 1, org_dir, n, &prog, &info, nbt, &trk, ro);
+    double per = per_sensor;
+    for (int attempt = 0; attempt < 4; attempt++) {
+        rc = run_sliced(G, &oo, 1, org_dir, n, &prog, &info, nbt, &trk, ro, per);
+        if (rc != GB_EOVERFLOW)
+            break;
+        per = 2 * (per > 0 ? per : slots_per_sensor(G, &oo));   /* a larger queue, fewer sensors per slice */
+    }
     if (ray_count)
         *ray_count = g_stats[0];
     if (rc == GB_OK && oo.c > 1) {
@@ -1238,6 +1321,126 @@ extern "C" int gb_rcontrib(gb_scene *G, const gb_opts *o, const gb_modspec *mods
             out[i] *= sf;
     }
     return rc;
+}
+
+extern "C" int gb_rcontrib(gb_scene *G, const gb_opts *o, const gb_modspec *mods, int nmods,
+                           const double *org_dir, int64_t n, double *out, int64_t *ray_count)
+{
+    if (!G || !o || !mods || nmods <= 0 || (!org_dir && n > 0) || !out)
+        return set_err(GB_EINVAL, "null argument or no modifiers");
+    return rcontrib_run(G, o, mods, nmods, org_dir, n, out, ray_count, 0.0);
+}
+
+/* Queue slots per sensor for a run over n sensors, from a pilot run of
+ * 1,024 of them (evenly spaced): the largest generation per sensor, with a
+ * margin; kept per scene and option set so that later calls skip the
+ * pilot.  0 (run()'s estimate) for n <= 4,096. */
+static double tune_slots(gb_scene *G, const gb_opts *o, const gb_modspec *mods, int nmods, const double *org_dir,
+                         int64_t n, int nbt)
+{
+    const int64_t m = 1024;
+    if (n <= 4 * m)
+        return 0.0;
+    char key[256];
+    snprintf(key, sizeof key, "%d %d %g %d %g %d %d", o->ab, o->ad, o->lw, o->lr, o->dj, o->I, o->c);
+    if (G->tuned_key == key)
+        return G->tuned_per_sensor;
+    int64_t stride = n / m, acc = o->c > 0 ? o->c : 1;
+    std::vector<double> sample;
+    sample.reserve((size_t)m * acc * 6);
+    for (int64_t i = 0; i < m; i++)                 /* whole records of -c sensors */
+        for (int64_t j = 0; j < acc; j++) {
+            int64_t s = (i * stride / acc) * acc + j;
+            if (s >= n) s = n - 1;
+            sample.insert(sample.end(), org_dir + 6 * s, org_dir + 6 * s + 6);
+        }
+    int64_t ns = (int64_t)(sample.size() / 6);
+    std::vector<double> scratch((size_t)(ns / acc + 1) * nbt * 3);
+    int64_t rays = 0;
+    if (rcontrib_run(G, o, mods, nmods, sample.data(), ns, scratch.data(), &rays, 0.0) != GB_OK || g_maxgen <= 0)
+        return 0.0;
+    G->tuned_key = key;
+    G->tuned_per_sensor = 1.5 * (double)g_maxgen / (double)ns;
+    return G->tuned_per_sensor;
+}
+
+extern "C" int gb_rcontrib_batch(int njobs, gb_scene *const *scenes, const gb_opts *o, const gb_modspec *mods,
+                                 int nmods, const double *const *org_dir, const int64_t *n, double *const *out,
+                                 int64_t *ray_count)
+{
+    if (njobs < 0 || (njobs > 0 && (!scenes || !org_dir || !n || !out)) || !o || !mods || nmods <= 0)
+        return set_err(GB_EINVAL, "null argument or no modifiers");
+    const int64_t acc = o->c > 0 ? o->c : 1;
+    int nbt = 0;
+    {
+        std::vector<gb_binins> prog;
+        std::vector<int4> info;
+        int rc = compile_mods(nullptr, mods, nmods, prog, info, nullptr, &nbt);
+        if (rc < 0)
+            return rc;
+    }
+    /* jobs grouped by scene; each group is one run over its jobs' sensors */
+    std::vector<gb_scene *> order;
+    std::vector<std::vector<int>> groups;
+    for (int j = 0; j < njobs; j++) {
+        if (!scenes[j] || (n[j] > 0 && (!org_dir[j] || !out[j])) || n[j] < 0)
+            return set_err(GB_EINVAL, "job %d: null scene, rays or output", j);
+        if (n[j] % acc)
+            return set_err(GB_EINVAL, "job %d: %lld rays is not a multiple of -c %lld", j, (long long)n[j],
+                           (long long)acc);
+        size_t g = 0;
+        while (g < order.size() && order[g] != scenes[j]) g++;
+        if (g == order.size()) {
+            order.push_back(scenes[j]);
+            groups.emplace_back();
+        }
+        groups[g].push_back(j);
+    }
+    std::vector<int> rcs(order.size(), GB_OK);
+    std::vector<int64_t> rays(order.size(), 0);
+    std::vector<std::string> errs(order.size());
+    auto work = [&](size_t g) {
+        gb_scene *G = order[g];
+        int64_t tot = 0;
+        for (int j : groups[g]) tot += n[j];
+        std::vector<double> in((size_t)tot * 6), res((size_t)(tot / acc) * nbt * 3);
+        int64_t at = 0;
+        for (int j : groups[g]) {
+            if (n[j])
+                memcpy(in.data() + 6 * at, org_dir[j], (size_t)n[j] * 6 * sizeof(double));
+            at += n[j];
+        }
+        double per = tune_slots(G, o, mods, nmods, in.data(), tot, nbt);
+        rcs[g] = rcontrib_run(G, o, mods, nmods, in.data(), tot, res.data(), &rays[g], per);
+        errs[g] = g_error;
+        if (rcs[g] != GB_OK)
+            return;
+        at = 0;
+        for (int j : groups[g]) {
+            const size_t rec = (size_t)(n[j] / acc) * nbt * 3;
+            memcpy(out[j], res.data() + (size_t)(at / acc) * nbt * 3, rec * sizeof(double));
+            at += n[j];
+        }
+    };
+    /* scenes run concurrently, each on its own stream, so that one
+     * scene's small last generations overlap another's large ones */
+    std::vector<std::thread> th;
+    for (size_t g = 1; g < order.size(); g++)
+        th.emplace_back(work, g);
+    if (!order.empty())
+        work(0);
+    for (auto &t : th)
+        t.join();
+    int64_t total = 0;
+    for (size_t g = 0; g < order.size(); g++) {
+        total += rays[g];
+        if (rcs[g] != GB_OK)
+            return set_err(rcs[g], "%s", errs[g].c_str());
+    }
+    if (ray_count)
+        *ray_count = total;
+    g_stats[0] = total;
+    return GB_OK;
 }
 
 /* ------------------------------------------------------------- dctimestep */
@@ -1454,6 +1657,8 @@ extern "C" int gb_rtrace_device_noalloc(gb_scene *G, const gb_opts *o, const dou
         CK(cudaStreamSynchronize(st));
         if (c == 0)
             break;
+        if ((long long)c > g_maxgen)
+            g_maxgen = (long long)c;
         if ((long long)c > qcap)
             return set_err(GB_EOVERFLOW, "ray queue overflow (%llu rays for %lld slots)", c, qcap);
         P.qin = in ? qb : qa;

@@ -201,7 +201,7 @@ __device__ void grad_add(const gb_run &P, uint32_t sensor, float3 v, const gb_qa
 {
     if (a.n == 0 || a.n > GB_ADJ_MAX)
         return;
-    const double *w = P.dlde + 3ull * sensor;
+    const double *w = P.dlde + 3ull * (sensor - P.sensor_base);
     const float3 wv = f3((float)w[0] * v.x, (float)w[1] * v.y, (float)w[2] * v.z);
     if (wv.x == 0.f && wv.y == 0.f && wv.z == 0.f)
         return;
@@ -236,7 +236,7 @@ __device__ __forceinline__ void add_value(const gb_run &P, uint32_t sensor, floa
         return;
     if (v.x == 0.f && v.y == 0.f && v.z == 0.f)
         return;
-    double *d = P.value + 3ull * sensor;
+    double *d = P.value + 3ull * (sensor - P.sensor_base);
     atomicAdd(d, (double)v.x);
     atomicAdd(d + 1, (double)v.y);
     atomicAdd(d + 2, (double)v.z);
@@ -256,7 +256,7 @@ __device__ __forceinline__ void add_bin(const gb_run &P, uint32_t sensor, int sl
         atomicAdd(P.stats + ST_BADBIN, 1ull);   /* rt/rcontrib.c:305-309 warning */
         return;
     }
-    uint32_t rec = sensor / (uint32_t)P.accum;
+    uint32_t rec = (sensor - P.sensor_base) / (uint32_t)P.accum;
     unsigned long long key = (unsigned long long)rec * (unsigned long long)P.nbins_total + (unsigned long long)(mi.z + bn);
     cnt.contrib++;
     /* warp aggregation: lanes with the same key sum through shuffles */
@@ -784,7 +784,7 @@ __device__ void direct(const gb_run &P, const Ray &r, float3 hp, const Surf &s, 
         const float3 c = r.coef * shadow_chain<true>(P, sr, sn, cnt, coef, pot, &fac);
         grad_add(P, r.sensor, c, fac);
         if (slot >= 0 && fac.n <= GB_ADJ_MAX) {  /* this surface's own reflectance: */
-            const double *w = P.dlde + 3ull * r.sensor;     /* the diffuse part of dirnorm */
+            const double *w = P.dlde + 3ull * (r.sensor - P.sensor_base);     /* the diffuse part */
             float g[3], cc[3] = {c.x, c.y, c.z}, cd[3] = {coefd.x, coefd.y, coefd.z}, ct[3] = {coef.x, coef.y, coef.z};
             float mc[3] = {s.mcolor.x, s.mcolor.y, s.mcolor.z};
             for (int i = 0; i < 3; i++)
@@ -1026,7 +1026,7 @@ __global__ void k_root(gb_run P)
         r.rlvl = 0;
         r.adepth = 0;
         r.path = GB_ROOT_PATH(P.replica);
-        r.sensor = (uint32_t)s;
+        r.sensor = (uint32_t)(s + P.sensor_base);
         r.adj.n = 0;
         float3 hp = f3((float)(sv[0] + 1e-4 * sv[3]), (float)(sv[1] + 1e-4 * sv[4]), (float)(sv[2] + 1e-4 * sv[5]));
         Surf su;
@@ -1084,7 +1084,7 @@ __global__ void __launch_bounds__(256) k_expand_root(gb_run P)
         parent.rlvl = 0;
         parent.adepth = 0;
         parent.path = GB_ROOT_PATH(P.replica);
-        parent.sensor = (uint32_t)s;
+        parent.sensor = (uint32_t)(s + P.sensor_base);
         Hemi hm;
         hm.n = rr->n;
         hm.atyp = GB_RAMBIENT;
@@ -1129,7 +1129,7 @@ __global__ void k_primary(gb_run P)
         r.rlvl = 0;
         r.adepth = 0;
         r.path = GB_ROOT_PATH(P.replica);
-        r.sensor = (uint32_t)s;
+        r.sensor = (uint32_t)(s + P.sensor_base);
         r.adj.n = 0;
         push_ray<G>(P, r);
     }

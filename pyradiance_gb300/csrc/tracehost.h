@@ -73,8 +73,11 @@ typedef struct {
     int   contrib_mode;        /* rcontrib -V */
     uint32_t k0, k1;           /* random stream key */
     uint32_t replica;
-    /* sensors */
+    /* sensors: this run's slice of a larger sensor set starts at index
+     * sensor_base of it; random streams are keyed by the index in the set,
+     * outputs by the index in the slice */
     long long nsensors;
+    uint32_t sensor_base;
     const double *sensors;     /* n x 6 */
     /* outputs */
     double *value;             /* n x 3 or NULL */
