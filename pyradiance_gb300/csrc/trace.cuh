@@ -512,22 +512,31 @@ GB_DFN bool walk_begin(const gb_dscene &S, float3 org, float3 dir, int skip, Wal
     return true;
 }
 
-/* One iteration of the walk: test one object of the current leaf, or move
- * to the next leaf (descending from the deepest ancestor it shares with the
- * last one, from the highest coordinate bit that changed).  Returns true
- * when the walk has ended. */
+/* One iteration of the walk: test objects of the current leaf, and when it
+ * is done move to the next leaf (descending from the deepest ancestor it
+ * shares with the last one, from the highest coordinate bit that changed).
+ * Returns true when the walk has ended. */
+#define WALK_TESTS 3
 template <typename Stack>
 GB_DFN bool walk_iter(const gb_dscene &S, Walk &W, Stack &stk)
 {
-    if (W.k <= W.cnt) {                          /* next object of this leaf */
+    /* up to WALK_TESTS objects of this leaf per iteration, then, if the
+     * leaf is done, the step to the next one in the same iteration: fewer
+     * iterations (and refill checks) per walk, and lanes testing and lanes
+     * stepping share more of each iteration (3 measured best of 1-6) */
+#pragma unroll
+    for (int u = 0; u < WALK_TESTS; u++) {
+        if (W.k > W.cnt)
+            break;
         int o = GB_LDG(S.set_data + W.set + W.k);
         W.k++;
         if (o != W.skip)
             hit_object(S, o, W.org, W.dir, W.best, D_FTINY);
         else if (W.curved_skip)                  /* curved origin surface */
             hit_object(S, o, W.org, W.dir, W.best, D_FTINY, true);
-        return false;
     }
+    if (W.k <= W.cnt)
+        return false;
     const float dd[3] = {W.dir.x, W.dir.y, W.dir.z};
     if (W.leaf) {
         if (W.best.obj >= 0 && W.best.t <= W.texit)
