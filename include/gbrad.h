@@ -108,7 +108,7 @@ int  gb_rtrace(gb_scene *scene, const gb_opts *opts, const double *org_dir, int6
  * latency-bound streams that cudaMalloc/cudaFree would stall by
  * synchronising the device.  Working memory comes from one static 64 MiB
  * device array per device; a call whose rays would not fit (1.25 KiB per
- * ray without ambient bounces, 640 bytes per first-hemisphere sample with
+ * ray without ambient bounces, about 650 bytes per first-hemisphere sample with
  * -I and -ab > 0) is rejected with GB_EINVAL and a message giving the
  * need.  The scene must have been loaded on the current
  * device.  The first call on a device looks the array up there (and may

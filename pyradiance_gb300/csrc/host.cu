@@ -106,7 +106,7 @@ struct gb_scene {
     gb_dscene ds;
     /* work buffers */
     DevBuf sensors, value, bins, stats, roots, rootspt, qa, qb, qcount, binprog, modinfo, hits, hitt, trkrun,
-        hitrec, adja, adjb, dlde, gradd;
+        hitrec, adja, adjb, dlde, gradd, rootdraw, rootlot;
     cudaStream_t stream = nullptr;
     int sms = 0;
     cudaEvent_t ev[2 * GB_TIMED_LAUNCHES + 2];
@@ -602,7 +602,7 @@ extern "C" void gb_scene_free(gb_scene *G)
     DevBuf *bufs[] = {&G->kids, &G->setoff, &G->setdata, &G->obj, &G->geo, &G->fvert, &G->fv4, &G->cone, &G->matd,
                       &G->srcd, &G->trk, &G->sensors, &G->value, &G->bins, &G->stats, &G->roots, &G->rootspt, &G->qa,
                       &G->qb, &G->qcount, &G->binprog, &G->modinfo, &G->hits, &G->hitt, &G->trkrun, &G->hitrec,
-                      &G->adja, &G->adjb, &G->dlde, &G->gradd};
+                      &G->adja, &G->adjb, &G->dlde, &G->gradd, &G->rootdraw, &G->rootlot};
     for (DevBuf *b : bufs)
         b->release();
     if (G->stream)
@@ -1015,16 +1015,28 @@ static int run(gb_scene *G, const gb_opts *o, int follow, const double *org_dir,
     if (o->I) {
         if (n0 > 0) {
             if (G->roots.ensure((size_t)n * sizeof(gb_rootrec)) < 0 ||
-                G->rootspt.ensure((size_t)n * n0 * n0 * sizeof(float2)) < 0)
+                G->rootspt.ensure((size_t)n * n0 * n0 * sizeof(float2)) < 0 ||
+                (n0 >= 4 && (G->rootdraw.ensure((size_t)n * n0 * n0 * sizeof(float2)) < 0 ||
+                             G->rootlot.ensure((size_t)n * 2 * GB_XLOT * sizeof(float)) < 0)))
                 return set_err(GB_ENOMEM, "device allocation failed");
             P.roots = (gb_rootrec *)G->roots.p;
             P.root_spt = (float2 *)G->rootspt.p;
+            P.root_draw = (float2 *)G->rootdraw.p;
+            P.root_lot = (float *)G->rootlot.p;
         }
         P.root_n = n0;
         int rc = launch(GB_K_ROOT, P, [&](gb_run &R) {
             return grad ? gb_launch_root_grad(&R, st, G->sms) : gb_launch_root(&R, st, G->sms); });
         if (rc < 0)
             return rc;
+        if (n0 >= 4) {                           /* the placement of the first hemispheres */
+            rc = launch(GB_K_ROOT, P, [&](gb_run &R) { return gb_launch_root_draws(&R, st, G->sms); });
+            if (rc < 0)
+                return rc;
+            rc = launch(GB_K_ROOT, P, [&](gb_run &R) { return gb_launch_root_place(&R, st, G->sms); });
+            if (rc < 0)
+                return rc;
+        }
         if (n0 > 0) {
             rc = launch(GB_K_EXPAND, P, [&](gb_run &R) {
                 return grad ? gb_launch_expand_root_grad(&R, st, G->sms) : gb_launch_expand_root(&R, st, G->sms); });
@@ -1572,7 +1584,9 @@ extern "C" int gb_rtrace_device_noalloc(gb_scene *G, const gb_opts *o, const dou
     size_t off_stats = 0, off_cnt = up(stat_bytes), off_trk = off_cnt + up(4 * sizeof(unsigned long long));
     size_t off_roots = off_trk + up(nobj * sizeof(int));
     size_t off_spt = off_roots + (n0 > 0 ? up((size_t)n * sizeof(gb_rootrec)) : 0);
-    size_t off_q = off_spt + (n0 > 0 ? up((size_t)n * n0 * n0 * sizeof(float2)) : 0);
+    size_t off_draw = off_spt + (n0 > 0 ? up((size_t)n * n0 * n0 * sizeof(float2)) : 0);
+    size_t off_lot = off_draw + (n0 >= 4 ? up((size_t)n * n0 * n0 * sizeof(float2)) : 0);
+    size_t off_q = off_lot + (n0 >= 4 ? up((size_t)n * 2 * GB_XLOT * sizeof(float)) : 0);
     /* the queue need gb_rtrace sizes for, without its 1M-ray minimum */
     long long est = (long long)n * (n0 > 0 ? (long long)n0 * n0 * 4 : (o->ab > 0 ? (long long)o->ad * 2 : 8));
     const size_t slot = 2 * sizeof(gb_qray) + sizeof(gb_qhit);   /* two queues and the walk results */
@@ -1634,9 +1648,13 @@ extern "C" int gb_rtrace_device_noalloc(gb_scene *G, const gb_opts *o, const dou
         if (n0 > 0) {
             P.roots = (gb_rootrec *)(base + off_roots);
             P.root_spt = (float2 *)(base + off_spt);
+            P.root_draw = (float2 *)(base + off_draw);
+            P.root_lot = (float *)(base + off_lot);
         }
         P.root_n = n0;
         if ((rc = go(GB_K_ROOT, gb_launch_root)) < 0)
+            return rc;
+        if (n0 >= 4 && ((rc = go(GB_K_ROOT, gb_launch_root_draws)) < 0 || (rc = go(GB_K_ROOT, gb_launch_root_place)) < 0))
             return rc;
         if (n0 > 0) {
             P.qout = qa;

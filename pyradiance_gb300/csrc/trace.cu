@@ -1051,8 +1051,7 @@ __global__ void k_root(gb_run P)
             rr->nrm[0] = dir.x; rr->nrm[1] = dir.y; rr->nrm[2] = dir.z;
             rr->ux[0] = hm.ux.x; rr->ux[1] = hm.ux.y; rr->ux[2] = hm.ux.z;
             rr->n = hm.n;
-            if (hm.n >= 4)
-                place_hemi(P, r, hm, P.root_spt + s * (long long)hm.n * hm.n);
+            /* hm.n >= 4: placed by k_root_draws and k_root_place */
         } else if (P.av[0] != 0.f || P.av[1] != 0.f || P.av[2] != 0.f) {
             add_value(P, r.sensor, su.mcolor * f3(P.av[0], P.av[1], P.av[2]));
         }
@@ -1060,6 +1059,114 @@ __global__ void k_root(gb_run P)
     flush_counters(P, cnt);
     if (G)
         grad_end(P);
+}
+
+/* the root ray and hemisphere of -I sensor s from its record (as k_root
+ * made them) */
+__device__ __forceinline__ void root_parent(const gb_run &P, long long s, Ray &parent, Hemi &hm)
+{
+    const gb_rootrec *rr = P.roots + s;
+    parent.org = f3(rr->hp[0], rr->hp[1], rr->hp[2]);
+    parent.coef = f3(1.f, 1.f, 1.f);
+    parent.weight = 1.f;
+    parent.lcoef = 1.f;
+    parent.origin = -1;
+    parent.rsrc = -1;
+    parent.crtype = GB_PRIMARY;
+    parent.rlvl = 0;
+    parent.adepth = 0;
+    parent.path = GB_ROOT_PATH(P.replica);
+    parent.sensor = (uint32_t)(s + P.sensor_base);
+    parent.adj.n = 0;
+    hm.n = rr->n;
+    hm.atyp = GB_RAMBIENT;
+    hm.onrm = f3(rr->nrm[0], rr->nrm[1], rr->nrm[2]);
+    hm.ux = f3(rr->ux[0], rr->ux[1], rr->ux[2]);
+    hm.uy = cross3(hm.onrm, hm.ux);
+    float a = D_PI / (float)(hm.n * hm.n);
+    hm.acoef = f3(a, a, a);
+}
+
+/* The random numbers of the root placement, drawn in parallel: for every
+ * (sensor, stratum) the stratum's creation draw (ray_origin: Russian
+ * roulette and the jitter), and for every sensor the first fill of its lot
+ * (the 512 positions gb_trade_patchsamp draws on its first call, from the
+ * lot stream's blocks 0..255, in gb_lot_u32's order).  The sequential
+ * placement then reads them instead of drawing. */
+__global__ void k_root_draws(gb_run P)
+{
+    const long long nn = (long long)P.root_n * P.root_n;
+    const long long total = nn * P.nsensors, lots = (long long)P.nsensors * (GB_XLOT / 2);
+    for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < total + lots;
+         g += (long long)gridDim.x * blockDim.x) {
+        if (g < total) {
+            const long long s = g / nn;
+            const int k = (int)(g - s * nn);
+            Ray parent, c;
+            Hemi hm;
+            root_parent(P, s, parent, hm);
+            float4 u;
+            bool alive = ray_origin(P, parent, hm.atyp, hm.acoef, true, GB_C_STRATUM(k), c, &u);
+            P.root_draw[g] = make_float2(alive ? u.y : 3.f, u.z);
+        } else {
+            const long long h = g - total, s = h / (GB_XLOT / 2);
+            const int b = (int)(h - s * (GB_XLOT / 2));          /* lot block: positions 2b, 2b+1 */
+            gb_u4 u = gb_draw(GB_ROOT_PATH(P.replica), (uint32_t)(s + P.sensor_base), GB_G_LOT0 + b, P.k0, P.k1);
+            float4 *o = reinterpret_cast<float4 *>(P.root_lot + s * (2 * GB_XLOT)) + b;
+            *o = make_float4(gb_u01(u.v[3]), gb_u01(u.v[2]), gb_u01(u.v[1]), gb_u01(u.v[0]));
+        }
+    }
+}
+
+/* The sequential placement of every -I sensor's first hemisphere (n >= 4),
+ * one thread per sensor, from the precomputed draws and lot. */
+__global__ void k_root_place(gb_run P)
+{
+    const long long nn = (long long)P.root_n * P.root_n;
+    for (long long s = blockIdx.x * (long long)blockDim.x + threadIdx.x; s < P.nsensors;
+         s += (long long)gridDim.x * blockDim.x) {
+        const int n = P.roots[s].n;
+        if (n < 4 || n > MAX_HEMI_N)
+            continue;
+        gb_lot L;
+        gb_lot_init(&L, GB_ROOT_PATH(P.replica), (uint32_t)(s + P.sensor_base), P.k0, P.k1);
+        const float4 *lf = reinterpret_cast<const float4 *>(P.root_lot + s * (2 * GB_XLOT));
+        for (int b = 0; b < GB_XLOT / 2; b++) {
+            float4 v = lf[b];
+            L.lot[2 * b][0] = v.x;
+            L.lot[2 * b][1] = v.y;
+            L.lot[2 * b + 1][0] = v.z;
+            L.lot[2 * b + 1][1] = v.w;
+        }
+        L.gterm[GB_COTHER] = GB_XLOT;                  /* filled: the lazy fill is skipped */
+        L.blk = GB_XLOT / 2;
+        float rows[2][MAX_HEMI_N][2];
+        float (*prev)[2] = rows[0], (*cur)[2] = rows[1];
+        for (int k = 0; k < n; k++) {
+            rows[0][k][0] = rows[0][k][1] = 2.f;
+            rows[1][k][0] = rows[1][k][1] = 2.f;
+        }
+        const float2 *dr = P.root_draw + s * nn;
+        float2 *out = P.root_spt + s * nn;
+        for (int i = n - 1; i >= 0; i--) {
+            for (int j = n - 1; j >= 0; j--) {
+                const int k = i * n + j;
+                const float2 d = dr[k];
+                float sp[2] = {2.f, 2.f};
+                if (d.x < 1.5f)
+                    gb_place_sample(&L, n, i, j, d.x, d.y, i + 1 < n ? (const float(*)[2])prev : nullptr,
+                                    (const float(*)[2])cur, sp);
+                cur[j][0] = sp[0];
+                cur[j][1] = sp[1];
+                out[k] = make_float2(sp[0], sp[1]);
+            }
+            float(*t)[2] = prev;
+            prev = cur;
+            cur = t;
+            for (int k = 0; k < n; k++)
+                cur[k][0] = cur[k][1] = 2.f;
+        }
+    }
 }
 
 /* first hemisphere of every -I sensor: one ray per (sensor, stratum) into
@@ -1072,27 +1179,9 @@ __global__ void __launch_bounds__(256) k_expand_root(gb_run P)
     persistent_items(P.work, total, [&](unsigned long long g) {
         long long s = (long long)(g / (unsigned long long)nn);
         int k = (int)(g - (unsigned long long)s * nn);
-        const gb_rootrec *rr = P.roots + s;
         Ray parent;
-        parent.org = f3(rr->hp[0], rr->hp[1], rr->hp[2]);
-        parent.coef = f3(1.f, 1.f, 1.f);
-        parent.weight = 1.f;
-        parent.lcoef = 1.f;
-        parent.origin = -1;
-        parent.rsrc = -1;
-        parent.crtype = GB_PRIMARY;
-        parent.rlvl = 0;
-        parent.adepth = 0;
-        parent.path = GB_ROOT_PATH(P.replica);
-        parent.sensor = (uint32_t)(s + P.sensor_base);
         Hemi hm;
-        hm.n = rr->n;
-        hm.atyp = GB_RAMBIENT;
-        hm.onrm = f3(rr->nrm[0], rr->nrm[1], rr->nrm[2]);
-        hm.ux = f3(rr->ux[0], rr->ux[1], rr->ux[2]);
-        hm.uy = cross3(hm.onrm, hm.ux);
-        float a = D_PI / (float)(hm.n * hm.n);
-        hm.acoef = f3(a, a, a);
+        root_parent(P, s, parent, hm);
         const float *sp = nullptr;
         float2 pk;
         if (hm.n >= 4) {
@@ -1294,7 +1383,22 @@ static size_t grad_smem_bytes(const gb_run *P, gb_run &R)
 
 int gb_launch_root(const gb_run *P, cudaStream_t st, int sms)
 {
-    k_root<false><<<grid_for(P->nsensors, 128, sms), 128, 0, st>>>(*P);
+    k_root<false><<<grid_for(P->nsensors, 32, sms), 32, 0, st>>>(*P);
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+int gb_launch_root_draws(const gb_run *P, cudaStream_t st, int sms)
+{
+    long long work = (long long)P->root_n * P->root_n * P->nsensors + P->nsensors * (GB_XLOT / 2);
+    k_root_draws<<<grid_for(work, 256, sms), 256, 0, st>>>(*P);
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+int gb_launch_root_place(const gb_run *P, cudaStream_t st, int sms)
+{
+    /* a few sensors per warp: the placement is a long dependent chain per
+     * sensor, so more warps on every SM hide more of its latency */
+    k_root_place<<<grid_for(P->nsensors, 8, sms), 8, 0, st>>>(*P);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
@@ -1302,7 +1406,7 @@ int gb_launch_root_grad(const gb_run *P, cudaStream_t st, int sms)
 {
     gb_run R;
     size_t sm = grad_smem_bytes(P, R);
-    k_root<true><<<grid_for(P->nsensors, 128, sms), 128, sm, st>>>(R);
+    k_root<true><<<grid_for(P->nsensors, 32, sms), 32, sm, st>>>(R);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 

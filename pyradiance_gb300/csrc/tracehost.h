@@ -90,6 +90,9 @@ typedef struct {
     /* work */
     gb_rootrec *roots;
     float2 *root_spt;          /* n x root_n^2 placed disk positions (root_n >= 4) */
+    float2 *root_draw;         /* n x root_n^2 stratum jitters, x > 1.5 for a stratum
+                                * that died in Russian roulette (root_n >= 4) */
+    float *root_lot;           /* n x 2 * GB_XLOT: the first fill of each sensor's lot */
     int   root_n;
     const gb_qray *qin;
     const unsigned long long *qin_count;
@@ -110,6 +113,10 @@ typedef struct {
 
 int gb_launch_cast(const gb_run *P, int *hit_obj, float *hit_t, float *hit_pn, cudaStream_t st, int sms);
 int gb_launch_root(const gb_run *P, cudaStream_t st, int sms);
+/* -I roots with root_n >= 4: the strata's draws and the lots in parallel,
+ * then the sequential placement per sensor */
+int gb_launch_root_draws(const gb_run *P, cudaStream_t st, int sms);
+int gb_launch_root_place(const gb_run *P, cudaStream_t st, int sms);
 int gb_launch_expand_root(const gb_run *P, cudaStream_t st, int sms);
 int gb_launch_primary(const gb_run *P, cudaStream_t st, int sms);
 int gb_launch_trace(const gb_run *P, cudaStream_t st, int sms);
