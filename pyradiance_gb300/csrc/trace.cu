@@ -2,18 +2,21 @@
  * trace.cu -- the GB300 wavefront path engine behind rtrace and rcontrib.
  *
  * Work is organised by ray generation instead of by recursion:
- *   k_root      one thread per sensor: the -I "pretend hit" Lambertian at the
- *               sensor (rt/rtrace.c:416-433, rt/rcontrib.c:321-338), its
- *               direct component, and the frame of its ambient hemisphere;
- *   k_gen_root  the first hemisphere, expanded lazily: ray index ->
- *               (sensor, stratum), so the 1,024 strata of every sensor are
- *               traced in parallel without being written to memory;
- *   k_primary   radiance mode: the sensor rays themselves as generation 0;
- *   k_gen       any later generation, from a queue of 64-byte ray records.
- * Each ray is traced, shaded, and continues in the same thread with one of
- * its children; the other children are appended to the next generation's
- * queue with one atomic per coalesced group.  Contributions are added to
- * FP64 per-sensor values and per-record bins with warp-aggregated atomics.
+ *   k_root         one thread per sensor: the -I "pretend hit" Lambertian at
+ *                  the sensor (rt/rtrace.c:416-433, rt/rcontrib.c:321-338),
+ *                  its direct component and its hemisphere's frame and size;
+ *   k_root_draws   the random numbers of the first hemispheres' placement,
+ *   k_root_place   and the placement itself, sequential per sensor;
+ *   k_expand_root  the first generation: one ray per (sensor, stratum);
+ *   k_primary      radiance mode: the sensor rays as the first generation;
+ * then for every generation, from a queue of 64-byte ray records:
+ *   k_trace        the octree walk of every ray (a 32-byte result each),
+ *   k_shade        shading, contributions, and every child ray appended to
+ *                  the next generation's queue (one atomic per coalesced
+ *                  group).
+ * Contributions are added to FP64 per-sensor values and per-record bins
+ * with warp-aggregated atomics; gradient runs (k_*<true>) replay the same
+ * rays and accumulate derivatives instead.
  *
  * Shading follows the reference: m_normal for plastic/metal with pure
  * specular reflection (rt/normal.c:177-360, dirnorm :72-173), m_glass
@@ -462,41 +465,6 @@ __device__ __forceinline__ bool hemi_child(const gb_run &P, const Ray &parent, c
 }
 
 #define MAX_HEMI_N 128
-
-/* Place every stratum of an n x n (n >= 4) hemisphere in the reference's
- * order with collision avoidance; positions go to out (n*n float2, dead
- * strata get x = 2).  Runs sequentially in one thread. */
-__device__ __noinline__ void place_hemi(const gb_run &P, const Ray &parent, const Hemi &h, float2 *out)
-{
-    gb_lot L;
-    float rows[2][MAX_HEMI_N][2];
-    float (*prev)[2] = rows[0], (*cur)[2] = rows[1];
-    gb_lot_init(&L, parent.path, parent.sensor, P.k0, P.k1);
-    const int n = h.n;
-    for (int k = 0; k < n; k++) {
-        rows[0][k][0] = rows[0][k][1] = 2.f;
-        rows[1][k][0] = rows[1][k][1] = 2.f;
-    }
-    for (int i = n - 1; i >= 0; i--) {
-        for (int j = n - 1; j >= 0; j--) {
-            Ray c;
-            float4 u;
-            int k = i * n + j;
-            float s[2] = {2.f, 2.f};
-            if (ray_origin(P, parent, h.atyp, h.acoef, true, GB_C_STRATUM(k), c, &u))
-                gb_place_sample(&L, n, i, j, u.y, u.z, i + 1 < n ? (const float(*)[2])prev : nullptr,
-                                (const float(*)[2])cur, s);
-            cur[j][0] = s[0];
-            cur[j][1] = s[1];
-            out[k] = make_float2(s[0], s[1]);
-        }
-        float(*t)[2] = prev;
-        prev = cur;
-        cur = t;
-        for (int k = 0; k < n; k++)
-            cur[k][0] = cur[k][1] = 2.f;
-    }
-}
 
 /* Spawn all children of a hemisphere of 4 x 4 strata or more met after the
  * first generation: placed sequentially with collision avoidance and
@@ -1298,7 +1266,7 @@ __global__ void __launch_bounds__(TRACE_BLOCK, 4) k_trace(gb_run P)
 /* One generation, second half: shade every traced ray and queue its
  * children for the next generation. */
 template <bool G>
-__global__ void __launch_bounds__(256) k_shade(gb_run P)
+__global__ void __launch_bounds__(256, 4) k_shade(gb_run P)
 {
     if (G)
         grad_begin(P);
