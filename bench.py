@@ -475,10 +475,11 @@ def gpu_arm(args):
             "cpu_baseline": {"value": None if cpu_v is None else round(cpu_v, 4), "unit": "Mrays/s",
                              "cores": cores, "kind": "port", "sample": sample},
             "clocks": ck,
-            "dctimestep": dct_measure(dev, args.steps),
-            "gradient": grad_measure(args.steps),
-            "batching": batch_measure(min(args.steps, 3)),
         }
+        if not (args.sensors or args.no_extras):
+            line["dctimestep"] = dct_measure(dev, args.steps)
+            line["gradient"] = grad_measure(args.steps)
+            line["batching"] = batch_measure(min(args.steps, 3))
         print(json.dumps(line), flush=True)
 
 
@@ -490,7 +491,10 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--sensors", type=int, default=0,
-                    help="profile a smaller case: this many sensors of the grid (the metric is not reported)")
+                    help="profile a smaller case: this many sensors of the grid, without the dctimestep, "
+                         "gradient and batching legs")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="the rcontrib workload only (no dctimestep, gradient and batching legs)")
     args = ap.parse_args()
     if args.impl == "reference":
         reference_arm(args)
