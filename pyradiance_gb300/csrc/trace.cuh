@@ -486,11 +486,16 @@ GB_DFN bool walk_begin(const gb_dscene &S, float3 org, float3 dir, int skip, Wal
         t += D_FTINY;
         if (t >= D_FHUGE)
             return false;
+        /* the entry point in FP32 carries the rounding of t (about 1e-7 t),
+         * far more than the FTINY step the reference takes into the cube,
+         * so it is accepted within that rounding; a ray that misses the
+         * cube by less walks boundary cells and meets nothing */
+        const float eps = 1e-5f * fmaxf(cs, t);
         bool in = true;
 #pragma unroll
         for (int i = 0; i < 3; i++) {
             float p = rr[i] + dd[i] * t;
-            in &= p >= 0.f && p < cs;
+            in &= p >= -eps && p < cs + eps;
         }
         if (!in)
             return false;
