@@ -888,34 +888,106 @@ static void dirnorm(const ctx *X, double sc[3], const NORMDAT *np, const RAY *r,
     }
 }
 
-/* rt/source.c:398-556 with one partition per source and all shadows tested */
+/* Partitions of a flat local source as seen from point ro (rt/srcsamp.c:
+ * 260-330 flatpart, flt_partit): a source larger than -ds times its
+ * distance (scaled by the ray weight) is halved along its longer side,
+ * recursively, up to MAXSPART pieces.  Each piece is returned as its centre
+ * and size in units of 1/MAXSPART of the source's half-size vectors (the
+ * coordinates of rt/srcsamp.c:178-210 skipparts), in the reference's order.
+ * Sources the point is behind have none. */
+#define MAXSPART 64
+typedef struct { int ct[2], sz[2]; } spart;
+
+static void flt_partit(const double ro[3], int mp, const double cent[3], const double u[3], const double v[3],
+                       double du2, double dv2, int ct0, int ct1, int sz0, int sz1, spart *out, int *np)
+{
+    double d2 = 0, newax[3], newct[3], nu[3], nv[3];
+    int i, axis;
+    for (i = 0; i < 3; i++) d2 += (ro[i] - cent[i]) * (ro[i] - cent[i]);
+    if (mp < 2 || (d2 >= du2 && d2 >= dv2)) {
+        out[*np].ct[0] = ct0; out[*np].ct[1] = ct1;
+        out[*np].sz[0] = sz0; out[*np].sz[1] = sz1;
+        (*np)++;
+        return;
+    }
+    memcpy(nu, u, sizeof nu);
+    memcpy(nv, v, sizeof nv);
+    axis = du2 > dv2 ? 0 : 1;
+    if (axis == 0) {
+        for (i = 0; i < 3; i++) newax[i] = nu[i] = .5 * u[i];
+        du2 *= 0.25;
+        sz0 >>= 1;
+    } else {
+        for (i = 0; i < 3; i++) newax[i] = nv[i] = .5 * v[i];
+        dv2 *= 0.25;
+        sz1 >>= 1;
+    }
+    for (i = 0; i < 3; i++) newct[i] = cent[i] - newax[i];
+    flt_partit(ro, mp / 2, newct, nu, nv, du2, dv2, ct0 - (axis == 0 ? sz0 : 0), ct1 - (axis == 1 ? sz1 : 0),
+               sz0, sz1, out, np);
+    for (i = 0; i < 3; i++) newct[i] = cent[i] + newax[i];
+    flt_partit(ro, mp / 2, newct, nu, nv, du2, dv2, ct0 + (axis == 0 ? sz0 : 0), ct1 + (axis == 1 ? sz1 : 0),
+               sz0, sz1, out, np);
+}
+
+static int source_parts(const ctx *X, const osrc *s, const RAY *r, spart *out)
+{
+    int np = 0;
+    if (X->o->ds <= FTINY || (s->flags & S_DISTANT) || !(s->flags & S_FLAT)) {   /* nopart */
+        out[0].ct[0] = out[0].ct[1] = 0;
+        out[0].sz[0] = out[0].sz[1] = MAXSPART;
+        return 1;
+    }
+    {
+        double v[3] = {r->rop[0] - s->sloc[0], r->rop[1] - s->sloc[1], r->rop[2] - s->sloc[2]};
+        double dv2, du2;
+        if (vdot(v, s->snorm) <= 0.) return 0;          /* behind the source */
+        dv2 = 2. * r->rweight / X->o->ds;
+        dv2 *= dv2;
+        du2 = dv2 * vdot(s->ss[0], s->ss[0]);
+        dv2 *= vdot(s->ss[1], s->ss[1]);
+        flt_partit(r->rop, MAXSPART, s->sloc, s->ss[0], s->ss[1], du2, dv2, 0, 0, MAXSPART, MAXSPART, out, &np);
+    }
+    return np;
+}
+
+/* rt/source.c:398-556 with every partition's shadow tested (the reference's
+ * -dt threshold, which estimates untested sources from run-wide hit
+ * statistics, is taken as 0) */
 static void direct(ctx *X, RAY *r, const NORMDAT *nd)
 {
     const oscene *O = X->O;
     int sn;
+    spart parts[MAXSPART];
     for (sn = 0; sn < O->nsrc; sn++) {
         const osrc *s = &O->src[sn];
-        double vpos[3] = {0, 0, 0}, dir[3], d, dom, coef[3], val[3];
-        RAY sr;
-        int i;
+        int np, pi;
         if (s->flags & S_SKIP) continue;
         if ((s->flags & (S_PROX | S_DISTANT)) == S_PROX) {
             double dv[3] = {r->rop[0] - s->sloc[0], r->rop[1] - s->sloc[1], r->rop[2] - s->sloc[2]};
             if (vdot(dv, dv) > (s->prox + s->srad) * (s->prox + s->srad)) continue;
         }
+        np = source_parts(X, s, r, parts);
+        for (pi = 0; pi < np; pi++) {
+        double vpos[3] = {0, 0, 0}, dir[3], d, dom, coef[3], val[3];
+        const uint32_t code = GB_C_SHADOWP(sn, pi);
+        RAY sr;
+        int i;
         if (X->o->dj > FTINY) {
             double u[4];
-            draw(X, gb_child(r->path, GB_C_SHADOW(sn)), r->sensor, GB_G_SRC, u, NULL);
-            vpos[0] = X->o->dj * (1. - 2. * u[0]);
-            vpos[1] = X->o->dj * (1. - 2. * u[1]);
+            draw(X, gb_child(r->path, code), r->sensor, GB_G_SRC, u, NULL);
+            vpos[0] = X->o->dj * (1. - 2. * u[0]) * parts[pi].sz[0] * (1.0 / MAXSPART);
+            vpos[1] = X->o->dj * (1. - 2. * u[1]) * parts[pi].sz[1] * (1.0 / MAXSPART);
             vpos[2] = (s->flags & S_FLAT) ? 0 : X->o->dj * (1. - 2. * u[2]);
-            if ((s->flags & S_DISTANT) && X->o->dj > 0.7) {
-                double t0 = 1.12837917 * sqrt(1.0 - 0.5 * vpos[1] * vpos[1]);
-                double t1 = 1.12837917 * sqrt(1.0 - 0.5 * vpos[0] * vpos[0]);
-                vpos[0] *= t0;
-                vpos[1] *= t1;
-                vpos[2] = 0;
-            }
+        }
+        vpos[0] += parts[pi].ct[0] * (1.0 / MAXSPART);
+        vpos[1] += parts[pi].ct[1] * (1.0 / MAXSPART);
+        if ((s->flags & S_DISTANT) && X->o->dj > 0.7) {   /* circular source trim */
+            double t0 = 1.12837917 * sqrt(1.0 - 0.5 * vpos[1] * vpos[1]);
+            double t1 = 1.12837917 * sqrt(1.0 - 0.5 * vpos[0] * vpos[0]);
+            vpos[0] *= t0;
+            vpos[1] *= t1;
+            vpos[2] = 0;
         }
         for (i = 0; i < 3; i++)
             dir[i] = s->sloc[i] + vpos[0] * s->ss[0][i] + vpos[1] * s->ss[1][i] + vpos[2] * s->ss[2][i];
@@ -923,6 +995,7 @@ static void direct(ctx *X, RAY *r, const NORMDAT *nd)
             for (i = 0; i < 3; i++) dir[i] -= r->rop[i];
         if ((d = vnormalize(dir)) == 0.0) continue;
         dom = (s->flags & S_FLAT) ? -vdot(s->snorm, dir) : 1.0;
+        dom *= parts[pi].sz[0] * parts[pi].sz[1] * (1.0 / MAXSPART / MAXSPART);
         if (s->flags & S_DISTANT) {
             dom *= s->ss2;
             d = FHUGE;
@@ -935,7 +1008,7 @@ static void direct(ctx *X, RAY *r, const NORMDAT *nd)
         if (maxc(coef) <= 0) continue;
         /* potential: srcvalue on the source alone */
         memset(&sr, 0, sizeof sr);
-        rayorigin(X, &sr, GB_SHADOW, r, NULL, GB_C_SHADOW(sn));
+        rayorigin(X, &sr, GB_SHADOW, r, NULL, code);
         memcpy(sr.rdir, dir, sizeof dir);
         sr.rsrc = sn;
         rayclear(&sr);
@@ -949,7 +1022,7 @@ static void direct(ctx *X, RAY *r, const NORMDAT *nd)
         /* shadow test */
         {
             int thru = (r->rod > 0) ^ (vdot(r->ron, dir) > 0);
-            rayorigin(X, &sr, thru ? GB_TSHADOW : GB_RSHADOW, r, NULL, GB_C_SHADOW(sn));
+            rayorigin(X, &sr, thru ? GB_TSHADOW : GB_RSHADOW, r, NULL, code);
         }
         memcpy(sr.rcoef, coef, sizeof coef);
         memcpy(sr.rdir, dir, sizeof dir);
@@ -1000,6 +1073,7 @@ static void direct(ctx *X, RAY *r, const NORMDAT *nd)
             trace_contrib(X, &sr);
         }
         for (i = 0; i < 3; i++) r->rcol[i] += val[i];
+        }
     }
 }
 

@@ -106,7 +106,8 @@ GB_HD uint64_t gb_child(uint64_t parent, uint32_t code)
 #define GB_C_REFL       0x100001u
 #define GB_C_TRANS      0x100002u
 #define GB_C_PASS       0x100003u                   /* continue through (raytrans) */
-#define GB_C_SHADOW(s)  (0x200000u + (uint32_t)(s))
+#define GB_C_SHADOWP(s, p) (0x200000u + (uint32_t)(s) + ((uint32_t)(p) << 12))   /* partition p < 64 */
+#define GB_C_SHADOW(s)  GB_C_SHADOWP(s, 0)
 /* root path id of replica r of a sensor (replicas give independent samples) */
 #define GB_ROOT_PATH(r) ((uint64_t)(r) * 0xD1B54A32D192ED03ull)
 

@@ -796,11 +796,12 @@ static int check_shading(gb_scene *G, const gb_opts *o)
         return set_err(GB_EUNSUPPORTED, "-dv- is not implemented");
     if (o->ld != 0)
         return set_err(GB_EUNSUPPORTED, "-ld is not implemented");
-    if (o->ds > GB_FTINY) {
+    if (o->ds > GB_FTINY) {                      /* partitions are built for flat local sources */
         for (const gb_dsrc &s : G->src)
-            if (!(s.flags & (DS_SKIP | DS_DISTANT)))
+            if (!(s.flags & (DS_SKIP | DS_DISTANT)) && !(s.flags & DS_FLAT))
                 return set_err(GB_EUNSUPPORTED,
-                               "source subdivision (-ds %g) of local sources is not implemented; use -ds 0", o->ds);
+                               "source subdivision (-ds %g) of non-flat local sources is not implemented; use -ds 0",
+                               o->ds);
     }
     /* rough specular needing sampling (rt/normal.c:364 gaussamp) */
     for (size_t sl = 0; sl < G->matobj.size(); sl++) {
@@ -903,6 +904,7 @@ static int run(gb_scene *G, const gb_opts *o, int follow, const double *org_dir,
     P.maxdepth = o->lr;
     for (int j = 0; j < 3; j++) P.av[j] = (float)o->av[j];
     P.dstrsrc = (float)o->dj;
+    P.srcsizerat = (float)o->ds;
     P.specthresh = (float)o->st;
     P.follow = follow;
     P.contrib_mode = o->V;
@@ -1623,6 +1625,7 @@ extern "C" int gb_rtrace_device_noalloc(gb_scene *G, const gb_opts *o, const dou
     P.maxdepth = o->lr;
     for (int j = 0; j < 3; j++) P.av[j] = (float)o->av[j];
     P.dstrsrc = (float)o->dj;
+    P.srcsizerat = (float)o->ds;
     P.specthresh = (float)o->st;
     P.contrib_mode = o->V;
     uint64_t seed = seed_of(o);

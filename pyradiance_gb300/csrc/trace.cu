@@ -651,8 +651,122 @@ __device__ float3 shadow_chain(const gb_run &P, Ray sr, int s, Counters &cnt, fl
     return zero;
 }
 
-/* rt/source.c:398-556 (direct) with single-partition sources
- * (nextssamp/nopart) and every shadow tested */
+#define MAXSPART 64                /* pieces of a partitioned source */
+
+/* One sample of source sn's piece pi (centre ct, size sz in 1/MAXSPART of
+ * the source's half-size vectors; the whole source is 0, 0, 64, 64):
+ * rt/srcsamp.c:37-145 nextssamp, then the coefficient, the potential and
+ * the shadow ray of rt/source.c:398-556 (direct). */
+template <bool G>
+__device__ __noinline__ void direct_sample(const gb_run &P, const Ray &r, float3 hp, const Surf &s, int origin,
+                                           Counters &cnt, int slot, int sn, int pi, int ct0, int ct1, int sz0,
+                                           int sz1)
+{
+    const gb_dscene &S = P.S;
+    const gb_dsrc &src = S.src[sn];
+    const float3 sloc = f3(src.sloc[0], src.sloc[1], src.sloc[2]);
+    const uint32_t code = GB_C_SHADOWP(sn, pi);
+    float vpos[3] = {0.f, 0.f, 0.f};
+    if (P.dstrsrc > D_FTINY) {
+        gb_u4 u = gb_draw(gb_child(r.path, code), r.sensor, GB_G_SRC, P.k0, P.k1);
+        vpos[0] = P.dstrsrc * (1.f - 2.f * gb_u01(u.v[0])) * (float)sz0 * (1.f / MAXSPART);
+        vpos[1] = P.dstrsrc * (1.f - 2.f * gb_u01(u.v[1])) * (float)sz1 * (1.f / MAXSPART);
+        vpos[2] = (src.flags & DS_FLAT) ? 0.f : P.dstrsrc * (1.f - 2.f * gb_u01(u.v[2]));
+    }
+    vpos[0] += (float)ct0 * (1.f / MAXSPART);
+    vpos[1] += (float)ct1 * (1.f / MAXSPART);
+    if ((src.flags & DS_DISTANT) && P.dstrsrc > 0.7f) {
+        /* circular source trim (rt/srcsamp.c:85-96) */
+        float d = 1.12837917f;
+        float t0 = d * sqrtf(1.f - 0.5f * vpos[1] * vpos[1]);
+        float t1 = d * sqrtf(1.f - 0.5f * vpos[0] * vpos[0]);
+        vpos[0] *= t0;
+        vpos[1] *= t1;
+        vpos[2] = 0.f;
+    }
+    float3 dir = sloc + f3(src.ss[0][0], src.ss[0][1], src.ss[0][2]) * vpos[0] +
+                 f3(src.ss[1][0], src.ss[1][1], src.ss[1][2]) * vpos[1] +
+                 f3(src.ss[2][0], src.ss[2][1], src.ss[2][2]) * vpos[2];
+    if (!(src.flags & DS_DISTANT))
+        dir = dir - hp;
+    float dist = sqrtf(dot3(dir, dir));
+    if (dist == 0.f)
+        return;
+    dir = dir * (1.f / dist);
+    float dom;
+    if (src.flags & DS_FLAT)
+        dom = -(src.snorm[0] * dir.x + src.snorm[1] * dir.y + src.snorm[2] * dir.z);
+    else
+        dom = 1.f;
+    dom *= (float)(sz0 * sz1) * (1.f / (MAXSPART * MAXSPART));
+    if (src.flags & DS_DISTANT) {
+        dom *= src.ss2;
+    } else {
+        if (dom <= 1e-4f)
+            return;
+        dom *= src.ss2 / (dist * dist);
+        if ((src.flags & DS_PROX) && dist > src.prox)
+            return;
+    }
+    float3 coefd;
+    float3 coef = dirnorm(P, s, r.dir, dir, dom, G ? &coefd : nullptr);
+    if (maxc(coef) <= 0.f)
+        return;
+    /* potential (srcvalue): the source alone */
+    float4 m0 = S.mat[2 * src.mat];
+    float3 L = f3(m0.y, m0.z, m0.w);
+    if (src.flags & DS_DISTANT) {
+        float dt = dot3(sloc, dir);
+        if (2.f * D_PI * (1.f - dt) > src.ss2)
+            return;
+    } else {
+        Hit hs;
+        hs.obj = -1;
+        hs.t = D_FHUGE;
+        hs.rod = 1.f;
+        hit_object(S, src.so, hp, dir, hs, D_FTINY);
+        if (hs.obj != src.so)
+            return;                            /* aiming failure */
+        if (hs.rod < 0.f)
+            return;                            /* behind the source: black */
+    }
+    float3 pot = coef * L;
+    if (0.2126f * pot.x + 0.7152f * pot.y + 0.0722f * pot.z <= 0.f)
+        return;
+    /* shadow ray (rt/source.c:497-510) */
+    Ray sr;
+    bool thru = !(dot3(dir, s.pnorm) > 0.f);          /* thrudir, rt/ray.h:87 */
+    ray_origin(P, r, thru ? GB_TSHADOW : GB_RSHADOW, f3(1.f, 1.f, 1.f), false, code, sr, nullptr);
+    sr.coef = r.coef * coef;
+    sr.lcoef = maxc(coef);
+    sr.rsrc = sn;
+    sr.org = hp;
+    sr.dir = dir;
+    sr.origin = origin;
+    if (!G) {
+        float3 v = shadow_chain(P, sr, sn, cnt, coef, pot, nullptr);
+        add_value(P, r.sensor, r.coef * v);
+        return;
+    }
+    gb_qadj fac = r.adj;                       /* the path's factors and the shadow's glass */
+    const float3 c = r.coef * shadow_chain<true>(P, sr, sn, cnt, coef, pot, &fac);
+    grad_add(P, r.sensor, c, fac);
+    if (slot >= 0 && fac.n <= GB_ADJ_MAX) {    /* this surface's own reflectance: */
+        const double *w = P.dlde + 3ull * (r.sensor - P.sensor_base);     /* the diffuse part */
+        float g[3], cc[3] = {c.x, c.y, c.z}, cd[3] = {coefd.x, coefd.y, coefd.z}, ct[3] = {coef.x, coef.y, coef.z};
+        float mc[3] = {s.mcolor.x, s.mcolor.y, s.mcolor.z};
+        for (int i = 0; i < 3; i++)
+            g[i] = (ct[i] > 0.f && mc[i] > 0.f) ? (float)w[i] * cc[i] * (cd[i] / ct[i]) / mc[i] : 0.f;
+        grad_slot_add(P, slot, f3(g[0], g[1], g[2]));
+    }
+}
+
+/* rt/source.c:398-556 (direct) with every piece's shadow tested (the
+ * reference's -dt threshold, which estimates untested pieces from run-wide
+ * hit statistics, is taken as 0).  A flat local source larger than -ds
+ * times its distance is split as rt/srcsamp.c:260-330 (flatpart,
+ * flt_partit) splits it: halved along its longer side, recursively, up to
+ * MAXSPART pieces, lower half first; other sources are one piece. */
 template <bool G = false>
 __device__ void direct(const gb_run &P, const Ray &r, float3 hp, const Surf &s, int origin, Counters &cnt,
                        int slot)
@@ -662,102 +776,64 @@ __device__ void direct(const gb_run &P, const Ray &r, float3 hp, const Surf &s, 
         const gb_dsrc &src = S.src[sn];
         if (src.flags & DS_SKIP)
             continue;
-        float3 sloc = f3(src.sloc[0], src.sloc[1], src.sloc[2]);
+        const float3 sloc = f3(src.sloc[0], src.sloc[1], src.sloc[2]);
         if ((src.flags & (DS_PROX | DS_DISTANT)) == DS_PROX) {
             float3 dv = hp - sloc;
             float rr = src.prox + src.srad;
             if (dot3(dv, dv) > rr * rr)
                 continue;
         }
-        float vpos[3] = {0.f, 0.f, 0.f};
-        if (P.dstrsrc > D_FTINY) {
-            gb_u4 u = gb_draw(gb_child(r.path, GB_C_SHADOW(sn)), r.sensor, GB_G_SRC, P.k0, P.k1);
-            vpos[0] = P.dstrsrc * (1.f - 2.f * gb_u01(u.v[0]));
-            vpos[1] = P.dstrsrc * (1.f - 2.f * gb_u01(u.v[1]));
-            vpos[2] = (src.flags & DS_FLAT) ? 0.f : P.dstrsrc * (1.f - 2.f * gb_u01(u.v[2]));
-            if ((src.flags & DS_DISTANT) && P.dstrsrc > 0.7f) {
-                /* circular source trim (rt/srcsamp.c:85-96) */
-                float d = 1.12837917f;
-                float t0 = d * sqrtf(1.f - 0.5f * vpos[1] * vpos[1]);
-                float t1 = d * sqrtf(1.f - 0.5f * vpos[0] * vpos[0]);
-                vpos[0] *= t0;
-                vpos[1] *= t1;
-                vpos[2] = 0.f;
+        if (P.srcsizerat <= D_FTINY || (src.flags & DS_DISTANT) || !(src.flags & DS_FLAT)) {
+            direct_sample<G>(P, r, hp, s, origin, cnt, slot, sn, 0, 0, 0, MAXSPART, MAXSPART);
+            continue;
+        }
+        const float3 snorm = f3(src.snorm[0], src.snorm[1], src.snorm[2]);
+        if (dot3(hp - sloc, snorm) <= 0.f)
+            continue;                          /* behind the source: no pieces */
+        const float3 su = f3(src.ss[0][0], src.ss[0][1], src.ss[0][2]);
+        const float3 sv = f3(src.ss[1][0], src.ss[1][1], src.ss[1][2]);
+        float dv2 = 2.f * r.weight / P.srcsizerat;
+        dv2 *= dv2;
+        /* depth-first over the halving tree: a stack of pending upper halves */
+        struct Piece {
+            float3 cent, u, v;
+            float du2, dv2;
+            int mp, ct0, ct1, sz0, sz1;
+        } stack[8];
+        int top = 0, pi = 0;
+        stack[top++] = {sloc, su, sv, dv2 * dot3(su, su), dv2 * dot3(sv, sv), MAXSPART, 0, 0, MAXSPART, MAXSPART};
+        while (top > 0) {
+            Piece f = stack[--top];
+            for (;;) {
+                const float3 dc = hp - f.cent;
+                const float d2 = dot3(dc, dc);
+                if (f.mp < 2 || (d2 >= f.du2 && d2 >= f.dv2)) {
+                    direct_sample<G>(P, r, hp, s, origin, cnt, slot, sn, pi++, f.ct0, f.ct1, f.sz0, f.sz1);
+                    break;
+                }
+                Piece lo = f, hi = f;
+                float3 ax;
+                if (f.du2 > f.dv2) {                 /* halve along U */
+                    ax = f.u * 0.5f;
+                    lo.u = hi.u = ax;
+                    lo.du2 = hi.du2 = f.du2 * 0.25f;
+                    lo.sz0 = hi.sz0 = f.sz0 >> 1;
+                    lo.ct0 = f.ct0 - lo.sz0;
+                    hi.ct0 = f.ct0 + lo.sz0;
+                } else {                             /* halve along V */
+                    ax = f.v * 0.5f;
+                    lo.v = hi.v = ax;
+                    lo.dv2 = hi.dv2 = f.dv2 * 0.25f;
+                    lo.sz1 = hi.sz1 = f.sz1 >> 1;
+                    lo.ct1 = f.ct1 - lo.sz1;
+                    hi.ct1 = f.ct1 + lo.sz1;
+                }
+                lo.mp = hi.mp = f.mp / 2;
+                lo.cent = f.cent - ax;
+                hi.cent = f.cent + ax;
+                stack[top++] = hi;
+                f = lo;
             }
-        }
-        float3 dir = sloc + f3(src.ss[0][0], src.ss[0][1], src.ss[0][2]) * vpos[0] +
-                     f3(src.ss[1][0], src.ss[1][1], src.ss[1][2]) * vpos[1] +
-                     f3(src.ss[2][0], src.ss[2][1], src.ss[2][2]) * vpos[2];
-        if (!(src.flags & DS_DISTANT))
-            dir = dir - hp;
-        float dist = sqrtf(dot3(dir, dir));
-        if (dist == 0.f)
-            continue;
-        dir = dir * (1.f / dist);
-        float dom;
-        if (src.flags & DS_FLAT)
-            dom = -(src.snorm[0] * dir.x + src.snorm[1] * dir.y + src.snorm[2] * dir.z);
-        else
-            dom = 1.f;
-        if (src.flags & DS_DISTANT) {
-            dom *= src.ss2;
-        } else {
-            if (dom <= 1e-4f)
-                continue;
-            dom *= src.ss2 / (dist * dist);
-            if ((src.flags & DS_PROX) && dist > src.prox)
-                continue;
-        }
-        float3 coefd;
-        float3 coef = dirnorm(P, s, r.dir, dir, dom, G ? &coefd : nullptr);
-        if (maxc(coef) <= 0.f)
-            continue;
-        /* potential (srcvalue): the source alone */
-        float4 m0 = S.mat[2 * src.mat];
-        float3 L = f3(m0.y, m0.z, m0.w);
-        if (src.flags & DS_DISTANT) {
-            float dt = dot3(sloc, dir);
-            if (2.f * D_PI * (1.f - dt) > src.ss2)
-                continue;
-        } else {
-            Hit hs;
-            hs.obj = -1;
-            hs.t = D_FHUGE;
-            hs.rod = 1.f;
-            hit_object(S, src.so, hp, dir, hs, D_FTINY);
-            if (hs.obj != src.so)
-                continue;                      /* aiming failure */
-            if (hs.rod < 0.f)
-                continue;                      /* behind the source: black */
-        }
-        float3 pot = coef * L;
-        if (0.2126f * pot.x + 0.7152f * pot.y + 0.0722f * pot.z <= 0.f)
-            continue;
-        /* shadow ray (rt/source.c:497-510) */
-        Ray sr;
-        bool thru = !(dot3(dir, s.pnorm) > 0.f);      /* thrudir, rt/ray.h:87 */
-        ray_origin(P, r, thru ? GB_TSHADOW : GB_RSHADOW, f3(1.f, 1.f, 1.f), false, GB_C_SHADOW(sn), sr, nullptr);
-        sr.coef = r.coef * coef;
-        sr.lcoef = maxc(coef);
-        sr.rsrc = sn;
-        sr.org = hp;
-        sr.dir = dir;
-        sr.origin = origin;
-        if (!G) {
-            float3 v = shadow_chain(P, sr, sn, cnt, coef, pot, nullptr);
-            add_value(P, r.sensor, r.coef * v);
-            continue;
-        }
-        gb_qadj fac = r.adj;                   /* the path's factors and the shadow's glass */
-        const float3 c = r.coef * shadow_chain<true>(P, sr, sn, cnt, coef, pot, &fac);
-        grad_add(P, r.sensor, c, fac);
-        if (slot >= 0 && fac.n <= GB_ADJ_MAX) {  /* this surface's own reflectance: */
-            const double *w = P.dlde + 3ull * (r.sensor - P.sensor_base);     /* the diffuse part */
-            float g[3], cc[3] = {c.x, c.y, c.z}, cd[3] = {coefd.x, coefd.y, coefd.z}, ct[3] = {coef.x, coef.y, coef.z};
-            float mc[3] = {s.mcolor.x, s.mcolor.y, s.mcolor.z};
-            for (int i = 0; i < 3; i++)
-                g[i] = (ct[i] > 0.f && mc[i] > 0.f) ? (float)w[i] * cc[i] * (cd[i] / ct[i]) / mc[i] : 0.f;
-            grad_slot_add(P, slot, f3(g[0], g[1], g[2]));
         }
     }
 }

@@ -68,6 +68,7 @@ typedef struct {
     int   maxdepth;
     float av[3];
     float dstrsrc;
+    float srcsizerat;          /* -ds: split flat local sources larger than this times their distance */
     float specthresh;
     int   follow;              /* rcontrib: every source is followed (SFOLLOW) */
     int   contrib_mode;        /* rcontrib -V */

@@ -64,6 +64,22 @@ def c1_direct(tmp: Path) -> None:
     print("c1_direct: lit fraction %.4f" % (irr[:, 0] > 0).mean())
 
 
+def c1_partitioned(tmp: Path) -> None:
+    """Direct irradiance with the light partitioned (rtrace -I -ab 0 -dj 0
+    -ds 0.2 -dr 0 -dt 0): the 100 x 100 grid at 0.8 m and a 50 x 50 grid at
+    2.5 m, half a metre below the light, where it splits into many pieces.
+    -dt 0 tests every partition's shadow (the default -dt estimates untested
+    ones from run-wide statistics)."""
+    octp = oconv(w.daylight_room(), tmp, "c1p")
+    rays = np.vstack([w.sensor_grid(100, 100), w.sensor_grid(50, 50, z=2.5)])
+    inp = rays.astype("<f8").tobytes()
+    irr = np.frombuffer(run(["rtrace", "-h", "-u-", "-I", "-ab", "0", "-dj", "0", "-ds", "0.2", "-dr", "0",
+                             "-dt", "0", "-fdd", "-ov", octp], inp), dtype="<f8").reshape(-1, 3)
+    np.savez_compressed(OUT / "c1_partitioned.npz", rays=rays, irradiance=irr,
+                        cmd="rtrace -h -u- -I -ab 0 -dj 0 -ds 0.2 -dr 0 -dt 0 -fdd -ov")
+    print("c1_partitioned: lit fraction %.4f" % (irr[:, 0] > 0).mean())
+
+
 def zoo(tmp: Path) -> None:
     """Every primitive type: first-hit surface and distance of random rays,
     and deterministic -ab 0 radiance (direct + mirror reflections)."""
@@ -166,15 +182,14 @@ def ref_fixture_trace() -> None:
 def main() -> None:
     if not (BIN / "rtrace").exists():
         sys.exit("reference programs missing: make -f oracle/build_ref.mk REF=/root/reference -j8")
+    parts = {"octree": octree_digests, "c1": c1_direct, "c1p": c1_partitioned, "zoo": zoo,
+             "dct": lambda tmp: dct_small(), "trace_oct": lambda tmp: ref_fixture_trace(),
+             "c2ab1": lambda tmp: c2_stats(tmp, ab=1, K=256), "c2ab3": lambda tmp: c2_stats(tmp, ab=3, K=256)}
+    only = sys.argv[1:] or list(parts)         # e.g. make_golden.py c1p
     with tempfile.TemporaryDirectory() as td:
         tmp = Path(td)
-        octree_digests(tmp)
-        c1_direct(tmp)
-        zoo(tmp)
-        dct_small()
-        ref_fixture_trace()
-        c2_stats(tmp, ab=1, K=256)
-        c2_stats(tmp, ab=3, K=256)
+        for name in only:
+            parts[name](tmp)
 
 
 if __name__ == "__main__":

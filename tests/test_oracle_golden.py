@@ -41,6 +41,18 @@ def test_c1_direct_irradiance_and_hits(oscenes):
     np.testing.assert_allclose(ht, g["hit_dist"], rtol=1e-7)  # frozen-octree float precision
 
 
+def test_c1_partitioned_source(oscenes):
+    """-ds 0.2: the light split into pieces as rt/srcsamp.c:260-330 does
+    (many near the 2.5 m grid); -dt 0, every piece's shadow tested."""
+    g = golden("c1_partitioned.npz")
+    o = po.default_opts("rtrace", I=1, ab=0, dj=0, ds=0.2, dr=0, dt=0, u=0)
+    rgb, _, _, _ = po.rtrace(oscenes["c1"], o, g["rays"], hits=False, threads=8)
+    ref = g["irradiance"]
+    lit = ref[:, 0] > 0
+    np.testing.assert_array_equal(rgb[~lit], 0.0)
+    assert (np.abs(rgb[lit] - ref[lit]) / ref[lit]).max() < 1e-6
+
+
 def test_zoo_cast_and_direct(oscenes):
     g = golden("zoo.npz")
     sc = oscenes["zoo"]
