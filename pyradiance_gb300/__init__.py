@@ -142,8 +142,17 @@ def _rtrace(rays: bytes, octree, header: bool = True, inform: str = "a", outform
     args.append(f"-f{inform}{outform}")
     if outspec:
         args.append(f"-o{outspec}")
-    if trace_exclude or trace_include or trace_exclude_file or trace_include_file:
-        raise GbError(-3, "trace include/exclude lists are not supported")
+    # the same single argument as src/pyradiance/rt.py:342-349, which the
+    # option parser rejects as rt/rtmain.c:210-214 does (the list's name
+    # must be a separate argument): a command line error either way
+    if trace_exclude:
+        args.append(f"-te{trace_exclude}")
+    elif trace_include:
+        args.append(f"-ti{trace_include}")
+    elif trace_exclude_file:
+        args.append(f"-tE{trace_exclude_file}")
+    elif trace_include_file:
+        args.append(f"-tI{trace_include_file}")
     if uncorrelated:
         args.append("-u+")
     if xres is not None:

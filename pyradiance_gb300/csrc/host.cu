@@ -754,7 +754,22 @@ extern "C" int gb_opts_parse(int argc, const char *const *argv, int prog, gb_opt
         case 'e': case 'p': case 'M':
             ok = false;
             break;
-        case 't': NEED(1); i++; break;            /* report interval */
+        case 't':
+            /* -t N report interval; -ti/-te modifier and -tI/-tE file of
+             * the ray-tree trace lists (rt/rtmain.c:210-260), which select
+             * what the '~' part of -o prints; the value and the first-hit
+             * outputs do not depend on them */
+            if (a[2] && (!strchr("iIeE", a[2]) || a[3])) { ok = false; break; }
+            NEED(1);
+            if (a[2] == 'I' || a[2] == 'E') {
+                FILE *f = fopen(argv[i + 1], "r");
+                if (!f)
+                    return set_err(GB_EIO, "cannot open trace %s file \"%s\"", a[2] == 'I' ? "include" : "exclude",
+                                   argv[i + 1]);
+                fclose(f);
+            }
+            i++;
+            break;
         default: ok = false;
         }
         if (!ok) {

@@ -48,6 +48,25 @@ def test_option_parsing(lib):
         lib.parse_opts(["-me", "1", "1", "1"], lib.GB_PROG_RTRACE)
 
 
+def test_trace_list_options(lib, tmp_path):
+    """-ti/-te take the modifier as the next argument and -tI/-tE a file
+    that must open (rt/rtmain.c:210-260); the single-argument form that
+    pyradiance's rtrace wrapper builds (src/pyradiance/rt.py:342-349) is a
+    command line error, as it is for the reference's rtrace."""
+    o, used = lib.parse_opts(["-ti", "glass", "-te", "light", "-t", "10", "-ab", "1"], lib.GB_PROG_RTRACE)
+    assert used == 8 and o.ab == 1
+    f = tmp_path / "mods.txt"
+    f.write_text("glass light\n")
+    _, used = lib.parse_opts(["-tI", str(f), "-tE", str(f)], lib.GB_PROG_RTRACE)
+    assert used == 4
+    for bad in (["-teglass"], ["-tI", str(tmp_path / "none.txt")], ["-ti"], ["-tx", "a"]):
+        with pytest.raises(lib.GbError):
+            lib.parse_opts(bad, lib.GB_PROG_RTRACE)
+    import pyradiance_gb300 as gb
+    with pytest.raises(RuntimeError):
+        gb.rtrace(b"0 0 0 0 0 1\n", b"", trace_exclude="glass")
+
+
 def nbins(lib, mods):
     arr = (lib.GbModspec * len(mods))()
     keep = []
