@@ -26,8 +26,8 @@
  *   m_light            rt/source.c:749-793
  *   direct             rt/source.c:398-556 (srcray :219, srcvalue :261,
  *                      nextssamp rt/srcsamp.c:37-145 single partition)
- *   m_normal/dirnorm   rt/normal.c:72-360 (pure specular; rough specular
- *                      below -st only)
+ *   m_normal/dirnorm   rt/normal.c:72-360
+ *   gaussamp           rt/normal.c:364-440 (reflection)
  *   m_glass            rt/glass.c:45-165
  *   multambient        rt/ambient.c:229-300 (-aa 0 branch)
  *   samp_hemi/ambsample rt/ambcomp.c:177-250, 351-421
@@ -284,6 +284,33 @@ static void draw(const ctx *X, uint64_t path, uint32_t sensor, uint32_t group, d
     int i;
     for (i = 0; i < 4; i++) u[i] = (double)gb_u01(v.v[i]);
     if (raw) *raw = v.v[3];
+}
+
+/* getperpendicular(ux, onrm, 1) (common/fvect.c:159-196) with the
+ * randomisation drawn from group `group` of ray r */
+static void rand_perp(const ctx *X, const RAY *r, uint32_t group, const double onrm[3], double ux[3])
+{
+    double u[4], v1[3];
+    uint32_t raw;
+    int ord[3], ii;
+    draw(X, r->path, r->sensor, group, u, &raw);
+    v1[0] = 0.5 - u[0];
+    v1[1] = 0.5 - u[1];
+    v1[2] = 0.5 - u[2];
+    switch (gb_irand(raw, 6u)) {
+    case 0: ord[0] = 0; ord[1] = 1; ord[2] = 2; break;
+    case 1: ord[0] = 0; ord[1] = 2; ord[2] = 1; break;
+    case 2: ord[0] = 1; ord[1] = 0; ord[2] = 2; break;
+    case 3: ord[0] = 1; ord[1] = 2; ord[2] = 0; break;
+    case 4: ord[0] = 2; ord[1] = 0; ord[2] = 1; break;
+    default: ord[0] = 2; ord[1] = 1; ord[2] = 0; break;
+    }
+    for (ii = 3; ii--;)
+        if ((-0.6 < onrm[ord[ii]]) & (onrm[ord[ii]] < 0.6)) break;
+    if (ii < 0) ii = 0;
+    v1[ord[ii]] = 1.0;
+    vcross(ux, v1, onrm);
+    vnormalize(ux);
 }
 
 /* rayclear (rt/raytrace.c:138-159) */
@@ -1106,31 +1133,8 @@ static void multambient(ctx *X, double aval[3], RAY *r, const double nrm[3])
     if (n < 1) n = 1;
     memcpy(onrm, r->ron, sizeof onrm);
     for (k = 0; k < 3; k++) acoef[k] = aval[k] / (n * n);
-    {
-        /* getperpendicular(ux, onrm, 1) with the frame draw */
-        double u[4], v1[3];
-        uint32_t raw;
-        int ord[3], ii;
-        draw(X, r->path, r->sensor, GB_G_FRAME, u, &raw);
-        v1[0] = 0.5 - u[0];
-        v1[1] = 0.5 - u[1];
-        v1[2] = 0.5 - u[2];
-        switch (gb_irand(raw, 6u)) {
-        case 0: ord[0] = 0; ord[1] = 1; ord[2] = 2; break;
-        case 1: ord[0] = 0; ord[1] = 2; ord[2] = 1; break;
-        case 2: ord[0] = 1; ord[1] = 0; ord[2] = 2; break;
-        case 3: ord[0] = 1; ord[1] = 2; ord[2] = 0; break;
-        case 4: ord[0] = 2; ord[1] = 0; ord[2] = 1; break;
-        default: ord[0] = 2; ord[1] = 1; ord[2] = 0; break;
-        }
-        for (ii = 3; ii--;)
-            if ((-0.6 < onrm[ord[ii]]) & (onrm[ord[ii]] < 0.6)) break;
-        if (ii < 0) ii = 0;
-        v1[ord[ii]] = 1.0;
-        vcross(ux, v1, onrm);
-        vnormalize(ux);
-        vcross(uy, onrm, ux);
-    }
+    rand_perp(X, r, GB_G_FRAME, onrm, ux);
+    vcross(uy, onrm, ux);
     {
         gb_lot *L = (gb_lot *)malloc(sizeof(gb_lot));
         float (*rows)[2] = (float (*)[2])malloc(sizeof(float) * 4 * n);
@@ -1173,6 +1177,78 @@ static void multambient(ctx *X, double aval[3], RAY *r, const double nrm[3])
     }
 dumbamb:
     for (k = 0; k < 3; k++) aval[k] *= X->o->av[k];
+}
+
+/* The gaussamp trial of rt/normal.c:398-420 (see gaussamp below): returns
+ * the cosine of the sampled direction with the surface normal. */
+static double spec_trial(const ctx *X, const RAY *r, const NORMDAT *np, const double u[3], const double v[3], int t,
+                         double sdir[3])
+{
+    double q[4], rv0, rv1, d, cosp, sinp, h[3], s;
+    int i;
+    draw(X, r->path, r->sensor, GB_G_SPEC + (uint32_t)(t >> 1), q, NULL);
+    rv0 = q[(t & 1) * 2];
+    rv1 = q[(t & 1) * 2 + 1];
+    d = 2.0 * PI * rv0;
+    cosp = cos(d);
+    sinp = sin(d);
+    if ((0. <= X->o->ss) & (X->o->ss < 1.)) rv1 = 1.0 - X->o->ss * rv1;
+    d = rv1 <= FTINY ? 1.0 : sqrt(np->alpha2 * -log(rv1));
+    for (i = 0; i < 3; i++) h[i] = np->pnorm[i] + d * (cosp * u[i] + sinp * v[i]);
+    s = -2.0 * vdot(h, r->rdir) / (1.0 + d * d);
+    for (i = 0; i < 3; i++) sdir[i] = r->rdir[i] + s * h[i];
+    vnormalize(sdir);
+    return vdot(sdir, r->ron);
+}
+
+/* rt/normal.c:364-440 gaussamp, reflected part (opaque materials): one
+ * sample of the rough specular lobe, or with -ss above 1.5 ss times the ray
+ * weight of them with the W-G-M-D weighting.  Trials draw from the hit
+ * ray's GB_G_SPEC groups instead of urand/frandom; sample k traces as child
+ * GB_C_SPEC(k), all samples sharing the first one's rayorigin. */
+#define MAXITER 10
+static void gaussamp(ctx *X, NORMDAT *np, RAY *r)
+{
+    RAY sr;
+    double u[3], v[3], scol[3] = {0, 0, 0}, d;
+    int nstarget, nstaken, ntrials, maxiter, i;
+    if (!np->refl || np->rblt) return;
+    rand_perp(X, r, GB_G_SPECF, np->pnorm, u);
+    vcross(v, np->pnorm, u);
+    if (rayorigin(X, &sr, GB_RSPECULAR, r, np->scolor, GB_C_SPEC(0)) != 0) return;
+    nstarget = 1;
+    if (X->o->ss > 1.5) {
+        nstarget = (int)(X->o->ss * r->rweight + .5);
+        if (sr.rweight <= X->o->lw * nstarget) nstarget = (int)(sr.rweight / X->o->lw);
+        if (nstarget > 1) {
+            d = 1. / nstarget;
+            for (i = 0; i < 3; i++) sr.rcoef[i] *= d;
+            sr.rweight *= d;
+        } else
+            nstarget = 1;
+    }
+    maxiter = MAXITER * nstarget;
+    for (nstaken = ntrials = 0; nstaken < nstarget && ntrials < maxiter; ntrials++) {
+        double sdir[3];
+        d = spec_trial(X, r, np, u, v, ntrials, sdir);
+        if (d <= FTINY) continue;
+        if (nstaken) {
+            rayclear(&sr);
+            sr.path = gb_child(r->path, GB_C_SPEC(nstaken));
+        }
+        memcpy(sr.rdir, sdir, sizeof sr.rdir);
+        raytrace(X, &sr);
+        if (nstarget > 1) {
+            d = 2. / (1. + r->rod / d);
+            for (i = 0; i < 3; i++) scol[i] += sr.rcol[i] * d;
+        } else
+            for (i = 0; i < 3; i++) r->rcol[i] += sr.rcol[i] * sr.rcoef[i];
+        ++nstaken;
+    }
+    if (nstarget > 1) {
+        d = (double)nstarget / ntrials;
+        for (i = 0; i < 3; i++) r->rcol[i] += scol[i] * sr.rcoef[i] * d;
+    }
 }
 
 static int m_normal(ctx *X, int m, RAY *r)
@@ -1218,6 +1294,7 @@ static int m_normal(ctx *X, int m, RAY *r)
         }
     }
     if (nd.pure && nd.rdiff <= FTINY) return 1;
+    if (!nd.pure) gaussamp(X, &nd, r);
     if (nd.rdiff > FTINY) {
         for (i = 0; i < 3; i++) sct[i] = nd.mcolor[i] * nd.rdiff + (nd.rblt ? nd.scolor[i] : 0);
         multambient(X, sct, r, nd.pnorm);

@@ -82,10 +82,15 @@ GB_HD uint32_t gb_irand(uint32_t x, uint32_t m) { return (uint32_t)(((uint64_t)x
  *   1  drawn at the ray's hit for a hemisphere frame: [0..2] perpendicular
  *      randomisation, [3] axis order
  *   2+ per source sample jitter (2 + source index)
+ *   GB_G_SPECF  drawn at the hit for the frame of the specular lobe
+ *   GB_G_SPEC+j two trials of specular lobe sampling per group: trial t
+ *      uses words 2(t&1) and 2(t&1)+1 of group GB_G_SPEC + (t >> 1)
  */
 #define GB_G_CREATE 0u
 #define GB_G_FRAME  1u
 #define GB_G_SRC    2u
+#define GB_G_SPECF  0x7F000000u
+#define GB_G_SPEC   0x7F000001u
 
 GB_HD gb_u4 gb_draw(uint64_t path, uint32_t sensor, uint32_t group, uint32_t k0, uint32_t k1)
 {
@@ -106,6 +111,8 @@ GB_HD uint64_t gb_child(uint64_t parent, uint32_t code)
 #define GB_C_REFL       0x100001u
 #define GB_C_TRANS      0x100002u
 #define GB_C_PASS       0x100003u                   /* continue through (raytrans) */
+#define GB_SPEC_MAXITER 10                            /* rt/normal.c:25 MAXITER */
+#define GB_C_SPEC(k)    (0x110000u + (uint32_t)(k))   /* specular lobe sample k < 2^16 */
 #define GB_C_SHADOWP(s, p) (0x200000u + (uint32_t)(s) + ((uint32_t)(p) << 12))   /* partition p < 64 */
 #define GB_C_SHADOW(s)  GB_C_SHADOWP(s, 0)
 /* root path id of replica r of a sensor (replicas give independent samples) */

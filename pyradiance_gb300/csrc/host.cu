@@ -818,16 +818,22 @@ static int check_shading(gb_scene *G, const gb_opts *o)
                                "source subdivision (-ds %g) of non-flat local sources is not implemented; use -ds 0",
                                o->ds);
     }
-    /* rough specular needing sampling (rt/normal.c:364 gaussamp) */
-    for (size_t sl = 0; sl < G->matobj.size(); sl++) {
-        float4 a = G->mat[2 * sl], b = G->mat[2 * sl + 1];
-        int k = (int)a.x;
-        if ((k == DM_PLASTIC || k == DM_METAL) && b.y * b.y > GB_FTINY) {
+    /* rough specular sampled with several samples per hit (-ss > 1.5,
+     * rt/normal.c:387-398): the reference weights their values, not their
+     * ray coefficients, by the W-G-M-D adjustment, so rcontrib's bins (built
+     * from the coefficients, rt/raytrace.c:408-442) would differ from the
+     * values; rtrace is supported */
+    if (o->prog == GB_PROG_RCONTRIB && o->ss > 1.5) {
+        for (size_t sl = 0; sl < G->matobj.size(); sl++) {
+            float4 a = G->mat[2 * sl], b = G->mat[2 * sl + 1];
+            int k = (int)a.x;
             double rspec = b.x;
-            if (rspec > GB_FTINY && !(o->st >= rspec - GB_FTINY))
+            if ((k == DM_PLASTIC || k == DM_METAL) && b.y * b.y > GB_FTINY && rspec > GB_FTINY &&
+                !(o->st >= rspec - GB_FTINY))
                 return set_err(GB_EUNSUPPORTED,
-                               "rough specular sampling of \"%s\" (specularity %g above -st %g) is not implemented",
-                               G->H.objs[G->matobj[sl]].name, rspec, o->st);
+                               "rcontrib with -ss %g samples the rough specular lobe of \"%s\" several times per "
+                               "hit, which is not implemented; use -ss 1 or less",
+                               o->ss, G->H.objs[G->matobj[sl]].name);
         }
     }
     return GB_OK;
@@ -921,6 +927,7 @@ static int run(gb_scene *G, const gb_opts *o, int follow, const double *org_dir,
     P.dstrsrc = (float)o->dj;
     P.srcsizerat = (float)o->ds;
     P.specthresh = (float)o->st;
+    P.specjitter = (float)o->ss;
     P.follow = follow;
     P.contrib_mode = o->V;
     uint64_t seed = seed_of(o);
@@ -1642,6 +1649,7 @@ extern "C" int gb_rtrace_device_noalloc(gb_scene *G, const gb_opts *o, const dou
     P.dstrsrc = (float)o->dj;
     P.srcsizerat = (float)o->ds;
     P.specthresh = (float)o->st;
+    P.specjitter = (float)o->ss;
     P.contrib_mode = o->V;
     uint64_t seed = seed_of(o);
     P.k0 = (uint32_t)seed;

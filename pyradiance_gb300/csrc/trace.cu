@@ -869,6 +869,89 @@ __device__ __forceinline__ void setup_surf(const gb_run &P, int mk, float4 m0, f
     s.rblt = !s.pure && P.specthresh >= s.rspec - D_FTINY;
 }
 
+/* One trial of the specular lobe (rt/normal.c:398-420): a half vector
+ * drawn about the normal with a Gaussian slope of variance alpha2, the
+ * incident direction mirrored about it.  Returns the cosine of the sample
+ * with the surface normal (the caller rejects samples at or below FTINY). */
+__device__ __forceinline__ float spec_trial(const gb_run &P, const Ray &r, const Surf &su, float3 u, float3 v, int t,
+                                            float3 &sdir)
+{
+    const gb_u4 q = gb_draw(r.path, r.sensor, GB_G_SPEC + (uint32_t)(t >> 1), P.k0, P.k1);
+    const int w = (t & 1) * 2;
+    float rv0 = gb_u01(q.v[w]), rv1 = gb_u01(q.v[w + 1]);
+    float sinp, cosp;
+    sincosf(2.f * (float)M_PI * rv0, &sinp, &cosp);
+    if ((0.f <= P.specjitter) & (P.specjitter < 1.f))
+        rv1 = 1.f - P.specjitter * rv1;
+    const float d = rv1 <= D_FTINY ? 1.f : sqrtf(su.alpha2 * -logf(rv1));
+    const float3 h = su.pnorm + (u * cosp + v * sinp) * d;
+    const float s = -2.f * dot3(h, r.dir) / (1.f + d * d);
+    sdir = normalize3(r.dir + h * s);
+    return dot3(sdir, su.pnorm);
+}
+
+/* rt/normal.c:364-440 gaussamp, reflection: sample the rough specular lobe
+ * of a plastic or metal hit (specularity above -st).  One sample, or with
+ * -ss above 1.5 ss times the ray weight of them, each weighted by the
+ * W-G-M-D adjustment 2/(1 + cos_in/cos_out) and by samples wanted over
+ * trials made; every trial is drawn here, so the weights are known before
+ * the children are queued.  Children share one Russian-roulette decision,
+ * as the reference's samples share one rayorigin. */
+template <bool G>
+__device__ __noinline__ void gaussamp(const gb_run &P, const Ray &r, const Surf &su, float rod, float3 hp, int obj)
+{
+    const gb_u4 uf = gb_draw(r.path, r.sensor, GB_G_SPECF, P.k0, P.k1);
+    const float3 u = perpendicular(su.pnorm, make_float4(gb_u01(uf.v[0]), gb_u01(uf.v[1]), gb_u01(uf.v[2]), 0.f),
+                                   uf.v[3]);
+    const float3 v = cross3(su.pnorm, u);
+    Ray c;
+    if (!ray_origin(P, r, GB_RSPECULAR, su.scolor, true, GB_C_SPEC(0), c, nullptr))
+        return;
+    int nst = 1;
+    if (P.specjitter > 1.5f) {
+        nst = (int)(P.specjitter * r.weight + .5f);
+        if (c.weight <= P.minweight * (float)nst)
+            nst = (int)(c.weight / P.minweight);
+        if (nst > 1) {
+            const float d = 1.f / (float)nst;
+            c.coef = c.coef * d;
+            c.weight *= d;
+        } else
+            nst = 1;
+    }
+    const int maxiter = GB_SPEC_MAXITER * nst;
+    float post = 1.f;                   /* samples wanted / trials made */
+    if (nst > 1) {
+        int taken = 0, t = 0;
+        for (; taken < nst && t < maxiter; t++) {
+            float3 sd;
+            if (spec_trial(P, r, su, u, v, t, sd) > D_FTINY)
+                taken++;
+        }
+        post = (float)nst / (float)t;
+    }
+    c.org = hp;
+    c.origin = obj;
+    if (G)                              /* specular color: not a parameter */
+        c.adj = r.adj;
+    const float3 coef = c.coef;
+    int taken = 0;
+    for (int t = 0; taken < nst && t < maxiter; t++) {
+        float3 sd;
+        const float cs = spec_trial(P, r, su, u, v, t, sd);
+        if (cs <= D_FTINY)
+            continue;
+        c.dir = sd;
+        if (nst > 1) {
+            if (taken)
+                c.path = gb_child(r.path, GB_C_SPEC(taken));
+            c.coef = coef * (2.f / (1.f + rod / cs) * post);
+        }
+        push_ray<G>(P, c);
+        taken++;
+    }
+}
+
 /* Shade ray r given its trace result (h.obj < 0: the ray left the scene)
  * and push every child ray to the next generation's queue
  * (rt/raytrace.c:163-256 raytrace / rayshade, the material routines). */
@@ -1001,6 +1084,11 @@ __device__ void shade_ray(const gb_run &P, const Ray &r, const Hit &h, Counters 
     }
     if (S.nsrc > 0)
         direct<G>(P, r, hp, su, h.obj, cnt, ms);
+    /* the rough specular lobe (the reference samples it before the diffuse
+     * terms; every draw is keyed by the path, so the order is free, and
+     * last keeps the fewest values live across the call) */
+    if (su.refl && !su.pure && !su.rblt)
+        gaussamp<G>(P, r, su, rod, hp, h.obj);
 }
 
 /* Persistent work loop: each warp takes work items 32 at a time with one

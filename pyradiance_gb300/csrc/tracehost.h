@@ -70,6 +70,7 @@ typedef struct {
     float dstrsrc;
     float srcsizerat;          /* -ds: split flat local sources larger than this times their distance */
     float specthresh;
+    float specjitter;          /* -ss */
     int   follow;              /* rcontrib: every source is followed (SFOLLOW) */
     int   contrib_mode;        /* rcontrib -V */
     uint32_t k0, k1;           /* random stream key */

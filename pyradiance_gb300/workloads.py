@@ -21,6 +21,8 @@ Workloads (sizes are the defaults):
   interior triangles (two edges of length U[0.05, 0.5] m from a random
   vertex, reflectance U[0.1, 0.8], one material each), and the glow sky and
   ground of the reference's own test fixture (tests/Resources/skyglow.rad).
+* ``glossy_room`` -- the room with rough specular plastic and metal
+  (the specular-lobe sampling workload).
 * ``sensor_grid`` -- cell-centred n x m grid at z = 0.8 facing +z.
 * ``dc_sky`` -- daylight-coefficient and sky matrices with the value
   distributions of the annual dctimestep workload.
@@ -154,6 +156,51 @@ def window_room(seed: int = 0, ntri: int = 20000, nmat: int | None = None) -> st
     for i in range(ntri):
         out.append(_poly(f"tri_mat{i % nm}", f"tri{i}", [v0[i], v1[i], v2[i]]))
     out.append(SKY_GLOW)
+    return "".join(out)
+
+
+def glossy_room(seed: int = 0, nboxes: int = 40, nspheres: int = 8) -> str:
+    """The room of ``daylight_room`` with rough specular surfaces: a rough
+    metal floor (specularity 0.5, roughness 0.08), rough plastic walls and
+    ceiling (0.04, 0.12), floor-standing boxes cycling through rough plastic
+    (0.06, 0.2), rough metal (0.8, 0.04), pure metal (0.9, 0) and matte
+    plastic, rough metal spheres (0.7, 0.1), and the ceiling light."""
+    rng = np.random.default_rng(seed)
+    X, Y, Z = ROOM
+    out = ["void metal floor_mat\n0\n0\n5 .7 .65 .6 .5 .08\n\n",
+           "void plastic wall_mat\n0\n0\n5 .6 .6 .6 .04 .12\n\n",
+           "void metal ball_mat\n0\n0\n5 .8 .8 .75 .7 .1\n\n"]
+    out.append(_poly("floor_mat", "floor", [(0, 0, 0), (X, 0, 0), (X, Y, 0), (0, Y, 0)]))
+    out.append(_poly("wall_mat", "ceiling", [(0, 0, Z), (0, Y, Z), (X, Y, Z), (X, 0, Z)]))
+    out.append(_poly("wall_mat", "north", [(0, Y, 0), (X, Y, 0), (X, Y, Z), (0, Y, Z)]))
+    out.append(_poly("wall_mat", "west", [(0, 0, 0), (0, Y, 0), (0, Y, Z), (0, 0, Z)]))
+    out.append(_poly("wall_mat", "east", [(X, 0, 0), (X, 0, Z), (X, Y, Z), (X, Y, 0)]))
+    out.append(_poly("wall_mat", "south", [(0, 0, 0), (0, 0, Z), (X, 0, Z), (X, 0, 0)]))
+    sizes = rng.uniform(0.3, 1.2, size=(nboxes, 3))
+    pos = rng.uniform(0.0, 1.0, size=(nboxes, 2))
+    rho = rng.uniform(0.3, 0.8, size=nboxes)
+    lift = rng.uniform(0.002, 0.02, size=nboxes)
+    for i in range(nboxes):
+        s = sizes[i]
+        r = rho[i]
+        kind = i % 4
+        if kind == 0:
+            out.append(f"void plastic box_mat{i}\n0\n0\n5 {r:.9g} {r:.9g} {r:.9g} .06 .2\n\n")
+        elif kind == 1:
+            out.append(f"void metal box_mat{i}\n0\n0\n5 {r:.9g} {r * .9:.9g} {r * .8:.9g} .8 .04\n\n")
+        elif kind == 2:
+            out.append(f"void metal box_mat{i}\n0\n0\n5 {r:.9g} {r:.9g} {r:.9g} .9 0\n\n")
+        else:
+            out.append(_mat_plastic(f"box_mat{i}", (r,) * 3))
+        out.append(_box(f"box_mat{i}", f"box{i}", (pos[i, 0] * (X - s[0]), pos[i, 1] * (Y - s[1]), lift[i]), s))
+    c = rng.uniform((1, 1, 0.4), (X - 1, Y - 1, Z - 0.8), size=(nspheres, 3))
+    rad = rng.uniform(0.15, 0.4, size=nspheres)
+    for i in range(nspheres):
+        out.append(f"ball_mat sphere ball{i}\n0\n0\n4 {c[i, 0]:.9g} {c[i, 1]:.9g} {c[i, 2]:.9g} {rad[i]:.9g}\n\n")
+    out.append("void light light_mat\n0\n0\n3 100 100 100\n\n")
+    cx, cy = X / 2, Y / 2
+    out.append(_poly("light_mat", "light", [(cx - .5, cy - .5, Z - 0.01), (cx - .5, cy + .5, Z - 0.01),
+                                            (cx + .5, cy + .5, Z - 0.01), (cx + .5, cy - .5, Z - 0.01)]))
     return "".join(out)
 
 

@@ -25,7 +25,7 @@ def scene_dir(tmp_path_factory):
     from pyradiance_gb300 import workloads as w
     d = tmp_path_factory.mktemp("scenes")
     for name, text in (("c1", w.daylight_room()), ("c2", w.window_room()), ("zoo", w.shape_zoo()),
-                       ("c2e", w.window_room(ntri=0))):
+                       ("c2e", w.window_room(ntri=0)), ("glossy", w.glossy_room())):
         (d / f"{name}.rad").write_text(text)
     return d
 

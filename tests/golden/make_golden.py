@@ -98,6 +98,32 @@ def zoo(tmp: Path) -> None:
                                                                    "west", "light")) for n in hit))
 
 
+def glossy(tmp: Path, n: int = 300, K: int = 1024) -> None:
+    """Rough specular plastic and metal (glossy_room), radiance of view rays
+    from random interior points: deterministic with -st 1 (every rough lobe
+    below the specular threshold: direct Gaussian term only, no sampling),
+    and with the lobe sampled (-st 0 one sample; -ss 3 several per hit) as
+    per-ray means and standard errors over K replicas of each ray.  The
+    sampled runs use -u+ (the reference's default): with -u- the replicas'
+    first trials come from successive entries of one urand table shared by
+    every bounce of the path, and their mean is off by up to 1% on some
+    rays (measured against -u+ runs)."""
+    octp = oconv(w.glossy_room(), tmp, "glossy")
+    rays = w.random_rays(n, seed=5)
+    base = ["rtrace", "-h", "-u-", "-ab", "0", "-dj", "0", "-ds", "0", "-dr", "0", "-dt", "0", "-fdd", "-ov"]
+    det = np.frombuffer(run([*base, "-st", "1", octp], rays.astype("<f8").tobytes()), dtype="<f8").reshape(-1, 3)
+    rep = np.repeat(rays, K, axis=0).astype("<f8").tobytes()
+    stats = {}
+    for key, extra in (("st0", ["-st", "0"]), ("ss3", ["-ss", "3"])):
+        a = np.frombuffer(run([*base, "-u+", *extra, octp], rep), dtype="<f8").reshape(n, K, 3)
+        stats[f"{key}_mean"] = a.mean(1)
+        stats[f"{key}_se"] = a.std(1, ddof=1) / np.sqrt(K)
+    np.savez_compressed(OUT / "glossy.npz", rays=rays, K=K, radiance_st1=det, **stats,
+                        cmd=" ".join(base[1:]) + " with -st 1 | -u+ -st 0 | -u+ -ss 3 (K replicas)")
+    print("glossy: mean radiance st1 %.4g, st0 %.4g, ss3 %.4g" % (det.mean(), stats["st0_mean"].mean(),
+                                                                  stats["ss3_mean"].mean()))
+
+
 # bin groups of the 146 columns: ground, then the 8 Reinhart MF:1 altitude rows
 ROW_EDGES = [0, 1, 31, 61, 85, 109, 127, 139, 145, 146]
 
@@ -182,7 +208,7 @@ def ref_fixture_trace() -> None:
 def main() -> None:
     if not (BIN / "rtrace").exists():
         sys.exit("reference programs missing: make -f oracle/build_ref.mk REF=/root/reference -j8")
-    parts = {"octree": octree_digests, "c1": c1_direct, "c1p": c1_partitioned, "zoo": zoo,
+    parts = {"octree": octree_digests, "c1": c1_direct, "c1p": c1_partitioned, "zoo": zoo, "glossy": glossy,
              "dct": lambda tmp: dct_small(), "trace_oct": lambda tmp: ref_fixture_trace(),
              "c2ab1": lambda tmp: c2_stats(tmp, ab=1, K=256), "c2ab3": lambda tmp: c2_stats(tmp, ab=3, K=256)}
     only = sys.argv[1:] or list(parts)         # e.g. make_golden.py c1p

@@ -26,7 +26,7 @@ def gb():
 
 @pytest.fixture(scope="module")
 def scenes(gb, scene_dir):
-    return {k: gb.Scene(rad_files=[scene_dir / f"{k}.rad"]) for k in ("c1", "c2", "zoo", "c2e")}
+    return {k: gb.Scene(rad_files=[scene_dir / f"{k}.rad"]) for k in ("c1", "c2", "zoo", "c2e", "glossy")}
 
 
 def opts(prog, **kw):
@@ -108,6 +108,51 @@ def test_c1_partitioned_source(gb, scenes):
     rel = np.abs(rgb[lit] - ref[lit]).max(1) / ref[lit].max(1)
     print("partitioned source: max rel %.3g, share above 1e-5 %.4f" % (rel.max(), (rel > 1e-5).mean()))
     assert (rel <= 1e-5).mean() >= 0.995 and rel.max() < 1e-2
+
+
+def test_glossy_direct_lobe(gb, scenes):
+    """Rough plastic and metal below -st 1: diffuse plus the direct Gaussian
+    specular term, deterministic.  Paths through the pure-metal boxes are
+    mirror chains (1e-4, as for the shape zoo); a ray whose mirror chain
+    meets an edge within FP32 rounding may end on another surface."""
+    g = golden("glossy.npz")
+    rgb, _, _ = rtrace_c(gb, scenes["glossy"], opts("rtrace", ab=0, dj=0, ds=0, dr=0, dt=0, st=1, u=0), g["rays"])
+    ref = g["radiance_st1"]
+    rel = np.abs(rgb - ref).max(1) / np.maximum(np.abs(ref).max(1), 1e-9)
+    assert (rel <= 1e-4).mean() >= 0.99 and np.median(rel) < 1e-5, (np.median(rel), np.sort(rel)[-5:])
+
+
+@pytest.mark.parametrize("kw", [{"st": 0}, {"ss": 3}])
+def test_glossy_lobe_matches_oracle_sample_for_sample(gb, scenes, scene_dir, kw):
+    """The sampled specular lobe (rt/normal.c:364-440) with the same random
+    streams on the GPU (FP32) and in the oracle (FP64): the same trials are
+    taken and rejected, so values agree closely ray for ray; a sample that
+    grazes an edge can end on another surface."""
+    from oracle import pyoracle as po
+    g = golden("glossy.npz")
+    rays = np.repeat(g["rays"], 4, axis=0)
+    o = opts("rtrace", ab=0, dj=0, ds=0, dr=0, dt=0, u=0, seed=99, **kw)
+    rgb, _, _ = rtrace_c(gb, scenes["glossy"], o, rays)
+    oo = po.default_opts("rtrace", ab=0, dj=0, ds=0, dr=0, dt=0, u=0, seed=99, **kw)
+    ref, _, _, _ = po.rtrace(po.Scene(scene_dir / "glossy.rad"), oo, rays, hits=False, threads=8)
+    rel = np.abs(rgb - ref).max(1) / np.maximum(np.abs(ref).max(1), 1e-9)
+    assert np.median(rel) < 1e-5 and (rel <= 1e-3).mean() >= 0.98, (np.median(rel), (rel > 1e-3).mean())
+
+
+@pytest.mark.parametrize("key,kw", [("st0", {"st": 0}), ("ss3", {"ss": 3})])
+def test_glossy_lobe_statistics_vs_reference(gb, scenes, key, kw):
+    """Per-ray means of 1,024 replicas against the reference's 1,024 (-u+):
+    z-scores within 5, their mean within 4 standard errors of zero."""
+    g = golden("glossy.npz")
+    n, K = len(g["rays"]), 1024
+    rgb, _, _ = rtrace_c(gb, scenes["glossy"], opts("rtrace", ab=0, dj=0, ds=0, dr=0, dt=0, u=0, seed=5, **kw),
+                         np.repeat(g["rays"], K, axis=0))
+    a = rgb.reshape(n, K, 3)
+    m, se = a.mean(1), a.std(1, ddof=1) / np.sqrt(K)
+    rm = g[f"{key}_mean"]
+    z = (m - rm) / np.sqrt(se ** 2 + g[f"{key}_se"] ** 2 + (1e-5 * np.abs(rm) + 1e-9) ** 2)
+    print("glossy %s: max |z| %.2f, mean z %.3f" % (key, np.abs(z).max(), z.mean()))
+    assert np.abs(z).max() < 5 and abs(z.mean()) < 4 / np.sqrt(n)
 
 
 def test_zoo_all_primitives(gb, scenes):
