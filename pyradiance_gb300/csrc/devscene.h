@@ -3,8 +3,8 @@
  *
  * Layout (structure of arrays, all read-only during a run):
  *   kids      int32[8 * nnodes]   octree children codes (>= 0 node, -1 empty,
- *                                 <= -2 leaf set), 32 B per node
- *   set_off   int32[nsets]        start of each leaf set in set_data
+ *                                 <= -2 full leaf: gb_leaf_code of its set's
+ *                                 offset in set_data and size), 32 B per node
  *   set_data  int32[...]          [count, members in DESCENDING object order]
  *                                 (the order rt/raytrace.c:585 tests them)
  *   obj       int4[nobjs]         x: kind | flags << 8 | nv << 16,
@@ -36,6 +36,15 @@ enum { DK_NONE = 0, DK_FACE, DK_SPHERE, DK_BUBBLE, DK_CONE, DK_CUP, DK_CYL, DK_T
 #define DF_HASMAT  0x01   /* has a material (findmaterial != NULL) */
 #define DF_TRANSP  0x02   /* material is nominally transparent */
 #define DF_AXSHIFT 2      /* bits 2-3: dominant normal axis of a face */
+
+/* full-leaf code: -2 - (offset << 6 | min(size, 63)); a size field of 63
+ * means "63 or more: read the count word" */
+#define GB_LEAF_SIZEBITS 6
+#define GB_LEAF_MAXOFF (1 << (31 - GB_LEAF_SIZEBITS))
+static inline int gb_leaf_code(int off, int size)
+{
+    return -2 - ((off << GB_LEAF_SIZEBITS) | (size < 63 ? size : 63));
+}
 
 /* material kinds on the device */
 enum { DM_NONE = 0, DM_PLASTIC, DM_METAL, DM_GLASS, DM_LIGHT, DM_GLOW, DM_TRANS };
@@ -69,7 +78,6 @@ typedef struct {
     int   root;
     int   nnodes;
     const int   *kids;
-    const int   *set_off;
     const int   *set_data;
     /* objects */
     int   nobjs;

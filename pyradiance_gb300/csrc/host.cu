@@ -94,7 +94,7 @@ struct gb_scene {
     std::string src_error;             /* non-empty if a source is unsupported */
     std::vector<std::string> modname, matname;
     /* host arrays of the device scene */
-    std::vector<int> hkids, hsetoff, hsetdata;
+    std::vector<int> hkids, hsetdata;
     std::vector<int4> hobj;
     std::vector<float4> hgeo;
     std::vector<float2> hfvert;
@@ -102,7 +102,7 @@ struct gb_scene {
     std::vector<float> hcone;
     std::vector<gb_dsrc> hsrc;
     /* device scene */
-    DevBuf kids, setoff, setdata, obj, geo, fvert, fv4, cone, matd, srcd, trk;
+    DevBuf kids, setdata, obj, geo, fvert, fv4, cone, matd, srcd, trk;
     gb_dscene ds;
     /* work buffers */
     DevBuf sensors, value, bins, stats, roots, rootspt, qa, qb, qcount, binprog, modinfo, hits, hitt, trkrun,
@@ -349,14 +349,13 @@ static int prepare_device(gb_scene *G)
     cudaDeviceGetLimit(&stack, cudaLimitStackSize);
     if (stack < 16384)
         CK(cudaDeviceSetLimit(cudaLimitStackSize, 16384));
-    if (upload(G->kids, G->hkids) < 0 || upload(G->setoff, G->hsetoff) < 0 || upload(G->setdata, G->hsetdata) < 0 ||
+    if (upload(G->kids, G->hkids) < 0 || upload(G->setdata, G->hsetdata) < 0 ||
         upload(G->obj, G->hobj) < 0 || upload(G->geo, G->hgeo) < 0 || upload(G->fvert, G->hfvert) < 0 ||
         upload(G->fv4, G->hfv4) < 0 || upload(G->cone, G->hcone) < 0 || upload(G->matd, G->mat) < 0 ||
         upload(G->srcd, G->hsrc) < 0)
         return set_err(GB_ENOMEM, "device upload of the scene failed");
     gb_dscene &d = G->ds;
     d.kids = (const int *)G->kids.p;
-    d.set_off = (const int *)G->setoff.p;
     d.set_data = (const int *)G->setdata.p;
     d.obj = (const int4 *)G->obj.p;
     d.geo = (const float4 *)G->geo.p;
@@ -494,23 +493,33 @@ static int build_arrays(gb_scene *G)
     int rc = mark_sources(G);
     if (rc < 0)
         return rc;
-    /* octree: sets in descending member order (rt/raytrace.c:585) */
+    /* octree: sets in descending member order (rt/raytrace.c:585); a full
+     * leaf's code carries its set's place in set_data and its size (sizes
+     * from 63 up read the count word), so that entering a leaf needs no
+     * load before its members' */
     std::vector<int> kids(H.kids, H.kids + 8 * (size_t)H.nnodes);
     if (kids.empty()) kids.assign(8, -1);
-    std::vector<int> setoff(H.nsets), setdata((size_t)H.set_len);
+    std::vector<int> setdata((size_t)H.set_len > 0 ? (size_t)H.set_len : 1, 0);
     for (int32_t s = 0; s < H.nsets; s++) {
         const int32_t *st = H.set_data + H.set_off[s];
-        setoff[s] = (int)H.set_off[s];
         setdata[H.set_off[s]] = st[0];
         for (int k = 1; k <= st[0]; k++)
             setdata[H.set_off[s] + k] = st[st[0] + 1 - k];
     }
-    if (setoff.empty()) setoff.push_back(0);
-    if (setdata.empty()) setdata.push_back(0);
+    if ((int64_t)H.set_len >= GB_LEAF_MAXOFF)
+        return set_err(GB_EUNSUPPORTED, "octree sets of %lld entries exceed the %d a leaf code addresses",
+                       (long long)H.set_len, GB_LEAF_MAXOFF);
+    auto leaf_code = [&](int k) {
+        if (k > -2)
+            return k;
+        int64_t off = H.set_off[-k - 2];
+        return gb_leaf_code((int)off, H.set_data[off]);
+    };
+    for (int &k : kids)
+        k = leaf_code(k);
     std::vector<gb_dsrc> src = G->src;
     if (src.empty()) src.resize(1);
     G->hkids.swap(kids);
-    G->hsetoff.swap(setoff);
     G->hsetdata.swap(setdata);
     G->hobj.swap(obj);
     G->hgeo.swap(geo);
@@ -524,10 +533,9 @@ static int build_arrays(gb_scene *G)
     d.cusize = (float)H.cusize;
     d.grid_scale = (float)((double)(1 << GRID_BITS_HOST) / H.cusize);
     d.cell = (float)(H.cusize / (double)(1 << GRID_BITS_HOST));
-    d.root = H.root;
+    d.root = leaf_code(H.root);
     d.nnodes = H.nnodes;
     d.kids = G->hkids.data();
-    d.set_off = G->hsetoff.data();
     d.set_data = G->hsetdata.data();
     d.nobjs = H.nobjs;
     d.obj = G->hobj.data();
@@ -599,7 +607,7 @@ extern "C" void gb_scene_free(gb_scene *G)
 {
     if (!G)
         return;
-    DevBuf *bufs[] = {&G->kids, &G->setoff, &G->setdata, &G->obj, &G->geo, &G->fvert, &G->fv4, &G->cone, &G->matd,
+    DevBuf *bufs[] = {&G->kids, &G->setdata, &G->obj, &G->geo, &G->fvert, &G->fv4, &G->cone, &G->matd,
                       &G->srcd, &G->trk, &G->sensors, &G->value, &G->bins, &G->stats, &G->roots, &G->rootspt, &G->qa,
                       &G->qb, &G->qcount, &G->binprog, &G->modinfo, &G->hits, &G->hitt, &G->trkrun, &G->hitrec,
                       &G->adja, &G->adjb, &G->dlde, &G->gradd, &G->rootdraw, &G->rootlot};

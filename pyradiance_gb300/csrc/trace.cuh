@@ -533,7 +533,7 @@ GB_DFN bool walk_iter(const gb_dscene &S, Walk &W, Stack &stk)
     for (int u = 0; u < WALK_TESTS; u++) {
         if (W.k > W.cnt)
             break;
-        int o = GB_LDG(S.set_data + W.set + W.k);
+        const int o = GB_LDG(S.set_data + W.set + W.k);
         W.k++;
         if (o != W.skip)
             hit_object(S, o, W.org, W.dir, W.best, D_FTINY);
@@ -598,8 +598,11 @@ GB_DFN bool walk_iter(const gb_dscene &S, Walk &W, Stack &stk)
     W.k = 1;
     W.cnt = 0;
     if (node <= -2) {                            /* full leaf: its set to test */
-        W.set = GB_LDG(S.set_off + (-node - 2));
-        W.cnt = GB_LDG(S.set_data + W.set);
+        const int code = -node - 2;
+        W.set = code >> GB_LEAF_SIZEBITS;
+        W.cnt = code & ((1 << GB_LEAF_SIZEBITS) - 1);
+        if (W.cnt == (1 << GB_LEAF_SIZEBITS) - 1)
+            W.cnt = GB_LDG(S.set_data + W.set);
         W.tests += W.cnt;
     }
     return false;
