@@ -259,7 +259,7 @@ def dct_measure(dev, steps: int):
     return res
 
 
-GRAD_ARGS = ["-I+", "-ab", "2", "-ad", "1024", "-aa", "0", "-lw", "1e-4", "-u-"]
+GRAD_ARGS = ["-I+", "-ab", "2", "-ad", "1024", "-aa", "0", "-as", "0", "-lw", "1e-4", "-u-"]
 
 
 def grad_measure(steps: int):

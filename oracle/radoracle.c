@@ -31,7 +31,8 @@
  *   m_glass            rt/glass.c:45-165
  *   multambient        rt/ambient.c:229-300 (-aa 0 branch)
  *   samp_hemi/ambsample rt/ambcomp.c:177-250, 351-421
- *   rtcompute/rayirrad rt/rtrace.c:416-468
+ *   getambdiffs/ambsupersamp rt/ambcomp.c:256-346 (-I first hemispheres)
+ *   rtcompute/rayirrad rt/rtrace.c:416-468, raytirrad rt/raytrace.c:211-236
  *   eval_irrad/eval_rad/trace_contrib rt/rcontrib.c:272-353
  *   cm_multiply        util/cmatrix.c:421-474
  * Deviations shared with the GPU path: uniform jitter inside each
@@ -274,6 +275,7 @@ typedef struct {
     const int *trk;          /* per object */
     double *bins;            /* nbins_total x 3 for the current record */
     int64_t rays;
+    int ssamp_root;          /* the next hemisphere is an rtrace -I sensor's first */
 } ctx;
 
 static double maxc(const double c[3]) { return c[0] > c[1] ? (c[0] > c[2] ? c[0] : c[2]) : (c[1] > c[2] ? c[1] : c[2]); }
@@ -1119,10 +1121,107 @@ static void square2disk(double ds[2], double seedx, double seedy)
 }
 
 /* rt/ambient.c:229-300 (-aa 0) with rt/ambcomp.c:351-421 and :177-250 */
+/* rt/ambcomp.c:256-346 getambdiffs + ambsupersamp on the first hemisphere
+ * of an rtrace -I sensor (the only hemispheres the GPU path super-samples),
+ * in the arithmetic of the GPU's k_ssamp_plan: v holds each stratum's
+ * first value (coefficient applied); each stratum's extra samples are
+ * traced as children GB_C_SSAMP(k, m) and averaged with it. */
+#define PB(c) (0.265074126f * (float)(c)[0] + 0.670114631f * (float)(c)[1] + 0.064811243f * (float)(c)[2])
+static void supersample_root(ctx *X, RAY *r, int n, const double acoef[3], const double ux[3], const double uy[3],
+                             const double onrm[3], double (*v)[3], double acol[3])
+{
+    float *earr = (float *)calloc(2 * (size_t)n * n, sizeof(float)), *ep2 = earr + n * n, e2rem = 0.f;
+    int *m = (int *)calloc((size_t)n * n, sizeof(int));
+    float wt = 1.f, dd = 3.14159265358979323846f * 0.8f / ((float)X->o->ad * (float)X->o->lw + 1e-20f);
+    const float normf = 1.f / (PB(acoef) + 1e-6f);
+    int cnt, i, j, k, c;
+    if (wt > dd) wt = dd;
+    cnt = (int)((float)X->o->as * wt + .5f);
+    for (i = 0; i < n; i++)
+        for (j = 0; j < n; j++) {
+            const float b = PB(v[i * n + j]);
+            float b1, d2;
+            k = i * n + j;
+            if (i) {
+                b1 = PB(v[k - n]);
+                d2 = b - b1;
+                d2 *= d2 * normf / (b + b1 + 1e-6f);
+                ep2[k] += d2;
+                ep2[k - n] += d2;
+            }
+            if (!j) continue;
+            b1 = PB(v[k - 1]);
+            d2 = b - b1;
+            d2 *= d2 * normf / (b + b1 + 1e-6f);
+            ep2[k] += d2;
+            ep2[k - 1] += d2;
+            if (!i) continue;
+            b1 = PB(v[k - n - 1]);
+            d2 = b - b1;
+            d2 *= d2 * normf / (b + b1 + 1e-6f);
+            ep2[k] += d2;
+            ep2[k - n - 1] += d2;
+        }
+    ep2[0] *= 6.f / 3.f;
+    ep2[n - 1] *= 6.f / 3.f;
+    ep2[(n - 1) * n] *= 6.f / 3.f;
+    ep2[(n - 1) * n + n - 1] *= 6.f / 3.f;
+    for (i = 1; i < n - 1; i++) {
+        ep2[i * n] *= 6.f / 5.f;
+        ep2[i * n + n - 1] *= 6.f / 5.f;
+    }
+    for (j = 1; j < n - 1; j++) {
+        ep2[j] *= 6.f / 5.f;
+        ep2[(n - 1) * n + j] *= 6.f / 5.f;
+    }
+    for (i = 0; i < n - 1; i++)
+        for (j = 0; j < n - 1; j++) {
+            k = i * n + j;
+            earr[k] += .5f * ep2[k] + .125f * (ep2[k + 1] + ep2[k + n]);
+            earr[k + 1] += .125f * ep2[k];
+            earr[k + n] += .125f * ep2[k];
+        }
+    for (k = n * n; k--;) e2rem += earr[k];
+    for (k = 0; k < n * n && cnt > 0; k++) {
+        double q[4];
+        int nss, mm;
+        if (e2rem <= 1e-6f) break;
+        draw(X, r->path, r->sensor, GB_G_SSAMP + (uint32_t)(k >> 2), q, NULL);
+        nss = (int)(earr[k] / e2rem * (float)cnt + (float)q[k & 3]);
+        for (mm = 1; mm <= nss; mm++) {
+            RAY ar;
+            double u[4], zd;
+            float fs[2];
+            memset(&ar, 0, sizeof ar);
+            if (rayorigin(X, &ar, GB_RAMBIENT, r, acoef, GB_C_SSAMP(k, mm)) < 0) break;
+            ar.adepth = r->adepth + 1;
+            draw(X, ar.path, ar.sensor, GB_G_CREATE, u, NULL);
+            gb_square2disk(fs, ((float)(k % n) + (float)u[2]) / (float)n, ((float)(k / n) + (float)u[1]) / (float)n);
+            zd = sqrt(fmax(0., 1. - (double)fs[0] * fs[0] - (double)fs[1] * fs[1]));
+            for (c = 0; c < 3; c++) ar.rdir[c] = fs[0] * ux[c] + fs[1] * uy[c] + zd * onrm[c];
+            vnormalize(ar.rdir);
+            rayclear(&ar);
+            raytrace(X, &ar);
+            for (c = 0; c < 3; c++) v[k][c] += ar.rcol[c] * ar.rcoef[c];
+            m[k]++;
+            if (!--cnt) break;
+        }
+        e2rem -= earr[k];
+    }
+    acol[0] = acol[1] = acol[2] = 0;
+    for (k = 0; k < n * n; k++)
+        for (c = 0; c < 3; c++) acol[c] += v[k][c] / (1 + m[k]);
+    free(earr);
+    free(m);
+}
+#undef PB
+
 static void multambient(ctx *X, double aval[3], RAY *r, const double nrm[3])
 {
     double d, wt, acoef[3], onrm[3], ux[3], uy[3], acol[3] = {0, 0, 0};
-    int n, i, j, k, ok = 0;
+    double (*sv)[3] = NULL;
+    int n, i, j, k, ok = 0, ssroot = X->ssamp_root;
+    X->ssamp_root = 0;
     if (X->o->ad <= 0 || r->adepth >= X->o->ab) goto dumbamb;
     d = maxc(aval);
     if (d <= FTINY) goto dumbamb;
@@ -1135,6 +1234,8 @@ static void multambient(ctx *X, double aval[3], RAY *r, const double nrm[3])
     for (k = 0; k < 3; k++) acoef[k] = aval[k] / (n * n);
     rand_perp(X, r, GB_G_FRAME, onrm, ux);
     vcross(uy, onrm, ux);
+    if (ssroot && X->o->as > 0 && X->o->aa <= FTINY && n * n > 49)
+        sv = (double (*)[3])calloc((size_t)n * n, sizeof *sv);
     {
         gb_lot *L = (gb_lot *)malloc(sizeof(gb_lot));
         float (*rows)[2] = (float (*)[2])malloc(sizeof(float) * 4 * n);
@@ -1163,6 +1264,8 @@ static void multambient(ctx *X, double aval[3], RAY *r, const double nrm[3])
             rayclear(&ar);
             raytrace(X, &ar);
             for (k = 0; k < 3; k++) acol[k] += ar.rcol[k] * ar.rcoef[k];
+            if (sv)
+                for (k = 0; k < 3; k++) sv[kk][k] = ar.rcol[k] * ar.rcoef[k];
             ok++;
         }
         tmp = prev; prev = cur; cur = tmp;
@@ -1170,6 +1273,15 @@ static void multambient(ctx *X, double aval[3], RAY *r, const double nrm[3])
     }
         free(rows);
         free(L);
+    }
+    if (sv) {
+        if (ok == n * n) {                       /* samp_hemi's super-sampling test (rt/ambcomp.c:403-409) */
+            float wf = 1.f, df = 3.14159265358979323846f * 0.8f / ((float)X->o->ad * (float)X->o->lw + 1e-20f);
+            if (wf > df) wf = df;
+            if ((int)((float)X->o->as * wf + .5f) >= 4 * n)
+                supersample_root(X, r, n, acoef, ux, uy, onrm, sv, acol);
+        }
+        free(sv);
     }
     if (ok) {
         memcpy(aval, acol, sizeof acol);
@@ -1251,9 +1363,20 @@ static void gaussamp(ctx *X, NORMDAT *np, RAY *r)
     }
 }
 
+static int m_normal_obj(ctx *X, const gb_object *mo, RAY *r);
+
 static int m_normal(ctx *X, int m, RAY *r)
 {
-    const gb_object *mo = &X->O->H.objs[m];
+    return m_normal_obj(X, &X->O->H.objs[m], r);
+}
+
+/* the Lambertian of reflectance pi that -i substitutes (rt/raytrace.c:24-28
+ * Lamb) */
+static double lamb_farg[5] = {PI, PI, PI, 0., 0.};
+static const gb_object lamb_obj = {GT_PLASTIC, -1, (char *)"Lambertian", 0, NULL, 5, lamb_farg};
+
+static int m_normal_obj(ctx *X, const gb_object *mo, RAY *r)
+{
     NORMDAT nd;
     double fest = 0, sct[3];
     int i;
@@ -1358,6 +1481,12 @@ static void rayshade(ctx *X, RAY *r)
     int t;
     if (m < 0) { raytrans(X, r); return; }
     t = X->O->H.objs[m].otype;
+    /* -i: rt/raytrace.c:211-236 raytirrad for primary rays and those
+     * passed on through transparent surfaces */
+    if (X->o->i && !(r->crtype & ~(GB_PRIMARY | GB_TRANS))) {
+        if (gb_is_transp(t)) { raytrans(X, r); return; }
+        if (!gb_is_light(t)) { m_normal_obj(X, &lamb_obj, r); return; }
+    }
     if (gb_is_light(t)) m_light(X, m, r);
     else if (t == GT_GLASS) m_glass(X, m, r);
     else if (t == GT_PLASTIC || t == GT_METAL) m_normal(X, m, r);
@@ -1422,7 +1551,9 @@ static void eval_irrad(ctx *X, const double *rv, uint32_t sensor, double rgb[3])
     nd.rblt = 0;
     nd.flat = 0;
     sct[0] = sct[1] = sct[2] = PI;
+    X->ssamp_root = X->o->prog == GB_PROG_RTRACE;
     multambient(X, sct, &r, nd.pnorm);
+    X->ssamp_root = 0;
     for (i = 0; i < 3; i++) r.rcol[i] += sct[i];
     direct(X, &r, &nd);
     memcpy(rgb, r.rcol, 3 * sizeof(double));

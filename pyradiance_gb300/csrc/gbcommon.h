@@ -85,12 +85,15 @@ GB_HD uint32_t gb_irand(uint32_t x, uint32_t m) { return (uint32_t)(((uint64_t)x
  *   GB_G_SPECF  drawn at the hit for the frame of the specular lobe
  *   GB_G_SPEC+j two trials of specular lobe sampling per group: trial t
  *      uses words 2(t&1) and 2(t&1)+1 of group GB_G_SPEC + (t >> 1)
+ *   GB_G_SSAMP+j drawn at a super-sampled hemisphere's parent: the random
+ *      rounding of each stratum's share of the extra samples
  */
 #define GB_G_CREATE 0u
 #define GB_G_FRAME  1u
 #define GB_G_SRC    2u
 #define GB_G_SPECF  0x7F000000u
 #define GB_G_SPEC   0x7F000001u
+#define GB_G_SSAMP  0x7E000000u   /* super-sampling allocation: stratum k uses word k&3 of group + (k >> 2) */
 
 GB_HD gb_u4 gb_draw(uint64_t path, uint32_t sensor, uint32_t group, uint32_t k0, uint32_t k1)
 {
@@ -112,6 +115,8 @@ GB_HD uint64_t gb_child(uint64_t parent, uint32_t code)
 #define GB_C_TRANS      0x100002u
 #define GB_C_PASS       0x100003u                   /* continue through (raytrans) */
 #define GB_SPEC_MAXITER 10                            /* rt/normal.c:25 MAXITER */
+#define GB_C_SSAMP(k, m) (0x400000u + (uint32_t)(k) + ((uint32_t)(m) << 12))  /* extra sample m >= 1 of stratum k < 4096 */
+#define GB_NOTAG 0xffffffffu
 #define GB_C_SPEC(k)    (0x110000u + (uint32_t)(k))   /* specular lobe sample k < 2^16 */
 #define GB_C_SHADOWP(s, p) (0x200000u + (uint32_t)(s) + ((uint32_t)(p) << 12))   /* partition p < 64 */
 #define GB_C_SHADOW(s)  GB_C_SHADOWP(s, 0)

@@ -106,7 +106,7 @@ struct gb_scene {
     gb_dscene ds;
     /* work buffers */
     DevBuf sensors, value, bins, stats, roots, rootspt, qa, qb, qcount, binprog, modinfo, hits, hitt, trkrun,
-        hitrec, adja, adjb, dlde, gradd, rootdraw, rootlot;
+        hitrec, adja, adjb, dlde, gradd, rootdraw, rootlot, tga, tgb, ssval, sscnt, sserr;
     cudaStream_t stream = nullptr;
     int sms = 0;
     cudaEvent_t ev[2 * GB_TIMED_LAUNCHES + 2];
@@ -610,7 +610,8 @@ extern "C" void gb_scene_free(gb_scene *G)
     DevBuf *bufs[] = {&G->kids, &G->setdata, &G->obj, &G->geo, &G->fvert, &G->fv4, &G->cone, &G->matd,
                       &G->srcd, &G->trk, &G->sensors, &G->value, &G->bins, &G->stats, &G->roots, &G->rootspt, &G->qa,
                       &G->qb, &G->qcount, &G->binprog, &G->modinfo, &G->hits, &G->hitt, &G->trkrun, &G->hitrec,
-                      &G->adja, &G->adjb, &G->dlde, &G->gradd, &G->rootdraw, &G->rootlot};
+                      &G->adja, &G->adjb, &G->dlde, &G->gradd, &G->rootdraw, &G->rootlot, &G->tga, &G->tgb,
+                      &G->ssval, &G->sscnt, &G->sserr};
     for (DevBuf *b : bufs)
         b->release();
     if (G->stream)
@@ -811,8 +812,6 @@ static int check_shading(gb_scene *G, const gb_opts *o)
         return set_err(GB_EUNSUPPORTED, "the ambient cache (-aa %g) is not implemented; use -aa 0", o->aa);
     if (o->as > 0 && o->ab > 0 && o->aa > GB_FTINY)
         return set_err(GB_EUNSUPPORTED, "ambient super-sampling (-as) is not implemented");
-    if (o->i)
-        return set_err(GB_EUNSUPPORTED, "-i (irradiance at the hit surface) is not implemented");
     if (!o->bv)
         return set_err(GB_EUNSUPPORTED, "-bv- is not implemented");
     if (!o->dv)
@@ -854,6 +853,48 @@ static uint64_t seed_of(const gb_opts *o)
     if (!o->u)
         return 0;
     return (uint64_t)time(nullptr) * 0x9E3779B97F4A7C15ull;
+}
+
+/* Extra samples per -I first hemisphere of n0 x n0 strata under -as
+ * (rt/ambcomp.c:403-409): rtrace only (rcontrib forces -as 0,
+ * rt/rcmain.c:167), with -aa 0 (the cache is not implemented), hemispheres
+ * of more than 7 x 7 strata, and at least four times n0 samples; 0 when
+ * there is no super-sampling. */
+static int supersamples(const gb_opts *o, int n0)
+{
+    if (o->prog != GB_PROG_RTRACE || !o->I || o->ab <= 0 || o->aa > GB_FTINY || o->as <= 0 || n0 * n0 <= 49)
+        return 0;
+    double d = M_PI * 0.8 / (o->ad * o->lw + 1e-20), wt = 1.0;
+    if (wt > d) wt = d;
+    int cnt = (int)((float)o->as * (float)wt + .5f);
+    return cnt >= 4 * n0 ? cnt : 0;
+}
+
+/* Whether a hemisphere sampled at ray weight w (with a reflectance of at
+ * most 1, or pi for the -I/-i Lambertian) would be super-sampled. */
+static bool hemi_supersampled(const gb_opts *o, double w, double rho)
+{
+    double d = rho * 0.8 * w / (o->ad * o->lw + 1e-20), wt = w;
+    if (wt > d) wt = d;
+    int n = (int)(sqrt(o->ad * wt) + 0.5);
+    return n * n > 49 && (int)(o->as * wt + .5) >= 4 * n;
+}
+
+/* -as super-sampling that is not implemented: of any hemisphere but the
+ * -I first ones (rtrace with -aa 0 only; rcontrib forces -as 0) */
+static int check_supersampling(const gb_opts *o, int n0)
+{
+    if (o->prog != GB_PROG_RTRACE || o->ab <= 0 || o->aa > GB_FTINY || o->as <= 0)
+        return GB_OK;
+    bool other;
+    if (o->I)                                    /* below the first hemisphere: weight <= pi / n0^2 */
+        other = o->ab > 1 && hemi_supersampled(o, fmin(1.0, M_PI / ((double)n0 * n0)), M_PI);
+    else                                         /* primary hits at weight 1 */
+        other = hemi_supersampled(o, 1.0, o->i ? M_PI : 1.0);
+    if (other)
+        return set_err(GB_EUNSUPPORTED, "ambient super-sampling (-as %d) is implemented for the first hemisphere "
+                       "of -I sensors only; this run would super-sample others: use -as 0", o->as);
+    return GB_OK;
 }
 
 static int root_divisions(const gb_opts *o)
@@ -936,6 +977,7 @@ static int run(gb_scene *G, const gb_opts *o, int follow, const double *org_dir,
     P.srcsizerat = (float)o->ds;
     P.specthresh = (float)o->st;
     P.specjitter = (float)o->ss;
+    P.do_irrad = o->i;
     P.follow = follow;
     P.contrib_mode = o->V;
     uint64_t seed = seed_of(o);
@@ -1011,8 +1053,19 @@ static int run(gb_scene *G, const gb_opts *o, int follow, const double *org_dir,
     size_t freeb = 0, totalb = 0;
     cudaMemGetInfo(&freeb, &totalb);
     const bool grad = out.grad != nullptr;
-    /* two queues, the walk results, and in gradient runs the factor lists */
-    const size_t slot = 2 * sizeof(gb_qray) + sizeof(gb_qhit) + (grad ? 2 * sizeof(gb_qadj) : 0);
+    {
+        int rc = check_supersampling(o, n0);
+        if (rc < 0)
+            return rc;
+    }
+    const int ss = supersamples(o, n0);
+    if (ss > 0 && (grad || !out.value))
+        return set_err(GB_EUNSUPPORTED, "ambient super-sampling (-as %d) in a gradient run is not implemented; "
+                       "use -as 0", o->as);
+    /* two queues, the walk results, in gradient runs the factor lists, in
+     * super-sampled runs the strata tags */
+    const size_t slot = 2 * sizeof(gb_qray) + sizeof(gb_qhit) + (grad ? 2 * sizeof(gb_qadj) : 0) +
+                        (ss > 0 ? 2 * sizeof(uint32_t) : 0);
     long long qmax = (long long)(freeb / 3 / slot);
     if (qmax > (1ll << 28)) qmax = 1ll << 28;
     if (qcap > qmax) qcap = qmax;
@@ -1033,6 +1086,22 @@ static int run(gb_scene *G, const gb_opts *o, int follow, const double *org_dir,
         P.grad = (double *)G->gradd.p;
         P.nslots = nslots;
     }
+    uint32_t *tags[2] = {nullptr, nullptr};
+    if (ss > 0) {
+        const size_t nn = (size_t)n0 * n0;
+        if (G->tga.ensure((size_t)qcap * sizeof(uint32_t)) < 0 || G->tgb.ensure((size_t)qcap * sizeof(uint32_t)) < 0 ||
+            G->ssval.ensure((size_t)n * nn * 3 * sizeof(double)) < 0 ||
+            G->sscnt.ensure((size_t)n * nn * sizeof(int)) < 0 || G->sserr.ensure((size_t)n * nn * 2 * sizeof(float)) < 0)
+            return set_err(GB_ENOMEM, "cannot allocate the super-sampling buffers");
+        CK(cudaMemsetAsync(G->ssval.p, 0, (size_t)n * nn * 3 * sizeof(double), st));
+        CK(cudaMemsetAsync(G->sscnt.p, 0, (size_t)n * nn * sizeof(int), st));
+        tags[0] = (uint32_t *)G->tga.p;
+        tags[1] = (uint32_t *)G->tgb.p;
+        P.ss_samples = o->as;
+        P.ss_val = (double *)G->ssval.p;
+        P.ss_cnt = (int *)G->sscnt.p;
+        P.ss_err = (float *)G->sserr.p;
+    }
     gb_qadj *adja = (gb_qadj *)G->adja.p, *adjb = (gb_qadj *)G->adjb.p;
     unsigned long long *cnt = (unsigned long long *)G->qcount.p;   /* [0] A, [1] B, [2] work items */
     CK(cudaMemsetAsync(cnt, 0, 3 * sizeof(unsigned long long), st));
@@ -1043,6 +1112,7 @@ static int run(gb_scene *G, const gb_opts *o, int follow, const double *org_dir,
     P.qout = qa;
     P.qout_count = cnt;
     P.adj_out = adja;
+    P.tag_out = tags[0];
     CK(cudaEventRecord(G->ev[0], st));
     if (o->I) {
         if (n0 > 0) {
@@ -1083,34 +1153,59 @@ static int run(gb_scene *G, const gb_opts *o, int follow, const double *org_dir,
     }
     /* generations until the queue drains: walk, then shade into the other queue */
     int in = 0;
-    for (int gen = 0; gen < GB_MAX_GENERATIONS; gen++) {
-        unsigned long long c = 0;
-        CK(cudaMemcpyAsync(&c, cnt + in, sizeof c, cudaMemcpyDeviceToHost, st));
-        CK(cudaStreamSynchronize(st));
-        if (c == 0)
-            break;
-        if ((long long)c > g_maxgen)
-            g_maxgen = (long long)c;
-        if ((long long)c > qcap)
-            return set_err(GB_EOVERFLOW, "ray queue overflow (%llu rays for %lld slots)", c, qcap);
-        P.qin = in ? qb : qa;
-        P.qin_count = cnt + in;
-        P.qout = in ? qa : qb;
-        P.qout_count = cnt + (1 - in);
-        P.adj_in = in ? adjb : adja;
-        P.adj_out = in ? adja : adjb;
-        CK(cudaMemsetAsync(cnt + (1 - in), 0, sizeof(unsigned long long), st));
-        CK(cudaMemsetAsync(P.work, 0, sizeof(unsigned long long), st));
-        int rc = launch(GB_K_TRACE, P, [&](gb_run &R) { return gb_launch_trace(&R, st, G->sms); });
+    auto drain = [&]() -> int {
+        for (int gen = 0; gen < GB_MAX_GENERATIONS; gen++) {
+            unsigned long long c = 0;
+            CK(cudaMemcpyAsync(&c, cnt + in, sizeof c, cudaMemcpyDeviceToHost, st));
+            CK(cudaStreamSynchronize(st));
+            if (c == 0)
+                break;
+            if ((long long)c > g_maxgen)
+                g_maxgen = (long long)c;
+            if ((long long)c > qcap)
+                return set_err(GB_EOVERFLOW, "ray queue overflow (%llu rays for %lld slots)", c, qcap);
+            P.qin = in ? qb : qa;
+            P.qin_count = cnt + in;
+            P.qout = in ? qa : qb;
+            P.qout_count = cnt + (1 - in);
+            P.adj_in = in ? adjb : adja;
+            P.adj_out = in ? adja : adjb;
+            P.tag_in = tags[in];
+            P.tag_out = tags[1 - in];
+            CK(cudaMemsetAsync(cnt + (1 - in), 0, sizeof(unsigned long long), st));
+            CK(cudaMemsetAsync(P.work, 0, sizeof(unsigned long long), st));
+            int rc = launch(GB_K_TRACE, P, [&](gb_run &R) { return gb_launch_trace(&R, st, G->sms); });
+            if (rc < 0)
+                return rc;
+            CK(cudaMemsetAsync(P.work, 0, sizeof(unsigned long long), st));
+            rc = launch(GB_K_SHADE, P, [&](gb_run &R) {
+                return grad ? gb_launch_shade_grad(&R, st, G->sms) : gb_launch_shade(&R, st, G->sms); });
+            if (rc < 0)
+                return rc;
+            CK(cudaMemsetAsync(cnt + in, 0, sizeof(unsigned long long), st));
+            in = 1 - in;
+        }
+        return GB_OK;
+    };
+    int drc = drain();
+    if (drc < 0)
+        return drc;
+    if (ss > 0) {
+        /* the extra samples of the first hemispheres, queued into the
+         * drained queue and traced as a second pass, then every stratum's
+         * mean into its sensor */
+        P.qout = in ? qb : qa;
+        P.qout_count = cnt + in;
+        P.tag_out = tags[in];
+        int rc = launch(GB_K_ROOT, P, [&](gb_run &R) { return gb_launch_ssamp_plan(&R, st, G->sms); });
         if (rc < 0)
             return rc;
-        CK(cudaMemsetAsync(P.work, 0, sizeof(unsigned long long), st));
-        rc = launch(GB_K_SHADE, P, [&](gb_run &R) {
-            return grad ? gb_launch_shade_grad(&R, st, G->sms) : gb_launch_shade(&R, st, G->sms); });
+        drc = drain();
+        if (drc < 0)
+            return drc;
+        rc = launch(GB_K_ROOT, P, [&](gb_run &R) { return gb_launch_ssamp_final(&R, st, G->sms); });
         if (rc < 0)
             return rc;
-        CK(cudaMemsetAsync(cnt + in, 0, sizeof(unsigned long long), st));
-        in = 1 - in;
     }
     CK(cudaEventRecord(G->ev[1], st));
     unsigned long long stats[GB_K_N][GB_ST_N];
@@ -1152,7 +1247,8 @@ static int run(gb_scene *G, const gb_opts *o, int follow, const double *org_dir,
 static double slots_per_sensor(const gb_scene *G, const gb_opts *o)
 {
     int n0 = (o->I && o->ab > 0 && o->ad > 0) ? root_divisions(o) : 0;
-    return n0 > 0 ? (double)n0 * n0 * 4 : (o->ab > 0 ? (double)o->ad * 2 : 8.0);
+    double per = n0 > 0 ? (double)n0 * n0 * 4 : (o->ab > 0 ? (double)o->ad * 2 : 8.0);
+    return fmax(per, 4.0 * supersamples(o, n0));    /* the second pass of super-sampled runs */
 }
 
 /* run() over slices of at most as many sensors as keep the work buffers
@@ -1217,7 +1313,15 @@ extern "C" int gb_rtrace(gb_scene *G, const gb_opts *o, const double *org_dir, i
             return rc;
     }
     RunOut out = {out_rgb, nullptr, hit_id, hit_t, nullptr, nullptr};
-    return run_sliced(G, o, 0, org_dir, n, nullptr, nullptr, 0, nullptr, out, 0.0);
+    double per = 0.0;
+    int rc = GB_OK;
+    for (int attempt = 0; attempt < 4; attempt++) {
+        rc = run_sliced(G, o, 0, org_dir, n, nullptr, nullptr, 0, nullptr, out, per);
+        if (rc != GB_EOVERFLOW)
+            break;
+        per = 2 * (per > 0 ? per : slots_per_sensor(G, o));   /* a larger queue, fewer sensors per slice */
+    }
+    return rc;
 }
 
 extern "C" int gb_rtrace_grad(gb_scene *G, const gb_opts *o, const double *org_dir, int64_t n,
@@ -1612,6 +1716,9 @@ extern "C" int gb_rtrace_device_noalloc(gb_scene *G, const gb_opts *o, const dou
     if (n0 > 128)
         return set_err(GB_EUNSUPPORTED, "-ad %d gives %d x %d hemisphere divisions; at most 128 x 128 are "
                        "supported", o->ad, n0, n0);
+    if (check_supersampling(o, n0) < 0 || supersamples(o, n0) > 0)
+        return set_err(GB_EUNSUPPORTED, "ambient super-sampling (-as %d) is not implemented without allocation; "
+                       "use -as 0", o->as);
     const size_t nobj = G->H.nobjs > 0 ? (size_t)G->H.nobjs : 1;
     size_t off_stats = 0, off_cnt = up(stat_bytes), off_trk = off_cnt + up(4 * sizeof(unsigned long long));
     size_t off_roots = off_trk + up(nobj * sizeof(int));
@@ -1658,6 +1765,7 @@ extern "C" int gb_rtrace_device_noalloc(gb_scene *G, const gb_opts *o, const dou
     P.srcsizerat = (float)o->ds;
     P.specthresh = (float)o->st;
     P.specjitter = (float)o->ss;
+    P.do_irrad = o->i;
     P.contrib_mode = o->V;
     uint64_t seed = seed_of(o);
     P.k0 = (uint32_t)seed;

@@ -53,6 +53,7 @@ struct Ray {
     int rlvl, adepth;
     uint64_t path;
     uint32_t sensor;
+    uint32_t tag;           /* super-sampled first-hemisphere stratum the path descends from, or GB_NOTAG */
     gb_qadj adj;            /* gradient runs only: parameter factors of the path */
 };
 
@@ -110,6 +111,7 @@ __device__ __forceinline__ Ray load_ray(const gb_qray *q)
     r.rlvl = (d.w >> 16) & 0xff;
     r.adepth = (d.w >> 24) & 0xff;
     r.rsrc = -1;
+    r.tag = GB_NOTAG;
     return r;
 }
 
@@ -125,6 +127,8 @@ __device__ __forceinline__ void push_ray(const gb_run &P, const Ray &r)
         store_ray(P.qout + base, r);
         if (G)
             P.adj_out[base] = r.adj;
+        if (P.tag_out)
+            P.tag_out[base] = r.tag;
     } else if (g.thread_rank() == 0)
         atomicAdd(P.stats + ST_OVERFLOW, 1ull);
 }
@@ -145,6 +149,8 @@ extern __shared__ double grad_smem[];
 
 __device__ __forceinline__ void adj_append(gb_qadj &a, int slot, uint32_t kind, float pd)
 {
+    if (slot < 0)                            /* a factor that is no parameter */
+        return;
     if (a.n < GB_ADJ_MAX) {
         a.e[a.n] = ((uint32_t)slot << 2) | kind;
         a.pd[a.n] = pd;
@@ -233,13 +239,14 @@ __device__ __forceinline__ void grad_end(const gb_run &P)
 
 /* ------------------------------------------------------- contributions */
 
-__device__ __forceinline__ void add_value(const gb_run &P, uint32_t sensor, float3 v)
+__device__ __forceinline__ void add_value(const gb_run &P, uint32_t sensor, uint32_t tag, float3 v)
 {
     if (!P.value)
         return;
     if (v.x == 0.f && v.y == 0.f && v.z == 0.f)
         return;
-    double *d = P.value + 3ull * (sensor - P.sensor_base);
+    /* a path from a super-sampled first hemisphere adds to its stratum */
+    double *d = tag != GB_NOTAG ? P.ss_val + 3ull * tag : P.value + 3ull * (sensor - P.sensor_base);
     atomicAdd(d, (double)v.x);
     atomicAdd(d + 1, (double)v.y);
     atomicAdd(d + 2, (double)v.z);
@@ -309,7 +316,7 @@ __device__ __forceinline__ void light_hit(const gb_run &P, const Ray &r, int obj
             if (G)
                 grad_add(P, r.sensor, rc * rcol, r.adj);
             else
-                add_value(P, r.sensor, rc * rcol);
+                add_value(P, r.sensor, r.tag, rc * rcol);
         }
         if (P.binprog) {
             int slot = S.trk[obj];
@@ -351,6 +358,7 @@ __device__ __forceinline__ bool ray_origin(const gb_run &P, const Ray &parent, u
         rc = f3(1.f, 1.f, 1.f);
     c.path = gb_child(parent.path, code);
     c.sensor = parent.sensor;
+    c.tag = parent.tag;
     c.rsrc = parent.rsrc;
     c.rlvl = parent.rlvl + ((rt & GB_RAYREFL) ? 1 : 0);
     if ((rt & GB_RAYREFL) && c.rsrc >= 0)
@@ -443,10 +451,11 @@ __device__ __forceinline__ bool make_hemi(const gb_run &P, const Ray &r, float3 
  * collision test); otherwise spt is the position placed by
  * gb_place_sample. */
 __device__ __forceinline__ bool hemi_child(const gb_run &P, const Ray &parent, const Hemi &h, float3 hp,
-                                           int origin, int k, const float *spt, Ray &c)
+                                           int origin, int k, const float *spt, Ray &c,
+                                           uint32_t code = GB_NOTAG)
 {
     float4 u;
-    if (!ray_origin(P, parent, h.atyp, h.acoef, true, GB_C_STRATUM(k), c, &u))
+    if (!ray_origin(P, parent, h.atyp, h.acoef, true, code == GB_NOTAG ? GB_C_STRATUM(k) : code, c, &u))
         return false;
     float s[2];
     if (spt) {
@@ -745,7 +754,7 @@ __device__ __noinline__ void direct_sample(const gb_run &P, const Ray &r, float3
     sr.origin = origin;
     if (!G) {
         float3 v = shadow_chain(P, sr, sn, cnt, coef, pot, nullptr);
-        add_value(P, r.sensor, r.coef * v);
+        add_value(P, r.sensor, r.tag, r.coef * v);
         return;
     }
     gb_qadj fac = r.adj;                       /* the path's factors and the shadow's glass */
@@ -968,6 +977,17 @@ __device__ void shade_ray(const gb_run &P, const Ray &r, const Hit &h, Counters 
     int ms = S.obj[h.obj].y;
     int mk = ms >= 0 ? (int)S.mat[2 * ms].x : DM_NONE;
     float3 hp = r.org + r.dir * h.t;
+    /* -i (rt/raytrace.c:211-236 raytirrad): a primary ray, or one passed
+     * on through transparent surfaces, passes through glass and meets
+     * every other non-light material as a Lambertian of reflectance pi,
+     * whose radiance is the irradiance there */
+    bool lamb = false;
+    if (P.do_irrad && !(r.crtype & ~(GB_PRIMARY | GB_TRANS))) {
+        if (mk == DM_GLASS)
+            mk = DM_NONE;
+        else if (mk != DM_LIGHT && mk != DM_GLOW && mk != DM_NONE)
+            lamb = true;
+    }
     if (mk == DM_LIGHT || mk == DM_GLOW) {
         light_hit<G>(P, r, h.obj, ms, h.t, h.rod, cnt, nullptr);
         return;
@@ -984,7 +1004,16 @@ __device__ void shade_ray(const gb_run &P, const Ray &r, const Hit &h, Counters 
         push_ray<G>(P, c);
         return;
     }
-    float4 m0 = S.mat[2 * ms], m1 = S.mat[2 * ms + 1];
+    float4 m0, m1;
+    if (lamb) {
+        mk = DM_PLASTIC;
+        m0 = make_float4(DM_PLASTIC, (float)M_PI, (float)M_PI, (float)M_PI);
+        m1 = make_float4(0.f, 0.f, 0.f, 0.f);
+        ms = -1;                                 /* no material parameter on the path */
+    } else {
+        m0 = S.mat[2 * ms];
+        m1 = S.mat[2 * ms + 1];
+    }
     float3 n = h.n;
     float rod = h.rod;
     if (rod < 0.f) {                            /* flipsurface (backvis on) */
@@ -1079,7 +1108,7 @@ __device__ void shade_ray(const gb_run &P, const Ray &r, const Hit &h, Counters 
                 }
             }
         } else if (P.av[0] != 0.f || P.av[1] != 0.f || P.av[2] != 0.f) {
-            add_value(P, r.sensor, r.coef * aval * f3(P.av[0], P.av[1], P.av[2]));
+            add_value(P, r.sensor, r.tag, r.coef * aval * f3(P.av[0], P.av[1], P.av[2]));
         }
     }
     if (S.nsrc > 0)
@@ -1159,6 +1188,7 @@ __global__ void k_root(gb_run P)
         r.adepth = 0;
         r.path = GB_ROOT_PATH(P.replica);
         r.sensor = (uint32_t)(s + P.sensor_base);
+        r.tag = GB_NOTAG;
         r.adj.n = 0;
         float3 hp = f3((float)(sv[0] + 1e-4 * sv[3]), (float)(sv[1] + 1e-4 * sv[4]), (float)(sv[2] + 1e-4 * sv[5]));
         Surf su;
@@ -1185,7 +1215,7 @@ __global__ void k_root(gb_run P)
             rr->n = hm.n;
             /* hm.n >= 4: placed by k_root_draws and k_root_place */
         } else if (P.av[0] != 0.f || P.av[1] != 0.f || P.av[2] != 0.f) {
-            add_value(P, r.sensor, su.mcolor * f3(P.av[0], P.av[1], P.av[2]));
+            add_value(P, r.sensor, GB_NOTAG, su.mcolor * f3(P.av[0], P.av[1], P.av[2]));
         }
     }
     flush_counters(P, cnt);
@@ -1209,6 +1239,7 @@ __device__ __forceinline__ void root_parent(const gb_run &P, long long s, Ray &p
     parent.adepth = 0;
     parent.path = GB_ROOT_PATH(P.replica);
     parent.sensor = (uint32_t)(s + P.sensor_base);
+    parent.tag = GB_NOTAG;
     parent.adj.n = 0;
     hm.n = rr->n;
     hm.atyp = GB_RAMBIENT;
@@ -1325,9 +1356,157 @@ __global__ void __launch_bounds__(256) k_expand_root(gb_run P)
         Ray c;
         if (hemi_child(P, parent, hm, parent.org, -1, k, sp, c)) {
             c.adj.n = 0;                       /* the -I sensor is not a parameter */
+            if (P.ss_val)                      /* its value is kept per stratum */
+                c.tag = (uint32_t)g;
             push_ray<G>(P, c);
         }
     });
+}
+
+/* Ambient super-sampling of the -I first hemispheres (rt/ambcomp.c:256-346
+ * getambdiffs and ambsupersamp, called from samp_hemi :403-409), one
+ * thread per sensor, after the first pass has traced every stratum's whole
+ * path tree into ss_val.  A hemisphere of more than 7 x 7 strata, all of
+ * them alive, gets (int)(as * wt + .5) extra samples when that is at least
+ * four times its side: strata are weighted by the squared brightness
+ * differences with their neighbours (corrected for the number of
+ * neighbours and blurred), and each receives its share with random
+ * rounding, in row order, stopping at a sample lost to Russian roulette or
+ * when the budget is spent.  Extra sample m of stratum k is child
+ * GB_C_SSAMP(k, m) with a fresh jitter in the stratum and no collision
+ * test; it is queued for the second pass with the stratum's tag. */
+#define GB_MINADIV 7
+#define GB_CIE_RF 0.265074126f          /* common/color.h:253 default weights of pbright */
+#define GB_CIE_GF 0.670114631f
+#define GB_CIE_BF 0.064811243f
+__device__ __forceinline__ float pbright(const double *v)
+{
+    return GB_CIE_RF * (float)v[0] + GB_CIE_GF * (float)v[1] + GB_CIE_BF * (float)v[2];
+}
+
+__global__ void k_ssamp_plan(gb_run P)
+{
+    const long long nn = (long long)P.root_n * P.root_n;
+    for (long long s = blockIdx.x * (long long)blockDim.x + threadIdx.x; s < P.nsensors;
+         s += (long long)gridDim.x * blockDim.x) {
+        Ray parent;
+        Hemi hm;
+        root_parent(P, s, parent, hm);
+        const int n = hm.n;
+        if (n * n <= GB_MINADIV * GB_MINADIV || n < 4)
+            continue;
+        const float2 *dr = P.root_draw + s * nn;
+        bool all = true;                               /* every stratum sampled (sampOK) */
+        for (int k = 0; k < n * n && all; k++)
+            all = dr[k].x < 1.5f;
+        if (!all)
+            continue;
+        /* samp_hemi's weight for the Lambertian at weight 1 (make_hemi) */
+        float wt = 1.f, d = (float)D_PI * 0.8f / ((float)P.ad * P.minweight + 1e-20f);
+        if (wt > d)
+            wt = d;
+        int cnt = (int)((float)P.ss_samples * wt + .5f);
+        if (cnt < 4 * n)
+            continue;
+        const double *v = P.ss_val + 3ull * (s * nn);
+        float *earr = P.ss_err + 2ull * (s * nn), *ep2 = earr + n * n;
+        const float normf =
+            1.f / (GB_CIE_RF * hm.acoef.x + GB_CIE_GF * hm.acoef.y + GB_CIE_BF * hm.acoef.z + D_FTINY);
+        for (int k = 0; k < 2 * n * n; k++)
+            earr[k] = 0.f;
+        for (int i = 0; i < n; i++)
+            for (int j = 0; j < n; j++) {
+                const int k = i * n + j;
+                const float b = pbright(v + 3 * k);
+                float b1, d2;
+                if (i) {                               /* from above */
+                    b1 = pbright(v + 3 * (k - n));
+                    d2 = b - b1;
+                    d2 *= d2 * normf / (b + b1 + D_FTINY);
+                    ep2[k] += d2;
+                    ep2[k - n] += d2;
+                }
+                if (!j)
+                    continue;
+                b1 = pbright(v + 3 * (k - 1));         /* from behind */
+                d2 = b - b1;
+                d2 *= d2 * normf / (b + b1 + D_FTINY);
+                ep2[k] += d2;
+                ep2[k - 1] += d2;
+                if (!i)
+                    continue;
+                b1 = pbright(v + 3 * (k - n - 1));     /* diagonal */
+                d2 = b - b1;
+                d2 *= d2 * normf / (b + b1 + D_FTINY);
+                ep2[k] += d2;
+                ep2[k - n - 1] += d2;
+            }
+        ep2[0] *= 6.f / 3.f;                           /* corners and edges: fewer neighbours */
+        ep2[n - 1] *= 6.f / 3.f;
+        ep2[(n - 1) * n] *= 6.f / 3.f;
+        ep2[(n - 1) * n + n - 1] *= 6.f / 3.f;
+        for (int i = 1; i < n - 1; i++) {
+            ep2[i * n] *= 6.f / 5.f;
+            ep2[i * n + n - 1] *= 6.f / 5.f;
+        }
+        for (int j = 1; j < n - 1; j++) {
+            ep2[j] *= 6.f / 5.f;
+            ep2[(n - 1) * n + j] *= 6.f / 5.f;
+        }
+        for (int i = 0; i < n - 1; i++)                /* blur into the final map */
+            for (int j = 0; j < n - 1; j++) {
+                const int k = i * n + j;
+                earr[k] += .5f * ep2[k] + .125f * (ep2[k + 1] + ep2[k + n]);
+                earr[k + 1] += .125f * ep2[k];
+                earr[k + n] += .125f * ep2[k];
+            }
+        float e2rem = 0.f;
+        for (int k = n * n; k--;)
+            e2rem += earr[k];
+        for (int k = 0; k < n * n; k++) {
+            if (e2rem <= D_FTINY)
+                break;
+            const gb_u4 q = gb_draw(parent.path, parent.sensor, GB_G_SSAMP + (uint32_t)(k >> 2), P.k0, P.k1);
+            const int nss = (int)(earr[k] / e2rem * (float)cnt + gb_u01(q.v[k & 3]));
+            for (int m = 1; m <= nss; m++) {
+                Ray c;
+                if (!hemi_child(P, parent, hm, parent.org, -1, k, nullptr, c, GB_C_SSAMP(k, m)))
+                    break;
+                c.adj.n = 0;
+                c.tag = (uint32_t)(s * nn + k);
+                push_ray(P, c);
+                P.ss_cnt[s * nn + k]++;
+                if (!--cnt)
+                    break;
+            }
+            if (!cnt)
+                break;
+            e2rem -= earr[k];
+        }
+    }
+}
+
+/* each super-sampled stratum's value is the mean of its samples; the
+ * first hemisphere's value, their sum, goes to the sensor */
+__global__ void k_ssamp_final(gb_run P)
+{
+    const long long nn = (long long)P.root_n * P.root_n;
+    for (long long s = blockIdx.x * (long long)blockDim.x + threadIdx.x; s < P.nsensors;
+         s += (long long)gridDim.x * blockDim.x) {
+        double a[3] = {0., 0., 0.};
+        const double *v = P.ss_val + 3ull * (s * nn);
+        const int *m = P.ss_cnt + s * nn;
+        for (long long k = 0; k < nn; k++) {
+            const double w = 1.0 / (1.0 + m[k]);
+            a[0] += v[3 * k] * w;
+            a[1] += v[3 * k + 1] * w;
+            a[2] += v[3 * k + 2] * w;
+        }
+        double *o = P.value + 3ull * s;
+        o[0] += a[0];
+        o[1] += a[1];
+        o[2] += a[2];
+    }
 }
 
 /* radiance-mode primaries (rt/rtrace.c:436-468, rt/rcontrib.c:343-353)
@@ -1351,6 +1530,7 @@ __global__ void k_primary(gb_run P)
         r.adepth = 0;
         r.path = GB_ROOT_PATH(P.replica);
         r.sensor = (uint32_t)(s + P.sensor_base);
+        r.tag = GB_NOTAG;
         r.adj.n = 0;
         push_ray<G>(P, r);
     }
@@ -1442,6 +1622,8 @@ __global__ void __launch_bounds__(256, 4) k_shade(gb_run P)
         Ray r = load_ray(P.qin + g);
         if (G)
             r.adj = P.adj_in[g];
+        if (P.tag_in)
+            r.tag = P.tag_in[g];
         const Hit h = load_hit(P.hits + g);
         shade_ray<G>(P, r, h, cnt);
     });
@@ -1531,6 +1713,18 @@ int gb_launch_root_place(const gb_run *P, cudaStream_t st, int sms)
     /* a few sensors per warp: the placement is a long dependent chain per
      * sensor, so more warps on every SM hide more of its latency */
     k_root_place<<<grid_for(P->nsensors, 8, sms), 8, 0, st>>>(*P);
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+int gb_launch_ssamp_plan(const gb_run *P, cudaStream_t st, int sms)
+{
+    k_ssamp_plan<<<grid_for(P->nsensors, 32, sms), 32, 0, st>>>(*P);
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+int gb_launch_ssamp_final(const gb_run *P, cudaStream_t st, int sms)
+{
+    k_ssamp_final<<<grid_for(P->nsensors, 128, sms), 128, 0, st>>>(*P);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 

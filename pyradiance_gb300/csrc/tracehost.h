@@ -72,6 +72,7 @@ typedef struct {
     float specthresh;
     float specjitter;          /* -ss */
     int   follow;              /* rcontrib: every source is followed (SFOLLOW) */
+    int   do_irrad;            /* -i: primary hits shaded as a Lambertian irradiance meter */
     int   contrib_mode;        /* rcontrib -V */
     uint32_t k0, k1;           /* random stream key */
     uint32_t replica;
@@ -111,6 +112,16 @@ typedef struct {
     gb_qadj *adj_out;
     long long qcap;
     unsigned long long *work;  /* work-item counter of the persistent kernels (zeroed per launch) */
+    /* ambient super-sampling of the -I first hemispheres (rtrace -as):
+     * paths carry the index (sensor * root_n^2 + stratum) of the stratum
+     * they descend from in queue-parallel tag arrays, their values add to
+     * ss_val there; ss_cnt counts each stratum's extra samples */
+    int   ss_samples;          /* -as */
+    const uint32_t *tag_in;
+    uint32_t *tag_out;
+    double *ss_val;            /* n x root_n^2 x 3, or NULL: no super-sampling */
+    int   *ss_cnt;             /* n x root_n^2 */
+    float *ss_err;             /* n x 2 root_n^2 scratch of the error map */
 } gb_run;
 
 int gb_launch_cast(const gb_run *P, int *hit_obj, float *hit_t, float *hit_pn, cudaStream_t st, int sms);
@@ -119,6 +130,10 @@ int gb_launch_root(const gb_run *P, cudaStream_t st, int sms);
  * then the sequential placement per sensor */
 int gb_launch_root_draws(const gb_run *P, cudaStream_t st, int sms);
 int gb_launch_root_place(const gb_run *P, cudaStream_t st, int sms);
+/* -as super-sampling of the -I first hemispheres: the extra samples after
+ * the first pass, and the strata's means into the sensors after the second */
+int gb_launch_ssamp_plan(const gb_run *P, cudaStream_t st, int sms);
+int gb_launch_ssamp_final(const gb_run *P, cudaStream_t st, int sms);
 int gb_launch_expand_root(const gb_run *P, cudaStream_t st, int sms);
 int gb_launch_primary(const gb_run *P, cudaStream_t st, int sms);
 int gb_launch_trace(const gb_run *P, cudaStream_t st, int sms);

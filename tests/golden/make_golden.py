@@ -124,6 +124,61 @@ def glossy(tmp: Path, n: int = 300, K: int = 1024) -> None:
                                                                   stats["ss3_mean"].mean()))
 
 
+def surface_irradiance(tmp: Path, K: int = 256) -> None:
+    """rtrace -i (irradiance at the surface each ray hits): deterministic
+    with -ab 0 in the box room and in the empty window room (rays pass
+    through the glass, those leaving through the window see the sky and
+    ground glows), and with
+    one diffuse bounce (-ab 1 -aa 0 -as 0 -ad 256) as per-ray means and standard errors
+    of K replicas (-u+)."""
+    det = ["rtrace", "-h", "-u-", "-i", "-ab", "0", "-dj", "0", "-ds", "0", "-dr", "0", "-dt", "0", "-fdd", "-ov"]
+    out = {}
+    for key, text, seed in (("c1", w.daylight_room(), 7), ("c2e", w.window_room(ntri=0), 8)):
+        octp = oconv(text, tmp, f"irr_{key}")
+        rays = w.random_rays(2000, seed=seed)
+        if key == "c2e":                         # half of them aimed at the window
+            rng = np.random.default_rng(seed)
+            x0, x1, z0, z1 = w.WINDOW
+            tgt = np.stack([rng.uniform(x0, x1, 1000), np.zeros(1000), rng.uniform(z0, z1, 1000)], 1)
+            d = tgt - rays[:1000, :3]
+            rays[:1000, 3:] = d / np.linalg.norm(d, axis=1, keepdims=True)
+        out[f"{key}_rays"] = rays
+        out[f"{key}_irr"] = np.frombuffer(run([*det, octp], rays.astype("<f8").tobytes()),
+                                          dtype="<f8").reshape(-1, 3)
+    octp = tmp / "irr_c1.oct"
+    rays = w.random_rays(100, seed=9)
+    a = np.frombuffer(run(["rtrace", "-h", "-u+", "-i", "-ab", "1", "-aa", "0", "-as", "0", "-ad", "256", "-lw", "1e-4",
+                           "-dj", "0",
+                           "-ds", "0", "-dr", "0", "-dt", "0", "-fdd", "-ov", octp],
+                          np.repeat(rays, K, axis=0).astype("<f8").tobytes()), dtype="<f8").reshape(100, K, 3)
+    np.savez_compressed(OUT / "surface_irradiance.npz", **out, ab1_rays=rays, K=K, ab1_mean=a.mean(1),
+                        ab1_se=a.std(1, ddof=1) / np.sqrt(K),
+                        cmd="rtrace -h -u- -i -ab 0 -dj 0 -ds 0 -dr 0 -dt 0 | -u+ -i -ab 1 -aa 0 -as 0 -ad 256 -lw 1e-4")
+    print("surface_irradiance: c1 lit %.3f, c2e nonzero %.3f, ab1 mean %.4g" % (
+        (out["c1_irr"][:, 0] > 0).mean(), (out["c2e_irr"][:, 0] > 0).mean(), a.mean()))
+
+
+def supersampled_irradiance(tmp: Path, n: int = 100, K: int = 512) -> None:
+    """rtrace -I with ambient super-sampling (-as 512, rtrace's default;
+    -ab 2 -aa 0 -ad 256: 16 x 16 first hemispheres get 512 extra samples
+    placed by the strata's brightness differences, rt/ambcomp.c:256-346):
+    per-sensor means and standard errors of K replicas (-u+), with the same
+    run at -as 0 beside it."""
+    octp = oconv(w.daylight_room(), tmp, "ss_c1")
+    rays = w.random_rays(n, seed=9)
+    rep = np.repeat(rays, K, axis=0).astype("<f8").tobytes()
+    out = {}
+    for key, extra in (("as512", []), ("as0", ["-as", "0"])):
+        a = np.frombuffer(run(["rtrace", "-h", "-u+", "-I", "-ab", "2", "-aa", "0", "-ad", "256", "-lw", "1e-4",
+                               "-dj", "0", "-ds", "0", "-dr", "0", "-dt", "0", *extra, "-fdd", "-ov", octp], rep),
+                          dtype="<f8").reshape(n, K, 3)
+        out[f"{key}_mean"] = a.mean(1)
+        out[f"{key}_se"] = a.std(1, ddof=1) / np.sqrt(K)
+    np.savez_compressed(OUT / "supersampled.npz", rays=rays, K=K, **out,
+                        cmd="rtrace -h -u+ -I -ab 2 -aa 0 -ad 256 -lw 1e-4 -dj 0 -ds 0 -dr 0 -dt 0 [-as 0]")
+    print("supersampled: mean %.4g (as 512) vs %.4g (as 0)" % (out["as512_mean"].mean(), out["as0_mean"].mean()))
+
+
 # bin groups of the 146 columns: ground, then the 8 Reinhart MF:1 altitude rows
 ROW_EDGES = [0, 1, 31, 61, 85, 109, 127, 139, 145, 146]
 
@@ -208,7 +263,8 @@ def ref_fixture_trace() -> None:
 def main() -> None:
     if not (BIN / "rtrace").exists():
         sys.exit("reference programs missing: make -f oracle/build_ref.mk REF=/root/reference -j8")
-    parts = {"octree": octree_digests, "c1": c1_direct, "c1p": c1_partitioned, "zoo": zoo, "glossy": glossy,
+    parts = {"octree": octree_digests, "c1": c1_direct, "c1p": c1_partitioned, "zoo": zoo, "glossy": glossy, "irr": surface_irradiance,
+             "ss": supersampled_irradiance,
              "dct": lambda tmp: dct_small(), "trace_oct": lambda tmp: ref_fixture_trace(),
              "c2ab1": lambda tmp: c2_stats(tmp, ab=1, K=256), "c2ab3": lambda tmp: c2_stats(tmp, ab=3, K=256)}
     only = sys.argv[1:] or list(parts)         # e.g. make_golden.py c1p

@@ -14,7 +14,7 @@ import pytest
 
 pytestmark = pytest.mark.gpu
 
-ARGS = ("-I+", "-ab", "2", "-ad", "64", "-aa", "0", "-lw", "1e-6", "-u-")
+ARGS = ("-I+", "-ab", "2", "-ad", "64", "-aa", "0", "-as", "0", "-lw", "1e-6", "-u-")
 NMAT = 8
 
 

@@ -222,10 +222,73 @@ def test_c2_full_grid_bins_equal_irradiance(gb, scenes):
     rays = w.sensor_grid(64, 64)
     o = opts("rcontrib", I=1, ab=3, ad=1024, lw=1e-4, c=1, u=0, seed=99)
     out, nr = rcontrib_c(gb, scenes["c2"], o, rays)
-    ort = opts("rtrace", I=1, ab=3, ad=1024, lw=1e-4, aa=0, u=0, seed=99, dj=0.9, ds=0.2, st=0.02, dt=0)
+    ort = opts("rtrace", I=1, ab=3, ad=1024, lw=1e-4, aa=0, as_=0, u=0, seed=99, dj=0.9, ds=0.2, st=0.02, dt=0)
     rgb, _, _ = rtrace_c(gb, scenes["c2"], ort, rays)
     np.testing.assert_allclose(out.sum(1)[:, 0], rgb[:, 0], rtol=1e-5, atol=1e-12)
     assert nr > 4096 * 5000
+
+
+def test_supersampled_matches_oracle_sample_for_sample(gb, scenes, scene_dir):
+    """rtrace -I -ab 2 -aa 0 -ad 256 with -as 512 (rtrace's default): the
+    16 x 16 first hemispheres get 512 extra samples each after the first
+    pass, placed by their strata's brightness differences.  Same streams on
+    the GPU and in the oracle: the extra samples' placement depends on
+    FP32 versus FP64 values only where a stratum's share rounds differently,
+    so sensors agree closely."""
+    from oracle import pyoracle as po
+    g = golden("supersampled.npz")
+    rays = np.repeat(g["rays"][:40], 3, axis=0)
+    o = opts("rtrace", I=1, ab=2, aa=0, ad=256, lw=1e-4, dj=0, ds=0, dr=0, dt=0, u=0, seed=12)
+    assert o.as_ == 512
+    rgb, _, _ = rtrace_c(gb, scenes["c1"], o, rays)
+    oo = po.default_opts("rtrace", I=1, ab=2, aa=0, ad=256, lw=1e-4, dj=0, ds=0, dr=0, dt=0, u=0, seed=12)
+    ref, _, _, _ = po.rtrace(po.Scene(scene_dir / "c1.rad"), oo, rays, hits=False, threads=16)
+    rel = np.abs(rgb - ref).max(1) / np.maximum(np.abs(ref).max(1), 1e-9)
+    print("super-sampled vs oracle: median rel %.3g, share above 1e-3 %.3f, max %.3g" %
+          (np.median(rel), (rel > 1e-3).mean(), rel.max()))
+    assert np.median(rel) < 1e-4 and (rel <= 1e-3).mean() >= 0.9 and rel.max() < 5e-2
+
+
+@pytest.mark.parametrize("key,asn", [("as512", 512), ("as0", 0)])
+def test_supersampled_statistics_vs_reference(gb, scenes, key, asn):
+    """Per-sensor means of 512 replicas against the reference's 512 (-u+),
+    with and without super-sampling: z-scores within 5, their mean within 4
+    standard errors of zero."""
+    g = golden("supersampled.npz")
+    n, K = len(g["rays"]), 512
+    o = opts("rtrace", I=1, ab=2, aa=0, ad=256, lw=1e-4, dj=0, ds=0, dr=0, dt=0, u=0, seed=77, as_=asn)
+    rgb, _, _ = rtrace_c(gb, scenes["c1"], o, np.repeat(g["rays"], K, axis=0))
+    a = rgb.reshape(n, K, 3)
+    m, se = a.mean(1), a.std(1, ddof=1) / np.sqrt(K)
+    rm = g[f"{key}_mean"]
+    z = (m - rm) / np.sqrt(se ** 2 + g[f"{key}_se"] ** 2 + (1e-5 * np.abs(rm) + 1e-9) ** 2)
+    print("super-sampling %s: max |z| %.2f, mean z %.3f" % (key, np.abs(z).max(), z.mean()))
+    assert np.abs(z).max() < 5 and abs(z.mean()) < 4 / np.sqrt(n)
+
+
+@pytest.mark.parametrize("key", ["c1", "c2e"])
+def test_surface_irradiance(gb, scenes, key):
+    """-i (rt/raytrace.c:211-236): primary hits on non-light materials as a
+    Lambertian of reflectance pi, glass passed through; deterministic with
+    -ab 0.  The hit point is FP32, so a sensor near a shadow edge may differ
+    by the share of the light it sees from there."""
+    g = golden("surface_irradiance.npz")
+    rgb, _, _ = rtrace_c(gb, scenes[key], opts("rtrace", i=1, ab=0, dj=0, ds=0, dr=0, dt=0, u=0), g[f"{key}_rays"])
+    ref = g[f"{key}_irr"]
+    rel = np.abs(rgb - ref).max(1) / np.maximum(np.abs(ref).max(1), 1e-9)
+    assert np.median(rel) < 1e-5 and (rel <= 1e-4).mean() >= 0.99, (np.median(rel), (rel > 1e-4).mean())
+
+
+def test_surface_irradiance_one_bounce(gb, scenes):
+    g = golden("surface_irradiance.npz")
+    n, K = len(g["ab1_rays"]), 256
+    o = opts("rtrace", i=1, ab=1, aa=0, as_=0, ad=256, lw=1e-4, dj=0, ds=0, dr=0, dt=0, u=0, seed=3)
+    rgb, _, _ = rtrace_c(gb, scenes["c1"], o, np.repeat(g["ab1_rays"], K, axis=0))
+    a = rgb.reshape(n, K, 3)
+    m, se = a.mean(1), a.std(1, ddof=1) / np.sqrt(K)
+    z = (m - g["ab1_mean"]) / np.sqrt(se ** 2 + g["ab1_se"] ** 2 + (1e-5 * np.abs(g["ab1_mean"]) + 1e-9) ** 2)
+    print("-i -ab 1: max |z| %.2f, mean z %.3f" % (np.abs(z).max(), z.mean()))
+    assert np.abs(z).max() < 5 and abs(z.mean()) < 4 / np.sqrt(n)
 
 
 def test_dctimestep_fp32_fp64(gb):

@@ -16,7 +16,7 @@ REF_TRACE = Path("/root/reference/tests/Resources/trace.oct")
 
 @pytest.fixture(scope="module")
 def oscenes(scene_dir):
-    return {k: po.Scene(scene_dir / f"{k}.rad") for k in ("c1", "c2", "zoo", "glossy")}
+    return {k: po.Scene(scene_dir / f"{k}.rad") for k in ("c1", "c2", "zoo", "glossy", "c2e")}
 
 
 def test_octree_builder_matches_reference(scene_dir):
@@ -88,6 +88,50 @@ def test_glossy_sampled_lobe(oscenes, key, kw):
     assert np.abs(z).max() < 5, np.abs(z).max()
     assert abs(z.mean()) < 4 / np.sqrt(len(z)), z.mean()
     assert abs(m.mean() / g[f"{key}_mean"].mean() - 1) < 5e-3
+
+
+@pytest.mark.parametrize("key", ["c1", "c2e"])
+def test_surface_irradiance(oscenes, key):
+    """-i: primary hits on non-light materials shaded as a Lambertian of
+    reflectance pi, glass passed through (rt/raytrace.c:211-236)."""
+    g = golden("surface_irradiance.npz")
+    o = po.default_opts("rtrace", i=1, ab=0, dj=0, ds=0, dr=0, dt=0, u=0)
+    rgb, _, _, _ = po.rtrace(oscenes[key], o, g[f"{key}_rays"], hits=False, threads=8)
+    np.testing.assert_allclose(rgb, g[f"{key}_irr"], rtol=1e-6, atol=1e-9)
+
+
+def test_surface_irradiance_one_bounce(oscenes):
+    """-i -ab 1 -ad 256: per-ray means of 256 replicas against the
+    reference's (-u+), z-scores within 5, their mean within 4 standard
+    errors of zero."""
+    g = golden("surface_irradiance.npz")
+    K, n = 256, len(g["ab1_rays"])
+    o = po.default_opts("rtrace", i=1, ab=1, ad=256, lw=1e-4, dj=0, ds=0, dr=0, dt=0, u=0, aa=0)
+    rgb, _, _, _ = po.rtrace(oscenes["c1"], o, np.repeat(g["ab1_rays"], K, axis=0), hits=False, threads=8)
+    a = rgb.reshape(n, K, 3)
+    m, se = a.mean(1), a.std(1, ddof=1) / np.sqrt(K)
+    z = (m - g["ab1_mean"]) / np.sqrt(se ** 2 + g["ab1_se"] ** 2 + (1e-6 * np.abs(g["ab1_mean"]) + 1e-9) ** 2)
+    assert np.abs(z).max() < 5 and abs(z.mean()) < 4 / np.sqrt(n), (np.abs(z).max(), z.mean())
+
+
+@pytest.mark.parametrize("key,asn", [("as512", 512), ("as0", 0)])
+def test_supersampled_first_hemisphere(oscenes, key, asn):
+    """rtrace -I -ab 2 -aa 0 -ad 256 with ambient super-sampling (-as 512,
+    rtrace's default; rt/ambcomp.c:256-346) and without: per-sensor means of
+    96 replicas against the reference's 512 (-u+), z-scores within 5, their
+    mean within 4 standard errors of zero.  (Without the super-sampling the
+    -as 512 means differ from the reference's by up to 1.5% on single
+    sensors, many standard errors.)"""
+    g = golden("supersampled.npz")
+    K, n = 96, 40
+    o = po.default_opts("rtrace", I=1, ab=2, aa=0, ad=256, lw=1e-4, dj=0, ds=0, dr=0, dt=0, u=0)
+    o.as_ = asn
+    rgb, _, _, _ = po.rtrace(oscenes["c1"], o, np.repeat(g["rays"][:n], K, axis=0), hits=False, threads=16)
+    a = rgb.reshape(n, K, 3)
+    m, se = a.mean(1), a.std(1, ddof=1) / np.sqrt(K)
+    rm, rse = g[f"{key}_mean"][:n], g[f"{key}_se"][:n]
+    z = (m - rm) / np.sqrt(se ** 2 + rse ** 2 + (1e-6 * np.abs(rm) + 1e-9) ** 2)
+    assert np.abs(z).max() < 5 and abs(z.mean()) < 4 / np.sqrt(n), (np.abs(z).max(), z.mean())
 
 
 def test_zoo_cast_and_direct(oscenes):

@@ -59,8 +59,8 @@ CASES = {
     # radiance with mirror and glass chains: later generations through the queues
     "zoo_chains": ("zoo", dict(ab=0, dj=0, ds=0, dr=0, dt=0, u=0), 0.0),
     # Monte Carlo irradiance with one ambient bounce (first hemisphere queue)
-    "c2_ambient": ("c2", dict(I=1, ab=1, ad=64, lw=1e-4, aa=0, u=0, seed=31, dj=0.9, ds=0.2, st=0.02, dt=0),
-                   1e-9),
+    "c2_ambient": ("c2", dict(I=1, ab=1, ad=64, lw=1e-4, aa=0, as_=0, u=0, seed=31, dj=0.9, ds=0.2, st=0.02,
+                              dt=0), 1e-9),
 }
 
 
@@ -90,10 +90,15 @@ def test_noalloc_rejects_oversized_calls(env):
     torch, _lib, scenes = env
     from pyradiance_gb300 import workloads as w
     rays = np.ascontiguousarray(w.sensor_grid(16, 16), dtype=np.float64)
-    o = opts(_lib, I=1, ab=1, ad=1024, lw=1e-4, aa=0, u=0, seed=5)
+    o = opts(_lib, I=1, ab=1, ad=1024, lw=1e-4, aa=0, as_=0, u=0, seed=5)
     with pytest.raises(_lib.GbError) as e:
         noalloc_rtrace(torch, _lib, scenes["c2"], o, rays)
     assert e.value.code == -1 and "scratch" in str(e.value)
+    # super-sampling (-as, rtrace's default 512) needs allocation: refused
+    o.as_ = 512
+    with pytest.raises(_lib.GbError) as e:
+        noalloc_rtrace(torch, _lib, scenes["c2"], o, rays[:4])
+    assert e.value.code == -3 and "-as" in str(e.value)
     # a host pointer is refused before any launch
     d_rgb = torch.zeros((4, 3), dtype=torch.float64, device="cuda")
     host_rays = np.ascontiguousarray(rays[:4])
