@@ -71,6 +71,7 @@ typedef struct {
 typedef struct {
     gb_scene_host H;
     int *mat;                /* per object: material object or -1 */
+    int *inst_of;            /* per object: its instance record or -1 */
     osrc *src;
     int nsrc;
     char err[512];
@@ -124,7 +125,7 @@ static int mark_sources(oscene *O)
     int32_t i;
     O->src = (osrc *)calloc((size_t)H->nobjs + 1, sizeof(osrc));
     O->nsrc = 0;
-    for (i = 0; i < H->nobjs; i++) {
+    for (i = 0; i < H->nobjs_top; i++) {      /* not the objects of instanced octrees */
         const gb_object *o = &H->objs[i];
         int m = O->mat[i];
         osrc *s;
@@ -221,11 +222,23 @@ static oscene *scene_open(const char *path, int is_rad, char *err, int errlen)
             goto bad;
     } else if (gb_scene_read_oct(&O->H, path) < 0)
         goto bad;
+    {
+        char dir[4096];
+        const char *sl = strrchr(path, '/');
+        snprintf(dir, sizeof dir, "%.*s", sl ? (int)(sl - path) : 1, sl ? path : ".");
+        if (gb_scene_load_instances(&O->H, dir) < 0)
+            goto bad;
+    }
     if (gb_scene_prepare(&O->H) < 0)
         goto bad;
     O->mat = (int *)malloc(sizeof(int) * ((size_t)O->H.nobjs + 1));
-    for (i = 0; i < O->H.nobjs; i++)
+    O->inst_of = (int *)malloc(sizeof(int) * ((size_t)O->H.nobjs + 1));
+    for (i = 0; i < O->H.nobjs; i++) {
         O->mat[i] = gb_is_surface(O->H.objs[i].otype) ? gb_find_material(&O->H, i) : -1;
+        O->inst_of[i] = -1;
+    }
+    for (i = 0; i < O->H.ninst; i++)
+        O->inst_of[O->H.inst[i].obj] = i;
     if (mark_sources(O) < 0) {
         snprintf(err, errlen, "%s", O->err);
         return NULL;
@@ -243,6 +256,7 @@ static void scene_close(oscene *O)
     if (!O) return;
     gb_scene_clear(&O->H);
     free(O->mat);
+    free(O->inst_of);
     free(O->src);
     free(O);
 }
@@ -588,17 +602,66 @@ static int o_cone(const oscene *O, int o, RAY *r)
     return 0;
 }
 
+typedef struct { double cuorg[3]; double cusize; int cutree; } CUBE;
+
+static int localhit_cube(const oscene *O, RAY *r, const CUBE *scene);
+
+/* common/mat4.c multp3/multv3: row vector times a 4x4 transform */
+static void xf_vec(double out[3], const double v[3], const double m[4][4])
+{
+    double t[3];
+    int j;
+    for (j = 0; j < 3; j++) t[j] = v[0] * m[0][j] + v[1] * m[1][j] + v[2] * m[2][j];
+    memcpy(out, t, sizeof t);
+}
+
+static void xf_pnt(double out[3], const double p[3], const double m[4][4])
+{
+    xf_vec(out, p, m);
+    out[0] += m[3][0];
+    out[1] += m[3][1];
+    out[2] += m[3][2];
+}
+
+/* rt/o_instance.c:15-71: the ray in the instance's coordinates through its
+ * octree, the hit transformed back if it is closer */
+static int o_instance(const oscene *O, int o, RAY *r)
+{
+    const gb_instance *ins = &O->H.inst[O->inst_of[o]];
+    const gb_subscene *sc = &O->H.subs[ins->sub];
+    RAY rc = *r;
+    CUBE cu;
+    double d;
+    int i;
+    xf_pnt(rc.rorg, r->rorg, ins->b.xfm);
+    xf_vec(rc.rdir, r->rdir, ins->b.xfm);
+    for (i = 0; i < 3; i++) rc.rdir[i] /= ins->b.sca;
+    rayclear(&rc);
+    memcpy(cu.cuorg, sc->cuorg, sizeof cu.cuorg);
+    cu.cusize = sc->cusize;
+    cu.cutree = sc->root;
+    if (!localhit_cube(O, &rc, &cu)) return 0;
+    if (rc.rot * ins->f.sca >= r->rot) return 0;
+    r->ro = O->H.objs[o].omod >= 0 ? o : rc.ro;
+    r->rot = rc.rot * ins->f.sca;
+    xf_pnt(r->rop, rc.rop, ins->f.xfm);
+    xf_vec(r->ron, rc.ron, ins->f.xfm);
+    d = 1. / ins->f.sca;
+    for (i = 0; i < 3; i++) r->ron[i] *= d;
+    r->rod = rc.rod;
+    return 1;
+}
+
 static int object_hit(const oscene *O, int o, RAY *r)
 {
     switch (O->H.objs[o].otype) {
     case GT_POLYGON: return o_face(O, o, r);
     case GT_SPHERE: case GT_BUBBLE: return o_sphere(O, o, r);
     case GT_CONE: case GT_CUP: case GT_CYLINDER: case GT_TUBE: case GT_RING: return o_cone(O, o, r);
+    case GT_INSTANCE: return o_instance(O, o, r);
     default: return 0;
     }
 }
-
-typedef struct { double cuorg[3]; double cusize; int cutree; } CUBE;
 
 static int incube(const CUBE *cu, const double pt[3])
 {
@@ -695,15 +758,20 @@ static int raymove(const oscene *O, double pos[3], int32_t *cxs, int dirf, RAY *
 
 static int localhit(ctx *X, RAY *r)
 {
-    const oscene *O = X->O;
+    CUBE scene;
+    X->rays++;
+    memcpy(scene.cuorg, X->O->H.cuorg, sizeof scene.cuorg);
+    scene.cusize = X->O->H.cusize;
+    scene.cutree = X->O->H.root;
+    return localhit_cube(X->O, r, &scene);
+}
+
+static int localhit_cube(const oscene *O, RAY *r, const CUBE *scube)
+{
     int32_t cxset[MAXCSET + 1];
     double curpos[3], t, dt;
     int sflags = 0, i;
-    CUBE scene;
-    X->rays++;
-    memcpy(scene.cuorg, O->H.cuorg, sizeof scene.cuorg);
-    scene.cusize = O->H.cusize;
-    scene.cutree = O->H.root;
+    CUBE scene = *scube;
     for (i = 0; i < 3; i++) {
         curpos[i] = r->rorg[i];
         if (r->rdir[i] > 1e-7) sflags |= 1 << i;

@@ -24,6 +24,7 @@
  *   src       gb_dsrc[nsrc]       light sources (rt/source.h SRCREC subset)
  *   trk       int32[nobjs]        tracked-modifier slot of each object's
  *                                 direct modifier (-1 untracked)
+ *   inst      gb_dinst[ninst]     instances: transforms, octree, surface ids
  */
 #ifndef GB_DEVSCENE_H
 #define GB_DEVSCENE_H
@@ -31,7 +32,8 @@
 #include <stdint.h>
 
 /* object kinds on the device */
-enum { DK_NONE = 0, DK_FACE, DK_SPHERE, DK_BUBBLE, DK_CONE, DK_CUP, DK_CYL, DK_TUBE, DK_RING, DK_SOURCE };
+enum { DK_NONE = 0, DK_FACE, DK_SPHERE, DK_BUBBLE, DK_CONE, DK_CUP, DK_CYL, DK_TUBE, DK_RING, DK_SOURCE,
+       DK_INSTANCE };
 /* object flags */
 #define DF_HASMAT  0x01   /* has a material (findmaterial != NULL) */
 #define DF_TRANSP  0x02   /* material is nominally transparent */
@@ -69,6 +71,23 @@ typedef struct {
     int   pad;
 } gb_dsrc;
 
+/* An instance (rt/o_instance.c): the transforms to and from its octree's
+ * coordinates (rows of the 4x4 row-vector matrices of common/xf.c; the
+ * fourth row is the translation), that octree's cube and root, and its
+ * objects.  Surfaces inside instances are identified by surface ids
+ * sidbase + (object - firstobj), above every object index, so that the same
+ * instanced object in two instances has two ids. */
+typedef struct {
+    float bx[12], fx[12];      /* backward (world -> instance) and forward */
+    float bsca, fsca;
+    float cuorg[3], cusize, grid_scale, cell;
+    int   root;                /* leaf-coded root code of its octree */
+    int   obj;                 /* the instance object */
+    int   hasmod;              /* the instance's modifier replaces its surfaces' own */
+    int   sidbase;             /* first surface id */
+    int   firstobj, nobjs;     /* its octree's objects */
+} gb_dinst;
+
 typedef struct {
     /* octree */
     float cuorg[3];
@@ -93,6 +112,9 @@ typedef struct {
     const gb_dsrc *src;
     /* tracked modifiers (per object) */
     const int *trk;
+    /* instances, in order of sidbase */
+    int   ninst;
+    const gb_dinst *inst;
 } gb_dscene;
 
 #endif

@@ -95,6 +95,7 @@ struct gb_scene {
     std::vector<std::string> modname, matname;
     /* host arrays of the device scene */
     std::vector<int> hkids, hsetdata;
+    std::vector<gb_dinst> hinst;
     std::vector<int4> hobj;
     std::vector<float4> hgeo;
     std::vector<float2> hfvert;
@@ -102,11 +103,11 @@ struct gb_scene {
     std::vector<float> hcone;
     std::vector<gb_dsrc> hsrc;
     /* device scene */
-    DevBuf kids, setdata, obj, geo, fvert, fv4, cone, matd, srcd, trk;
+    DevBuf kids, setdata, obj, geo, fvert, fv4, cone, matd, srcd, trk, instd;
     gb_dscene ds;
     /* work buffers */
     DevBuf sensors, value, bins, stats, roots, rootspt, qa, qb, qcount, binprog, modinfo, hits, hitt, trkrun,
-        hitrec, adja, adjb, dlde, gradd, rootdraw, rootlot, tga, tgb, ssval, sscnt, sserr;
+        hitrec, adja, adjb, dlde, gradd, rootdraw, rootlot, tga, tgb, ssval, sscnt, sserr, slow;
     cudaStream_t stream = nullptr;
     int sms = 0;
     cudaEvent_t ev[2 * GB_TIMED_LAUNCHES + 2];
@@ -199,7 +200,9 @@ static double dist2line(const double p[3], const double a[3], const double b[3])
 static int mark_sources(gb_scene *G)
 {
     gb_scene_host &H = G->H;
-    for (int32_t i = 0; i < H.nobjs; i++) {
+    /* the scene's own objects only: the reference marks sources before any
+     * instance loads its octree (rt/source.c:47-142) */
+    for (int32_t i = 0; i < H.nobjs_top; i++) {
         const gb_object *o = &H.objs[i];
         if (!gb_is_surface(o->otype) || o->omod < 0)
             continue;
@@ -349,7 +352,7 @@ static int prepare_device(gb_scene *G)
     cudaDeviceGetLimit(&stack, cudaLimitStackSize);
     if (stack < 16384)
         CK(cudaDeviceSetLimit(cudaLimitStackSize, 16384));
-    if (upload(G->kids, G->hkids) < 0 || upload(G->setdata, G->hsetdata) < 0 ||
+    if (upload(G->kids, G->hkids) < 0 || upload(G->setdata, G->hsetdata) < 0 || upload(G->instd, G->hinst) < 0 ||
         upload(G->obj, G->hobj) < 0 || upload(G->geo, G->hgeo) < 0 || upload(G->fvert, G->hfvert) < 0 ||
         upload(G->fv4, G->hfv4) < 0 || upload(G->cone, G->hcone) < 0 || upload(G->matd, G->mat) < 0 ||
         upload(G->srcd, G->hsrc) < 0)
@@ -364,6 +367,7 @@ static int prepare_device(gb_scene *G)
     d.cone = (const float *)G->cone.p;
     d.mat = (const float4 *)G->matd.p;
     d.src = (const gb_dsrc *)G->srcd.p;
+    d.inst = (const gb_dinst *)G->instd.p;
     (void)H;
     return GB_OK;
 }
@@ -481,6 +485,13 @@ static int build_arrays(gb_scene *G)
         case GT_SOURCE:
             kind = DK_SOURCE;
             break;
+        case GT_INSTANCE:
+            for (int k = 0; k < H.ninst; k++)
+                if (H.inst[k].obj == i) {
+                    kind = DK_INSTANCE;
+                    aux = k;
+                }
+            break;
         default:
             break;
         }
@@ -517,6 +528,36 @@ static int build_arrays(gb_scene *G)
     };
     for (int &k : kids)
         k = leaf_code(k);
+    /* instances: surface ids of their objects above every object index */
+    std::vector<gb_dinst> inst((size_t)(H.ninst > 0 ? H.ninst : 1));
+    long long sid = H.nobjs;
+    for (int k = 0; k < H.ninst; k++) {
+        const gb_instance &I = H.inst[k];
+        const gb_subscene &sc = H.subs[I.sub];
+        gb_dinst &d = inst[k];
+        memset(&d, 0, sizeof d);
+        for (int r = 0; r < 4; r++)
+            for (int c = 0; c < 3; c++) {
+                d.bx[3 * r + c] = (float)I.b.xfm[r][c];
+                d.fx[3 * r + c] = (float)I.f.xfm[r][c];
+            }
+        d.bsca = (float)I.b.sca;
+        d.fsca = (float)I.f.sca;
+        for (int c = 0; c < 3; c++) d.cuorg[c] = (float)sc.cuorg[c];
+        d.cusize = (float)sc.cusize;
+        d.grid_scale = (float)((double)(1 << GRID_BITS_HOST) / sc.cusize);
+        d.cell = (float)(sc.cusize / (double)(1 << GRID_BITS_HOST));
+        d.root = leaf_code(sc.root);
+        d.obj = I.obj;
+        d.hasmod = H.objs[I.obj].omod >= 0;
+        d.sidbase = (int)sid;
+        d.firstobj = sc.firstobj;
+        d.nobjs = sc.nobjs;
+        sid += sc.nobjs;
+    }
+    if (sid >= 0x7fffffffll)
+        return set_err(GB_EUNSUPPORTED, "%lld instanced surfaces exceed the 2^31 surface ids", sid);
+    G->hinst.swap(inst);
     std::vector<gb_dsrc> src = G->src;
     if (src.empty()) src.resize(1);
     G->hkids.swap(kids);
@@ -546,6 +587,8 @@ static int build_arrays(gb_scene *G)
     d.mat = G->mat.data();
     d.nsrc = (int)G->src.size();
     d.src = G->hsrc.data();
+    d.ninst = H.ninst;
+    d.inst = G->hinst.data();
     /* names for output */
     G->modname.resize(H.nobjs);
     G->matname.resize(H.nobjs);
@@ -580,6 +623,14 @@ extern "C" int gb_scene_load(const char *oct_path, gb_scene **out)
         gb_scene_free(G);
         return rc;
     }
+    std::string dir(oct_path);                   /* instance octrees: also beside this one */
+    size_t sl = dir.find_last_of('/');
+    dir = sl == std::string::npos ? std::string(".") : dir.substr(0, sl);
+    if (gb_scene_load_instances(&G->H, dir.c_str()) < 0) {
+        int rc = set_err(GB_EIO, "%s", gb_scene_error());
+        gb_scene_free(G);
+        return rc;
+    }
     return finish_load(G, out);
 }
 
@@ -595,7 +646,14 @@ extern "C" int gb_scene_load_rad(const char *const *paths, int npaths, int objli
             gb_scene_free(G);
             return rc;
         }
-    if (gb_scene_build_octree(&G->H, objlim, resolu) < 0) {
+    for (int32_t i = 0; i < G->H.nobjs; i++)
+        if (gb_is_volume(G->H.objs[i].otype)) {
+            int rc = set_err(GB_EUNSUPPORTED, "%s: instances and meshes are read from an octree made by oconv, "
+                             "not built here", G->H.objs[i].name);
+            gb_scene_free(G);
+            return rc;
+        }
+    if (gb_scene_build_octree(&G->H, objlim, resolu) < 0 || gb_scene_load_instances(&G->H, ".") < 0) {
         int rc = set_err(GB_EIO, "octree build failed: %s", gb_scene_error());
         gb_scene_free(G);
         return rc;
@@ -607,11 +665,11 @@ extern "C" void gb_scene_free(gb_scene *G)
 {
     if (!G)
         return;
-    DevBuf *bufs[] = {&G->kids, &G->setdata, &G->obj, &G->geo, &G->fvert, &G->fv4, &G->cone, &G->matd,
+    DevBuf *bufs[] = {&G->kids, &G->setdata, &G->instd, &G->obj, &G->geo, &G->fvert, &G->fv4, &G->cone, &G->matd,
                       &G->srcd, &G->trk, &G->sensors, &G->value, &G->bins, &G->stats, &G->roots, &G->rootspt, &G->qa,
                       &G->qb, &G->qcount, &G->binprog, &G->modinfo, &G->hits, &G->hitt, &G->trkrun, &G->hitrec,
                       &G->adja, &G->adjb, &G->dlde, &G->gradd, &G->rootdraw, &G->rootlot, &G->tga, &G->tgb,
-                      &G->ssval, &G->sscnt, &G->sserr};
+                      &G->ssval, &G->sscnt, &G->sserr, &G->slow};
     for (DevBuf *b : bufs)
         b->release();
     if (G->stream)
@@ -1086,6 +1144,12 @@ static int run(gb_scene *G, const gb_opts *o, int follow, const double *org_dir,
         P.grad = (double *)G->gradd.p;
         P.nslots = nslots;
     }
+    if (G->H.ninst > 0) {                        /* walks that met an instance */
+        if (G->slow.ensure((size_t)qcap * sizeof(unsigned int)) < 0)
+            return set_err(GB_ENOMEM, "cannot allocate the instance walk list");
+        P.slow = (unsigned int *)G->slow.p;
+        P.slow_count = (unsigned long long *)G->qcount.p + 3;
+    }
     uint32_t *tags[2] = {nullptr, nullptr};
     if (ss > 0) {
         const size_t nn = (size_t)n0 * n0;
@@ -1174,6 +1238,8 @@ static int run(gb_scene *G, const gb_opts *o, int follow, const double *org_dir,
             P.tag_out = tags[1 - in];
             CK(cudaMemsetAsync(cnt + (1 - in), 0, sizeof(unsigned long long), st));
             CK(cudaMemsetAsync(P.work, 0, sizeof(unsigned long long), st));
+            if (P.slow_count)
+                CK(cudaMemsetAsync(P.slow_count, 0, sizeof(unsigned long long), st));
             int rc = launch(GB_K_TRACE, P, [&](gb_run &R) { return gb_launch_trace(&R, st, G->sms); });
             if (rc < 0)
                 return rc;
@@ -1716,6 +1782,8 @@ extern "C" int gb_rtrace_device_noalloc(gb_scene *G, const gb_opts *o, const dou
     if (n0 > 128)
         return set_err(GB_EUNSUPPORTED, "-ad %d gives %d x %d hemisphere divisions; at most 128 x 128 are "
                        "supported", o->ad, n0, n0);
+    if (G->H.ninst > 0)
+        return set_err(GB_EUNSUPPORTED, "scenes with instances are not traced without allocation");
     if (check_supersampling(o, n0) < 0 || supersamples(o, n0) > 0)
         return set_err(GB_EUNSUPPORTED, "ambient super-sampling (-as %d) is not implemented without allocation; "
                        "use -as 0", o->as);

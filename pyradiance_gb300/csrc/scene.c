@@ -120,6 +120,10 @@ void gb_scene_clear(gb_scene_host *S)
     for (k = 0; k < S->nfiles; k++)
         free(S->files[k]);
     free(S->files);
+    for (k = 0; k < S->nsubs; k++)
+        free(S->subs[k].name);
+    free(S->subs);
+    free(S->inst);
     gb_scene_init(S);
 }
 
@@ -971,5 +975,243 @@ int gb_scene_prepare(gb_scene_host *S)
         }
     }
     S->prepared = 1;
+    return 0;
+}
+
+/* ------------------------------------------------------------- instances */
+
+static void mat_ident(double m[4][4])
+{
+    int i, j;
+    for (i = 0; i < 4; i++)
+        for (j = 0; j < 4; j++)
+            m[i][j] = i == j;
+}
+
+static void mat_mul(double r[4][4], const double a[4][4], const double b[4][4])   /* r = a b */
+{
+    double t[4][4];
+    int i, j;
+    for (i = 0; i < 4; i++)
+        for (j = 0; j < 4; j++)
+            t[i][j] = a[i][0] * b[0][j] + a[i][1] * b[1][j] + a[i][2] * b[2][j] + a[i][3] * b[3][j];
+    memcpy(r, t, sizeof t);
+}
+
+/* the arguments after option av[i] match fmt ('f' real, 'i' integer) */
+static int xf_args_ok(int ac, char *const *av, int i, const char *fmt)
+{
+    int k;
+    for (k = 0; fmt[k]; k++) {
+        char *e;
+        if (i + 1 + k >= ac)
+            return 0;
+        if (fmt[k] == 'i')
+            (void)strtol(av[i + 1 + k], &e, 10);
+        else
+            (void)strtod(av[i + 1 + k], &e);
+        if (e == av[i + 1 + k] || *e)
+            return 0;
+    }
+    return 1;
+}
+
+/* common/xf.c xf (inverse = 0) and invxf (inverse = 1): transform options
+ * -t x y z, -rx/-ry/-rz degrees, -s factor, -mx/-my/-mz, -i count; each
+ * elementary transform multiplies on the right (forward) or on the left
+ * (inverse, with the elementary inverse), -i repeats what precedes it.
+ * Returns the number of arguments used. */
+static int xf_parse(gb_xf *ret, int ac, char *const *av, int inverse)
+{
+    double xfmat[4][4], m4[4][4], xfsca = 1.0, d;
+    int i, icnt = 1;
+    mat_ident(ret->xfm);
+    ret->sca = 1.0;
+    mat_ident(xfmat);
+    for (i = 0; i < ac && av[i][0] == '-'; i++) {
+        const char *o = av[i] + 1;
+        mat_ident(m4);
+        if (o[0] == 't' && !o[1] && xf_args_ok(ac, av, i, "fff")) {
+            int k;
+            for (k = 0; k < 3; k++)
+                m4[3][k] = (inverse ? -1.0 : 1.0) * atof(av[++i]);
+        } else if (o[0] == 'r' && o[1] >= 'x' && o[1] <= 'z' && !o[2] && xf_args_ok(ac, av, i, "f")) {
+            int a = (o[1] - 'x' + 1) % 3, b = (a + 1) % 3;     /* the rotation plane */
+            d = (inverse ? -1.0 : 1.0) * (M_PI / 180.0) * atof(av[++i]);
+            m4[a][a] = m4[b][b] = cos(d);
+            m4[a][b] = sin(d);
+            m4[b][a] = -m4[a][b];
+        } else if (o[0] == 's' && !o[1] && xf_args_ok(ac, av, i, "f")) {
+            d = atof(av[i + 1]);
+            if (d == 0.0)
+                break;
+            i++;
+            if (inverse)
+                d = 1.0 / d;
+            xfsca *= d;
+            m4[0][0] = m4[1][1] = m4[2][2] = d;
+        } else if (o[0] == 'm' && o[1] >= 'x' && o[1] <= 'z' && !o[2]) {
+            int a = o[1] - 'x';
+            xfsca *= -1.0;
+            m4[a][a] = -1.0;
+        } else if (o[0] == 'i' && !o[1] && xf_args_ok(ac, av, i, "i")) {
+            while (icnt-- > 0) {
+                if (inverse)
+                    mat_mul(ret->xfm, xfmat, ret->xfm);
+                else
+                    mat_mul(ret->xfm, ret->xfm, xfmat);
+                ret->sca *= xfsca;
+            }
+            icnt = atoi(av[++i]);
+            mat_ident(xfmat);
+            xfsca = 1.0;
+            continue;
+        } else
+            break;
+        if (inverse)
+            mat_mul(xfmat, m4, xfmat);
+        else
+            mat_mul(xfmat, xfmat, m4);
+    }
+    while (icnt-- > 0) {
+        if (inverse)
+            mat_mul(ret->xfm, xfmat, ret->xfm);
+        else
+            mat_mul(ret->xfm, ret->xfm, xfmat);
+        ret->sca *= xfsca;
+    }
+    return i;
+}
+
+int gb_fullxf(gb_xf *f, gb_xf *b, int ac, char *const *av)
+{
+    xf_parse(f, ac, av, 0);
+    return xf_parse(b, ac, av, 1);
+}
+
+static int32_t remap_code(int32_t code, int32_t nodebase, int32_t setbase)
+{
+    if (code >= 0)
+        return code + nodebase;
+    if (code == -1)
+        return -1;
+    return -2 - ((-code - 2) + setbase);
+}
+
+/* append the objects, nodes and sets of T to S; returns the sub-scene
+ * index or -1 */
+static int merge_subscene(gb_scene_host *S, gb_scene_host *T, const char *name)
+{
+    int32_t objbase = S->nobjs, nodebase = S->nnodes, setbase = S->nsets, i;
+    int k;
+    gb_subscene *ns;
+    for (i = 0; i < T->nobjs; i++) {
+        gb_object *o = new_object(S);
+        if (!o)
+            return fail("out of memory loading \"%s\"", name);
+        *o = T->objs[i];                       /* takes the strings and arguments */
+        if (o->omod >= 0)
+            o->omod += objbase;
+    }
+    T->nobjs = 0;
+    for (i = 0; i < T->nnodes; i++) {
+        int32_t nd = gb__new_node(S);
+        if (nd < 0)
+            return fail("out of memory loading \"%s\"", name);
+        for (k = 0; k < 8; k++)
+            S->kids[8 * nd + k] = remap_code(T->kids[8 * i + k], nodebase, setbase);
+    }
+    for (i = 0; i < T->nsets; i++) {
+        const int32_t *st = T->set_data + T->set_off[i];
+        int32_t *cp = (int32_t *)malloc(((size_t)st[0] + 1) * sizeof(int32_t));
+        if (!cp)
+            return fail("out of memory loading \"%s\"", name);
+        cp[0] = st[0];
+        for (k = 1; k <= st[0]; k++)
+            cp[k] = st[k] + objbase;
+        if (!gb__add_set(S, cp)) {
+            free(cp);
+            return fail("out of memory loading \"%s\"", name);
+        }
+        free(cp);
+    }
+    ns = (gb_subscene *)realloc(S->subs, (size_t)(S->nsubs + 1) * sizeof *ns);
+    if (!ns)
+        return fail("out of memory loading \"%s\"", name);
+    S->subs = ns;
+    ns = &S->subs[S->nsubs];
+    ns->name = strdup(name);
+    memcpy(ns->cuorg, T->cuorg, sizeof ns->cuorg);
+    ns->cusize = T->cusize;
+    ns->root = remap_code(T->root, nodebase, setbase);
+    ns->firstobj = objbase;
+    ns->nobjs = S->nobjs - objbase;
+    return S->nsubs++;
+}
+
+int gb_scene_load_instances(gb_scene_host *S, const char *base_dir)
+{
+    int32_t i, ntop = S->nobjs;
+    S->nobjs_top = ntop;
+    for (i = 0; i < ntop; i++) {
+        gb_object *o = &S->objs[i];
+        gb_instance *ni;
+        int sub = -1, k;
+        if (o->otype == GT_MESH)
+            return fail("%s: mesh objects are not supported", o->name);
+        if (o->otype != GT_INSTANCE)
+            continue;
+        if (o->nsargs < 1)
+            return fail("%s: bad # of arguments", o->name);
+        ni = (gb_instance *)realloc(S->inst, (size_t)(S->ninst + 1) * sizeof *ni);
+        if (!ni)
+            return fail("out of memory");
+        S->inst = ni;
+        ni = &S->inst[S->ninst];
+        ni->obj = i;
+        if (gb_fullxf(&ni->f, &ni->b, o->nsargs - 1, o->sarg + 1) != o->nsargs - 1)
+            return fail("%s: bad transform", o->name);
+        if (ni->f.sca < 0.0) {                 /* a mirror: common/instance.c:84-87 */
+            ni->f.sca = -ni->f.sca;
+            ni->b.sca = -ni->b.sca;
+        }
+        for (k = 0; k < S->nsubs; k++)
+            if (!strcmp(S->subs[k].name, o->sarg[0]))
+                sub = k;
+        if (sub < 0) {
+            gb_scene_host T;
+            char *path = o->sarg[0];
+            char *alt = NULL;
+            FILE *fp = fopen(path, "rb");
+            int32_t j;
+            if (fp)
+                fclose(fp);
+            else if (path[0] != '/' && base_dir) {
+                alt = (char *)malloc(strlen(base_dir) + strlen(path) + 2);
+                sprintf(alt, "%s/%s", base_dir, path);
+                path = alt;
+            }
+            gb_scene_init(&T);
+            if (gb_scene_read_oct(&T, path) < 0) {
+                char why[256];
+                snprintf(why, sizeof why, "%s", gb_scene_error());
+                free(alt);
+                gb_scene_clear(&T);
+                return fail("%s: cannot load octree \"%s\": %s", S->objs[i].name, S->objs[i].sarg[0], why);
+            }
+            free(alt);
+            for (j = 0; j < T.nobjs; j++)
+                if (gb_is_volume(T.objs[j].otype)) {
+                    gb_scene_clear(&T);
+                    return fail("%s: instances inside an instanced octree are not supported", S->objs[i].name);
+                }
+            sub = merge_subscene(S, &T, S->objs[i].sarg[0]);
+            gb_scene_clear(&T);
+            if (sub < 0)
+                return -1;
+        }
+        S->inst[S->ninst].sub = sub;
+        S->ninst++;
+    }
     return 0;
 }

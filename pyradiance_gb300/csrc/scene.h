@@ -75,6 +75,28 @@ typedef struct {
     int    ok;
 } gb_cone;
 
+/* common/xf.c XF: a 4x4 row-vector transform and its scale */
+typedef struct {
+    double xfm[4][4];
+    double sca;
+} gb_xf;
+
+/* an octree referenced by instances, merged into the scene's arrays
+ * (common/instance.c:23-60 getscene) */
+typedef struct {
+    char    *name;               /* the file name as the instance gives it */
+    double   cuorg[3], cusize;   /* its own cube */
+    int32_t  root;               /* its root code in the merged tree */
+    int32_t  firstobj, nobjs;    /* its objects in the merged object array */
+} gb_subscene;
+
+/* an instance object (common/instance.c:65-104 getinstance) */
+typedef struct {
+    int32_t  obj;                /* the instance object */
+    int32_t  sub;                /* its octree in subs[] */
+    gb_xf    f, b;               /* forward and backward transforms (common/xf.c fullxf) */
+} gb_instance;
+
 typedef struct {
     /* bounding cube */
     double   cuorg[3];
@@ -101,6 +123,12 @@ typedef struct {
     /* files named by an unfrozen octree */
     int       nfiles;
     char    **files;
+    /* instances: objects [0, nobjs_top) are the scene's own; the objects of
+     * the octrees its instances reference follow, loaded once per file */
+    int32_t   nobjs_top;
+    int32_t   ninst, nsubs;
+    gb_instance *inst;
+    gb_subscene *subs;
 } gb_scene_host;
 
 /* error text of the last failing call on this thread */
@@ -118,6 +146,17 @@ int gb_scene_read_oct(gb_scene_host *S, const char *path);
 /* Append the objects of a Radiance scene text file / buffer. */
 int gb_scene_read_rad_file(gb_scene_host *S, const char *path);
 int gb_scene_read_rad_text(gb_scene_host *S, const char *text, const char *what);
+
+/* Load the octrees of the scene's instance objects (common/instance.c:
+ * 65-104 getinstance: file name, then transform arguments, common/xf.c) and
+ * merge their objects, nodes and sets into the scene's arrays.  A relative
+ * file name is looked up in the working directory, then in base_dir.
+ * Instances inside instanced octrees are refused.  Returns 0 or -1. */
+int gb_scene_load_instances(gb_scene_host *S, const char *base_dir);
+
+/* common/xf.c fullxf: forward and inverse transform of ac arguments;
+ * returns the number of arguments used. */
+int gb_fullxf(gb_xf *f, gb_xf *b, int ac, char *const *av);
 
 /* Build the octree over the loaded objects with the reference's oconv
  * algorithm (ot/oconv.c:216-330): bounding cube from the surfaces' extent,

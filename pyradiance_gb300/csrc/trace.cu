@@ -27,6 +27,7 @@
  * roulette (rt/raytrace.c:39-135).  rcontrib's trace callback
  * (rt/rcontrib.c:272-316) is applied to every traced ray.
  */
+#include <type_traits>
 #include <cooperative_groups.h>
 #include <cooperative_groups/scan.h>
 #include "trace.cuh"
@@ -598,18 +599,19 @@ __device__ float3 shadow_chain(const gb_run &P, Ray sr, int s, Counters &cnt, fl
             light_hit(P, sr, src.so, src.mat, D_FHUGE, 1.f, cnt, &rc);
             return coef * T * rc;
         }
-        int ms = S.obj[h.obj].y;
+        const int ro = sid_object(S, h.obj);   /* h.obj: the surface id, the children's origin */
+        int ms = S.obj[ro].y;
         int mk = ms >= 0 ? (int)S.mat[2 * ms].x : DM_NONE;
-        if (h.obj == src.so && guard == 0 && !P.follow)
+        if (ro == src.so && guard == 0 && !P.follow)
             return potential;                 /* aimed and reached */
         float3 hp = sr.org + sr.dir * h.t;
         if (mk == DM_LIGHT || mk == DM_GLOW) {
             float3 rc;
-            light_hit(P, sr, h.obj, ms, h.t, h.rod, cnt, &rc);
+            light_hit(P, sr, ro, ms, h.t, h.rod, cnt, &rc);
             return coef * T * rc;
         }
         if (mk == DM_NONE) {
-            surface_contrib(P, sr, h.obj, cnt);
+            surface_contrib(P, sr, ro, cnt);
             Ray c;
             ray_origin(P, sr, GB_TRANS, f3(1.f, 1.f, 1.f), false, GB_C_PASS, c, nullptr);
             c.org = hp;
@@ -639,7 +641,7 @@ __device__ float3 shadow_chain(const gb_run &P, Ray sr, int s, Counters &cnt, fl
                 tc[i] = .5f * (1.f - r1e) * (1.f - r1e) * d / (1.f - r1e * r1e * d * d) +
                         .5f * (1.f - r1m) * (1.f - r1m) * d / (1.f - r1m * r1m * d * d);
             }
-            surface_contrib(P, sr, h.obj, cnt);
+            surface_contrib(P, sr, ro, cnt);
             Ray c;
             float3 tcv = f3(tc[0], tc[1], tc[2]);
             if (!ray_origin(P, sr, GB_TRANS, tcv, true, GB_C_TRANS, c, nullptr))
@@ -654,7 +656,7 @@ __device__ float3 shadow_chain(const gb_run &P, Ray sr, int s, Counters &cnt, fl
             continue;
         }
         /* opaque: blocked (rt/normal.c:190, m_normal's shadow test) */
-        surface_contrib(P, sr, h.obj, cnt);
+        surface_contrib(P, sr, ro, cnt);
         return zero;
     }
     return zero;
@@ -974,7 +976,8 @@ __device__ void shade_ray(const gb_run &P, const Ray &r, const Hit &h, Counters 
             light_hit<G>(P, r, S.src[sidx].so, S.src[sidx].mat, D_FHUGE, 1.f, cnt, nullptr);
         return;
     }
-    int ms = S.obj[h.obj].y;
+    const int ro = sid_object(S, h.obj);       /* h.obj: the surface id, the children's origin */
+    int ms = S.obj[ro].y;
     int mk = ms >= 0 ? (int)S.mat[2 * ms].x : DM_NONE;
     float3 hp = r.org + r.dir * h.t;
     /* -i (rt/raytrace.c:211-236 raytirrad): a primary ray, or one passed
@@ -989,11 +992,11 @@ __device__ void shade_ray(const gb_run &P, const Ray &r, const Hit &h, Counters 
             lamb = true;
     }
     if (mk == DM_LIGHT || mk == DM_GLOW) {
-        light_hit<G>(P, r, h.obj, ms, h.t, h.rod, cnt, nullptr);
+        light_hit<G>(P, r, ro, ms, h.t, h.rod, cnt, nullptr);
         return;
     }
     if (mk == DM_NONE) {
-        surface_contrib(P, r, h.obj, cnt);
+        surface_contrib(P, r, ro, cnt);
         Ray c;
         ray_origin(P, r, GB_TRANS, f3(1.f, 1.f, 1.f), false, GB_C_PASS, c, nullptr);
         c.org = hp;
@@ -1020,7 +1023,7 @@ __device__ void shade_ray(const gb_run &P, const Ray &r, const Hit &h, Counters 
         rod = -rod;
         n = -n;
     }
-    surface_contrib(P, r, h.obj, cnt);
+    surface_contrib(P, r, ro, cnt);
     if (mk == DM_GLASS) {
         float3 mc = f3(m0.y, m0.z, m0.w);
         float rindex = m1.x;
@@ -1070,7 +1073,7 @@ __device__ void shade_ray(const gb_run &P, const Ray &r, const Hit &h, Counters 
         return;
     }
     /* plastic / metal */
-    int okd = S.obj[h.obj].x & 0xff;
+    int okd = S.obj[ro].x & 0xff;
     Surf su;
     setup_surf(P, mk, m0, m1, n, rod, okd == DK_FACE || okd == DK_RING, su);
     if (su.refl && su.pure) {
@@ -1554,6 +1557,7 @@ struct ColumnStack {
     __device__ __forceinline__ int &operator[](int i) { return p[i * TRACE_BLOCK]; }
 };
 
+template <bool INST>
 __global__ void __launch_bounds__(TRACE_BLOCK, 4) k_trace(gb_run P)
 {
     __shared__ int stack_cols[(GRID_BITS + 1) * TRACE_BLOCK];
@@ -1565,6 +1569,10 @@ __global__ void __launch_bounds__(TRACE_BLOCK, 4) k_trace(gb_run P)
     if (total > (unsigned long long)P.qcap)
         total = P.qcap;
     Walk W;
+    /* scenes with instances defer the walks that meet one to k_trace_inst;
+     * the others carry no instance handling at all */
+    typedef typename std::conditional<INST, DeferCube, PlainCube>::type Cube;
+    const Cube C{};
     unsigned long long cur = 0;
     bool active = false, exhausted = false;
     for (;;) {
@@ -1584,7 +1592,7 @@ __global__ void __launch_bounds__(TRACE_BLOCK, 4) k_trace(gb_run P)
                     const float4 a = q[0], b = q[1], c = q[2];
                     cur = i;
                     cnt.rays++;
-                    active = walk_begin(P.S, f3(a.x, a.y, a.z), f3(b.x, b.y, b.z), __float_as_int(c.w), W,
+                    active = walk_begin(P.S, C, f3(a.x, a.y, a.z), f3(b.x, b.y, b.z), __float_as_int(c.w), W,
                                         stk);
                     if (!active)
                         store_hit(P.hits + i, W.best);     /* missed the scene cube */
@@ -1596,13 +1604,37 @@ __global__ void __launch_bounds__(TRACE_BLOCK, 4) k_trace(gb_run P)
                 break;
             continue;
         }
-        if (active && walk_iter(P.S, W, stk)) {
+        if (active && walk_iter(P.S, C, W, stk)) {
             uint32_t st[3] = {0, 0, 0};
             walk_tally(W, st);
             cnt.add(st);
-            store_hit(P.hits + cur, W.best);
+            if (INST && W.best.obj == HIT_DEFER)   /* met an instance: walked again there */
+                P.slow[atomicAdd(P.slow_count, 1ull)] = (uint32_t)cur;
+            else
+                store_hit(P.hits + cur, W.best);
             active = false;
         }
+    }
+    flush_counters(P, cnt);
+}
+
+/* The walks k_trace handed over because they met an instance: walked
+ * again from the start with the instances' octrees (hit_instance), one
+ * thread per ray.  Runs after k_trace in scenes with instances only. */
+__global__ void __launch_bounds__(128) k_trace_inst(gb_run P)
+{
+    Counters cnt = {0, 0, 0, 0, 0};
+    const unsigned long long n = *P.slow_count;
+    for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < n;
+         i += (unsigned long long)gridDim.x * blockDim.x) {
+        const unsigned long long q = P.slow[i];
+        const float4 *r = reinterpret_cast<const float4 *>(P.qin + q);
+        const float4 a = r[0], b = r[1], c = r[2];
+        Hit h;
+        uint32_t st[3] = {0, 0, 0};
+        local_hit(P.S, f3(a.x, a.y, a.z), f3(b.x, b.y, b.z), __float_as_int(c.w), h, st);
+        cnt.add(st);
+        store_hit(P.hits + q, h);
     }
     flush_counters(P, cnt);
 }
@@ -1646,7 +1678,7 @@ __global__ void k_cast(gb_run P, int *hit_obj, float *hit_t, float *hit_pn)
         float t = D_FHUGE;
         float3 n = f3(0.f, 0.f, 0.f);
         if (local_hit(P.S, org, dir, -1, h, st)) {
-            obj = h.obj;
+            obj = sid_object(P.S, h.obj);
             t = h.t;
             n = h.n;
         } else {
@@ -1778,11 +1810,24 @@ int gb_launch_primary_grad(const gb_run *P, cudaStream_t st, int sms)
 
 int gb_launch_trace(const gb_run *P, cudaStream_t st, int sms)
 {
-    static int grid = 0;
+    static int grid = 0, grid_inst = 0;
     if (!grid)
-        grid = resident_grid(k_trace, TRACE_BLOCK, sms);
-    k_trace<<<grid, TRACE_BLOCK, 0, st>>>(*P);
-    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+        grid = resident_grid(k_trace<false>, TRACE_BLOCK, sms);
+    if (P->S.ninst == 0) {
+        k_trace<false><<<grid, TRACE_BLOCK, 0, st>>>(*P);
+        return cudaGetLastError() == cudaSuccess ? 0 : -1;
+    }
+    if (!grid_inst)
+        grid_inst = resident_grid(k_trace<true>, TRACE_BLOCK, sms);
+    k_trace<true><<<grid_inst, TRACE_BLOCK, 0, st>>>(*P);
+    if (cudaGetLastError() != cudaSuccess)
+        return -1;
+    {
+        k_trace_inst<<<sms * 8, 128, 0, st>>>(*P);
+        if (cudaGetLastError() != cudaSuccess)
+            return -1;
+    }
+    return 0;
 }
 
 int gb_launch_shade(const gb_run *P, cudaStream_t st, int sms)

@@ -358,8 +358,23 @@ GB_DNI void hit_cone(const gb_dscene &S, int obj, int kind, int ci, float3 org,
     }
 }
 
+GB_DNI void hit_instance(const gb_dscene &S, int slot, float3 org, float3 dir, Hit &best, int skip);
+
+/* One object's test.  Instances (tested only from the scene's own octree:
+ * instances inside instanced octrees are refused when the scene loads) walk
+ * their octree in their own coordinates; skip is the surface id the ray
+ * leaves, passed on to that walk.  MODE: WALK_FULL tests instances,
+ * WALK_NESTED (inside an instance) has none to test, WALK_DEFER marks the
+ * walk for the instance-capable kernel instead (best.obj = HIT_DEFER at
+ * distance -1, which ends the walk at the end of the leaf), so that the
+ * bulk walk carries no nested walk. */
+#define WALK_FULL 0
+#define WALK_NESTED 1
+#define WALK_DEFER 2
+#define HIT_DEFER 0x7fffffff    /* with t = -1: every later test fails and the leaf ends the walk */
+template <int MODE = WALK_FULL>
 GB_DFN void hit_object(const gb_dscene &S, int obj, float3 org, float3 dir, Hit &best,
-                                           float tmin, bool self = false)
+                                           float tmin, bool self = false, int skip = -1)
 {
     /* the object record, plane and packed vertices depend on obj alone, so
      * all four loads are issued together */
@@ -389,6 +404,16 @@ GB_DFN void hit_object(const gb_dscene &S, int obj, float3 org, float3 dir, Hit 
         break;
     }
     default:
+        if (kind == DK_INSTANCE) {
+            if (MODE == WALK_FULL) {
+                Hit b = best;
+                hit_instance(S, od.w, org, dir, b, skip);
+                best = b;
+            } else if (MODE == WALK_DEFER) {
+                best.obj = HIT_DEFER;
+                best.t = -1.f;
+            }
+        }
         break;
     }
 }
@@ -431,29 +456,62 @@ struct WalkStack {
     GB_DFN int &operator[](int i) { return v[i]; }
 };
 
-GB_DFN float walk_rel(const gb_dscene &S, const Walk &W, int i)   /* origin - cube origin */
+/* The cube a walk runs through: the scene's, or the octree of an instance
+ * (in the instance's coordinates). */
+struct TopCube {                /* (holds nothing: the scene header is read in place) */
+    static constexpr int mode = WALK_FULL;
+    GB_DFN float org(const gb_dscene &S, int i) const { return S.cuorg[i]; }
+    GB_DFN float size(const gb_dscene &S) const { return S.cusize; }
+    GB_DFN float gscale(const gb_dscene &S) const { return S.grid_scale; }
+    GB_DFN float cell(const gb_dscene &S) const { return S.cell; }
+    GB_DFN int root(const gb_dscene &S) const { return S.root; }
+};
+
+/* the scene's cube, instances deferred */
+struct DeferCube : TopCube {
+    static constexpr int mode = WALK_DEFER;
+};
+
+/* the cube of a scene without instances: no instance handling compiled */
+struct PlainCube : TopCube {
+    static constexpr int mode = WALK_NESTED;
+};
+
+struct InstCube {
+    static constexpr int mode = WALK_NESTED;
+    float o[3], sz, gs, cl;
+    int rt;
+    GB_DFN float org(const gb_dscene &, int i) const { return o[i]; }
+    GB_DFN float size(const gb_dscene &) const { return sz; }
+    GB_DFN float gscale(const gb_dscene &) const { return gs; }
+    GB_DFN float cell(const gb_dscene &) const { return cl; }
+    GB_DFN int root(const gb_dscene &) const { return rt; }
+};
+
+template <typename Cube>
+GB_DFN float walk_rel(const gb_dscene &S, const Cube &C, const Walk &W, int i)   /* origin - cube origin */
 {
-    return comp(W.org, i) - S.cuorg[i];
+    return comp(W.org, i) - C.org(S, i);
 }
 
 /* Set up the walk of a ray; false when the ray misses the scene cube (no
  * hit, nothing to iterate). */
-template <typename Stack>
-GB_DFN bool walk_begin(const gb_dscene &S, float3 org, float3 dir, int skip, Walk &W, Stack &stk)
+template <typename Cube, typename Stack>
+GB_DFN bool walk_begin(const gb_dscene &S, const Cube &C, float3 org, float3 dir, int skip, Walk &W, Stack &stk)
 {
     W.best.obj = -1;
     W.best.t = D_FHUGE;
     W.best.rod = 1.f;
     W.best.n = f3(0.f, 0.f, 0.f);
     W.steps = W.nodes = W.tests = 0;
-    const float cs = S.cusize;
+    const float cs = C.size(S);
     /* Self-intersection: a ray leaving a planar surface cannot meet it
      * again, so that surface is skipped.  A curved origin surface is still
      * tested, since its far side is a legitimate hit, with the root at the
      * origin itself excluded (first_root). */
     W.skip = skip;
     W.curved_skip = false;
-    if (skip >= 0) {
+    if (skip >= 0 && skip < S.nobjs) {          /* (a surface inside an instance: tested there) */
         int kd = S.obj[skip].x & 0xff;
         W.curved_skip = kd != DK_FACE && kd != DK_RING;
     }
@@ -464,7 +522,7 @@ GB_DFN bool walk_begin(const gb_dscene &S, float3 org, float3 dir, int skip, Wal
     int anyd = 0;
 #pragma unroll
     for (int i = 0; i < 3; i++) {
-        rr[i] = walk_rel(S, W, i);
+        rr[i] = walk_rel(S, C, W, i);
         const bool pos = dd[i] > 1e-7f, neg = dd[i] < -1e-7f;
         W.inv[i] = (pos | neg) ? 1.f / dd[i] : 0.f;
         anyd |= pos | neg;
@@ -502,10 +560,10 @@ GB_DFN bool walk_begin(const gb_dscene &S, float3 org, float3 dir, int skip, Wal
     }
 #pragma unroll
     for (int i = 0; i < 3; i++) {
-        int v = GB_F2I_RD((rr[i] + dd[i] * t) * S.grid_scale);
+        int v = GB_F2I_RD((rr[i] + dd[i] * t) * C.gscale(S));
         W.q[i] = min(max(v, 0), GRID_N - 1);
     }
-    stk[0] = S.root;
+    stk[0] = C.root(S);
     W.rl = 0;
     W.k = 1;
     W.cnt = 0;
@@ -522,8 +580,8 @@ GB_DFN bool walk_begin(const gb_dscene &S, float3 org, float3 dir, int skip, Wal
  * shares with the last one, from the highest coordinate bit that changed).
  * Returns true when the walk has ended. */
 #define WALK_TESTS 3
-template <typename Stack>
-GB_DFN bool walk_iter(const gb_dscene &S, Walk &W, Stack &stk)
+template <typename Cube, typename Stack>
+GB_DFN bool walk_iter(const gb_dscene &S, const Cube &C, Walk &W, Stack &stk)
 {
     /* up to WALK_TESTS objects of this leaf per iteration, then, if the
      * leaf is done, the step to the next one in the same iteration: fewer
@@ -536,9 +594,9 @@ GB_DFN bool walk_iter(const gb_dscene &S, Walk &W, Stack &stk)
         const int o = GB_LDG(S.set_data + W.set + W.k);
         W.k++;
         if (o != W.skip)
-            hit_object(S, o, W.org, W.dir, W.best, D_FTINY);
+            hit_object<Cube::mode>(S, o, W.org, W.dir, W.best, D_FTINY, false, W.skip);
         else if (W.curved_skip)                  /* curved origin surface */
-            hit_object(S, o, W.org, W.dir, W.best, D_FTINY, true);
+            hit_object<Cube::mode>(S, o, W.org, W.dir, W.best, D_FTINY, true);
     }
     if (W.k <= W.cnt)
         return false;
@@ -561,7 +619,7 @@ GB_DFN bool walk_iter(const gb_dscene &S, Walk &W, Stack &stk)
             if (i == W.ax) {
                 W.q[i] = W.inv[i] > 0.f ? lo + W.span : lo - 1;
             } else {
-                int v = GB_F2I_RD((walk_rel(S, W, i) + dd[i] * W.texit) * S.grid_scale);
+                int v = GB_F2I_RD((walk_rel(S, C, W, i) + dd[i] * W.texit) * C.gscale(S));
                 W.q[i] = min(max(v, lo), lo + W.span - 1);
             }
         }
@@ -587,8 +645,8 @@ GB_DFN bool walk_iter(const gb_dscene &S, Walk &W, Stack &stk)
         if (W.inv[i] == 0.f)
             continue;
         const int lo = W.q[i] & mask;
-        float pl = (float)(W.inv[i] > 0.f ? lo + W.span : lo) * S.cell;
-        float dt = (pl - walk_rel(S, W, i)) * W.inv[i];
+        float pl = (float)(W.inv[i] > 0.f ? lo + W.span : lo) * C.cell(S);
+        float dt = (pl - walk_rel(S, C, W, i)) * W.inv[i];
         if (dt < W.texit) {
             W.texit = dt;
             W.ax = i;
@@ -606,6 +664,81 @@ GB_DFN bool walk_iter(const gb_dscene &S, Walk &W, Stack &stk)
         W.tests += W.cnt;
     }
     return false;
+}
+
+/* the walk in the scene's own cube */
+template <typename Stack>
+GB_DFN bool walk_begin(const gb_dscene &S, float3 org, float3 dir, int skip, Walk &W, Stack &stk)
+{
+    return walk_begin(S, TopCube{}, org, dir, skip, W, stk);
+}
+
+template <typename Stack>
+GB_DFN bool walk_iter(const gb_dscene &S, Walk &W, Stack &stk)
+{
+    return walk_iter(S, TopCube{}, W, stk);
+}
+
+/* rt/o_instance.c:15-71: the ray in the instance's coordinates (direction
+ * renormalised by the scale) walks the instance's octree; a hit closer than
+ * best is transformed back (distance and normal scaled by the forward
+ * transform's scale) and recorded with its surface id. */
+GB_DNI void hit_instance(const gb_dscene &S, int slot, float3 org, float3 dir, Hit &best, int skip)
+{
+    const gb_dinst &I = S.inst[slot];
+    const float *b = I.bx;
+    const float ib = 1.f / I.bsca;
+    const float3 o2 = f3(org.x * b[0] + org.y * b[3] + org.z * b[6] + b[9],
+                         org.x * b[1] + org.y * b[4] + org.z * b[7] + b[10],
+                         org.x * b[2] + org.y * b[5] + org.z * b[8] + b[11]);
+    const float3 d2 = f3((dir.x * b[0] + dir.y * b[3] + dir.z * b[6]) * ib,
+                         (dir.x * b[1] + dir.y * b[4] + dir.z * b[7]) * ib,
+                         (dir.x * b[2] + dir.y * b[5] + dir.z * b[8]) * ib);
+    const int local = skip >= I.sidbase && skip < I.sidbase + I.nobjs ? I.firstobj + (skip - I.sidbase) : -1;
+    InstCube C;
+    C.o[0] = I.cuorg[0];
+    C.o[1] = I.cuorg[1];
+    C.o[2] = I.cuorg[2];
+    C.sz = I.cusize;
+    C.gs = I.grid_scale;
+    C.cl = I.cell;
+    C.rt = I.root;
+    Walk W;
+    WalkStack stk;
+    if (walk_begin(S, C, o2, d2, local, W, stk))
+        while (!walk_iter(S, C, W, stk))
+            ;
+    if (W.best.obj < 0)
+        return;
+    const float t = W.best.t * I.fsca;
+    if (t >= best.t)
+        return;
+    const float *f = I.fx;
+    const float3 n = W.best.n, fi = f3(1.f, 1.f, 1.f) * (1.f / I.fsca);
+    best.obj = I.sidbase + (W.best.obj - I.firstobj);
+    best.t = t;
+    best.rod = W.best.rod;
+    best.n = f3((n.x * f[0] + n.y * f[3] + n.z * f[6]) * fi.x, (n.x * f[1] + n.y * f[4] + n.z * f[7]) * fi.y,
+                (n.x * f[2] + n.y * f[5] + n.z * f[8]) * fi.z);
+}
+
+/* the object Radiance reports for a surface id (r->ro): the object itself,
+ * or for a surface inside an instance the instance object when that has a
+ * modifier, else the instanced object */
+GB_DFN int sid_object(const gb_dscene &S, int sid)
+{
+    if (sid < S.nobjs || S.ninst == 0)
+        return sid;
+    int lo = 0, hi = S.ninst - 1;                 /* the last instance with sidbase <= sid */
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (S.inst[mid].sidbase <= sid)
+            lo = mid;
+        else
+            hi = mid - 1;
+    }
+    const gb_dinst &I = S.inst[lo];
+    return I.hasmod ? I.obj : I.firstobj + (sid - I.sidbase);
 }
 
 /* counters of a finished walk: cube visits, node descents, object tests */

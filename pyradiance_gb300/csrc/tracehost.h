@@ -116,6 +116,10 @@ typedef struct {
      * paths carry the index (sensor * root_n^2 + stratum) of the stratum
      * they descend from in queue-parallel tag arrays, their values add to
      * ss_val there; ss_cnt counts each stratum's extra samples */
+    /* scenes with instances: the queue indices whose walks met one, for
+     * k_trace_inst (zeroed count per generation) */
+    unsigned int *slow;
+    unsigned long long *slow_count;
     int   ss_samples;          /* -as */
     const uint32_t *tag_in;
     uint32_t *tag_out;

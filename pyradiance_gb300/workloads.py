@@ -23,6 +23,8 @@ Workloads (sizes are the defaults):
   ground of the reference's own test fixture (tests/Resources/skyglow.rad).
 * ``glossy_room`` -- the room with rough specular plastic and metal
   (the specular-lobe sampling workload).
+* ``furniture``, ``instance_room`` -- an object octree and a room holding
+  transformed instances of it (the instance workload).
 * ``sensor_grid`` -- cell-centred n x m grid at z = 0.8 facing +z.
 * ``dc_sky`` -- daylight-coefficient and sky matrices with the value
   distributions of the annual dctimestep workload.
@@ -197,6 +199,50 @@ def glossy_room(seed: int = 0, nboxes: int = 40, nspheres: int = 8) -> str:
     rad = rng.uniform(0.15, 0.4, size=nspheres)
     for i in range(nspheres):
         out.append(f"ball_mat sphere ball{i}\n0\n0\n4 {c[i, 0]:.9g} {c[i, 1]:.9g} {c[i, 2]:.9g} {rad[i]:.9g}\n\n")
+    out.append("void light light_mat\n0\n0\n3 100 100 100\n\n")
+    cx, cy = X / 2, Y / 2
+    out.append(_poly("light_mat", "light", [(cx - .5, cy - .5, Z - 0.01), (cx - .5, cy + .5, Z - 0.01),
+                                            (cx + .5, cy + .5, Z - 0.01), (cx + .5, cy - .5, Z - 0.01)]))
+    return "".join(out)
+
+
+def furniture(seed: int = 0) -> str:
+    """An object to instance, in its own coordinates around the origin: a
+    table (top and four legs as boxes), a sphere and a cylinder on it, a
+    cone beside it; plastic of three reflectances, one of them rough."""
+    rng = np.random.default_rng(seed)
+    rho = rng.uniform(0.3, 0.8, size=3)
+    out = [_mat_plastic("wood", (rho[0], rho[0] * 0.8, rho[0] * 0.6)),
+           f"void plastic paint\n0\n0\n5 {rho[1]:.9g} {rho[1]:.9g} {rho[1]:.9g} .04 .1\n\n",
+           _mat_plastic("steel", (rho[2],) * 3)]
+    out.append(_box("wood", "top", (-0.6, -0.4, 0.7), (1.2, 0.8, 0.05)))
+    for k, (x, y) in enumerate(((-0.55, -0.35), (0.5, -0.35), (-0.55, 0.3), (0.5, 0.3))):
+        out.append(_box("steel", f"leg{k}", (x, y, 0.0), (0.05, 0.05, 0.7)))
+    out.append("paint sphere ball\n0\n0\n4 0.2 0.1 0.95 0.2\n\n")
+    out.append("steel cylinder can\n0\n0\n7 -0.3 -0.1 0.75 -0.3 -0.1 1.05 0.08\n\n")
+    out.append("paint cone lamp\n0\n0\n8 0.9 0.0 0.0 0.9 0.0 0.6 0.25 0.02\n\n")
+    return "".join(out)
+
+
+def instance_room(sub_octree: str, seed: int = 0, n: int = 12) -> str:
+    """The room shell and ceiling light of ``daylight_room`` with ``n``
+    instances of the octree file ``sub_octree`` on the floor: rotated about
+    z, some scaled, one mirrored, every third one with its own material
+    (the instance's modifier replaces the instanced surfaces' own)."""
+    rng = np.random.default_rng(seed)
+    X, Y, Z = ROOM
+    out = [_mat_plastic("room_mat", (0.5, 0.5, 0.5)), _room_shell("room_mat"),
+           _mat_plastic("override", (0.7, 0.3, 0.2))]
+    for i in range(n):
+        x, y = rng.uniform((1.2, 1.2), (X - 1.2, Y - 1.2))
+        args = ["-rz", f"{rng.uniform(0, 360):.6g}"]
+        if i % 4 == 1:
+            args += ["-s", f"{rng.uniform(0.6, 1.4):.6g}"]
+        if i == 2:
+            args += ["-mx"]
+        args += ["-t", f"{x:.6g}", f"{y:.6g}", "0.002"]
+        mod = "override" if i % 3 == 0 else "void"
+        out.append(f"{mod} instance inst{i}\n{1 + len(args)} {sub_octree} {' '.join(args)}\n0\n0\n\n")
     out.append("void light light_mat\n0\n0\n3 100 100 100\n\n")
     cx, cy = X / 2, Y / 2
     out.append(_poly("light_mat", "light", [(cx - .5, cy - .5, Z - 0.01), (cx - .5, cy + .5, Z - 0.01),

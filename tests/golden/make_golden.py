@@ -179,6 +179,41 @@ def supersampled_irradiance(tmp: Path, n: int = 100, K: int = 512) -> None:
     print("supersampled: mean %.4g (as 512) vs %.4g (as 0)" % (out["as512_mean"].mean(), out["as0_mean"].mean()))
 
 
+def instances(tmp: Path) -> None:
+    """Instances (rt/o_instance.c, common/instance.c): the furniture octree
+    placed 12 times in the room, rotated, scaled, one mirrored, some with an
+    overriding material.  Both octrees (frozen, made by the reference oconv)
+    are kept as fixtures beside the vectors; the room octree names the
+    furniture octree by its file name.  Random interior rays: first-hit
+    surfaces and distances, deterministic -ab 0 radiance and -I
+    irradiance."""
+    (tmp / "inst_sub.rad").write_text(w.furniture())
+    (tmp / "inst_sub.oct").write_bytes(run(["oconv", "-f", "inst_sub.rad"], cwd=tmp))
+    (tmp / "inst_main.rad").write_text(w.instance_room("inst_sub.oct"))
+    (tmp / "inst_main.oct").write_bytes(run(["oconv", "-f", "inst_main.rad"], cwd=tmp))
+    rays = w.random_rays(4000, seed=11)
+    rng = np.random.default_rng(11)                # half of them aimed low, where the furniture stands
+    tgt = rng.uniform((0.5, 0.5, 0.0), (9.5, 7.5, 1.2), size=(2000, 3))
+    d = tgt - rays[:2000, :3]
+    rays[:2000, 3:] = d / np.linalg.norm(d, axis=1, keepdims=True)
+    inp = rays.astype("<f8").tobytes()
+    det = ["-dj", "0", "-ds", "0", "-dr", "0", "-dt", "0"]
+    hit = names(run(["rtrace", "-h", "-u-", "-ab", "0", "-fda", "-os", "inst_main.oct"], inp, cwd=tmp))
+    dist = np.frombuffer(run(["rtrace", "-h", "-u-", "-ab", "0", "-fdd", "-oL", "inst_main.oct"], inp, cwd=tmp),
+                         dtype="<f8")
+    val = np.frombuffer(run(["rtrace", "-h", "-u-", "-ab", "0", *det, "-fdd", "-ov", "inst_main.oct"], inp, cwd=tmp),
+                        dtype="<f8").reshape(-1, 3)
+    irr = np.frombuffer(run(["rtrace", "-h", "-u-", "-I", "-ab", "0", *det, "-fdd", "-ov", "inst_main.oct"], inp,
+                            cwd=tmp), dtype="<f8").reshape(-1, 3)
+    for f in ("inst_sub.oct", "inst_main.oct"):
+        (OUT / f).write_bytes((tmp / f).read_bytes())
+    np.savez_compressed(OUT / "instances.npz", rays=rays, hit_name=hit, hit_dist=dist, radiance=val,
+                        irradiance=irr, cmd="rtrace -h -u- -ab 0 -os | -oL | [-I] -dj 0 -ds 0 -dr 0 -dt 0 -ov")
+    print("instances: %d of %d rays hit instanced surfaces" % (
+        sum(not n.startswith(("floor", "ceiling", "north", "south", "east", "west", "light", "*")) for n in hit),
+        len(hit)))
+
+
 # bin groups of the 146 columns: ground, then the 8 Reinhart MF:1 altitude rows
 ROW_EDGES = [0, 1, 31, 61, 85, 109, 127, 139, 145, 146]
 
@@ -264,7 +299,7 @@ def main() -> None:
     if not (BIN / "rtrace").exists():
         sys.exit("reference programs missing: make -f oracle/build_ref.mk REF=/root/reference -j8")
     parts = {"octree": octree_digests, "c1": c1_direct, "c1p": c1_partitioned, "zoo": zoo, "glossy": glossy, "irr": surface_irradiance,
-             "ss": supersampled_irradiance,
+             "ss": supersampled_irradiance, "inst": instances,
              "dct": lambda tmp: dct_small(), "trace_oct": lambda tmp: ref_fixture_trace(),
              "c2ab1": lambda tmp: c2_stats(tmp, ab=1, K=256), "c2ab3": lambda tmp: c2_stats(tmp, ab=3, K=256)}
     only = sys.argv[1:] or list(parts)         # e.g. make_golden.py c1p

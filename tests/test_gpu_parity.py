@@ -291,6 +291,34 @@ def test_surface_irradiance_one_bounce(gb, scenes):
     assert np.abs(z).max() < 5 and abs(z.mean()) < 4 / np.sqrt(n)
 
 
+def test_instances(gb):
+    """Instanced octrees (rt/o_instance.c:15-71): the furniture octree 12
+    times in the room, rotated, scaled, mirrored, some with their own
+    material, read from the reference oconv's octrees.  The ray enters each
+    instance's coordinates in FP32, so hit names agree except where a ray
+    grazes an edge; distances, radiance and irradiance as for the shape
+    zoo."""
+    from pathlib import Path
+    g = golden("instances.npz")
+    sc = gb.Scene(str(Path(__file__).resolve().parent / "golden" / "inst_main.oct"))
+    rgb, hid, ht = rtrace_c(gb, sc, opts("rtrace", ab=0, dj=0, ds=0, dr=0, dt=0, u=0), g["rays"])
+    names = names_of(sc, hid)
+    match = names == g["hit_name"]
+    inst = np.array([not n.startswith(("floor", "ceiling", "north", "south", "east", "west", "light", "*"))
+                     for n in g["hit_name"]])
+    print("instances: %d of %d instanced hits named alike, %d of %d overall" %
+          ((match & inst).sum(), inst.sum(), match.sum(), len(match)))
+    assert match.mean() >= 0.998 and (match & inst).sum() >= 0.99 * inst.sum()
+    ok = match & (g["hit_dist"] < 1e9)
+    np.testing.assert_allclose(ht[ok], g["hit_dist"][ok], rtol=1e-4, atol=2e-6)
+    rel = np.abs(rgb - g["radiance"]).max(1) / np.maximum(np.abs(g["radiance"]).max(1), 1e-9)
+    assert (rel[match] <= 1e-4).mean() >= 0.99, np.sort(rel[match])[-5:]
+    o = opts("rtrace", I=1, ab=0, dj=0, ds=0, dr=0, dt=0, u=0)
+    irr, _, _ = rtrace_c(gb, sc, o, g["rays"])
+    rel = np.abs(irr - g["irradiance"]).max(1) / np.maximum(np.abs(g["irradiance"]).max(1), 1e-9)
+    assert (rel <= 1e-4).mean() >= 0.99, np.sort(rel)[-5:]
+
+
 def test_dctimestep_fp32_fp64(gb):
     g = golden("dct_small.npz")
     r64 = gb.dctimestep_array(g["dc"], g["sky"], mode="fp64")

@@ -134,6 +134,26 @@ def test_supersampled_first_hemisphere(oscenes, key, asn):
     assert np.abs(z).max() < 5 and abs(z.mean()) < 4 / np.sqrt(n), (np.abs(z).max(), z.mean())
 
 
+def test_instances():
+    """Instanced octrees (rt/o_instance.c:15-71, common/instance.c,
+    common/xf.c): the furniture octree 12 times in the room, rotated,
+    scaled, mirrored, some with their own material.  Hit surfaces by name
+    (the instance's when it has a modifier), distances, -ab 0 radiance and
+    -I irradiance."""
+    g = golden("instances.npz")
+    sc = po.Scene(Path(__file__).resolve().parent / "golden" / "inst_main.oct")
+    o = po.default_opts("rtrace", ab=0, dj=0, ds=0, dr=0, dt=0, u=0)
+    rgb, hid, ht, _ = po.rtrace(sc, o, g["rays"], threads=8)
+    names = np.array([sc.object_name(i) if i >= 0 else "*" for i in hid])
+    assert (names == g["hit_name"]).all(), np.nonzero(names != g["hit_name"])
+    hit = g["hit_dist"] < 1e9
+    np.testing.assert_allclose(ht[hit], g["hit_dist"][hit], rtol=1e-6, atol=1e-9)
+    np.testing.assert_allclose(rgb, g["radiance"], rtol=1e-6, atol=1e-9)
+    o.I = 1
+    irr, _, _, _ = po.rtrace(sc, o, g["rays"], hits=False, threads=8)
+    np.testing.assert_allclose(irr, g["irradiance"], rtol=1e-6, atol=1e-9)
+
+
 def test_zoo_cast_and_direct(oscenes):
     g = golden("zoo.npz")
     sc = oscenes["zoo"]
