@@ -62,7 +62,7 @@ int orc_compile_bins(const gb_modspec *mods, int nmods, gb_binins *prog, int pro
 /* ------------------------------------------------------------------ scene */
 
 typedef struct {
-    int flags;               /* DISTANT 1, SKIP 2, FLAT 4, PROX 8, FOLLOW 16 */
+    int flags;               /* DISTANT 1, SKIP 2, FLAT 4, PROX 8, FOLLOW 16, CIR 32 */
     double sloc[3], snorm[3], ss[3][3], ss2, srad, prox;
     int so;                  /* object */
     int mat;                 /* material object */
@@ -81,6 +81,7 @@ typedef struct {
 #define S_SKIP 2
 #define S_FLAT 4
 #define S_PROX 8
+#define S_CIR 32
 
 static void vcross(double r[3], const double a[3], const double b[3])
 {
@@ -196,7 +197,34 @@ static int mark_sources(oscene *O)
             perp0(s->ss[0], s->snorm);
             for (j = 0; j < 3; j++) s->ss[0][j] *= .5 * sqrt(s->ss2);
             vcross(s->ss[1], s->snorm, s->ss[0]);
-            s->flags = S_DISTANT;
+            s->flags = S_DISTANT | S_CIR;
+        } else if (o->otype == GT_SPHERE) {            /* rt/srcsupp.c:183-204 sphsetsrc */
+            int j;
+            if (o->nfargs != 4 || o->farg[3] <= FTINY) {
+                snprintf(O->err, sizeof O->err, "oracle: %s: illegal source radius", o->name);
+                return -1;
+            }
+            memcpy(s->sloc, o->farg, 3 * sizeof(double));
+            s->srad = o->farg[3];
+            s->ss2 = PI * s->srad * s->srad;
+            for (j = 0; j < 3; j++) s->ss[j][j] = 0.7236 * o->farg[3];
+            s->flags = S_CIR;
+        } else if (o->otype == GT_RING) {              /* rt/srcsupp.c:207-231 rsetsrc */
+            const gb_cone *c = &H->cones[i];
+            int j;
+            if (!c->ok || o->farg[c->r1] <= FTINY || o->farg[c->r0] > 0.0) {
+                snprintf(O->err, sizeof O->err, "oracle: %s: illegal ring source", o->name);
+                return -1;
+            }
+            memcpy(s->sloc, o->farg, 3 * sizeof(double));
+            memcpy(s->snorm, o->farg + 3, 3 * sizeof(double));
+            vnormalize(s->snorm);
+            s->srad = o->farg[c->r1];
+            s->ss2 = PI * s->srad * s->srad;
+            perp0(s->ss[0], s->snorm);                /* setflatss without the random rotation */
+            for (j = 0; j < 3; j++) s->ss[0][j] *= .5 * sqrt(s->ss2);
+            vcross(s->ss[1], s->snorm, s->ss[0]);
+            s->flags = S_FLAT | S_CIR;
         } else {
             snprintf(O->err, sizeof O->err, "oracle: source geometry %s not supported", gb_otype_name(o->otype));
             return -1;
@@ -1079,12 +1107,19 @@ static void direct(ctx *X, RAY *r, const NORMDAT *nd)
         }
         vpos[0] += parts[pi].ct[0] * (1.0 / MAXSPART);
         vpos[1] += parts[pi].ct[1] * (1.0 / MAXSPART);
-        if ((s->flags & S_DISTANT) && X->o->dj > 0.7) {   /* circular source trim */
-            double t0 = 1.12837917 * sqrt(1.0 - 0.5 * vpos[1] * vpos[1]);
-            double t1 = 1.12837917 * sqrt(1.0 - 0.5 * vpos[0] * vpos[0]);
-            vpos[0] *= t0;
-            vpos[1] *= t1;
-            vpos[2] = 0;
+        if ((s->flags & S_CIR) && (np > 1 || X->o->dj > 0.7)) {   /* rt/srcsamp.c:85-109 */
+            if (s->flags & (S_FLAT | S_DISTANT)) {
+                double t0 = 1.12837917 * sqrt(1.0 - 0.5 * vpos[1] * vpos[1]);
+                double t1 = 1.12837917 * sqrt(1.0 - 0.5 * vpos[0] * vpos[0]);
+                vpos[0] *= t0;
+                vpos[1] *= t1;
+                vpos[2] = 0;
+            } else {
+                double a = vpos[0] * vpos[0], b = vpos[1] * vpos[1], c = vpos[2] * vpos[2];
+                double sum = a + b + c, mx = fmax(a, fmax(b, c));
+                double t = sum > FTINY * FTINY ? (1.0 / 0.7236) * sqrt(mx / sum) : 0.0;
+                for (i = 0; i < 3; i++) vpos[i] *= t;
+            }
         }
         for (i = 0; i < 3; i++)
             dir[i] = s->sloc[i] + vpos[0] * s->ss[0][i] + vpos[1] * s->ss[1][i] + vpos[2] * s->ss[2][i];

@@ -294,7 +294,7 @@ static int mark_sources(gb_scene *G)
             sv[0] = d[1] * su[2] - d[2] * su[1];
             sv[1] = d[2] * su[0] - d[0] * su[2];
             sv[2] = d[0] * su[1] - d[1] * su[0];
-            s.flags = DS_DISTANT;
+            s.flags = DS_DISTANT | DS_CIR;
             for (int j = 0; j < 3; j++) {
                 s.sloc[j] = (float)d[j];
                 s.snorm[j] = (float)d[j];
@@ -303,6 +303,45 @@ static int mark_sources(gb_scene *G)
             }
             s.ss2 = (float)ss2;
             s.srad = (float)sqrt(ss2 / M_PI);
+        } else if (o->otype == GT_SPHERE) {          /* rt/srcsupp.c:183-204 sphsetsrc */
+            if (o->nfargs != 4)
+                return set_err(GB_EIO, "%s: bad # arguments", o->name);
+            if (o->farg[3] <= GB_FTINY)
+                return set_err(GB_EIO, "%s: illegal source radius", o->name);
+            s.flags = DS_CIR;
+            for (int j = 0; j < 3; j++) {
+                s.sloc[j] = (float)o->farg[j];
+                s.ss[j][j] = (float)(0.7236 * o->farg[3]);
+            }
+            s.srad = (float)o->farg[3];
+            s.ss2 = (float)(M_PI * o->farg[3] * o->farg[3]);
+        } else if (o->otype == GT_RING) {            /* rt/srcsupp.c:207-231 rsetsrc */
+            const gb_cone *c = &H.cones[i];
+            if (!c->ok)
+                return set_err(GB_EIO, "%s: illegal source", o->name);
+            const double r0 = o->farg[c->r0], r1 = o->farg[c->r1];
+            if (r1 <= GB_FTINY)
+                return set_err(GB_EIO, "%s: illegal source radius", o->name);
+            if (r0 > 0.0)
+                return set_err(GB_EIO, "%s: cannot hit source center", o->name);
+            double n[3] = {o->farg[3], o->farg[4], o->farg[5]};
+            double l = sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+            for (int j = 0; j < 3; j++) n[j] /= l;
+            double su[3], sv[3], ss2 = M_PI * r1 * r1;
+            perp(su, n);                             /* setflatss, without the random rotation */
+            for (int j = 0; j < 3; j++) su[j] *= .5 * sqrt(ss2);
+            sv[0] = n[1] * su[2] - n[2] * su[1];
+            sv[1] = n[2] * su[0] - n[0] * su[2];
+            sv[2] = n[0] * su[1] - n[1] * su[0];
+            s.flags = DS_FLAT | DS_CIR;
+            for (int j = 0; j < 3; j++) {
+                s.sloc[j] = (float)o->farg[j];
+                s.snorm[j] = (float)n[j];
+                s.ss[0][j] = (float)su[j];
+                s.ss[1][j] = (float)sv[j];
+            }
+            s.ss2 = (float)ss2;
+            s.srad = (float)r1;
         } else {
             if (G->src_error.empty())
                 G->src_error = std::string("light source geometry '") + gb_otype_name(o->otype) + "' (" +
@@ -876,13 +915,8 @@ static int check_shading(gb_scene *G, const gb_opts *o)
         return set_err(GB_EUNSUPPORTED, "-dv- is not implemented");
     if (o->ld != 0)
         return set_err(GB_EUNSUPPORTED, "-ld is not implemented");
-    if (o->ds > GB_FTINY) {                      /* partitions are built for flat local sources */
-        for (const gb_dsrc &s : G->src)
-            if (!(s.flags & (DS_SKIP | DS_DISTANT)) && !(s.flags & DS_FLAT))
-                return set_err(GB_EUNSUPPORTED,
-                               "source subdivision (-ds %g) of non-flat local sources is not implemented; use -ds 0",
-                               o->ds);
-    }
+    /* -ds: flat local sources are partitioned, spheres are one piece
+     * (rt/srcsupp.c:36 sphsobj nopart), as in the reference */
     /* rough specular sampled with several samples per hit (-ss > 1.5,
      * rt/normal.c:387-398): the reference weights their values, not their
      * ray coefficients, by the W-G-M-D adjustment, so rcontrib's bins (built

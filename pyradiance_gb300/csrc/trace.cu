@@ -671,7 +671,7 @@ __device__ float3 shadow_chain(const gb_run &P, Ray sr, int s, Counters &cnt, fl
 template <bool G>
 __device__ __noinline__ void direct_sample(const gb_run &P, const Ray &r, float3 hp, const Surf &s, int origin,
                                            Counters &cnt, int slot, int sn, int pi, int ct0, int ct1, int sz0,
-                                           int sz1)
+                                           int sz1, bool multi)
 {
     const gb_dscene &S = P.S;
     const gb_dsrc &src = S.src[sn];
@@ -686,14 +686,24 @@ __device__ __noinline__ void direct_sample(const gb_run &P, const Ray &r, float3
     }
     vpos[0] += (float)ct0 * (1.f / MAXSPART);
     vpos[1] += (float)ct1 * (1.f / MAXSPART);
-    if ((src.flags & DS_DISTANT) && P.dstrsrc > 0.7f) {
-        /* circular source trim (rt/srcsamp.c:85-96) */
-        float d = 1.12837917f;
-        float t0 = d * sqrtf(1.f - 0.5f * vpos[1] * vpos[1]);
-        float t1 = d * sqrtf(1.f - 0.5f * vpos[0] * vpos[0]);
-        vpos[0] *= t0;
-        vpos[1] *= t1;
-        vpos[2] = 0.f;
+    if ((src.flags & DS_CIR) && (multi || P.dstrsrc > 0.7f)) {
+        /* circular sources: samples pulled in from the square's corners
+         * (rt/srcsamp.c:85-109) */
+        if (src.flags & (DS_FLAT | DS_DISTANT)) {
+            const float d = 1.12837917f;
+            const float t0 = d * sqrtf(1.f - 0.5f * vpos[1] * vpos[1]);
+            const float t1 = d * sqrtf(1.f - 0.5f * vpos[0] * vpos[0]);
+            vpos[0] *= t0;
+            vpos[1] *= t1;
+            vpos[2] = 0.f;
+        } else {
+            const float a = vpos[0] * vpos[0], b = vpos[1] * vpos[1], c = vpos[2] * vpos[2];
+            const float sum = a + b + c, mx = fmaxf(a, fmaxf(b, c));
+            const float t = sum > D_FTINY * D_FTINY ? (1.f / 0.7236f) * sqrtf(mx / sum) : 0.f;
+            vpos[0] *= t;
+            vpos[1] *= t;
+            vpos[2] *= t;
+        }
     }
     float3 dir = sloc + f3(src.ss[0][0], src.ss[0][1], src.ss[0][2]) * vpos[0] +
                  f3(src.ss[1][0], src.ss[1][1], src.ss[1][2]) * vpos[1] +
@@ -795,7 +805,7 @@ __device__ void direct(const gb_run &P, const Ray &r, float3 hp, const Surf &s, 
                 continue;
         }
         if (P.srcsizerat <= D_FTINY || (src.flags & DS_DISTANT) || !(src.flags & DS_FLAT)) {
-            direct_sample<G>(P, r, hp, s, origin, cnt, slot, sn, 0, 0, 0, MAXSPART, MAXSPART);
+            direct_sample<G>(P, r, hp, s, origin, cnt, slot, sn, 0, 0, 0, MAXSPART, MAXSPART, false);
             continue;
         }
         const float3 snorm = f3(src.snorm[0], src.snorm[1], src.snorm[2]);
@@ -813,13 +823,15 @@ __device__ void direct(const gb_run &P, const Ray &r, float3 hp, const Surf &s, 
         } stack[8];
         int top = 0, pi = 0;
         stack[top++] = {sloc, su, sv, dv2 * dot3(su, su), dv2 * dot3(sv, sv), MAXSPART, 0, 0, MAXSPART, MAXSPART};
+        const float3 dc0 = hp - sloc;
+        const bool multi = !(dot3(dc0, dc0) >= stack[0].du2 && dot3(dc0, dc0) >= stack[0].dv2);   /* np > 1 */
         while (top > 0) {
             Piece f = stack[--top];
             for (;;) {
                 const float3 dc = hp - f.cent;
                 const float d2 = dot3(dc, dc);
                 if (f.mp < 2 || (d2 >= f.du2 && d2 >= f.dv2)) {
-                    direct_sample<G>(P, r, hp, s, origin, cnt, slot, sn, pi++, f.ct0, f.ct1, f.sz0, f.sz1);
+                    direct_sample<G>(P, r, hp, s, origin, cnt, slot, sn, pi++, f.ct0, f.ct1, f.sz0, f.sz1, multi);
                     break;
                 }
                 Piece lo = f, hi = f;

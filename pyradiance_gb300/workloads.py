@@ -23,6 +23,8 @@ Workloads (sizes are the defaults):
   ground of the reference's own test fixture (tests/Resources/skyglow.rad).
 * ``glossy_room`` -- the room with rough specular plastic and metal
   (the specular-lobe sampling workload).
+* ``lamp_room`` -- the room lit by a sphere and a disk light (circular
+  source shapes).
 * ``furniture``, ``instance_room`` -- an object octree and a room holding
   transformed instances of it (the instance workload).
 * ``sensor_grid`` -- cell-centred n x m grid at z = 0.8 facing +z.
@@ -203,6 +205,27 @@ def glossy_room(seed: int = 0, nboxes: int = 40, nspheres: int = 8) -> str:
     cx, cy = X / 2, Y / 2
     out.append(_poly("light_mat", "light", [(cx - .5, cy - .5, Z - 0.01), (cx - .5, cy + .5, Z - 0.01),
                                             (cx + .5, cy + .5, Z - 0.01), (cx + .5, cy - .5, Z - 0.01)]))
+    return "".join(out)
+
+
+def lamp_room(seed: int = 0, nboxes: int = 60) -> str:
+    """The room of ``daylight_room`` (fewer boxes) lit by a sphere light
+    (radius 0.15 m) and a disk light (ring of radius 0.3 m facing down)
+    instead of the polygon: the circular source shapes."""
+    rng = np.random.default_rng(seed)
+    X, Y, Z = ROOM
+    out = [_mat_plastic("room_mat", (0.5, 0.5, 0.5)), _room_shell("room_mat")]
+    sizes = rng.uniform(0.2, 1.2, size=(nboxes, 3))
+    pos = rng.uniform(0.0, 1.0, size=(nboxes, 2))
+    rho = rng.uniform(0.2, 0.7, size=nboxes)
+    for i in range(nboxes):
+        s = sizes[i]
+        out.append(_mat_plastic(f"box_mat{i}", (rho[i],) * 3))
+        out.append(_box(f"box_mat{i}", f"box{i}", (pos[i, 0] * (X - s[0]), pos[i, 1] * (Y - s[1]), 0.005), s))
+    out.append("void light bulb_mat\n0\n0\n3 200 180 160\n\n")
+    out.append(f"bulb_mat sphere bulb\n0\n0\n4 {X * 0.3:.9g} {Y * 0.5:.9g} {Z - 0.5:.9g} 0.15\n\n")
+    out.append("void light disk_mat\n0\n0\n3 80 80 90\n\n")
+    out.append(f"disk_mat ring disk\n0\n0\n8 {X * 0.7:.9g} {Y * 0.5:.9g} {Z - 0.01:.9g} 0 0 -1 0 0.3\n\n")
     return "".join(out)
 
 

@@ -179,6 +179,29 @@ def supersampled_irradiance(tmp: Path, n: int = 100, K: int = 512) -> None:
     print("supersampled: mean %.4g (as 512) vs %.4g (as 0)" % (out["as512_mean"].mean(), out["as0_mean"].mean()))
 
 
+def circular_sources(tmp: Path, K: int = 256) -> None:
+    """Sphere and disk lights (rt/srcsupp.c sphsetsrc, rsetsrc; the
+    circular trims of rt/srcsamp.c:85-109): -I direct irradiance on a grid
+    at 0.8 m and one at 2.3 m (close to the lights), deterministic with
+    -dj 0 -ds 0 and with -ds 0.2 (the disk split into pieces), and with
+    -dj 0.9 (jittered and trimmed samples) as per-sensor means and standard
+    errors of K replicas (-u+)."""
+    octp = oconv(w.lamp_room(), tmp, "lamp")
+    rays = np.vstack([w.sensor_grid(40, 40), w.sensor_grid(20, 20, z=2.3)])
+    inp = rays.astype("<f8").tobytes()
+    base = ["rtrace", "-h", "-u-", "-I", "-ab", "0", "-dr", "0", "-dt", "0", "-fdd", "-ov"]
+    ds0 = np.frombuffer(run([*base, "-dj", "0", "-ds", "0", octp], inp), dtype="<f8").reshape(-1, 3)
+    ds2 = np.frombuffer(run([*base, "-dj", "0", "-ds", "0.2", octp], inp), dtype="<f8").reshape(-1, 3)
+    sub = rays[::8]
+    a = np.frombuffer(run([*base[:2], "-u+", *base[3:], "-dj", "0.9", "-ds", "0.2", octp],
+                          np.repeat(sub, K, axis=0).astype("<f8").tobytes()), dtype="<f8").reshape(len(sub), K, 3)
+    np.savez_compressed(OUT / "circular_sources.npz", rays=rays, ds0=ds0, ds2=ds2, dj_rays=sub, K=K,
+                        dj_mean=a.mean(1), dj_se=a.std(1, ddof=1) / np.sqrt(K),
+                        cmd="rtrace -h -u- -I -ab 0 -dr 0 -dt 0 -dj 0 [-ds 0 | -ds 0.2] | -u+ -dj 0.9 -ds 0.2")
+    print("circular_sources: lit %.3f, ds0 mean %.4g, ds2 mean %.4g, dj mean %.4g" % (
+        (ds0[:, 0] > 0).mean(), ds0.mean(), ds2.mean(), a.mean()))
+
+
 def instances(tmp: Path) -> None:
     """Instances (rt/o_instance.c, common/instance.c): the furniture octree
     placed 12 times in the room, rotated, scaled, one mirrored, some with an
@@ -299,7 +322,7 @@ def main() -> None:
     if not (BIN / "rtrace").exists():
         sys.exit("reference programs missing: make -f oracle/build_ref.mk REF=/root/reference -j8")
     parts = {"octree": octree_digests, "c1": c1_direct, "c1p": c1_partitioned, "zoo": zoo, "glossy": glossy, "irr": surface_irradiance,
-             "ss": supersampled_irradiance, "inst": instances,
+             "ss": supersampled_irradiance, "inst": instances, "circ": circular_sources,
              "dct": lambda tmp: dct_small(), "trace_oct": lambda tmp: ref_fixture_trace(),
              "c2ab1": lambda tmp: c2_stats(tmp, ab=1, K=256), "c2ab3": lambda tmp: c2_stats(tmp, ab=3, K=256)}
     only = sys.argv[1:] or list(parts)         # e.g. make_golden.py c1p

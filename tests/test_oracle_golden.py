@@ -134,6 +134,28 @@ def test_supersampled_first_hemisphere(oscenes, key, asn):
     assert np.abs(z).max() < 5 and abs(z.mean()) < 4 / np.sqrt(n), (np.abs(z).max(), z.mean())
 
 
+def test_circular_sources(scene_dir, tmp_path):
+    """Sphere and disk lights: -I direct irradiance with -ds 0 and with the
+    disk partitioned (-ds 0.2, pieces trimmed to the circle), 1e-6; with
+    jittered samples (-dj 0.9) per-sensor means of 256 replicas within 5
+    standard errors of the reference's."""
+    from pyradiance_gb300 import workloads as w
+    g = golden("circular_sources.npz")
+    (tmp_path / "lamp.rad").write_text(w.lamp_room())
+    sc = po.Scene(tmp_path / "lamp.rad")
+    for key, ds in (("ds0", 0.0), ("ds2", 0.2)):
+        o = po.default_opts("rtrace", I=1, ab=0, dj=0, ds=ds, dr=0, dt=0, u=0)
+        rgb, _, _, _ = po.rtrace(sc, o, g["rays"], hits=False, threads=8)
+        np.testing.assert_allclose(rgb, g[key], rtol=1e-6, atol=1e-9, err_msg=key)
+    K, n = 256, len(g["dj_rays"])
+    o = po.default_opts("rtrace", I=1, ab=0, dj=0.9, ds=0.2, dr=0, dt=0, u=0)
+    rgb, _, _, _ = po.rtrace(sc, o, np.repeat(g["dj_rays"], K, axis=0), hits=False, threads=8)
+    a = rgb.reshape(n, K, 3)
+    m, se = a.mean(1), a.std(1, ddof=1) / np.sqrt(K)
+    z = (m - g["dj_mean"]) / np.sqrt(se ** 2 + g["dj_se"] ** 2 + (1e-6 * np.abs(g["dj_mean"]) + 1e-9) ** 2)
+    assert np.abs(z).max() < 5 and abs(z.mean()) < 4 / np.sqrt(n), (np.abs(z).max(), z.mean())
+
+
 def test_instances():
     """Instanced octrees (rt/o_instance.c:15-71, common/instance.c,
     common/xf.c): the furniture octree 12 times in the room, rotated,
