@@ -26,8 +26,8 @@
  *   m_light            rt/source.c:749-793
  *   direct             rt/source.c:398-556 (srcray :219, srcvalue :261,
  *                      nextssamp rt/srcsamp.c:37-145 single partition)
- *   m_normal/dirnorm   rt/normal.c:72-360
- *   gaussamp           rt/normal.c:364-440 (reflection)
+ *   m_normal/dirnorm   rt/normal.c:72-360 (plastic, metal, trans)
+ *   gaussamp           rt/normal.c:364-495
  *   m_glass            rt/glass.c:45-165
  *   multambient        rt/ambient.c:229-300 (-aa 0 branch)
  *   samp_hemi/ambsample rt/ambcomp.c:177-250, 351-421
@@ -850,6 +850,7 @@ static int sourcehit(const ctx *X, RAY *r)
 /* ------------------------------------------------------------- shading */
 
 static void raytrace(ctx *X, RAY *r);
+static int m_normal(ctx *X, int m, RAY *r);
 
 static void trace_contrib(ctx *X, const RAY *r)
 {
@@ -976,9 +977,10 @@ static int m_light(ctx *X, int m, RAY *r)
 }
 
 typedef struct {
-    double mcolor[3], scolor[3], pnorm[3];
+    double mcolor[3], scolor[3], pnorm[3], prdir[3];
     double rdiff, rspec, alpha2, pdot;
-    int pure, refl, rblt, flat;
+    double trans, tspec, tdiff;
+    int pure, refl, rblt, flat, tran, tblt;
 } NORMDAT;
 
 #define FRESNE(ci) (exp(-5.85 * (ci)) - 0.00202943064)
@@ -986,15 +988,32 @@ typedef struct {
 
 static void dirnorm(const ctx *X, double sc[3], const NORMDAT *np, const RAY *r, const double ldir[3], double omega)
 {
-    double ldot = vdot(np->pnorm, ldir), lrdiff, dtmp;
+    double ldot = vdot(np->pnorm, ldir), lrdiff, ltdiff, dtmp;
     int i;
     sc[0] = sc[1] = sc[2] = 0;
-    if (ldot < 0.0) return;
+    if (ldot < 0.0 ? np->trans <= FTINY : np->trans >= 1.0 - FTINY) return;    /* wrong side */
     lrdiff = np->rdiff;
-    if (np->pure && np->rspec >= FRESTHRESH && lrdiff > FTINY) lrdiff *= 1. - FRESNE(fabs(ldot));
+    ltdiff = np->tdiff;
+    if (np->pure && np->rspec >= FRESTHRESH && ((lrdiff > FTINY) | (ltdiff > FTINY))) {
+        dtmp = 1. - FRESNE(fabs(ldot));
+        lrdiff *= dtmp;
+        ltdiff *= dtmp;
+    }
     if ((ldot > FTINY) & (lrdiff > FTINY)) {
         dtmp = ldot * omega * lrdiff * (1.0 / PI);
         for (i = 0; i < 3; i++) sc[i] += np->mcolor[i] * dtmp;
+    }
+    if ((ldot < -FTINY) & (ltdiff > FTINY)) {                /* diffuse transmission */
+        dtmp = -ldot * omega * ltdiff * (1.0 / PI);
+        for (i = 0; i < 3; i++) sc[i] += np->mcolor[i] * dtmp;
+    }
+    if ((ldot < -FTINY) & np->tran & !np->pure) {            /* specular transmission */
+        dtmp = np->alpha2 + omega * (1.0 / PI);
+        dtmp = exp((2. * vdot(np->prdir, ldir) - 2.) / dtmp) / (PI * dtmp);
+        if (dtmp > FTINY) {
+            dtmp *= np->tspec * omega * sqrt(-ldot / np->pdot);
+            for (i = 0; i < 3; i++) sc[i] += np->mcolor[i] * dtmp;
+        }
     }
     if ((ldot > FTINY) & np->refl & !np->pure) {
         double vt[3], d2, d3, d4;
@@ -1194,7 +1213,8 @@ static void direct(ctx *X, RAY *r, const NORMDAT *nd)
                             for (i = 0; i < 3; i++) sr.rcol[i] += p.rcol[i] * p.rcoef[i];
                         }
                     }
-                }
+                } else if (t == GT_TRANS)
+                    m_normal(X, m, &sr);              /* its transmitted part (rt/normal.c:280-301) */
                 /* opaque materials: shadow stays black (rt/normal.c:189) */
             }
             trace_contrib(X, &sr);
@@ -1323,7 +1343,7 @@ static void multambient(ctx *X, double aval[3], RAY *r, const double nrm[3])
 {
     double d, wt, acoef[3], onrm[3], ux[3], uy[3], acol[3] = {0, 0, 0};
     double (*sv)[3] = NULL;
-    int n, i, j, k, ok = 0, ssroot = X->ssamp_root;
+    int n, i, j, k, ok = 0, ssroot = X->ssamp_root, back;
     X->ssamp_root = 0;
     if (X->o->ad <= 0 || r->adepth >= X->o->ab) goto dumbamb;
     d = maxc(aval);
@@ -1333,7 +1353,8 @@ static void multambient(ctx *X, double aval[3], RAY *r, const double nrm[3])
     if (wt > d) wt = d;
     n = (int)(sqrt(X->o->ad * wt) + 0.5);
     if (n < 1) n = 1;
-    memcpy(onrm, r->ron, sizeof onrm);
+    back = vdot(nrm, r->ron) < 0;                  /* rt/ambcomp.c:351-395 samp_hemi backside */
+    for (k = 0; k < 3; k++) onrm[k] = back ? -r->ron[k] : r->ron[k];
     for (k = 0; k < 3; k++) acoef[k] = aval[k] / (n * n);
     rand_perp(X, r, GB_G_FRAME, onrm, ux);
     vcross(uy, onrm, ux);
@@ -1352,7 +1373,7 @@ static void multambient(ctx *X, double aval[3], RAY *r, const double nrm[3])
             float fs[2];
             int kk = i * n + j;
             memset(&ar, 0, sizeof ar);
-            if (rayorigin(X, &ar, GB_RAMBIENT, r, acoef, GB_C_STRATUM(kk)) < 0) continue;
+            if (rayorigin(X, &ar, back ? GB_TAMBIENT : GB_RAMBIENT, r, acoef, GB_C_STRATUM(kk)) < 0) continue;
             ar.adepth = r->adepth + 1;
             draw(X, ar.path, ar.sensor, GB_G_CREATE, u, NULL);
             gb_place_sample(L, n, i, j, (float)u[1], (float)u[2], i + 1 < n ? (const float (*)[2])prev : NULL,
@@ -1422,14 +1443,18 @@ static double spec_trial(const ctx *X, const RAY *r, const NORMDAT *np, const do
  * ray's GB_G_SPEC groups instead of urand/frandom; sample k traces as child
  * GB_C_SPEC(k), all samples sharing the first one's rayorigin. */
 #define MAXITER 10
+static void gaussamp_trans(ctx *X, NORMDAT *np, RAY *r, const double u[3], const double v[3]);
+
 static void gaussamp(ctx *X, NORMDAT *np, RAY *r)
 {
     RAY sr;
     double u[3], v[3], scol[3] = {0, 0, 0}, d;
     int nstarget, nstaken, ntrials, maxiter, i;
-    if (!np->refl || np->rblt) return;
+    if ((!np->refl || np->rblt) && (!np->tran || np->tblt)) return;
     rand_perp(X, r, GB_G_SPECF, np->pnorm, u);
     vcross(v, np->pnorm, u);
+    if (np->tran && !np->tblt) gaussamp_trans(X, np, r, u, v);
+    if (!np->refl || np->rblt) return;
     if (rayorigin(X, &sr, GB_RSPECULAR, r, np->scolor, GB_C_SPEC(0)) != 0) return;
     nstarget = 1;
     if (X->o->ss > 1.5) {
@@ -1466,6 +1491,53 @@ static void gaussamp(ctx *X, NORMDAT *np, RAY *r)
     }
 }
 
+/* rt/normal.c:441-495, the transmitted part of gaussamp: samples about
+ * the transmitted direction, rejected at or above the surface, no W-G-M-D
+ * weighting; trials from GB_G_TSPEC, sample k traces as GB_C_TSPEC(k) */
+static void gaussamp_trans(ctx *X, NORMDAT *np, RAY *r, const double u[3], const double v[3])
+{
+    RAY sr;
+    double tc[3], q[4], rv0, rv1, d, cosp, sinp;
+    int nstarget = 1, nstaken, ntrials, maxiter, i, t;
+    for (i = 0; i < 3; i++) tc[i] = np->mcolor[i] * np->tspec;
+    if (rayorigin(X, &sr, GB_TSPECULAR, r, tc, GB_C_TSPEC(0)) != 0) return;
+    if (X->o->ss > 1.5) {
+        nstarget = (int)(X->o->ss * r->rweight + .5);
+        if (sr.rweight <= X->o->lw * nstarget) nstarget = (int)(sr.rweight / X->o->lw);
+        if (nstarget > 1) {
+            d = 1. / nstarget;
+            for (i = 0; i < 3; i++) sr.rcoef[i] *= d;
+            sr.rweight *= d;
+        } else
+            nstarget = 1;
+    }
+    maxiter = GB_SPEC_MAXITER * nstarget;
+    for (nstaken = ntrials = 0; nstaken < nstarget && ntrials < maxiter; ntrials++) {
+        t = ntrials;
+        draw(X, r->path, r->sensor, GB_G_TSPEC + (uint32_t)(t >> 1), q, NULL);
+        rv0 = q[(t & 1) * 2];
+        rv1 = q[(t & 1) * 2 + 1];
+        d = 2.0 * PI * rv0;
+        cosp = cos(d);
+        sinp = sin(d);
+        if ((0. <= X->o->ss) & (X->o->ss < 1.)) rv1 = 1.0 - X->o->ss * rv1;
+        d = rv1 <= FTINY ? 1.0 : sqrt(np->alpha2 * -log(rv1));
+        for (i = 0; i < 3; i++) sr.rdir[i] = np->prdir[i] + d * (cosp * u[i] + sinp * v[i]);
+        if (vdot(sr.rdir, r->ron) >= -FTINY) continue;
+        vnormalize(sr.rdir);
+        if (nstaken) {
+            double keep[3];
+            memcpy(keep, sr.rdir, sizeof keep);
+            rayclear(&sr);
+            sr.path = gb_child(r->path, GB_C_TSPEC(nstaken));
+            memcpy(sr.rdir, keep, sizeof keep);
+        }
+        raytrace(X, &sr);
+        for (i = 0; i < 3; i++) r->rcol[i] += sr.rcol[i] * sr.rcoef[i];
+        ++nstaken;
+    }
+}
+
 static int m_normal_obj(ctx *X, const gb_object *mo, RAY *r);
 
 static int m_normal(ctx *X, int m, RAY *r)
@@ -1482,8 +1554,8 @@ static int m_normal_obj(ctx *X, const gb_object *mo, RAY *r)
 {
     NORMDAT nd;
     double fest = 0, sct[3];
-    int i;
-    if (r->crtype & GB_SHADOW) return 1;
+    int i, istrans = mo->otype == GT_TRANS;
+    if ((r->crtype & GB_SHADOW) && !istrans) return 1;      /* trans: shadows pass the transmitted part */
     if (r->rod < 0.0) flipsurface(r);
     memcpy(nd.mcolor, mo->farg, sizeof nd.mcolor);
     nd.alpha2 = mo->farg[4] * mo->farg[4];
@@ -1496,7 +1568,30 @@ static int m_normal_obj(ctx *X, const gb_object *mo, RAY *r)
         fest = FRESNE(nd.pdot);
         nd.rspec += fest * (1. - nd.rspec);
     }
-    nd.rdiff = 1.0 - nd.rspec;
+    if (istrans) {                                  /* rt/normal.c:259-277 */
+        nd.trans = mo->farg[5] * (1.0 - nd.rspec);
+        nd.tspec = nd.trans * mo->farg[6];
+        nd.tdiff = nd.trans - nd.tspec;
+        nd.tran = nd.tspec > FTINY;
+        nd.tblt = nd.tran && !nd.pure && X->o->st >= nd.tspec - FTINY;
+        memcpy(nd.prdir, r->rdir, sizeof nd.prdir);
+    } else {
+        nd.trans = nd.tspec = nd.tdiff = 0;
+        nd.tran = nd.tblt = 0;
+    }
+    nd.rdiff = 1.0 - nd.trans - nd.rspec;
+    if (nd.tran && nd.pure) {                       /* the transmitted ray */
+        RAY lr;
+        double tc[3];
+        for (i = 0; i < 3; i++) tc[i] = nd.mcolor[i] * nd.tspec;
+        if (rayorigin(X, &lr, GB_TRANS, r, tc, GB_C_TRANS) == 0) {
+            memcpy(lr.rdir, nd.prdir, sizeof lr.rdir);
+            rayclear(&lr);
+            raytrace(X, &lr);
+            for (i = 0; i < 3; i++) r->rcol[i] += lr.rcol[i] * lr.rcoef[i];
+        }
+    }
+    if (r->crtype & GB_SHADOW) return 1;
     nd.refl = nd.rspec > FTINY;
     nd.rblt = 0;
     nd.scolor[0] = nd.scolor[1] = nd.scolor[2] = 0;
@@ -1519,11 +1614,20 @@ static int m_normal_obj(ctx *X, const gb_object *mo, RAY *r)
             for (i = 0; i < 3; i++) r->rcol[i] += lr.rcol[i] * lr.rcoef[i];
         }
     }
-    if (nd.pure && nd.rdiff <= FTINY) return 1;
+    if (nd.pure && nd.rdiff <= FTINY && nd.tdiff <= FTINY) return 1;
     if (!nd.pure) gaussamp(X, &nd, r);
     if (nd.rdiff > FTINY) {
         for (i = 0; i < 3; i++) sct[i] = nd.mcolor[i] * nd.rdiff + (nd.rblt ? nd.scolor[i] : 0);
         multambient(X, sct, r, nd.pnorm);
+        for (i = 0; i < 3; i++) r->rcol[i] += sct[i];
+    }
+    if (nd.tdiff > FTINY) {                         /* ambient from the other side */
+        double bnorm[3] = {-nd.pnorm[0], -nd.pnorm[1], -nd.pnorm[2]};
+        uint64_t path = r->path;
+        for (i = 0; i < 3; i++) sct[i] = nd.mcolor[i] * (nd.tblt ? nd.trans : nd.tdiff);
+        r->path = gb_child(path, GB_C_BACK);        /* its draws keyed apart from the front's */
+        multambient(X, sct, r, bnorm);
+        r->path = path;
         for (i = 0; i < 3; i++) r->rcol[i] += sct[i];
     }
     direct(X, r, &nd);
@@ -1592,7 +1696,7 @@ static void rayshade(ctx *X, RAY *r)
     }
     if (gb_is_light(t)) m_light(X, m, r);
     else if (t == GT_GLASS) m_glass(X, m, r);
-    else if (t == GT_PLASTIC || t == GT_METAL) m_normal(X, m, r);
+    else if (t == GT_PLASTIC || t == GT_METAL || t == GT_TRANS) m_normal(X, m, r);
     else raytrans(X, r);
 }
 

@@ -93,6 +93,7 @@ GB_HD uint32_t gb_irand(uint32_t x, uint32_t m) { return (uint32_t)(((uint64_t)x
 #define GB_G_SRC    2u
 #define GB_G_SPECF  0x7F000000u
 #define GB_G_SPEC   0x7F000001u
+#define GB_G_TSPEC  0x7D000000u   /* transmitted specular lobe trials, as GB_G_SPEC */
 #define GB_G_SSAMP  0x7E000000u   /* super-sampling allocation: stratum k uses word k&3 of group + (k >> 2) */
 
 GB_HD gb_u4 gb_draw(uint64_t path, uint32_t sensor, uint32_t group, uint32_t k0, uint32_t k1)
@@ -115,6 +116,8 @@ GB_HD uint64_t gb_child(uint64_t parent, uint32_t code)
 #define GB_C_TRANS      0x100002u
 #define GB_C_PASS       0x100003u                   /* continue through (raytrans) */
 #define GB_SPEC_MAXITER 10                            /* rt/normal.c:25 MAXITER */
+#define GB_C_TSPEC(k)   (0x120000u + (uint32_t)(k))   /* transmitted specular lobe sample k < 2^16 */
+#define GB_C_BACK       0x100004u                   /* the back side's hemisphere (its draws' parent) */
 #define GB_C_SSAMP(k, m) (0x400000u + (uint32_t)(k) + ((uint32_t)(m) << 12))  /* extra sample m >= 1 of stratum k < 4096 */
 #define GB_NOTAG 0xffffffffu
 #define GB_C_SPEC(k)    (0x110000u + (uint32_t)(k))   /* specular lobe sample k < 2^16 */

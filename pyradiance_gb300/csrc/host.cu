@@ -150,6 +150,11 @@ static int material_kind(const gb_object *m, float4 *m0, float4 *m1, std::string
         *m0 = make_float4(m->otype == GT_PLASTIC ? DM_PLASTIC : DM_METAL, f[0], f[1], f[2]);
         *m1 = make_float4(f[3], f[4], 0, 0);
         return 0;
+    case GT_TRANS:                               /* rt/normal.c: 7 arguments */
+        if (m->nfargs != 7) { why = "bad number of arguments"; return -1; }
+        *m0 = make_float4(DM_TRANS, f[0], f[1], f[2]);
+        *m1 = make_float4(f[3], f[4], f[5], f[6]);
+        return 0;
     case GT_GLASS:
         if (m->nfargs != 3 && m->nfargs != 4) { why = "bad arguments"; return -1; }
         *m0 = make_float4(DM_GLASS, f[0], f[1], f[2]);
@@ -927,7 +932,7 @@ static int check_shading(gb_scene *G, const gb_opts *o)
             float4 a = G->mat[2 * sl], b = G->mat[2 * sl + 1];
             int k = (int)a.x;
             double rspec = b.x;
-            if ((k == DM_PLASTIC || k == DM_METAL) && b.y * b.y > GB_FTINY && rspec > GB_FTINY &&
+            if ((k == DM_PLASTIC || k == DM_METAL || k == DM_TRANS) && b.y * b.y > GB_FTINY && rspec > GB_FTINY &&
                 !(o->st >= rspec - GB_FTINY))
                 return set_err(GB_EUNSUPPORTED,
                                "rcontrib with -ss %g samples the rough specular lobe of \"%s\" several times per "
@@ -1432,6 +1437,10 @@ extern "C" int gb_rtrace_grad(gb_scene *G, const gb_opts *o, const double *org_d
     if (nslots != (int64_t)G->matobj.size())
         return set_err(GB_EINVAL, "the gradient has %lld material slots, the scene %lld", (long long)nslots,
                        (long long)G->matobj.size());
+    for (size_t sl = 0; sl < G->matobj.size(); sl++)
+        if ((int)G->mat[2 * sl].x == DM_TRANS)
+            return set_err(GB_EUNSUPPORTED, "gradients through trans materials (\"%s\") are not implemented",
+                           G->H.objs[G->matobj[sl]].name);
     int rc = check_shading(G, o);
     if (rc < 0)
         return rc;

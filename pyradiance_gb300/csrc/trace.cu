@@ -423,7 +423,8 @@ struct Hemi {
     uint32_t atyp;
 };
 
-__device__ __forceinline__ bool make_hemi(const gb_run &P, const Ray &r, float3 aval, float3 ron, Hemi &h)
+__device__ __forceinline__ bool make_hemi(const gb_run &P, const Ray &r, float3 aval, float3 ron, Hemi &h,
+                                          bool back = false)
 {
     /* rt/ambcomp.c:351-421 (samp_hemi) for the ambacc <= FTINY case */
     float d = maxc(aval);
@@ -437,7 +438,7 @@ __device__ __forceinline__ bool make_hemi(const gb_run &P, const Ray &r, float3 
     if (n < 1)
         n = 1;
     h.n = n;
-    h.atyp = GB_RAMBIENT;
+    h.atyp = back ? GB_TAMBIENT : GB_RAMBIENT;   /* the back side: ron is its (flipped) normal */
     h.onrm = ron;
     h.acoef = aval * (1.f / (float)(n * n));
     gb_u4 u = gb_draw(r.path, r.sensor, GB_G_FRAME, P.k0, P.k1);
@@ -532,24 +533,37 @@ __device__ __noinline__ void spawn_hemi_big(const gb_run &P, const Ray &parent, 
 struct Surf {                 /* rt/normal.c NORMDAT */
     float3 mcolor, scolor, pnorm;
     float rdiff, rspec, alpha2, pdot;
-    bool pure, refl, rblt, flat;
+    float trans, tspec, tdiff;    /* trans material; 0 for plastic and metal */
+    bool pure, refl, rblt, flat, tran, tblt;
 };
 
-/* rt/normal.c:72-173 dirnorm (opaque materials: trans = 0) */
+/* rt/normal.c:72-173 dirnorm; the transmitted direction of a trans
+ * surface without texture is the ray's own (rdir) */
 __device__ __forceinline__ float3 dirnorm(const gb_run &P, const Surf &s, float3 rdir, float3 ldir, float omega,
                                           float3 *diffuse = nullptr)
 {
     float3 v = f3(0.f, 0.f, 0.f);
     float ldot = dot3(s.pnorm, ldir);
-    if (ldot < 0.f)
-        return v;
-    float lrdiff = s.rdiff;
-    if (s.pure && s.rspec >= FRESTHRESH && lrdiff > D_FTINY)
-        lrdiff *= 1.f - fresne(fabsf(ldot));
+    if (ldot < 0.f ? s.trans <= D_FTINY : s.trans >= 1.f - D_FTINY)
+        return v;                                /* wrong side */
+    float lrdiff = s.rdiff, ltdiff = s.tdiff;
+    if (s.pure && s.rspec >= FRESTHRESH && ((lrdiff > D_FTINY) | (ltdiff > D_FTINY))) {
+        const float f = 1.f - fresne(fabsf(ldot));
+        lrdiff *= f;
+        ltdiff *= f;
+    }
     if ((ldot > D_FTINY) & (lrdiff > D_FTINY))
         v = v + s.mcolor * (ldot * omega * lrdiff * (1.f / D_PI));
+    if ((ldot < -D_FTINY) & (ltdiff > D_FTINY))          /* diffuse transmission */
+        v = v + s.mcolor * (-ldot * omega * ltdiff * (1.f / D_PI));
     if (diffuse)
         *diffuse = v;
+    if ((ldot < -D_FTINY) & s.tran & !s.pure) {          /* specular transmission */
+        float dt = s.alpha2 + omega * (1.f / D_PI);
+        dt = expf((2.f * dot3(rdir, ldir) - 2.f) / dt) / (D_PI * dt);
+        if (dt > D_FTINY)
+            v = v + s.mcolor * (dt * s.tspec * omega * sqrtf(-ldot / s.pdot));
+    }
     if ((ldot > D_FTINY) & s.refl & !s.pure) {
         float dt = s.alpha2;
         if (s.flat)
@@ -655,8 +669,33 @@ __device__ float3 shadow_chain(const gb_run &P, Ray sr, int s, Counters &cnt, fl
             sr = c;
             continue;
         }
-        /* opaque: blocked (rt/normal.c:190, m_normal's shadow test) */
         surface_contrib(P, sr, ro, cnt);
+        if (mk == DM_TRANS) {
+            /* rt/normal.c:190-301 for a shadow ray: smooth trans passes its
+             * specular transmission on (a continuing TRANS ray) */
+            const float4 m0 = S.mat[2 * ms], m1 = S.mat[2 * ms + 1];
+            if (m1.y * m1.y <= D_FTINY) {
+                const float pdot = fmaxf(fabsf(h.rod), .001f);
+                float rspec = m1.x;
+                if (rspec >= FRESTHRESH)
+                    rspec += fresne(pdot) * (1.f - rspec);
+                const float tspec = m1.z * (1.f - rspec) * m1.w;
+                if (tspec > D_FTINY) {
+                    const float3 tcv = f3(m0.y, m0.z, m0.w) * tspec;
+                    Ray c;
+                    if (!ray_origin(P, sr, GB_TRANS, tcv, true, GB_C_TRANS, c, nullptr))
+                        return zero;
+                    c.org = hp;
+                    c.dir = sr.dir;
+                    c.origin = h.obj;
+                    T = T * tcv;
+                    sr = c;
+                    continue;
+                }
+            }
+        }
+        /* opaque (or rough trans): blocked (rt/normal.c:190, m_normal's
+         * shadow test) */
         return zero;
     }
     return zero;
@@ -877,7 +916,17 @@ __device__ __forceinline__ void setup_surf(const gb_run &P, int mk, float4 m0, f
         fest = fresne(s.pdot);
         s.rspec += fest * (1.f - s.rspec);
     }
-    s.rdiff = 1.f - s.rspec;
+    if (mk == DM_TRANS) {                        /* rt/normal.c:259-277 */
+        s.trans = m1.z * (1.f - s.rspec);
+        s.tspec = s.trans * m1.w;
+        s.tdiff = s.trans - s.tspec;
+        s.tran = s.tspec > D_FTINY;
+        s.tblt = s.tran && !s.pure && P.specthresh >= s.tspec - D_FTINY;
+    } else {
+        s.trans = s.tspec = s.tdiff = 0.f;
+        s.tran = s.tblt = false;
+    }
+    s.rdiff = 1.f - s.trans - s.rspec;
     s.refl = s.rspec > D_FTINY;
     if (s.refl) {
         if (mk != DM_METAL)
@@ -913,6 +962,55 @@ __device__ __forceinline__ float spec_trial(const gb_run &P, const Ray &r, const
     return dot3(sdir, su.pnorm);
 }
 
+/* rt/normal.c:441-495, the transmitted part of gaussamp: samples about
+ * the ray's own direction (no texture), rejected at or above the surface,
+ * without the W-G-M-D weighting; trials from GB_G_TSPEC, sample k is child
+ * GB_C_TSPEC(k), all sharing the first one's Russian roulette. */
+template <bool G>
+__device__ __forceinline__ void gaussamp_trans(const gb_run &P, const Ray &r, const Surf &su, float3 u, float3 v,
+                                               float3 hp, int obj)
+{
+    Ray c;
+    if (!ray_origin(P, r, GB_TSPECULAR, su.mcolor * su.tspec, true, GB_C_TSPEC(0), c, nullptr))
+        return;
+    int nst = 1;
+    if (P.specjitter > 1.5f) {
+        nst = (int)(P.specjitter * r.weight + .5f);
+        if (c.weight <= P.minweight * (float)nst)
+            nst = (int)(c.weight / P.minweight);
+        if (nst > 1) {
+            const float d = 1.f / (float)nst;
+            c.coef = c.coef * d;
+            c.weight *= d;
+        } else
+            nst = 1;
+    }
+    c.org = hp;
+    c.origin = obj;
+    if (G)
+        c.adj = r.adj;
+    const int maxiter = GB_SPEC_MAXITER * nst;
+    int taken = 0;
+    for (int t = 0; taken < nst && t < maxiter; t++) {
+        const gb_u4 q = gb_draw(r.path, r.sensor, GB_G_TSPEC + (uint32_t)(t >> 1), P.k0, P.k1);
+        const int w = (t & 1) * 2;
+        float rv0 = gb_u01(q.v[w]), rv1 = gb_u01(q.v[w + 1]);
+        float sinp, cosp;
+        sincosf(2.f * (float)M_PI * rv0, &sinp, &cosp);
+        if ((0.f <= P.specjitter) & (P.specjitter < 1.f))
+            rv1 = 1.f - P.specjitter * rv1;
+        const float d = rv1 <= D_FTINY ? 1.f : sqrtf(su.alpha2 * -logf(rv1));
+        const float3 sd = r.dir + (u * cosp + v * sinp) * d;
+        if (dot3(sd, su.pnorm) >= -D_FTINY)
+            continue;
+        c.dir = normalize3(sd);
+        if (taken)
+            c.path = gb_child(r.path, GB_C_TSPEC(taken));
+        push_ray<G>(P, c);
+        taken++;
+    }
+}
+
 /* rt/normal.c:364-440 gaussamp, reflection: sample the rough specular lobe
  * of a plastic or metal hit (specularity above -st).  One sample, or with
  * -ss above 1.5 ss times the ray weight of them, each weighted by the
@@ -927,6 +1025,10 @@ __device__ __noinline__ void gaussamp(const gb_run &P, const Ray &r, const Surf 
     const float3 u = perpendicular(su.pnorm, make_float4(gb_u01(uf.v[0]), gb_u01(uf.v[1]), gb_u01(uf.v[2]), 0.f),
                                    uf.v[3]);
     const float3 v = cross3(su.pnorm, u);
+    if (su.tran && !su.tblt)
+        gaussamp_trans<G>(P, r, su, u, v, hp, obj);
+    if (!su.refl || su.rblt)
+        return;
     Ray c;
     if (!ray_origin(P, r, GB_RSPECULAR, su.scolor, true, GB_C_SPEC(0), c, nullptr))
         return;
@@ -975,6 +1077,46 @@ __device__ __noinline__ void gaussamp(const gb_run &P, const Ray &r, const Surf 
     }
 }
 
+/* Ambient of one side of a surface (rt/ambient.c:229-300, -aa 0): the
+ * hemisphere about nrm (the back side's flipped normal, TAMBIENT rays), or
+ * the -av value beyond -ab bounces. */
+template <bool G>
+__device__ __forceinline__ void ambient_side(const gb_run &P, const Ray &r, float3 aval, float3 nrm, bool back,
+                                             float3 hp, int obj, int ms)
+{
+    if (P.ad > 0 && r.adepth < P.ab) {
+        Hemi hm;
+        if (make_hemi(P, r, aval, nrm, hm, back) && hm.n >= 4) {
+            spawn_hemi_big<G>(P, r, hm, hp, obj, ms);
+        } else if (hm.n > 0) {
+            int nn = hm.n * hm.n;
+            for (int k = 0; k < nn; k++) {
+                Ray c;
+                if (hemi_child(P, r, hm, hp, obj, k, nullptr, c)) {
+                    if (G) {
+                        c.adj = r.adj;
+                        adj_append(c.adj, ms, GB_ADJ_REFL, 0.f);
+                    }
+                    push_ray<G>(P, c);
+                }
+            }
+        }
+    } else if (P.av[0] != 0.f || P.av[1] != 0.f || P.av[2] != 0.f) {
+        add_value(P, r.sensor, r.tag, r.coef * aval * f3(P.av[0], P.av[1], P.av[2]));
+    }
+}
+
+/* the other side's ambient of a trans surface, out of line (rare): its
+ * draws are keyed by a child path of the ray, apart from the front's */
+template <bool G>
+__device__ __noinline__ void ambient_back(const gb_run &P, const Ray &r, float3 aval, float3 nrm, float3 hp,
+                                          int obj, int ms)
+{
+    Ray rb = r;
+    rb.path = gb_child(r.path, GB_C_BACK);
+    ambient_side<G>(P, rb, aval, nrm, true, hp, obj, ms);
+}
+
 /* Shade ray r given its trace result (h.obj < 0: the ray left the scene)
  * and push every child ray to the next generation's queue
  * (rt/raytrace.c:163-256 raytrace / rayshade, the material routines). */
@@ -998,7 +1140,7 @@ __device__ void shade_ray(const gb_run &P, const Ray &r, const Hit &h, Counters 
      * whose radiance is the irradiance there */
     bool lamb = false;
     if (P.do_irrad && !(r.crtype & ~(GB_PRIMARY | GB_TRANS))) {
-        if (mk == DM_GLASS)
+        if (mk == DM_GLASS || mk == DM_TRANS)
             mk = DM_NONE;
         else if (mk != DM_LIGHT && mk != DM_GLOW && mk != DM_NONE)
             lamb = true;
@@ -1088,6 +1230,17 @@ __device__ void shade_ray(const gb_run &P, const Ray &r, const Hit &h, Counters 
     int okd = S.obj[ro].x & 0xff;
     Surf su;
     setup_surf(P, mk, m0, m1, n, rod, okd == DK_FACE || okd == DK_RING, su);
+    if (su.tran && su.pure) {                    /* the transmitted ray (rt/normal.c:280-301) */
+        Ray c;
+        if (ray_origin(P, r, GB_TRANS, su.mcolor * su.tspec, true, GB_C_TRANS, c, nullptr)) {
+            c.org = hp;
+            c.dir = r.dir;
+            c.origin = h.obj;
+            if (G)
+                c.adj = r.adj;
+            push_ray<G>(P, c);
+        }
+    }
     if (su.refl && su.pure) {
         Ray c;
         if (ray_origin(P, r, GB_REFLECTED, su.scolor, true, GB_C_REFL, c, nullptr)) {
@@ -1099,39 +1252,22 @@ __device__ void shade_ray(const gb_run &P, const Ray &r, const Hit &h, Counters 
             push_ray<G>(P, c);
         }
     }
-    if (su.pure && su.rdiff <= D_FTINY)
+    if (su.pure && su.rdiff <= D_FTINY && su.tdiff <= D_FTINY)
         return;
     if (su.rdiff > D_FTINY) {
         float3 aval = su.mcolor * su.rdiff;
         if (su.rblt)
             aval = aval + su.scolor;
-        if (P.ad > 0 && r.adepth < P.ab) {
-            Hemi hm;
-            if (make_hemi(P, r, aval, n, hm) && hm.n >= 4) {
-                spawn_hemi_big<G>(P, r, hm, hp, h.obj, ms);
-            } else if (hm.n > 0) {
-                int nn = hm.n * hm.n;
-                for (int k = 0; k < nn; k++) {
-                    Ray c;
-                    if (hemi_child(P, r, hm, hp, h.obj, k, nullptr, c)) {
-                        if (G) {
-                            c.adj = r.adj;
-                            adj_append(c.adj, ms, GB_ADJ_REFL, 0.f);
-                        }
-                        push_ray<G>(P, c);
-                    }
-                }
-            }
-        } else if (P.av[0] != 0.f || P.av[1] != 0.f || P.av[2] != 0.f) {
-            add_value(P, r.sensor, r.tag, r.coef * aval * f3(P.av[0], P.av[1], P.av[2]));
-        }
+        ambient_side<G>(P, r, aval, n, false, hp, h.obj, ms);
     }
+    if (su.tdiff > D_FTINY)                      /* ambient from the other side (trans) */
+        ambient_back<G>(P, r, su.mcolor * (su.tblt ? su.trans : su.tdiff), -n, hp, h.obj, ms);
     if (S.nsrc > 0)
         direct<G>(P, r, hp, su, h.obj, cnt, ms);
-    /* the rough specular lobe (the reference samples it before the diffuse
-     * terms; every draw is keyed by the path, so the order is free, and
-     * last keeps the fewest values live across the call) */
-    if (su.refl && !su.pure && !su.rblt)
+    /* the rough specular lobes (the reference samples them before the
+     * diffuse terms; every draw is keyed by the path, so the order is free,
+     * and last keeps the fewest values live across the call) */
+    if (!su.pure && ((su.refl && !su.rblt) || (su.tran && !su.tblt)))
         gaussamp<G>(P, r, su, rod, hp, h.obj);
 }
 
@@ -1218,6 +1354,8 @@ __global__ void k_root(gb_run P)
         su.refl = false;
         su.rblt = false;
         su.flat = false;
+        su.trans = su.tspec = su.tdiff = 0.f;
+        su.tran = su.tblt = false;
         if (P.S.nsrc > 0)
             direct<G>(P, r, hp, su, -1, cnt, -1);
         if (P.root_n > 0) {

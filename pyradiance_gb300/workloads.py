@@ -25,6 +25,7 @@ Workloads (sizes are the defaults):
   (the specular-lobe sampling workload).
 * ``lamp_room`` -- the room lit by a sphere and a disk light (circular
   source shapes).
+* ``trans_room`` -- the room with translucent diffuser and frosted panels.
 * ``furniture``, ``instance_room`` -- an object octree and a room holding
   transformed instances of it (the instance workload).
 * ``sensor_grid`` -- cell-centred n x m grid at z = 0.8 facing +z.
@@ -203,6 +204,39 @@ def glossy_room(seed: int = 0, nboxes: int = 40, nspheres: int = 8) -> str:
         out.append(f"ball_mat sphere ball{i}\n0\n0\n4 {c[i, 0]:.9g} {c[i, 1]:.9g} {c[i, 2]:.9g} {rad[i]:.9g}\n\n")
     out.append("void light light_mat\n0\n0\n3 100 100 100\n\n")
     cx, cy = X / 2, Y / 2
+    out.append(_poly("light_mat", "light", [(cx - .5, cy - .5, Z - 0.01), (cx - .5, cy + .5, Z - 0.01),
+                                            (cx + .5, cy + .5, Z - 0.01), (cx + .5, cy - .5, Z - 0.01)]))
+    return "".join(out)
+
+
+def trans_room(seed: int = 0, nboxes: int = 30) -> str:
+    """The room with translucent (``trans``) surfaces: a smooth diffuser
+    sheet under the ceiling light (transmissivity 0.6, a fifth of it
+    specular), a few rough frosted panels standing in the room, and
+    plastic boxes; the ceiling light of ``daylight_room``."""
+    rng = np.random.default_rng(seed)
+    X, Y, Z = ROOM
+    out = [_mat_plastic("room_mat", (0.5, 0.5, 0.5)), _room_shell("room_mat"),
+           "void trans diffuser\n0\n0\n7 .8 .8 .8 0 0 .6 .2\n\n",
+           "void trans frosted\n0\n0\n7 .7 .75 .8 .05 .1 .5 .4\n\n"]
+    cx, cy = X / 2, Y / 2
+    out.append(_poly("diffuser", "sheet", [(cx - 2, cy - 1.5, 2.2), (cx + 2, cy - 1.5, 2.2),
+                                           (cx + 2, cy + 1.5, 2.2), (cx - 2, cy + 1.5, 2.2)]))
+    for i in range(4):
+        x0 = rng.uniform(1, X - 3)
+        y0 = rng.uniform(1, Y - 1)
+        ang = rng.uniform(0, np.pi)
+        dx, dy = 1.5 * np.cos(ang), 1.5 * np.sin(ang)
+        out.append(_poly("frosted", f"panel{i}", [(x0, y0, 0.1), (x0 + dx, y0 + dy, 0.1),
+                                                  (x0 + dx, y0 + dy, 1.9), (x0, y0, 1.9)]))
+    sizes = rng.uniform(0.2, 0.8, size=(nboxes, 3))
+    pos = rng.uniform(0.0, 1.0, size=(nboxes, 2))
+    rho = rng.uniform(0.2, 0.7, size=nboxes)
+    for i in range(nboxes):
+        sz = sizes[i]
+        out.append(_mat_plastic(f"box_mat{i}", (rho[i],) * 3))
+        out.append(_box(f"box_mat{i}", f"box{i}", (pos[i, 0] * (X - sz[0]), pos[i, 1] * (Y - sz[1]), 0.005), sz))
+    out.append("void light light_mat\n0\n0\n3 100 100 100\n\n")
     out.append(_poly("light_mat", "light", [(cx - .5, cy - .5, Z - 0.01), (cx - .5, cy + .5, Z - 0.01),
                                             (cx + .5, cy + .5, Z - 0.01), (cx + .5, cy - .5, Z - 0.01)]))
     return "".join(out)

@@ -179,6 +179,39 @@ def supersampled_irradiance(tmp: Path, n: int = 100, K: int = 512) -> None:
     print("supersampled: mean %.4g (as 512) vs %.4g (as 0)" % (out["as512_mean"].mean(), out["as0_mean"].mean()))
 
 
+def translucent(tmp: Path, K: int = 256) -> None:
+    """The trans material (rt/normal.c, MAT_TRANS): -I irradiance on a grid
+    at 0.8 m (the light seen through the diffuser: shadow rays pass its
+    specular transmission) and radiance of random view rays, deterministic
+    with -ab 0 -st 1 (no lobe sampling); and radiance of view rays aimed at
+    the translucent surfaces with -ab 1 -aa 0 -as 0 -st 0 (ambient from both
+    sides, transmitted and reflected lobes sampled) as per-ray means and
+    standard errors of K replicas (-u+)."""
+    octp = oconv(w.trans_room(), tmp, "trans")
+    grid = w.sensor_grid(40, 40)
+    view = w.random_rays(1000, seed=13)
+    base = ["rtrace", "-h", "-u-", "-ab", "0", "-dj", "0", "-ds", "0", "-dr", "0", "-dt", "0", "-st", "1", "-fdd", "-ov"]
+    irr = np.frombuffer(run([*base[:2], *base[2:3], "-I", *base[3:], octp], grid.astype("<f8").tobytes()),
+                        dtype="<f8").reshape(-1, 3)
+    rad = np.frombuffer(run([*base, octp], view.astype("<f8").tobytes()), dtype="<f8").reshape(-1, 3)
+    rng = np.random.default_rng(13)
+    org = rng.uniform((0.5, 0.5, 0.3), (9.5, 7.5, 2.0), size=(60, 3))
+    X, Y = 10.0, 8.0
+    tgt = np.column_stack([rng.uniform(X / 2 - 1.8, X / 2 + 1.8, 60), rng.uniform(Y / 2 - 1.3, Y / 2 + 1.3, 60),
+                           np.full(60, 2.2)])
+    tgt[30:] = rng.uniform((1, 1, 0.3), (9, 7, 1.7), size=(30, 3))       # towards the panels' region
+    d = tgt - org
+    aimed = np.hstack([org, d / np.linalg.norm(d, axis=1, keepdims=True)])
+    a = np.frombuffer(run(["rtrace", "-h", "-u+", "-ab", "1", "-aa", "0", "-as", "0", "-ad", "256", "-lw", "1e-4",
+                           "-dj", "0", "-ds", "0", "-dr", "0", "-dt", "0", "-st", "0", "-fdd", "-ov", octp],
+                          np.repeat(aimed, K, axis=0).astype("<f8").tobytes()), dtype="<f8").reshape(60, K, 3)
+    np.savez_compressed(OUT / "translucent.npz", grid=grid, irradiance=irr, view=view, radiance=rad, aimed=aimed,
+                        K=K, ab1_mean=a.mean(1), ab1_se=a.std(1, ddof=1) / np.sqrt(K),
+                        cmd="rtrace -h -u- -ab 0 -dj 0 -ds 0 -dr 0 -dt 0 -st 1 [-I] | -u+ -ab 1 -aa 0 -as 0 -ad 256 "
+                            "-lw 1e-4 -st 0")
+    print("translucent: irradiance mean %.4g, radiance mean %.4g, ab1 mean %.4g" % (irr.mean(), rad.mean(), a.mean()))
+
+
 def circular_sources(tmp: Path, K: int = 256) -> None:
     """Sphere and disk lights (rt/srcsupp.c sphsetsrc, rsetsrc; the
     circular trims of rt/srcsamp.c:85-109): -I direct irradiance on a grid
@@ -323,6 +356,7 @@ def main() -> None:
         sys.exit("reference programs missing: make -f oracle/build_ref.mk REF=/root/reference -j8")
     parts = {"octree": octree_digests, "c1": c1_direct, "c1p": c1_partitioned, "zoo": zoo, "glossy": glossy, "irr": surface_irradiance,
              "ss": supersampled_irradiance, "inst": instances, "circ": circular_sources,
+             "trans": translucent,
              "dct": lambda tmp: dct_small(), "trace_oct": lambda tmp: ref_fixture_trace(),
              "c2ab1": lambda tmp: c2_stats(tmp, ab=1, K=256), "c2ab3": lambda tmp: c2_stats(tmp, ab=3, K=256)}
     only = sys.argv[1:] or list(parts)         # e.g. make_golden.py c1p

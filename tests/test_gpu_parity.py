@@ -291,6 +291,42 @@ def test_surface_irradiance_one_bounce(gb, scenes):
     assert np.abs(z).max() < 5 and abs(z.mean()) < 4 / np.sqrt(n)
 
 
+def test_translucent(gb, tmp_path, scene_dir):
+    """The trans material (rt/normal.c, MAT_TRANS): -I irradiance through
+    the diffuser (shadow rays continue through its specular transmission)
+    and radiance of view rays with -ab 0 -st 1 against the reference
+    (99% within 1e-4: view rays through the diffuser continue as
+    transmitted rays); aimed view rays with -ab 1 -st 0 (ambient from both
+    sides, both lobes sampled) ray for ray against the oracle on the same
+    streams, and means of 256 replicas within 5 standard errors of the
+    reference's."""
+    from oracle import pyoracle as po
+    from pyradiance_gb300 import workloads as w
+    g = golden("translucent.npz")
+    (tmp_path / "trans.rad").write_text(w.trans_room())
+    sc = gb.Scene(rad_files=[tmp_path / "trans.rad"])
+    for key, rays, I in (("irradiance", g["grid"], 1), ("radiance", g["view"], 0)):
+        rgb, _, _ = rtrace_c(gb, sc, opts("rtrace", I=I, ab=0, dj=0, ds=0, dr=0, dt=0, st=1, u=0), rays)
+        rel = np.abs(rgb - g[key]).max(1) / np.maximum(np.abs(g[key]).max(1), 1e-9)
+        assert (rel <= 1e-4).mean() >= 0.99 and np.median(rel) < 1e-5, (key, np.sort(rel)[-5:])
+    kw = dict(ab=1, aa=0, as_=0, ad=256, lw=1e-4, dj=0, ds=0, dr=0, dt=0, st=0, u=0)
+    rays = np.repeat(g["aimed"], 4, axis=0)
+    rgb, _, _ = rtrace_c(gb, sc, opts("rtrace", seed=5, **kw), rays)
+    oo = po.default_opts("rtrace", seed=5, **{k: v for k, v in kw.items() if k != "as_"})
+    oo.as_ = 0
+    ref, _, _, _ = po.rtrace(po.Scene(tmp_path / "trans.rad"), oo, rays, hits=False, threads=16)
+    rel = np.abs(rgb - ref).max(1) / np.maximum(np.abs(ref).max(1), 1e-9)
+    print("trans vs oracle: median rel %.3g, share above 1e-3 %.3f" % (np.median(rel), (rel > 1e-3).mean()))
+    assert np.median(rel) < 1e-4 and (rel <= 1e-3).mean() >= 0.95
+    n, K = len(g["aimed"]), 256
+    rgb, _, _ = rtrace_c(gb, sc, opts("rtrace", seed=6, **kw), np.repeat(g["aimed"], K, axis=0))
+    a = rgb.reshape(n, K, 3)
+    m, se = a.mean(1), a.std(1, ddof=1) / np.sqrt(K)
+    z = (m - g["ab1_mean"]) / np.sqrt(se ** 2 + g["ab1_se"] ** 2 + (1e-5 * np.abs(g["ab1_mean"]) + 1e-9) ** 2)
+    print("trans -ab 1: max |z| %.2f, mean z %.3f" % (np.abs(z).max(), z.mean()))
+    assert np.abs(z).max() < 5 and abs(z.mean()) < 4 / np.sqrt(n)
+
+
 def test_circular_sources(gb, tmp_path):
     """Sphere and disk lights (rt/srcsupp.c sphsetsrc, rsetsrc): -I direct
     irradiance with -ds 0 and with the disk partitioned (-ds 0.2, pieces

@@ -134,6 +134,31 @@ def test_supersampled_first_hemisphere(oscenes, key, asn):
     assert np.abs(z).max() < 5 and abs(z.mean()) < 4 / np.sqrt(n), (np.abs(z).max(), z.mean())
 
 
+def test_translucent(tmp_path):
+    """The trans material: -I irradiance through the diffuser and radiance
+    of view rays with -ab 0 -st 1, 1e-6; aimed view rays with -ab 1 -st 0
+    (ambient from both sides, both lobes sampled): means of 256 replicas
+    within 5 standard errors of the reference's."""
+    from pyradiance_gb300 import workloads as w
+    g = golden("translucent.npz")
+    (tmp_path / "trans.rad").write_text(w.trans_room())
+    sc = po.Scene(tmp_path / "trans.rad")
+    o = po.default_opts("rtrace", I=1, ab=0, dj=0, ds=0, dr=0, dt=0, st=1, u=0)
+    rgb, _, _, _ = po.rtrace(sc, o, g["grid"], hits=False, threads=8)
+    np.testing.assert_allclose(rgb, g["irradiance"], rtol=1e-6, atol=1e-9)
+    o.I = 0
+    rgb, _, _, _ = po.rtrace(sc, o, g["view"], hits=False, threads=8)
+    np.testing.assert_allclose(rgb, g["radiance"], rtol=1e-6, atol=1e-9)
+    K, n = 256, len(g["aimed"])
+    o = po.default_opts("rtrace", ab=1, aa=0, ad=256, lw=1e-4, dj=0, ds=0, dr=0, dt=0, st=0, u=0)
+    o.as_ = 0
+    rgb, _, _, _ = po.rtrace(sc, o, np.repeat(g["aimed"], K, axis=0), hits=False, threads=8)
+    a = rgb.reshape(n, K, 3)
+    m, se = a.mean(1), a.std(1, ddof=1) / np.sqrt(K)
+    z = (m - g["ab1_mean"]) / np.sqrt(se ** 2 + g["ab1_se"] ** 2 + (1e-6 * np.abs(g["ab1_mean"]) + 1e-9) ** 2)
+    assert np.abs(z).max() < 5 and abs(z.mean()) < 4 / np.sqrt(n), (np.abs(z).max(), z.mean())
+
+
 def test_circular_sources(scene_dir, tmp_path):
     """Sphere and disk lights: -I direct irradiance with -ds 0 and with the
     disk partitioned (-ds 0.2, pieces trimmed to the circle), 1e-6; with
