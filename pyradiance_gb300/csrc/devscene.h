@@ -18,6 +18,8 @@
  *                                 vertices, packed at a fixed place per
  *                                 object (v0 v1 | v2 v3), so that a face
  *                                 test needs no second indirection
+ *   orec      float4[4 * nobjs]   obj, geo and fv4 of each object in one
+ *                                 64-byte record (the walk's object test)
  *   cone      float[24 * ncones]  3x4 world->canonical transform (rings),
  *                                 axis, base point, length, slant, radii
  *   mat       float4[2 * nmats]   material kind and parameters
@@ -105,6 +107,7 @@ typedef struct {
     const float4 *geo;
     const float2 *fvert;
     const float4 *fv4;
+    const float4 *orec;        /* per object: obj, geo and fv4 packed, 64 bytes */
     const float *cone;
     /* materials */
     const float4 *mat;

@@ -99,11 +99,11 @@ struct gb_scene {
     std::vector<int4> hobj;
     std::vector<float4> hgeo;
     std::vector<float2> hfvert;
-    std::vector<float4> hfv4;
+    std::vector<float4> hfv4, horec;
     std::vector<float> hcone;
     std::vector<gb_dsrc> hsrc;
     /* device scene */
-    DevBuf kids, setdata, obj, geo, fvert, fv4, cone, matd, srcd, trk, instd;
+    DevBuf kids, setdata, obj, geo, fvert, fv4, cone, matd, srcd, trk, instd, orec;
     gb_dscene ds;
     /* work buffers */
     DevBuf sensors, value, bins, stats, roots, rootspt, qa, qb, qcount, binprog, modinfo, hits, hitt, trkrun,
@@ -136,6 +136,13 @@ extern "C" int gb_last_profile(int kernel, double *ms, int64_t *launches, int64_
         counters[i] = (int64_t)g_prof.st[kernel][i];
     if (region_ms) *region_ms = g_prof.region_ms;
     return GB_OK;
+}
+
+static float __int_as_float_host(int v)
+{
+    float f;
+    memcpy(&f, &v, sizeof f);
+    return f;
 }
 
 static int material_kind(const gb_object *m, float4 *m0, float4 *m1, std::string &why)
@@ -397,6 +404,7 @@ static int prepare_device(gb_scene *G)
     if (stack < 16384)
         CK(cudaDeviceSetLimit(cudaLimitStackSize, 16384));
     if (upload(G->kids, G->hkids) < 0 || upload(G->setdata, G->hsetdata) < 0 || upload(G->instd, G->hinst) < 0 ||
+        upload(G->orec, G->horec) < 0 ||
         upload(G->obj, G->hobj) < 0 || upload(G->geo, G->hgeo) < 0 || upload(G->fvert, G->hfvert) < 0 ||
         upload(G->fv4, G->hfv4) < 0 || upload(G->cone, G->hcone) < 0 || upload(G->matd, G->mat) < 0 ||
         upload(G->srcd, G->hsrc) < 0)
@@ -408,6 +416,7 @@ static int prepare_device(gb_scene *G)
     d.geo = (const float4 *)G->geo.p;
     d.fvert = (const float2 *)G->fvert.p;
     d.fv4 = (const float4 *)G->fv4.p;
+    d.orec = (const float4 *)G->orec.p;
     d.cone = (const float *)G->cone.p;
     d.mat = (const float4 *)G->matd.p;
     d.src = (const gb_dsrc *)G->srcd.p;
@@ -602,6 +611,15 @@ static int build_arrays(gb_scene *G)
     if (sid >= 0x7fffffffll)
         return set_err(GB_EUNSUPPORTED, "%lld instanced surfaces exceed the 2^31 surface ids", sid);
     G->hinst.swap(inst);
+    std::vector<float4> orec(4 * obj.size());    /* obj | geo | fv4 (2): the walk's 64-byte record */
+    for (size_t i = 0; i < obj.size(); i++) {
+        orec[4 * i] = make_float4(__int_as_float_host(obj[i].x), __int_as_float_host(obj[i].y),
+                                  __int_as_float_host(obj[i].z), __int_as_float_host(obj[i].w));
+        orec[4 * i + 1] = geo[i];
+        orec[4 * i + 2] = fv4[2 * i];
+        orec[4 * i + 3] = fv4[2 * i + 1];
+    }
+    G->horec.swap(orec);
     std::vector<gb_dsrc> src = G->src;
     if (src.empty()) src.resize(1);
     G->hkids.swap(kids);
@@ -627,6 +645,7 @@ static int build_arrays(gb_scene *G)
     d.geo = G->hgeo.data();
     d.fvert = G->hfvert.data();
     d.fv4 = G->hfv4.data();
+    d.orec = G->horec.data();
     d.cone = G->hcone.data();
     d.mat = G->mat.data();
     d.nsrc = (int)G->src.size();
@@ -709,7 +728,7 @@ extern "C" void gb_scene_free(gb_scene *G)
 {
     if (!G)
         return;
-    DevBuf *bufs[] = {&G->kids, &G->setdata, &G->instd, &G->obj, &G->geo, &G->fvert, &G->fv4, &G->cone, &G->matd,
+    DevBuf *bufs[] = {&G->kids, &G->setdata, &G->instd, &G->orec, &G->obj, &G->geo, &G->fvert, &G->fv4, &G->cone, &G->matd,
                       &G->srcd, &G->trk, &G->sensors, &G->value, &G->bins, &G->stats, &G->roots, &G->rootspt, &G->qa,
                       &G->qb, &G->qcount, &G->binprog, &G->modinfo, &G->hits, &G->hitt, &G->trkrun, &G->hitrec,
                       &G->adja, &G->adjb, &G->dlde, &G->gradd, &G->rootdraw, &G->rootlot, &G->tga, &G->tgb,

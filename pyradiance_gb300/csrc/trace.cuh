@@ -377,10 +377,11 @@ GB_DFN void hit_object(const gb_dscene &S, int obj, float3 org, float3 dir, Hit 
                                            float tmin, bool self = false, int skip = -1)
 {
     /* the object record, plane and packed vertices depend on obj alone, so
-     * all four loads are issued together */
-    const int4 od = GB_LDG(S.obj + obj);
-    const float4 pl = GB_LDG(S.geo + obj);
-    const float4 va = GB_LDG(S.fv4 + 2 * obj), vb = GB_LDG(S.fv4 + 2 * obj + 1);
+     * all four loads are issued together, from one line */
+    const float4 *rec = S.orec + 4 * obj;        /* one 64-byte record: a single cache line */
+    const int4 od = GB_LDG(reinterpret_cast<const int4 *>(rec));
+    const float4 pl = GB_LDG(rec + 1);
+    const float4 va = GB_LDG(rec + 2), vb = GB_LDG(rec + 3);
     int kind = od.x & 0xff;
     switch (kind) {
     case DK_FACE:
