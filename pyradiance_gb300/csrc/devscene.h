@@ -6,7 +6,8 @@
  *                                 <= -2 full leaf: gb_leaf_code of its set's
  *                                 offset in set_data and size), 32 B per node
  *   set_data  int32[...]          [count, members in DESCENDING object order]
- *                                 (the order rt/raytrace.c:585 tests them)
+ *                                 (the order rt/raytrace.c:585 tests them),
+ *                                 each member given by its record slot
  *   obj       int4[nobjs]         x: kind | flags << 8 | nv << 16,
  *                                 y: material slot (-1 none), z: modifier
  *                                 object index, w: vertex / cone offset
@@ -18,8 +19,10 @@
  *                                 vertices, packed at a fixed place per
  *                                 object (v0 v1 | v2 v3), so that a face
  *                                 test needs no second indirection
- *   orec      float4[4 * nobjs]   obj, geo and fv4 of each object in one
- *                                 64-byte record (the walk's object test)
+ *   orec      float4[4 * nobjs]   obj (its y: the object's index), geo and
+ *                                 fv4 of each object in one 64-byte record,
+ *                                 in the order the leaves first reach them
+ *   oslot     int32[nobjs]        each object's record slot
  *   cone      float[24 * ncones]  3x4 world->canonical transform (rings),
  *                                 axis, base point, length, slant, radii
  *   mat       float4[2 * nmats]   material kind and parameters
@@ -107,7 +110,8 @@ typedef struct {
     const float4 *geo;
     const float2 *fvert;
     const float4 *fv4;
-    const float4 *orec;        /* per object: obj, geo and fv4 packed, 64 bytes */
+    const float4 *orec;        /* per record slot: obj (y: the object's index), geo, fv4; 64 bytes */
+    const int   *oslot;        /* per object: its record slot */
     const float *cone;
     /* materials */
     const float4 *mat;

@@ -100,10 +100,11 @@ struct gb_scene {
     std::vector<float4> hgeo;
     std::vector<float2> hfvert;
     std::vector<float4> hfv4, horec;
+    std::vector<int> hoslot;
     std::vector<float> hcone;
     std::vector<gb_dsrc> hsrc;
     /* device scene */
-    DevBuf kids, setdata, obj, geo, fvert, fv4, cone, matd, srcd, trk, instd, orec;
+    DevBuf kids, setdata, obj, geo, fvert, fv4, cone, matd, srcd, trk, instd, orec, oslot;
     gb_dscene ds;
     /* work buffers */
     DevBuf sensors, value, bins, stats, roots, rootspt, qa, qb, qcount, binprog, modinfo, hits, hitt, trkrun,
@@ -404,7 +405,7 @@ static int prepare_device(gb_scene *G)
     if (stack < 16384)
         CK(cudaDeviceSetLimit(cudaLimitStackSize, 16384));
     if (upload(G->kids, G->hkids) < 0 || upload(G->setdata, G->hsetdata) < 0 || upload(G->instd, G->hinst) < 0 ||
-        upload(G->orec, G->horec) < 0 ||
+        upload(G->orec, G->horec) < 0 || upload(G->oslot, G->hoslot) < 0 ||
         upload(G->obj, G->hobj) < 0 || upload(G->geo, G->hgeo) < 0 || upload(G->fvert, G->hfvert) < 0 ||
         upload(G->fv4, G->hfv4) < 0 || upload(G->cone, G->hcone) < 0 || upload(G->matd, G->mat) < 0 ||
         upload(G->srcd, G->hsrc) < 0)
@@ -417,6 +418,7 @@ static int prepare_device(gb_scene *G)
     d.fvert = (const float2 *)G->fvert.p;
     d.fv4 = (const float4 *)G->fv4.p;
     d.orec = (const float4 *)G->orec.p;
+    d.oslot = (const int *)G->oslot.p;
     d.cone = (const float *)G->cone.p;
     d.mat = (const float4 *)G->matd.p;
     d.src = (const gb_dsrc *)G->srcd.p;
@@ -563,12 +565,43 @@ static int build_arrays(gb_scene *G)
      * load before its members' */
     std::vector<int> kids(H.kids, H.kids + 8 * (size_t)H.nnodes);
     if (kids.empty()) kids.assign(8, -1);
+    /* record slots: objects in the order a depth-first pass over the leaves
+     * (the scene's octree, then each instanced one) first reaches them, so
+     * that the objects of neighbouring leaves share cache lines; set
+     * members are stored as slots */
+    std::vector<int> slot_of((size_t)(H.nobjs > 0 ? H.nobjs : 1), -1);
+    {
+        int next = 0;
+        std::vector<int32_t> stack;
+        std::vector<int32_t> roots(1, H.root);
+        for (int k = 0; k < H.nsubs; k++)
+            roots.push_back(H.subs[k].root);
+        for (int32_t rt : roots) {
+            stack.assign(1, rt);
+            while (!stack.empty()) {
+                const int32_t code = stack.back();
+                stack.pop_back();
+                if (code >= 0) {
+                    for (int k = 7; k >= 0; k--)          /* children 0..7 in order */
+                        stack.push_back(H.kids[8 * (size_t)code + k]);
+                } else if (code <= -2) {
+                    const int32_t *st = gb_scene_set(&H, code);
+                    for (int k = 1; k <= st[0]; k++)
+                        if (slot_of[st[k]] < 0)
+                            slot_of[st[k]] = next++;
+                }
+            }
+        }
+        for (int32_t i = 0; i < H.nobjs; i++)
+            if (slot_of[i] < 0)
+                slot_of[i] = next++;
+    }
     std::vector<int> setdata((size_t)H.set_len > 0 ? (size_t)H.set_len : 1, 0);
     for (int32_t s = 0; s < H.nsets; s++) {
         const int32_t *st = H.set_data + H.set_off[s];
         setdata[H.set_off[s]] = st[0];
         for (int k = 1; k <= st[0]; k++)
-            setdata[H.set_off[s] + k] = st[st[0] + 1 - k];
+            setdata[H.set_off[s] + k] = slot_of[st[st[0] + 1 - k]];
     }
     if ((int64_t)H.set_len >= GB_LEAF_MAXOFF)
         return set_err(GB_EUNSUPPORTED, "octree sets of %lld entries exceed the %d a leaf code addresses",
@@ -613,13 +646,17 @@ static int build_arrays(gb_scene *G)
     G->hinst.swap(inst);
     std::vector<float4> orec(4 * obj.size());    /* obj | geo | fv4 (2): the walk's 64-byte record */
     for (size_t i = 0; i < obj.size(); i++) {
-        orec[4 * i] = make_float4(__int_as_float_host(obj[i].x), __int_as_float_host(obj[i].y),
-                                  __int_as_float_host(obj[i].z), __int_as_float_host(obj[i].w));
-        orec[4 * i + 1] = geo[i];
-        orec[4 * i + 2] = fv4[2 * i];
-        orec[4 * i + 3] = fv4[2 * i + 1];
+        const size_t r = 4 * (size_t)slot_of[i];
+        orec[r] = make_float4(__int_as_float_host(obj[i].x), __int_as_float_host((int)i),
+                              __int_as_float_host(obj[i].z), __int_as_float_host(obj[i].w));
+        orec[r + 1] = geo[i];
+        orec[r + 2] = fv4[2 * i];
+        orec[r + 3] = fv4[2 * i + 1];
     }
+    if (orec.empty())
+        orec.assign(4, make_float4(0, 0, 0, 0));
     G->horec.swap(orec);
+    G->hoslot.swap(slot_of);
     std::vector<gb_dsrc> src = G->src;
     if (src.empty()) src.resize(1);
     G->hkids.swap(kids);
@@ -646,6 +683,7 @@ static int build_arrays(gb_scene *G)
     d.fvert = G->hfvert.data();
     d.fv4 = G->hfv4.data();
     d.orec = G->horec.data();
+    d.oslot = G->hoslot.data();
     d.cone = G->hcone.data();
     d.mat = G->mat.data();
     d.nsrc = (int)G->src.size();
@@ -728,7 +766,7 @@ extern "C" void gb_scene_free(gb_scene *G)
 {
     if (!G)
         return;
-    DevBuf *bufs[] = {&G->kids, &G->setdata, &G->instd, &G->orec, &G->obj, &G->geo, &G->fvert, &G->fv4, &G->cone, &G->matd,
+    DevBuf *bufs[] = {&G->kids, &G->setdata, &G->instd, &G->orec, &G->oslot, &G->obj, &G->geo, &G->fvert, &G->fv4, &G->cone, &G->matd,
                       &G->srcd, &G->trk, &G->sensors, &G->value, &G->bins, &G->stats, &G->roots, &G->rootspt, &G->qa,
                       &G->qb, &G->qcount, &G->binprog, &G->modinfo, &G->hits, &G->hitt, &G->trkrun, &G->hitrec,
                       &G->adja, &G->adjb, &G->dlde, &G->gradd, &G->rootdraw, &G->rootlot, &G->tga, &G->tgb,

@@ -373,15 +373,9 @@ GB_DNI void hit_instance(const gb_dscene &S, int slot, float3 org, float3 dir, H
 #define WALK_DEFER 2
 #define HIT_DEFER 0x7fffffff    /* with t = -1: every later test fails and the leaf ends the walk */
 template <int MODE = WALK_FULL>
-GB_DFN void hit_object(const gb_dscene &S, int obj, float3 org, float3 dir, Hit &best,
-                                           float tmin, bool self = false, int skip = -1)
+GB_DFN void hit_record(const gb_dscene &S, int obj, int4 od, float4 pl, float4 va, float4 vb, float3 org,
+                       float3 dir, Hit &best, float tmin, bool self, int skip)
 {
-    /* the object record, plane and packed vertices depend on obj alone, so
-     * all four loads are issued together, from one line */
-    const float4 *rec = S.orec + 4 * obj;        /* one 64-byte record: a single cache line */
-    const int4 od = GB_LDG(reinterpret_cast<const int4 *>(rec));
-    const float4 pl = GB_LDG(rec + 1);
-    const float4 va = GB_LDG(rec + 2), vb = GB_LDG(rec + 3);
     int kind = od.x & 0xff;
     switch (kind) {
     case DK_FACE:
@@ -417,6 +411,34 @@ GB_DFN void hit_object(const gb_dscene &S, int obj, float3 org, float3 dir, Hit 
         }
         break;
     }
+}
+
+/* The object in record slot sl (the records are laid out in the order the
+ * octree's leaves first reach their objects, so that the objects of a
+ * leaf share cache lines); the record carries the object's index.  The
+ * record, plane and packed vertices come from one 64-byte record, all four
+ * loads issued together.  The object the ray leaves (skip) is not tested,
+ * or, when curved, tested with its root at the origin excluded. */
+template <int MODE = WALK_FULL>
+GB_DFN void hit_slot(const gb_dscene &S, int sl, float3 org, float3 dir, Hit &best, float tmin, int skip,
+                     bool curved_skip)
+{
+    const float4 *rec = S.orec + 4 * sl;
+    const int4 od = GB_LDG(reinterpret_cast<const int4 *>(rec));
+    const float4 pl = GB_LDG(rec + 1);
+    const float4 va = GB_LDG(rec + 2), vb = GB_LDG(rec + 3);
+    const int obj = od.y;
+    if (obj != skip)
+        hit_record<MODE>(S, obj, od, pl, va, vb, org, dir, best, tmin, false, skip);
+    else if (curved_skip)                        /* curved origin surface */
+        hit_record<MODE>(S, obj, od, pl, va, vb, org, dir, best, tmin, true, skip);
+}
+
+/* the test of object obj (by index) */
+template <int MODE = WALK_FULL>
+GB_DFN void hit_object(const gb_dscene &S, int obj, float3 org, float3 dir, Hit &best, float tmin)
+{
+    hit_slot<MODE>(S, GB_LDG(S.oslot + obj), org, dir, best, tmin, -1, false);
 }
 
 /* ------------------------------------------------------------------------
@@ -592,12 +614,9 @@ GB_DFN bool walk_iter(const gb_dscene &S, const Cube &C, Walk &W, Stack &stk)
     for (int u = 0; u < WALK_TESTS; u++) {
         if (W.k > W.cnt)
             break;
-        const int o = GB_LDG(S.set_data + W.set + W.k);
+        const int sl = GB_LDG(S.set_data + W.set + W.k);
         W.k++;
-        if (o != W.skip)
-            hit_object<Cube::mode>(S, o, W.org, W.dir, W.best, D_FTINY, false, W.skip);
-        else if (W.curved_skip)                  /* curved origin surface */
-            hit_object<Cube::mode>(S, o, W.org, W.dir, W.best, D_FTINY, true);
+        hit_slot<Cube::mode>(S, sl, W.org, W.dir, W.best, D_FTINY, W.skip, W.curved_skip);
     }
     if (W.k <= W.cnt)
         return false;
