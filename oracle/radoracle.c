@@ -871,7 +871,7 @@ static void trace_contrib(ctx *X, const RAY *r)
     {
         /* evaluate the bin program in double (gbcommon.h byte code) */
         const gb_binins *pr = X->prog + X->modinfo[3 * slot];
-        double st[16];
+        double st[GB_BINSTACK], tmp[GB_BINTEMPS];
         int sp = 0, pc;
         bval = -1;
         for (pc = 0; pc < GB_BINPROG_MAX; pc++) {
@@ -890,6 +890,43 @@ static void trace_contrib(ctx *X, const RAY *r)
             case GB_OP_NEG: st[sp - 1] = -st[sp - 1]; break;
             case GB_OP_IF: sp -= 2; st[sp - 1] = st[sp - 1] > 0 ? st[sp] : st[sp + 1]; break;
             case GB_OP_FLOOR: st[sp - 1] = floor(st[sp - 1]); break;
+            case GB_OP_POW: sp--; st[sp - 1] = pow(st[sp - 1], st[sp]); break;
+            case GB_OP_FN1: {
+                double x = st[sp - 1];
+                switch ((int)in.a) {
+                case GB_FN_SQRT: x = sqrt(x); break;
+                case GB_FN_SIN: x = sin(x); break;
+                case GB_FN_COS: x = cos(x); break;
+                case GB_FN_TAN: x = tan(x); break;
+                case GB_FN_ASIN: x = asin(x); break;
+                case GB_FN_ACOS: x = acos(x); break;
+                case GB_FN_ATAN: x = atan(x); break;
+                case GB_FN_EXP: x = exp(x); break;
+                case GB_FN_LOG: x = log(x); break;
+                case GB_FN_LOG10: x = log10(x); break;
+                default: x = ceil(x); break;
+                }
+                st[sp - 1] = x;
+                break;
+            }
+            case GB_OP_ATAN2: sp--; st[sp - 1] = atan2(st[sp - 1], st[sp]); break;
+            case GB_OP_MAXN: case GB_OP_MINN: {
+                int k = (int)in.a, j;
+                double m = st[sp - k];
+                for (j = sp - k + 1; j < sp; j++) m = op == GB_OP_MAXN ? fmax(m, st[j]) : fmin(m, st[j]);
+                sp -= k;
+                st[sp++] = m;
+                break;
+            }
+            case GB_OP_SELECT: {
+                int k = (int)in.a, i = (int)(st[sp - k - 1] + .5);
+                double v = i == 0 ? (double)k : (i > 0 && i <= k ? st[sp - k - 1 + i] : -1.0);
+                sp -= k + 1;
+                st[sp++] = v;
+                break;
+            }
+            case GB_OP_STORE: tmp[(int)in.a & (GB_BINTEMPS - 1)] = st[--sp]; break;
+            case GB_OP_LOAD: st[sp++] = tmp[(int)in.a & (GB_BINTEMPS - 1)]; break;
             case GB_OP_RBIN: {
                 /* util/reinhartb.cal:17-47 */
                 const gb_binins *q = pr + pc + 1;
@@ -1757,6 +1794,9 @@ static void eval_irrad(ctx *X, const double *rv, uint32_t sensor, double rgb[3])
     nd.refl = 0;
     nd.rblt = 0;
     nd.flat = 0;
+    nd.trans = nd.tspec = nd.tdiff = 0;
+    nd.tran = nd.tblt = 0;
+    memcpy(nd.prdir, r.rdir, sizeof nd.prdir);
     sct[0] = sct[1] = sct[2] = PI;
     X->ssamp_root = X->o->prog == GB_PROG_RTRACE;
     multambient(X, sct, &r, nd.pnorm);

@@ -327,9 +327,21 @@ enum gb_binop {
     GB_OP_FLOOR,
     GB_OP_RBIN,      /* Reinhart bin; params in the next 2 records:
                         {MF, RHS, rNx, rNy} {rNz, Ux, Uy, Uz} */
+    GB_OP_POW,       /* pop b, a: push a^b */
+    GB_OP_FN1,       /* apply one-argument function a (GB_FN_*) to the top */
+    GB_OP_ATAN2,     /* pop x, y: push atan2(y, x) */
+    GB_OP_MAXN,      /* pop a values, push their maximum */
+    GB_OP_MINN,      /* pop a values, push their minimum */
+    GB_OP_SELECT,    /* pop a values and an index i: push value i (1-based); i 0: a */
+    GB_OP_STORE,     /* pop into temporary a */
+    GB_OP_LOAD,      /* push temporary a */
     GB_OP_MAX
 };
-#define GB_BINPROG_MAX 64
+enum gb_binfn { GB_FN_SQRT, GB_FN_SIN, GB_FN_COS, GB_FN_TAN, GB_FN_ASIN, GB_FN_ACOS, GB_FN_ATAN, GB_FN_EXP,
+                GB_FN_LOG, GB_FN_LOG10, GB_FN_CEIL };
+#define GB_BINPROG_MAX 1024   /* instructions of one bin program */
+#define GB_BINSTACK 32        /* evaluation stack */
+#define GB_BINTEMPS 32        /* temporaries (arguments used more than once) */
 
 typedef struct { float op, a, b, c; } gb_binins;
 

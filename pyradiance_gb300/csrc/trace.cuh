@@ -858,9 +858,28 @@ GB_DFN float reinhart_bin(float Dx, float Dy, float Dz, const gb_binins *p)
     return acc + azn;
 }
 
+GB_DFN float bin_fn1(int f, float x)
+{
+    switch (f) {
+    case GB_FN_SQRT: return sqrtf(x);
+    case GB_FN_SIN: return sinf(x);
+    case GB_FN_COS: return cosf(x);
+    case GB_FN_TAN: return tanf(x);
+    case GB_FN_ASIN: return asinf(x);
+    case GB_FN_ACOS: return acosf(x);
+    case GB_FN_ATAN: return atanf(x);
+    case GB_FN_EXP: return expf(x);
+    case GB_FN_LOG: return logf(x);
+    case GB_FN_LOG10: return log10f(x);
+    default: return ceilf(x);
+    }
+}
+
+/* the bin program of a contributing ray (binexpr.cpp); -1 when the program
+ * is malformed or selects outside its values */
 GB_DFN float eval_bin(const gb_binins *prog, float3 d)
 {
-    float st[16];
+    float st[GB_BINSTACK], tmp[GB_BINTEMPS];
     int sp = 0;
     for (int pc = 0; pc < GB_BINPROG_MAX; pc++) {
         gb_binins in = prog[pc];
@@ -883,10 +902,32 @@ GB_DFN float eval_bin(const gb_binins *prog, float3 d)
             st[sp++] = reinhart_bin(d.x, d.y, d.z, prog + pc + 1);
             pc += 2;
             break;
+        case GB_OP_POW: sp--; st[sp - 1] = powf(st[sp - 1], st[sp]); break;
+        case GB_OP_FN1: st[sp - 1] = bin_fn1((int)in.a, st[sp - 1]); break;
+        case GB_OP_ATAN2: sp--; st[sp - 1] = atan2f(st[sp - 1], st[sp]); break;
+        case GB_OP_MAXN: case GB_OP_MINN: {
+            const int k = (int)in.a;
+            float m = st[sp - k];
+            for (int j = sp - k + 1; j < sp; j++)
+                m = op == GB_OP_MAXN ? fmaxf(m, st[j]) : fminf(m, st[j]);
+            sp -= k;
+            st[sp++] = m;
+            break;
+        }
+        case GB_OP_SELECT: {                     /* common/calfunc.c select(): index rounded */
+            const int k = (int)in.a;
+            const int i = (int)(st[sp - k - 1] + .5f);
+            const float v = i == 0 ? (float)k : (i > 0 && i <= k ? st[sp - k - 1 + i] : -1.f);
+            sp -= k + 1;
+            st[sp++] = v;
+            break;
+        }
+        case GB_OP_STORE: tmp[(int)in.a & (GB_BINTEMPS - 1)] = st[--sp]; break;
+        case GB_OP_LOAD: st[sp++] = tmp[(int)in.a & (GB_BINTEMPS - 1)]; break;
         default:
             return -1.f;
         }
-        if (sp >= 15)
+        if (sp >= GB_BINSTACK - 1 || sp < 0)
             return -1.f;
     }
     return -1.f;

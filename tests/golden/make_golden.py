@@ -179,6 +179,32 @@ def supersampled_irradiance(tmp: Path, n: int = 100, K: int = 512) -> None:
     print("supersampled: mean %.4g (as 512) vs %.4g (as 0)" % (out["as512_mean"].mean(), out["as0_mean"].mean()))
 
 
+def general_bins(tmp: Path) -> None:
+    """General bin expressions: the sky subdivision of
+    tests/golden/patchbins.cal (recursion, select, if, asin, atan2, floor,
+    sqrt, max, min, ^) with rcontrib -ab 0 in radiance mode: rays from
+    inside the empty window room aimed out of the window reach the sky or
+    the ground glow through the glass, so each record has the one bin of
+    its ray's direction (deterministic)."""
+    import shutil
+    octp = oconv(w.window_room(ntri=0), tmp, "bins")
+    shutil.copy(OUT / "patchbins.cal", tmp / "patchbins.cal")
+    rng = np.random.default_rng(17)
+    org = rng.uniform((1.0, 1.0, 0.5), (9.0, 5.0, 2.5), size=(3000, 3))
+    x0, x1, z0, z1 = w.WINDOW
+    tgt = np.column_stack([rng.uniform(x0 + .05, x1 - .05, 3000), np.zeros(3000), rng.uniform(z0 + .05, z1 - .05, 3000)])
+    d = tgt - org
+    rays = np.hstack([org, d / np.linalg.norm(d, axis=1, keepdims=True)])
+    out = run(["rcontrib", "-h", "-u-", "-ab", "0", "-fdd", "-f", "patchbins.cal", "-b", "pbin", "-bn", "Npbins",
+               "-m", "skyglow", "-m", "groundglow", octp.name], rays.astype("<f8").tobytes(), cwd=tmp)
+    a = np.frombuffer(out, dtype="<f8").reshape(len(rays), -1, 3)
+    np.savez_compressed(OUT / "general_bins.npz", rays=rays, bins=a[..., 0].astype(np.float32),
+                        cmd="rcontrib -h -u- -ab 0 -fdd -f patchbins.cal -b pbin -bn Npbins -m skyglow -m groundglow")
+    hit = a[..., 0] > 0
+    print("general_bins: %d bins, %d rays with a bin, %d distinct bins hit" % (a.shape[1], hit.any(1).sum(),
+                                                                                hit.any(0).sum()))
+
+
 def translucent(tmp: Path, K: int = 256) -> None:
     """The trans material (rt/normal.c, MAT_TRANS): -I irradiance on a grid
     at 0.8 m (the light seen through the diffuser: shadow rays pass its
@@ -356,7 +382,7 @@ def main() -> None:
         sys.exit("reference programs missing: make -f oracle/build_ref.mk REF=/root/reference -j8")
     parts = {"octree": octree_digests, "c1": c1_direct, "c1p": c1_partitioned, "zoo": zoo, "glossy": glossy, "irr": surface_irradiance,
              "ss": supersampled_irradiance, "inst": instances, "circ": circular_sources,
-             "trans": translucent,
+             "trans": translucent, "bins": general_bins,
              "dct": lambda tmp: dct_small(), "trace_oct": lambda tmp: ref_fixture_trace(),
              "c2ab1": lambda tmp: c2_stats(tmp, ab=1, K=256), "c2ab3": lambda tmp: c2_stats(tmp, ab=3, K=256)}
     only = sys.argv[1:] or list(parts)         # e.g. make_golden.py c1p

@@ -291,6 +291,22 @@ def test_surface_irradiance_one_bounce(gb, scenes):
     assert np.abs(z).max() < 5 and abs(z.mean()) < 4 / np.sqrt(n)
 
 
+def test_general_bin_expressions(gb, scenes):
+    """Bins from a function file of our own (recursion on constant
+    arguments, select, if, asin, atan2, floor, sqrt, max, min, ^), compiled
+    to the device byte code: rcontrib -ab 0 radiance-mode rays leaving
+    through the window each land in the reference's bin (FP32 directions:
+    a ray within rounding of a bin edge may land beside it), values within
+    1e-5."""
+    from test_oracle_golden import MODS_PATCH
+    g = golden("general_bins.npz")
+    out, _ = rcontrib_c(gb, scenes["c2e"], opts("rcontrib", I=0, ab=0, c=1, u=0), g["rays"], mods=MODS_PATCH)
+    got = out[..., 0]
+    same = ((got > 0) == (g["bins"] > 0)).all(1)
+    assert same.mean() >= 0.999, np.nonzero(~same)
+    np.testing.assert_allclose(got[same], g["bins"][same], rtol=1e-5, atol=1e-9)
+
+
 def test_translucent(gb, tmp_path, scene_dir):
     """The trans material (rt/normal.c, MAT_TRANS): -I irradiance through
     the diffuser (shadow rays continue through its specular transmission)

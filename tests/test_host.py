@@ -88,8 +88,17 @@ def test_bin_expressions(lib):
                             nbins="Nrbins")]) == 577
     assert nbins(lib, [dict(modifier="s", binv="if(-Dx*0-Dy*0-Dz*-1,0,-1)", nbins="1")]) == 1
     assert nbins(lib, [dict(modifier="s", expr="b=floor(Dz*10)", binv="b", nbins="10")]) == 10
-    with pytest.raises(lib.GbError):
-        nbins(lib, [dict(modifier="s", binv="sin(Dx)", nbins="4")])
+    # general calcomp: functions with arguments, recursion on constants, built-ins
+    cal = str(ROOT / "tests" / "golden" / "patchbins.cal")
+    assert nbins(lib, [dict(modifier="s", calfile=cal, binv="pbin", nbins="Npbins")]) == 81
+    assert nbins(lib, [dict(modifier="s", expr="f(x,n)=floor(x*n)+n*0;k(r):if(r-.5,r+k(r-1),0)",
+                            binv="min(f(Dz+1,k(3)),5)", nbins="k(3)")]) == 6
+    assert nbins(lib, [dict(modifier="s", binv="floor(4*(sin(Dx)+1)/2.01)", nbins="4")]) == 4
+    for bad in ("rand(Dx)", "g(Dx)", "select(Dx)", "q"):
+        with pytest.raises(lib.GbError):
+            nbins(lib, [dict(modifier="s", binv=bad, nbins="4")])
+    with pytest.raises(lib.GbError):                          # unbounded recursion on the ray
+        nbins(lib, [dict(modifier="s", expr="r(x)=if(x,r(x-1),0)", binv="r(Dz)", nbins="2")])
     with pytest.raises(lib.GbError):
         nbins(lib, [dict(modifier="s", binv="3")])          # non-zero constant bin
     with pytest.raises(lib.GbError):

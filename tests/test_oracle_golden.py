@@ -134,6 +134,23 @@ def test_supersampled_first_hemisphere(oscenes, key, asn):
     assert np.abs(z).max() < 5 and abs(z.mean()) < 4 / np.sqrt(n), (np.abs(z).max(), z.mean())
 
 
+CAL = Path(__file__).resolve().parent / "golden" / "patchbins.cal"
+MODS_PATCH = [dict(modifier=m, calfile=str(CAL), binv="pbin", nbins="Npbins") for m in ("skyglow", "groundglow")]
+
+
+def test_general_bin_expressions(oscenes):
+    """A function file of our own (recursion on constant arguments, select,
+    if, asin, atan2, floor, sqrt, max, min, ^) compiled to the bin byte
+    code: rcontrib -ab 0 radiance-mode rays leaving through the window each
+    land in the reference's bin, with its value."""
+    g = golden("general_bins.npz")
+    o = po.default_opts("rcontrib", I=0, ab=0, c=1, u=0)
+    out, _ = po.rcontrib(oscenes["c2e"], o, MODS_PATCH, g["rays"], threads=8)
+    got = out[..., 0]
+    np.testing.assert_array_equal(got > 0, g["bins"] > 0)
+    np.testing.assert_allclose(got, g["bins"], rtol=1e-6, atol=1e-9)
+
+
 def test_translucent(tmp_path):
     """The trans material: -I irradiance through the diffuser and radiance
     of view rays with -ab 0 -st 1, 1e-6; aimed view rays with -ab 1 -st 0
