@@ -82,6 +82,7 @@ typedef struct {
 #define S_FLAT 4
 #define S_PROX 8
 #define S_CIR 32
+#define S_CYL 64
 
 static void vcross(double r[3], const double a[3], const double b[3])
 {
@@ -209,6 +210,26 @@ static int mark_sources(oscene *O)
             s->ss2 = PI * s->srad * s->srad;
             for (j = 0; j < 3; j++) s->ss[j][j] = 0.7236 * o->farg[3];
             s->flags = S_CIR;
+        } else if (o->otype == GT_CYLINDER) {          /* rt/srcsupp.c:234-264 cylsetsrc */
+            const gb_cone *c = &H->cones[i];
+            double ad[3], al = 0, r0;
+            int j;
+            if (!c->ok || (r0 = o->farg[c->r0]) <= FTINY) {
+                snprintf(O->err, sizeof O->err, "oracle: %s: illegal source radius", o->name);
+                return -1;
+            }
+            for (j = 0; j < 3; j++) {
+                ad[j] = o->farg[c->p1 + j] - o->farg[c->p0 + j];
+                s->sloc[j] = .5 * (o->farg[c->p1 + j] + o->farg[c->p0 + j]);
+            }
+            al = vnormalize(ad);
+            s->srad = .5 * al;
+            s->ss2 = 2. * r0 * al;
+            for (j = 0; j < 3; j++) s->ss[0][j] = .5 * al * ad[j];
+            perp0(s->ss[2], ad);                       /* getperpendicular without the random rotation */
+            for (j = 0; j < 3; j++) s->ss[2][j] *= .8559 * r0;
+            vcross(s->ss[1], s->ss[2], ad);
+            s->flags = S_CYL;
         } else if (o->otype == GT_RING) {              /* rt/srcsupp.c:207-231 rsetsrc */
             const gb_cone *c = &H->cones[i];
             int j;
@@ -1111,9 +1132,47 @@ static void flt_partit(const double ro[3], int mp, const double cent[3], const d
                sz0, sz1, out, np);
 }
 
+/* rt/srcsamp.c:187-221 cyl_partit: halves along the cylinder's axis */
+static void cyl_partit(const double ro[3], int mp, const double cent[3], const double axis[3], double d2, int ct0,
+                       int sz0, spart *out, int *np)
+{
+    double nc[3], na[3], v[3];
+    int i;
+    for (i = 0; i < 3; i++) v[i] = ro[i] - cent[i];
+    if (mp < 2 || vdot(v, v) >= d2) {
+        out[*np].ct[0] = ct0;
+        out[*np].ct[1] = 0;
+        out[*np].sz[0] = sz0;
+        out[*np].sz[1] = MAXSPART;
+        (*np)++;
+        return;
+    }
+    for (i = 0; i < 3; i++) na[i] = .5 * axis[i];
+    d2 *= 0.25;
+    sz0 >>= 1;
+    for (i = 0; i < 3; i++) nc[i] = cent[i] - na[i];
+    cyl_partit(ro, mp / 2, nc, na, d2, ct0 - sz0, sz0, out, np);
+    for (i = 0; i < 3; i++) nc[i] = cent[i] + na[i];
+    cyl_partit(ro, mp / 2, nc, na, d2, ct0 + sz0, sz0, out, np);
+}
+
 static int source_parts(const ctx *X, const osrc *s, const RAY *r, spart *out)
 {
     int np = 0;
+    if (X->o->ds > FTINY && (s->flags & S_CYL)) {         /* rt/srcsamp.c:240-273 cylpart */
+        double v[3] = {r->rop[0] - s->sloc[0], r->rop[1] - s->sloc[1], r->rop[2] - s->sloc[2]};
+        double rad2 = 1.365 * vdot(s->ss[1], s->ss[1]), safe2 = vdot(s->ss[0], s->ss[0]);
+        double d = vdot(v, s->ss[0]), cent2 = vdot(v, v), perp2 = cent2 - d * d / safe2;
+        if (perp2 <= rad2) return 0;
+        safe2 *= 4. * r->rweight * r->rweight / (X->o->ds * X->o->ds);
+        if (perp2 <= 4. * rad2 || cent2 >= safe2) {
+            out[0].ct[0] = out[0].ct[1] = 0;
+            out[0].sz[0] = out[0].sz[1] = MAXSPART;
+            return 1;
+        }
+        cyl_partit(r->rop, MAXSPART, s->sloc, s->ss[0], safe2, 0, MAXSPART, out, &np);
+        return np;
+    }
     if (X->o->ds <= FTINY || (s->flags & S_DISTANT) || !(s->flags & S_FLAT)) {   /* nopart */
         out[0].ct[0] = out[0].ct[1] = 0;
         out[0].sz[0] = out[0].sz[1] = MAXSPART;
@@ -1182,7 +1241,12 @@ static void direct(ctx *X, RAY *r, const NORMDAT *nd)
         if (!(s->flags & S_DISTANT))
             for (i = 0; i < 3; i++) dir[i] -= r->rop[i];
         if ((d = vnormalize(dir)) == 0.0) continue;
-        dom = (s->flags & S_FLAT) ? -vdot(s->snorm, dir) : 1.0;
+        if (s->flags & S_FLAT) dom = -vdot(s->snorm, dir);
+        else if (s->flags & S_CYL) {                   /* rt/srcsamp.c:364-376 scylform */
+            double d2 = vdot(dir, s->ss[0]);
+            d2 *= d2 / vdot(s->ss[0], s->ss[0]);
+            dom = sqrt(1. - d2);
+        } else dom = 1.0;
         dom *= parts[pi].sz[0] * parts[pi].sz[1] * (1.0 / MAXSPART / MAXSPART);
         if (s->flags & S_DISTANT) {
             dom *= s->ss2;

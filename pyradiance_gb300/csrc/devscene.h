@@ -63,6 +63,7 @@ enum { DM_NONE = 0, DM_PLASTIC, DM_METAL, DM_GLASS, DM_LIGHT, DM_GLOW, DM_TRANS 
 #define DS_PROX    0x08
 #define DS_FOLLOW  0x10
 #define DS_CIR     0x20   /* circular (disk, sphere, distant): SCIR */
+#define DS_CYL     0x40   /* cylinder: SCYL */
 
 typedef struct {
     float sloc[3];      /* centre (local) or direction (distant) */

@@ -328,6 +328,33 @@ static int mark_sources(gb_scene *G)
             }
             s.srad = (float)o->farg[3];
             s.ss2 = (float)(M_PI * o->farg[3] * o->farg[3]);
+        } else if (o->otype == GT_CYLINDER) {        /* rt/srcsupp.c:234-264 cylsetsrc */
+            const gb_cone *c = &H.cones[i];
+            if (!c->ok)
+                return set_err(GB_EIO, "%s: illegal source", o->name);
+            const double r0 = o->farg[c->r0];
+            if (r0 <= GB_FTINY)
+                return set_err(GB_EIO, "%s: illegal source radius", o->name);
+            double ad[3], al = 0, sw[3];
+            for (int j = 0; j < 3; j++) {
+                ad[j] = o->farg[c->p1 + j] - o->farg[c->p0 + j];
+                al += ad[j] * ad[j];
+            }
+            al = sqrt(al);
+            for (int j = 0; j < 3; j++) ad[j] /= al;
+            perp(sw, ad);                            /* getperpendicular, without the random rotation */
+            for (int j = 0; j < 3; j++) sw[j] *= .8559 * r0;
+            s.flags = DS_CYL;
+            for (int j = 0; j < 3; j++) {
+                s.sloc[j] = (float)(.5 * (o->farg[c->p1 + j] + o->farg[c->p0 + j]));
+                s.ss[0][j] = (float)(.5 * al * ad[j]);
+                s.ss[2][j] = (float)sw[j];
+            }
+            s.ss[1][0] = (float)(sw[1] * ad[2] - sw[2] * ad[1]);   /* SW x axis */
+            s.ss[1][1] = (float)(sw[2] * ad[0] - sw[0] * ad[2]);
+            s.ss[1][2] = (float)(sw[0] * ad[1] - sw[1] * ad[0]);
+            s.srad = (float)(.5 * al);
+            s.ss2 = (float)(2. * r0 * al);
         } else if (o->otype == GT_RING) {            /* rt/srcsupp.c:207-231 rsetsrc */
             const gb_cone *c = &H.cones[i];
             if (!c->ok)

@@ -756,7 +756,12 @@ __device__ __noinline__ void direct_sample(const gb_run &P, const Ray &r, float3
     float dom;
     if (src.flags & DS_FLAT)
         dom = -(src.snorm[0] * dir.x + src.snorm[1] * dir.y + src.snorm[2] * dir.z);
-    else
+    else if (src.flags & DS_CYL) {               /* rt/srcsamp.c:364-376 scylform */
+        const float3 su = f3(src.ss[0][0], src.ss[0][1], src.ss[0][2]);
+        float d = dot3(dir, su);
+        d *= d / dot3(su, su);
+        dom = sqrtf(1.f - d);
+    } else
         dom = 1.f;
     dom *= (float)(sz0 * sz1) * (1.f / (MAXSPART * MAXSPART));
     if (src.flags & DS_DISTANT) {
@@ -827,6 +832,62 @@ __device__ __noinline__ void direct_sample(const gb_run &P, const Ray &r, float3
  * times its distance is split as rt/srcsamp.c:260-330 (flatpart,
  * flt_partit) splits it: halved along its longer side, recursively, up to
  * MAXSPART pieces, lower half first; other sources are one piece. */
+/* The pieces of a cylinder source under -ds (rt/srcsamp.c:187-273 cylpart,
+ * cyl_partit): none from inside the cylinder's extended radius, the whole
+ * source from close by or far away, else halved along the axis, lower half
+ * first, until a piece is farther than its scaled length. */
+template <bool G>
+__device__ __noinline__ void direct_cyl(const gb_run &P, const Ray &r, float3 hp, const Surf &s, int origin,
+                                        Counters &cnt, int slot, int sn)
+{
+    const gb_dsrc &src = P.S.src[sn];
+    const float3 sloc = f3(src.sloc[0], src.sloc[1], src.sloc[2]);
+    const float3 su = f3(src.ss[0][0], src.ss[0][1], src.ss[0][2]);
+    const float3 sv = f3(src.ss[1][0], src.ss[1][1], src.ss[1][2]);
+    const float rad2 = 1.365f * dot3(sv, sv);
+    const float3 v = hp - sloc;
+    float safe2 = dot3(su, su);
+    float d = dot3(v, su);
+    const float cent2 = dot3(v, v), perp2 = cent2 - d * d / safe2;
+    if (perp2 <= rad2)
+        return;                                  /* inside the extended cylinder */
+    safe2 *= 4.f * r.weight * r.weight / (P.srcsizerat * P.srcsizerat);
+    if (perp2 <= 4.f * rad2 || cent2 >= safe2) {
+        direct_sample<G>(P, r, hp, s, origin, cnt, slot, sn, 0, 0, 0, MAXSPART, MAXSPART, false);
+        return;
+    }
+    struct Piece {
+        float3 cent, ax;
+        float d2;
+        int mp, ct0, sz0;
+    } stack[8];
+    int top = 0, pi = 0;
+    stack[top++] = {sloc, su, safe2, MAXSPART, 0, MAXSPART};
+    while (top > 0) {
+        Piece f = stack[--top];
+        for (;;) {
+            const float3 dc = hp - f.cent;
+            if (f.mp < 2 || dot3(dc, dc) >= f.d2) {
+                direct_sample<G>(P, r, hp, s, origin, cnt, slot, sn, pi++, f.ct0, 0, f.sz0, MAXSPART, true);
+                break;
+            }
+            Piece lo = f, hi = f;
+            const float3 ax = f.ax * 0.5f;
+            lo.ax = hi.ax = ax;
+            lo.d2 = hi.d2 = f.d2 * 0.25f;
+            lo.mp = hi.mp = f.mp / 2;
+            lo.sz0 = hi.sz0 = f.sz0 >> 1;
+            lo.ct0 = f.ct0 - lo.sz0;
+            hi.ct0 = f.ct0 + lo.sz0;
+            lo.cent = f.cent - ax;
+            hi.cent = f.cent + ax;
+            if (top < 8)
+                stack[top++] = hi;
+            f = lo;
+        }
+    }
+}
+
 template <bool G = false>
 __device__ void direct(const gb_run &P, const Ray &r, float3 hp, const Surf &s, int origin, Counters &cnt,
                        int slot)
@@ -842,6 +903,10 @@ __device__ void direct(const gb_run &P, const Ray &r, float3 hp, const Surf &s, 
             float rr = src.prox + src.srad;
             if (dot3(dv, dv) > rr * rr)
                 continue;
+        }
+        if (P.srcsizerat > D_FTINY && (src.flags & DS_CYL)) {
+            direct_cyl<G>(P, r, hp, s, origin, cnt, slot, sn);
+            continue;
         }
         if (P.srcsizerat <= D_FTINY || (src.flags & DS_DISTANT) || !(src.flags & DS_FLAT)) {
             direct_sample<G>(P, r, hp, s, origin, cnt, slot, sn, 0, 0, 0, MAXSPART, MAXSPART, false);

@@ -24,7 +24,7 @@ Workloads (sizes are the defaults):
 * ``glossy_room`` -- the room with rough specular plastic and metal
   (the specular-lobe sampling workload).
 * ``lamp_room`` -- the room lit by a sphere and a disk light (circular
-  source shapes).
+  source shapes); ``tube_room`` -- lit by two cylinder lights.
 * ``trans_room`` -- the room with translucent diffuser and frosted panels.
 * ``furniture``, ``instance_room`` -- an object octree and a room holding
   transformed instances of it (the instance workload).
@@ -260,6 +260,29 @@ def lamp_room(seed: int = 0, nboxes: int = 60) -> str:
     out.append(f"bulb_mat sphere bulb\n0\n0\n4 {X * 0.3:.9g} {Y * 0.5:.9g} {Z - 0.5:.9g} 0.15\n\n")
     out.append("void light disk_mat\n0\n0\n3 80 80 90\n\n")
     out.append(f"disk_mat ring disk\n0\n0\n8 {X * 0.7:.9g} {Y * 0.5:.9g} {Z - 0.01:.9g} 0 0 -1 0 0.3\n\n")
+    return "".join(out)
+
+
+def tube_room(seed: int = 0, nboxes: int = 60) -> str:
+    """The boxes of ``lamp_room`` lit by two cylinder lights (fluorescent
+    tubes of 1.2 m, radius 2 cm, one along x and one along y, 0.3 m under
+    the ceiling)."""
+    rng = np.random.default_rng(seed)
+    X, Y, Z = ROOM
+    out = [_mat_plastic("room_mat", (0.5, 0.5, 0.5)), _room_shell("room_mat")]
+    sizes = rng.uniform(0.2, 1.2, size=(nboxes, 3))
+    pos = rng.uniform(0.0, 1.0, size=(nboxes, 2))
+    rho = rng.uniform(0.2, 0.7, size=nboxes)
+    for i in range(nboxes):
+        s = sizes[i]
+        out.append(_mat_plastic(f"box_mat{i}", (rho[i],) * 3))
+        out.append(_box(f"box_mat{i}", f"box{i}", (pos[i, 0] * (X - s[0]), pos[i, 1] * (Y - s[1]), 0.005), s))
+    out.append("void light tube_mat\n0\n0\n3 300 300 280\n\n")
+    z = Z - 0.3
+    out.append(f"tube_mat cylinder tube_x\n0\n0\n7 {X * .3 - .6:.9g} {Y * .5:.9g} {z:.9g} {X * .3 + .6:.9g} "
+               f"{Y * .5:.9g} {z:.9g} 0.02\n\n")
+    out.append(f"tube_mat cylinder tube_y\n0\n0\n7 {X * .7:.9g} {Y * .5 - .6:.9g} {z:.9g} {X * .7:.9g} "
+               f"{Y * .5 + .6:.9g} {z:.9g} 0.02\n\n")
     return "".join(out)
 
 

@@ -240,12 +240,18 @@ def translucent(tmp: Path, K: int = 256) -> None:
 
 def circular_sources(tmp: Path, K: int = 256) -> None:
     """Sphere and disk lights (rt/srcsupp.c sphsetsrc, rsetsrc; the
-    circular trims of rt/srcsamp.c:85-109): -I direct irradiance on a grid
+    circular trims of rt/srcsamp.c:85-109), and cylinder lights (cylsetsrc,
+    cylpart, scylform) in a second room: -I direct irradiance on a grid
     at 0.8 m and one at 2.3 m (close to the lights), deterministic with
     -dj 0 -ds 0 and with -ds 0.2 (the disk split into pieces), and with
     -dj 0.9 (jittered and trimmed samples) as per-sensor means and standard
     errors of K replicas (-u+)."""
-    octp = oconv(w.lamp_room(), tmp, "lamp")
+    _circular(tmp, K, "lamp", w.lamp_room(), "circular_sources.npz")
+    _circular(tmp, K, "tube", w.tube_room(), "cylinder_sources.npz")
+
+
+def _circular(tmp: Path, K: int, name: str, text: str, fixture: str) -> None:
+    octp = oconv(text, tmp, name)
     rays = np.vstack([w.sensor_grid(40, 40), w.sensor_grid(20, 20, z=2.3)])
     inp = rays.astype("<f8").tobytes()
     base = ["rtrace", "-h", "-u-", "-I", "-ab", "0", "-dr", "0", "-dt", "0", "-fdd", "-ov"]
@@ -254,11 +260,11 @@ def circular_sources(tmp: Path, K: int = 256) -> None:
     sub = rays[::8]
     a = np.frombuffer(run([*base[:2], "-u+", *base[3:], "-dj", "0.9", "-ds", "0.2", octp],
                           np.repeat(sub, K, axis=0).astype("<f8").tobytes()), dtype="<f8").reshape(len(sub), K, 3)
-    np.savez_compressed(OUT / "circular_sources.npz", rays=rays, ds0=ds0, ds2=ds2, dj_rays=sub, K=K,
+    np.savez_compressed(OUT / fixture, rays=rays, ds0=ds0, ds2=ds2, dj_rays=sub, K=K,
                         dj_mean=a.mean(1), dj_se=a.std(1, ddof=1) / np.sqrt(K),
                         cmd="rtrace -h -u- -I -ab 0 -dr 0 -dt 0 -dj 0 [-ds 0 | -ds 0.2] | -u+ -dj 0.9 -ds 0.2")
-    print("circular_sources: lit %.3f, ds0 mean %.4g, ds2 mean %.4g, dj mean %.4g" % (
-        (ds0[:, 0] > 0).mean(), ds0.mean(), ds2.mean(), a.mean()))
+    print("%s: lit %.3f, ds0 mean %.4g, ds2 mean %.4g, dj mean %.4g" % (
+        fixture, (ds0[:, 0] > 0).mean(), ds0.mean(), ds2.mean(), a.mean()))
 
 
 def instances(tmp: Path) -> None:

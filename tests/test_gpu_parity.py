@@ -343,16 +343,19 @@ def test_translucent(gb, tmp_path, scene_dir):
     assert np.abs(z).max() < 5 and abs(z.mean()) < 4 / np.sqrt(n)
 
 
-def test_circular_sources(gb, tmp_path):
-    """Sphere and disk lights (rt/srcsupp.c sphsetsrc, rsetsrc): -I direct
+@pytest.mark.parametrize("room,fixture", [("lamp_room", "circular_sources.npz"),
+                                          ("tube_room", "cylinder_sources.npz")])
+def test_circular_sources(gb, tmp_path, room, fixture):
+    """Sphere and disk lights (rt/srcsupp.c sphsetsrc, rsetsrc), and
+    cylinder lights (cylsetsrc, cylpart, scylform): -I direct
     irradiance with -ds 0 and with the disk partitioned (-ds 0.2, pieces
     trimmed to the circle) within 1e-5 for 99.5% of the sensors (a sensor
     whose distance to a piece sits on the splitting threshold within FP32
     rounding may split differently), and jittered (-dj 0.9) per-sensor
     means of 256 replicas within 5 standard errors of the reference's."""
     from pyradiance_gb300 import workloads as w
-    g = golden("circular_sources.npz")
-    (tmp_path / "lamp.rad").write_text(w.lamp_room())
+    g = golden(fixture)
+    (tmp_path / "lamp.rad").write_text(getattr(w, room)())
     sc = gb.Scene(rad_files=[tmp_path / "lamp.rad"])
     for key, ds in (("ds0", 0.0), ("ds2", 0.2)):
         rgb, _, _ = rtrace_c(gb, sc, opts("rtrace", I=1, ab=0, dj=0, ds=ds, dr=0, dt=0, u=0), g["rays"])

@@ -176,14 +176,17 @@ def test_translucent(tmp_path):
     assert np.abs(z).max() < 5 and abs(z.mean()) < 4 / np.sqrt(n), (np.abs(z).max(), z.mean())
 
 
-def test_circular_sources(scene_dir, tmp_path):
-    """Sphere and disk lights: -I direct irradiance with -ds 0 and with the
+@pytest.mark.parametrize("room,fixture", [("lamp_room", "circular_sources.npz"),
+                                          ("tube_room", "cylinder_sources.npz")])
+def test_circular_sources(scene_dir, tmp_path, room, fixture):
+    """Sphere and disk lights, and cylinder lights (partitioned along their
+    axis, rt/srcsamp.c:187-273): -I direct irradiance with -ds 0 and with the
     disk partitioned (-ds 0.2, pieces trimmed to the circle), 1e-6; with
     jittered samples (-dj 0.9) per-sensor means of 256 replicas within 5
     standard errors of the reference's."""
     from pyradiance_gb300 import workloads as w
-    g = golden("circular_sources.npz")
-    (tmp_path / "lamp.rad").write_text(w.lamp_room())
+    g = golden(fixture)
+    (tmp_path / "lamp.rad").write_text(getattr(w, room)())
     sc = po.Scene(tmp_path / "lamp.rad")
     for key, ds in (("ds0", 0.0), ("ds2", 0.2)):
         o = po.default_opts("rtrace", I=1, ab=0, dj=0, ds=ds, dr=0, dt=0, u=0)
