@@ -64,6 +64,7 @@ int orc_compile_bins(const gb_modspec *mods, int nmods, gb_binins *prog, int pro
 typedef struct {
     int flags;               /* DISTANT 1, SKIP 2, FLAT 4, PROX 8, FOLLOW 16, CIR 32 */
     double sloc[3], snorm[3], ss[3][3], ss2, srad, prox;
+    double spsiz, spaim[3], spflen;    /* spotlight (rt/srcsupp.c:268-288 makespot) */
     int so;                  /* object */
     int mat;                 /* material object */
 } osrc;
@@ -83,6 +84,7 @@ typedef struct {
 #define S_PROX 8
 #define S_CIR 32
 #define S_CYL 64
+#define S_SPOT 128
 
 static void vcross(double r[3], const double a[3], const double b[3])
 {
@@ -255,6 +257,17 @@ static int mark_sources(oscene *O)
             s->prox = mo->farg[3];
             if (s->flags & S_DISTANT)
                 s->flags |= S_SKIP;
+        } else if (mo->otype == GT_SPOT) {           /* rt/source.c:104-116 */
+            int j;
+            double d = 0, d1;
+            s->flags |= S_SPOT;
+            s->spsiz = 2.0 * PI * (1.0 - cos(PI / 180.0 / 2.0 * mo->farg[3]));
+            memcpy(s->spaim, mo->farg + 4, sizeof s->spaim);
+            s->spflen = vnormalize(s->spaim);
+            for (j = 0; j < 3; j++) d += s->spaim[j] * s->snorm[j];
+            d1 = 1. - s->spsiz / (2. * PI);
+            if ((s->flags & S_FLAT) && !(d > FTINY) && !(1. - FTINY - d * d < d1 * d1))
+                s->flags |= S_SKIP;                     /* checkspot: invalid direction */
         }
         O->nsrc++;
     }
@@ -1028,6 +1041,11 @@ static int m_light(ctx *X, int m, RAY *r)
         return 1;
     }
     if (r->rod < 0.0) return 1;
+    if (mo->otype == GT_SPOT) {                      /* rt/source.c:782 spotout (local source) */
+        double aim[3] = {mo->farg[4], mo->farg[5], mo->farg[6]};
+        vnormalize(aim);
+        if (2.0 * PI * (1.0 - cos(PI / 180.0 / 2.0 * mo->farg[3])) < 2.0 * PI * (1.0 + vdot(aim, r->rdir))) return 1;
+    }
     r->rcol[0] = mo->farg[0];
     r->rcol[1] = mo->farg[1];
     r->rcol[2] = mo->farg[2];
@@ -1255,6 +1273,12 @@ static void direct(ctx *X, RAY *r, const NORMDAT *nd)
             if (dom <= 1e-4) continue;
             dom *= s->ss2 / (d * d);
             if ((s->flags & S_PROX) && d > s->prox) continue;
+            if (s->flags & S_SPOT) {                    /* rt/source.c:246-252 */
+                if (s->spsiz < 2.0 * PI * (1.0 + vdot(s->spaim, dir))) continue;
+                dom *= d * d;
+                d += s->spflen;
+                dom /= d * d;
+            }
         }
         dirnorm(X, coef, nd, r, dir, dom);
         if (maxc(coef) <= 0) continue;

@@ -64,6 +64,7 @@ enum { DM_NONE = 0, DM_PLASTIC, DM_METAL, DM_GLASS, DM_LIGHT, DM_GLOW, DM_TRANS 
 #define DS_FOLLOW  0x10
 #define DS_CIR     0x20   /* circular (disk, sphere, distant): SCIR */
 #define DS_CYL     0x40   /* cylinder: SCYL */
+#define DS_SPOT    0x80   /* spotlight: SSPOT */
 
 typedef struct {
     float sloc[3];      /* centre (local) or direction (distant) */
@@ -76,6 +77,8 @@ typedef struct {
     int   so;           /* source object index */
     int   mat;          /* material slot of the source */
     int   pad;
+    float spot[5];      /* spotlight: cone solid angle, unit aim, focus length (rt/srcsupp.c makespot) */
+    float pad2[3];
 } gb_dsrc;
 
 /* An instance (rt/o_instance.c): the transforms to and from its octree's

@@ -172,6 +172,16 @@ static int material_kind(const gb_object *m, float4 *m0, float4 *m1, std::string
         if (m->nfargs != 3) { why = "bad # arguments"; return -1; }
         *m0 = make_float4(DM_LIGHT, f[0], f[1], f[2]);
         return 0;
+    case GT_SPOT: {                              /* a light with a cone (rt/srcsupp.c:268-288 makespot) */
+        if (m->nfargs != 7) { why = "bad # arguments"; return -1; }
+        if (f[3] <= GB_FTINY) { why = "zero angle"; return -1; }
+        double l = sqrt(f[4] * f[4] + f[5] * f[5] + f[6] * f[6]);
+        if (l == 0.0) { why = "zero focus vector"; return -1; }
+        *m0 = make_float4(DM_LIGHT, f[0], f[1], f[2]);
+        *m1 = make_float4((float)(2.0 * M_PI * (1.0 - cos(M_PI / 180.0 / 2.0 * f[3]))), (float)(f[4] / l),
+                          (float)(f[5] / l), (float)(f[6] / l));
+        return 0;
+    }
     case GT_GLOW:
         if (m->nfargs != 4) { why = "bad # arguments"; return -1; }
         *m0 = make_float4(DM_GLOW, f[0], f[1], f[2]);
@@ -393,7 +403,25 @@ static int mark_sources(gb_scene *G)
             s.prox = (float)mo->farg[3];
             if (s.flags & DS_DISTANT)
                 s.flags |= DS_SKIP;
-        } else if (mo->otype == GT_SPOT || mo->otype == GT_ILLUM) {
+        } else if (mo->otype == GT_SPOT) {            /* rt/source.c:104-116 */
+            if (s.flags & DS_DISTANT) {
+                if (G->src_error.empty())
+                    G->src_error = std::string("distant spotlight '") + o->name + "' is not implemented on the GPU path";
+            } else {
+                const double *f = mo->farg;
+                double l = sqrt(f[4] * f[4] + f[5] * f[5] + f[6] * f[6]);
+                s.flags |= DS_SPOT;
+                s.spot[0] = (float)(2.0 * M_PI * (1.0 - cos(M_PI / 180.0 / 2.0 * f[3])));
+                for (int j = 0; j < 3; j++) s.spot[1 + j] = (float)(f[4 + j] / l);
+                s.spot[4] = (float)l;
+                if (s.flags & DS_FLAT) {             /* checkspot (rt/srcsupp.c:452-465) */
+                    double d = 0, d1 = 1. - s.spot[0] / (2. * M_PI);
+                    for (int j = 0; j < 3; j++) d += (f[4 + j] / l) * s.snorm[j];
+                    if (!(d > GB_FTINY) && !(1. - GB_FTINY - d * d < d1 * d1))
+                        s.flags |= DS_SKIP;          /* invalid spotlight direction */
+                }
+            }
+        } else if (mo->otype == GT_ILLUM) {
             if (G->src_error.empty())
                 G->src_error = std::string("light material '") + gb_otype_name(mo->otype) + "' (" + mo->name +
                                ") is not implemented on the GPU path";

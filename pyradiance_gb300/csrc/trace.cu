@@ -308,7 +308,8 @@ __device__ __forceinline__ void light_hit(const gb_run &P, const Ray &r, int obj
     bool wrong = r.rsrc >= 0 && S.src[r.rsrc].so != obj;
     if (bad || wrong)
         rc = f3(0.f, 0.f, 0.f);
-    else if (rod >= 0.f)
+    else if (rod >= 0.f && !(mk == DM_LIGHT && m1.x > 0.f &&       /* a spotlight seen from outside */
+                             m1.x < 2.f * (float)D_PI * (1.f + m1.y * r.dir.x + m1.z * r.dir.y + m1.w * r.dir.z)))
         rcol = col;
     if (rcol_out)
         *rcol_out = rcol;
@@ -772,6 +773,13 @@ __device__ __noinline__ void direct_sample(const gb_run &P, const Ray &r, float3
         dom *= src.ss2 / (dist * dist);
         if ((src.flags & DS_PROX) && dist > src.prox)
             return;
+        if (src.flags & DS_SPOT) {               /* rt/source.c:246-252: outside the cone, none */
+            if (src.spot[0] < 2.f * (float)D_PI * (1.f + src.spot[1] * dir.x + src.spot[2] * dir.y +
+                                                   src.spot[3] * dir.z))
+                return;
+            const float df = dist + src.spot[4];   /* the solid angle seen from the focus */
+            dom *= dist * dist / (df * df);
+        }
     }
     float3 coefd;
     float3 coef = dirnorm(P, s, r.dir, dir, dom, G ? &coefd : nullptr);

@@ -24,7 +24,8 @@ Workloads (sizes are the defaults):
 * ``glossy_room`` -- the room with rough specular plastic and metal
   (the specular-lobe sampling workload).
 * ``lamp_room`` -- the room lit by a sphere and a disk light (circular
-  source shapes); ``tube_room`` -- lit by two cylinder lights.
+  source shapes); ``tube_room`` -- lit by two cylinder lights;
+  ``spot_room`` -- lit by two spotlights.
 * ``trans_room`` -- the room with translucent diffuser and frosted panels.
 * ``furniture``, ``instance_room`` -- an object octree and a room holding
   transformed instances of it (the instance workload).
@@ -283,6 +284,29 @@ def tube_room(seed: int = 0, nboxes: int = 60) -> str:
                f"{Y * .5:.9g} {z:.9g} 0.02\n\n")
     out.append(f"tube_mat cylinder tube_y\n0\n0\n7 {X * .7:.9g} {Y * .5 - .6:.9g} {z:.9g} {X * .7:.9g} "
                f"{Y * .5 + .6:.9g} {z:.9g} 0.02\n\n")
+    return "".join(out)
+
+
+def spot_room(seed: int = 0, nboxes: int = 60) -> str:
+    """The boxes of ``lamp_room`` lit by spotlights: a ceiling panel with a
+    100 degree cone aimed down and tilted, and a sphere with a 140 degree
+    cone aimed down towards +x."""
+    rng = np.random.default_rng(seed)
+    X, Y, Z = ROOM
+    out = [_mat_plastic("room_mat", (0.5, 0.5, 0.5)), _room_shell("room_mat")]
+    sizes = rng.uniform(0.2, 1.2, size=(nboxes, 3))
+    pos = rng.uniform(0.0, 1.0, size=(nboxes, 2))
+    rho = rng.uniform(0.2, 0.7, size=nboxes)
+    for i in range(nboxes):
+        s = sizes[i]
+        out.append(_mat_plastic(f"box_mat{i}", (rho[i],) * 3))
+        out.append(_box(f"box_mat{i}", f"box{i}", (pos[i, 0] * (X - s[0]), pos[i, 1] * (Y - s[1]), 0.005), s))
+    out.append("void spotlight panel_mat\n0\n0\n7 150 150 140 100 0.3 0 -1\n\n")
+    cx, cy = X * 0.35, Y / 2
+    out.append(_poly("panel_mat", "panel", [(cx - .4, cy - .4, Z - 0.01), (cx - .4, cy + .4, Z - 0.01),
+                                            (cx + .4, cy + .4, Z - 0.01), (cx + .4, cy - .4, Z - 0.01)]))
+    out.append("void spotlight bulb_mat\n0\n0\n7 300 280 250 140 1 0 -1.2\n\n")
+    out.append(f"bulb_mat sphere bulb\n0\n0\n4 {X * 0.7:.9g} {Y * 0.5:.9g} {Z - 0.6:.9g} 0.1\n\n")
     return "".join(out)
 
 

@@ -179,6 +179,27 @@ def supersampled_irradiance(tmp: Path, n: int = 100, K: int = 512) -> None:
     print("supersampled: mean %.4g (as 512) vs %.4g (as 0)" % (out["as512_mean"].mean(), out["as0_mean"].mean()))
 
 
+def spotlights(tmp: Path) -> None:
+    """Spotlights (rt/srcsupp.c makespot, spotout; rt/source.c:246-252 and
+    782): -I direct irradiance on grids at 0.8 m and 2.3 m, and the
+    radiance of view rays aimed at the lights' centres from random points
+    (lit only from inside the cones), deterministic (-ab 0 -dj 0 -ds 0)."""
+    octp = oconv(w.spot_room(), tmp, "spot")
+    grid = np.vstack([w.sensor_grid(40, 40), w.sensor_grid(20, 20, z=2.3)])
+    rng = np.random.default_rng(19)
+    org = rng.uniform((0.3, 0.3, 0.1), (9.7, 7.7, 2.0), size=(1000, 3))
+    tgt = np.array([[3.5, 4.0, 2.985], [7.0, 4.0, 2.4]])[np.arange(1000) % 2]
+    d = tgt - org
+    view = np.hstack([org, d / np.linalg.norm(d, axis=1, keepdims=True)])
+    base = ["rtrace", "-h", "-u-", "-ab", "0", "-dj", "0", "-ds", "0", "-dr", "0", "-dt", "0", "-fdd", "-ov"]
+    irr = np.frombuffer(run([*base, "-I", octp], grid.astype("<f8").tobytes()), dtype="<f8").reshape(-1, 3)
+    rad = np.frombuffer(run([*base, octp], view.astype("<f8").tobytes()), dtype="<f8").reshape(-1, 3)
+    np.savez_compressed(OUT / "spotlights.npz", grid=grid, irradiance=irr, view=view, radiance=rad,
+                        cmd="rtrace -h -u- -ab 0 -dj 0 -ds 0 -dr 0 -dt 0 -fdd -ov [-I]")
+    print("spotlights: lit %.3f, irradiance mean %.4g, view lit %.3f" % ((irr[:, 0] > 0).mean(), irr.mean(),
+                                                                        (rad[:, 0] > 50).mean()))
+
+
 def general_bins(tmp: Path) -> None:
     """General bin expressions: the sky subdivision of
     tests/golden/patchbins.cal (recursion, select, if, asin, atan2, floor,
@@ -389,6 +410,7 @@ def main() -> None:
     parts = {"octree": octree_digests, "c1": c1_direct, "c1p": c1_partitioned, "zoo": zoo, "glossy": glossy, "irr": surface_irradiance,
              "ss": supersampled_irradiance, "inst": instances, "circ": circular_sources,
              "trans": translucent, "bins": general_bins,
+             "spot": spotlights,
              "dct": lambda tmp: dct_small(), "trace_oct": lambda tmp: ref_fixture_trace(),
              "c2ab1": lambda tmp: c2_stats(tmp, ab=1, K=256), "c2ab3": lambda tmp: c2_stats(tmp, ab=3, K=256)}
     only = sys.argv[1:] or list(parts)         # e.g. make_golden.py c1p

@@ -373,6 +373,20 @@ def test_circular_sources(gb, tmp_path, room, fixture):
     assert np.abs(z).max() < 5 and abs(z.mean()) < 4 / np.sqrt(n)
 
 
+def test_spotlights(gb, tmp_path):
+    """Spotlights (rt/srcsupp.c makespot, spotout): -I direct irradiance
+    and view rays at the lights within 1e-5 for 99.5% (a sample on a cone's
+    edge within FP32 rounding may fall on the other side)."""
+    from pyradiance_gb300 import workloads as w
+    g = golden("spotlights.npz")
+    (tmp_path / "spot.rad").write_text(w.spot_room())
+    sc = gb.Scene(rad_files=[tmp_path / "spot.rad"])
+    for key, rays, I in (("irradiance", g["grid"], 1), ("radiance", g["view"], 0)):
+        rgb, _, _ = rtrace_c(gb, sc, opts("rtrace", I=I, ab=0, dj=0, ds=0, dr=0, dt=0, u=0), rays)
+        rel = np.abs(rgb - g[key]).max(1) / np.maximum(np.abs(g[key]).max(1), 1e-9)
+        assert (rel <= 1e-5).mean() >= 0.995, (key, np.sort(rel)[-5:])
+
+
 def test_instances(gb):
     """Instanced octrees (rt/o_instance.c:15-71): the furniture octree 12
     times in the room, rotated, scaled, mirrored, some with their own

@@ -201,6 +201,22 @@ def test_circular_sources(scene_dir, tmp_path, room, fixture):
     assert np.abs(z).max() < 5 and abs(z.mean()) < 4 / np.sqrt(n), (np.abs(z).max(), z.mean())
 
 
+def test_spotlights(tmp_path):
+    """Spotlights: -I direct irradiance (samples outside a cone dropped,
+    the solid angle seen from the focus) and view rays at the lights (lit
+    only from inside the cones), 1e-6."""
+    from pyradiance_gb300 import workloads as w
+    g = golden("spotlights.npz")
+    (tmp_path / "spot.rad").write_text(w.spot_room())
+    sc = po.Scene(tmp_path / "spot.rad")
+    o = po.default_opts("rtrace", I=1, ab=0, dj=0, ds=0, dr=0, dt=0, u=0)
+    rgb, _, _, _ = po.rtrace(sc, o, g["grid"], hits=False, threads=8)
+    np.testing.assert_allclose(rgb, g["irradiance"], rtol=1e-6, atol=1e-9)
+    o.I = 0
+    rgb, _, _, _ = po.rtrace(sc, o, g["view"], hits=False, threads=8)
+    np.testing.assert_allclose(rgb, g["radiance"], rtol=1e-6, atol=1e-9)
+
+
 def test_instances():
     """Instanced octrees (rt/o_instance.c:15-71, common/instance.c,
     common/xf.c): the furniture octree 12 times in the room, rotated,
