@@ -1806,6 +1806,24 @@ static int m_glass(ctx *X, int m, RAY *r)
     return 1;
 }
 
+/* rt/m_mirror.c m_mirror (no substitute material, no virtual sources):
+ * shadow rays stop, the back is black, else the reflected ray */
+static int m_mirror(ctx *X, int m, RAY *r)
+{
+    const gb_object *mo = &X->O->H.objs[m];
+    RAY nr;
+    int i;
+    if (r->rsrc >= 0 && X->O->src[r->rsrc].so != r->ro) return 1;
+    if (r->rod < 0.) return 1;
+    if (rayorigin(X, &nr, GB_REFLECTED, r, mo->farg, GB_C_REFL) < 0) return 1;
+    for (i = 0; i < 3; i++) nr.rdir[i] = r->rdir[i] + 2. * r->rod * r->ron[i];
+    vnormalize(nr.rdir);
+    rayclear(&nr);
+    raytrace(X, &nr);
+    for (i = 0; i < 3; i++) r->rcol[i] += nr.rcol[i] * nr.rcoef[i];
+    return 1;
+}
+
 /* rayshade with the material found for object r->ro */
 static void rayshade(ctx *X, RAY *r)
 {
@@ -1822,6 +1840,7 @@ static void rayshade(ctx *X, RAY *r)
     if (gb_is_light(t)) m_light(X, m, r);
     else if (t == GT_GLASS) m_glass(X, m, r);
     else if (t == GT_PLASTIC || t == GT_METAL || t == GT_TRANS) m_normal(X, m, r);
+    else if (t == GT_MIRROR) m_mirror(X, m, r);
     else raytrans(X, r);
 }
 

@@ -54,7 +54,7 @@ static inline int gb_leaf_code(int off, int size)
 }
 
 /* material kinds on the device */
-enum { DM_NONE = 0, DM_PLASTIC, DM_METAL, DM_GLASS, DM_LIGHT, DM_GLOW, DM_TRANS };
+enum { DM_NONE = 0, DM_PLASTIC, DM_METAL, DM_GLASS, DM_LIGHT, DM_GLOW, DM_TRANS, DM_MIRROR };
 
 /* source flags (rt/source.h:24-37) */
 #define DS_DISTANT 0x01

@@ -158,6 +158,11 @@ static int material_kind(const gb_object *m, float4 *m0, float4 *m1, std::string
         *m0 = make_float4(m->otype == GT_PLASTIC ? DM_PLASTIC : DM_METAL, f[0], f[1], f[2]);
         *m1 = make_float4(f[3], f[4], 0, 0);
         return 0;
+    case GT_MIRROR:                              /* rt/m_mirror.c: 3 arguments, no substitute */
+        if (m->nfargs != 3) { why = "bad number of arguments"; return -1; }
+        if (m->nsargs > 0) { why = "mirror with a substitute material is not implemented on the GPU path"; return -1; }
+        *m0 = make_float4(DM_MIRROR, f[0], f[1], f[2]);
+        return 0;
     case GT_TRANS:                               /* rt/normal.c: 7 arguments */
         if (m->nfargs != 7) { why = "bad number of arguments"; return -1; }
         *m0 = make_float4(DM_TRANS, f[0], f[1], f[2]);
@@ -1032,6 +1037,17 @@ static int check_shading(gb_scene *G, const gb_opts *o)
         return set_err(GB_EUNSUPPORTED, "-dv- is not implemented");
     if (o->ld != 0)
         return set_err(GB_EUNSUPPORTED, "-ld is not implemented");
+    /* mirrors relay sources as virtual sources under -dr (rt/virtuals.c),
+     * which is not built: only -dr 0, or mirrors on curved surfaces (which
+     * make none) */
+    if (o->dr > 0 && !G->src.empty())
+        for (int32_t i = 0; i < G->H.nobjs; i++) {
+            const int ms = G->matslot[i];
+            if (ms >= 0 && (int)G->mat[2 * ms].x == DM_MIRROR &&
+                (G->H.objs[i].otype == GT_POLYGON || G->H.objs[i].otype == GT_RING))
+                return set_err(GB_EUNSUPPORTED, "virtual sources of mirror \"%s\" (-dr %d) are not implemented; "
+                               "use -dr 0", G->H.objs[i].name, o->dr);
+        }
     /* -ds: flat local sources are partitioned, spheres are one piece
      * (rt/srcsupp.c:36 sphsobj nopart), as in the reference */
     /* rough specular sampled with several samples per hit (-ss > 1.5,
@@ -1550,9 +1566,9 @@ extern "C" int gb_rtrace_grad(gb_scene *G, const gb_opts *o, const double *org_d
         return set_err(GB_EINVAL, "the gradient has %lld material slots, the scene %lld", (long long)nslots,
                        (long long)G->matobj.size());
     for (size_t sl = 0; sl < G->matobj.size(); sl++)
-        if ((int)G->mat[2 * sl].x == DM_TRANS)
-            return set_err(GB_EUNSUPPORTED, "gradients through trans materials (\"%s\") are not implemented",
-                           G->H.objs[G->matobj[sl]].name);
+        if ((int)G->mat[2 * sl].x == DM_TRANS || (int)G->mat[2 * sl].x == DM_MIRROR)
+            return set_err(GB_EUNSUPPORTED, "gradients through trans and mirror materials (\"%s\") are not "
+                           "implemented", G->H.objs[G->matobj[sl]].name);
     int rc = check_shading(G, o);
     if (rc < 0)
         return rc;

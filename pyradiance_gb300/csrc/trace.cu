@@ -1299,6 +1299,20 @@ __device__ void shade_ray(const gb_run &P, const Ray &r, const Hit &h, Counters 
         }
         return;
     }
+    if (mk == DM_MIRROR) {                       /* rt/m_mirror.c: black from behind, else reflected */
+        if (h.rod < 0.f)
+            return;
+        Ray c;
+        if (ray_origin(P, r, GB_REFLECTED, f3(m0.y, m0.z, m0.w), true, GB_C_REFL, c, nullptr)) {
+            c.org = hp;
+            c.dir = normalize3(r.dir + h.n * (2.f * h.rod));
+            c.origin = h.obj;
+            if (G)
+                c.adj = r.adj;
+            push_ray<G>(P, c);
+        }
+        return;
+    }
     /* plastic / metal */
     int okd = S.obj[ro].x & 0xff;
     Surf su;

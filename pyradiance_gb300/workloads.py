@@ -25,7 +25,7 @@ Workloads (sizes are the defaults):
   (the specular-lobe sampling workload).
 * ``lamp_room`` -- the room lit by a sphere and a disk light (circular
   source shapes); ``tube_room`` -- lit by two cylinder lights;
-  ``spot_room`` -- lit by two spotlights.
+  ``spot_room`` -- lit by two spotlights; ``mirror_room`` -- with mirrors.
 * ``trans_room`` -- the room with translucent diffuser and frosted panels.
 * ``furniture``, ``instance_room`` -- an object octree and a room holding
   transformed instances of it (the instance workload).
@@ -307,6 +307,32 @@ def spot_room(seed: int = 0, nboxes: int = 60) -> str:
                                             (cx + .4, cy + .4, Z - 0.01), (cx + .4, cy - .4, Z - 0.01)]))
     out.append("void spotlight bulb_mat\n0\n0\n7 300 280 250 140 1 0 -1.2\n\n")
     out.append(f"bulb_mat sphere bulb\n0\n0\n4 {X * 0.7:.9g} {Y * 0.5:.9g} {Z - 0.6:.9g} 0.1\n\n")
+    return "".join(out)
+
+
+def mirror_room(seed: int = 0, nboxes: int = 60) -> str:
+    """The boxes of ``lamp_room`` under the ceiling light of
+    ``daylight_room``, with two wall mirrors (one tinted) and a mirror
+    sphere."""
+    rng = np.random.default_rng(seed)
+    X, Y, Z = ROOM
+    out = [_mat_plastic("room_mat", (0.5, 0.5, 0.5)), _room_shell("room_mat"),
+           "void mirror silver\n0\n0\n3 .9 .9 .9\n\n", "void mirror bronze\n0\n0\n3 .8 .6 .4\n\n"]
+    sizes = rng.uniform(0.2, 1.2, size=(nboxes, 3))
+    pos = rng.uniform(0.0, 1.0, size=(nboxes, 2))
+    rho = rng.uniform(0.2, 0.7, size=nboxes)
+    for i in range(nboxes):
+        s = sizes[i]
+        out.append(_mat_plastic(f"box_mat{i}", (rho[i],) * 3))
+        out.append(_box(f"box_mat{i}", f"box{i}", (pos[i, 0] * (X - s[0]), pos[i, 1] * (Y - s[1]), 0.005), s))
+    out.append(_poly("silver", "mirror_w", [(0.01, 2, 0.5), (0.01, 2, 2.5), (0.01, 6, 2.5), (0.01, 6, 0.5)]))
+    out.append(_poly("bronze", "mirror_n", [(3, Y - 0.01, 0.5), (7, Y - 0.01, 0.5), (7, Y - 0.01, 2.5),
+                                            (3, Y - 0.01, 2.5)]))
+    out.append(f"silver sphere ball\n0\n0\n4 {X * 0.6:.9g} {Y * 0.4:.9g} 1.8 0.3\n\n")
+    out.append("void light light_mat\n0\n0\n3 100 100 100\n\n")
+    cx, cy = X / 2, Y / 2
+    out.append(_poly("light_mat", "light", [(cx - .5, cy - .5, Z - 0.01), (cx - .5, cy + .5, Z - 0.01),
+                                            (cx + .5, cy + .5, Z - 0.01), (cx + .5, cy - .5, Z - 0.01)]))
     return "".join(out)
 
 

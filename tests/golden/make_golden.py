@@ -200,6 +200,21 @@ def spotlights(tmp: Path) -> None:
                                                                         (rad[:, 0] > 50).mean()))
 
 
+def mirrors(tmp: Path) -> None:
+    """The mirror material (rt/m_mirror.c without virtual sources, -dr 0):
+    -I direct irradiance (mirrors block shadow rays) and the radiance of
+    random view rays (mirror chains), deterministic."""
+    octp = oconv(w.mirror_room(), tmp, "mirror")
+    grid = w.sensor_grid(40, 40)
+    view = w.random_rays(2000, seed=23)
+    base = ["rtrace", "-h", "-u-", "-ab", "0", "-dj", "0", "-ds", "0", "-dr", "0", "-dt", "0", "-fdd", "-ov"]
+    irr = np.frombuffer(run([*base, "-I", octp], grid.astype("<f8").tobytes()), dtype="<f8").reshape(-1, 3)
+    rad = np.frombuffer(run([*base, octp], view.astype("<f8").tobytes()), dtype="<f8").reshape(-1, 3)
+    np.savez_compressed(OUT / "mirrors.npz", grid=grid, irradiance=irr, view=view, radiance=rad,
+                        cmd="rtrace -h -u- -ab 0 -dj 0 -ds 0 -dr 0 -dt 0 -fdd -ov [-I]")
+    print("mirrors: irradiance mean %.4g, radiance mean %.4g" % (irr.mean(), rad.mean()))
+
+
 def general_bins(tmp: Path) -> None:
     """General bin expressions: the sky subdivision of
     tests/golden/patchbins.cal (recursion, select, if, asin, atan2, floor,
@@ -410,7 +425,7 @@ def main() -> None:
     parts = {"octree": octree_digests, "c1": c1_direct, "c1p": c1_partitioned, "zoo": zoo, "glossy": glossy, "irr": surface_irradiance,
              "ss": supersampled_irradiance, "inst": instances, "circ": circular_sources,
              "trans": translucent, "bins": general_bins,
-             "spot": spotlights,
+             "spot": spotlights, "mirror": mirrors,
              "dct": lambda tmp: dct_small(), "trace_oct": lambda tmp: ref_fixture_trace(),
              "c2ab1": lambda tmp: c2_stats(tmp, ab=1, K=256), "c2ab3": lambda tmp: c2_stats(tmp, ab=3, K=256)}
     only = sys.argv[1:] or list(parts)         # e.g. make_golden.py c1p

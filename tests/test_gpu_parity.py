@@ -387,6 +387,24 @@ def test_spotlights(gb, tmp_path):
         assert (rel <= 1e-5).mean() >= 0.995, (key, np.sort(rel)[-5:])
 
 
+def test_mirrors(gb, tmp_path):
+    """Mirrors (rt/m_mirror.c) with -dr 0: -I irradiance and view rays
+    through mirror chains (1e-4 for 99.5%, as for mirror chains in the
+    shape zoo); with -dr above 0 the virtual sources of flat mirrors are
+    refused."""
+    from pyradiance_gb300 import workloads as w
+    from pyradiance_gb300 import _lib
+    g = golden("mirrors.npz")
+    (tmp_path / "mirror.rad").write_text(w.mirror_room())
+    sc = gb.Scene(rad_files=[tmp_path / "mirror.rad"])
+    for key, rays, I in (("irradiance", g["grid"], 1), ("radiance", g["view"], 0)):
+        rgb, _, _ = rtrace_c(gb, sc, opts("rtrace", I=I, ab=0, dj=0, ds=0, dr=0, dt=0, u=0), rays)
+        rel = np.abs(rgb - g[key]).max(1) / np.maximum(np.abs(g[key]).max(1), 1e-9)
+        assert (rel <= 1e-4).mean() >= 0.995, (key, np.sort(rel)[-5:])
+    with pytest.raises(_lib.GbError):
+        rtrace_c(gb, sc, opts("rtrace", ab=0, dr=2, u=0), g["view"][:4])
+
+
 def test_instances(gb):
     """Instanced octrees (rt/o_instance.c:15-71): the furniture octree 12
     times in the room, rotated, scaled, mirrored, some with their own

@@ -217,6 +217,21 @@ def test_spotlights(tmp_path):
     np.testing.assert_allclose(rgb, g["radiance"], rtol=1e-6, atol=1e-9)
 
 
+def test_mirrors(tmp_path):
+    """Mirrors with -dr 0: -I irradiance (mirrors block shadow rays) and
+    view rays through mirror chains, 1e-6."""
+    from pyradiance_gb300 import workloads as w
+    g = golden("mirrors.npz")
+    (tmp_path / "mirror.rad").write_text(w.mirror_room())
+    sc = po.Scene(tmp_path / "mirror.rad")
+    o = po.default_opts("rtrace", I=1, ab=0, dj=0, ds=0, dr=0, dt=0, u=0)
+    rgb, _, _, _ = po.rtrace(sc, o, g["grid"], hits=False, threads=8)
+    np.testing.assert_allclose(rgb, g["irradiance"], rtol=1e-6, atol=1e-9)
+    o.I = 0
+    rgb, _, _, _ = po.rtrace(sc, o, g["view"], hits=False, threads=8)
+    np.testing.assert_allclose(rgb, g["radiance"], rtol=1e-6, atol=1e-9)
+
+
 def test_instances():
     """Instanced octrees (rt/o_instance.c:15-71, common/instance.c,
     common/xf.c): the furniture octree 12 times in the room, rotated,
