@@ -79,7 +79,9 @@ typedef struct gb_scene gb_scene;
  * call of rt/rtmain.c and rt/rcmain.c:352). */
 int  gb_scene_load(const char *oct_path, gb_scene **out);
 /* Build the octree from scene text files as oconv does (ot/oconv.c:42-180),
- * then load it.  objlim <= 0 and resolu <= 0 select oconv's 6 and 16384. */
+ * then load it.  objlim <= 0 and resolu <= 0 select oconv's 6 and 16384.
+ * An octree among the paths contributes its objects (oconv -i, as rfluxmtx
+ * runs it: util/rfluxmtx.c:139-178). */
 int  gb_scene_load_rad(const char *const *paths, int npaths, int objlim, int resolu, gb_scene **out);
 void gb_scene_free(gb_scene *scene);
 /* Number of objects; name, modifier name and material name of an object

@@ -1,5 +1,5 @@
 # Builds the reference Radiance programs that pin the oracle: rtrace, rcontrib,
-# oconv and dctimestep, compiled straight from the reference's own C sources
+# oconv, dctimestep and rfluxmtx, compiled straight from the reference's own C sources
 # (read in place, never copied) with the reference's release flags.
 #
 #   make -f oracle/build_ref.mk REF=/root/reference -j8
@@ -45,9 +45,11 @@ LIBRTRAD := $(OBJ)/librtrad.a
 LIBRAD   := $(OBJ)/libradiance.a
 LIBRL    := $(OBJ)/libraycalls.a
 
-all: $(OUT)/bin/rtrace $(OUT)/bin/rcontrib $(OUT)/bin/oconv $(OUT)/bin/dctimestep
-	@cp $(RAD)/rt/rayinit.cal $(RAD)/util/reinhartb.cal $(OUT)/lib/ 2>/dev/null || \
-	  (mkdir -p $(OUT)/lib && cp $(RAD)/rt/rayinit.cal $(RAD)/util/reinhartb.cal $(OUT)/lib/)
+CALS := $(RAD)/rt/rayinit.cal $(RAD)/util/reinhartb.cal $(RAD)/util/klems_full.cal $(RAD)/util/klems_half.cal \
+        $(RAD)/util/klems_quarter.cal
+
+all: $(OUT)/bin/rtrace $(OUT)/bin/rcontrib $(OUT)/bin/oconv $(OUT)/bin/dctimestep $(OUT)/bin/rfluxmtx
+	@mkdir -p $(OUT)/lib && cp $(CALS) $(OUT)/lib/
 
 $(OBJ)/common/%.o: $(RAD)/common/%.c
 	@mkdir -p $(@D)
@@ -79,6 +81,9 @@ $(OUT)/bin/rcontrib: $(addprefix $(OBJ)/rt/,rcmain.o rcontrib.o rc2.o rc3.o) $(L
 	@mkdir -p $(@D)
 	$(CXX) -o $@ $^ -lm
 $(OUT)/bin/oconv: $(addprefix $(OBJ)/ot/,bbox.o initotypes.o o_cone.o o_face.o o_instance.o oconv.o sphere.o writeoct.o) $(LIBRTRAD)
+	@mkdir -p $(@D)
+	$(CXX) -o $@ $^ -lm
+$(OUT)/bin/rfluxmtx: $(OBJ)/util/rfluxmtx.o $(LIBRTRAD)
 	@mkdir -p $(@D)
 	$(CXX) -o $@ $^ -lm
 $(OUT)/bin/dctimestep: $(addprefix $(OBJ)/util/,dctimestep.o cmbsdf.o cmconst.o cmatrix.o) $(LIBRTRAD)

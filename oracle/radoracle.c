@@ -992,6 +992,30 @@ static void trace_contrib(ctx *X, const RAY *r)
                 pc += 2;
                 break;
             }
+            case GB_OP_KBIN: {
+                /* util/klems_full.cal:10-40 (and klems_half.cal, klems_quarter.cal) */
+                static const double fp[9] = {5, 15, 25, 35, 45, 55, 65, 75, 90}, fn[9] = {1, 8, 16, 20, 24, 24, 24, 16, 12};
+                static const double hp[7] = {6.5, 19.5, 32.5, 45.5, 58.5, 71.5, 90}, hn[7] = {1, 8, 12, 16, 20, 12, 8};
+                static const double qp[5] = {9, 27, 45, 63, 90}, qn[5] = {1, 8, 12, 12, 8};
+                const gb_binins *q = pr + pc + 1;
+                int kind = (int)q[0].op, nrow = kind == 1 ? 9 : kind == 2 ? 7 : 5, row = 0;
+                const double *pola = kind == 1 ? fp : kind == 2 ? hp : qp, *naz = kind == 1 ? fn : kind == 2 ? hn : qn;
+                double RHS = q[0].a, Nx = q[0].b, Ny = q[0].c, Nz = q[1].op, Ux = q[1].a, Uy = q[1].b, Uz = q[1].c;
+                double Dx = r->rdir[0], Dy = r->rdir[1], Dz = r->rdir[2], DEG = PI / 180;
+                double c = -Dx * Nx - Dy * Ny - Dz * Nz;
+                double pol = c - 1 > 0 ? 0 : (-1 - c > 0 ? 180 : acos(c) / DEG);
+                if (pol - 90 > 0) st[sp++] = -1;
+                else {
+                    double y = -Dx * Ux - Dy * Uy - Dz * Uz + (Nx * Dx + Ny * Dy + Nz * Dz) * (Nx * Ux + Ny * Uy + Nz * Uz);
+                    double x = -RHS * (Dx * (Uy * Nz - Uz * Ny) + Dy * (Uz * Nx - Ux * Nz) + Dz * (Ux * Ny - Uy * Nx));
+                    double a = atan2(y, x), azi = (-a > 0 ? a + 2 * PI : a) / DEG, acc = 0, inc;
+                    while (row < nrow - 1 && pol - pola[row] > 0) acc += naz[row++];
+                    inc = 360 / naz[row];
+                    st[sp++] = acc + ((360 - .5 * inc) - azi > 0 ? floor((azi + .5 * inc) / inc) : 0);
+                }
+                pc += 2;
+                break;
+            }
             default: return;
             }
         }

@@ -20,7 +20,7 @@ import numpy as np
 from . import _lib
 from ._lib import GbError, GbModspec, Scene, check, last_stats, lib, parse_opts, ptr
 
-__all__ = ["rtrace", "Rcontrib", "dctimestep", "Scene", "load_scene", "read_rays", "GbError", "last_stats"]
+__all__ = ["rtrace", "Rcontrib", "dctimestep", "rfluxmtx", "Scene", "load_scene", "read_rays", "GbError", "last_stats"]
 
 _SCENES: dict = {}
 
@@ -76,7 +76,7 @@ def read_rays(data: bytes, fmt: str) -> np.ndarray:
     raise RuntimeError(f"Illegal i/o format: {fmt}")
 
 
-def _header(prog: str, args: list[str], octree, fmt: str, ncomp: int | None) -> bytes:
+def _header(prog: str, args: list[str], octree, fmt: str, ncomp: int | None, extra: list[str] | None = None) -> bytes:
     lines = ["#?RADIANCE"]
     if octree is not None and not isinstance(octree, (Scene, list, tuple)):
         try:
@@ -95,6 +95,7 @@ def _header(prog: str, args: list[str], octree, fmt: str, ncomp: int | None) -> 
     lines.append(time.strftime("GMT= %Y:%m:%d %H:%M:%S", time.gmtime(now)))
     if ncomp:
         lines.append(f"NCOMP={ncomp}")
+    lines.extend(extra or [])
     if fmt in ("f", "d"):
         lines.append("BigEndian=0")
     name = {"a": "ascii", "f": "float", "d": "double", "c": "32-bit_rle_rgbe"}[fmt]
@@ -352,8 +353,13 @@ class Rcontrib:
         fout = opts.fout.decode()
         parts = []
         if opts.h:
+            extra = []                                      # rt/rc2.c:158-166
+            if opts.y > 0:
+                extra.append(f"NROWS={opts.y * max(opts.x, 1)}")
+            if opts.x <= 0 or arr.shape[1] > 1:
+                extra.append(f"NCOLS={arr.shape[1]}")
             parts.append(_header("rcontrib", self.args + [a for m in self.mods for a in ("-m", m["modifier"])],
-                                 self.octree, fout, 3))
+                                 self.octree, fout, 3, extra))
         if fout == "a":
             flat = arr.reshape(arr.shape[0], -1)
             parts.append("".join("".join(f"{x:.6e}\t" for x in row) + "\n" for row in flat).encode())
@@ -460,3 +466,7 @@ def _dctimestep(*mtx, nstep: int | None = None, header: bool = True, xres: int |
 
 
 dctimestep = _wrap(_dctimestep)
+
+from .rflux import _rfluxmtx  # noqa: E402
+
+rfluxmtx = _wrap(_rfluxmtx)

@@ -17,7 +17,10 @@
  *    select, floor, ceil, sqrt, exp, log, log10, sin, cos, tan, asin, acos,
  *    atan, atan2, max, min;
  *  - the ray direction Dx, Dy, Dz and PI;
- *  - the Reinhart sky bins of util/reinhartb.cal (rbin, Nrbins) built in.
+ *  - the Reinhart sky bins of util/reinhartb.cal (rbin, Nrbins) built in;
+ *  - the LBNL/Klems full, half and quarter bases of util/klems_full.cal,
+ *    klems_half.cal and klems_quarter.cal (kbin, khbin, kqbin with their bin
+ *    counts) built in: rfluxmtx receivers name these files.
  *
  * Calls are expanded where they are used (partial evaluation): arguments
  * that are constants are substituted and folded, so recursion on constant
@@ -45,7 +48,7 @@ using NP = std::shared_ptr<Node>;
 
 struct Node {
     enum Kind {
-        NUM, DX, DY, DZ, NEG, ADD, SUB, MUL, DIV, POW, IF, FN1, ATAN2, MAXN, MINN, SELECT, FLOOR, RBIN,
+        NUM, DX, DY, DZ, NEG, ADD, SUB, MUL, DIV, POW, IF, FN1, ATAN2, MAXN, MINN, SELECT, FLOOR, RBIN, KBIN,
         TEMP, LET,              /* residual only: temporary t, and let t = a[0] in a[1] */
         VAR, CALL               /* parsed only */
     } k;
@@ -73,6 +76,7 @@ struct Def {
 struct Ctx {
     std::map<std::string, Def> defs;
     bool reinhart = false;
+    int klems = 0;              /* 1, 2, 4: built-in full, half, quarter Klems bins */
     std::string err;
     int temps = 0;
     NP fail(const std::string &m)
@@ -305,6 +309,22 @@ struct Eval {
         }
     }
 
+    static std::string klems_fn(int kind) { return kind == 1 ? "kbin" : kind == 2 ? "khbin" : "kqbin"; }
+
+    /* A Klems bin of the built-in basis for a constant normal and up vector;
+     * RHS (+1 right-handed, -1 left-handed) comes from the parameters. */
+    NP klems_node(const std::vector<NP> &a)
+    {
+        NP rhs = C.defs.count("RHS") ? var("RHS", Env()) : num(1);
+        if (!rhs) return nullptr;
+        if (!isnum(rhs)) return C.fail("RHS must be constant");
+        NP n = mk(Node::KBIN);
+        n->a.push_back(num(C.klems));
+        n->a.push_back(rhs);
+        for (auto &x : a) n->a.push_back(x);
+        return n;
+    }
+
     NP var(const std::string &name, const Env &env)
     {
         auto e = env.find(name);
@@ -323,6 +343,21 @@ struct Eval {
                 n->a.push_back(v);
             }
             return n;
+        }
+        if (C.klems && !C.defs.count(name)) {
+            /* Nkbins / Nkhbins / Nkqbins, and the full basis's kbinN, kbinE,
+             * kbinS, kbinW (walls, up +Z) and kbinD (skylight, up +Y) */
+            const std::string fn = klems_fn(C.klems);
+            if (name == "N" + fn + "s") return num(C.klems == 1 ? 145 : C.klems == 2 ? 77 : 41);
+            static const struct { const char *suf; double v[6]; } pre[5] = {
+                {"N", {0, -1, 0, 0, 0, 1}}, {"E", {-1, 0, 0, 0, 0, 1}}, {"S", {0, 1, 0, 0, 0, 1}},
+                {"W", {1, 0, 0, 0, 0, 1}}, {"D", {0, 0, -1, 0, 1, 0}}};
+            for (auto &q : pre)
+                if (C.klems == 1 && name == fn + q.suf) {
+                    std::vector<NP> a;
+                    for (double v : q.v) a.push_back(num(v));
+                    return klems_node(a);
+                }
         }
         if (C.reinhart && name == "Nrbins") {
             NP mf = var("MF", Env());
@@ -422,6 +457,12 @@ struct Eval {
         }
         if (f == "rand")
             return C.fail("rand() is not supported in bin expressions");
+        if (C.klems && f == klems_fn(C.klems) && !C.defs.count(f)) {
+            if (na != 6) return C.fail(f + "() takes a normal and an up vector");
+            if (!eval_args()) return nullptr;
+            if (!allnum()) return C.fail(f + "() needs constant normal and up vectors");
+            return klems_node(args);
+        }
         auto d = C.defs.find(f);
         if (d == C.defs.end())
             return C.fail("function '" + f + "' is not defined");
@@ -497,10 +538,10 @@ struct Emitter {
                 (float)(n->k == Node::SELECT ? k - 1 : k), 1 - k);
             return;
         }
-        case Node::RBIN: {
+        case Node::RBIN: case Node::KBIN: {
             float p[8];
             for (int i = 0; i < 8; i++) p[i] = (float)n->a[i]->v;
-            put(GB_OP_RBIN, 0, 1);
+            put(n->k == Node::RBIN ? GB_OP_RBIN : GB_OP_KBIN, 0, 1);
             out.push_back({p[0], p[1], p[2], p[3]});
             out.push_back({p[4], p[5], p[6], p[7]});
             return;
@@ -538,6 +579,12 @@ int gb_compile_bin(const char *binv, const char *params, const char *calfile, co
         b = b ? b + 1 : calfile;
         if (!strcmp(b, "reinhartb.cal") || !strcmp(b, "reinhart.cal"))
             C.reinhart = true;
+        else if (!strcmp(b, "klems_full.cal"))
+            C.klems = 1;
+        else if (!strcmp(b, "klems_half.cal"))
+            C.klems = 2;
+        else if (!strcmp(b, "klems_quarter.cal"))
+            C.klems = 4;
         else {
             FILE *fp = fopen(calfile, "r");
             if (!fp) { err = std::string("cannot open function file \"") + calfile + "\""; return -1; }

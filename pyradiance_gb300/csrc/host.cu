@@ -795,6 +795,22 @@ extern "C" int gb_scene_load(const char *oct_path, gb_scene **out)
     return finish_load(G, out);
 }
 
+/* An octree among the scene files (oconv -i): its objects join the others
+ * and the octree is built again over all of them. */
+static bool is_octree_file(const char *path)
+{
+    FILE *fp = fopen(path, "rb");
+    if (!fp)
+        return false;
+    char buf[4096];
+    size_t n = fread(buf, 1, sizeof buf - 1, fp);
+    fclose(fp);
+    buf[n] = '\0';
+    const char *end = strstr(buf, "\n\n");
+    const char *f = strstr(buf, "FORMAT=Radiance_octree");
+    return !strncmp(buf, "#?RADIANCE", 10) && f && (!end || f < end);
+}
+
 extern "C" int gb_scene_load_rad(const char *const *paths, int npaths, int objlim, int resolu, gb_scene **out)
 {
     if (!paths || npaths <= 0 || !out)
@@ -802,7 +818,7 @@ extern "C" int gb_scene_load_rad(const char *const *paths, int npaths, int objli
     gb_scene *G = new gb_scene();
     gb_scene_init(&G->H);
     for (int i = 0; i < npaths; i++)
-        if (gb_scene_read_rad_file(&G->H, paths[i]) < 0) {
+        if ((is_octree_file(paths[i]) ? gb_scene_read_oct(&G->H, paths[i]) : gb_scene_read_rad_file(&G->H, paths[i])) < 0) {
             int rc = set_err(GB_EIO, "%s", gb_scene_error());
             gb_scene_free(G);
             return rc;

@@ -858,6 +858,40 @@ GB_DFN float reinhart_bin(float Dx, float Dy, float Dz, const gb_binins *p)
     return acc + azn;
 }
 
+/* Klems bin of the LBNL/Klems full, half or quarter basis for the incident
+ * direction -D about normal N with up vector U (util/klems_full.cal:10-40,
+ * klems_half.cal, klems_quarter.cal): the polar angle picks the ring (the
+ * first whose upper bound is not below it, the last ring otherwise) and the
+ * azimuth the patch, patches centred on azimuth 0; -1 behind the surface.
+ */
+GB_DFN float klems_bin(float Dx, float Dy, float Dz, const gb_binins *p)
+{
+    const int kind = (int)p[0].op;
+    float RHS = p[0].a, Nx = p[0].b, Ny = p[0].c;
+    float Nz = p[1].op, Ux = p[1].a, Uy = p[1].b, Uz = p[1].c;
+    const float DEG = D_PI / 180.f;
+    float c = -Dx * Nx - Dy * Ny - Dz * Nz;
+    float pol = c - 1.f > 0.f ? 0.f : (-1.f - c > 0.f ? 180.f : acosf(c) / DEG);
+    if (pol - 90.f > 0.f)
+        return -1.f;
+    float y = -Dx * Ux - Dy * Uy - Dz * Uz + (Nx * Dx + Ny * Dy + Nz * Dz) * (Nx * Ux + Ny * Uy + Nz * Uz);
+    float x = -RHS * (Dx * (Uy * Nz - Uz * Ny) + Dy * (Uz * Nx - Ux * Nz) + Dz * (Ux * Ny - Uy * Nx));
+    float a = atan2f(y, x);
+    float azi = (-a > 0.f ? a + 2.f * D_PI : a) / DEG;
+    const float full_pol[9] = {5, 15, 25, 35, 45, 55, 65, 75, 90}, full_naz[9] = {1, 8, 16, 20, 24, 24, 24, 16, 12};
+    const float half_pol[7] = {6.5f, 19.5f, 32.5f, 45.5f, 58.5f, 71.5f, 90}, half_naz[7] = {1, 8, 12, 16, 20, 12, 8};
+    const float quar_pol[5] = {9, 27, 45, 63, 90}, quar_naz[5] = {1, 8, 12, 12, 8};
+    const float *pola = kind == 1 ? full_pol : kind == 2 ? half_pol : quar_pol;
+    const float *naz = kind == 1 ? full_naz : kind == 2 ? half_naz : quar_naz;
+    const int nrow = kind == 1 ? 9 : kind == 2 ? 7 : 5;
+    int row = 0;
+    float acc = 0.f;
+    while (row < nrow - 1 && pol - pola[row] > 0.f)
+        acc += naz[row++];
+    float inc = 360.f / naz[row];
+    return acc + ((360.f - .5f * inc) - azi > 0.f ? floorf((azi + .5f * inc) / inc) : 0.f);
+}
+
 GB_DFN float bin_fn1(int f, float x)
 {
     switch (f) {
@@ -900,6 +934,10 @@ GB_DFN float eval_bin(const gb_binins *prog, float3 d)
         case GB_OP_FLOOR: st[sp - 1] = floorf(st[sp - 1]); break;
         case GB_OP_RBIN:
             st[sp++] = reinhart_bin(d.x, d.y, d.z, prog + pc + 1);
+            pc += 2;
+            break;
+        case GB_OP_KBIN:
+            st[sp++] = klems_bin(d.x, d.y, d.z, prog + pc + 1);
             pc += 2;
             break;
         case GB_OP_POW: sp--; st[sp - 1] = powf(st[sp - 1], st[sp]); break;

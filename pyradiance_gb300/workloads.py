@@ -165,6 +165,35 @@ def window_room(seed: int = 0, ntri: int = 20000, nmat: int | None = None) -> st
     return "".join(out)
 
 
+def flux_files(ntri: int = 2000, seed: int = 0) -> dict:
+    """Scene text for flux-matrix (rfluxmtx) runs around ``window_room``:
+    ``system`` (the room without its sky), ``interior`` (the room without
+    sky or glass), ``sky`` (receiver: ground as one uniform bin, sky in
+    Reinhart MF:1 bins), ``window_kf`` (receiver: the window opening as a
+    glow facing into the room, Klems full bins, up +Z), ``window_send``
+    (sender: the window facing into the room, Klems full, up +Z) and
+    ``obstruction`` (an exterior block south of the window)."""
+    room = window_room(seed=seed, ntri=ntri)
+    assert room.endswith(SKY_GLOW)
+    system = room[:-len(SKY_GLOW)]
+    x0, x1, z0, z1 = WINDOW
+    win = [(x0, 0, z0), (x0, 0, z1), (x1, 0, z1), (x1, 0, z0)]
+    glass = "void glass window_glass\n0\n0\n3 .6 .6 .6\n\n" + _poly("window_glass", "window", win)
+    assert glass in system
+    interior = system.replace(glass, "")
+    sky = ("#@rfluxmtx h=u u=Y\nvoid glow groundglow\n0\n0\n4 1 1 1 0\n\n"
+           "groundglow source ground\n0\n0\n4 0 0 -1 180\n\n"
+           "#@rfluxmtx h=r1 u=Y\nvoid glow skyglow\n0\n0\n4 1 1 1 0\n\n"
+           "skyglow source skydome\n0\n0\n4 0 0 1 180\n\n")
+    window_kf = "#@rfluxmtx h=kf u=Z\nvoid glow windowglow\n0\n0\n4 1 1 1 0\n\n" + _poly("windowglow", "wrecv", win)
+    window_send = "#@rfluxmtx h=kf u=Z\nvoid polygon wsend\n0\n0\n12 " + " ".join(
+        "%.9g %.9g %.9g" % v for v in win) + "\n\n"
+    obstruction = _mat_plastic("block_mat", (0.3, 0.3, 0.3)) + _box("block_mat", "block", (-5.0, -14.0, 0.0),
+                                                                   (20.0, 4.0, 9.0))
+    return dict(system=system, interior=interior, sky=sky, window_kf=window_kf, window_send=window_send,
+                obstruction=obstruction)
+
+
 def glossy_room(seed: int = 0, nboxes: int = 40, nspheres: int = 8) -> str:
     """The room of ``daylight_room`` with rough specular surfaces: a rough
     metal floor (specularity 0.5, roughness 0.08), rough plastic walls and

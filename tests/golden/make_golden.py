@@ -29,7 +29,7 @@ REFERENCE_TREE = Path(os.environ.get("GB_REFERENCE", "/root/reference"))
 
 
 def run(args, inp: bytes | None = None, cwd=None) -> bytes:
-    env = dict(os.environ, RAYPATH=f".:{REF / 'lib'}")
+    env = dict(os.environ, RAYPATH=f".:{REF / 'lib'}", PATH=f"{BIN}:{os.environ.get('PATH', '')}")
     p = subprocess.run([str(BIN / args[0]), *map(str, args[1:])], input=inp, capture_output=True, env=env,
                        cwd=cwd)
     if p.returncode != 0:
@@ -213,6 +213,34 @@ def mirrors(tmp: Path) -> None:
     np.savez_compressed(OUT / "mirrors.npz", grid=grid, irradiance=irr, view=view, radiance=rad,
                         cmd="rtrace -h -u- -ab 0 -dj 0 -ds 0 -dr 0 -dt 0 -fdd -ov [-I]")
     print("mirrors: irradiance mean %.4g, radiance mean %.4g" % (irr.mean(), rad.mean()))
+
+
+def flux_matrices(tmp: Path) -> None:
+    """rfluxmtx (util/rfluxmtx.c) in its two modes, -ab 0: view rays passed
+    through to a sky receiver (ground uniform, sky Reinhart MF:1) seen through
+    the glass, and to the window opening binned by the Klems full basis
+    (deterministic); and the window as a Klems sender towards the sky behind an
+    exterior block (2000 samples per sender bin; a statistical fixture)."""
+    f = w.flux_files()
+    for k, v in f.items():
+        (tmp / f"{k}.rad").write_text(v)
+    rng = np.random.default_rng(31)
+    org = rng.uniform((0.2, 0.2, 0.2), (9.8, 7.8, 2.8), size=(1500, 3))
+    tgt = np.stack([rng.uniform(3.5, 6.5, 1500), np.zeros(1500), rng.uniform(0.5, 2.5, 1500)], axis=1)
+    d = tgt - org
+    rays = np.hstack([org, d / np.linalg.norm(d, axis=1, keepdims=True)])      # aimed at the window
+    rb = rays.astype("<f8").tobytes()
+    base = ["rfluxmtx", "-h", "-ab", "0", "-u-", "-fd"]
+    sky = np.frombuffer(run([*base, "-", tmp / "sky.rad", tmp / "system.rad"], rb, cwd=tmp),
+                        dtype="<f8").reshape(len(rays), -1, 3)
+    kf = np.frombuffer(run([*base, "-", tmp / "window_kf.rad", tmp / "interior.rad"], rb, cwd=tmp),
+                       dtype="<f8").reshape(len(rays), -1, 3)
+    send = np.frombuffer(run(["rfluxmtx", "-h", "-ab", "0", "-u-", "-fd", "-c", "2000", tmp / "window_send.rad",
+                              tmp / "sky.rad", tmp / "obstruction.rad"], cwd=tmp), dtype="<f8").reshape(145, -1, 3)
+    np.savez_compressed(OUT / "flux_matrices.npz", rays=rays, sky=sky, window_kf=kf, send=send, send_count=2000,
+                        cmd="rfluxmtx -h -ab 0 -u- -fd [-c 2000] sender receiver scene")
+    print("flux: rows reaching the sky %.3f, the window %.3f; sender row mean %.4f" % (
+        (sky.sum(axis=(1, 2)) > 0).mean(), (kf.sum(axis=(1, 2)) > 0).mean(), send[:, :, 0].sum(1).mean()))
 
 
 def general_bins(tmp: Path) -> None:
@@ -425,7 +453,7 @@ def main() -> None:
     parts = {"octree": octree_digests, "c1": c1_direct, "c1p": c1_partitioned, "zoo": zoo, "glossy": glossy, "irr": surface_irradiance,
              "ss": supersampled_irradiance, "inst": instances, "circ": circular_sources,
              "trans": translucent, "bins": general_bins,
-             "spot": spotlights, "mirror": mirrors,
+             "spot": spotlights, "mirror": mirrors, "flux": flux_matrices,
              "dct": lambda tmp: dct_small(), "trace_oct": lambda tmp: ref_fixture_trace(),
              "c2ab1": lambda tmp: c2_stats(tmp, ab=1, K=256), "c2ab3": lambda tmp: c2_stats(tmp, ab=3, K=256)}
     only = sys.argv[1:] or list(parts)         # e.g. make_golden.py c1p

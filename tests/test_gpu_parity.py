@@ -405,6 +405,40 @@ def test_mirrors(gb, tmp_path):
         rtrace_c(gb, sc, opts("rtrace", ab=0, dr=2, u=0), g["view"][:4])
 
 
+def test_rfluxmtx(gb, tmp_path):
+    """rfluxmtx end to end on the GPU against the reference program: view
+    rays passed through to the sky receiver (glass in between) and to the
+    window opening in Klems bins (1e-4 for 99.5% of the rows), the window as
+    a Klems sender towards the sky behind an exterior block (sampling
+    error), and the matrix header."""
+    from pyradiance_gb300 import workloads as w
+    from test_oracle_golden import flux_close
+    g = golden("flux_matrices.npz")
+    f = w.flux_files()
+    for k, v in f.items():
+        (tmp_path / f"{k}.rad").write_text(v)
+    rb = g["rays"].astype("<f8").tobytes()
+    for key, recv, scene in (("sky", "sky", "system"), ("window_kf", "window_kf", "interior")):
+        out = gb.rfluxmtx(tmp_path / f"{recv}.rad", rays=rb, params=["-h", "-ab", "0", "-u-", "-fd"],
+                          scene=[tmp_path / f"{scene}.rad"])
+        a = np.frombuffer(out, dtype="<f8").reshape(g[key].shape)
+        rel = np.abs(a - g[key]).max(axis=(1, 2)) / np.maximum(np.abs(g[key]).max(axis=(1, 2)), 1e-9)
+        assert (rel <= 1e-4).mean() >= 0.995, (key, np.sort(rel)[-5:])
+    n = int(g["send_count"])
+    out = gb.rfluxmtx(tmp_path / "sky.rad", surface=tmp_path / "window_send.rad",
+                      params=["-h", "-ab", "0", "-u-", "-fd", "-c", str(n)], scene=[tmp_path / "obstruction.rad"])
+    a = np.frombuffer(out, dtype="<f8").reshape(g["send"].shape)
+    flux_close(a[:, :, 0], g["send"][:, :, 0], n)
+    out = gb.rfluxmtx(tmp_path / "sky.rad", surface=tmp_path / "window_send.rad", params=["-ab", "0", "-c", "4"],
+                      scene=[tmp_path / "obstruction.rad"])
+    head = out.split(b"\n\n")[0].decode()
+    assert "NROWS=145" in head and "NCOLS=146" in head and "NCOMP=3" in head and "FORMAT=ascii" in head
+    body = out.split(b"\n\n", 1)[1].decode().split("\n")
+    assert len([ln for ln in body if ln.strip()]) == 145 and len(body[0].split()) == 146 * 3
+    with pytest.raises(RuntimeError):
+        gb.rfluxmtx(tmp_path / "sky.rad", surface=tmp_path / "window_send.rad", params=["-I", "-c", "4"])
+
+
 def test_instances(gb):
     """Instanced octrees (rt/o_instance.c:15-71): the furniture octree 12
     times in the room, rotated, scaled, mirrored, some with their own

@@ -122,3 +122,36 @@ def test_read_rays_formats():
     np.testing.assert_array_equal(gb.read_rays(b"0 1 2 3 4 5\n6 7 8 9 10 11\n", "a"), r)
     np.testing.assert_array_equal(gb.read_rays(r.astype(np.float32).tobytes(), "f"), r)
     np.testing.assert_array_equal(gb.read_rays(r.tobytes(), "d"), r)
+
+
+def test_rfluxmtx_receiver_arguments(tmp_path):
+    """Receiver directives give the rcontrib modifier arguments the reference
+    rfluxmtx passes on (its -v report for these files: util/rfluxmtx.c:427-582);
+    directives and options it rejects raise."""
+    from pyradiance_gb300 import rflux
+    from pyradiance_gb300 import workloads as w
+    f = w.flux_files(ntri=10)
+    for k, v in f.items():
+        (tmp_path / f"{k}.rad").write_text(v)
+    sky = rflux._receivers(tmp_path / "sky.rad")
+    assert [(m["modifier"], m["calfile"], m["params"], m["nbins"], m["binv"]) for m in sky] == [
+        ("groundglow", None, None, "1", "0"),
+        ("skyglow", "reinhartb.cal", "MF=1,rNx=0,rNy=0,rNz=-1,Ux=0,Uy=1,Uz=0,RHS=+1", "Nrbins", "rbin")]
+    kf = rflux._receivers(tmp_path / "window_kf.rad")
+    assert [(m["modifier"], m["calfile"], m["params"], m["nbins"], m["binv"]) for m in kf] == [
+        ("windowglow", "klems_full.cal", "RHS=+1", "Nkbins", "kbin(0,1,0,0,0,1)")]
+    (tmp_path / "bad.rad").write_text("#@rfluxmtx h=sc4\nvoid glow g\n0\n0\n4 1 1 1 0\n\n"
+                                      "g polygon p\n0\n0\n9 0 0 0 1 0 0 0 1 0\n")
+    with pytest.raises(Exception):
+        rflux._receivers(tmp_path / "bad.rad")
+    with pytest.raises(Exception):
+        rflux._screen(["-bj", ".5"])
+    rc, fmt, xres, yres, cnt, iropt, ld = rflux._screen(["-v", "-ab", "2", "-ff", "-c", "30", "-I+", "-y", "4",
+                                                         "-av", "1", "1", "1", "-ld-"])
+    assert rc == ["-ab", "2", "-av", "1", "1", "1"] and fmt == ["f", "f"] and cnt == 30 and iropt == "-I+"
+    assert yres == "4" and ld == "-ld-"
+    p = rflux._sender(tmp_path / "window_send.rad")
+    rays, nb = rflux._sender_rays(p, 50, np.random.default_rng(1))
+    assert nb == 145 and rays.shape == (145 * 50, 6)
+    assert (rays[:, 4] < 0).all()                       # leaving the window away from its normal (+y)
+    assert np.allclose(rays[:, 1], 0) and (rays[:, 0] >= 3.5).all() and (rays[:, 0] <= 6.5).all()

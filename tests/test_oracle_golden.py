@@ -232,6 +232,43 @@ def test_mirrors(tmp_path):
     np.testing.assert_allclose(rgb, g["radiance"], rtol=1e-6, atol=1e-9)
 
 
+def flux_close(a, b, n):
+    """Sender matrices: each entry is a mean over n rays of a coefficient in
+    [0, 1]; both within 5 combined standard errors (plus a 1.5/n floor)."""
+    tol = 5 * np.sqrt((a * (1 - a) + b * (1 - b)) / n) + 1.5 / n
+    bad = np.abs(a - b) > tol
+    assert bad.mean() <= 2e-3, (bad.sum(), np.argwhere(bad)[:5])
+    np.testing.assert_allclose(a.sum(axis=1), b.sum(axis=1), atol=0.05)
+
+
+def test_flux_matrices(tmp_path):
+    """rfluxmtx (util/rfluxmtx.c): the receiver directives become the
+    reference's rcontrib modifier arguments, which the oracle traces to the
+    reference's pass-through matrices (sky in Reinhart bins through the glass,
+    the window opening in Klems bins; 1e-6), and the host's Klems sender rays
+    give the reference's sender matrix within sampling error."""
+    from pyradiance_gb300 import rflux
+    from pyradiance_gb300 import workloads as w
+    g = golden("flux_matrices.npz")
+    f = w.flux_files()
+    for k, v in f.items():
+        (tmp_path / f"{k}.rad").write_text(v)
+    o = po.default_opts("rcontrib", ab=0, u=0)
+    for key, recv, scene in (("sky", "sky", "system"), ("window_kf", "window_kf", "interior")):
+        specs = rflux._receivers(tmp_path / f"{recv}.rad")
+        (tmp_path / "all.rad").write_text(f[scene] + f[recv])
+        out, _ = po.rcontrib(po.Scene(tmp_path / "all.rad"), o, specs, g["rays"], threads=8)
+        np.testing.assert_allclose(out, g[key], rtol=1e-6, atol=1e-9)
+    n = int(g["send_count"])
+    rays, nb = rflux._sender_rays(rflux._sender(tmp_path / "window_send.rad"), n, np.random.default_rng(0))
+    assert nb == 145 and rays.shape == (145 * n, 6)
+    o.c = n
+    (tmp_path / "all.rad").write_text(f["obstruction"] + f["sky"])
+    out, _ = po.rcontrib(po.Scene(tmp_path / "all.rad"), o, rflux._receivers(tmp_path / "sky.rad"), rays,
+                         threads=8)
+    flux_close(out[:, :, 0], g["send"][:, :, 0], n)
+
+
 def test_instances():
     """Instanced octrees (rt/o_instance.c:15-71, common/instance.c,
     common/xf.c): the furniture octree 12 times in the room, rotated,
