@@ -438,17 +438,31 @@ def dctimestep_array(dc: np.ndarray, sky: np.ndarray, mode: str = "fp32") -> np.
 def _dctimestep(*mtx, nstep: int | None = None, header: bool = True, xres: int | None = None,
                 yres: int | None = None, inform: str | None = None, outform: str | None = None,
                 ospec: str | None = None) -> bytes | None:
-    """dctimestep on the GPU (same signature as pyradiance.dctimestep);
-    the two-matrix form DC x sky."""
+    """dctimestep on the GPU (same signature as pyradiance.dctimestep): the
+    two-matrix form DC x sky, and the four-matrix form V x T x D x sky of
+    util/dctimestep.c:243-264 and :324-330, multiplied as the reference
+    does, D x sky first, then T, then V, each product on the GPU with FP32
+    intermediates (the reference's matrices hold floats).  A transmission
+    matrix given as an XML BSDF (cm_loadBTDF) raises."""
     if len(mtx) not in (2, 4):
         raise ValueError("mtx must be a list of 2 or 4 items")
-    if len(mtx) == 4:
-        raise GbError(-3, "the four-matrix (view/BSDF/daylight) form is not supported")
     if ospec:
         raise GbError(-3, "output specification files are not supported")
-    dc = _read_matrix(mtx[0])
-    sky = _read_matrix(mtx[1], inform)
-    R = dctimestep_array(dc, sky)
+    if len(mtx) == 4:
+        if isinstance(mtx[1], (str, Path)) and str(mtx[1]).lower().endswith(".xml"):
+            raise GbError(-3, "XML BSDF transmission matrices (cm_loadBTDF) are not supported; "
+                          "give the matrix as a Radiance matrix file")
+        V, T, D = (_read_matrix(m) for m in mtx[:3])
+        sky = _read_matrix(mtx[3], inform)
+        for a, b, what in ((D, sky, "daylight and sky"), (T, D, "transmission and daylight"),
+                           (V, T, "view and transmission")):
+            if a.shape[1] != b.shape[0]:
+                raise GbError(-1, f"{what} matrices do not match ({a.shape[1]} columns, {b.shape[0]} rows)")
+        R = dctimestep_array(V, dctimestep_array(T, dctimestep_array(D, sky)))
+    else:
+        dc = _read_matrix(mtx[0])
+        sky = _read_matrix(mtx[1], inform)
+        R = dctimestep_array(dc, sky)
     fout = outform or "a"
     parts = []
     if header:

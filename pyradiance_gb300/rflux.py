@@ -12,7 +12,8 @@ Hemisphere bases: uniform (``h=u``), Klems full / half / quarter (``h=kf``,
 ``kh``, ``kq``; the bases of util/klems_full.cal, klems_half.cal and
 klems_quarter.cal, built into the bin compiler) and Reinhart (``h=r``,
 ``h=rN``).  Shirley-Chiu (``h=sc``) and CIE (``h=cie``) bins, bin jitter
-(``-bj``) and per-receiver output files (``o=``) raise ``RuntimeError``.
+(``-bj``) and per-bin output files (``o=`` with ``%d``) raise
+``RuntimeError``; receivers with ``o=`` write their columns to that file.
 """
 from __future__ import annotations
 
@@ -212,10 +213,12 @@ def _receivers(path) -> list[dict]:
             groups[-1][1].surfs.append(s)
     if not groups:
         raise GbError(-1, "missing receiver surface!")
-    specs = []
+    specs, ospec = [], None
     for mod, p in groups:
-        if p.outfn is not None:
-            raise GbError(-3, f"receiver output files (o={p.outfn}) are not supported; results are returned as bytes")
+        if p.outfn is not None:                 # rcontrib -o: this and the following modifiers
+            ospec = p.outfn
+            if "%d" in ospec or "%i" in ospec:
+                raise GbError(-3, f"per-bin output files (o={ospec}) are not supported")
         if not p.hemis:
             raise GbError(-1, "missing hemisphere sampling type!")
         if not p.surfs:
@@ -223,7 +226,7 @@ def _receivers(path) -> list[dict]:
         nrm = p.normal()
         vup = p.up(nrm)
         h = p.hemis.lower()
-        spec = dict(modifier=mod, calfile=None, params=None, nbins=None, binv=None, expr=None)
+        spec = dict(modifier=mod, calfile=None, params=None, nbins=None, binv=None, expr=None, output=ospec)
         if h[0] in "u1":
             if p.surfs[-1].styp != "source":
                 spec["binv"] = "if(-Dx*%g-Dy*%g-Dz*%g,0,-1)" % tuple(nrm)
@@ -528,7 +531,8 @@ def rfluxmtx_array(receiver, surface=None, rays=None, params: Sequence[str] | No
         nrows = nsbins
     R = Rcontrib(b"", sc, params=rc)
     for s in specs:
-        R.mods.append(s)
+        R.mods.append({k: v for k, v in s.items() if k != "output"})
+    R.outputs = [s.get("output") for s in specs]
     out = R.run_array(r)
     return out, R, fmt[1], nrows
 
@@ -539,18 +543,51 @@ def _rfluxmtx(receiver, surface=None, rays: bytes | None = None, params: Sequenc
     matrix as rcontrib writes it."""
     from . import _fmt_values, _header
     out, R, fout, nrows = rfluxmtx_array(receiver, surface, rays, params, octree, scene)
-    parts = []
-    if R._opts.h:
-        extra = []
-        if nrows:
-            extra.append(f"NROWS={nrows}")
-        extra.append(f"NCOLS={out.shape[1]}")
-        args = R.args + [a for m in R.mods for a in ("-m", m["modifier"])]
-        parts.append(_header("rcontrib", args, octree, fout, 3, extra))
-    if fout == "a":
-        flat = out.reshape(out.shape[0], -1)
-        parts.append("".join("".join(f"{x:.6e}\t" for x in row) + "\n" for row in flat).encode())
-    else:
-        parts.append(_fmt_values(out.reshape(-1, 3), fout))
-    return b"".join(parts)
+    args = R.args + [a for m in R.mods for a in ("-m", m["modifier"])]
+
+    def write(arr) -> bytes:
+        parts = []
+        if R._opts.h:
+            extra = [f"NROWS={nrows}"] if nrows else []
+            extra.append(f"NCOLS={arr.shape[1]}")
+            parts.append(_header("rcontrib", args, octree, fout, 3, extra))
+        if fout == "a":
+            flat = arr.reshape(arr.shape[0], -1)
+            parts.append("".join("".join(f"{x:.6e}\t" for x in row) + "\n" for row in flat).encode())
+        else:
+            parts.append(_fmt_values(arr.reshape(-1, 3), fout))
+        return b"".join(parts)
+
+    if not any(R.outputs):
+        return write(out)
+    # receivers with o=: their columns go to files (a %s in the name is the
+    # modifier), the others to the standard output (rt/rc2.c:131-250)
+    files: dict[str | None, list[np.ndarray]] = {}
+    col = 0
+    for m, spec, nb in zip(R.mods, R.outputs, _nbins_each(R.mods)):
+        name = None if spec is None else (spec.replace("%s", m["modifier"]) if "%s" in spec else spec)
+        files.setdefault(name, []).append(out[:, col:col + nb])
+        col += nb
+    stdout = b""
+    for name, cols in files.items():
+        data = write(np.concatenate(cols, axis=1))
+        if name is None:
+            stdout = data
+        else:
+            Path(name).parent.mkdir(parents=True, exist_ok=True)
+            Path(name).write_bytes(data)
+    return stdout
+
+
+def _nbins_each(mods: list[dict]) -> list[int]:
+    out = []
+    for m in mods:
+        v = {k: (str(m[k]).encode() if m.get(k) is not None else None)
+             for k in ("modifier", "binv", "nbins", "params", "calfile", "expr")}
+        arr = (_lib.GbModspec * 1)(_lib.GbModspec(v["modifier"], v["binv"], v["nbins"], v["params"], v["calfile"],
+                                                  v["expr"]))
+        n = _lib.C.c_int(0)
+        _lib.check(_lib.lib().gb_rcontrib_nbins(arr, 1, _lib.C.byref(n)))
+        out.append(n.value)
+    return out
 

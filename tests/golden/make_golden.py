@@ -394,6 +394,29 @@ def c2_stats(tmp: Path, nsens: int = 32, K: int = 256, ab: int = 3) -> None:
     print("c2_stats ab%d: mean total %.4g" % (ab, a.sum(2).mean()))
 
 
+def dct_four() -> None:
+    """dctimestep's four-matrix form (util/dctimestep.c:243-264): view
+    (sensors x 145 Klems), transmission (145 x 145), daylight (145 x 146) and
+    sky (146 x 12 hours), random non-negative values with zeros."""
+    rng = np.random.default_rng(9)
+    mats = {}
+    for name, shp, zf in (("V", (40, 145), .3), ("T", (145, 145), .5), ("D", (145, 146), .3), ("S", (146, 12), .2)):
+        m = rng.lognormal(-2, 1, size=(*shp, 3)).astype(np.float32)
+        m[rng.random(shp) < zf] = 0
+        mats[name] = m
+    with tempfile.TemporaryDirectory() as td:
+        td = Path(td)
+        for name, m in mats.items():
+            hdr = (f"#?RADIANCE\nNROWS={m.shape[0]}\nNCOLS={m.shape[1]}\nNCOMP=3\nBigEndian=0\n"
+                   "FORMAT=float\n\n").encode()
+            (td / f"{name}.mtx").write_bytes(hdr + m.astype("<f4").tobytes())
+        out = run(["dctimestep", "-h", "-od", *(td / f"{n}.mtx" for n in "VTDS")])
+    res = np.frombuffer(out, dtype="<f8").reshape(40, 12, 3)
+    np.savez_compressed(OUT / "dct_four.npz", out=res, cmd="dctimestep -h -od V.mtx T.mtx D.mtx S.mtx",
+                        **mats)
+    print("dct_four: max %.4g" % res.max())
+
+
 def dct_small() -> None:
     """dctimestep on small matrices with the annual workload's value
     distributions (DC lognormal with zeros, sky spikes and night columns)."""
@@ -454,7 +477,7 @@ def main() -> None:
              "ss": supersampled_irradiance, "inst": instances, "circ": circular_sources,
              "trans": translucent, "bins": general_bins,
              "spot": spotlights, "mirror": mirrors, "flux": flux_matrices,
-             "dct": lambda tmp: dct_small(), "trace_oct": lambda tmp: ref_fixture_trace(),
+             "dct": lambda tmp: dct_small(), "dct4": lambda tmp: dct_four(), "trace_oct": lambda tmp: ref_fixture_trace(),
              "c2ab1": lambda tmp: c2_stats(tmp, ab=1, K=256), "c2ab3": lambda tmp: c2_stats(tmp, ab=3, K=256)}
     only = sys.argv[1:] or list(parts)         # e.g. make_golden.py c1p
     with tempfile.TemporaryDirectory() as td:

@@ -437,6 +437,21 @@ def test_rfluxmtx(gb, tmp_path):
     assert len([ln for ln in body if ln.strip()]) == 145 and len(body[0].split()) == 146 * 3
     with pytest.raises(RuntimeError):
         gb.rfluxmtx(tmp_path / "sky.rad", surface=tmp_path / "window_send.rad", params=["-I", "-c", "4"])
+    # o= on the sky receiver: its 145 columns go to a file, the ground's to stdout
+    (tmp_path / "sky_o.rad").write_text(f["sky"].replace("#@rfluxmtx h=r1 u=Y", "#@rfluxmtx h=r1 u=Y o=%s.mtx"))
+    import os
+    cwd = os.getcwd()
+    os.chdir(tmp_path)
+    try:
+        out = gb.rfluxmtx(tmp_path / "sky_o.rad", rays=rb, params=["-h", "-ab", "0", "-u-", "-fd"],
+                          scene=[tmp_path / "system.rad"])
+        sky = np.frombuffer((tmp_path / "skyglow.mtx").read_bytes(), dtype="<f8").reshape(-1, 145, 3)
+    finally:
+        os.chdir(cwd)
+    ground = np.frombuffer(out, dtype="<f8").reshape(-1, 1, 3)
+    a = np.concatenate([ground, sky], axis=1)
+    rel = np.abs(a - g["sky"]).max(axis=(1, 2)) / np.maximum(np.abs(g["sky"]).max(axis=(1, 2)), 1e-9)
+    assert (rel <= 1e-4).mean() >= 0.995
 
 
 def test_instances(gb):
@@ -473,6 +488,27 @@ def test_dctimestep_fp32_fp64(gb):
     np.testing.assert_allclose(r64, g["out"], rtol=1e-6, atol=1e-30)
     r32 = gb.dctimestep_array(g["dc"], g["sky"], mode="fp32")
     np.testing.assert_allclose(r32, g["out"], rtol=1e-4, atol=1e-6 * np.abs(g["out"]).max())
+
+
+def test_dctimestep_four_matrix(gb, tmp_path):
+    """dctimestep V T D sky (util/dctimestep.c:243-264) through the drop-in:
+    matrix files in, the reference program's output within 1e-5; an XML
+    BSDF transmission raises."""
+    g = golden("dct_four.npz")
+    paths = []
+    for n in "VTDS":
+        m = g[n]
+        hdr = (f"#?RADIANCE\nNROWS={m.shape[0]}\nNCOLS={m.shape[1]}\nNCOMP=3\nBigEndian=0\n"
+               "FORMAT=float\n\n").encode()
+        (tmp_path / f"{n}.mtx").write_bytes(hdr + m.astype("<f4").tobytes())
+        paths.append(tmp_path / f"{n}.mtx")
+    out = gb.dctimestep(*paths, header=False, outform="d")
+    r = np.frombuffer(out, dtype="<f8").reshape(g["out"].shape)
+    np.testing.assert_allclose(r, g["out"], rtol=1e-5, atol=1e-6 * np.abs(g["out"]).max())
+    with pytest.raises(RuntimeError):
+        gb.dctimestep(paths[0], tmp_path / "T.xml", paths[2], paths[3])
+    with pytest.raises(RuntimeError):
+        gb.dctimestep(paths[0], paths[0], paths[2], paths[3])
 
 
 def _dc_pair(rng, M, K, N):

@@ -322,6 +322,14 @@ def test_dctimestep_oracle():
     np.testing.assert_array_equal(out, g["out"])
 
 
+def test_dctimestep_four_matrix_oracle():
+    """V x T x D x sky as the reference multiplies it (D x sky, then T, then
+    V, float intermediates): the oracle's product chain within 1e-6."""
+    g = golden("dct_four.npz")
+    out = po.dctimestep(g["V"], po.dctimestep(g["T"], po.dctimestep(g["D"], g["S"])))
+    np.testing.assert_allclose(out, g["out"], rtol=1e-6, atol=1e-12)
+
+
 def check_c2_statistics(a, g, K):
     """a: (sensors, K, 146) samples of channel 0.  Compares with the golden
     reference statistics: per-sensor totals, per-sensor altitude-row groups
