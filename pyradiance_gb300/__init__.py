@@ -484,3 +484,7 @@ dctimestep = _wrap(_dctimestep)
 from .rflux import _rfluxmtx  # noqa: E402
 
 rfluxmtx = _wrap(_rfluxmtx)
+
+from .simul import (RCcontrib, RcontribSimulManager, RcOutputOp, RTdoFIFO, RTimmIrrad, RTlimDist,  # noqa: E402
+                    RTmask, RtraceSimulManager, RTtraceSources, get_default_ray_params, get_ray_params, loadfunc,
+                    set_ray_params)
