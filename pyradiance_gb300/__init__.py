@@ -20,7 +20,7 @@ import numpy as np
 from . import _lib
 from ._lib import GbError, GbModspec, Scene, check, last_stats, lib, parse_opts, ptr
 
-__all__ = ["rtrace", "Rcontrib", "dctimestep", "rfluxmtx", "Scene", "load_scene", "read_rays", "GbError", "last_stats"]
+__all__ = ["rtrace", "Rcontrib", "dctimestep", "rfluxmtx", "rmtxop", "Scene", "load_scene", "read_rays", "GbError", "last_stats"]
 
 _SCENES: dict = {}
 
@@ -484,6 +484,10 @@ dctimestep = _wrap(_dctimestep)
 from .rflux import _rfluxmtx  # noqa: E402
 
 rfluxmtx = _wrap(_rfluxmtx)
+
+from .rmtx import _rmtxop  # noqa: E402
+
+rmtxop = _wrap(_rmtxop)
 
 from .simul import (RCcontrib, RcontribSimulManager, RcOutputOp, RTdoFIFO, RTimmIrrad, RTlimDist,  # noqa: E402
                     RTmask, RtraceSimulManager, RTtraceSources, get_default_ray_params, get_ray_params, loadfunc,

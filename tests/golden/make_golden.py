@@ -417,6 +417,24 @@ def dct_four() -> None:
     print("dct_four: max %.4g" % res.max())
 
 
+def rmtxop_cases() -> None:
+    """rmtxop (util/rmtxop.c) on one 5 x 7 x 3 matrix: transpose, scale,
+    component transform with and without a folded scale, both together."""
+    rng = np.random.default_rng(13)
+    m = rng.lognormal(-1, 1, size=(5, 7, 3))
+    cases = [[], ["-t"], ["-s", "2.5"], ["-c", ".265", ".67", ".065"], ["-s", "3", "-c", ".2", ".3", ".5"],
+             ["-t", "-s", "0.5", "-c", "1", "0", "0", "0", "0", "1"]]
+    outs = {}
+    with tempfile.TemporaryDirectory() as td:
+        f = Path(td) / "m.mtx"
+        f.write_bytes(b"#?RADIANCE\nNROWS=5\nNCOLS=7\nNCOMP=3\nBigEndian=0\nFORMAT=double\n\n" +
+                      m.astype("<f8").tobytes())
+        for i, c in enumerate(cases):
+            outs[f"out{i}"] = np.frombuffer(run(["rmtxop", "-fd", *c, f]).split(b"\n\n", 1)[1], dtype="<f8")
+    np.savez_compressed(OUT / "rmtxop.npz", m=m, cases=np.array([" ".join(c) for c in cases]), **outs)
+    print("rmtxop: %d cases" % len(cases))
+
+
 def dct_small() -> None:
     """dctimestep on small matrices with the annual workload's value
     distributions (DC lognormal with zeros, sky spikes and night columns)."""
@@ -477,7 +495,7 @@ def main() -> None:
              "ss": supersampled_irradiance, "inst": instances, "circ": circular_sources,
              "trans": translucent, "bins": general_bins,
              "spot": spotlights, "mirror": mirrors, "flux": flux_matrices,
-             "dct": lambda tmp: dct_small(), "dct4": lambda tmp: dct_four(), "trace_oct": lambda tmp: ref_fixture_trace(),
+             "dct": lambda tmp: dct_small(), "dct4": lambda tmp: dct_four(), "rmtxop": lambda tmp: rmtxop_cases(), "trace_oct": lambda tmp: ref_fixture_trace(),
              "c2ab1": lambda tmp: c2_stats(tmp, ab=1, K=256), "c2ab3": lambda tmp: c2_stats(tmp, ab=3, K=256)}
     only = sys.argv[1:] or list(parts)         # e.g. make_golden.py c1p
     with tempfile.TemporaryDirectory() as td:
