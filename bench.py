@@ -486,7 +486,8 @@ def gpu_arm(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=None,
+                    help="timed steps (default 30; 5 for the reference arm, whose steps are CPU samples)")
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
@@ -496,6 +497,8 @@ def main():
     ap.add_argument("--no-extras", action="store_true",
                     help="the rcontrib workload only (no dctimestep, gradient and batching legs)")
     args = ap.parse_args()
+    if args.steps is None:
+        args.steps = 5 if args.impl == "reference" else 30
     if args.impl == "reference":
         reference_arm(args)
     else:
