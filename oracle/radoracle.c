@@ -1016,6 +1016,34 @@ static void trace_contrib(ctx *X, const RAY *r)
                 pc += 2;
                 break;
             }
+            case GB_OP_SCBIN: {
+                /* util/disk2square.cal: the inverse concentric map and scbin */
+                const gb_binins *q = pr + pc + 1;
+                double SC = q[0].op, RHS = q[0].a, rNx = q[0].b, rNy = q[0].c, rNz = q[1].op, Ux = q[1].a,
+                       Uy = q[1].b, Uz = q[1].c, Q = PI / 4;
+                double Dx = r->rdir[0], Dy = r->rdir[1], Dz = r->rdir[2];
+                double dz = -Dx * rNx - Dy * rNy - Dz * rNz;
+                if (!(dz > 0)) st[sp++] = -1;
+                else {
+                    double rx = -RHS * (Dx * (Uy * rNz - Uz * rNy) + Dy * (Uz * rNx - Ux * rNz) + Dz * (Ux * rNy - Uy * rNx));
+                    double ry = Dx * Ux + Dy * Uy + Dz * Uz + dz * (rNx * Ux + rNy * Uy + rNz * Uz);
+                    double den2 = rx * rx + ry * ry, radf = den2 - 1e-7 > 0 ? sqrt((1 - dz * dz) / den2) : 0;
+                    double x = rx * radf, y = -ry * radf, rr = sqrt(x * x + y * y), phi = atan2(y, x), a, b;
+                    int rgn;
+                    if (-phi - Q > 0) phi += 2 * PI;
+                    rgn = (int)floor((phi + Q) / (2 * Q)) + 1;
+                    switch (rgn) {
+                    case 1: a = rr; b = phi * rr / Q; break;
+                    case 2: a = (2 * Q - phi) * rr / Q; b = rr; break;
+                    case 3: a = -rr; b = (PI - phi) * rr / Q; break;
+                    case 4: a = (phi - 6 * Q) * rr / Q; b = -rr; break;
+                    default: a = rr; b = -rr; break;
+                    }
+                    st[sp++] = floor((a + 1) * .5 * SC) * SC + floor((b + 1) * .5 * SC);
+                }
+                pc += 2;
+                break;
+            }
             default: return;
             }
         }

@@ -20,7 +20,9 @@
  *  - the Reinhart sky bins of util/reinhartb.cal (rbin, Nrbins) built in;
  *  - the LBNL/Klems full, half and quarter bases of util/klems_full.cal,
  *    klems_half.cal and klems_quarter.cal (kbin, khbin, kqbin with their bin
- *    counts) built in: rfluxmtx receivers name these files.
+ *    counts) built in: rfluxmtx receivers name these files;
+ *  - the Shirley-Chiu square bins of util/disk2square.cal (scbin, with
+ *    SCdim and the frame parameters) built in.
  *
  * Calls are expanded where they are used (partial evaluation): arguments
  * that are constants are substituted and folded, so recursion on constant
@@ -48,7 +50,7 @@ using NP = std::shared_ptr<Node>;
 
 struct Node {
     enum Kind {
-        NUM, DX, DY, DZ, NEG, ADD, SUB, MUL, DIV, POW, IF, FN1, ATAN2, MAXN, MINN, SELECT, FLOOR, RBIN, KBIN,
+        NUM, DX, DY, DZ, NEG, ADD, SUB, MUL, DIV, POW, IF, FN1, ATAN2, MAXN, MINN, SELECT, FLOOR, RBIN, KBIN, SCBIN,
         TEMP, LET,              /* residual only: temporary t, and let t = a[0] in a[1] */
         VAR, CALL               /* parsed only */
     } k;
@@ -77,6 +79,7 @@ struct Ctx {
     std::map<std::string, Def> defs;
     bool reinhart = false;
     int klems = 0;              /* 1, 2, 4: built-in full, half, quarter Klems bins */
+    bool shirchiu = false;      /* built-in Shirley-Chiu bins (scbin) */
     std::string err;
     int temps = 0;
     NP fail(const std::string &m)
@@ -333,9 +336,12 @@ struct Eval {
         if (name == "Dy") return mk(Node::DY);
         if (name == "Dz") return mk(Node::DZ);
         if (name == "PI") return num(M_PI);
-        if (C.reinhart && name == "rbin") {
-            static const char *pn[8] = {"MF", "RHS", "rNx", "rNy", "rNz", "Ux", "Uy", "Uz"};
-            NP n = mk(Node::RBIN);
+        if ((C.reinhart && name == "rbin") || (C.shirchiu && name == "scbin" && !C.defs.count(name))) {
+            const bool sc = name == "scbin";
+            static const char *rn[8] = {"MF", "RHS", "rNx", "rNy", "rNz", "Ux", "Uy", "Uz"};
+            static const char *sn[8] = {"SCdim", "RHS", "rNx", "rNy", "rNz", "Ux", "Uy", "Uz"};
+            const char *const *pn = sc ? sn : rn;
+            NP n = mk(sc ? Node::SCBIN : Node::RBIN);
             for (int i = 0; i < 8; i++) {
                 NP v = var(pn[i], Env());
                 if (!v) return nullptr;
@@ -369,6 +375,12 @@ struct Eval {
             if (!d->second.params.empty())
                 return C.fail("function " + name + " used without arguments");
             return pe(d->second.body, Env());
+        }
+        if (C.shirchiu) {
+            static const std::map<std::string, double> dflt = {
+                {"RHS", 1}, {"rNx", 0}, {"rNy", 0}, {"rNz", -1}, {"Ux", 0}, {"Uy", 1}, {"Uz", 0}};
+            auto f = dflt.find(name);
+            if (f != dflt.end()) return num(f->second);
         }
         if (C.reinhart) {
             static const std::map<std::string, double> dflt = {
@@ -538,10 +550,10 @@ struct Emitter {
                 (float)(n->k == Node::SELECT ? k - 1 : k), 1 - k);
             return;
         }
-        case Node::RBIN: case Node::KBIN: {
+        case Node::RBIN: case Node::KBIN: case Node::SCBIN: {
             float p[8];
             for (int i = 0; i < 8; i++) p[i] = (float)n->a[i]->v;
-            put(n->k == Node::RBIN ? GB_OP_RBIN : GB_OP_KBIN, 0, 1);
+            put(n->k == Node::RBIN ? GB_OP_RBIN : n->k == Node::KBIN ? GB_OP_KBIN : GB_OP_SCBIN, 0, 1);
             out.push_back({p[0], p[1], p[2], p[3]});
             out.push_back({p[4], p[5], p[6], p[7]});
             return;
@@ -579,6 +591,8 @@ int gb_compile_bin(const char *binv, const char *params, const char *calfile, co
         b = b ? b + 1 : calfile;
         if (!strcmp(b, "reinhartb.cal") || !strcmp(b, "reinhart.cal"))
             C.reinhart = true;
+        else if (!strcmp(b, "disk2square.cal"))
+            C.shirchiu = true;
         else if (!strcmp(b, "klems_full.cal"))
             C.klems = 1;
         else if (!strcmp(b, "klems_half.cal"))

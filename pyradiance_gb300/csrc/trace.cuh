@@ -892,6 +892,40 @@ GB_DFN float klems_bin(float Dx, float Dy, float Dz, const gb_binins *p)
     return acc + ((360.f - .5f * inc) - azi > 0.f ? floorf((azi + .5f * inc) / inc) : 0.f);
 }
 
+/* Shirley-Chiu bin: the incident direction in the surface frame, its disk
+ * position mapped back to the unit square by the inverse of Shirley and
+ * Chiu's concentric map, the square cut into SCdim x SCdim cells, the up
+ * direction changing fastest; -1 behind the surface (util/disk2square.cal).
+ */
+GB_DFN float shirchiu_bin(float Dx, float Dy, float Dz, const gb_binins *p)
+{
+    float SC = p[0].op, RHS = p[0].a, rNx = p[0].b, rNy = p[0].c;
+    float rNz = p[1].op, Ux = p[1].a, Uy = p[1].b, Uz = p[1].c;
+    const float Q = D_PI / 4.f;
+    float dz = -Dx * rNx - Dy * rNy - Dz * rNz;
+    if (!(dz > 0.f))
+        return -1.f;
+    float rx = -RHS * (Dx * (Uy * rNz - Uz * rNy) + Dy * (Uz * rNx - Ux * rNz) + Dz * (Ux * rNy - Uy * rNx));
+    float ry = Dx * Ux + Dy * Uy + Dz * Uz + dz * (rNx * Ux + rNy * Uy + rNz * Uz);
+    float den2 = rx * rx + ry * ry;
+    float radf = den2 - 1e-7f > 0.f ? sqrtf((1.f - dz * dz) / den2) : 0.f;
+    float x = rx * radf, y = -ry * radf;
+    float r = sqrtf(x * x + y * y);
+    float phi = atan2f(y, x);
+    if (-phi - Q > 0.f)
+        phi += 2.f * D_PI;
+    int rgn = (int)floorf((phi + Q) / (2.f * Q)) + 1;
+    float a, b;
+    switch (rgn) {
+    case 1: a = r; b = phi * r / Q; break;
+    case 2: a = (2.f * Q - phi) * r / Q; b = r; break;
+    case 3: a = -r; b = (D_PI - phi) * r / Q; break;
+    case 4: a = (phi - 6.f * Q) * r / Q; b = -r; break;
+    default: a = r; b = -r; break;
+    }
+    return floorf((a + 1.f) * .5f * SC) * SC + floorf((b + 1.f) * .5f * SC);
+}
+
 GB_DFN float bin_fn1(int f, float x)
 {
     switch (f) {
@@ -938,6 +972,10 @@ GB_DFN float eval_bin(const gb_binins *prog, float3 d)
             break;
         case GB_OP_KBIN:
             st[sp++] = klems_bin(d.x, d.y, d.z, prog + pc + 1);
+            pc += 2;
+            break;
+        case GB_OP_SCBIN:
+            st[sp++] = shirchiu_bin(d.x, d.y, d.z, prog + pc + 1);
             pc += 2;
             break;
         case GB_OP_POW: sp--; st[sp - 1] = powf(st[sp - 1], st[sp]); break;

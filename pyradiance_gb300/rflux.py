@@ -10,8 +10,9 @@ bin.  Here the same arguments drive the in-process GPU rcontrib
 
 Hemisphere bases: uniform (``h=u``), Klems full / half / quarter (``h=kf``,
 ``kh``, ``kq``; the bases of util/klems_full.cal, klems_half.cal and
-klems_quarter.cal, built into the bin compiler) and Reinhart (``h=r``,
-``h=rN``).  Shirley-Chiu (``h=sc``) and CIE (``h=cie``) bins, bin jitter
+klems_quarter.cal, built into the bin compiler), Reinhart (``h=r``,
+``h=rN``) and Shirley-Chiu (``h=scN``, util/disk2square.cal's scbin, built
+in).  CIE (``h=cie``) bins, bin jitter
 (``-bj``) and per-bin output files (``o=`` with ``%d``) raise
 ``RuntimeError``; receivers with ``o=`` write their columns to that file.
 """
@@ -233,6 +234,13 @@ def _receivers(path) -> list[dict]:
             else:
                 spec["binv"] = "0"
             spec["nbins"] = "1"
+        elif h[:2] == "sc":
+            if p.hsiz <= 1:
+                raise GbError(-1, "missing size for Shirley-Chiu sampling!")
+            spec["calfile"] = "disk2square.cal"
+            spec["params"] = "SCdim=%d,rNx=%g,rNy=%g,rNz=%g,Ux=%g,Uy=%g,Uz=%g,RHS=%s1" % (
+                p.hsiz, *nrm, *vup, p.sign)
+            spec["binv"], spec["nbins"] = "scbin", "SCdim*SCdim"
         elif h[0] in "rt":
             spec["calfile"] = "reinhartb.cal"
             spec["params"] = "MF=%d,rNx=%g,rNy=%g,rNz=%g,Ux=%g,Uy=%g,Uz=%g,RHS=%s1" % (
@@ -328,6 +336,28 @@ def _origins(s: _Surf, x: np.ndarray, rng) -> np.ndarray:
     return v0 + a[:, None] * (v1 - v0) + b[:, None] * (v2_ - v0)
 
 
+def _square2disk(x: np.ndarray, y: np.ndarray):
+    """Shirley and Chiu's concentric map of the unit square onto the unit
+    disk ("A Low Distortion Map Between Disk and Square", 1997), the square's
+    four triangular regions about its centre each mapped to a quarter of the
+    disk (common/disk2square.c)."""
+    a, b = 2 * x - 1, 2 * y - 1
+    r = np.empty_like(a)
+    phi = np.zeros_like(a)
+    q = math.pi / 4
+    m1 = (a > -b) & (a > b)
+    m2 = (a > -b) & ~(a > b)
+    m3 = ~(a > -b) & (a < b)
+    m4 = ~(a > -b) & ~(a < b)
+    r[m1], phi[m1] = a[m1], q * (b[m1] / a[m1])
+    r[m2], phi[m2] = b[m2], q * (2 - a[m2] / b[m2])
+    r[m3], phi[m3] = -a[m3], q * (4 + b[m3] / a[m3])
+    r[m4] = -b[m4]
+    nz = m4 & (b != 0)
+    phi[nz] = q * (6 - a[nz] / b[nz])
+    return r * np.cos(phi), r * np.sin(phi)
+
+
 def _sender_rays(p: _Params, sampcnt: int, rng) -> tuple[np.ndarray, int]:
     """Rays leaving the sender, sampcnt per bin of its basis, bin by bin
     (rfluxmtx.c:724-1010: sample_origin, sample_uniform, sample_reinhart,
@@ -353,6 +383,15 @@ def _sender_rays(p: _Params, sampcnt: int, rng) -> tuple[np.ndarray, int]:
         ph = 2 * math.pi * rng.random(n)
         duvw = np.stack([r * np.cos(ph), r * np.sin(ph), np.sqrt(np.maximum(0, 1 - r * r))], axis=1)
         bins = [duvw]
+    elif h[:2] == "sc":
+        sc = p.hsiz
+        if sc <= 1:
+            raise GbError(-1, "missing size for Shirley-Chiu sampling!")
+        nb = sc * sc
+        bins = []
+        for b in range(nb):
+            dx, dy = _square2disk((b // sc + rng.random(n)) / sc, (b % sc + rng.random(n)) / sc)
+            bins.append(np.stack([dx, dy, np.sqrt(np.maximum(0.0, 1 - dx * dx - dy * dy))], axis=1))
     elif h[0] in "rt":
         mf = p.hsiz
         rowmax = 7 * mf + 1

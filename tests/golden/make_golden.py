@@ -243,6 +243,28 @@ def flux_matrices(tmp: Path) -> None:
         (sky.sum(axis=(1, 2)) > 0).mean(), (kf.sum(axis=(1, 2)) > 0).mean(), send[:, :, 0].sum(1).mean()))
 
 
+def flux_shirchiu(tmp: Path) -> None:
+    """rfluxmtx with Shirley-Chiu bases (h=sc4, util/disk2square.cal), -ab 0:
+    view rays passed through to the window opening binned as a receiver
+    (deterministic), and the window as a sender towards the sky behind an
+    exterior block (2000 samples per bin)."""
+    f = w.flux_files()
+    f["window_sc"] = f["window_kf"].replace("h=kf u=Z", "h=sc4 u=Z")
+    f["send_sc"] = f["window_send"].replace("h=kf u=Z", "h=sc4 u=Z")
+    for k, v in f.items():
+        (tmp / f"{k}.rad").write_text(v)
+    rays = np.load(OUT / "flux_matrices.npz")["rays"]
+    base = ["rfluxmtx", "-h", "-ab", "0", "-u-", "-fd"]
+    recv = np.frombuffer(run([*base, "-", tmp / "window_sc.rad", tmp / "interior.rad"], rays.astype("<f8").tobytes(),
+                             cwd=tmp), dtype="<f8").reshape(len(rays), -1, 3)
+    send = np.frombuffer(run([*base, "-c", "2000", tmp / "send_sc.rad", tmp / "sky.rad", tmp / "obstruction.rad"],
+                             cwd=tmp), dtype="<f8").reshape(16, -1, 3)
+    np.savez_compressed(OUT / "flux_shirchiu.npz", rays=rays, window_sc=recv, send=send, send_count=2000,
+                        cmd="rfluxmtx -h -ab 0 -u- -fd [-c 2000] sender receiver scene (h=sc4)")
+    print("flux sc: rows reaching the window %.3f, bins used %d; sender row mean %.4f" % (
+        (recv.sum(axis=(1, 2)) > 0).mean(), (recv.sum(axis=(0, 2)) > 0).sum(), send[:, :, 0].sum(1).mean()))
+
+
 def general_bins(tmp: Path) -> None:
     """General bin expressions: the sky subdivision of
     tests/golden/patchbins.cal (recursion, select, if, asin, atan2, floor,
@@ -494,7 +516,7 @@ def main() -> None:
     parts = {"octree": octree_digests, "c1": c1_direct, "c1p": c1_partitioned, "zoo": zoo, "glossy": glossy, "irr": surface_irradiance,
              "ss": supersampled_irradiance, "inst": instances, "circ": circular_sources,
              "trans": translucent, "bins": general_bins,
-             "spot": spotlights, "mirror": mirrors, "flux": flux_matrices,
+             "spot": spotlights, "mirror": mirrors, "flux": flux_matrices, "flux_sc": flux_shirchiu,
              "dct": lambda tmp: dct_small(), "dct4": lambda tmp: dct_four(), "rmtxop": lambda tmp: rmtxop_cases(), "trace_oct": lambda tmp: ref_fixture_trace(),
              "c2ab1": lambda tmp: c2_stats(tmp, ab=1, K=256), "c2ab3": lambda tmp: c2_stats(tmp, ab=3, K=256)}
     only = sys.argv[1:] or list(parts)         # e.g. make_golden.py c1p

@@ -454,6 +454,29 @@ def test_rfluxmtx(gb, tmp_path):
     assert (rel <= 1e-4).mean() >= 0.995
 
 
+def test_rfluxmtx_shirchiu(gb, tmp_path):
+    """Shirley-Chiu bases (h=sc4) end to end on the GPU: receiver bins of the
+    window opening (1e-4 for 99.5% of the rows) and the window as a sender
+    (sampling error) against the reference program."""
+    from pyradiance_gb300 import workloads as w
+    from test_oracle_golden import flux_close
+    g = golden("flux_shirchiu.npz")
+    f = w.flux_files()
+    (tmp_path / "recv.rad").write_text(f["window_kf"].replace("h=kf u=Z", "h=sc4 u=Z"))
+    (tmp_path / "send.rad").write_text(f["window_send"].replace("h=kf u=Z", "h=sc4 u=Z"))
+    for k in ("sky", "interior", "obstruction"):
+        (tmp_path / f"{k}.rad").write_text(f[k])
+    out = gb.rfluxmtx(tmp_path / "recv.rad", rays=g["rays"].astype("<f8").tobytes(),
+                      params=["-h", "-ab", "0", "-u-", "-fd"], scene=[tmp_path / "interior.rad"])
+    a = np.frombuffer(out, dtype="<f8").reshape(g["window_sc"].shape)
+    rel = np.abs(a - g["window_sc"]).max(axis=(1, 2)) / np.maximum(np.abs(g["window_sc"]).max(axis=(1, 2)), 1e-9)
+    assert (rel <= 1e-4).mean() >= 0.995, np.sort(rel)[-5:]
+    n = int(g["send_count"])
+    out = gb.rfluxmtx(tmp_path / "sky.rad", surface=tmp_path / "send.rad",
+                      params=["-h", "-ab", "0", "-u-", "-fd", "-c", str(n)], scene=[tmp_path / "obstruction.rad"])
+    flux_close(np.frombuffer(out, dtype="<f8").reshape(g["send"].shape)[:, :, 0], g["send"][:, :, 0], n)
+
+
 def test_instances(gb):
     """Instanced octrees (rt/o_instance.c:15-71): the furniture octree 12
     times in the room, rotated, scaled, mirrored, some with their own

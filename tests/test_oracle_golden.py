@@ -269,6 +269,32 @@ def test_flux_matrices(tmp_path):
     flux_close(out[:, :, 0], g["send"][:, :, 0], n)
 
 
+def test_flux_shirchiu(tmp_path):
+    """Shirley-Chiu bases (h=sc4, util/disk2square.cal) in rfluxmtx: the
+    window opening as a receiver, view rays passed through (1e-6), and the
+    window as a sender within sampling error."""
+    from pyradiance_gb300 import rflux
+    from pyradiance_gb300 import workloads as w
+    g = golden("flux_shirchiu.npz")
+    f = w.flux_files()
+    (tmp_path / "recv.rad").write_text(f["window_kf"].replace("h=kf u=Z", "h=sc4 u=Z"))
+    (tmp_path / "send.rad").write_text(f["window_send"].replace("h=kf u=Z", "h=sc4 u=Z"))
+    (tmp_path / "sky.rad").write_text(f["sky"])
+    o = po.default_opts("rcontrib", ab=0, u=0)
+    (tmp_path / "all.rad").write_text(f["interior"] + f["window_kf"])
+    out, _ = po.rcontrib(po.Scene(tmp_path / "all.rad"), o, rflux._receivers(tmp_path / "recv.rad"), g["rays"],
+                         threads=8)
+    np.testing.assert_allclose(out, g["window_sc"], rtol=1e-6, atol=1e-9)
+    n = int(g["send_count"])
+    rays, nb = rflux._sender_rays(rflux._sender(tmp_path / "send.rad"), n, np.random.default_rng(0))
+    assert nb == 16
+    o.c = n
+    (tmp_path / "all.rad").write_text(f["obstruction"] + f["sky"])
+    out, _ = po.rcontrib(po.Scene(tmp_path / "all.rad"), o, rflux._receivers(tmp_path / "sky.rad"), rays,
+                         threads=8)
+    flux_close(out[:, :, 0], g["send"][:, :, 0], n)
+
+
 def test_instances():
     """Instanced octrees (rt/o_instance.c:15-71, common/instance.c,
     common/xf.c): the furniture octree 12 times in the room, rotated,
