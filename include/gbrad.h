@@ -112,16 +112,22 @@ int  gb_rtrace(gb_scene *scene, const gb_opts *opts, const double *org_dir, int6
  * device array per device; a call whose rays would not fit (1.25 KiB per
  * ray without ambient bounces, about 650 bytes per first-hemisphere sample with
  * -I and -ab > 0) is rejected with GB_EINVAL and a message giving the
- * need.  The scene must have been loaded on the current
- * device.  The first call on a device looks the array up there (and may
- * load this library's device code); make that first call before capturing
- * work on any stream.  Calls on the same device share the array: calls that
- * overlap in time, from several threads or scenes, race and corrupt each
- * other's results; serialise them.  The call returns when the output is
- * complete.  No counterpart in the reference (its rtrace reads rays from a
+ * need.  All work is enqueued on `stream` (a cudaStream_t; NULL is the
+ * legacy default stream), after whatever the caller enqueued there before,
+ * so the rays may still be being written on that stream when the call is
+ * made; work on other streams must be complete.  The call returns when the
+ * output is complete; on an error return d_rgb is undefined, and no work of
+ * the call is left running.  The scene must have been loaded on the
+ * current device.  The first call on a device looks the array up there
+ * (and may load this library's device code) and keeps that address for the
+ * life of the process (a cudaDeviceReset() makes it stale); make that first
+ * call before capturing work on any stream.  Calls on the same device
+ * share the array: calls that overlap in time, from several threads,
+ * streams or scenes, race and corrupt each other's results; serialise
+ * them.  No counterpart in the reference (its rtrace reads rays from a
  * pipe, rt/rtrace.c:146-236). */
 int  gb_rtrace_device_noalloc(gb_scene *scene, const gb_opts *opts, const double *d_org_dir, int64_t n,
-                              double *d_rgb);
+                              double *d_rgb, void *stream);
 
 /* Material parameters.  Every material the scene's surfaces use has a
  * slot; gb_scene_material_rgb reads (get_rgb) and/or replaces (set_rgb) its

@@ -1900,12 +1900,13 @@ extern "C" int gb_dctimestep(const float *dc, const float *sky, int64_t M, int64
  * All working memory of a call -- the per-kernel counters, the queue
  * counters, the table of tracked modifiers (none for rtrace), the sensor
  * hemisphere records of -I, the two ray queues and the walk results -- is
- * carved from the one
- * static device array below; the rays and the output are the caller's.  The
- * kernels are those of gb_rtrace, so results agree with it up to the order
- * of the FP64 atomic additions.
+ * carved from the one static device array below; the rays and the output
+ * are the caller's.  The kernels are those of gb_rtrace, so results agree
+ * with it up to the order of the FP64 atomic additions.  Everything is
+ * enqueued on the caller's stream, so the call is ordered after whatever
+ * the caller enqueued there to write the rays.
  */
-#define GB_NOALLOC_SCRATCH_BYTES (64u << 20)   /* 64 MiB per device */
+#define GB_NOALLOC_SCRATCH_BYTES ((size_t)64 << 20)   /* 64 MiB per device */
 #define GB_NOALLOC_MAX_DEVICES 64
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[GB_NOALLOC_SCRATCH_BYTES];
@@ -1913,7 +1914,8 @@ static std::atomic<void *> g_noalloc_addr[GB_NOALLOC_MAX_DEVICES];
 
 /* Device address of the scratch on the current device.  The first call on a
  * device looks it up (which loads this module there if it is not loaded
- * yet); later calls reuse the address. */
+ * yet); later calls reuse the address for the life of the process, so a
+ * cudaDeviceReset() of that device leaves it stale. */
 static int noalloc_scratch(int dev, unsigned char **p)
 {
     if (dev < 0 || dev >= GB_NOALLOC_MAX_DEVICES)
@@ -1939,65 +1941,18 @@ static int on_device(const void *p, int dev)
     return (at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged) && at.device == dev;
 }
 
-extern "C" int gb_rtrace_device_noalloc(gb_scene *G, const gb_opts *o, const double *d_org_dir, int64_t n,
-                                        double *d_rgb)
+/* The launches of one call, all on stream st over the scratch at base. */
+static int noalloc_run(gb_scene *G, const gb_opts *o, const double *d_org_dir, int64_t n, double *d_rgb,
+                       cudaStream_t st, unsigned char *base, int n0, size_t stat_bytes, size_t nobj,
+                       const size_t *off, long long qcap)
 {
-    if (!G || !o || (n > 0 && (!d_org_dir || !d_rgb)) || n < 0)
-        return set_err(GB_EINVAL, "null argument or negative ray count");
-    g_stats[0] = g_stats[1] = g_stats[2] = g_stats[3] = 0;
-    memset(&g_prof, 0, sizeof g_prof);
-    int rc = check_shading(G, o);
-    if (rc < 0)
-        return rc;
-    if (n == 0)
-        return GB_OK;
-    int dev = 0;
-    CK(cudaGetDevice(&dev));
-    if (!on_device(G->ds.obj, dev))
-        return set_err(GB_EINVAL, "the scene was loaded on another device than the current one (%d)", dev);
-    if (!on_device(d_org_dir, dev) || !on_device(d_rgb, dev))
-        return set_err(GB_EINVAL, "rays and output must be device memory of the current device (%d)", dev);
-    unsigned char *base = nullptr;
-    rc = noalloc_scratch(dev, &base);
-    if (rc < 0)
-        return rc;
-
-    /* scratch layout, each part on a 256-byte boundary */
-    auto up = [](size_t b) { return (b + 255) & ~(size_t)255; };
-    const size_t stat_bytes = GB_K_N * GB_ST_N * sizeof(unsigned long long);
-    const int n0 = (o->I && o->ab > 0 && o->ad > 0) ? root_divisions(o) : 0;
-    if (n0 > 128)
-        return set_err(GB_EUNSUPPORTED, "-ad %d gives %d x %d hemisphere divisions; at most 128 x 128 are "
-                       "supported", o->ad, n0, n0);
-    if (G->H.ninst > 0)
-        return set_err(GB_EUNSUPPORTED, "scenes with instances are not traced without allocation");
-    if (check_supersampling(o, n0) < 0 || supersamples(o, n0) > 0)
-        return set_err(GB_EUNSUPPORTED, "ambient super-sampling (-as %d) is not implemented without allocation; "
-                       "use -as 0", o->as);
-    const size_t nobj = G->H.nobjs > 0 ? (size_t)G->H.nobjs : 1;
-    size_t off_stats = 0, off_cnt = up(stat_bytes), off_trk = off_cnt + up(4 * sizeof(unsigned long long));
-    size_t off_roots = off_trk + up(nobj * sizeof(int));
-    size_t off_spt = off_roots + (n0 > 0 ? up((size_t)n * sizeof(gb_rootrec)) : 0);
-    size_t off_draw = off_spt + (n0 > 0 ? up((size_t)n * n0 * n0 * sizeof(float2)) : 0);
-    size_t off_lot = off_draw + (n0 >= 4 ? up((size_t)n * n0 * n0 * sizeof(float2)) : 0);
-    size_t off_q = off_lot + (n0 >= 4 ? up((size_t)n * 2 * GB_XLOT * sizeof(float)) : 0);
-    /* the queue need gb_rtrace sizes for, without its 1M-ray minimum */
-    long long est = (long long)n * (n0 > 0 ? (long long)n0 * n0 * 4 : (o->ab > 0 ? (long long)o->ad * 2 : 8));
-    const size_t slot = 2 * sizeof(gb_qray) + sizeof(gb_qhit);   /* two queues and the walk results */
-    long long qcap = off_q < GB_NOALLOC_SCRATCH_BYTES ? (long long)((GB_NOALLOC_SCRATCH_BYTES - off_q) / slot) : 0;
-    if (est > qcap)
-        return set_err(GB_EINVAL, "%lld rays with these options need %.1f MiB of scratch; the static scratch "
-                       "is %u MiB (trace fewer rays per call)", (long long)n,
-                       (off_q + (double)est * slot) / 1048576.0, GB_NOALLOC_SCRATCH_BYTES >> 20);
-    qcap = (qcap / 4) * 4;
-
-    cudaStream_t st = G->stream;
-    unsigned long long *stats = (unsigned long long *)(base + off_stats);
-    unsigned long long *cnt = (unsigned long long *)(base + off_cnt);   /* [0] A, [1] B, [2] work items */
-    int *trk = (int *)(base + off_trk);
-    gb_qray *qa = (gb_qray *)(base + off_q);
+    unsigned long long *stats = (unsigned long long *)(base + off[0]);
+    unsigned long long *cnt = (unsigned long long *)(base + off[1]);   /* [0] A, [1] B, [2] work items */
+    int *trk = (int *)(base + off[2]);
+    gb_qray *qa = (gb_qray *)(base + off[6]);
     gb_qray *qb = qa + qcap;
     gb_qhit *hits = (gb_qhit *)(qb + qcap);
+    int rc;
     /* what must start at zero: the counters and the output, which the
      * kernels accumulate into; the table of tracked modifiers is all -1
      * (no modifier is tracked); queues and hemisphere records are written
@@ -2043,10 +1998,10 @@ extern "C" int gb_rtrace_device_noalloc(gb_scene *G, const gb_opts *o, const dou
     };
     if (o->I) {
         if (n0 > 0) {
-            P.roots = (gb_rootrec *)(base + off_roots);
-            P.root_spt = (float2 *)(base + off_spt);
-            P.root_draw = (float2 *)(base + off_draw);
-            P.root_lot = (float *)(base + off_lot);
+            P.roots = (gb_rootrec *)(base + off[3]);
+            P.root_spt = (float2 *)(base + off[4]);
+            P.root_draw = (float2 *)(base + off[5]);
+            P.root_lot = (float *)(base + off[7]);
         }
         P.root_n = n0;
         if ((rc = go(GB_K_ROOT, gb_launch_root)) < 0)
@@ -2104,4 +2059,89 @@ extern "C" int gb_rtrace_device_noalloc(gb_scene *G, const gb_opts *o, const dou
     if (overflow)
         return set_err(GB_EOVERFLOW, "ray queue overflow (%llu records dropped)", overflow);
     return GB_OK;
+}
+
+extern "C" int gb_rtrace_device_noalloc(gb_scene *G, const gb_opts *o, const double *d_org_dir, int64_t n,
+                                        double *d_rgb, void *stream)
+{
+    if (!G || !o || (n > 0 && (!d_org_dir || !d_rgb)) || n < 0)
+        return set_err(GB_EINVAL, "null argument or negative ray count");
+    g_stats[0] = g_stats[1] = g_stats[2] = g_stats[3] = 0;
+    memset(&g_prof, 0, sizeof g_prof);
+    int rc = check_shading(G, o);
+    if (rc < 0)
+        return rc;
+    if (n == 0)
+        return GB_OK;
+    int dev = 0;
+    CK(cudaGetDevice(&dev));
+    if (!on_device(G->ds.obj, dev))
+        return set_err(GB_EINVAL, "the scene was loaded on another device than the current one (%d)", dev);
+    if (!on_device(d_org_dir, dev) || !on_device(d_rgb, dev))
+        return set_err(GB_EINVAL, "rays and output must be device memory of the current device (%d)", dev);
+    unsigned char *base = nullptr;
+    rc = noalloc_scratch(dev, &base);
+    if (rc < 0)
+        return rc;
+
+    const int n0 = (o->I && o->ab > 0 && o->ad > 0) ? root_divisions(o) : 0;
+    if (n0 > 128)
+        return set_err(GB_EUNSUPPORTED, "-ad %d gives %d x %d hemisphere divisions; at most 128 x 128 are "
+                       "supported", o->ad, n0, n0);
+    if (G->H.ninst > 0)
+        return set_err(GB_EUNSUPPORTED, "scenes with instances are not traced without allocation");
+    if ((rc = check_supersampling(o, n0)) < 0)
+        return rc;
+    if (supersamples(o, n0) > 0)
+        return set_err(GB_EUNSUPPORTED, "ambient super-sampling (-as %d) is not implemented without allocation; "
+                       "use -as 0", o->as);
+
+    /* every ray needs at least 8 queue slots of 160 bytes: larger counts
+     * cannot fit, and rejecting them here keeps the sizes below from
+     * overflowing */
+    if (n > (int64_t)(GB_NOALLOC_SCRATCH_BYTES / 1024))
+        return set_err(GB_EINVAL, "%lld rays need more than the %u MiB static scratch (trace fewer rays per "
+                       "call)", (long long)n, (unsigned)(GB_NOALLOC_SCRATCH_BYTES >> 20));
+
+    /* scratch layout, each part on a 256-byte boundary: [0] kernel counters,
+     * [1] queue counters, [2] tracked-modifier table, [3] hemisphere records,
+     * [4] placed samples, [5] placement draws, [7] collision lots, [6] the
+     * two queues and the walk results (qcap slots each) */
+    auto up = [](size_t b) { return (b + 255) & ~(size_t)255; };
+    const size_t stat_bytes = GB_K_N * GB_ST_N * sizeof(unsigned long long);
+    const size_t nobj = G->H.nobjs > 0 ? (size_t)G->H.nobjs : 1;
+    const size_t un = (size_t)n, nn0 = (size_t)n0 * (size_t)n0;
+    size_t off[8];
+    off[0] = 0;
+    off[1] = up(stat_bytes);
+    off[2] = off[1] + up(4 * sizeof(unsigned long long));
+    off[3] = off[2] + up(nobj * sizeof(int));
+    off[4] = off[3] + (n0 > 0 ? up(un * sizeof(gb_rootrec)) : 0);
+    off[5] = off[4] + (n0 > 0 ? up(un * nn0 * sizeof(float2)) : 0);
+    off[7] = off[5] + (n0 >= 4 ? up(un * nn0 * sizeof(float2)) : 0);
+    off[6] = off[7] + (n0 >= 4 ? up(un * 2 * GB_XLOT * sizeof(float)) : 0);
+    /* the queue need gb_rtrace sizes for, without its 1M-ray minimum, and
+     * never less than 8 slots per ray */
+    long long est = (long long)n * (n0 > 0 ? (long long)nn0 * 4 : (o->ab > 0 ? (long long)o->ad * 2 : 8));
+    if (est < 8 * (long long)n)
+        est = 8 * (long long)n;
+    const size_t slot = 2 * sizeof(gb_qray) + sizeof(gb_qhit);   /* two queues and the walk results */
+    long long qcap = off[6] < GB_NOALLOC_SCRATCH_BYTES ? (long long)((GB_NOALLOC_SCRATCH_BYTES - off[6]) / slot) : 0;
+    if (off[6] >= GB_NOALLOC_SCRATCH_BYTES || est > qcap)
+        return set_err(GB_EINVAL, "%lld rays with these options need %.1f MiB of scratch; the static scratch "
+                       "is %u MiB (trace fewer rays per call)", (long long)n,
+                       (off[6] + (double)est * slot) / 1048576.0, (unsigned)(GB_NOALLOC_SCRATCH_BYTES >> 20));
+    qcap = (qcap / 4) * 4;
+    if (off[6] + (size_t)qcap * slot > GB_NOALLOC_SCRATCH_BYTES)   /* cannot happen: qcap was cut to fit */
+        return set_err(GB_EINVAL, "scratch layout exceeds the static array");
+
+    cudaStream_t st = (cudaStream_t)stream;
+    rc = noalloc_run(G, o, d_org_dir, n, d_rgb, st, base, n0, stat_bytes, nobj, off, qcap);
+    if (rc < 0) {
+        /* work may still be queued over the scratch and d_rgb: let it end
+         * before returning, so the next call does not race with it */
+        cudaStreamSynchronize(st);
+        cudaGetLastError();
+    }
+    return rc;
 }

@@ -752,7 +752,7 @@ static void make_face(const gb_object *o, gb_face *f)
 {
     const double *va = o->farg;
     double v1[3], v2[3], v3[3], d1;
-    int i, smalloff, badvert = 0;
+    int i;
     f->nv = o->nfargs / 3;
     if (f->nv > 3) {
         const double *a = va, *b = va + 3 * (f->nv - 1);
@@ -786,16 +786,10 @@ static void make_face(const gb_object *o, gb_face *f)
     }
     f->area *= 0.5;
     f->offset = f->norm[0] * va[0] + f->norm[1] * va[1] + f->norm[2] * va[2];
-    smalloff = fabs(f->offset) <= 1e-5;
     for (i = 1; i < f->nv; i++) {
         d1 = f->norm[0] * va[3 * i] + f->norm[1] * va[3 * i + 1] + f->norm[2] * va[3 * i + 2];
-        if (smalloff)
-            badvert += fabs(d1 - f->offset / i) > 1e-5;
-        else
-            badvert += fabs(1.0 - d1 * i / f->offset) > 1e-5;
         f->offset += d1;
     }
-    (void)badvert;
     f->offset /= (double)f->nv;
     f->ax = fabs(f->norm[1]) > fabs(f->norm[0]);
     if (fabs(f->norm[2]) > fabs(f->norm[f->ax]))

@@ -14,6 +14,16 @@ def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300)")
 
 
+def reference_tree():
+    """The reference source tree the reference programs were built from
+    (GB_REFERENCE, else the record the build leaves beside them), or None
+    where it is absent (the GPU machine)."""
+    env = os.environ.get("GB_REFERENCE")
+    rec = ROOT / "oracle" / "_ref" / "REFERENCE_TREE"
+    p = Path(env) if env else (Path(rec.read_text().strip()) if rec.exists() else None)
+    return p if p is not None and p.exists() else None
+
+
 def golden(name: str):
     return np.load(GOLDEN / name, allow_pickle=False)
 

@@ -8,10 +8,11 @@ from pathlib import Path
 import numpy as np
 import pytest
 
-from conftest import MODS_C2, golden, zscores
+from conftest import MODS_C2, golden, reference_tree, zscores
 from oracle import pyoracle as po
 
-REF_TRACE = Path("/root/reference/tests/Resources/trace.oct")
+_TREE = reference_tree()
+REF_TRACE = _TREE / "tests" / "Resources" / "trace.oct" if _TREE else Path("/nonexistent")
 
 
 @pytest.fixture(scope="module")

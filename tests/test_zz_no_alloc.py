@@ -4,7 +4,10 @@ The entry point traces rays that are already in device memory and carves
 all of its working memory from a static device array.  It runs the same
 kernels as gb_rtrace, so the values agree up to the order of FP64 atomic
 additions; each case calls it twice in a row, which also checks that the
-counters in the static array are reset between calls.  The file name sorts
+counters in the static array are reset between calls.  The rays are
+written on a torch side stream that the call is given, with no host
+synchronisation in between, so the test also checks that the call is
+ordered after the caller's writes.  The file name sorts
 last so that the cases also run after every other GPU test in one process.
 """
 import ctypes as C
@@ -43,14 +46,19 @@ def host_rtrace(_lib, sc, o, rays):
     return rgb
 
 
-def noalloc_rtrace(torch, _lib, sc, o, rays):
-    d_rays = torch.from_numpy(rays).to("cuda")
-    d_rgb = torch.full((len(rays), 3), float("nan"), dtype=torch.float64, device="cuda")
-    torch.cuda.synchronize()
-    rc = _lib.lib().gb_rtrace_device_noalloc(sc.handle, o, C.c_void_p(d_rays.data_ptr()), len(rays),
-                                             C.c_void_p(d_rgb.data_ptr()))
-    _lib.check(rc)
-    return d_rgb.cpu().numpy()
+def noalloc_rtrace(torch, _lib, sc, o, rays, side=True):
+    """Rays copied in and the output cleared on a torch side stream, with no
+    host synchronisation before the call: the call is enqueued on that
+    stream, so it must see the rays (side=False: torch's default stream)."""
+    stream = torch.cuda.Stream() if side else torch.cuda.default_stream()
+    with torch.cuda.stream(stream):
+        h_rays = torch.from_numpy(rays).pin_memory()
+        d_rays = h_rays.to("cuda", non_blocking=True)
+        d_rgb = torch.full((len(rays), 3), float("nan"), dtype=torch.float64, device="cuda")
+        rc = _lib.lib().gb_rtrace_device_noalloc(sc.handle, o, C.c_void_p(d_rays.data_ptr()), len(rays),
+                                                 C.c_void_p(d_rgb.data_ptr()), C.c_void_p(stream.cuda_stream))
+        _lib.check(rc)
+        return d_rgb.cpu().numpy()
 
 
 CASES = {
@@ -79,8 +87,8 @@ def test_noalloc_matches_rtrace_twice(env, case):
     o = opts(_lib, **kw)
     ref = host_rtrace(_lib, sc, o, rays)
     assert np.isfinite(ref).all() and ref.max() > 0
-    for _ in range(2):
-        got = noalloc_rtrace(torch, _lib, sc, o, rays)
+    for side in (True, False):
+        got = noalloc_rtrace(torch, _lib, sc, o, rays, side=side)
         np.testing.assert_allclose(got, ref, rtol=rtol, atol=1e-300)
 
 
@@ -103,5 +111,12 @@ def test_noalloc_rejects_oversized_calls(env):
     d_rgb = torch.zeros((4, 3), dtype=torch.float64, device="cuda")
     host_rays = np.ascontiguousarray(rays[:4])
     rc = _lib.lib().gb_rtrace_device_noalloc(scenes["c2"].handle, opts(_lib, ab=0), _lib.ptr(host_rays), 4,
-                                             C.c_void_p(d_rgb.data_ptr()))
+                                             C.c_void_p(d_rgb.data_ptr()), None)
     assert rc == -1
+    # more rays than the scratch can hold at any options: refused before any
+    # size arithmetic
+    big = torch.zeros((1 << 20, 6), dtype=torch.float64, device="cuda")
+    out = torch.zeros((1 << 20, 3), dtype=torch.float64, device="cuda")
+    rc = _lib.lib().gb_rtrace_device_noalloc(scenes["c2"].handle, opts(_lib, ab=1, ad=0), C.c_void_p(big.data_ptr()),
+                                             1 << 20, C.c_void_p(out.data_ptr()), None)
+    assert rc == -1 and "scratch" in _lib.lib().gb_last_error().decode()
