@@ -43,6 +43,9 @@ WORKLOAD = ("rcontrib daylight coefficients: 4096 sensors (64x64 grid, z=0.8, +z
             "triangles; glow sky + ground, Reinhart MF:1 + ground = 146 bins")
 # algorithmic bytes per unit of traversal work: one child code per node descent,
 # set offset + count per cube visit, object record + vertices per test
+# the config of both arms' lines (the driver compares them)
+CONFIG = {"workload": None, "sensors_per_gpu": 4096,
+          "l2": "GPU arm: L2 flushed (256 MB write) before each step; CPU arm: no cache control"}
 B_NODE, B_STEP, B_TEST = 4, 8, 60
 B_RAYIO = 48 + 32          # the walk kernel reads origin, direction, origin object; writes a 32-byte result
 
@@ -118,42 +121,56 @@ def make_scene(tmp: Path):
 
 # ------------------------------------------------------------ CPU baseline
 
-def cpu_baseline(rad: Path, rays: np.ndarray, seconds: float = 15.0):
-    """The oracle (a scalar FP64 port of the reference algorithm) on the host
-    cores, on a bounded sample: sensors of the same grid, OpenMP threads over
-    sensors.  Returns (Mrays/s, threads, sample description)."""
+def port_sample(rad: Path, rays: np.ndarray, nsteps: int, per_step: int, threads: int):
+    """The oracle (an FP64 port of the reference algorithm, OpenMP threads
+    over sensors) on `nsteps` samples of `per_step` sensors each, drawn in
+    turn from a fixed shuffle of the grid (wrapping around).  Returns (rays,
+    seconds) of each step."""
     from oracle import pyoracle as po
-    threads = os.cpu_count() or 1
     sc = po.Scene(rad)
     o = po.default_opts("rcontrib", I=1, ab=3, ad=1024, lw=1e-4, c=1, u=0, seed=1)
     mods = [dict(modifier="groundglow"),
             dict(modifier="skyglow", calfile="reinhartb.cal", params="MF=1", binv="rbin", nbins="Nrbins")]
-    n = threads * 2
-    total_rays, total_t, used = 0, 0.0, 0
-    idx = np.linspace(0, len(rays) - 1, len(rays)).astype(int)
-    rng = np.random.default_rng(0)
-    rng.shuffle(idx)
-    while total_t < seconds and used < len(rays):
-        sel = rays[idx[used:used + n]]
+    idx = np.arange(len(rays))
+    np.random.default_rng(0).shuffle(idx)
+    out, pos = [], 0
+    for _ in range(nsteps):
+        sel = rays[np.take(idx, np.arange(pos, pos + per_step), mode="wrap")]
+        pos += per_step
+        o.replica = pos
         t0 = time.perf_counter()
         _, nr = po.rcontrib(sc, o, mods, sel, threads=threads)
-        total_t += time.perf_counter() - t0
-        total_rays += nr
-        used += len(sel)
-    return total_rays / total_t / 1e6, threads, f"{used} of the 4096 sensors (random subset), full -ab 3 -ad 1024 paths"
+        out.append((nr, time.perf_counter() - t0))
+    return out
+
+
+def cpu_baseline(rad: Path, rays: np.ndarray, seconds: float = 15.0):
+    """The oracle port on all host cores over a bounded sample of the grid's
+    sensors (about `seconds` of work).  Returns (Mrays/s, threads, sample
+    description)."""
+    threads = os.cpu_count() or 1
+    per = 2 * threads
+    first = port_sample(rad, rays, 1, per, threads)[0]
+    steps = max(1, int(seconds / max(first[1], 1e-3)))
+    res = [first] + port_sample(rad, rays, steps, per, threads)
+    nr, t = sum(r[0] for r in res), sum(r[1] for r in res)
+    return nr / t / 1e6, threads, f"{per * len(res)} sensor paths of the grid in {len(res)} samples of {per}"
 
 
 def reference_arm(args):
     """--impl reference: the reference's CPU implementation of the path on
-    the host cores: the reference rcontrib compiled from its sources where it
-    is present (oracle/_ref), else the oracle port of it."""
+    the host cores, one bounded sample of the workload's sensors per step:
+    the reference rcontrib compiled from its sources where it is present
+    (oracle/_ref), else the oracle port of it.  Rays are counted with the
+    oracle's counters on the same sensors (the GPU's definition)."""
     rank, world, _ = dist_env()
     if rank != 0:
         return
+    threads = os.cpu_count() or 1
     with tempfile.TemporaryDirectory() as td:
         rad, rays = make_scene(Path(td))
         ref_bin = ROOT / "oracle" / "_ref" / "bin"
-        threads = os.cpu_count() or 1
+        per = 4 * threads
         if (ref_bin / "rcontrib").exists() and (ref_bin / "oconv").exists():
             from oracle import pyoracle as po
             from pyradiance_gb300 import workloads as w
@@ -161,33 +178,38 @@ def reference_arm(args):
             octp = Path(td) / "scene.oct"
             octp.write_bytes(subprocess.run([str(ref_bin / "oconv"), str(rad)], capture_output=True,
                                             check=True, env=env).stdout)
-            n = threads * 32
-            sel = rays[np.linspace(0, len(rays) - 1, n).astype(int)]
-            # ray count of this sample from the oracle's counters (same definition as the GPU's)
             sc = po.Scene(rad)
             o = po.default_opts("rcontrib", I=1, ab=3, ad=1024, lw=1e-4, c=1, u=0, seed=3)
             mods = [dict(modifier="groundglow"),
                     dict(modifier="skyglow", calfile="reinhartb.cal", params="MF=1", binv="rbin",
                          nbins="Nrbins")]
-            _, nrays = po.rcontrib(sc, o, mods, sel, threads=threads)
-            times = []
-            for _ in range(max(1, args.steps)):
+            idx = np.arange(len(rays))
+            np.random.default_rng(0).shuffle(idx)
+            total_rays, total_t = 0, 0.0
+            for step in range(args.warmup + args.steps):
+                sel = rays[np.take(idx, np.arange(step * per, (step + 1) * per), mode="wrap")]
                 t0 = time.perf_counter()
                 subprocess.run([str(ref_bin / "rcontrib"), "-h", "-n", str(threads), "-I+", "-ab", "3", "-ad",
                                 "1024", "-lw", "1e-4", "-c", "1", "-fad", "-m", "groundglow", "-f",
                                 "reinhartb.cal", "-p", "MF=1", "-b", "rbin", "-bn", "Nrbins", "-m", "skyglow",
                                 str(octp)], input=w.rays_ascii(sel), capture_output=True, check=True, env=env,
                                cwd=td)
-                times.append(time.perf_counter() - t0)
-            v = nrays / statistics.median(times) / 1e6
-            kind, sample = "reference", f"{n} sensors of the grid, rcontrib -n {threads}"
+                t = time.perf_counter() - t0
+                if step >= args.warmup:
+                    _, nr = po.rcontrib(sc, o, mods, sel, threads=threads)
+                    total_rays += nr
+                    total_t += t
+            kind, sample = "reference", f"{args.steps} samples of {per} sensors of the grid, rcontrib -n {threads}"
         else:
-            v, threads, sample = cpu_baseline(rad, rays, seconds=max(10.0, 5.0 * args.steps))
-            kind = "port"
+            port_sample(rad, rays, args.warmup, per, threads)
+            res = port_sample(rad, rays, args.steps, per, threads)
+            total_rays, total_t = sum(r[0] for r in res), sum(r[1] for r in res)
+            kind, sample = "port", f"{args.steps} samples of {per} sensors of the grid, {threads} threads"
+    v = total_rays / total_t / 1e6
     line = {"metric": METRIC, "value": round(v, 4), "unit": "Mrays/s", "impl": "reference", "n_gpus": world,
-            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
-            "config": {"workload": WORKLOAD},
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(total_t * 1e3 / args.steps, 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded scene and sensor grid)", "config": dict(CONFIG, workload=WORKLOAD),
             "cpu_baseline": {"value": round(v, 4), "unit": "Mrays/s", "cores": threads, "kind": kind,
                              "sample": sample},
             "e2e": {"value": round(v, 4), "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -208,54 +230,129 @@ def traffic_from_profiles(kernel: str):
     return None
 
 
-DCT_SHAPE = (1024, 2306, 8760)     # 1/16 of the rows of a 16,384-sensor x 2,306-patch x 8,760-hour run
+DCT_SHAPE = (16384, 2306, 8760)    # 16,384 sensors x 2,306 Reinhart MF:4 patches x 8,760 hours
+
+
+def dct_operands(dev, M, K, N, seed=0):
+    """Annual daylight-coefficient operands: DC lognormal(-6, 2) with 30%
+    exact zeros; sky lognormal(2, 1) diffuse background plus, in each
+    daylight hour, one sun patch of 1e4..1e6 (log-uniform); about half of
+    the hours are night (all-zero columns)."""
+    import torch
+    g = torch.Generator(device=dev).manual_seed(seed)
+    dc = torch.exp(torch.randn(M, K, 3, device=dev, generator=g) * 2 - 6)
+    dc[torch.rand(M, K, device=dev, generator=g) < 0.3] = 0
+    sky = torch.exp(torch.randn(K, N, 3, device=dev, generator=g) + 2)
+    sun = torch.randint(0, K, (N,), device=dev, generator=g)
+    peak = torch.exp(torch.empty(N, device=dev).uniform_(np.log(1e4), np.log(1e6), generator=g))
+    sky[sun, torch.arange(N, device=dev), :] = peak[:, None]
+    sky[:, torch.rand(N, device=dev, generator=g) < 0.5] = 0
+    return dc, sky
+
+
+def dct_cpu_baseline(dc, sky):
+    """The oracle's restatement of cm_multiply (FP64 accumulation, zero rows
+    and columns skipped, OpenMP over rows) on all host cores for two row
+    samples of the operands (r and 2r rows): the difference gives the cost
+    per row, the rest the fixed cost (the zero-column scan), and the sum
+    scales to all rows."""
+    from oracle import pyoracle as po
+    threads = os.cpu_count() or 1
+    M = dc.shape[0]
+    b = np.ascontiguousarray(sky.cpu().numpy())
+    r = 2 * threads
+    ts = []
+    for n in (r, 2 * r):
+        a = np.ascontiguousarray(dc[np.linspace(0, M - 1, n).astype(int)].cpu().numpy())
+        t0 = time.perf_counter()
+        po.dctimestep(a, b, threads=threads)
+        ts.append(time.perf_counter() - t0)
+    per_row = max(ts[1] - ts[0], 1e-9) / r
+    fixed = max(ts[0] - per_row * r, 0.0)
+    return {"value": round(fixed + per_row * M, 2), "unit": "s per product", "cores": threads, "kind": "port",
+            "sample": f"{r} and {2 * r} of the {M} rows ({ts[0]:.2f} s, {ts[1]:.2f} s), scaled to all rows"}
 
 
 def dct_measure(dev, steps: int):
-    """DC x sky (dctimestep) on the device: BF16x3 on the tensor cores and
-    the FP32 CUDA-core kernel on the same resident operands (lognormal DC
-    with 30% zeros, half of the sky's hours dark), each timed with CUDA
-    events on the calling stream (best of `steps`), and the error of both
-    against an FP64 product of the same operands."""
+    """DC x sky (dctimestep) on the device at the annual workload's full
+    size: the tensor-core forms (FP16X3, BF16X3, FP16) and the FP32 CUDA-core
+    kernel on the same resident operands, each a whole gb_dctimestep_device
+    call timed with CUDA events on the calling stream (best of `steps`), the
+    error of each against the FP64 kernel's product of the same operands,
+    cuBLAS FP32 (torch.matmul per channel on de-interleaved copies, TF32
+    off) for comparison, and the CPU restatement on a row sample."""
     import ctypes as C
     import torch
     from pyradiance_gb300 import _lib
     L = _lib.lib()
     M, K, N = DCT_SHAPE
-    g = torch.Generator(device=dev).manual_seed(0)
-    dc = torch.exp(torch.randn(M, K, 3, device=dev, generator=g) * 2 - 6)
-    dc[torch.rand(M, K, device=dev, generator=g) < 0.3] = 0
-    sky = torch.exp(torch.randn(K, N, 3, device=dev, generator=g) + 2)
-    sky[:, torch.rand(N, device=dev, generator=g) < 0.5] = 0
+    dc, sky = dct_operands(dev, M, K, N)
     st = torch.cuda.current_stream(dev)
-    outs, ms = {}, {}
-    for mode, name, reps in ((_lib.GB_DCT_FP64, "fp64", 1), (_lib.GB_DCT_FP32, "fp32", max(3, steps)),
-                             (_lib.GB_DCT_BF16X3, "bf16x3", max(3, steps))):
-        out = torch.empty(M, N, 3, device=dev)
+
+    def timed(fn, reps):
         ts = []
         for _ in range(reps):
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             e0.record(st)
-            _lib.check(L.gb_dctimestep_device(C.c_void_p(dc.data_ptr()), C.c_void_p(sky.data_ptr()), M, K, N,
-                                              mode, C.c_void_p(out.data_ptr()), C.c_void_p(st.cuda_stream)))
+            fn()
             e1.record(st)
             torch.cuda.synchronize(dev)
             ts.append(e0.elapsed_time(e1))
-        outs[name], ms[name] = out, min(ts)
-    ref = outs["fp64"].double()
-    nz = ref > 0
+        return min(ts)
+
+    out = torch.empty(M, N, 3, device=dev)
+
+    def call(mode):
+        _lib.check(L.gb_dctimestep_device(C.c_void_p(dc.data_ptr()), C.c_void_p(sky.data_ptr()), M, K, N,
+                                          mode, C.c_void_p(out.data_ptr()), C.c_void_p(st.cuda_stream)))
+
+    call(_lib.GB_DCT_FP64)
+    ref = out.double()
+    nz = ref != 0
     flops = 2.0 * M * K * N * 3
-    res = {"shape": {"M": M, "K": K, "N": N}, "flops": flops}
-    for name in ("fp32", "bf16x3"):
-        rel = (outs[name].double() - ref).abs()[nz] / ref[nz]
-        res[name] = {"ms": round(ms[name], 3), "tflops": round(flops / ms[name] / 1e9, 1),
+    day = int((sky.abs().amax(dim=(0, 2)) > 0).sum())
+    rows = int((dc.abs().amax(dim=(1, 2)) > 0).sum())
+    flops_nz = 2.0 * rows * K * day * 3
+    res = {"shape": {"M": M, "K": K, "N": N}, "flops": flops, "nonzero_columns": day, "nonzero_rows": rows,
+           "flops_nonzero": flops_nz, "l2": "operands and output larger than L2"}
+    reps = max(3, steps)
+    for mode, name in ((_lib.GB_DCT_FP16X3, "fp16x3"), (_lib.GB_DCT_BF16X3, "bf16x3"), (_lib.GB_DCT_FP16, "fp16"),
+                       (_lib.GB_DCT_FP32, "fp32")):
+        call(mode)
+        ms = timed(lambda: call(mode), reps if name != "fp32" else 3)
+        rel = (out.double() - ref).abs()[nz] / ref.abs()[nz]
+        res[name] = {"ms": round(ms, 3), "tflops": round(flops / ms / 1e9, 1),
                      "err_vs_fp64": {"mean_rel": float(rel.mean()), "max_rel": float(rel.max())}}
-    res["speedup_bf16x3_vs_fp32"] = round(ms["fp32"] / ms["bf16x3"], 2)
+        del rel
+    del ref, nz
+    # cuBLAS FP32 on de-interleaved copies (copies outside the timed region)
+    prev = torch.backends.cuda.matmul.allow_tf32
+    torch.backends.cuda.matmul.allow_tf32 = False
+    a = [dc[..., c].contiguous() for c in range(3)]
+    b = [sky[..., c].contiguous() for c in range(3)]
+    o = [torch.empty(M, N, device=dev) for _ in range(3)]
+
+    def sgemm():
+        for c in range(3):
+            torch.matmul(a[c], b[c], out=o[c])
+    sgemm()
+    ms = timed(sgemm, 3)
+    torch.backends.cuda.matmul.allow_tf32 = prev
+    res["cublas_fp32"] = {"ms": round(ms, 3), "tflops": round(flops / ms / 1e9, 1),
+                          "note": "torch.matmul per channel on planar copies, TF32 off"}
+    del a, b, o
+    res["speedup_fp16x3_vs_fp32"] = round(res["fp32"]["ms"] / res["fp16x3"]["ms"], 2)
+    res["speedup_fp16x3_vs_cublas_fp32"] = round(res["cublas_fp32"]["ms"] / res["fp16x3"]["ms"], 2)
+    res["speedup_bf16x3_vs_fp32"] = round(res["fp32"]["ms"] / res["bf16x3"]["ms"], 2)
     peak, kind = peaks("bf16")
-    res["tensor_frac"] = {"achieved_tflops": round(3 * flops / ms["bf16x3"] / 1e9, 1), "peak": peak,
-                          "frac": round(3 * flops / ms["bf16x3"] / 1e9 / peak, 4), "peak_source": kind,
-                          "note": "three bf16 products per useful product (hi*hi + hi*lo + lo*hi); the time "
-                                  "includes the hi/lo split of both operands"}
+    tc = 3 * flops_nz / res["fp16x3"]["ms"] / 1e9
+    res["tensor_frac"] = {"achieved_tflops": round(tc, 1), "peak": peak, "frac": round(tc / peak, 4),
+                          "peak_source": kind,
+                          "note": "FP16X3: three fp16 products per useful product over the non-zero rows and "
+                                  "columns; the time is the whole call (scans, split, zero fill, product)"}
+    res["cpu_baseline"] = dct_cpu_baseline(dc, sky)
+    del dc, sky, out
+    torch.cuda.empty_cache()
     return res
 
 
@@ -460,10 +557,10 @@ def gpu_arm(args):
             "steps": args.steps, "warmup": max(3, args.warmup), "ms_per_step": round(dev_s * 1e3 / args.steps, 3),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded scene and sensor grid)",
-            "config": {"workload": WORKLOAD, "sensors_per_gpu": int(len(rays)), "l2": "flushed before each step",
-                       "rays_per_step_per_gpu": int(rays_tot / args.steps), "kernels": {k: {
-                           "ms_per_step": round(v["ms"] / args.steps, 3), "launches": v["launches"]}
-                           for k, v in agg.items()}},
+            "config": dict(CONFIG, workload=WORKLOAD, sensors_per_gpu=int(len(rays))),
+            "detail": {"rays_per_step_per_gpu": int(rays_tot / args.steps), "kernels": {k: {
+                "ms_per_step": round(v["ms"] / args.steps, 3), "launches": v["launches"]}
+                for k, v in agg.items()}},
             "e2e": {"value": round(e2e, 3), "unit": "Mrays/s", "h2d_bytes_per_step": int(rays.nbytes),
                     "d2h_bytes_per_step": int(len(rays) * 146 * 3 * 8)},
             "gpu_launches": int(launches),

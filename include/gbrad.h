@@ -177,11 +177,26 @@ int  gb_rcontrib_nbins(const gb_modspec *mods, int nmods, int *nbins_total);
 /* dctimestep's two-matrix product R[m,n,c] = sum_k DC[m,k,c] * S[k,n,c]
  * (util/dctimestep.c:324-393, util/cmatrix.c:421-474); all matrices are
  * interleaved RGB float32 (row-major, 3 floats per element).  mode selects
- * the arithmetic: GB_DCT_FP32 (FP32 FMA), GB_DCT_BF16X3 (bf16 split,
- * 3 tensor-core products, FP32 accumulate), GB_DCT_FP64 (FP64 FMA). */
-#define GB_DCT_FP32  0
+ * the arithmetic:
+ *   GB_DCT_FP32    FP32 FMA on the CUDA cores
+ *   GB_DCT_BF16X3  bf16 hi/lo split, 3 tensor-core products, FP32 accumulate
+ *                  (up to about 2e-5 relative error where one product
+ *                  dominates an output)
+ *   GB_DCT_FP64    FP64 FMA on the CUDA cores
+ *   GB_DCT_FP16X3  rows of DC and columns of S scaled by powers of two into
+ *                  the FP16 range, fp16 hi/lo split, 3 tensor-core products,
+ *                  FP32 accumulate (within 1e-5 relative of FP64)
+ *   GB_DCT_FP16    the same scaled fp16 operands, one product (about 1e-3)
+ * The tensor-core forms skip all-zero rows of DC and all-zero columns of S
+ * as cm_multiply does (their outputs are zero).  The environment variable
+ * GB_DCT_WAIT_NS (nanoseconds, read at each call) shortens the limit of the
+ * tensor-core pipeline's waits, normally 2 s, after which a call returns
+ * GB_ECUDA: for tests of that error path. */
+#define GB_DCT_FP32   0
 #define GB_DCT_BF16X3 1
-#define GB_DCT_FP64  2
+#define GB_DCT_FP64   2
+#define GB_DCT_FP16X3 3
+#define GB_DCT_FP16   4
 int  gb_dctimestep(const float *dc, const float *sky, int64_t M, int64_t K, int64_t N, int mode,
                    float *out);
 /* Same on device pointers already resident in HBM (no copies). */

@@ -22,6 +22,8 @@ GB_PROG_RCONTRIB = 1
 GB_DCT_FP32 = 0
 GB_DCT_BF16X3 = 1
 GB_DCT_FP64 = 2
+GB_DCT_FP16X3 = 3
+GB_DCT_FP16 = 4
 
 ERRORS = {-1: "EINVAL", -2: "EIO", -3: "EUNSUPPORTED", -4: "ECUDA", -5: "ENOMEM", -6: "EOVERFLOW"}
 

@@ -93,8 +93,8 @@ int gb_dct_device(const float *A, const float *B, int64_t M, int64_t K, int64_t 
         err = "bad matrix dimensions";
         return GB_EINVAL;
     }
-    if (mode == GB_DCT_BF16X3)
-        return gb_dct_bf16x3(A, B, M, K, N, C, st, err);
+    if (mode == GB_DCT_BF16X3 || mode == GB_DCT_FP16X3 || mode == GB_DCT_FP16)
+        return gb_dct_tc(A, B, M, K, N, mode, C, st, err);
     dim3 grid((unsigned)((N + TN - 1) / TN), (unsigned)((M + TM - 1) / TM));
     if (grid.y > 65535) {
         err = "too many rows for one launch";

@@ -11,8 +11,8 @@
 int gb_dct_device(const float *A, const float *B, int64_t M, int64_t K, int64_t N, int mode, float *C,
                   cudaStream_t st, std::string &err);
 
-/* BF16x3 tensor-core path (dct_tc.cu) */
-int gb_dct_bf16x3(const float *A, const float *B, int64_t M, int64_t K, int64_t N, float *C, cudaStream_t st,
-                  std::string &err);
+/* tensor-core forms (dct_tc.cu): GB_DCT_BF16X3, GB_DCT_FP16X3, GB_DCT_FP16 */
+int gb_dct_tc(const float *A, const float *B, int64_t M, int64_t K, int64_t N, int mode, float *C,
+              cudaStream_t st, std::string &err);
 
 #endif

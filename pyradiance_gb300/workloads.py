@@ -62,6 +62,14 @@ def _room_shell(mod: str, window=None) -> str:
     out.append(_poly(mod, "east", [(X, 0, 0), (X, 0, Z), (X, Y, Z), (X, Y, 0)]))
     if window is None:
         out.append(_poly(mod, "south", [(0, 0, 0), (0, 0, Z), (X, 0, Z), (X, 0, 0)]))
+    elif isinstance(window, list):               # several openings side by side
+        xl = 0.0
+        for i, (x0, x1, z0, z1) in enumerate(window):
+            out.append(_poly(mod, f"south_s{i}", [(xl, 0, 0), (xl, 0, Z), (x0, 0, Z), (x0, 0, 0)]))
+            out.append(_poly(mod, f"south_b{i}", [(x0, 0, 0), (x0, 0, z0), (x1, 0, z0), (x1, 0, 0)]))
+            out.append(_poly(mod, f"south_t{i}", [(x0, 0, z1), (x0, 0, Z), (x1, 0, Z), (x1, 0, z1)]))
+            xl = x1
+        out.append(_poly(mod, "south_r", [(xl, 0, 0), (xl, 0, Z), (X, 0, Z), (X, 0, 0)]))
     else:
         x0, x1, z0, z1 = window
         out.append(_poly(mod, "south_l", [(0, 0, 0), (0, 0, Z), (x0, 0, Z), (x0, 0, 0)]))
@@ -135,19 +143,33 @@ def daylight_room(seed: int = 0, nboxes: int = 200, light: bool = True) -> str:
 WINDOW = (3.5, 6.5, 0.5, 2.5)
 
 
-def window_room(seed: int = 0, ntri: int = 20000, nmat: int | None = None) -> str:
-    """Room shell with a glass window in the south wall, random interior
+def window_room(seed: int = 0, ntri: int = 20000, nmat: int | None = None, nwin: int = 1,
+                tessellated: bool = False) -> str:
+    """Room shell with glass windows in the south wall (one 2 x 3 m window,
+    or ``nwin`` of 1..8 smaller ones side by side), random interior
     triangles and the glow sky/ground.  ``nmat`` groups the triangles into
-    that many materials (default: one material per triangle)."""
+    that many materials (default: one material per triangle).  Triangle
+    edges are 0.05..0.5 m; with ``tessellated`` they shrink as
+    sqrt(20000 / ntri), so that any count covers the area of 20,000 such
+    triangles, as a finer tessellation of the same furniture would."""
     rng = np.random.default_rng(seed)
     X, Y, Z = ROOM
-    out = [_mat_plastic("room_mat", (0.5, 0.5, 0.5)), _room_shell("room_mat", WINDOW)]
-    out.append("void glass window_glass\n0\n0\n3 .6 .6 .6\n\n")
     x0, x1, z0, z1 = WINDOW
-    out.append(_poly("window_glass", "window", [(x0, 0, z0), (x0, 0, z1), (x1, 0, z1), (x1, 0, z0)]))
+    if nwin <= 1:
+        wins = [WINDOW]
+    else:
+        w = (x1 - x0) * 2.0 / (2 * nwin - 1) if nwin <= 4 else 8.0 / (2 * nwin - 1)
+        xs = (X - (2 * nwin - 1) * w) / 2
+        wins = [(xs + 2 * i * w, xs + 2 * i * w + w, z0, z1) for i in range(nwin)]
+    out = [_mat_plastic("room_mat", (0.5, 0.5, 0.5)), _room_shell("room_mat", wins if nwin > 1 else WINDOW)]
+    out.append("void glass window_glass\n0\n0\n3 .6 .6 .6\n\n")
+    for i, (a0, a1, b0, b1) in enumerate(wins):
+        out.append(_poly("window_glass", "window" if i == 0 else f"window{i}",
+                         [(a0, 0, b0), (a0, 0, b1), (a1, 0, b1), (a1, 0, b0)]))
     margin = 0.05
     v0 = rng.uniform((margin, margin, margin), (X - margin, Y - margin, Z - margin), size=(ntri, 3))
-    lens = rng.uniform(0.05, 0.5, size=(ntri, 2))
+    scale = np.sqrt(20000.0 / ntri) if tessellated and ntri > 20000 else 1.0
+    lens = rng.uniform(0.05, 0.5, size=(ntri, 2)) * scale
     dirs = rng.normal(size=(ntri, 2, 3))
     dirs /= np.linalg.norm(dirs, axis=2, keepdims=True)
     v1 = v0 + lens[:, 0:1] * dirs[:, 0]
@@ -159,8 +181,10 @@ def window_room(seed: int = 0, ntri: int = 20000, nmat: int | None = None) -> st
     rho = rng.uniform(0.1, 0.8, size=nm)
     for m in range(nm):
         out.append(_mat_plastic(f"tri_mat{m}", (rho[m],) * 3))
-    for i in range(ntri):
-        out.append(_poly(f"tri_mat{i % nm}", f"tri{i}", [v0[i], v1[i], v2[i]]))
+    fmt = "tri_mat%d polygon tri%d\n0\n0\n9 " + " ".join(["%.9g"] * 9) + "\n\n"   # as _poly formats
+    idx = np.arange(ntri)
+    rows = np.column_stack([idx % nm, idx, v0, v1, v2]).tolist()
+    out.append("".join([fmt % (int(r[0]), int(r[1]), *r[2:]) for r in rows]))
     out.append(SKY_GLOW)
     return "".join(out)
 

@@ -37,6 +37,38 @@ def run(args, inp: bytes | None = None, cwd=None) -> bytes:
     return p.stdout
 
 
+def run_independent(args, rays: np.ndarray, shards: int | None = None) -> bytes:
+    """A -u+ (time-seeded) rcontrib or rtrace run over many rays in parallel
+    with independent random streams: `shards` separate single-process runs
+    over contiguous parts of the rays, started more than a second apart.
+    The reference seeds its generator once per process with the time in
+    seconds (rt/rcmain.c:330-336), and the workers of -n N are forked after
+    that seeding, so they draw identical random sequences: replicas of one
+    sensor handled by different workers come out equal.  Outputs are
+    concatenated in ray order."""
+    import time
+    shards = shards or (os.cpu_count() or 1)
+    env = dict(os.environ, RAYPATH=f".:{REF / 'lib'}", PATH=f"{BIN}:{os.environ.get('PATH', '')}")
+    parts = np.array_split(np.ascontiguousarray(rays, dtype="<f8"), shards)
+    procs = []
+    with tempfile.TemporaryDirectory() as td:
+        for i, part in enumerate(parts):
+            fin = Path(td) / f"in{i}"
+            fin.write_bytes(part.tobytes())
+            if i:
+                time.sleep(1.1)
+            with open(fin, "rb") as fi, open(Path(td) / f"out{i}", "wb") as fo, \
+                    open(Path(td) / f"err{i}", "wb") as fe:
+                procs.append(subprocess.Popen([str(BIN / args[0]), *map(str, args[1:])], stdin=fi, stdout=fo,
+                                              stderr=fe, env=env))
+        outs = []
+        for i, p in enumerate(procs):
+            if p.wait() != 0:
+                raise RuntimeError(f"{args[0]} failed: {(Path(td) / f'err{i}').read_text()}")
+            outs.append((Path(td) / f"out{i}").read_bytes())
+    return b"".join(outs)
+
+
 def oconv(rad_text: str, tmp: Path, name: str) -> Path:
     rad = tmp / f"{name}.rad"
     rad.write_text(rad_text)
@@ -397,23 +429,66 @@ MODS = ["-m", "groundglow", "-f", "reinhartb.cal", "-p", "MF=1", "-b", "rbin", "
 def c2_stats(tmp: Path, nsens: int = 32, K: int = 256, ab: int = 3) -> None:
     """rcontrib daylight coefficients on a subset of the 64 x 64 grid, each
     sensor replicated K times with uncorrelated sampling (-u+, the
-    reference's default): per-sensor, per-bin sample mean and standard
-    error of channel 0 (the scene is gray)."""
+    reference's default) in independent processes: per-sensor, per-bin
+    sample mean and standard error of channel 0 (the scene is gray)."""
     octp = oconv(w.window_room(), tmp, "c2")
     grid = w.sensor_grid(64, 64)
     idx = np.linspace(0, len(grid) - 1, nsens).astype(int)
     rays = grid[idx]
     rep = np.repeat(rays, K, axis=0)
-    out = run(["rcontrib", "-h", "-u+", "-n", str(os.cpu_count() or 1), "-I+", "-ab", str(ab), "-ad", "1024",
-               "-lw", "1e-4", "-c", "1", "-fdd", *MODS, octp], rep.astype("<f8").tobytes())
-    a = np.frombuffer(out, dtype="<f8").reshape(nsens, K, 146, 3)[..., 0]
+    out = run_independent(["rcontrib", "-h", "-u+", "-I+", "-ab", str(ab), "-ad", "1024", "-lw", "1e-4", "-c", "1",
+                           "-fdd", *MODS, octp], rep)
+    a = np.frombuffer(out, dtype="<f8").reshape(nsens, K, 146, 3)
+    assert (a[..., 0] == a[..., 1]).all() and (a[..., 0] == a[..., 2]).all()
+    a = a[..., 0]
+    check_independent(a)
     grp = np.stack([a[:, :, e0:e1].sum(2) for e0, e1 in zip(ROW_EDGES[:-1], ROW_EDGES[1:])], 2)
     np.savez_compressed(OUT / f"c2_stats_ab{ab}.npz", sensor_index=idx, rays=rays, K=K,
                         mean=a.mean(1), se=a.std(1, ddof=1) / np.sqrt(K), nnz=(a > 0).sum(1),
                         group_mean=grp.mean(1), group_se=grp.std(1, ddof=1) / np.sqrt(K),
                         total_mean=a.sum(2).mean(1), total_se=a.sum(2).std(1, ddof=1) / np.sqrt(K),
-                        cmd="rcontrib -h -u+ -I+ -ab %d -ad 1024 -lw 1e-4 -c 1 " % ab + " ".join(MODS))
+                        cmd="rcontrib -h -u+ -I+ -ab %d -ad 1024 -lw 1e-4 -c 1 " % ab + " ".join(MODS)
+                        + " (independent -n 1 processes)")
     print("c2_stats ab%d: mean total %.4g" % (ab, a.sum(2).mean()))
+
+
+def check_independent(a: np.ndarray) -> None:
+    """No two replicas of a sensor that reach ten bins or more may be equal
+    (equal replicas mean shared random streams; records of a few sky
+    samples through the window can coincide by chance)."""
+    for s in range(a.shape[0]):
+        rich = a[s][(a[s] > 0).sum(1) >= 10]
+        if len(rich) > 1:
+            assert len(np.unique(rich, axis=0)) == len(rich), f"sensor {s}: replicas repeat"
+
+
+def c2_headline(tmp: Path, nsens: int = 256, K: int = 64) -> None:
+    """The headline rcontrib workload (the window room, -I+ -ab 3 -ad 1024
+    -lw 1e-4 -c 1, Reinhart MF:1 + ground) on 256 evenly spaced sensors of
+    its 64 x 64 grid, each replicated 64 times with -u+ in independent
+    processes: 64 x 1,024 = 2^16 first-hemisphere samples per sensor.
+    Per-sensor, per-bin mean and standard error of channel 0 (the scene is
+    gray), float32."""
+    octp = oconv(w.window_room(), tmp, "c2")
+    grid = w.sensor_grid(64, 64)
+    idx = np.linspace(0, len(grid) - 1, nsens).astype(int)
+    rays = grid[idx]
+    rep = np.repeat(rays, K, axis=0)
+    out = run_independent(["rcontrib", "-h", "-u+", "-I+", "-ab", "3", "-ad", "1024", "-lw", "1e-4", "-c", "1",
+                           "-fdd", *MODS, octp], rep)
+    a = np.frombuffer(out, dtype="<f8").reshape(nsens, K, 146, 3)
+    assert (a[..., 0] == a[..., 1]).all() and (a[..., 0] == a[..., 2]).all()
+    a = a[..., 0]
+    check_independent(a)
+    grp = np.stack([a[:, :, e0:e1].sum(2) for e0, e1 in zip(ROW_EDGES[:-1], ROW_EDGES[1:])], 2)
+    np.savez_compressed(OUT / "c2_headline.npz", sensor_index=idx, rays=rays, K=K,
+                        mean=a.mean(1).astype(np.float32), se=(a.std(1, ddof=1) / np.sqrt(K)).astype(np.float32),
+                        nnz=(a > 0).sum(1).astype(np.int16),
+                        group_mean=grp.mean(1), group_se=grp.std(1, ddof=1) / np.sqrt(K),
+                        total_mean=a.sum(2).mean(1), total_se=a.sum(2).std(1, ddof=1) / np.sqrt(K),
+                        cmd="rcontrib -h -u+ -I+ -ab 3 -ad 1024 -lw 1e-4 -c 1 " + " ".join(MODS)
+                        + " (64 replicas per sensor in independent -n 1 processes)")
+    print("c2_headline: mean total %.4g, lit sensors %d" % (a.sum(2).mean(), (a.sum((1, 2)) > 0).sum()))
 
 
 def dct_four() -> None:
@@ -518,7 +593,8 @@ def main() -> None:
              "trans": translucent, "bins": general_bins,
              "spot": spotlights, "mirror": mirrors, "flux": flux_matrices, "flux_sc": flux_shirchiu,
              "dct": lambda tmp: dct_small(), "dct4": lambda tmp: dct_four(), "rmtxop": lambda tmp: rmtxop_cases(), "trace_oct": lambda tmp: ref_fixture_trace(),
-             "c2ab1": lambda tmp: c2_stats(tmp, ab=1, K=256), "c2ab3": lambda tmp: c2_stats(tmp, ab=3, K=256)}
+             "c2ab1": lambda tmp: c2_stats(tmp, ab=1, K=256), "c2ab3": lambda tmp: c2_stats(tmp, ab=3, K=256),
+             "c2head": c2_headline}
     only = sys.argv[1:] or list(parts)         # e.g. make_golden.py c1p
     with tempfile.TemporaryDirectory() as td:
         tmp = Path(td)

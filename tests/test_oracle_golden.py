@@ -3,6 +3,7 @@
 These pin the oracle (and the host scene loader and octree builder it
 shares with the library) before it is used to check the GPU.  CPU only.
 """
+import os
 from pathlib import Path
 
 import numpy as np
@@ -379,6 +380,87 @@ def check_c2_statistics(a, g, K):
     if len(zb) >= 20:
         assert abs(zb.mean()) < 0.5 and zb.std() < 1.5 and (np.abs(zb) > 4).mean() < 0.01, (zb.mean(), zb.std())
     return zt, zg, zb
+
+
+def headline_stats(a, g):
+    """a: (sensors, K, 146) samples of channel 0 of the headline rcontrib
+    workload; g: the reference's statistics of the same 256 sensors (64
+    replicas of 1,024 first-hemisphere samples).  Returns
+      z   the z-scores (difference of means over the combined standard
+          error) of every sensor x bin that both sides sample in at least
+          two replicas;
+      zg  the same for each sensor's sums over the Reinhart altitude rows
+          (and the ground bin), where both sides sample the row in a
+          quarter of their replicas or more;
+      p   for every sensor x bin that either side samples, the two-sided
+          p-value of its replica counts under equal rates (given the total
+          count, this side's count is binomial with probability K/(K+Kr)).
+    Most sensor x bin pairs are sampled by neither side (sensors under
+    boxes, bins no path reaches)."""
+    from scipy.stats import binom
+    from conftest import ROW_EDGES
+    K, Kr = a.shape[1], int(g["K"])
+    m, se, nn = a.mean(1), a.std(1, ddof=1) / np.sqrt(K), (a > 0).sum(1)
+    rm, rse, rn = g["mean"].astype(np.float64), g["se"].astype(np.float64), g["nnz"].astype(np.int64)
+    both = (nn >= 2) & (rn >= 2)
+    z = (m - rm)[both] / np.sqrt(se ** 2 + rse ** 2)[both]
+    grp = np.stack([a[:, :, e0:e1].sum(2) for e0, e1 in zip(ROW_EDGES[:-1], ROW_EDGES[1:])], 2)
+    gm, gs, gn = grp.mean(1), grp.std(1, ddof=1) / np.sqrt(K), (grp > 0).sum(1)
+    ok = (gn * 4 >= K) & (g["group_se"] > 0)
+    zg = (gm - g["group_mean"])[ok] / np.sqrt(gs ** 2 + g["group_se"] ** 2)[ok]
+    any_ = (nn > 0) | (rn > 0)
+    x, t = nn[any_], (nn + rn)[any_]
+    q = K / (K + Kr)
+    p = np.minimum(1.0, 2 * np.minimum(binom.cdf(x, t, q), binom.sf(x - 1, t, q)))
+    return z, zg, p
+
+
+def within_normal_rate(z, zmax):
+    """The share of |z| beyond 3 may exceed its rate under equal means
+    (0.27%) by at most four binomial standard deviations; no |z| beyond
+    zmax."""
+    n, p3 = len(z), 0.0027
+    share = (np.abs(z) > 3).mean()
+    assert share <= p3 + 4 * np.sqrt(p3 * (1 - p3) / n), (share, n)
+    assert np.abs(z).max() <= zmax, np.sort(np.abs(z))[-5:]
+
+
+def check_headline_bins(a, g):
+    """Every sensor x bin mean that both sides sample twice or more within
+    the reference's at the rate a normal variable allows, none beyond 5.5
+    standard errors (probability about 1e-3 over these bins under equal
+    means); every sensor's altitude-row sums likewise, none beyond 5, their
+    mean z within four standard errors of 0; the sampling rate of every bin
+    that either side reaches consistent with the reference's (count
+    p-values: at most 0.27% below 0.0027 plus four binomial standard
+    deviations, none below 1e-3 / the number of bins)."""
+    z, zg, p = headline_stats(a, g)
+    assert len(z) >= 1000 and len(zg) >= 300 and len(p) >= 2000, (len(z), len(zg), len(p))
+    within_normal_rate(z, 5.5)
+    within_normal_rate(zg, 5.0)
+    assert abs(zg.mean()) < 4 / np.sqrt(len(zg)), zg.mean()
+    n, p3 = len(p), 0.0027
+    assert (p < p3).mean() <= p3 + 4 * np.sqrt(p3 * (1 - p3) / n), ((p < p3).mean(), n)
+    assert p.min() * n >= 1e-3, np.sort(p)[:5]
+    return z, zg, p
+
+
+def test_headline_rcontrib_bins_vs_reference(oscenes):
+    """The oracle at 64 replicas of the headline workload's 256 sensors
+    against the reference's 64 independent replicas (2^16 first-hemisphere
+    samples per sensor on each side): per sensor x bin.  Equal replica
+    counts keep the comparison symmetric: the mean of a few skewed samples
+    falls below the true mean more often than above, and unequal counts
+    would shift the z-scores."""
+    g = golden("c2_headline.npz")
+    K = int(g["K"])
+    rays = np.repeat(g["rays"], K, axis=0)
+    o = po.default_opts("rcontrib", I=1, ab=3, ad=1024, lw=1e-4, c=1, u=0, seed=97)
+    out, _ = po.rcontrib(oscenes["c2"], o, MODS_C2, rays, threads=os.cpu_count() or 1)
+    z, zg, p = check_headline_bins(out[..., 0].reshape(len(g["rays"]), K, 146), g)
+    print("oracle vs reference: %d bins, share |z|>3 %.4f, max %.2f; %d row sums, max %.2f; %d counts, "
+          "min p %.2g" % (len(z), (np.abs(z) > 3).mean(), np.abs(z).max(), len(zg), np.abs(zg).max(), len(p),
+                          p.min()))
 
 
 @pytest.mark.parametrize("ab,K", [(1, 128), (3, 48)])

@@ -117,6 +117,7 @@ def test_noalloc_rejects_oversized_calls(env):
     # size arithmetic
     big = torch.zeros((1 << 20, 6), dtype=torch.float64, device="cuda")
     out = torch.zeros((1 << 20, 3), dtype=torch.float64, device="cuda")
-    rc = _lib.lib().gb_rtrace_device_noalloc(scenes["c2"].handle, opts(_lib, ab=1, ad=0), C.c_void_p(big.data_ptr()),
+    rc = _lib.lib().gb_rtrace_device_noalloc(scenes["c2"].handle, opts(_lib, ab=1, ad=0, aa=0),
+                                             C.c_void_p(big.data_ptr()),
                                              1 << 20, C.c_void_p(out.data_ptr()), None)
     assert rc == -1 and "scratch" in _lib.lib().gb_last_error().decode()
