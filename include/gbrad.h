@@ -84,6 +84,14 @@ int  gb_scene_load(const char *oct_path, gb_scene **out);
  * runs it: util/rfluxmtx.c:139-178). */
 int  gb_scene_load_rad(const char *const *paths, int npaths, int objlim, int resolu, gb_scene **out);
 void gb_scene_free(gb_scene *scene);
+/* The octree of a loaded scene: node and set counts, an FNV-1a digest of
+ * its pre-order structure with each leaf's sorted object set (equal
+ * digests, equal trees), and whether gb_scene_load_rad built it on the GPU
+ * (scenes of polygons and spheres on a machine with a GPU; the host builder
+ * otherwise, or with GB_OCTREE_BUILDER=host).  No counterpart in the
+ * reference (oconv writes the tree to a file, ot/writeoct.c). */
+int  gb_scene_octree_info(const gb_scene *scene, int64_t *nodes, int64_t *sets, uint64_t *digest,
+                          int *built_on_device);
 /* Number of objects; name, modifier name and material name of an object
  * (the -os/-om/-oM outputs of rt/rtrace.c:824-860). */
 int64_t     gb_scene_nobjects(const gb_scene *scene);

@@ -161,13 +161,14 @@ def dctimestep(dc: np.ndarray, sky: np.ndarray, threads: int = 1) -> np.ndarray:
     return out
 
 
-def octree_digest(path, rad: bool | None = None):
-    """(nodes, sets, hash) of an octree file or of the octree built from scene text."""
+def octree_digest(path, rad: bool | None = None, objlim: int = 6, resolu: int = 16384):
+    """(nodes, sets, hash) of an octree file or of the octree built from scene
+    text (oconv's -n objlim and -r resolution)."""
     path = str(path)
     is_rad = path.endswith(".rad") if rad is None else rad
     L = lib()
-    L.orc_octree_digest.argtypes = [C.c_char_p, C.c_int, C.POINTER(C.c_uint64)]
+    L.orc_octree_digest.argtypes = [C.c_char_p, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_uint64)]
     out = (C.c_uint64 * 3)()
-    if L.orc_octree_digest(path.encode(), int(is_rad), out) != 0:
+    if L.orc_octree_digest(path.encode(), int(is_rad), objlim, resolu, out) != 0:
         raise RuntimeError("oracle: " + L.orc_last_error().decode())
     return [int(out[0]), int(out[1]), int(out[2])]

@@ -2137,13 +2137,13 @@ static void digest_tree(const gb_scene_host *H, int32_t code, uint64_t *h)
 #undef MIX
 }
 
-int orc_octree_digest(const char *path, int is_rad, uint64_t out[3])
+int orc_octree_digest(const char *path, int is_rad, int objlim, int resolu, uint64_t out[3])
 {
     gb_scene_host H;
     uint64_t h = 1469598103934665603ull;
     int rc;
     gb_scene_init(&H);
-    rc = is_rad ? (gb_scene_read_rad_file(&H, path) < 0 || gb_scene_build_octree(&H, 6, 16384) < 0)
+    rc = is_rad ? (gb_scene_read_rad_file(&H, path) < 0 || gb_scene_build_octree(&H, objlim, resolu) < 0)
                 : gb_scene_read_oct(&H, path) < 0;
     if (rc) {
         snprintf(orc_err, sizeof orc_err, "%s", gb_scene_error());

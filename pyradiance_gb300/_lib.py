@@ -56,6 +56,8 @@ _SIGS = {
     "gb_scene_load": (C.c_int, [C.c_char_p, C.POINTER(C.c_void_p)]),
     "gb_scene_load_rad": (C.c_int, [C.POINTER(C.c_char_p), C.c_int, C.c_int, C.c_int, C.POINTER(C.c_void_p)]),
     "gb_scene_free": (None, [C.c_void_p]),
+    "gb_scene_octree_info": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64),
+                                       C.POINTER(C.c_uint64), C.POINTER(C.c_int)]),
     "gb_scene_nobjects": (C.c_int64, [C.c_void_p]),
     "gb_scene_object_name": (C.c_char_p, [C.c_void_p, C.c_int64]),
     "gb_scene_modifier_name": (C.c_char_p, [C.c_void_p, C.c_int64]),

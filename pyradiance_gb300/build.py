@@ -21,7 +21,10 @@ OBJ = HERE / "_build"
 LIB = HERE / "libgbrad.so"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CU_SOURCES = ["trace.cu", "host.cu", "dct.cu", "dct_tc.cu"]
+CU_SOURCES = ["trace.cu", "host.cu", "dct.cu", "dct_tc.cu", "octbuild_gpu.cu"]
+# per-file flags: the device octree builder's FP64 tests must round as the
+# host builder's (no contracted multiply-adds)
+CU_FLAGS = {"octbuild_gpu.cu": ["-fmad=false"]}
 CXX_SOURCES = ["binexpr.cpp"]
 C_SOURCES = ["scene.c", "octbuild.c"]
 
@@ -56,7 +59,7 @@ def build(verbose: bool = False, force: bool = False) -> Path:
         src, obj = CSRC / s, OBJ / (s + ".o")
         objs.append(obj)
         if force or _stale(src, obj, headers):
-            jobs.append([nvcc, *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
+            jobs.append([nvcc, *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", *CU_FLAGS.get(s, []),
                          "-Xptxas", "-v" if verbose else "-O3", "-c", str(src), "-o", str(obj)])
     for s in CXX_SOURCES:
         src, obj = CSRC / s, OBJ / (s + ".o")

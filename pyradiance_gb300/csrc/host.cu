@@ -113,6 +113,7 @@ struct gb_scene {
     int sms = 0;
     cudaEvent_t ev[2 * GB_TIMED_LAUNCHES + 2];
     int nev = 0;
+    int octree_on_device = 0;          /* the octree was built by the device builder */
     std::string tuned_key;             /* options of the queue-size pilot */
     double tuned_per_sensor = 0.0;     /* its queue slots per sensor */
 };
@@ -830,12 +831,63 @@ extern "C" int gb_scene_load_rad(const char *const *paths, int npaths, int objli
             gb_scene_free(G);
             return rc;
         }
-    if (gb_scene_build_octree(&G->H, objlim, resolu) < 0 || gb_scene_load_instances(&G->H, ".") < 0) {
+    /* the octree: on the device where there is one and the scene is of
+     * polygons and spheres (GB_OCTREE_BUILDER=host forces the host
+     * builder); both give the same tree */
+    int dev_rc = 1, ndev = 0;
+    const char *which = getenv("GB_OCTREE_BUILDER");
+    if (!(which && !strcmp(which, "host")) && cudaGetDeviceCount(&ndev) == cudaSuccess && ndev > 0) {
+        char why[256] = "";
+        dev_rc = gb_scene_build_octree_device(&G->H, objlim, resolu, why, sizeof why);
+        if (dev_rc < 0)
+            cudaGetLastError();          /* the host builder below starts afresh */
+    } else
+        cudaGetLastError();
+    G->octree_on_device = dev_rc == 0;
+    if ((dev_rc != 0 && gb_scene_build_octree(&G->H, objlim, resolu) < 0) || gb_scene_load_instances(&G->H, ".") < 0) {
         int rc = set_err(GB_EIO, "octree build failed: %s", gb_scene_error());
         gb_scene_free(G);
         return rc;
     }
     return finish_load(G, out);
+}
+
+/* node count, set count and an FNV-1a hash over the pre-order tree with
+ * each leaf's sorted set: equal for equal octrees */
+static void digest_code(const gb_scene_host *H, int32_t code, uint64_t *h)
+{
+    auto mix = [h](uint32_t v) { *h = (*h ^ (uint64_t)v) * 1099511628211ull; };
+    if (code >= 0) {
+        mix(2);
+        for (int k = 0; k < 8; k++)
+            digest_code(H, H->kids[8 * code + k], h);
+    } else if (code == -1) {
+        mix(0);
+    } else {
+        const int32_t *st = gb_scene_set(H, code);
+        mix(1);
+        for (int k = 0; k <= st[0]; k++)
+            mix((uint32_t)st[k]);
+    }
+}
+
+extern "C" int gb_scene_octree_info(const gb_scene *G, int64_t *nodes, int64_t *sets, uint64_t *digest,
+                                    int *built_on_device)
+{
+    if (!G)
+        return set_err(GB_EINVAL, "null scene");
+    if (nodes)
+        *nodes = G->H.nnodes;
+    if (sets)
+        *sets = G->H.nsets;
+    if (digest) {
+        uint64_t h = 1469598103934665603ull;
+        digest_code(&G->H, G->H.root, &h);
+        *digest = h;
+    }
+    if (built_on_device)
+        *built_on_device = G->octree_on_device;
+    return GB_OK;
 }
 
 extern "C" void gb_scene_free(gb_scene *G)

@@ -442,9 +442,6 @@ static int leaf_equal(const bnode *a, const bnode *b)
            (a->n == 0 || !memcmp(a->set, b->set, (size_t)a->n * sizeof(int32_t)));
 }
 
-int32_t gb__add_set(gb_scene_host *S, const int32_t *set);
-int32_t gb__new_node(gb_scene_host *S);
-
 /* merge a tree whose 8 children are identical leaves into that leaf
  * (common/octree.c:73-90) */
 static void combine(builder *B, int32_t nd)
@@ -503,12 +500,13 @@ static int32_t flatten(builder *B, int32_t nd, int *ok)
     }
 }
 
-int gb_scene_build_octree(gb_scene_host *S, int objlim, int resolu)
+/* Prepares the objects and sets the scene cube from their bounding box
+ * (ot/oconv.c:128-150); -1 for objects no octree is built over here. */
+int gb_scene_octree_cube(gb_scene_host *S)
 {
     double bbmin[3], bbmax[3];
-    builder B;
-    int32_t i, root;
-    int k, ok = 1;
+    int32_t i;
+    int k;
     if (gb_scene_prepare(S) < 0)
         return -1;
     for (k = 0; k < 3; k++) {
@@ -570,6 +568,16 @@ int gb_scene_build_octree(gb_scene_host *S, int objlim, int resolu)
         for (k = 0; k < 3; k++)
             S->cuorg[k] = (bbmax[k] + bbmin[k] - S->cusize) * .5;
     }
+    return 0;
+}
+
+int gb_scene_build_octree(gb_scene_host *S, int objlim, int resolu)
+{
+    builder B;
+    int32_t i, root;
+    int ok = 1;
+    if (gb_scene_octree_cube(S) < 0)
+        return -1;
     memset(&B, 0, sizeof B);
     B.S = S;
     B.objlim = objlim > 0 ? objlim : 6;

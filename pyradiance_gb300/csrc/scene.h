@@ -163,6 +163,16 @@ int gb_fullxf(gb_xf *f, gb_xf *b, int ac, char *const *av);
  * objects added in definition order, full nodes split above objlim objects
  * until the cube is smaller than cusize/resolu. */
 int gb_scene_build_octree(gb_scene_host *S, int objlim, int resolu);
+/* the first step of gb_scene_build_octree: objects prepared and the scene
+ * cube set from their bounding box */
+int gb_scene_octree_cube(gb_scene_host *S);
+/* the same octree built on the current CUDA device (octbuild_gpu.cu):
+ * 0 built, 1 the scene holds objects only the host builder handles, < 0
+ * failure (reason in err) */
+int gb_scene_build_octree_device(gb_scene_host *S, int objlim, int resolu, char *err, size_t errlen);
+/* the builder's storage of nodes and leaf sets (scene.c) */
+int32_t gb__add_set(gb_scene_host *S, const int32_t *set);
+int32_t gb__new_node(gb_scene_host *S);
 
 /* Precompute faces and cones; checks argument counts. */
 int gb_scene_prepare(gb_scene_host *S);
