@@ -404,27 +404,49 @@ def grad_measure(steps: int):
 BATCH_ARGS = ["-I+", "-ab", "2", "-ad", "512", "-lw", "1e-4", "-c", "1", "-u-"]
 
 
+def _room_text(args):
+    """Scene text of one batching room (run in a worker process)."""
+    import sys as _s
+    _s.path.insert(0, str(ROOT))
+    from pyradiance_gb300 import workloads as w
+    path, seed, ntri, nwin = args
+    Path(path).write_text(w.window_room(seed=seed, ntri=ntri, nmat=64, nwin=nwin, tessellated=True))
+    return path
+
+
 def batch_measure(steps: int):
     """Batched grids: 256 sensor grids of lognormal sizes (median 1,024,
-    clipped to 64..16,384) over 16 window rooms with log-uniform triangle
-    counts, rcontrib -ab 2 -ad 512 into Reinhart MF:1 + ground, all in one
-    gb_rcontrib_batch call; against one 16,384-sensor grid on the median
-    scene with the same options.  Wall-clock rays/s of whole calls (host
-    buffers in and out), best of `steps`."""
+    clipped to 64..16,384) over 16 window rooms of log-uniform triangle
+    counts in [5e4, 2e6] (finer tessellations of the same furniture: edges
+    shrink as the count grows, so the area stays that of 20,000 triangles)
+    with 1..8 windows, rcontrib -ab 2 -ad 512 into Reinhart MF:1 + ground,
+    all in one gb_rcontrib_batch call (per scene: one wavefront over its
+    grids, the generation loop captured in a CUDA graph, queue size and walk
+    shape from the scene's tuner); against one 16,384-sensor grid on the
+    median scene with the same options.  Wall-clock rays/s of whole calls
+    (host buffers in and out), best of `steps`; scene text is written by
+    worker processes and loaded (octrees built on the GPU) before timing."""
     import concurrent.futures as cf
+    import multiprocessing as mp
     import pyradiance_gb300 as gb
-    from pyradiance_gb300 import workloads as w
     rng = np.random.default_rng(2026)
-    ntri = np.exp(rng.uniform(np.log(2e4), np.log(1.6e5), 16)).astype(int)
+    ntri = np.exp(rng.uniform(np.log(5e4), np.log(2e6), 16)).astype(int)
+    nwin = rng.integers(1, 9, 16)
     sizes = np.clip(np.exp(rng.normal(np.log(1024), 1.0, 256)), 64, 16384).astype(int)
     owner = rng.integers(0, 16, 256)
     with tempfile.TemporaryDirectory() as td:
-        def build(k):
-            p = Path(td) / f"room{k}.rad"
-            p.write_text(w.window_room(seed=100 + k, ntri=int(ntri[k]), nmat=64))
-            return gb.Scene(rad_files=[p])
+        jobs_txt = [(str(Path(td) / f"room{k}.rad"), 100 + k, int(ntri[k]), int(nwin[k])) for k in range(16)]
+        t0 = time.perf_counter()
+        with cf.ProcessPoolExecutor(max_workers=min(16, os.cpu_count() or 1),
+                                    mp_context=mp.get_context("spawn")) as ex:
+            paths = list(ex.map(_room_text, jobs_txt))
+        t_text = time.perf_counter() - t0
+        t0 = time.perf_counter()
         with cf.ThreadPoolExecutor(max_workers=min(16, os.cpu_count() or 1)) as ex:
-            scenes = list(ex.map(build, range(16)))
+            scenes = list(ex.map(lambda p: gb.Scene(rad_files=[p]), paths))
+        t_load = time.perf_counter() - t0
+    on_dev = sum(_octree_on_device(s) for s in scenes)
+
     def sensors(n, seed):
         r = np.random.default_rng(seed)
         xy = r.uniform((0.3, 0.3), (9.7, 7.7), size=(n, 2))
@@ -436,7 +458,9 @@ def batch_measure(steps: int):
     rc.seed = 7
     median = int(np.argsort(ntri)[8])
     single = sensors(16384, 99)
-    rc.run_batch(jobs)                                   # warm-up (and queue-size pilots)
+    t0 = time.perf_counter()
+    rc.run_batch(jobs)                                   # warm-up (and the scenes' tuners)
+    t_first = time.perf_counter() - t0
     rc.octree = scenes[median]
     rc.run_array(single)
     tb, tsg, rays_b, rays_s = [], [], 0, 0
@@ -451,11 +475,23 @@ def batch_measure(steps: int):
         rays_s = rc.last_rays
     vb, vs = rays_b / min(tb) / 1e6, rays_s / min(tsg) / 1e6
     return {"workload": f"256 grids (sizes lognormal median 1024, 64..16384; {int(sizes.sum())} sensors) over 16 "
-                        f"window rooms of {int(ntri.min())}..{int(ntri.max())} triangles, rcontrib "
+                        f"window rooms of {int(ntri.min())}..{int(ntri.max())} triangles "
+                        f"({int(ntri.sum())} in all) with {int(nwin.min())}..{int(nwin.max())} windows, rcontrib "
                         + " ".join(BATCH_ARGS) + ", Reinhart MF:1 + ground",
             "batch_mrays_s": round(vb, 1), "single_grid_mrays_s": round(vs, 1),
             "batch_vs_single": round(vb / vs, 3), "batch_s": round(min(tb), 3), "rays_batch": int(rays_b),
-            "single_grid": "16384 sensors on the median scene"}
+            "single_grid": f"16384 sensors on the median scene ({int(ntri[median])} triangles)",
+            "scene_text_s": round(t_text, 2), "scene_load_s": round(t_load, 2),
+            "octrees_built_on_gpu": int(on_dev), "first_batch_s_with_tuners": round(t_first, 3),
+            "graphs": os.environ.get("GB_GRAPHS", "1") != "0"}
+
+
+def _octree_on_device(sc) -> int:
+    import ctypes as C
+    from pyradiance_gb300 import _lib
+    d = C.c_int()
+    _lib.check(_lib.lib().gb_scene_octree_info(sc.handle, None, None, None, C.byref(d)))
+    return d.value
 
 
 def combine_ranks(dev_s: float, wall_s: float, rays: float, world: int, device=None):

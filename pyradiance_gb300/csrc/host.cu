@@ -114,6 +114,10 @@ struct gb_scene {
     cudaEvent_t ev[2 * GB_TIMED_LAUNCHES + 2];
     int nev = 0;
     int octree_on_device = 0;          /* the octree was built by the device builder */
+    /* walk kernel shape picked by the tuner (0: defaults), and whether runs
+     * capture their generation loop in a CUDA graph (batched runs) */
+    int tuned_refill = 0, tuned_blocks = 0;
+    bool use_graph = false;
     std::string tuned_key;             /* options of the queue-size pilot */
     double tuned_per_sensor = 0.0;     /* its queue slots per sensor */
 };
@@ -1237,11 +1241,12 @@ static int run(gb_scene *G, const gb_opts *o, int follow, const double *org_dir,
     }
     int evused = 2;                                /* ev[0], ev[1]: the kernel region */
     int evkid[GB_TIMED_LAUNCHES];
+    bool capturing = false;                        /* launches go into a graph: not timed one by one */
     /* one launch, bracketed by events, counting into its kernel's block */
     auto launch = [&](int kid, gb_run &PR, auto fn) -> int {
         PR.stats = (unsigned long long *)G->stats.p + kid * GB_ST_N;
         int slot = (evused - 2) / 2;
-        bool timed = slot < GB_TIMED_LAUNCHES;
+        bool timed = !capturing && slot < GB_TIMED_LAUNCHES;
         if (timed)
             cudaEventRecord(G->ev[evused], st);
         if (fn(PR) < 0)
@@ -1283,6 +1288,8 @@ static int run(gb_scene *G, const gb_opts *o, int follow, const double *org_dir,
     P.stats = (unsigned long long *)G->stats.p;
     P.accum = o->c > 0 ? o->c : 1;
     P.nbins_total = nbins_total;
+    P.walk_refill = G->tuned_refill;
+    P.walk_blocks_per_sm = G->tuned_blocks;
 
     /* cast-only outputs */
     if (out.hit_id) {
@@ -1488,6 +1495,55 @@ static int run(gb_scene *G, const gb_opts *o, int follow, const double *org_dir,
         }
         return GB_OK;
     };
+    /* Batched runs capture the generations in a CUDA graph: the kernels
+     * read each queue's count on the device, so no generation waits for
+     * the host.  Paths are at most -lr bounces long, so -lr + 3 generations
+     * drain the queue; whatever is left (none, when -lr bounds the paths)
+     * is drained by the host loop below, which then finds the queue empty
+     * at once. */
+    if (G->use_graph && o->lr > 0 && ss == 0 && !grad && G->H.ninst == 0) {
+        cudaGraph_t graph = nullptr;
+        cudaGraphExec_t exec = nullptr;
+        CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+        capturing = true;
+        int rc = GB_OK;
+        for (int gen = 0; gen < o->lr + 3 && rc == GB_OK; gen++) {
+            P.qin = in ? qb : qa;
+            P.qin_count = cnt + in;
+            P.qout = in ? qa : qb;
+            P.qout_count = cnt + (1 - in);
+            P.adj_in = in ? adjb : adja;
+            P.adj_out = in ? adja : adjb;
+            P.tag_in = tags[in];
+            P.tag_out = tags[1 - in];
+            if (cudaMemsetAsync(cnt + (1 - in), 0, sizeof(unsigned long long), st) != cudaSuccess ||
+                cudaMemsetAsync(P.work, 0, sizeof(unsigned long long), st) != cudaSuccess)
+                rc = set_err(GB_ECUDA, "graph capture: %s", cudaGetErrorString(cudaGetLastError()));
+            if (rc == GB_OK)
+                rc = launch(GB_K_TRACE, P, [&](gb_run &R) { return gb_launch_trace(&R, st, G->sms); });
+            if (rc == GB_OK && cudaMemsetAsync(P.work, 0, sizeof(unsigned long long), st) != cudaSuccess)
+                rc = set_err(GB_ECUDA, "graph capture: %s", cudaGetErrorString(cudaGetLastError()));
+            if (rc == GB_OK)
+                rc = launch(GB_K_SHADE, P, [&](gb_run &R) { return gb_launch_shade(&R, st, G->sms); });
+            if (rc == GB_OK && cudaMemsetAsync(cnt + in, 0, sizeof(unsigned long long), st) != cudaSuccess)
+                rc = set_err(GB_ECUDA, "graph capture: %s", cudaGetErrorString(cudaGetLastError()));
+            in = 1 - in;
+        }
+        capturing = false;
+        cudaError_t e = cudaStreamEndCapture(st, &graph);
+        if (rc == GB_OK && e != cudaSuccess)
+            rc = set_err(GB_ECUDA, "graph capture: %s", cudaGetErrorString(e));
+        if (rc == GB_OK && cudaGraphInstantiate(&exec, graph, 0) != cudaSuccess)
+            rc = set_err(GB_ECUDA, "graph instantiation: %s", cudaGetErrorString(cudaGetLastError()));
+        if (rc == GB_OK && cudaGraphLaunch(exec, st) != cudaSuccess)
+            rc = set_err(GB_ECUDA, "graph launch: %s", cudaGetErrorString(cudaGetLastError()));
+        if (exec)
+            cudaGraphExecDestroy(exec);            /* freed once the launch completes */
+        if (graph)
+            cudaGraphDestroy(graph);
+        if (rc < 0)
+            return rc;
+    }
     int drc = drain();
     if (drc < 0)
         return drc;
@@ -1784,10 +1840,14 @@ extern "C" int gb_rcontrib(gb_scene *G, const gb_opts *o, const gb_modspec *mods
     return rcontrib_run(G, o, mods, nmods, org_dir, n, out, ray_count, 0.0);
 }
 
-/* Queue slots per sensor for a run over n sensors, from a pilot run of
- * 1,024 of them (evenly spaced): the largest generation per sensor, with a
- * margin; kept per scene and option set so that later calls skip the
- * pilot.  0 (run()'s estimate) for n <= 4,096. */
+/* The tuner of a scene's runs, from pilot runs over 1,024 of the run's
+ * sensors (evenly spaced): the queue slots per sensor (the largest
+ * generation per sensor, with a margin), then the walk kernel's shape --
+ * the idle lanes a warp waits for before refilling them, and the resident
+ * blocks per SM -- of five candidates, each timed twice on the pilot
+ * (the walk's device milliseconds, CUDA events), the fastest kept.  Kept
+ * per scene and option set so that later calls skip the pilots.  0 (run()'s
+ * estimate and the default shape) for n <= 4,096. */
 static double tune_slots(gb_scene *G, const gb_opts *o, const gb_modspec *mods, int nmods, const double *org_dir,
                          int64_t n, int nbt)
 {
@@ -1810,10 +1870,29 @@ static double tune_slots(gb_scene *G, const gb_opts *o, const gb_modspec *mods, 
     int64_t ns = (int64_t)(sample.size() / 6);
     std::vector<double> scratch((size_t)(ns / acc + 1) * nbt * 3);
     int64_t rays = 0;
+    G->tuned_refill = G->tuned_blocks = 0;
     if (rcontrib_run(G, o, mods, nmods, sample.data(), ns, scratch.data(), &rays, 0.0) != GB_OK || g_maxgen <= 0)
         return 0.0;
+    const double per = 1.5 * (double)g_maxgen / (double)ns;
+    static const int shapes[][2] = {{8, 0}, {4, 0}, {16, 0}, {8, 3}, {8, 2}};
+    double best = 1e30;
+    int br = 0, bb = 0;
+    for (int rep = 0; rep < 2; rep++)
+        for (const auto &sh : shapes) {
+            G->tuned_refill = sh[0];
+            G->tuned_blocks = sh[1];
+            if (rcontrib_run(G, o, mods, nmods, sample.data(), ns, scratch.data(), &rays, per) != GB_OK)
+                continue;
+            if (g_prof.ms[GB_K_TRACE] > 0 && g_prof.ms[GB_K_TRACE] < best) {
+                best = g_prof.ms[GB_K_TRACE];
+                br = sh[0];
+                bb = sh[1];
+            }
+        }
+    G->tuned_refill = br;
+    G->tuned_blocks = bb;
     G->tuned_key = key;
-    G->tuned_per_sensor = 1.5 * (double)g_maxgen / (double)ns;
+    G->tuned_per_sensor = per;
     return G->tuned_per_sensor;
 }
 
@@ -1849,6 +1928,9 @@ extern "C" int gb_rcontrib_batch(int njobs, gb_scene *const *scenes, const gb_op
         }
         groups[g].push_back(j);
     }
+    /* generation loops captured in CUDA graphs (GB_GRAPHS=0: host loop) */
+    const char *gv = getenv("GB_GRAPHS");
+    const bool graphs = !(gv && !strcmp(gv, "0"));
     std::vector<int> rcs(order.size(), GB_OK);
     std::vector<int64_t> rays(order.size(), 0);
     std::vector<std::string> errs(order.size());
@@ -1864,7 +1946,9 @@ extern "C" int gb_rcontrib_batch(int njobs, gb_scene *const *scenes, const gb_op
             at += n[j];
         }
         double per = tune_slots(G, o, mods, nmods, in.data(), tot, nbt);
+        G->use_graph = graphs;
         rcs[g] = rcontrib_run(G, o, mods, nmods, in.data(), tot, res.data(), &rays[g], per);
+        G->use_graph = false;
         errs[g] = g_error;
         if (rcs[g] != GB_OK)
             return;

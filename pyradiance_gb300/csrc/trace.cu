@@ -30,6 +30,8 @@
 #include <type_traits>
 #include <cooperative_groups.h>
 #include <cooperative_groups/scan.h>
+#include <algorithm>
+
 #include "trace.cuh"
 #include "tracehost.h"
 
@@ -1812,9 +1814,10 @@ __global__ void __launch_bounds__(TRACE_BLOCK, 4) k_trace(gb_run P)
     const Cube C{};
     unsigned long long cur = 0;
     bool active = false, exhausted = false;
+    const int refill = P.walk_refill > 0 ? P.walk_refill : 8;
     for (;;) {
         const unsigned idle = __ballot_sync(FULL, !active);
-        if (!exhausted && (__popc(idle) >= 8 || idle == FULL)) {
+        if (!exhausted && (__popc(idle) >= refill || idle == FULL)) {
             unsigned long long base = 0;
             const int leader = __ffs(idle) - 1;
             if (lane == leader)
@@ -2051,12 +2054,14 @@ int gb_launch_trace(const gb_run *P, cudaStream_t st, int sms)
     if (!grid)
         grid = resident_grid(k_trace<false>, TRACE_BLOCK, sms);
     if (P->S.ninst == 0) {
-        k_trace<false><<<grid, TRACE_BLOCK, 0, st>>>(*P);
+        const int g = P->walk_blocks_per_sm > 0 ? std::min(grid, P->walk_blocks_per_sm * sms) : grid;
+        k_trace<false><<<g, TRACE_BLOCK, 0, st>>>(*P);
         return cudaGetLastError() == cudaSuccess ? 0 : -1;
     }
     if (!grid_inst)
         grid_inst = resident_grid(k_trace<true>, TRACE_BLOCK, sms);
-    k_trace<true><<<grid_inst, TRACE_BLOCK, 0, st>>>(*P);
+    const int gi = P->walk_blocks_per_sm > 0 ? std::min(grid_inst, P->walk_blocks_per_sm * sms) : grid_inst;
+    k_trace<true><<<gi, TRACE_BLOCK, 0, st>>>(*P);
     if (cudaGetLastError() != cudaSuccess)
         return -1;
     {

@@ -112,6 +112,11 @@ typedef struct {
     gb_qadj *adj_out;
     long long qcap;
     unsigned long long *work;  /* work-item counter of the persistent kernels (zeroed per launch) */
+    /* walk kernel shape, picked per scene by the host's tuner (0: defaults):
+     * idle lanes a warp waits for before it refills them from the queue,
+     * and resident blocks per SM */
+    int   walk_refill;
+    int   walk_blocks_per_sm;
     /* ambient super-sampling of the -I first hemispheres (rtrace -as):
      * paths carry the index (sensor * root_n^2 + stratum) of the stratum
      * they descend from in queue-parallel tag arrays, their values add to

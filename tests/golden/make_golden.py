@@ -491,6 +491,65 @@ def c2_headline(tmp: Path, nsens: int = 256, K: int = 64) -> None:
     print("c2_headline: mean total %.4g, lit sensors %d" % (a.sum(2).mean(), (a.sum((1, 2)) > 0).sum()))
 
 
+def grad_fd(tmp: Path, nx: int = 32) -> None:
+    """Differenced reference runs for the gradients: the window room with
+    its 20,000 triangles in 64 plastic materials and the glass window,
+    rtrace -u- -I -ab 2 -ad 1024 -aa 0 -as 0 -lw 1e-6 at a 32 x 32 grid of
+    sensors, with one parameter at a time moved by -delta and +delta: the
+    gray reflectance of three materials (irradiance is quadratic in each at
+    two bounces, so the central difference is exact for the reference's
+    fixed-seed estimate), and the window's transmissivity.  With -lw 1e-6
+    no ray's fate depends on the weights, so the two runs of a pair draw
+    the same random numbers (common random numbers).  The sensors run in
+    eight fixed shards (the same in every run), one process each."""
+    import re
+    base = w.window_room(seed=0, ntri=20000, nmat=64)
+    rays = w.sensor_grid(nx, nx)
+    args = ["rtrace", "-h", "-u-", "-I", "-ab", "2", "-ad", "1024", "-aa", "0", "-as", "0", "-lw", "1e-6",
+            "-fdd", "-ov"]
+    params = [("tri_mat3", 0.05), ("tri_mat17", 0.05), ("tri_mat40", 0.05), ("window_glass", 0.02)]
+
+    def with_value(name, dv):
+        def mat(m):
+            vals = [float(v) for v in m.group(2).split()]
+            if name == "window_glass":
+                vals = [v + dv for v in vals]
+            else:
+                vals = [v + dv for v in vals[:3]] + vals[3:]
+            return m.group(1) + " ".join("%.9g" % v for v in vals) + "\n"
+        pat = r"(void (?:plastic|glass) " + re.escape(name) + r"\n0\n0\n\d+ )([^\n]*)\n"
+        out, k = re.subn(pat, mat, base)
+        assert k == 1, name
+        return out
+
+    def irradiance(text, tag):
+        octp = oconv(text, tmp, f"g_{tag}")
+        parts = np.array_split(rays, 8)
+        env = dict(os.environ, RAYPATH=f".:{REF / 'lib'}")
+        procs = []
+        for i, part in enumerate(parts):
+            fi = tmp / f"g_{tag}_{i}.in"
+            fi.write_bytes(part.astype("<f8").tobytes())
+            procs.append(subprocess.Popen([str(BIN / args[0]), *args[1:], str(octp)], stdin=open(fi, "rb"),
+                                          stdout=open(tmp / f"g_{tag}_{i}.out", "wb"), env=env))
+        for p in procs:
+            assert p.wait() == 0
+        return np.concatenate([np.frombuffer((tmp / f"g_{tag}_{i}.out").read_bytes(), dtype="<f8")
+                               for i in range(8)]).reshape(-1, 3)
+
+    e0 = irradiance(base, "base")
+    fd = []
+    for name, d in params:
+        ep = irradiance(with_value(name, +d), name + "p")
+        em = irradiance(with_value(name, -d), name + "m")
+        fd.append((ep - em) / (2 * d))
+    fd = np.stack(fd, 0)                                   # params x sensors x 3
+    np.savez_compressed(OUT / "grad_fd.npz", rays=rays, e0=e0, fd=fd,
+                        names=np.array([p[0] for p in params]), deltas=np.array([p[1] for p in params]),
+                        cmd=" ".join(args[1:]) + " (central differences of the parameters, 8 fixed shards)")
+    print("grad_fd: mean irradiance %.4g; mean derivatives %s" % (e0[:, 0].mean(), fd[:, :, 0].mean(1)))
+
+
 def dct_four() -> None:
     """dctimestep's four-matrix form (util/dctimestep.c:243-264): view
     (sensors x 145 Klems), transmission (145 x 145), daylight (145 x 146) and
@@ -594,7 +653,7 @@ def main() -> None:
              "spot": spotlights, "mirror": mirrors, "flux": flux_matrices, "flux_sc": flux_shirchiu,
              "dct": lambda tmp: dct_small(), "dct4": lambda tmp: dct_four(), "rmtxop": lambda tmp: rmtxop_cases(), "trace_oct": lambda tmp: ref_fixture_trace(),
              "c2ab1": lambda tmp: c2_stats(tmp, ab=1, K=256), "c2ab3": lambda tmp: c2_stats(tmp, ab=3, K=256),
-             "c2head": c2_headline}
+             "c2head": c2_headline, "gradfd": grad_fd}
     only = sys.argv[1:] or list(parts)         # e.g. make_golden.py c1p
     with tempfile.TemporaryDirectory() as td:
         tmp = Path(td)

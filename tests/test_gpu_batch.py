@@ -68,3 +68,22 @@ def test_jobs_sharing_a_scene(setup):
     # the two jobs is the separate call over all 1,500 sensors
     np.testing.assert_allclose(got, ref, rtol=1e-6, atol=1e-12)
     assert rc.last_rays > 0
+
+
+def test_tuned_graph_batch_equals_host_loop(setup, monkeypatch):
+    """A job of more than 4,096 sensors runs the scene's tuner (queue size
+    and walk shape from pilot runs) and its generation loop as a CUDA
+    graph; the same batch with the host-driven loop (GB_GRAPHS=0) and the
+    separate call give the same bins up to rounding."""
+    gb, scenes = setup
+    rc = rc_for(gb)
+    big = grid(6000, 5)
+    jobs = [(scenes[1], big), (scenes[0], grid(300, 6))]
+    graph = rc.run_batch(jobs)
+    monkeypatch.setenv("GB_GRAPHS", "0")
+    host = rc.run_batch(jobs)
+    for a, b in zip(graph, host):
+        np.testing.assert_allclose(a, b, rtol=1e-6, atol=1e-12)
+    monkeypatch.delenv("GB_GRAPHS")
+    rc.octree = scenes[1]
+    np.testing.assert_allclose(graph[0], rc.run_array(big), rtol=1e-6, atol=1e-12)
