@@ -11,6 +11,7 @@ programs.  Errors raise ``RuntimeError`` as the reference's
 from __future__ import annotations
 
 import os
+import re
 import time
 from pathlib import Path
 from typing import Sequence
@@ -107,9 +108,22 @@ def _header(prog: str, args: list[str], octree, fmt: str, ncomp: int | None, ext
     return (text + "\n\n").encode()
 
 
+def _ascii_rows(vals: np.ndarray, sep: str = "\t", end: str = "\t\n") -> list[str]:
+    """Each row of a 2-D array as text: numbers in %e (six digits, as the
+    reference's puta in rt/rtrace.c and rt/rc2.c) joined by sep, the row
+    ended by end."""
+    vals = np.asarray(vals, dtype=np.float64)
+    if vals.ndim == 1:
+        vals = vals[:, None]
+    if vals.shape[1] == 0:
+        return [end] * len(vals)
+    row = sep.join(["%e"] * vals.shape[1]) + end
+    return [row % tuple(r) for r in vals.tolist()]
+
+
 def _fmt_values(vals: np.ndarray, fmt: str) -> bytes:
     if fmt == "a":
-        return "".join("".join(f"{x:e}\t" for x in row) + "\n" for row in vals).encode()
+        return "".join(_ascii_rows(vals)).encode()
     if fmt == "f":
         return np.ascontiguousarray(vals, dtype=np.float32).tobytes()
     if fmt == "d":
@@ -190,48 +204,57 @@ def _rtrace(rays: bytes, octree, header: bool = True, inform: str = "a", outform
     hit[good] = gh
     hitt[good] = gt
     out = []
-    ncomp = 0
+    ncomp = 0                                    # rt/rtrace.c:244-370 setrtoutput
     for ch in spec:
-        ncomp += {"v": 3, "o": 3, "d": 3, "p": 3, "N": 3, "n": 3, "L": 1, "l": 1, "w": 1}.get(ch, 0)
+        ncomp += {"v": 3, "o": 3, "d": 3, "p": 3, "N": 3, "n": 3, "L": 1, "l": 1, "w": 1, "s": 1, "m": 1,
+                  "M": 1}.get(ch, 0)
     if opts.h:
         out.append(_header("rtrace", args, octree, fout, ncomp or None))
     unit = np.where(good[:, None], r[:, 3:6] / np.where(dirlen > 0, dirlen, 1)[:, None], 0.0) if n else r[:, 3:6]
-    for i in range(n):
-        cols = []
-        text = []
-        for ch in spec:
-            if ch == "v":
-                cols.append(vals[i])
-            elif ch == "o":
-                cols.append(r[i, 0:3])
-            elif ch == "d":
-                cols.append(unit[i])
-            elif ch == "L":
-                cols.append(np.array([hitt[i] if hit[i] >= 0 else 1e10]))
-            elif ch == "p":
-                cols.append(r[i, 0:3] + unit[i] * (hitt[i] if hit[i] >= 0 else 0.0) if hit[i] >= 0 else np.zeros(3))
-            elif ch in "smM":
-                if cols:
-                    text.append(_fmt_values(np.concatenate(cols)[None, :], "a").decode().rstrip("\n")
-                                if fout == "a" else None)
-                    cols = []
-                name = "*"
-                if hit[i] >= 0:
-                    name = {"s": sc.object_name, "m": sc.modifier_name, "M": sc.material_name}[ch](int(hit[i]))
-                text.append(name + "\t")
-            elif ch == "w":
-                cols.append(np.array([1.0]))
-            else:
-                raise GbError(-3, f"output option -o{ch} is not supported")
-        if fout == "a":
-            if cols:
-                text.append("".join(f"{x:e}\t" for x in np.concatenate(cols)))
-            out.append(("".join(t for t in text if t is not None) + "\n").encode())
+    hitm = hit >= 0
+    # the output columns in spec order: numeric blocks (n x k) or names (n)
+    items = []
+    for ch in spec:
+        if ch == "v":
+            items.append(vals)
+        elif ch == "o":
+            items.append(r[:, 0:3])
+        elif ch == "d":
+            items.append(unit)
+        elif ch == "L":
+            items.append(np.where(hitm, hitt, 1e10)[:, None])
+        elif ch == "p":
+            items.append(np.where(hitm[:, None], r[:, 0:3] + unit * np.where(hitm, hitt, 0.0)[:, None], 0.0))
+        elif ch in "smM":
+            get = {"s": sc.object_name, "m": sc.modifier_name, "M": sc.material_name}[ch]
+            cache: dict[int, str] = {}
+            names = []
+            for h in hit.tolist():
+                if h < 0:
+                    names.append("*")
+                else:
+                    if h not in cache:
+                        cache[h] = get(h)
+                    names.append(cache[h])
+            items.append(names)
+        elif ch == "w":
+            items.append(np.ones((n, 1)))
         else:
-            if any(ch in "smM" for ch in spec):
-                raise GbError(-1, "names need ascii output")
-            if cols:
-                out.append(_fmt_values(np.concatenate(cols)[None, :], fout))
+            raise GbError(-3, f"output option -o{ch} is not supported")
+    if fout == "a":
+        # every value and name followed by a tab, a newline after each ray
+        # (rt/rtrace.c:471-500 printvals, puta, oputs)
+        cols = [_ascii_rows(it, end="\t") if isinstance(it, np.ndarray) else [nm + "\t" for nm in it]
+                for it in items]
+        if n:
+            rows = ["".join(parts) + "\n" for parts in zip(*cols)] if cols else ["\n"] * n
+            out.append("".join(rows).encode())
+    else:
+        if any(not isinstance(it, np.ndarray) for it in items):
+            raise GbError(-1, "names need ascii output")
+        if items and n:
+            out.append(_fmt_values(np.concatenate([np.asarray(it, dtype=np.float64) for it in items], axis=1),
+                                   fout))
     return b"".join(out)
 
 
@@ -257,6 +280,10 @@ class Rcontrib:
         if report:
             self.args.extend(["-t", str(report)])
         self.mods: list[dict] = []
+        self.mod_args: list[str] = []
+        self._ospec: str | None = None
+        self._xres: int | None = None
+        self._yres: int | None = None
         self.seed = None
         self.replica = 0
         self.last_rays = 0
@@ -265,23 +292,39 @@ class Rcontrib:
                      calfile: str | None = None, expression: str | None = None, nbins: str | None = None,
                      binv: str | None = None, param: str | None = None, xres: int | None = None,
                      yres: int | None = None, output: str | None = None):
-        if modifier is None and modifier_path is None:
+        # the arguments pyradiance passes for this modifier, in its order
+        # (src/pyradiance/rt.py:190-228); -o, -x and -y stay in force for
+        # the modifiers after it, as rcontrib reads them
+        arglist: list[str] = []
+        for flag, v in (("-f", calfile), ("-e", expression), ("-bn", nbins), ("-b", binv), ("-p", param),
+                        ("-x", xres), ("-y", yres), ("-o", output)):
+            if v is not None:
+                arglist += [flag, str(v)]
+        if modifier is not None:
+            arglist += ["-m", modifier]
+        elif modifier_path is not None:
+            arglist += ["-M", str(modifier_path)]
+        else:
             raise ValueError("Modifier or modifier path must be provided.")
+        self.mod_args.extend(arglist)
+        if output is not None:
+            self._ospec = str(output)
+        if xres is not None:
+            self._xres = int(xres)
+        if yres is not None:
+            self._yres = int(yres)
         names = [modifier] if modifier is not None else [
             w for w in Path(modifier_path).read_text().split() if w]
-        if output is not None:
-            raise RuntimeError("An error occurred with exit code 3: per-modifier output files (-o) "
-                               "are not supported; results are returned as bytes")
         for nm in names:
             self.mods.append(dict(modifier=nm, calfile=calfile, expr=expression, nbins=nbins, binv=binv,
-                                  params=param))
+                                  params=param, output=self._ospec))
         return self
 
     def _specs(self):
         keep = []
         arr = (GbModspec * len(self.mods))()
         for i, m in enumerate(self.mods):
-            vals = {k: (str(v).encode() if v is not None else None) for k, v in m.items()}
+            vals = {k: (str(v).encode() if v is not None else None) for k, v in m.items() if k != "output"}
             keep.append(vals)
             arr[i] = GbModspec(vals["modifier"], vals["binv"], vals["nbins"], vals["params"], vals["calfile"],
                                vals["expr"])
@@ -292,6 +335,10 @@ class Rcontrib:
         opts, used = parse_opts(self.args, _lib.GB_PROG_RCONTRIB)
         if used != len(self.args):
             raise GbError(-1, f"command line error at '{self.args[used]}'")
+        if self._xres is not None:
+            opts.x = self._xres
+        if self._yres is not None:
+            opts.y = self._yres
         if self.seed is not None:
             opts.seed = int(self.seed)
         opts.replica = int(self.replica)
@@ -348,24 +395,57 @@ class Rcontrib:
         return outs
 
     def _call(self) -> bytes:
+        """rcontrib's output streams (rt/rc2.c:131-250 getostream): the
+        modifiers without an output specification go to the returned bytes,
+        the others to files named by their specification (%s: the
+        modifier), each stream with its own header; an existing file is an
+        error, as rcontrib does not overwrite without -fo."""
+        from .rflux import _nbins_each
+        streams: list[tuple[str | None, list[int]]] = []
+        for i, m in enumerate(self.mods):
+            spec = m.get("output")
+            if spec is not None and re.search(r"%[0-9]*d", spec):
+                raise GbError(-3, f"per-bin output files ({spec}) are not supported")
+            name = None if spec is None else (spec.replace("%s", m["modifier"]) if "%s" in spec else spec)
+            for nm, idx in streams:
+                if nm == name:
+                    idx.append(i)
+                    break
+            else:
+                streams.append((name, [i]))
+        for name, _ in streams:
+            if name is not None and Path(name).exists():
+                raise GbError(-2, f"cannot open '{name}' for writing")
         arr = self.run_array()
         opts = self._opts
         fout = opts.fout.decode()
-        parts = []
-        if opts.h:
-            extra = []                                      # rt/rc2.c:158-166
-            if opts.y > 0:
-                extra.append(f"NROWS={opts.y * max(opts.x, 1)}")
-            if opts.x <= 0 or arr.shape[1] > 1:
-                extra.append(f"NCOLS={arr.shape[1]}")
-            parts.append(_header("rcontrib", self.args + [a for m in self.mods for a in ("-m", m["modifier"])],
-                                 self.octree, fout, 3, extra))
-        if fout == "a":
-            flat = arr.reshape(arr.shape[0], -1)
-            parts.append("".join("".join(f"{x:.6e}\t" for x in row) + "\n" for row in flat).encode())
-        else:
-            parts.append(_fmt_values(arr.reshape(-1, 3), fout))
-        return b"".join(parts)
+        nb = _nbins_each(self.mods)
+        start = np.concatenate([[0], np.cumsum(nb)]).astype(int)
+        result = b""
+        for name, idx in streams:
+            cols = np.concatenate([arr[:, start[i]:start[i + 1]] for i in idx], axis=1)
+            parts = []
+            if opts.h:
+                extra = []
+                spec = self.mods[idx[0]].get("output")
+                if name is not None and ((spec is not None and "%s" in spec) or cols.shape[1] == 1):
+                    extra.append(f"MODIFIER={self.mods[idx[0]]['modifier']}")
+                if opts.y > 0:
+                    extra.append(f"NROWS={opts.y * max(opts.x, 1)}")
+                if opts.x <= 0 or cols.shape[1] > 1:
+                    extra.append(f"NCOLS={cols.shape[1]}")
+                parts.append(_header("rcontrib", self.args + self.mod_args, self.octree, fout, 3, extra))
+            if fout == "a":
+                parts.append("".join(_ascii_rows(cols.reshape(cols.shape[0], -1), end="\t\n")).encode())
+            else:
+                parts.append(_fmt_values(cols.reshape(-1, 3), fout))
+            data = b"".join(parts)
+            if name is None:
+                result = data
+            else:
+                Path(name).parent.mkdir(parents=True, exist_ok=True)
+                Path(name).write_bytes(data)
+        return result
 
     def __call__(self) -> bytes:
         return _wrap(self._call)()
@@ -473,15 +553,32 @@ def _dctimestep(*mtx, nstep: int | None = None, header: bool = True, xres: int |
         R = dctimestep_array(dc, sky)
     fout = outform or "a"
     parts = []
-    if header:
-        lines = ["#?RADIANCE", "dctimestep", "SOFTWARE= " + lib().gb_version().decode(),
+    if header:                                   # util/dctimestep.c: the command, the time, the shape
+        cmd = ["dctimestep"]
+        if nstep:
+            cmd += ["-n", str(nstep)]
+        for flag, v in (("-x", xres), ("-y", yres)):
+            if v:
+                cmd += [flag, str(v)]
+        if inform:
+            cmd.append(f"-i{inform}")
+        if outform:
+            cmd.append(f"-o{outform}")
+        cmd += [str(m) for m in mtx if not isinstance(m, bytes)]
+        now = time.time()
+        lines = ["#?RADIANCE", " ".join(cmd), time.strftime("CAPDATE= %Y:%m:%d %H:%M:%S", time.localtime(now)),
+                 time.strftime("GMT= %Y:%m:%d %H:%M:%S", time.gmtime(now)),
                  f"NROWS={R.shape[0]}", f"NCOLS={R.shape[1]}", "NCOMP=3"]
         if fout in ("f", "d"):
             lines.append("BigEndian=0")
         lines.append("FORMAT=" + {"a": "ascii", "f": "float", "d": "double"}[fout])
         parts.append(("\n".join(lines) + "\n\n").encode())
-    if fout == "a":
-        parts.append("".join("\t".join(f"{v:.6e}" for v in row.ravel()) + "\n" for row in R).encode())
+    if fout == "a":                              # a colour's three values by spaces, colours by tabs
+        if R.shape[1]:
+            row = "\t".join([" ".join(["%e"] * 3)] * R.shape[1]) + "\n"
+            parts.append("".join(row % tuple(r) for r in R.reshape(R.shape[0], -1).tolist()).encode())
+        else:
+            parts.append(b"\n" * R.shape[0])
     else:
         parts.append(_fmt_values(R.reshape(-1, 3), fout))
     return b"".join(parts)
