@@ -216,7 +216,8 @@ int  gb_dctimestep_device(const float *d_dc, const float *d_sky, int64_t M, int6
 int  gb_last_stats(int64_t *rays, int64_t *steps, int64_t *contribs, int64_t *launches);
 /* Per-kernel profile of the last rtrace/rcontrib call on this thread:
  * kernel 0 cast, 1 sensor roots, 2 first-hemisphere rays, 3 primaries,
- * 4 octree walks, 5 shading (one launch of 4 and 5 per generation); device
+ * 4 octree walks, 5 shading (one launch of 4 and 5 per generation), 6 the
+ * walk order of a generation's queue (when rays are reordered); device
  * milliseconds (CUDA events on the library's stream), launches, counters
  * (rays, cube steps, contributions, queue overflows, bad bins, node
  * descents, object tests, spare) and the milliseconds of the whole kernel

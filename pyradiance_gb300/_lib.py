@@ -118,7 +118,7 @@ def last_stats() -> dict:
     return {"rays": v[0].value, "steps": v[1].value, "contribs": v[2].value, "launches": v[3].value}
 
 
-KERNELS = ["cast", "root", "expand", "primary", "trace", "shade"]
+KERNELS = ["cast", "root", "expand", "primary", "trace", "shade", "order"]
 COUNTERS = ["rays", "steps", "contribs", "overflow", "badbin", "nodes", "tests", "spare"]
 
 

@@ -108,7 +108,7 @@ struct gb_scene {
     gb_dscene ds;
     /* work buffers */
     DevBuf sensors, value, bins, stats, roots, rootspt, qa, qb, qcount, binprog, modinfo, hits, hitt, trkrun,
-        hitrec, adja, adjb, dlde, gradd, rootdraw, rootlot, tga, tgb, ssval, sscnt, sserr, slow;
+        hitrec, adja, adjb, dlde, gradd, rootdraw, rootlot, tga, tgb, ssval, sscnt, sserr, slow, worder, whist;
     cudaStream_t stream = nullptr;
     int sms = 0;
     cudaEvent_t ev[2 * GB_TIMED_LAUNCHES + 2];
@@ -902,7 +902,7 @@ extern "C" void gb_scene_free(gb_scene *G)
                       &G->srcd, &G->trk, &G->sensors, &G->value, &G->bins, &G->stats, &G->roots, &G->rootspt, &G->qa,
                       &G->qb, &G->qcount, &G->binprog, &G->modinfo, &G->hits, &G->hitt, &G->trkrun, &G->hitrec,
                       &G->adja, &G->adjb, &G->dlde, &G->gradd, &G->rootdraw, &G->rootlot, &G->tga, &G->tgb,
-                      &G->ssval, &G->sscnt, &G->sserr, &G->slow};
+                      &G->ssval, &G->sscnt, &G->sserr, &G->slow, &G->worder, &G->whist};
     for (DevBuf *b : bufs)
         b->release();
     if (G->stream)
@@ -1408,6 +1408,24 @@ static int run(gb_scene *G, const gb_opts *o, int follow, const double *org_dir,
         P.ss_cnt = (int *)G->sscnt.p;
         P.ss_err = (float *)G->sserr.p;
     }
+    /* rays reordered for the walk of each generation (GB_WALK_ORDER=1) */
+    const char *wo = getenv("GB_WALK_ORDER");
+    const bool reorder = wo && wo[0] == '1';
+    if (reorder && (G->worder.ensure((size_t)qcap * sizeof(uint32_t)) < 0 ||
+                    G->whist.ensure(2 * GB_SORT_BUCKETS * sizeof(uint32_t)) < 0))
+        return set_err(GB_ENOMEM, "cannot allocate the walk order");
+    auto walk = [&](gb_run &R) -> int {
+        if (reorder) {
+            int rc = launch(GB_K_ORDER, R, [&](gb_run &Q) {
+                return gb_launch_walk_order(&Q, (uint32_t *)G->worder.p, (uint32_t *)G->whist.p, st, G->sms); });
+            if (rc < 0)
+                return rc;
+            R.walk_order = (const uint32_t *)G->worder.p;
+        }
+        int rc = launch(GB_K_TRACE, R, [&](gb_run &Q) { return gb_launch_trace(&Q, st, G->sms); });
+        R.walk_order = nullptr;
+        return rc;
+    };
     gb_qadj *adja = (gb_qadj *)G->adja.p, *adjb = (gb_qadj *)G->adjb.p;
     unsigned long long *cnt = (unsigned long long *)G->qcount.p;   /* [0] A, [1] B, [2] work items */
     CK(cudaMemsetAsync(cnt, 0, 3 * sizeof(unsigned long long), st));
@@ -1482,7 +1500,7 @@ static int run(gb_scene *G, const gb_opts *o, int follow, const double *org_dir,
             CK(cudaMemsetAsync(P.work, 0, sizeof(unsigned long long), st));
             if (P.slow_count)
                 CK(cudaMemsetAsync(P.slow_count, 0, sizeof(unsigned long long), st));
-            int rc = launch(GB_K_TRACE, P, [&](gb_run &R) { return gb_launch_trace(&R, st, G->sms); });
+            int rc = walk(P);
             if (rc < 0)
                 return rc;
             CK(cudaMemsetAsync(P.work, 0, sizeof(unsigned long long), st));
@@ -1520,7 +1538,7 @@ static int run(gb_scene *G, const gb_opts *o, int follow, const double *org_dir,
                 cudaMemsetAsync(P.work, 0, sizeof(unsigned long long), st) != cudaSuccess)
                 rc = set_err(GB_ECUDA, "graph capture: %s", cudaGetErrorString(cudaGetLastError()));
             if (rc == GB_OK)
-                rc = launch(GB_K_TRACE, P, [&](gb_run &R) { return gb_launch_trace(&R, st, G->sms); });
+                rc = walk(P);
             if (rc == GB_OK && cudaMemsetAsync(P.work, 0, sizeof(unsigned long long), st) != cudaSuccess)
                 rc = set_err(GB_ECUDA, "graph capture: %s", cudaGetErrorString(cudaGetLastError()));
             if (rc == GB_OK)

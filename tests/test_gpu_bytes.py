@@ -53,7 +53,7 @@ def norm_header(lines):
     for ln in lines:
         if ln.startswith(VARIABLE):
             continue
-        toks = [t.rsplit("/", 1)[1] if t.endswith(".mtx") else t for t in ln.split(" ")]
+        toks = [t.rsplit("/", 1)[-1] if t.endswith(".mtx") else t for t in ln.split(" ")]
         out.append(" ".join(toks).rstrip())
     return out
 
