@@ -112,32 +112,20 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def l2_gather_ceiling(dev):
-    """The rate at which an SM array reads random 64-byte records from a
-    table resident in L2 -- the kind of access the octree walk makes (node
-    codes, set members, 64-byte object records), without its dependence of
-    one load on the last: torch.embedding_bag summing bags of 32 random rows
-    of 16 floats from a 32 MB table (L2 is 126 MB), so that only the gathers
-    and not the output move much data.  GB/s of rows read, best of 5 after
-    warm-up, CUDA events."""
-    import torch
-    rows = (32 << 20) // 64
-    table = torch.randn(rows, 16, device=dev)
-    nidx = 1 << 24
-    idx = torch.randint(0, rows, (nidx,), device=dev)
-    offs = torch.arange(0, nidx, 32, device=dev)
-    st = torch.cuda.current_stream(dev)
-    best = None
-    for rep in range(8):
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(st)
-        torch.nn.functional.embedding_bag(idx, table, offs, mode="sum")
-        e1.record(st)
-        torch.cuda.synchronize(dev)
-        if rep >= 3:
-            ms = e0.elapsed_time(e1)
-            best = ms if best is None else min(best, ms)
-    return nidx * 64 / (best / 1e3) / 1e9
+def l2_ceilings():
+    """The walk's ceilings, measured on this GPU (gb_probe_l2): random
+    64-byte record reads from a 32 MB table (L2-resident), independent
+    (gather) and each from the place the last record names (chase, the
+    dependent chain the walk's descent and object records form), with the
+    walk kernel's launch shape.  GB/s."""
+    import ctypes as C
+    from pyradiance_gb300 import _lib
+    out = {}
+    for name, chase in (("gather", 0), ("chase", 1)):
+        v = C.c_double(0)
+        _lib.check(_lib.lib().gb_probe_l2(32 << 20, chase, C.byref(v)))
+        out[name] = v.value
+    return out
 
 
 def make_scene(tmp: Path):
@@ -623,7 +611,7 @@ def gpu_arm(args):
         ms_per_launch = d["ms"] / d["launches"]
         achieved = bytes_per_launch / (ms_per_launch / 1e3) / 1e9
         peak, peak_kind = peaks()
-        l2c = l2_gather_ceiling(dev)
+        l2c = l2_ceilings()
         traffic = traffic_from_profiles(dom)
         cpu_v, cores, sample = cpu_baseline(rad, rays, seconds=12.0) if not args.no_cpu else (None, 0, "skipped")
         value = rays_all / dev_s / 1e6
@@ -643,12 +631,15 @@ def gpu_arm(args):
             "roofline": {"bound": "hbm", "kernel": "k_" + dom, "achieved": round(achieved, 1), "peak": peak,
                          "unit": "GB/s", "frac": round(achieved / peak, 4),
                          "traffic": traffic, "peak_source": peak_kind,
-                         "l2_gather_ceiling": round(l2c, 1), "frac_of_l2_gather": round(achieved / l2c, 4),
+                         "l2_gather_ceiling": round(l2c["gather"], 1),
+                         "frac_of_l2_gather": round(achieved / l2c["gather"], 4),
+                         "l2_chase_ceiling": round(l2c["chase"], 1),
+                         "frac_of_l2_chase": round(achieved / l2c["chase"], 4),
                          "note": "algorithmic bytes = node descents*4 + cube visits*8 + object tests*60 (+ rays*80 for "
-                                 "the walk kernel's ray record and result); the scene lives in L1/L2, so the binding "
-                                 "ceiling is the measured rate of random 64-byte reads from L2 (l2_gather_ceiling, "
-                                 "independent loads; the walk's loads depend on each other); DRAM traffic is a few "
-                                 "percent of the algorithmic bytes"},
+                                 "the walk kernel's ray record and result); the scene lives in L1/L2 (DRAM traffic is "
+                                 "a few percent of the algorithmic bytes), so the binding ceilings are the measured "
+                                 "rates of random 64-byte reads from L2: independent (gather) and dependent (chase), "
+                                 "gb_probe_l2 with the walk's launch shape"},
             "cpu_baseline": {"value": None if cpu_v is None else round(cpu_v, 4), "unit": "Mrays/s",
                              "cores": cores, "kind": "port", "sample": sample},
             "clocks": ck,

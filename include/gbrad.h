@@ -216,8 +216,7 @@ int  gb_dctimestep_device(const float *d_dc, const float *d_sky, int64_t M, int6
 int  gb_last_stats(int64_t *rays, int64_t *steps, int64_t *contribs, int64_t *launches);
 /* Per-kernel profile of the last rtrace/rcontrib call on this thread:
  * kernel 0 cast, 1 sensor roots, 2 first-hemisphere rays, 3 primaries,
- * 4 octree walks, 5 shading (one launch of 4 and 5 per generation), 6 the
- * walk order of a generation's queue (when rays are reordered); device
+ * 4 octree walks, 5 shading (one launch of 4 and 5 per generation); device
  * milliseconds (CUDA events on the library's stream), launches, counters
  * (rays, cube steps, contributions, queue overflows, bad bins, node
  * descents, object tests, spare) and the milliseconds of the whole kernel
@@ -225,6 +224,15 @@ int  gb_last_stats(int64_t *rays, int64_t *steps, int64_t *contribs, int64_t *la
  * rays only). */
 int  gb_last_profile(int kernel, double *ms, int64_t *launches, int64_t *counters, int ncounters,
                      double *region_ms);
+
+/* Measurement aid: the rate (GB/s into *gbps) at which this GPU reads
+ * random 64-byte records from a table of table_bytes (L2-resident when it
+ * is below the L2 size), with the walk kernel's launch shape: independent
+ * reads (chase = 0), or each read's place taken from the last record read
+ * (chase = 1: a chain of dependent loads, as in the octree walk).  The
+ * ceilings the walk's algorithmic bytes are held against.  No counterpart
+ * in the reference. */
+int  gb_probe_l2(int64_t table_bytes, int chase, double *gbps);
 
 const char *gb_last_error(void);
 const char *gb_version(void);

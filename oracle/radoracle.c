@@ -100,6 +100,23 @@ static double vnormalize(double v[3])
     return l;
 }
 
+/* common/fvect.c:132-155 normalize: the first-order form near unit length,
+ * as rtrace normalises the directions it reads (rt/rtrace.c) */
+static double normalize_ref(double v[3])
+{
+    double len, d = vdot(v, v);
+    if (d == 0.0) return 0.0;
+    if ((d <= 1.0 + FTINY) & (d >= 1.0 - FTINY)) {
+        len = 0.5 + 0.5 * d;
+        d = 2.0 - len;
+    } else {
+        len = sqrt(d);
+        d = 1.0 / len;
+    }
+    v[0] *= d; v[1] *= d; v[2] *= d;
+    return len;
+}
+
 static void perp0(double vp[3], const double v[3])
 {
     double v1[3] = {0, 0, 0};
@@ -2011,7 +2028,7 @@ int orc_rtrace(void *sp, const gb_opts *o, const double *rays, int64_t n, double
                 memset(&c, 0, sizeof c);
                 memcpy(c.rorg, rv, 3 * sizeof(double));
                 memcpy(c.rdir, rv + 3, 3 * sizeof(double));
-                vnormalize(c.rdir);
+                normalize_ref(c.rdir);
                 rayclear(&c);
                 c.rsrc = -1;
                 if (!localhit(&X, &c))

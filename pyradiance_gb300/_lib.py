@@ -56,6 +56,7 @@ _SIGS = {
     "gb_scene_load": (C.c_int, [C.c_char_p, C.POINTER(C.c_void_p)]),
     "gb_scene_load_rad": (C.c_int, [C.POINTER(C.c_char_p), C.c_int, C.c_int, C.c_int, C.POINTER(C.c_void_p)]),
     "gb_scene_free": (None, [C.c_void_p]),
+    "gb_probe_l2": (C.c_int, [C.c_int64, C.c_int, C.POINTER(C.c_double)]),
     "gb_scene_octree_info": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64),
                                        C.POINTER(C.c_uint64), C.POINTER(C.c_int)]),
     "gb_scene_nobjects": (C.c_int64, [C.c_void_p]),
@@ -118,7 +119,7 @@ def last_stats() -> dict:
     return {"rays": v[0].value, "steps": v[1].value, "contribs": v[2].value, "launches": v[3].value}
 
 
-KERNELS = ["cast", "root", "expand", "primary", "trace", "shade", "order"]
+KERNELS = ["cast", "root", "expand", "primary", "trace", "shade"]
 COUNTERS = ["rays", "steps", "contribs", "overflow", "badbin", "nodes", "tests", "spare"]
 
 

@@ -1,6 +1,8 @@
 """Builds libgbrad.so (the CUDA library behind the C ABI in include/gbrad.h).
 
-Plain nvcc/gcc invocations, compiled in parallel, for sm_103a only:
+Plain nvcc/gcc invocations, compiled in parallel, for sm_103a only.  Host
+code is compiled with -ffp-contract=off, so that it rounds alike on x86 and
+on aarch64 (where GCC contracts multiply-adds by default):
 
     python -m pyradiance_gb300.build          # or build() from Python
 
@@ -21,10 +23,11 @@ OBJ = HERE / "_build"
 LIB = HERE / "libgbrad.so"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CU_SOURCES = ["trace.cu", "host.cu", "dct.cu", "dct_tc.cu", "octbuild_gpu.cu"]
+CU_SOURCES = ["trace.cu", "host.cu", "dct.cu", "dct_tc.cu", "octbuild_gpu.cu", "cast64.cu"]
 # per-file flags: the device octree builder's FP64 tests must round as the
-# host builder's (no contracted multiply-adds)
-CU_FLAGS = {"octbuild_gpu.cu": ["-fmad=false"]}
+# host builder's, and the FP64 first-hit casts as the reference's (no
+# contracted multiply-adds)
+CU_FLAGS = {"octbuild_gpu.cu": ["-fmad=false"], "cast64.cu": ["-fmad=false"]}
 CXX_SOURCES = ["binexpr.cpp"]
 C_SOURCES = ["scene.c", "octbuild.c"]
 
@@ -59,19 +62,20 @@ def build(verbose: bool = False, force: bool = False) -> Path:
         src, obj = CSRC / s, OBJ / (s + ".o")
         objs.append(obj)
         if force or _stale(src, obj, headers):
-            jobs.append([nvcc, *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", *CU_FLAGS.get(s, []),
+            jobs.append([nvcc, *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off",
+                         *CU_FLAGS.get(s, []),
                          "-Xptxas", "-v" if verbose else "-O3", "-c", str(src), "-o", str(obj)])
     for s in CXX_SOURCES:
         src, obj = CSRC / s, OBJ / (s + ".o")
         objs.append(obj)
         if force or _stale(src, obj, headers):
-            jobs.append(["g++", "-O2", "-fPIC", "-std=c++17", "-I", "/usr/local/cuda/include",
+            jobs.append(["g++", "-O2", "-fPIC", "-std=c++17", "-ffp-contract=off", "-I", "/usr/local/cuda/include",
                          "-c", str(src), "-o", str(obj)])
     for s in C_SOURCES:
         src, obj = CSRC / s, OBJ / (s + ".o")
         objs.append(obj)
         if force or _stale(src, obj, headers):
-            jobs.append(["gcc", "-O2", "-fPIC", "-std=gnu99", "-c", str(src), "-o", str(obj)])
+            jobs.append(["gcc", "-O2", "-fPIC", "-std=gnu99", "-ffp-contract=off", "-c", str(src), "-o", str(obj)])
     with cf.ThreadPoolExecutor(max_workers=min(8, max(1, len(jobs)))) as ex:
         list(ex.map(_run, jobs))
     if force or jobs or not LIB.exists():

@@ -30,6 +30,12 @@
  *   trk       int32[nobjs]        tracked-modifier slot of each object's
  *                                 direct modifier (-1 untracked)
  *   inst      gb_dinst[ninst]     instances: transforms, octree, surface ids
+ *   g64       double[...]         per object (at g64off[object]) its FP64
+ *                                 geometry for the first-hit casts: faces
+ *                                 normal, offset, ok, axis, count, vertices;
+ *                                 spheres centre, radius; cones ok, alpha,
+ *                                 slant, transform, end points, radii;
+ *                                 instances transforms, scales, octree
  */
 #ifndef GB_DEVSCENE_H
 #define GB_DEVSCENE_H
@@ -127,6 +133,11 @@ typedef struct {
     /* instances, in order of sidbase */
     int   ninst;
     const gb_dinst *inst;
+    /* FP64 geometry of the first-hit casts (cast64.cu): the scene cube, and
+     * per object a record at g64 + g64off[object] */
+    double cuorg64[3], cusize64;
+    const double *g64;
+    const long long *g64off;
 } gb_dscene;
 
 #endif

@@ -103,12 +103,14 @@ struct gb_scene {
     std::vector<int> hoslot;
     std::vector<float> hcone;
     std::vector<gb_dsrc> hsrc;
+    std::vector<double> hg64;          /* FP64 geometry of the first-hit casts */
+    std::vector<long long> hg64off;
     /* device scene */
-    DevBuf kids, setdata, obj, geo, fvert, fv4, cone, matd, srcd, trk, instd, orec, oslot;
+    DevBuf kids, setdata, obj, geo, fvert, fv4, cone, matd, srcd, trk, instd, orec, oslot, g64, g64off;
     gb_dscene ds;
     /* work buffers */
     DevBuf sensors, value, bins, stats, roots, rootspt, qa, qb, qcount, binprog, modinfo, hits, hitt, trkrun,
-        hitrec, adja, adjb, dlde, gradd, rootdraw, rootlot, tga, tgb, ssval, sscnt, sserr, slow, worder, whist;
+        hitrec, adja, adjb, dlde, gradd, rootdraw, rootlot, tga, tgb, ssval, sscnt, sserr, slow;
     cudaStream_t stream = nullptr;
     int sms = 0;
     cudaEvent_t ev[2 * GB_TIMED_LAUNCHES + 2];
@@ -473,7 +475,7 @@ static int prepare_device(gb_scene *G)
         upload(G->orec, G->horec) < 0 || upload(G->oslot, G->hoslot) < 0 ||
         upload(G->obj, G->hobj) < 0 || upload(G->geo, G->hgeo) < 0 || upload(G->fvert, G->hfvert) < 0 ||
         upload(G->fv4, G->hfv4) < 0 || upload(G->cone, G->hcone) < 0 || upload(G->matd, G->mat) < 0 ||
-        upload(G->srcd, G->hsrc) < 0)
+        upload(G->srcd, G->hsrc) < 0 || upload(G->g64, G->hg64) < 0 || upload(G->g64off, G->hg64off) < 0)
         return set_err(GB_ENOMEM, "device upload of the scene failed");
     gb_dscene &d = G->ds;
     d.kids = (const int *)G->kids.p;
@@ -488,6 +490,8 @@ static int prepare_device(gb_scene *G)
     d.mat = (const float4 *)G->matd.p;
     d.src = (const gb_dsrc *)G->srcd.p;
     d.inst = (const gb_dinst *)G->instd.p;
+    d.g64 = (const double *)G->g64.p;
+    d.g64off = (const long long *)G->g64off.p;
     (void)H;
     return GB_OK;
 }
@@ -722,6 +726,64 @@ static int build_arrays(gb_scene *G)
         orec.assign(4, make_float4(0, 0, 0, 0));
     G->horec.swap(orec);
     G->hoslot.swap(slot_of);
+    /* FP64 geometry per object for the first-hit casts (cast64.cu) */
+    {
+        std::vector<double> g64;
+        std::vector<long long> g64off((size_t)(H.nobjs > 0 ? H.nobjs : 1), 0);
+        g64.push_back(0.0);                      /* offset 0: objects with no record */
+        std::vector<int> inst_of((size_t)(H.nobjs > 0 ? H.nobjs : 1), -1);
+        for (int k = 0; k < H.ninst; k++)
+            inst_of[H.inst[k].obj] = k;
+        for (int32_t i = 0; i < H.nobjs; i++) {
+            const gb_object *o = &H.objs[i];
+            const int kind = obj[i].x & 0xff;
+            const long long at = (long long)g64.size();
+            if (kind == DK_FACE) {
+                const gb_face *f = &H.faces[i];
+                for (int j = 0; j < 3; j++) g64.push_back(f->norm[j]);
+                g64.push_back(f->offset);
+                g64.push_back(f->ok ? 1.0 : 0.0);
+                g64.push_back((double)f->ax);
+                g64.push_back((double)f->nv);
+                for (int j = 0; j < 3 * f->nv; j++) g64.push_back(o->farg[j]);
+            } else if (kind == DK_SPHERE || kind == DK_BUBBLE) {
+                for (int j = 0; j < 4; j++) g64.push_back(o->farg[j]);
+            } else if (kind == DK_CONE || kind == DK_CUP || kind == DK_CYL || kind == DK_TUBE || kind == DK_RING) {
+                const gb_cone *co = &H.cones[i];
+                g64.push_back(co->ok ? 1.0 : 0.0);
+                g64.push_back(co->al);
+                g64.push_back(co->sl);
+                for (int a = 0; a < 4; a++)
+                    for (int b = 0; b < 4; b++) g64.push_back(co->tm[a][b]);
+                if (kind == DK_RING)
+                    for (int j = 0; j < 6; j++) g64.push_back(o->farg[j]);
+                else {
+                    for (int j = 0; j < 3; j++) g64.push_back(o->farg[co->p0 + j]);
+                    for (int j = 0; j < 3; j++) g64.push_back(o->farg[co->p1 + j]);
+                }
+                const double r0 = co->r0 >= 0 ? o->farg[co->r0] : 0.0;
+                g64.push_back(r0);
+                g64.push_back(co->r1 >= 0 ? o->farg[co->r1] : r0);
+            } else if (kind == DK_INSTANCE && inst_of[i] >= 0) {
+                const gb_instance &I = H.inst[inst_of[i]];
+                const gb_subscene &sc = H.subs[I.sub];
+                for (int a = 0; a < 4; a++)
+                    for (int b = 0; b < 4; b++) g64.push_back(I.b.xfm[a][b]);
+                g64.push_back(I.b.sca);
+                for (int a = 0; a < 4; a++)
+                    for (int b = 0; b < 4; b++) g64.push_back(I.f.xfm[a][b]);
+                g64.push_back(I.f.sca);
+                for (int j = 0; j < 3; j++) g64.push_back(sc.cuorg[j]);
+                g64.push_back(sc.cusize);
+                g64.push_back((double)leaf_code(sc.root));
+                g64.push_back(o->omod >= 0 ? 1.0 : 0.0);
+            } else
+                continue;
+            g64off[i] = at;
+        }
+        G->hg64.swap(g64);
+        G->hg64off.swap(g64off);
+    }
     std::vector<gb_dsrc> src = G->src;
     if (src.empty()) src.resize(1);
     G->hkids.swap(kids);
@@ -755,6 +817,10 @@ static int build_arrays(gb_scene *G)
     d.src = G->hsrc.data();
     d.ninst = H.ninst;
     d.inst = G->hinst.data();
+    for (int j = 0; j < 3; j++) d.cuorg64[j] = H.cuorg[j];
+    d.cusize64 = H.cusize;
+    d.g64 = G->hg64.data();
+    d.g64off = G->hg64off.data();
     /* names for output */
     G->modname.resize(H.nobjs);
     G->matname.resize(H.nobjs);
@@ -898,11 +964,12 @@ extern "C" void gb_scene_free(gb_scene *G)
 {
     if (!G)
         return;
-    DevBuf *bufs[] = {&G->kids, &G->setdata, &G->instd, &G->orec, &G->oslot, &G->obj, &G->geo, &G->fvert, &G->fv4, &G->cone, &G->matd,
+    DevBuf *bufs[] = {&G->kids, &G->setdata, &G->instd, &G->orec, &G->oslot, &G->obj, &G->geo, &G->fvert, &G->fv4,
+                      &G->cone, &G->matd, &G->g64, &G->g64off,
                       &G->srcd, &G->trk, &G->sensors, &G->value, &G->bins, &G->stats, &G->roots, &G->rootspt, &G->qa,
                       &G->qb, &G->qcount, &G->binprog, &G->modinfo, &G->hits, &G->hitt, &G->trkrun, &G->hitrec,
                       &G->adja, &G->adjb, &G->dlde, &G->gradd, &G->rootdraw, &G->rootlot, &G->tga, &G->tgb,
-                      &G->ssval, &G->sscnt, &G->sserr, &G->slow, &G->worder, &G->whist};
+                      &G->ssval, &G->sscnt, &G->sserr, &G->slow};
     for (DevBuf *b : bufs)
         b->release();
     if (G->stream)
@@ -1297,7 +1364,7 @@ static int run(gb_scene *G, const gb_opts *o, int follow, const double *org_dir,
             return set_err(GB_ENOMEM, "device allocation failed");
         P.S.trk = nullptr;
         int rc = launch(GB_K_CAST, P, [&](gb_run &R) {
-            return gb_launch_cast(&R, (int *)G->hits.p, (float *)G->hitt.p, nullptr, st, G->sms); });
+            return gb_launch_cast64(&R, (int *)G->hits.p, (float *)G->hitt.p, nullptr, st, G->sms); });
         if (rc < 0)
             return rc;
         std::vector<int> h(n);
@@ -1408,23 +1475,8 @@ static int run(gb_scene *G, const gb_opts *o, int follow, const double *org_dir,
         P.ss_cnt = (int *)G->sscnt.p;
         P.ss_err = (float *)G->sserr.p;
     }
-    /* rays reordered for the walk of each generation (GB_WALK_ORDER=1) */
-    const char *wo = getenv("GB_WALK_ORDER");
-    const bool reorder = wo && wo[0] == '1';
-    if (reorder && (G->worder.ensure((size_t)qcap * sizeof(uint32_t)) < 0 ||
-                    G->whist.ensure(2 * GB_SORT_BUCKETS * sizeof(uint32_t)) < 0))
-        return set_err(GB_ENOMEM, "cannot allocate the walk order");
     auto walk = [&](gb_run &R) -> int {
-        if (reorder) {
-            int rc = launch(GB_K_ORDER, R, [&](gb_run &Q) {
-                return gb_launch_walk_order(&Q, (uint32_t *)G->worder.p, (uint32_t *)G->whist.p, st, G->sms); });
-            if (rc < 0)
-                return rc;
-            R.walk_order = (const uint32_t *)G->worder.p;
-        }
-        int rc = launch(GB_K_TRACE, R, [&](gb_run &Q) { return gb_launch_trace(&Q, st, G->sms); });
-        R.walk_order = nullptr;
-        return rc;
+        return launch(GB_K_TRACE, R, [&](gb_run &Q) { return gb_launch_trace(&Q, st, G->sms); });
     };
     gb_qadj *adja = (gb_qadj *)G->adja.p, *adjb = (gb_qadj *)G->adjb.p;
     unsigned long long *cnt = (unsigned long long *)G->qcount.p;   /* [0] A, [1] B, [2] work items */
@@ -1996,6 +2048,74 @@ extern "C" int gb_rcontrib_batch(int njobs, gb_scene *const *scenes, const gb_op
         *ray_count = total;
     g_stats[0] = total;
     return GB_OK;
+}
+
+/* ------------------------------------------------- measurement of ceilings */
+
+extern "C" int gb_probe_l2(int64_t table_bytes, int chase, double *gbps)
+{
+    if (!gbps || table_bytes < 64)
+        return set_err(GB_EINVAL, "bad probe arguments");
+    int dev = 0, sms = 0;
+    CK(cudaGetDevice(&dev));
+    CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    const uint32_t nrec = (uint32_t)(table_bytes / 64);
+    float4 *table = nullptr;
+    float *sink = nullptr;
+    cudaStream_t st = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    int rc = GB_OK;
+    do {
+        if (cudaMalloc(&table, (size_t)nrec * 64) != cudaSuccess || cudaMalloc(&sink, 4) != cudaSuccess) {
+            rc = set_err(GB_ENOMEM, "probe allocation failed");
+            break;
+        }
+        /* random contents: the chase's next place comes from them */
+        std::vector<float4> h((size_t)nrec * 4);
+        uint32_t x = 2463534242u;
+        for (auto &v : h) {
+            float *f = &v.x;
+            for (int k = 0; k < 4; k++) {
+                x ^= x << 13;
+                x ^= x >> 17;
+                x ^= x << 5;
+                uint32_t u = (x & 0x007fffffu) | 0x3f800000u;   /* a float in [1, 2) */
+                memcpy(f + k, &u, 4);
+            }
+        }
+        if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess ||
+            cudaMemcpy(table, h.data(), h.size() * sizeof(float4), cudaMemcpyHostToDevice) != cudaSuccess ||
+            cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) {
+            rc = set_err(GB_ECUDA, "probe set-up failed");
+            break;
+        }
+        const int iters = 256;
+        double best = 1e30;
+        for (int rep = 0; rep < 6; rep++) {
+            cudaEventRecord(e0, st);
+            if (gb_launch_probe_l2(table, nrec, iters, chase, sink, st, sms) < 0) {
+                rc = set_err(GB_ECUDA, "probe launch failed");
+                break;
+            }
+            cudaEventRecord(e1, st);
+            if (cudaEventSynchronize(e1) != cudaSuccess) {
+                rc = set_err(GB_ECUDA, "probe failed");
+                break;
+            }
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, e0, e1);
+            if (rep >= 2 && ms < best)
+                best = ms;
+        }
+        if (rc == GB_OK)
+            *gbps = (double)4 * sms * 256 * iters * 64 / (best / 1e3) / 1e9;
+    } while (0);
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    if (st) cudaStreamDestroy(st);
+    cudaFree(table);
+    cudaFree(sink);
+    return rc;
 }
 
 /* ------------------------------------------------------------- dctimestep */

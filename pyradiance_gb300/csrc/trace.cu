@@ -1826,10 +1826,8 @@ __global__ void __launch_bounds__(TRACE_BLOCK, 4) k_trace(gb_run P)
             if (base + __popc(idle) >= total)
                 exhausted = true;
             if (!active) {
-                unsigned long long i = base + __popc(idle & ((1u << lane) - 1u));
+                const unsigned long long i = base + __popc(idle & ((1u << lane) - 1u));
                 if (i < total) {
-                    if (P.walk_order)
-                        i = P.walk_order[i];
                     const float4 *q = reinterpret_cast<const float4 *>(P.qin + i);
                     const float4 a = q[0], b = q[1], c = q[2];
                     cur = i;
@@ -2050,97 +2048,35 @@ int gb_launch_primary_grad(const gb_run *P, cudaStream_t st, int sms)
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
-/* ---- walk order: rays grouped by direction octant and origin cell ---- */
-__device__ __forceinline__ uint32_t spread3(uint32_t v)     /* 4 bits -> every third bit */
+/* ---- ceilings of the walk: random 64-byte reads from an L2-resident table.
+ * Each thread reads `iters` records of 4 x float4: at independent random
+ * places (gather), or at places that depend on the last record's contents
+ * (chase: a chain of dependent loads, as the walk's descent and object
+ * records are).  Launched like the walk kernel (256 threads, 4 blocks per
+ * SM). */
+__global__ void __launch_bounds__(256, 4) k_probe_l2(const float4 *__restrict__ table, uint32_t nrec, int iters,
+                                                    int chase, float *sink)
 {
-    v &= 15u;
-    v = (v | (v << 4)) & 0x0c3u;
-    v = (v | (v << 2)) & 0x249u;
-    return v;
+    uint32_t x = (blockIdx.x * blockDim.x + threadIdx.x) * 2654435761u + 12345u;
+    float acc = 0.f;
+    for (int it = 0; it < iters; it++) {
+        const uint32_t r = x % nrec;
+        const float4 *p = table + 4 * (size_t)r;
+        const float4 a = __ldg(p), b = __ldg(p + 1), c = __ldg(p + 2), d = __ldg(p + 3);
+        acc += a.x + b.y + c.z + d.w;
+        if (chase)
+            x = (__float_as_uint(a.y) ^ (x * 1664525u)) + 1013904223u;
+        else
+            x = x * 1664525u + 1013904223u;
+    }
+    if (acc == 1234.5f)
+        sink[0] = acc;
 }
 
-__device__ __forceinline__ uint32_t walk_key(const gb_run &P, const gb_qray *q)
+int gb_launch_probe_l2(const float4 *table, uint32_t nrec, int iters, int chase, float *sink, cudaStream_t st,
+                       int sms)
 {
-    const float4 *p = reinterpret_cast<const float4 *>(q);
-    const float4 a = p[0], b = p[1];
-    const float sc = 16.f / P.S.cusize;
-    const int cx = min(max((int)((a.x - P.S.cuorg[0]) * sc), 0), 15);
-    const int cy = min(max((int)((a.y - P.S.cuorg[1]) * sc), 0), 15);
-    const int cz = min(max((int)((a.z - P.S.cuorg[2]) * sc), 0), 15);
-    const uint32_t oct = (b.x < 0.f) | ((b.y < 0.f) << 1) | ((b.z < 0.f) << 2);
-    return (oct << 12) | spread3(cx) | (spread3(cy) << 1) | (spread3(cz) << 2);
-}
-
-/* bucket counts; rays of a warp in the same bucket add once */
-__global__ void k_order_hist(gb_run P, uint32_t *hist)
-{
-    const unsigned long long n = min(*P.qin_count, (unsigned long long)P.qcap);
-    for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i - threadIdx.x < n;
-         i += (unsigned long long)gridDim.x * blockDim.x) {
-        const bool in = i < n;
-        const uint32_t key = in ? walk_key(P, P.qin + i) : 0xffffffffu;
-        const unsigned act = __ballot_sync(0xffffffffu, in);
-        if (in) {
-            const unsigned peers = __match_any_sync(act, key);
-            if ((threadIdx.x & 31) == __ffs(peers) - 1)
-                atomicAdd(hist + key, (uint32_t)__popc(peers));
-        }
-    }
-}
-
-/* exclusive scan of the bucket counts into the cursors (one block) */
-__global__ void __launch_bounds__(1024) k_order_scan(const uint32_t *hist, uint32_t *cursor)
-{
-    __shared__ uint32_t part[1024];
-    constexpr int PER = GB_SORT_BUCKETS / 1024;
-    const int t = threadIdx.x;
-    uint32_t v[PER], s = 0;
-    for (int k = 0; k < PER; k++) {
-        v[k] = hist[t * PER + k];
-        s += v[k];
-    }
-    part[t] = s;
-    __syncthreads();
-    for (int o = 1; o < 1024; o <<= 1) {
-        const uint32_t x = t >= o ? part[t - o] : 0;
-        __syncthreads();
-        part[t] += x;
-        __syncthreads();
-    }
-    uint32_t run = part[t] - s;
-    for (int k = 0; k < PER; k++) {
-        cursor[t * PER + k] = run;
-        run += v[k];
-    }
-}
-
-__global__ void k_order_scatter(gb_run P, uint32_t *cursor, uint32_t *order)
-{
-    const unsigned long long n = min(*P.qin_count, (unsigned long long)P.qcap);
-    for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i - threadIdx.x < n;
-         i += (unsigned long long)gridDim.x * blockDim.x) {
-        const bool in = i < n;
-        const uint32_t key = in ? walk_key(P, P.qin + i) : 0xffffffffu;
-        const unsigned act = __ballot_sync(0xffffffffu, in);
-        if (in) {
-            const unsigned peers = __match_any_sync(act, key);
-            const int leader = __ffs(peers) - 1;
-            uint32_t base = 0;
-            if ((int)(threadIdx.x & 31) == leader)
-                base = atomicAdd(cursor + key, (uint32_t)__popc(peers));
-            base = __shfl_sync(peers, base, leader);
-            order[base + __popc(peers & ((1u << (threadIdx.x & 31)) - 1u))] = (uint32_t)i;
-        }
-    }
-}
-
-int gb_launch_walk_order(const gb_run *P, uint32_t *order, uint32_t *hist, cudaStream_t st, int sms)
-{
-    if (cudaMemsetAsync(hist, 0, GB_SORT_BUCKETS * sizeof(uint32_t), st) != cudaSuccess)
-        return -1;
-    k_order_hist<<<sms * 8, 256, 0, st>>>(*P, hist);
-    k_order_scan<<<1, 1024, 0, st>>>(hist, hist + GB_SORT_BUCKETS);
-    k_order_scatter<<<sms * 8, 256, 0, st>>>(*P, hist + GB_SORT_BUCKETS, order);
+    k_probe_l2<<<4 * sms, 256, 0, st>>>(table, nrec, iters, chase, sink);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 

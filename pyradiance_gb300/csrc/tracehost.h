@@ -25,8 +25,7 @@
 #define GB_K_PRIMARY   3   /* primaries into the queue */
 #define GB_K_TRACE     4   /* octree walk of one generation */
 #define GB_K_SHADE     5   /* shading of one generation, children queued */
-#define GB_K_ORDER     6   /* walk order of one generation's queue */
-#define GB_K_N         7
+#define GB_K_N         6
 
 #define GRID_BITS_HOST 24      /* must equal GRID_BITS of trace.cuh */
 
@@ -118,9 +117,6 @@ typedef struct {
      * and resident blocks per SM */
     int   walk_refill;
     int   walk_blocks_per_sm;
-    /* rays of qin in walk order (a permutation of 0..count-1 grouping rays
-     * of one direction octant and origin cell), or NULL: queue order */
-    const uint32_t *walk_order;
     /* ambient super-sampling of the -I first hemispheres (rtrace -as):
      * paths carry the index (sensor * root_n^2 + stratum) of the stratum
      * they descend from in queue-parallel tag arrays, their values add to
@@ -138,6 +134,8 @@ typedef struct {
 } gb_run;
 
 int gb_launch_cast(const gb_run *P, int *hit_obj, float *hit_t, float *hit_pn, cudaStream_t st, int sms);
+/* the same first hits in FP64 (cast64.cu) */
+int gb_launch_cast64(const gb_run *P, int *hit_obj, float *hit_t, float *hit_pn, cudaStream_t st, int sms);
 int gb_launch_root(const gb_run *P, cudaStream_t st, int sms);
 /* -I roots with root_n >= 4: the strata's draws and the lots in parallel,
  * then the sequential placement per sensor */
@@ -150,11 +148,9 @@ int gb_launch_ssamp_final(const gb_run *P, cudaStream_t st, int sms);
 int gb_launch_expand_root(const gb_run *P, cudaStream_t st, int sms);
 int gb_launch_primary(const gb_run *P, cudaStream_t st, int sms);
 int gb_launch_trace(const gb_run *P, cudaStream_t st, int sms);
-/* The walk order of qin (P->walk_order, written): a counting sort of the
- * queued rays by direction octant and a 16^3 grid of origin cells over the
- * scene cube; hist is GB_SORT_BUCKETS x 2 words of scratch. */
-#define GB_SORT_BUCKETS 32768
-int gb_launch_walk_order(const gb_run *P, uint32_t *order, uint32_t *hist, cudaStream_t st, int sms);
+/* the L2 read ceilings of the walk (k_probe_l2) */
+int gb_launch_probe_l2(const float4 *table, uint32_t nrec, int iters, int chase, float *sink, cudaStream_t st,
+                       int sms);
 int gb_launch_shade(const gb_run *P, cudaStream_t st, int sms);
 /* gradient runs: the same kernels, shading with the factor lists */
 int gb_launch_root_grad(const gb_run *P, cudaStream_t st, int sms);

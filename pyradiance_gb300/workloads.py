@@ -523,3 +523,42 @@ def dc_sky(M: int, K: int, N: int, seed: int = 0):
     night = rng.random(N) < 0.5
     sky[:, night, :] = 0.0
     return dc, sky
+
+
+def polygons(rad_text: str) -> list:
+    """vertices of every polygon in a scene text"""
+    toks = rad_text.split()
+    polys, i = [], 0
+    while i + 2 < len(toks):
+        if toks[i + 1] == "polygon":
+            j = i + 3
+            ns = int(toks[j]); j += 1 + ns
+            ni = int(toks[j]); j += 1 + ni
+            nr = int(toks[j])
+            v = np.array(toks[j + 1:j + 1 + nr], dtype=float).reshape(-1, 3)
+            polys.append(v)
+            i = j + 1 + nr
+        else:
+            i += 1
+    return polys
+
+
+def aimed_rays(polys: list, inset: float, seed: int = 9):
+    """rays from random points of the room to a vertex and an edge midpoint
+    of each of 400 box faces, moved `inset` metres towards the face centre;
+    also the cosine between each ray and its face's normal"""
+    rng = np.random.default_rng(seed)
+    pts, nrm = [], []
+    for v in polys[6:406]:                        # box faces (the room shell first)
+        k = rng.integers(0, len(v))
+        c = v.mean(0)
+        n = np.cross(v[1] - v[0], v[2] - v[1])
+        for q in (v[k], 0.5 * (v[k] + v[(k + 1) % len(v)])):
+            u = c - q
+            pts.append(q + inset * u / np.linalg.norm(u))
+            nrm.append(n / np.linalg.norm(n))
+    pts = np.array(pts)
+    org = np.clip(pts + rng.normal(size=pts.shape) * 2.0, (0.05, 0.05, 0.05), (9.95, 7.95, 2.95))
+    d = pts - org
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    return np.hstack([org, d]), np.abs((d * np.array(nrm)).sum(1))

@@ -644,6 +644,24 @@ def bytes_surface(tmp: Path) -> None:
           (len(c1_a), len(c1_d), len(c1_s), len(c2_out), len(c2_file), len(dct_a), len(dct_d)))
 
 
+def edge_rays(tmp: Path) -> None:
+    """First-hit names of rays aimed at the edges and corners of the
+    direct-irradiance room's box faces (exactly, and 0.1 mm inside), from
+    the reference rtrace -ab 0 -os: where the FTINY edge rules of
+    common/face.c and the ties of rt/raytrace.c decide."""
+    text = w.daylight_room()
+    octp = oconv(text, tmp, "c1e")
+    polys = w.polygons(text)
+    out = {}
+    for key, inset in (("near", 1e-4), ("exact", 0.0)):
+        rays, _ = w.aimed_rays(polys, inset)
+        out[key + "_rays"] = rays
+        out[key + "_names"] = names(run(["rtrace", "-h", "-u-", "-ab", "0", "-fda", "-os", octp],
+                                        rays.astype("<f8").tobytes(), cwd=octp.parent))
+    np.savez_compressed(OUT / "edges.npz", cmd="rtrace -h -u- -ab 0 -fda -os", **out)
+    print("edges: %d + %d rays" % (len(out["near_rays"]), len(out["exact_rays"])))
+
+
 def dct_four() -> None:
     """dctimestep's four-matrix form (util/dctimestep.c:243-264): view
     (sensors x 145 Klems), transmission (145 x 145), daylight (145 x 146) and
@@ -747,7 +765,8 @@ def main() -> None:
              "spot": spotlights, "mirror": mirrors, "flux": flux_matrices, "flux_sc": flux_shirchiu,
              "dct": lambda tmp: dct_small(), "dct4": lambda tmp: dct_four(), "rmtxop": lambda tmp: rmtxop_cases(), "trace_oct": lambda tmp: ref_fixture_trace(),
              "c2ab1": lambda tmp: c2_stats(tmp, ab=1, K=256), "c2ab3": lambda tmp: c2_stats(tmp, ab=3, K=256),
-             "c2head": c2_headline, "gradfd": grad_fd, "bytes": bytes_surface}
+             "c2head": c2_headline, "gradfd": grad_fd, "bytes": bytes_surface,
+             "edges": edge_rays}
     only = sys.argv[1:] or list(parts)         # e.g. make_golden.py c1p
     with tempfile.TemporaryDirectory() as td:
         tmp = Path(td)

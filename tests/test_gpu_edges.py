@@ -6,7 +6,7 @@ a trailing partial record.  Hit objects are compared with the oracle."""
 import numpy as np
 import pytest
 
-from conftest import MODS_C2
+from conftest import MODS_C2, golden
 
 pytestmark = pytest.mark.gpu
 
@@ -75,76 +75,58 @@ def test_axis_rays_and_rays_from_outside(env):
     o_id, o_t = oracle_cast(po, osc, rays)
     np.testing.assert_array_equal(g_id, o_id)
     hit = o_id >= 0
-    np.testing.assert_allclose(g_t[hit], o_t[hit], rtol=1e-5, atol=2e-6)   # FP32 positions, scene of ~10 m
+    np.testing.assert_allclose(g_t[hit], o_t[hit], rtol=1e-6, atol=1e-7)   # FP64 casts, distances stored in FP32
 
 
 def _polygons(rad_text):
-    """vertices of every polygon in a scene text"""
-    toks = rad_text.split()
-    polys, i = [], 0
-    while i + 2 < len(toks):
-        if toks[i + 1] == "polygon":
-            j = i + 3
-            ns = int(toks[j]); j += 1 + ns
-            ni = int(toks[j]); j += 1 + ni
-            nr = int(toks[j])
-            v = np.array(toks[j + 1:j + 1 + nr], dtype=float).reshape(-1, 3)
-            polys.append(v)
-            i = j + 1 + nr
-        else:
-            i += 1
-    return polys
+    from pyradiance_gb300 import workloads as w
+    return w.polygons(rad_text)
 
 
 def _aimed_rays(polys, inset, seed=9):
-    """rays from random points of the room to a vertex and an edge midpoint
-    of each of 400 box faces, moved `inset` metres towards the face centre;
-    also the cosine between each ray and its face's normal"""
-    rng = np.random.default_rng(seed)
-    pts, nrm = [], []
-    for v in polys[6:406]:                        # box faces (the room shell first)
-        k = rng.integers(0, len(v))
-        c = v.mean(0)
-        n = np.cross(v[1] - v[0], v[2] - v[1])
-        for q in (v[k], 0.5 * (v[k] + v[(k + 1) % len(v)])):
-            u = c - q
-            pts.append(q + inset * u / np.linalg.norm(u))
-            nrm.append(n / np.linalg.norm(n))
-    pts = np.array(pts)
-    org = np.clip(pts + rng.normal(size=pts.shape) * 2.0, (0.05, 0.05, 0.05), (9.95, 7.95, 2.95))
-    d = pts - org
-    d /= np.linalg.norm(d, axis=1, keepdims=True)
-    return np.hstack([org, d]), np.abs((d * np.array(nrm)).sum(1))
+    from pyradiance_gb300 import workloads as w
+    return w.aimed_rays(polys, inset, seed)
+
+
+def _names(sc, hid):
+    return np.array([sc.object_name(int(i)) if i >= 0 else "*" for i in hid])
 
 
 def test_rays_near_edges_and_corners(env):
     """Aimed 0.1 mm inside box faces next to a vertex or an edge midpoint,
-    where the walk crosses leaf boundaries and tests neighbouring faces.
-    The ray also crosses the plane of the face on the other side of that
-    edge close to the edge, sometimes within FTINY plus the FP32 rounding of
-    the hit point, where the two arithmetics can decide the edge rule of
-    common/face.c:121-161 differently (measured: 1 ray in 800 on the GPU,
-    none on the host build of the same code).  Bound: 99.5%."""
+    where the walk crosses leaf boundaries and tests neighbouring faces and
+    the ray crosses the plane of the face beyond the edge within FTINY of
+    the edge.  The first hits are cast in FP64 as the reference casts them:
+    every hit object equals the reference's (tests/golden/edges.npz) and
+    the oracle's."""
     gb, _lib, po, sc, osc, scene_dir = env
-    rays, _ = _aimed_rays(_polygons((scene_dir / "c1.rad").read_text()), 1e-4)
-    g_id, g_t = cast(_lib, sc, rays)
-    o_id, o_t = oracle_cast(po, osc, rays)
-    assert (g_id == o_id).mean() >= 0.995, np.nonzero(g_id != o_id)
+    g = golden("edges.npz")
+    rays = g["near_rays"]
+    g_id, _ = cast(_lib, sc, rays)
+    o_id, _ = oracle_cast(po, osc, rays)
+    np.testing.assert_array_equal(g_id, o_id)
+    assert (_names(sc, g_id) == g["near_names"]).all(), np.nonzero(_names(sc, g_id) != g["near_names"])
 
 
 def test_rays_exactly_at_edges_and_corners(env):
     """Aimed exactly at a vertex or an edge midpoint.  There both faces
     meeting at the edge, or neither, pass the FTINY edge rules of
-    common/face.c:121-161 depending on the last bits of the hit point, which
-    FP32 and the reference's FP64 round differently (measured: about 3% of
-    these rays pick the other face or the object behind).  Bound: 95%
-    agreement; off the edges the walk agrees exactly (sensor grids, axis
-    rays, rays from outside the scene above)."""
+    common/face.c:121-161 depending on the last bits of the hit point.  The
+    FP64 casts equal the oracle's (IEEE FP64 in the reference's operation
+    order) on every ray.  The reference program is built with -ffast-math,
+    whose reordered arithmetic decides some of these ties differently from
+    any IEEE evaluation in source order: the oracle agrees with it on 94.75%
+    of these rays (and on all rays 0.1 mm off the edges), so the bar against
+    the reference is the oracle's own agreement."""
     gb, _lib, po, sc, osc, scene_dir = env
-    rays, _ = _aimed_rays(_polygons((scene_dir / "c1.rad").read_text()), 0.0)
+    g = golden("edges.npz")
+    rays = g["exact_rays"]
     g_id, _ = cast(_lib, sc, rays)
     o_id, _ = oracle_cast(po, osc, rays)
-    assert (g_id == o_id).mean() >= 0.95, np.nonzero(g_id != o_id)
+    np.testing.assert_array_equal(g_id, o_id)
+    agree = (_names(sc, g_id) == g["exact_names"]).mean()
+    print("exact-edge rays: %.4f of the hits named as the reference" % agree)
+    assert agree >= 0.945
 
 
 def test_rcontrib_records_of_c_rays(env, scene_dir):
