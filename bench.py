@@ -289,7 +289,7 @@ def dct_cpu_baseline(dc, sky):
             "sample": f"{r} and {2 * r} of the {M} rows ({ts[0]:.2f} s, {ts[1]:.2f} s), scaled to all rows"}
 
 
-def dct_measure(dev, steps: int):
+def dct_measure(dev, steps: int, rows: int | None = None):
     """DC x sky (dctimestep) on the device at the annual workload's full
     size: the tensor-core forms (FP16X3, BF16X3, FP16) and the FP32 CUDA-core
     kernel on the same resident operands, each a whole gb_dctimestep_device
@@ -302,6 +302,8 @@ def dct_measure(dev, steps: int):
     from pyradiance_gb300 import _lib
     L = _lib.lib()
     M, K, N = DCT_SHAPE
+    if rows:
+        M = rows
     dc, sky = dct_operands(dev, M, K, N)
     st = torch.cuda.current_stream(dev)
 
@@ -662,6 +664,9 @@ def main():
     ap.add_argument("--sensors", type=int, default=0,
                     help="profile a smaller case: this many sensors of the grid, without the dctimestep, "
                          "gradient and batching legs")
+    ap.add_argument("--dct-rows", type=int, default=0,
+                    help="profile dctimestep alone at this many rows (2,306 x 8,760 otherwise as the annual "
+                         "workload); prints its result")
     ap.add_argument("--no-extras", action="store_true",
                     help="the rcontrib workload only (no dctimestep, gradient and batching legs)")
     args = ap.parse_args()
@@ -669,6 +674,9 @@ def main():
         args.steps = 5 if args.impl == "reference" else 30
     if args.impl == "reference":
         reference_arm(args)
+    elif args.dct_rows:
+        import torch
+        print(json.dumps(dct_measure(torch.device("cuda", 0), args.steps, rows=args.dct_rows)), flush=True)
     else:
         gpu_arm(args)
 
