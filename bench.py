@@ -249,11 +249,22 @@ def traffic_from_profiles(kernel: str):
 DCT_SHAPE = (16384, 2306, 8760)    # 16,384 sensors x 2,306 Reinhart MF:4 patches x 8,760 hours
 
 
+def night_hours(N):
+    """The night hours of an annual hourly sky (column n = hour n % 24 of
+    day n // 24): day length 12 +- 4 h over the year (longest at day 172),
+    centred on noon, so that half of the hours are night, in one run per
+    night as in an annual sky of a mid-latitude site."""
+    n = np.arange(N)
+    day, hour = n // 24, n % 24 + 0.5
+    length = 12 + 4 * np.cos(2 * np.pi * (day - 172) / 365)
+    return np.abs(hour - 12) >= length / 2
+
+
 def dct_operands(dev, M, K, N, seed=0):
     """Annual daylight-coefficient operands: DC lognormal(-6, 2) with 30%
     exact zeros; sky lognormal(2, 1) diffuse background plus, in each
-    daylight hour, one sun patch of 1e4..1e6 (log-uniform); about half of
-    the hours are night (all-zero columns)."""
+    daylight hour, one sun patch of 1e4..1e6 (log-uniform); the night hours
+    (half of them, one run per night) are all-zero columns."""
     import torch
     g = torch.Generator(device=dev).manual_seed(seed)
     dc = torch.exp(torch.randn(M, K, 3, device=dev, generator=g) * 2 - 6)
@@ -262,7 +273,7 @@ def dct_operands(dev, M, K, N, seed=0):
     sun = torch.randint(0, K, (N,), device=dev, generator=g)
     peak = torch.exp(torch.empty(N, device=dev).uniform_(np.log(1e4), np.log(1e6), generator=g))
     sky[sun, torch.arange(N, device=dev), :] = peak[:, None]
-    sky[:, torch.rand(N, device=dev, generator=g) < 0.5] = 0
+    sky[:, torch.as_tensor(night_hours(N), device=dev)] = 0
     return dc, sky
 
 

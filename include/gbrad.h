@@ -195,11 +195,14 @@ int  gb_rcontrib_nbins(const gb_modspec *mods, int nmods, int *nbins_total);
  *                  the FP16 range, fp16 hi/lo split, 3 tensor-core products,
  *                  FP32 accumulate (within 1e-5 relative of FP64)
  *   GB_DCT_FP16    the same scaled fp16 operands, one product (about 1e-3)
- * The tensor-core forms skip all-zero rows of DC and all-zero columns of S
- * as cm_multiply does (their outputs are zero).  The environment variable
- * GB_DCT_WAIT_NS (nanoseconds, read at each call) shortens the limit of the
- * tensor-core pipeline's waits, normally 2 s, after which a call returns
- * GB_ECUDA: for tests of that error path. */
+ * The tensor-core forms skip all-zero columns of S as cm_multiply does
+ * (their outputs are zero); all-zero rows of DC are multiplied (their
+ * outputs are the same zeros).  The environment variable GB_DCT_WAIT_NS
+ * (nanoseconds, read at each call) shortens the limit of the tensor-core
+ * pipeline's waits, normally 2 s, after which a call returns GB_ECUDA: for
+ * tests of that error path.  GB_DCT_CLUSTER=1 (read at each call) runs one
+ * CTA per row tile instead of clusters of two that share the column tile's
+ * copies: the same results, for tests and measurement. */
 #define GB_DCT_FP32   0
 #define GB_DCT_BF16X3 1
 #define GB_DCT_FP64   2

@@ -3,10 +3,11 @@
  *
  * R[m,n,c] = sum_k A[m,k,c] * B[k,n,c] for each colour channel c
  * (util/cmatrix.c:421-474 cm_multiply; the channels do not mix), with the
- * reference's skip of all-zero rows of A and all-zero columns of B (a row
- * or column is zero when every byte of its colours is, cmatrix.c:435-450):
- * their outputs are written as zeros and the product runs over the others
- * only.  Three arithmetic forms share one kernel:
+ * reference's skip of all-zero columns of B (a column is zero when every
+ * byte of its colours is, cmatrix.c:435-450): their outputs are written as
+ * zeros and the product runs over the other columns only.  All-zero rows of
+ * A (rare in daylight coefficients) are not skipped: their products are
+ * exact zeros, the same output.  Three arithmetic forms share one kernel:
  *
  *   BF16X3  x = hi + lo + r, hi = bf16(x), lo = bf16(x - hi), |r| <= 2^-16 |x|;
  *           product hi*hi + hi*lo + lo*hi (three bf16 products).  The
@@ -22,21 +23,25 @@
  *           (three fp16 products, exact in the FP32 accumulator).  The
  *           epilogue undoes both scales exactly (powers of two).
  *   FP16    the scaled hi*hi product alone (one fp16 product, about 2^-11
- *           relative per operand): the fast low-precision form.
+ *           relative per operand): the fast low-precision form, with all
+ *           of K accumulated in the tensor cores.
  *
- * 1. k_row_scan / k_col_scan: per row of A and column of B, the largest
- *    magnitude of each channel and whether any colour is non-zero.
- *    k_compact: the lists of non-zero rows and columns and their scale
- *    exponents.  k_zero_fill: the outputs of zero rows and columns.
- * 2. k_split_a / k_split_b (memory bound) gather the non-zero rows and
- *    columns, scale them, and split them into 16-bit hi/lo planes, K
- *    contiguous, zero padded to the tile sizes: As[c][h][Mp][Kp] and
- *    Bs[c][h][Np][Kp] (B transposed through shared memory).
- * 3. k_dct_tc: a persistent kernel, one CTA per SM, 10 warps:
- *      warp 0  TMA producer: 128x64 (A) and 256x64 (B) 16-bit boxes with the
- *              128-byte swizzle, of each plane in use, into a ring of
- *              shared-memory stages (2 stages of 96 KB for the split forms,
- *              4 of 48 KB for FP16)
+ * 1. k_col_scan: per column of B, the largest magnitude of each channel
+ *    and whether any colour is non-zero; k_compact: the list of non-zero
+ *    columns and their scale exponents (the one host synchronisation of a
+ *    call reads their count).
+ * 2. k_split_rows (memory bound, one pass over A from HBM): per row of A,
+ *    its scale exponents, then the row scaled and split into 16-bit hi/lo
+ *    planes.  k_split_b gathers, scales and splits the non-zero columns of
+ *    B.  Both K contiguous, zero padded to the tile sizes: As[c][h][Mp][Kp]
+ *    and Bs[c][h][Np][Kp] (B transposed through shared memory).
+ * 3. k_dct_tc: a persistent kernel, one CTA per SM, 12 warps:
+ *      warp 0  TMA producer: 128x32 (A) and 256x32 (B) 16-bit boxes with the
+ *              64-byte swizzle, of each plane in use, into a ring of
+ *              shared-memory stages (4 stages of 48 KB for the split forms,
+ *              8 of 24 KB for FP16): three stages in flight while the
+ *              products run on the fourth.  (Two stages of 96 KB, with
+ *              128-byte boxes, left the products waiting on the copies.)
  *      warp 1  allocates 512 TMEM columns (two 128x256 FP32 accumulators)
  *              and one lane issues tcgen05.mma (M=128, N=256, K=16),
  *              committing each stage back to the producer and each finished
@@ -54,9 +59,19 @@
  *              of the next.  The finished tile is transposed through shared
  *              memory, 32 x 32 per warp, so that each store instruction
  *              writes 32 consecutive columns of one output row.
- *    Tiles run channel-innermost, so the three channels of one output block
+ *      warps 10-11  the zeros of the zero columns of B among each unit's
+ *              output columns (from its first column to the next column
+ *              tile's first), all three channels of a third of the rows
+ *              per channel unit, as runs of consecutive floats, while the
+ *              products run; every output is written once, by this kernel.
+ *    Units run channel-innermost, so the three channels of one output block
  *    are written at the same time by neighbouring CTAs and merge in L2, and
- *    in groups of 16 row tiles for operand reuse in L2.
+ *    in groups of 2048 rows of A for operand reuse in L2.
+ *    With two or more row tiles the CTAs run in clusters of two on row
+ *    tiles 2p and 2p + 1 of the same column tile: each copies its A tile
+ *    and one half of the B tile, multicast to both CTAs (half the L2 reads
+ *    of B), and a stage is released when both CTAs' products over it are
+ *    done.
  *
  * Every wait on an mbarrier is bounded (two seconds of %globaltimer); on
  * expiry the CTA records an error code, stops issuing work, waits (bounded,
@@ -81,13 +96,19 @@
 
 namespace {
 
-constexpr int TM = 128, TN = 256, TK = 64;          /* tile; TK 16-bit elements = 128 bytes */
-constexpr int A_BYTES = TM * TK * 2;                /* 16 KB per plane */
-constexpr int B_BYTES = TN * TK * 2;                /* 32 KB per plane */
+constexpr int TM = 128, TN = 256, TK = 32;          /* tile; TK 16-bit elements = 64 bytes */
+constexpr int SWZ = TK * 2;                         /* swizzle span: one K row of a box (64 bytes) */
+constexpr int A_BYTES = TM * TK * 2;                /* 8 KB per plane */
+constexpr int B_BYTES = TN * TK * 2;                /* 16 KB per plane */
 constexpr int TMEM_COLS = 512;                      /* 2 accumulators x TN */
-constexpr int GROUP_M = 16;                         /* row tiles per raster group */
-constexpr int NTHREADS = 320;                       /* producer, MMA, 8 epilogue warps */
-constexpr int CHUNK_KB = 2;                         /* K blocks per accumulator chunk (K = 128) */
+constexpr int GROUP_ROWS = 2048;                    /* rows of A per raster group (their planes stay in L2) */
+constexpr int NTHREADS = 384;                       /* producer, MMA, 8 epilogue warps, 2 zero-column warps */
+constexpr int CHUNK_KB = 128 / TK;                  /* K blocks per accumulator chunk (K = 128) */
+/* the FP16 form (one product, operands rounded to 2^-11) accumulates all of
+ * K in one accumulator: the tensor cores' accumulation error (about 1e-5)
+ * is far below its operand rounding, and the epilogue runs once per tile */
+template <int NH>
+__host__ __device__ constexpr int chunk_kb() { return NH == 2 ? CHUNK_KB : 1 << 20; }
 constexpr int EPI_COLS = TN / 2;                    /* columns per epilogue thread */
 constexpr int XPOSE_BYTES = 8 * 32 * 32 * 4;        /* one 32 x 32 float block per epilogue warp */
 constexpr uint64_t WAIT_NS = 2000000000ull;         /* limit of every wait: 2 s */
@@ -96,7 +117,7 @@ constexpr uint64_t WAIT_NS = 2000000000ull;         /* limit of every wait: 2 s 
 template <int NH>
 struct Ring {
     static constexpr int STAGE_BYTES = NH * (A_BYTES + B_BYTES);
-    static constexpr int STAGES = NH == 2 ? 2 : 4;
+    static constexpr int STAGES = NH == 2 ? 4 : 8;
     static constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + XPOSE_BYTES + 1024 /* alignment */ + 256 /* barriers */;
 };
 
@@ -114,10 +135,12 @@ enum { ERR_NONE = 0, ERR_FULL = 1, ERR_EMPTY = 2, ERR_TFULL = 3, ERR_TEMPTY = 4,
 
 struct Shape {
     int M, K, N;          /* true sizes */
-    int Mc, Nc;           /* non-zero rows of A, columns of B */
-    int Mp, Kp, Np;       /* Mc, K, Nc padded to TM, TK, TN */
+    int Nc;               /* non-zero columns of B */
+    int Mp, Kp, Np;       /* M, K, Nc padded to the tiles (M to pairs of row tiles in clusters) */
     int mt, nt, kb;       /* tile counts, K blocks */
     long long tiles;      /* mt * nt * 3 */
+    int mu;               /* row units: row tiles, or pairs of them in clusters of two */
+    long long units;      /* mu * nt * 3 */
     int scaled;           /* rows and columns carry power-of-two scales */
     unsigned long long wait_ns;
 };
@@ -191,15 +214,41 @@ __device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap *map
         : "memory");
 }
 
-/* shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row groups
- * 1024 bytes apart (stride byte offset), descriptor version 1 (bit 46) */
+/* the same box into this CTA's and its cluster peer's shared memory (same
+ * offset in each), each CTA's mbarrier at the same offset signalled */
+__device__ __forceinline__ void tma_load_2d_mc(uint32_t dst, const CUtensorMap *map, int x, int y, uint32_t bar,
+                                               uint16_t mask)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes.multicast::cluster "
+        "[%0], [%1, {%2, %3}], [%4], %5;"
+        ::"r"(dst), "l"((uint64_t)map), "r"(x), "r"(y), "r"(bar), "h"(mask)
+        : "memory");
+}
+
+__device__ __forceinline__ uint32_t cluster_rank()
+{
+    uint32_t r;
+    asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+    return r;
+}
+
+__device__ __forceinline__ void cluster_sync_all()
+{
+    asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+
+/* shared-memory matrix descriptor: K-major, rows of SWZ bytes with the
+ * SWZ-byte swizzle (layout type 2: 128 bytes, 4: 64 bytes), 8-row groups
+ * 8 * SWZ bytes apart (stride byte offset), descriptor version 1 (bit 46) */
 __device__ __forceinline__ uint64_t sdesc(uint32_t saddr)
 {
+    static_assert(SWZ == 128 || SWZ == 64, "swizzle span");
     uint64_t d = (uint64_t)((saddr & 0x3FFFFu) >> 4);
     d |= (uint64_t)(16u >> 4) << 16;
-    d |= (uint64_t)(1024u >> 4) << 32;
+    d |= (uint64_t)((8u * SWZ) >> 4) << 32;
     d |= (uint64_t)1 << 46;
-    d |= (uint64_t)2 << 61;
+    d |= (uint64_t)(SWZ == 128 ? 2 : 4) << 61;
     return d;
 }
 
@@ -217,6 +266,15 @@ __device__ __forceinline__ void mma16(uint32_t dt, uint64_t a, uint64_t b, uint3
 __device__ __forceinline__ void mma_commit(uint32_t bar)
 {
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
+                 : "memory");
+}
+
+/* arrive, once these products finish, on the mbarrier at this offset in
+ * every CTA of the mask */
+__device__ __forceinline__ void mma_commit_mc(uint32_t bar, uint16_t mask)
+{
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 [%0], %1;"
+                 ::"r"(bar), "h"(mask)
                  : "memory");
 }
 
@@ -238,31 +296,47 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float v[16])
         v[i] = __uint_as_float(r[i]);
 }
 
-/* tile t -> (channel, row tile, column tile): channel innermost, then row
- * tiles in groups of GROUP_M sweeping the column tiles */
+/* work unit t -> (channel, row unit, column tile): channel innermost, then
+ * the row units of a group of GROUP_ROWS rows (row tiles, or pairs of them)
+ * sweeping the column tiles, so that the group's A planes (2048 rows: 57 MB
+ * in the split forms) are reused from L2 by every column tile of B.
+ * Measured at 16384 x 2306 x 8760: groups of 1024 and 2048 rows take the
+ * same time, groups of 4096 rows 4.5% longer. */
+template <int CL>
 __device__ __forceinline__ void tile_coords(const Shape &s, long long t, int &c, int &mi, int &ni)
 {
+    constexpr int G = GROUP_ROWS / (TM * CL);
     c = (int)(t % 3);
-    long long u = t / 3;
-    long long per_group = (long long)GROUP_M * s.nt;
-    int g = (int)(u / per_group);
-    int r = (int)(u % per_group);
-    int gm = s.mt - g * GROUP_M;
-    if (gm > GROUP_M)
-        gm = GROUP_M;
-    mi = g * GROUP_M + r % gm;
+    const long long u = t / 3;
+    const long long per_group = (long long)G * s.nt;
+    const int g = (int)(u / per_group);
+    const int r = (int)(u % per_group);
+    int gm = s.mu - g * G;
+    if (gm > G)
+        gm = G;
+    mi = g * G + r % gm;
     ni = r / gm;
 }
 
-/* The product over the compacted operands.  rowidx/colidx map compact rows
- * and columns to output rows and columns; ea[c][i] and eb[c][j] are the
- * scale exponents of compact row i and column j (scaled forms). */
-template <int NH, bool BF16>
+/* The product over the rows of A and the compacted columns of B.  colidx
+ * maps compact columns to output columns, colflag marks the non-zero
+ * columns of B; ea[c][m] and eb[c][j] are the scale exponents of row m and
+ * compact column j (scaled forms).  Each tile also writes the zeros of the
+ * zero columns among its output columns. */
+template <int NH, bool BF16, int CL>
 __global__ void __launch_bounds__(NTHREADS, 1)
 k_dct_tc(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB, Shape s,
-         float *__restrict__ C, const int *__restrict__ rowidx, const int *__restrict__ colidx,
+         float *__restrict__ C, const int *__restrict__ colidx, const int *__restrict__ colflag,
          const int *__restrict__ ea, const int *__restrict__ eb, int *err)
 {
+    /* CL = 2: the two CTAs of a cluster take row tiles 2p and 2p + 1 of the
+     * same column tile and channel; each loads its own A tile and one half
+     * of the shared B tile, multicast into both CTAs, and a stage is free
+     * once both CTAs' products over it have finished.  The work units are
+     * the pairs of row tiles (s.mu of them), in the same order on both
+     * CTAs. */
+    const int rank = CL == 2 ? (int)cluster_rank() : 0;
+    const int unit0 = blockIdx.x / CL, ustride = gridDim.x / CL;
     using R = Ring<NH>;
     constexpr int STAGES = R::STAGES, STAGE_BYTES = R::STAGE_BYTES;
     constexpr uint32_t IDESC = idesc<BF16>();
@@ -281,11 +355,11 @@ k_dct_tc(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUten
     if (threadIdx.x == 0) {
         for (int i = 0; i < STAGES; i++) {
             mbar_init(full0 + 8 * i, 1);
-            mbar_init(empty0 + 8 * i, 1);
+            mbar_init(empty0 + 8 * i, CL);
         }
         for (int i = 0; i < 2; i++) {
             mbar_init(tfull0 + 8 * i, 1);
-            mbar_init(tempty0 + 8 * i, 8 * 32);
+            mbar_init(tempty0 + 8 * i, 8);           /* one arrival per epilogue warp */
         }
         mbar_init(drain, 1);
         *abort_flag = 0;
@@ -301,6 +375,8 @@ k_dct_tc(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUten
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
+    if (CL == 2)
+        cluster_sync_all();              /* the peer's barriers are initialised */
     const uint32_t tmem = *tmem_slot;
 
     if (warp == 0) {
@@ -309,9 +385,10 @@ k_dct_tc(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUten
             asm volatile("prefetch.tensormap [%0];" ::"l"((uint64_t)&mapA) : "memory");
             asm volatile("prefetch.tensormap [%0];" ::"l"((uint64_t)&mapB) : "memory");
             long long it = 0;
-            for (long long t = blockIdx.x; t < s.tiles && !*abort_flag; t += gridDim.x) {
+            for (long long t = unit0; t < s.units && !*abort_flag; t += ustride) {
                 int c, mi, ni;
-                tile_coords(s, t, c, mi, ni);
+                tile_coords<CL>(s, t, c, mi, ni);
+                mi = mi * CL + rank;
                 const int ya = NH * c * s.Mp + mi * TM, yb = NH * c * s.Np + ni * TN;
                 for (int kb = 0; kb < s.kb; kb++, it++) {
                     const int st = (int)(it % STAGES);
@@ -323,7 +400,11 @@ k_dct_tc(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUten
 #pragma unroll
                     for (int h = 0; h < NH; h++) {
                         tma_load_2d(base + h * A_BYTES, &mapA, kb * TK, ya + h * s.Mp, fb);
-                        tma_load_2d(base + NH * A_BYTES + h * B_BYTES, &mapB, kb * TK, yb + h * s.Np, fb);
+                        if (CL == 2)             /* this CTA's half of the B tile, into both CTAs */
+                            tma_load_2d_mc(base + NH * A_BYTES + h * B_BYTES + rank * (B_BYTES / 2), &mapB, kb * TK,
+                                           yb + h * s.Np + rank * (TN / 2), fb, (uint16_t)3);
+                        else
+                            tma_load_2d(base + NH * A_BYTES + h * B_BYTES, &mapB, kb * TK, yb + h * s.Np, fb);
                     }
                 }
             }
@@ -341,8 +422,8 @@ k_dct_tc(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUten
         if (lane == 0) {
             long long it = 0, cl = 0;
             bool ok = true;
-            for (long long t = blockIdx.x; t < s.tiles && ok; t += gridDim.x) {
-                for (int k0 = 0; k0 < s.kb && ok; k0 += CHUNK_KB, cl++) {
+            for (long long t = unit0; t < s.units && ok; t += ustride) {
+                for (int k0 = 0; k0 < s.kb && ok; k0 += chunk_kb<NH>(), cl++) {
                     const int buf = (int)(cl & 1);
                     const uint32_t use = (uint32_t)((cl >> 1) & 1);
                     if (!mbar_wait(tempty0 + 8 * buf, use ^ 1, abort_flag, err, ERR_TEMPTY, wns)) {
@@ -351,7 +432,7 @@ k_dct_tc(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUten
                     }
                     tc_fence_after();
                     const uint32_t dt = tmem + (uint32_t)(buf * TN);
-                    const int k1 = k0 + CHUNK_KB < s.kb ? k0 + CHUNK_KB : s.kb;
+                    const int k1 = k0 + chunk_kb<NH>() < s.kb ? k0 + chunk_kb<NH>() : s.kb;
                     for (int kb = k0; kb < k1; kb++, it++) {
                         const int st = (int)(it % STAGES);
                         const uint32_t ph = (uint32_t)((it / STAGES) & 1);
@@ -373,7 +454,10 @@ k_dct_tc(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUten
                                 mma16<IDESC>(dt, alo, bhi, 1);
                             }
                         }
-                        mma_commit(empty0 + 8 * st);      /* stage free once these products finish */
+                        if (CL == 2)                      /* the stage is free in both CTAs once */
+                            mma_commit_mc(empty0 + 8 * st, (uint16_t)3);   /* both CTAs' products finish */
+                        else
+                            mma_commit(empty0 + 8 * st);  /* stage free once these products finish */
                     }
                     if (ok)
                         mma_commit(tfull0 + 8 * buf);     /* chunk complete */
@@ -384,21 +468,22 @@ k_dct_tc(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUten
             mbar_wait(drain, 0, abort_flag, err, ERR_DRAIN, WAIT_NS, false);
         }
         __syncwarp();
-    } else {
+    } else if (warp < 10) {
         /* ---------------- epilogue: warps 2..9; TMEM sub-partition warp % 4,
          * column half (warp - 2) / 4.  Each K chunk's FP32 accumulator is
          * added into registers (IEEE round to nearest), so the tensor cores'
-         * accumulation rounding acts on chains of CHUNK_KB * TK products only */
+         * accumulation rounding acts on chains of CHUNK_KB * TK products only
+         * (split forms) */
         const int sub = warp & 3, half = (warp - 2) >> 2;
         float *xs = xpose + (warp - 2) * 1024;
         long long cl = 0;
         bool ok = true;
-        for (long long t = blockIdx.x; t < s.tiles && ok; t += gridDim.x) {
+        for (long long t = unit0; t < s.units && ok; t += ustride) {
             float acc[EPI_COLS];
 #pragma unroll
             for (int i = 0; i < EPI_COLS; i++)
                 acc[i] = 0.f;
-            for (int k0 = 0; k0 < s.kb; k0 += CHUNK_KB, cl++) {
+            for (int k0 = 0; k0 < s.kb; k0 += chunk_kb<NH>(), cl++) {
                 const int buf = (int)(cl & 1);
                 const uint32_t use = (uint32_t)((cl >> 1) & 1);
                 ok = mbar_wait(tfull0 + 8 * buf, use, abort_flag, err, ERR_TFULL, wns);
@@ -416,18 +501,20 @@ k_dct_tc(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUten
                         acc[cb + i] += v[i];
                 }
                 tc_fence_before();
-                mbar_arrive(tempty0 + 8 * buf);
+                __syncwarp();
+                if (lane == 0)
+                    mbar_arrive(tempty0 + 8 * buf);
             }
             if (!ok)
                 break;
             int c, mi, ni;
-            tile_coords(s, t, c, mi, ni);
-            /* this warp's 32 compact rows: lane r holds row r's output index
-             * and scale exponent, broadcast below */
-            const int ir = mi * TM + sub * 32 + lane;
-            const int my_m = ir < s.Mc ? rowidx[ir] : -1;
-            const int my_ea = (ir < s.Mc && s.scaled) ? ea[(long long)c * s.Mc + ir] : 0;
-            const int nrows = min(32, s.Mc - (mi * TM + sub * 32));
+            tile_coords<CL>(s, t, c, mi, ni);
+            mi = mi * CL + rank;
+            /* this warp's 32 rows: lane r holds row r's scale exponent,
+             * broadcast below */
+            const int row0 = mi * TM + sub * 32, ir = row0 + lane;
+            const int my_ea = (ir < s.M && s.scaled) ? ea[(long long)c * s.M + ir] : 0;
+            const int nrows = min(32, s.M - row0);
             const int jc0 = ni * TN + half * EPI_COLS;
 #pragma unroll
             for (int b = 0; b < EPI_COLS / 32; b++) {
@@ -440,14 +527,56 @@ k_dct_tc(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUten
                 const bool colok = jc < s.Nc;
                 const int n = colok ? colidx[jc] : 0;
                 const int ebn = (colok && s.scaled) ? eb[(long long)c * s.Nc + jc] : 0;
-                for (int r = 0; r < nrows; r++) {
+                float *out = C + ((long long)row0 * s.N + n) * 3 + c;
+                const long long rstride = 3LL * s.N;
+                for (int r = 0; r < nrows; r++, out += rstride) {
                     const float v = xs[r * 32 + (lane ^ r)];
-                    const int m = __shfl_sync(0xffffffffu, my_m, r);
                     const int e = __shfl_sync(0xffffffffu, my_ea, r) + ebn;
+                    /* v * 2^-e: one multiply by the power of two when it is a
+                     * normal float (exact, or rounded once as ldexpf rounds) */
                     if (colok)
-                        C[((long long)m * s.N + n) * 3 + c] = s.scaled ? ldexpf(v, -e) : v;
+                        *out = !s.scaled                  ? v
+                               : (e >= -126 && e <= 126) ? v * __int_as_float((127 - e) << 23)
+                                                         : ldexpf(v, -e);
                 }
                 __syncwarp();
+            }
+        }
+    } else {
+        /* ---------------- warps 10-11: the outputs of the zero columns of
+         * B.  For each unit of this CTA, among the unit's output columns
+         * (from its first column to the next column tile's first; from 0
+         * for the first tile, to N for the last), all three channels, in
+         * the unit's rows r with r % 3 == c (the unit's channel): runs of
+         * consecutive floats, written while the products run.  The three
+         * channel units of a tile cover all its rows. */
+        const int hw = warp - 10;
+        const long long rstride = 3LL * s.N;
+        for (long long t = unit0; t < s.units && !*abort_flag; t += ustride) {
+            int c, mi, ni;
+            tile_coords<CL>(s, t, c, mi, ni);
+            mi = mi * CL + rank;
+            const int lo = ni == 0 ? 0 : colidx[ni * TN];
+            const int hi = ni + 1 == s.nt ? s.N : colidx[(ni + 1) * TN];
+            const int r1 = min(mi * TM + TM, s.M);
+            /* windows of 64 x 32 floats: the zero pattern is the same in
+             * every row, so each lane first gathers its bit per 32-float
+             * step of the window, then the rows are plain stores */
+            for (int w0 = 3 * lo; w0 < 3 * hi; w0 += 64 * 32) {
+                const int w1 = min(3 * hi, w0 + 64 * 32);
+                unsigned long long zmask = 0;
+                for (int i = 0; w0 + 32 * i < w1; i++) {
+                    const int f = w0 + 32 * i + lane;
+                    if (f < w1 && !colflag[f / 3])
+                        zmask |= 1ull << i;
+                }
+                if (!__any_sync(0xffffffffu, zmask != 0))
+                    continue;
+                for (int row = mi * TM + c + 3 * hw; row < r1; row += 6) {
+                    float *out = C + row * rstride + w0 + lane;
+                    for (unsigned long long m = zmask; m; m &= m - 1)
+                        out[32 * __ffsll((long long)m) - 32] = 0.f;
+                }
             }
         }
     }
@@ -458,43 +587,11 @@ k_dct_tc(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUten
     if (warp == 1)
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS)
                      : "memory");
+    if (CL == 2)
+        cluster_sync_all();              /* no copy or arrival of the peer targets this CTA any more */
 }
 
 /* ----------------------------------------------------------------- scans */
-
-/* Per row m of A[m][k][c]: the largest magnitude of each channel (as the
- * bits of a non-negative float, which order as unsigned integers) and
- * whether any byte of the row is non-zero.  One warp per row. */
-__global__ void k_row_scan(const float *__restrict__ A, int M, int K, unsigned *__restrict__ rowmax,
-                           int *__restrict__ rowflag)
-{
-    const int m = (int)(((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
-    if (m >= M)
-        return;
-    const float *a = A + (long long)m * K * 3;
-    unsigned mx[3] = {0, 0, 0}, any = 0;
-    const int n3 = 3 * K;
-    for (int j = lane; j < n3; j += 32) {
-        const unsigned u = __float_as_uint(a[j]);
-        any |= u;
-        const int ch = j % 3;
-        const unsigned v = u & 0x7fffffffu;
-        mx[ch] = v > mx[ch] ? v : mx[ch];
-    }
-#pragma unroll
-    for (int o = 16; o; o >>= 1) {
-        any |= __shfl_xor_sync(0xffffffffu, any, o);
-#pragma unroll
-        for (int ch = 0; ch < 3; ch++)
-            mx[ch] = max(mx[ch], __shfl_xor_sync(0xffffffffu, mx[ch], o));
-    }
-    if (lane == 0) {
-        rowflag[m] = any != 0;
-        rowmax[3 * m] = mx[0];
-        rowmax[3 * m + 1] = mx[1];
-        rowmax[3 * m + 2] = mx[2];
-    }
-}
 
 /* Per column n of B[k][n][c], over the rows k in [blockIdx.y * kspan, ...):
  * the same, merged with atomics (colmax and colflag start at zero). */
@@ -563,23 +660,6 @@ __global__ void __launch_bounds__(1024) k_compact(const int *__restrict__ flag, 
         *count = total;
 }
 
-/* Outputs of zero rows of A or zero columns of B are zero (the product
- * kernel writes the others): rows over the grid's y, columns over x. */
-__global__ void k_zero_fill(float *__restrict__ C, const int *__restrict__ rowflag, const int *__restrict__ colflag,
-                            int M, int N)
-{
-    for (int m = blockIdx.y; m < M; m += gridDim.y) {
-        const bool zr = !rowflag[m];
-        float *row = C + (long long)m * N * 3;
-        for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < N; n += gridDim.x * blockDim.x)
-            if (zr || !colflag[n]) {
-                row[3 * n] = 0.f;
-                row[3 * n + 1] = 0.f;
-                row[3 * n + 2] = 0.f;
-            }
-    }
-}
-
 /* ----------------------------------------------------------------- splits */
 
 template <bool BF16>
@@ -589,38 +669,73 @@ struct Half16<true> {
     typedef __nv_bfloat16 T;
     static __device__ __forceinline__ T rn(float x) { return __float2bfloat16_rn(x); }
     static __device__ __forceinline__ float f(T h) { return __bfloat162float(h); }
+    static __device__ __forceinline__ unsigned bits(T h) { return __bfloat16_as_ushort(h); }
 };
 template <>
 struct Half16<false> {
     typedef __half T;
     static __device__ __forceinline__ T rn(float x) { return __float2half_rn(x); }
     static __device__ __forceinline__ float f(T h) { return __half2float(h); }
+    static __device__ __forceinline__ unsigned bits(T h) { return __half_as_ushort(h); }
 };
 
-/* Compact row i of A (row rowidx[i]), scaled by 2^ea[c][i] -> As[c][h][Mp][Kp]
- * hi (and lo), one thread per element of the padded plane (zeros in the
- * padding). */
+/* Row m of A, one block of 256 threads per row of the padded planes: the
+ * largest magnitude of each channel gives the row's scale exponents
+ * ea[c][m] (scaled forms), and the row, scaled, is split into the hi (and
+ * lo) planes As[c][h][Mp][Kp], K contiguous, zeros in the padding (k >= K,
+ * m >= M).  The second pass over the row reads it from L2. */
 template <int NH, bool BF16>
-__global__ void k_split_a(const float *__restrict__ A, typename Half16<BF16>::T *__restrict__ As,
-                          const int *__restrict__ rowidx, const int *__restrict__ ea, Shape s)
+__global__ void __launch_bounds__(256) k_split_rows(const float *__restrict__ A,
+                                                    typename Half16<BF16>::T *__restrict__ As,
+                                                    int *__restrict__ ea, Shape s)
 {
     typedef Half16<BF16> H;
-    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= (long long)s.Mp * s.Kp)
-        return;
-    const int r = (int)(i / s.Kp), k = (int)(i % s.Kp);
-    const bool in = r < s.Mc && k < s.K;
+    __shared__ unsigned red[3][8];
+    const int m = blockIdx.x, t = threadIdx.x, lane = t & 31, w = t >> 5;
     const size_t plane = (size_t)s.Mp * s.Kp;
-    const float *a = in ? A + 3 * ((long long)rowidx[r] * s.K + k) : A;
+    const bool live = m < s.M;
+    const float *a = A + (size_t)(live ? m : 0) * s.K * 3;
+    int e[3] = {0, 0, 0};
+    if (live && s.scaled) {
+        unsigned mx[3] = {0, 0, 0};
+        for (int k = t; k < s.K; k += 256) {
 #pragma unroll
-    for (int c = 0; c < 3; c++) {
-        float x = in ? a[c] : 0.f;
-        if (in && s.scaled)
-            x = ldexpf(x, ea[(long long)c * s.Mc + r]);
-        const typename H::T hi = H::rn(x);
-        As[(NH * c) * plane + i] = hi;
-        if (NH == 2)
-            As[(NH * c + 1) * plane + i] = H::rn(x - H::f(hi));
+            for (int c = 0; c < 3; c++)
+                mx[c] = max(mx[c], __float_as_uint(a[3 * k + c]) & 0x7fffffffu);
+        }
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            mx[c] = __reduce_max_sync(0xffffffffu, mx[c]);
+            if (lane == 0)
+                red[c][w] = mx[c];
+        }
+        __syncthreads();
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            unsigned v = 0;
+            for (int i = 0; i < 8; i++)
+                v = max(v, red[c][i]);
+            e[c] = scale_exp(v);
+        }
+        if (t < 3)
+            ea[(long long)t * s.M + m] = e[t];
+    }
+    unsigned *dst = (unsigned *)(As + (size_t)m * s.Kp);      /* pairs of 16-bit elements */
+    for (int k = 2 * t; k < s.Kp; k += 512) {
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            float x0 = live && k < s.K ? a[3 * k + c] : 0.f;
+            float x1 = live && k + 1 < s.K ? a[3 * k + 3 + c] : 0.f;
+            if (s.scaled) {
+                x0 = ldexpf(x0, e[c]);
+                x1 = ldexpf(x1, e[c]);
+            }
+            const typename H::T h0 = H::rn(x0), h1 = H::rn(x1);
+            dst[(NH * c) * plane / 2 + k / 2] = H::bits(h0) | (H::bits(h1) << 16);
+            if (NH == 2)
+                dst[(NH * c + 1) * plane / 2 + k / 2] =
+                    H::bits(H::rn(x0 - H::f(h0))) | (H::bits(H::rn(x1 - H::f(h1))) << 16);
+        }
     }
 }
 
@@ -677,7 +792,7 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_fn()
     return fn;
 }
 
-/* rows x Kp 16-bit matrix, box TK x box_rows, 128-byte swizzle */
+/* rows x Kp 16-bit matrix, box TK x box_rows, SWZ-byte swizzle */
 bool make_map(CUtensorMap *m, const void *base, uint64_t rows, uint64_t kp, uint32_t box_rows, bool bf16)
 {
     auto fn = encode_fn();
@@ -689,7 +804,7 @@ bool make_map(CUtensorMap *m, const void *base, uint64_t rows, uint64_t kp, uint
     cuuint32_t estr[2] = {1, 1};
     return fn(m, bf16 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2,
               const_cast<void *>(base), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
-              CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+              SWZ == 128 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
@@ -700,38 +815,72 @@ struct Work {
     size_t size = 0;
 };
 
-template <int NH, bool BF16>
-int run_tc(const float *A, const float *B, Shape s, float *C, cudaStream_t st, unsigned char *ws,
-           const size_t *off, int sms, std::string &err)
+template <int NH, bool BF16, int CL>
+int launch_tc(const CUtensorMap &ma, const CUtensorMap &mb, const Shape &s, float *C, cudaStream_t st,
+              const int *colidx, const int *colflag, const int *ea, const int *eb, int *d_err, int sms,
+              std::string &err)
 {
-    typedef typename Half16<BF16>::T T;
-    int *d_err = (int *)(ws + off[0]);
-    int *rowidx = (int *)(ws + off[3]), *colidx = (int *)(ws + off[4]);
-    int *ea = (int *)(ws + off[5]), *eb = (int *)(ws + off[6]);
-    T *As = (T *)(ws + off[8]), *Bs = (T *)(ws + off[9]);
-    const long long na = (long long)s.Mp * s.Kp;
-    k_split_a<NH, BF16><<<(unsigned)((na + 255) / 256), 256, 0, st>>>(A, As, rowidx, ea, s);
-    k_split_b<NH, BF16><<<dim3((unsigned)(s.Np / 32), (unsigned)(s.Kp / 32)), dim3(32, 8), 0, st>>>(B, Bs, colidx,
-                                                                                                 eb, s);
-    CUtensorMap ma, mb;
-    if (!make_map(&ma, As, (uint64_t)NH * 3 * s.Mp, (uint64_t)s.Kp, TM, BF16) ||
-        !make_map(&mb, Bs, (uint64_t)NH * 3 * s.Np, (uint64_t)s.Kp, TN, BF16)) {
-        err = "cannot encode the TMA tensor maps";
-        return GB_ECUDA;
-    }
     static bool attr_set = false;
     if (!attr_set) {
-        if (cudaFuncSetAttribute(k_dct_tc<NH, BF16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        if (cudaFuncSetAttribute(k_dct_tc<NH, BF16, CL>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  Ring<NH>::SMEM_BYTES) != cudaSuccess) {
             err = "cannot reserve shared memory for the tensor-core kernel";
             return GB_ECUDA;
         }
         attr_set = true;
     }
-    const long long grid = s.tiles < sms ? s.tiles : sms;
-    k_dct_tc<NH, BF16><<<(unsigned)grid, NTHREADS, Ring<NH>::SMEM_BYTES, st>>>(ma, mb, s, C, rowidx, colidx, ea,
-                                                                              eb, d_err);
+    const long long units = s.units;
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute attr[1];
+    cfg.blockDim = dim3(NTHREADS);
+    cfg.dynamicSmemBytes = Ring<NH>::SMEM_BYTES;
+    cfg.stream = st;
+    long long groups = sms / CL;               /* persistent: one CTA per SM */
+    if (CL == 2) {
+        attr[0].id = cudaLaunchAttributeClusterDimension;
+        attr[0].val.clusterDim.x = 2;
+        attr[0].val.clusterDim.y = 1;
+        attr[0].val.clusterDim.z = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        cfg.gridDim = dim3((unsigned)(2 * groups));
+        int active = 0;                        /* clusters the GPCs hold at once */
+        if (cudaOccupancyMaxActiveClusters(&active, k_dct_tc<NH, BF16, CL>, &cfg) == cudaSuccess && active > 0)
+            groups = std::min<long long>(groups, active);
+        cudaGetLastError();
+    }
+    groups = std::min<long long>(groups, units);
+    cfg.gridDim = dim3((unsigned)(CL * groups));
+    if (cudaLaunchKernelEx(&cfg, k_dct_tc<NH, BF16, CL>, ma, mb, s, C, colidx, colflag, ea, eb, d_err) !=
+        cudaSuccess) {
+        err = std::string("tensor-core launch: ") + cudaGetErrorString(cudaGetLastError());
+        return GB_ECUDA;
+    }
     return GB_OK;
+}
+
+template <int NH, bool BF16>
+int run_tc(const float *A, const float *B, Shape s, int cl, float *C, cudaStream_t st, unsigned char *ws,
+           const size_t *off, int sms, std::string &err)
+{
+    typedef typename Half16<BF16>::T T;
+    int *d_err = (int *)(ws + off[0]);
+    int *colidx = (int *)(ws + off[2]), *colflag = (int *)(ws + off[5]);
+    int *ea = (int *)(ws + off[3]), *eb = (int *)(ws + off[4]);
+    T *As = (T *)(ws + off[6]), *Bs = (T *)(ws + off[7]);
+    k_split_rows<NH, BF16><<<(unsigned)s.Mp, 256, 0, st>>>(A, As, ea, s);
+    k_split_b<NH, BF16><<<dim3((unsigned)(s.Np / 32), (unsigned)(s.Kp / 32)), dim3(32, 8), 0, st>>>(B, Bs, colidx,
+                                                                                                 eb, s);
+    /* with clusters of two each CTA copies one half (TN / 2 rows) of a B tile */
+    CUtensorMap ma, mb;
+    if (!make_map(&ma, As, (uint64_t)NH * 3 * s.Mp, (uint64_t)s.Kp, TM, BF16) ||
+        !make_map(&mb, Bs, (uint64_t)NH * 3 * s.Np, (uint64_t)s.Kp, cl == 2 ? TN / 2 : TN, BF16)) {
+        err = "cannot encode the TMA tensor maps";
+        return GB_ECUDA;
+    }
+    if (cl == 2)
+        return launch_tc<NH, BF16, 2>(ma, mb, s, C, st, colidx, colflag, ea, eb, d_err, sms, err);
+    return launch_tc<NH, BF16, 1>(ma, mb, s, C, st, colidx, colflag, ea, eb, d_err, sms, err);
 }
 
 }  // namespace
@@ -746,24 +895,22 @@ int gb_dct_tc(const float *A, const float *B, int64_t M, int64_t K, int64_t N, i
     }
     const int NH = mode == GB_DCT_FP16 ? 1 : 2;
     const bool scaled = mode != GB_DCT_BF16X3;
-    const int64_t Mp_max = rnd(M, TM), Np_max = rnd(N, TN), Kp = rnd(K, TK);
-    /* workspace layout: [0] error flag + counts, [1] row max, [2] column
-     * max, [3] row list, [4] column list, [5] row exponents, [6] column
-     * exponents, [7] row and column flags, [8] A planes, [9] B planes */
+    const int64_t Mp_max = rnd(M, 2 * TM), Np_max = rnd(N, TN), Kp = rnd(K, TK);
+    /* workspace layout: [0] error flag + column count, [1] column max, [2]
+     * column list, [3] row exponents, [4] column exponents, [5] column
+     * flags, [6] A planes, [7] B planes */
     auto up = [](size_t b) { return (b + 255) & ~(size_t)255; };
-    size_t off[11];
+    size_t off[9];
     off[0] = 0;
     off[1] = 256;
-    off[2] = off[1] + up((size_t)M * 3 * 4);
-    off[3] = off[2] + up((size_t)N * 3 * 4);
-    off[4] = off[3] + up((size_t)M * 4);
-    off[5] = off[4] + up((size_t)N * 4);
-    off[6] = off[5] + up((size_t)M * 3 * 4);
-    off[7] = off[6] + up((size_t)N * 3 * 4);
-    off[8] = off[7] + up((size_t)(M + N) * 4);
-    off[9] = off[8] + up((size_t)NH * 3 * Mp_max * Kp * 2);
-    off[10] = off[9] + up((size_t)NH * 3 * Np_max * Kp * 2);
-    const size_t total = off[10];
+    off[2] = off[1] + up((size_t)N * 3 * 4);
+    off[3] = off[2] + up((size_t)N * 4);
+    off[4] = off[3] + up((size_t)M * 3 * 4);
+    off[5] = off[4] + up((size_t)N * 3 * 4);
+    off[6] = off[5] + up((size_t)N * 4);
+    off[7] = off[6] + up((size_t)NH * 3 * Mp_max * Kp * 2);
+    off[8] = off[7] + up((size_t)NH * 3 * Np_max * Kp * 2);
+    const size_t total = off[8];
     static std::mutex lock;
     static Work work[64];
     static int sms_of[64];
@@ -793,53 +940,55 @@ int gb_dct_tc(const float *A, const float *B, int64_t M, int64_t K, int64_t N, i
         cudaDeviceGetAttribute(&sms_of[dev], cudaDevAttrMultiProcessorCount, dev);
     unsigned char *ws = w.p;
     int *d_err = (int *)ws, *d_cnt = d_err + 1;
-    unsigned *rowmax = (unsigned *)(ws + off[1]), *colmax = (unsigned *)(ws + off[2]);
-    int *rowidx = (int *)(ws + off[3]), *colidx = (int *)(ws + off[4]);
-    int *ea = (int *)(ws + off[5]), *eb = (int *)(ws + off[6]);
-    int *rowflag = (int *)(ws + off[7]), *colflag = rowflag + M;
+    unsigned *colmax = (unsigned *)(ws + off[1]);
+    int *colidx = (int *)(ws + off[2]), *eb = (int *)(ws + off[4]), *colflag = (int *)(ws + off[5]);
 
     auto cuda_fail = [&](const char *what) {
         err = std::string(what) + ": " + cudaGetErrorString(cudaGetLastError());
         cudaStreamSynchronize(st);
         return GB_ECUDA;
     };
-    /* zero rows and columns, scales, and the lists of the others */
+    /* zero columns of B, column scales, and the list of the others; rows of
+     * A are not compacted (a zero row's products are zeros) */
     if (cudaMemsetAsync(ws, 0, 256, st) != cudaSuccess ||
         cudaMemsetAsync(colmax, 0, (size_t)N * 3 * 4, st) != cudaSuccess ||
         cudaMemsetAsync(colflag, 0, (size_t)N * 4, st) != cudaSuccess)
         return cuda_fail("memset");
-    k_row_scan<<<(unsigned)((M * 32LL + 255) / 256), 256, 0, st>>>(A, (int)M, (int)K, rowmax, rowflag);
     const int kspan = 64;
     k_col_scan<<<dim3((unsigned)((3 * N + 255) / 256), (unsigned)((K + kspan - 1) / kspan)), 256, 0, st>>>(
         B, (int)K, (int)N, kspan, colmax, colflag);
-    k_compact<<<1, 1024, 0, st>>>(rowflag, (int)M, scaled ? rowmax : nullptr, rowidx, ea, d_cnt);
-    k_compact<<<1, 1024, 0, st>>>(colflag, (int)N, scaled ? colmax : nullptr, colidx, eb, d_cnt + 1);
-    {
-        const int gx = (int)std::min<int64_t>((N + 255) / 256, 64);
-        const int gy = (int)std::min<int64_t>(M, std::max(1, 8 * sms_of[dev] / gx));
-        k_zero_fill<<<dim3((unsigned)gx, (unsigned)gy), 256, 0, st>>>(C, rowflag, colflag, (int)M, (int)N);
-    }
-    int cnt[2] = {0, 0};
+    k_compact<<<1, 1024, 0, st>>>(colflag, (int)N, scaled ? colmax : nullptr, colidx, eb, d_cnt);
+    int nc = 0;
     if (cudaGetLastError() != cudaSuccess ||
-        cudaMemcpyAsync(cnt, d_cnt, sizeof cnt, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaMemcpyAsync(&nc, d_cnt, sizeof nc, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
         cudaStreamSynchronize(st) != cudaSuccess)
-        return cuda_fail("scan of zero rows and columns");
-    if (cnt[0] == 0 || cnt[1] == 0)
+        return cuda_fail("scan of zero columns");
+    if (nc == 0) {                             /* every column of B is zero */
+        if (cudaMemsetAsync(C, 0, (size_t)M * N * 3 * 4, st) != cudaSuccess)
+            return cuda_fail("memset");
         return GB_OK;
+    }
 
     Shape s;
     s.M = (int)M;
     s.K = (int)K;
     s.N = (int)N;
-    s.Mc = cnt[0];
-    s.Nc = cnt[1];
-    s.Mp = (int)rnd(s.Mc, TM);
+    s.Nc = nc;
+    /* two row tiles share each B tile in clusters of two CTAs (rows padded
+     * to a pair of tiles); a single row tile runs alone */
+    int cl = rnd(M, TM) >= 2 * TM ? 2 : 1;
+    if (const char *e = getenv("GB_DCT_CLUSTER"))
+        if (atoi(e) == 1)
+            cl = 1;
+    s.Mp = (int)rnd(M, cl * TM);
     s.Kp = (int)Kp;
     s.Np = (int)rnd(s.Nc, TN);
     s.mt = s.Mp / TM;
     s.nt = s.Np / TN;
     s.kb = s.Kp / TK;
     s.tiles = (long long)s.mt * s.nt * 3;
+    s.mu = s.mt / cl;
+    s.units = (long long)s.mu * s.nt * 3;
     s.scaled = scaled;
     s.wait_ns = WAIT_NS;
     if (const char *w = getenv("GB_DCT_WAIT_NS")) {
@@ -849,11 +998,11 @@ int gb_dct_tc(const float *A, const float *B, int64_t M, int64_t K, int64_t N, i
     }
     int rc;
     if (mode == GB_DCT_BF16X3)
-        rc = run_tc<2, true>(A, B, s, C, st, ws, off, sms_of[dev], err);
+        rc = run_tc<2, true>(A, B, s, cl, C, st, ws, off, sms_of[dev], err);
     else if (mode == GB_DCT_FP16X3)
-        rc = run_tc<2, false>(A, B, s, C, st, ws, off, sms_of[dev], err);
+        rc = run_tc<2, false>(A, B, s, cl, C, st, ws, off, sms_of[dev], err);
     else
-        rc = run_tc<1, false>(A, B, s, C, st, ws, off, sms_of[dev], err);
+        rc = run_tc<1, false>(A, B, s, cl, C, st, ws, off, sms_of[dev], err);
     if (rc < 0) {
         cudaStreamSynchronize(st);
         return rc;

@@ -111,6 +111,29 @@ def test_wide_dynamic_range_rows(gb):
     assert rel.max() <= 1e-5, rel.max()
 
 
+@pytest.mark.parametrize("mode", ["fp16x3", "fp16"])
+def test_clusters_of_two_equal_single_ctas(gb, mode):
+    """Row tiles paired in clusters of two CTAs, each copying half of the
+    shared column tile into both, give the same bits as one CTA per tile
+    (GB_DCT_CLUSTER=1); a single row tile (M <= 128) runs without
+    clusters and meets the same bounds."""
+    dc, sky, ref = dc_pair(np.random.default_rng(5), 700, 500, 900)
+    pair = gb.dctimestep_array(dc, sky, mode=mode)
+    os.environ["GB_DCT_CLUSTER"] = "1"
+    try:
+        single = gb.dctimestep_array(dc, sky, mode=mode)
+    finally:
+        del os.environ["GB_DCT_CLUSTER"]
+    np.testing.assert_array_equal(pair, single)
+    dc, sky, ref = dc_pair(np.random.default_rng(6), 100, 500, 900)
+    out = gb.dctimestep_array(dc, sky, mode=mode)
+    nz = ref != 0
+    np.testing.assert_array_equal(out[~nz], 0.0)
+    rel = np.abs(out[nz] - ref[nz]) / np.abs(ref[nz])
+    mx, mean = BOUNDS[mode]
+    assert rel.max() <= mx and rel.mean() <= mean, (rel.max(), rel.mean())
+
+
 def test_pipeline_wait_limit_returns_error(gb):
     """A pipeline wait limit of 1 ns (GB_DCT_WAIT_NS) makes the first wait
     that is not met at once run out: the kernel records the error, drains
