@@ -1,5 +1,5 @@
 # Builds the reference Radiance programs that pin the oracle: rtrace, rcontrib,
-# oconv, dctimestep, rfluxmtx and rmtxop, compiled straight from the reference's own C sources
+# oconv, obj2mesh, dctimestep, rfluxmtx and rmtxop, compiled straight from the reference's own C sources
 # (read in place, never copied) with the reference's release flags.
 #
 #   make -f oracle/build_ref.mk REF=/root/reference -j8
@@ -48,7 +48,7 @@ LIBRL    := $(OBJ)/libraycalls.a
 CALS := $(RAD)/rt/rayinit.cal $(RAD)/util/reinhartb.cal $(RAD)/util/klems_full.cal $(RAD)/util/klems_half.cal \
         $(RAD)/util/klems_quarter.cal $(RAD)/util/disk2square.cal
 
-all: $(OUT)/bin/rtrace $(OUT)/bin/rcontrib $(OUT)/bin/oconv $(OUT)/bin/dctimestep $(OUT)/bin/rfluxmtx $(OUT)/bin/rmtxop
+all: $(OUT)/bin/rtrace $(OUT)/bin/rcontrib $(OUT)/bin/oconv $(OUT)/bin/obj2mesh $(OUT)/bin/dctimestep $(OUT)/bin/rfluxmtx $(OUT)/bin/rmtxop
 	@mkdir -p $(OUT)/lib && cp $(CALS) $(OUT)/lib/
 
 $(OBJ)/common/%.o: $(RAD)/common/%.c
@@ -81,6 +81,9 @@ $(OUT)/bin/rcontrib: $(addprefix $(OBJ)/rt/,rcmain.o rcontrib.o rc2.o rc3.o) $(L
 	@mkdir -p $(@D)
 	$(CXX) -o $@ $^ -lm
 $(OUT)/bin/oconv: $(addprefix $(OBJ)/ot/,bbox.o initotypes.o o_cone.o o_face.o o_instance.o oconv.o sphere.o writeoct.o) $(LIBRTRAD)
+	@mkdir -p $(@D)
+	$(CXX) -o $@ $^ -lm
+$(OUT)/bin/obj2mesh: $(addprefix $(OBJ)/ot/,cvmesh.o o_face.o obj2mesh.o wfconv.o writemesh.o) $(LIBRTRAD)
 	@mkdir -p $(@D)
 	$(CXX) -o $@ $^ -lm
 $(OUT)/bin/rmtxop: $(addprefix $(OBJ)/util/,rmtxop.o rmatrix.o cmconst.o cmbsdf.o cmatrix.o rmconvert.o) $(LIBRTRAD)

@@ -737,7 +737,7 @@ static int object_hit(const oscene *O, int o, RAY *r)
     case GT_POLYGON: return o_face(O, o, r);
     case GT_SPHERE: case GT_BUBBLE: return o_sphere(O, o, r);
     case GT_CONE: case GT_CUP: case GT_CYLINDER: case GT_TUBE: case GT_RING: return o_cone(O, o, r);
-    case GT_INSTANCE: return o_instance(O, o, r);
+    case GT_INSTANCE: case GT_MESH: return o_instance(O, o, r);
     default: return 0;
     }
 }

@@ -610,6 +610,7 @@ static int build_arrays(gb_scene *G)
             kind = DK_SOURCE;
             break;
         case GT_INSTANCE:
+        case GT_MESH:                                  /* an instance of its triangles (scene.c) */
             for (int k = 0; k < H.ninst; k++)
                 if (H.inst[k].obj == i) {
                     kind = DK_INSTANCE;

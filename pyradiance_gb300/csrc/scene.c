@@ -1143,6 +1143,275 @@ static int merge_subscene(gb_scene_host *S, gb_scene_host *T, const char *name)
     return S->nsubs++;
 }
 
+/* ------------------------------------------------------------------ meshes */
+
+/* One patch of a compiled mesh (common/readmesh.c:139-253 getpatch): up to
+ * 256 vertices as 32-bit positions in the mesh's cube, local triangles,
+ * triangles joining one or two vertices of other patches. */
+typedef struct {
+    uint32_t (*xyz)[3];
+    int nverts, ntris, nj1, nj2;
+    unsigned char (*tri)[3];
+    int16_t *trimat, solemat;
+    int32_t (*j1v)[2];           /* non-local vertex id; local vertices packed as v2 | v3 << 8 */
+    int16_t *j1mat;
+    int32_t (*j2v)[3];           /* two non-local vertex ids, local vertex */
+    int16_t *j2mat;
+} mpatch;
+
+static void mpatch_free(mpatch *pp, int n)
+{
+    int i;
+    for (i = 0; i < n; i++) {
+        free(pp[i].xyz);
+        free(pp[i].tri);
+        free(pp[i].trimat);
+        free(pp[i].j1v);
+        free(pp[i].j1mat);
+        free(pp[i].j2v);
+        free(pp[i].j2mat);
+    }
+    free(pp);
+}
+
+static int read_patch(rdr *R, mpatch *pp, const char *path)
+{
+    int ok = 1, i, j;
+    long flags = r_int(R, 1, &ok), n;
+    if (!ok || !(flags & 1) || (flags & ~7L))
+        return fail("(%s): bad patch flags", path);
+    if (flags & 2)
+        return fail("(%s): mesh vertex normals are not supported", path);
+    pp->nverts = (int)r_int(R, 2, &ok);
+    if (!ok || pp->nverts <= 0 || pp->nverts > 256)
+        return fail("(%s): bad number of patch vertices", path);
+    pp->xyz = (uint32_t(*)[3])malloc((size_t)pp->nverts * sizeof *pp->xyz);
+    if (!pp->xyz)
+        return fail("out of memory");
+    for (i = 0; i < pp->nverts; i++)
+        for (j = 0; j < 3; j++)
+            pp->xyz[i][j] = (uint32_t)r_int(R, 4, &ok);
+    if (flags & 4)                               /* (u,v): read past, unused */
+        for (i = 0; i < 2 * pp->nverts; i++)
+            r_int(R, 4, &ok);
+    pp->ntris = (int)r_int(R, 2, &ok);
+    if (!ok || pp->ntris < 0 || pp->ntris > 512)
+        return fail("(%s): bad number of local triangles", path);
+    pp->tri = (unsigned char(*)[3])malloc(((size_t)pp->ntris + 1) * sizeof *pp->tri);
+    if (!pp->tri)
+        return fail("out of memory");
+    for (i = 0; i < pp->ntris; i++)
+        for (j = 0; j < 3; j++)
+            pp->tri[i][j] = (unsigned char)r_int(R, 1, &ok);
+    n = r_int(R, 2, &ok);
+    if (n > 1) {
+        pp->trimat = (int16_t *)malloc(((size_t)pp->ntris + 1) * sizeof(int16_t));
+        if (!pp->trimat)
+            return fail("out of memory");
+        for (i = 0; i < pp->ntris; i++)
+            pp->trimat[i] = (int16_t)r_int(R, 2, &ok);
+    } else
+        pp->solemat = (int16_t)r_int(R, 2, &ok);
+    pp->nj1 = (int)r_int(R, 2, &ok);
+    if (!ok || pp->nj1 < 0 || pp->nj1 > 256)
+        return fail("(%s): bad number of joiner triangles", path);
+    pp->j1v = (int32_t(*)[2])malloc(((size_t)pp->nj1 + 1) * sizeof *pp->j1v);
+    pp->j1mat = (int16_t *)malloc(((size_t)pp->nj1 + 1) * sizeof(int16_t));
+    if (!pp->j1v || !pp->j1mat)
+        return fail("out of memory");
+    for (i = 0; i < pp->nj1; i++) {
+        int v2, v3;
+        pp->j1v[i][0] = (int32_t)r_int(R, 4, &ok);
+        v2 = (int)r_int(R, 1, &ok) & 0xff;
+        v3 = (int)r_int(R, 1, &ok) & 0xff;
+        pp->j1v[i][1] = v2 | v3 << 8;
+        pp->j1mat[i] = (int16_t)r_int(R, 2, &ok);
+    }
+    pp->nj2 = (int)r_int(R, 2, &ok);
+    if (!ok || pp->nj2 < 0 || pp->nj2 > 256)
+        return fail("(%s): bad number of double joiner triangles", path);
+    pp->j2v = (int32_t(*)[3])malloc(((size_t)pp->nj2 + 1) * sizeof *pp->j2v);
+    pp->j2mat = (int16_t *)malloc(((size_t)pp->nj2 + 1) * sizeof(int16_t));
+    if (!pp->j2v || !pp->j2mat)
+        return fail("out of memory");
+    for (i = 0; i < pp->nj2; i++) {
+        pp->j2v[i][0] = (int32_t)r_int(R, 4, &ok);
+        pp->j2v[i][1] = (int32_t)r_int(R, 4, &ok);
+        pp->j2v[i][2] = (int32_t)r_int(R, 1, &ok) & 0xff;
+        pp->j2mat[i] = (int16_t)r_int(R, 2, &ok);
+    }
+    return ok ? 0 : fail("(%s): truncated mesh file", path);
+}
+
+/* vertex id (patch << 8 | index) -> position (common/mesh.c:236-279
+ * getmeshvert: the 32-bit cube coordinates at their cells' centres) */
+static int mesh_vertex(const mpatch *pp, int npatches, const double org[3], double size, int32_t vid, double *v)
+{
+    int pn = vid >> 8, k;
+    double res = size * (1. / 4294967296.);
+    if (vid < 0 || pn >= npatches || (vid & 0xff) >= pp[pn].nverts)
+        return 0;
+    for (k = 0; k < 3; k++)
+        v[k] = org[k] + (pp[pn].xyz[vid & 0xff][k] + .5) * res;
+    return 1;
+}
+
+/* A compiled mesh file (common/readmesh.c:256-328 readmesh, format written
+ * by ot/writemesh.c) as a sub-scene T: the mesh's cube and octree, its
+ * materials, then each triangle as a three-vertex polygon whose modifier is
+ * the triangle's material, named "M-Tri" as the pseudo object that stands
+ * for the triangle in a hit on a mesh without its own modifier
+ * (rt/o_mesh.c:186-190, common/mesh.c:281-300 getmeshpseudo).  Triangle ids in the octree's sets (patch << 10 |
+ * local index, 0x200 joiners, 0x100 of those joining two patches:
+ * common/mesh.c:174-233 getmeshtrivid) become the polygons' indices, in
+ * the same order. */
+static int read_mesh(gb_scene_host *T, const char *path, const char *mesh_name)
+{
+    size_t len = 0;
+    char *buf = slurp(path, &len);
+    rdr R;
+    int ok = 1, objsize, i, k, np = 0;
+    mpatch *pp = NULL;
+    int32_t *map = NULL, nmats, ntri = 0, t;
+    char line[256];
+    int rc = -1;
+    if (!buf)
+        return fail("cannot open mesh file \"%s\"", path);
+    R.p = (const unsigned char *)buf;
+    R.end = R.p + len;
+    for (;;) {                                   /* information header */
+        size_t n = 0;
+        while (R.p < R.end && *R.p != '\n') {
+            if (n + 1 < sizeof line)
+                line[n++] = (char)*R.p;
+            R.p++;
+        }
+        if (R.p >= R.end) {
+            fail("(%s): not a compiled mesh", path);
+            goto done;
+        }
+        R.p++;
+        line[n] = '\0';
+        if (!n)
+            break;
+        if (!strncmp(line, "FORMAT=", 7) && strcmp(line + 7, "Radiance_tmesh")) {
+            fail("(%s): not a compiled mesh", path);
+            goto done;
+        }
+    }
+    objsize = (int)(r_int(&R, 2, &ok) - (1 * 8 + 311));
+    if (!ok || objsize <= 0 || objsize > 8) {
+        fail("(%s): incompatible mesh format", path);
+        goto done;
+    }
+    for (i = 0; i < 3; i++)
+        T->cuorg[i] = atof(r_str(&R, &ok));
+    T->cusize = atof(r_str(&R, &ok));
+    for (i = 0; i < 4; i++)                      /* (u,v) limits */
+        r_flt(&R, &ok);
+    T->root = read_tree(T, &R, objsize, 0, &ok, 0);
+    if (!ok) {
+        fail("(%s): truncated or damaged mesh octree", path);
+        goto done;
+    }
+    if (read_frozen(T, &R, objsize, 0) < 0)
+        goto done;
+    nmats = T->nobjs;
+    np = (int)r_int(&R, 4, &ok);
+    if (!ok || np < 0 || np > (1 << 21)) {
+        fail("(%s): bad patch count", path);
+        goto done;
+    }
+    pp = (mpatch *)calloc((size_t)np + 1, sizeof *pp);
+    map = (int32_t *)malloc(((size_t)np + 1) * 1024 * sizeof(int32_t));
+    if (!pp || !map) {
+        fail("out of memory");
+        goto done;
+    }
+    for (i = 0; i < np; i++)
+        if (read_patch(&R, &pp[i], path) < 0)
+            goto done;
+    for (i = 0; i < np * 1024; i++)
+        map[i] = -1;
+    for (i = 0; i < np; i++) {
+        for (t = 0; t < 1024; t++) {
+            int32_t v[3], m;
+            double xyz[9];
+            gb_object *o;
+            if (!(t & 0x200)) {                  /* local triangle */
+                if (t >= pp[i].ntris)
+                    continue;
+                for (k = 0; k < 3; k++)
+                    v[k] = i << 8 | pp[i].tri[t][k];
+                m = pp[i].trimat ? pp[i].trimat[t] : pp[i].solemat;
+            } else if (!(t & 0x100)) {           /* joins one other patch's vertex */
+                int j = t & 0xff;
+                if (j >= pp[i].nj1)
+                    continue;
+                v[0] = pp[i].j1v[j][0];
+                v[1] = i << 8 | (pp[i].j1v[j][1] & 0xff);
+                v[2] = i << 8 | (pp[i].j1v[j][1] >> 8);
+                m = pp[i].j1mat[j];
+            } else {                             /* joins two */
+                int j = t & 0xff;
+                if (j >= pp[i].nj2)
+                    continue;
+                v[0] = pp[i].j2v[j][0];
+                v[1] = pp[i].j2v[j][1];
+                v[2] = i << 8 | pp[i].j2v[j][2];
+                m = pp[i].j2mat[j];
+            }
+            for (k = 0; k < 3; k++)
+                if (!mesh_vertex(pp, np, T->cuorg, T->cusize, v[k], xyz + 3 * k)) {
+                    fail("(%s): missing mesh vertex", path);
+                    goto done;
+                }
+            if (m != -1 && (m < 0 || m >= nmats)) {
+                fail("(%s): bad triangle material", path);
+                goto done;
+            }
+            o = new_object(T);
+            if (!o) {
+                fail("out of memory");
+                goto done;
+            }
+            o->otype = GT_POLYGON;
+            o->omod = m;
+            o->name = strdup(m >= 0 ? "M-Tri" : mesh_name);
+            o->nsargs = 0;
+            o->sarg = NULL;
+            o->nfargs = 9;
+            o->farg = (double *)malloc(9 * sizeof(double));
+            if (!o->name || !o->farg) {
+                fail("out of memory");
+                goto done;
+            }
+            memcpy(o->farg, xyz, sizeof xyz);
+            map[i * 1024 + t] = ntri++;
+        }
+    }
+    /* set members: triangle ids -> polygon objects (the map is increasing,
+     * so the sets stay sorted) */
+    for (i = 0; i < T->nsets; i++) {
+        int32_t *st = T->set_data + T->set_off[i];
+        for (k = 1; k <= st[0]; k++) {
+            int32_t id = st[k];
+            if (id < 0 || (id >> 10) >= np || map[id] < 0) {
+                fail("(%s): octree names a missing triangle", path);
+                goto done;
+            }
+            st[k] = nmats + map[id];
+        }
+    }
+    rc = 0;
+done:
+    if (pp)
+        mpatch_free(pp, np);
+    free(map);
+    free(buf);
+    return rc;
+}
+
 int gb_scene_load_instances(gb_scene_host *S, const char *base_dir)
 {
     int32_t i, ntop = S->nobjs;
@@ -1151,9 +1420,10 @@ int gb_scene_load_instances(gb_scene_host *S, const char *base_dir)
         gb_object *o = &S->objs[i];
         gb_instance *ni;
         int sub = -1, k;
-        if (o->otype == GT_MESH)
-            return fail("%s: mesh objects are not supported", o->name);
-        if (o->otype != GT_INSTANCE)
+        /* a mesh (rt/o_mesh.c) is an instance of the sub-scene of its
+         * triangles (read_mesh) */
+        const int is_mesh = o->otype == GT_MESH;
+        if (o->otype != GT_INSTANCE && !is_mesh)
             continue;
         if (o->nsargs < 1)
             return fail("%s: bad # of arguments", o->name);
@@ -1186,12 +1456,13 @@ int gb_scene_load_instances(gb_scene_host *S, const char *base_dir)
                 path = alt;
             }
             gb_scene_init(&T);
-            if (gb_scene_read_oct(&T, path) < 0) {
+            if ((is_mesh ? read_mesh(&T, path, S->objs[i].name) : gb_scene_read_oct(&T, path)) < 0) {
                 char why[256];
                 snprintf(why, sizeof why, "%s", gb_scene_error());
                 free(alt);
                 gb_scene_clear(&T);
-                return fail("%s: cannot load octree \"%s\": %s", S->objs[i].name, S->objs[i].sarg[0], why);
+                return fail("%s: cannot load %s \"%s\": %s", S->objs[i].name, is_mesh ? "mesh" : "octree",
+                            S->objs[i].sarg[0], why);
             }
             free(alt);
             for (j = 0; j < T.nobjs; j++)

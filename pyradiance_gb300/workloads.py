@@ -433,6 +433,73 @@ def instance_room(sub_octree: str, seed: int = 0, n: int = 12) -> str:
     return "".join(out)
 
 
+def mesh_obj(nu: int = 24, nv: int = 12, nsheet: int = 16, seed: int = 0) -> str:
+    """A Wavefront OBJ for obj2mesh, in its own coordinates around the
+    origin: a UV sphere of radius 0.45 centred 0.45 above the origin
+    (material ``mesh_red``) and a bumpy square sheet of side 1.2 at height
+    0.9 .. 1.0 (``mesh_grey``), triangles only, no vertex normals."""
+    rng = np.random.default_rng(seed)
+    V, out = [], []
+    for j in range(nv + 1):
+        th = np.pi * j / nv
+        for i in range(nu):
+            ph = 2 * np.pi * i / nu
+            V.append((0.45 * np.sin(th) * np.cos(ph), 0.45 * np.sin(th) * np.sin(ph), 0.45 + 0.45 * np.cos(th)))
+    out.append("usemtl mesh_red")
+    for j in range(nv):
+        for i in range(nu):
+            a, b = j * nu + i % nu + 1, j * nu + (i + 1) % nu + 1
+            c, d = (j + 1) * nu + (i + 1) % nu + 1, (j + 1) * nu + i % nu + 1
+            if j > 0:
+                out.append(f"f {a} {c} {b}")
+            if j < nv - 1:
+                out.append(f"f {a} {d} {c}")
+    base = len(V)
+    h = rng.uniform(0.9, 1.0, size=(nsheet + 1, nsheet + 1))
+    for j in range(nsheet + 1):
+        for i in range(nsheet + 1):
+            V.append((-0.6 + 1.2 * i / nsheet, -0.6 + 1.2 * j / nsheet, h[j, i]))
+    out.append("usemtl mesh_grey")
+    for j in range(nsheet):
+        for i in range(nsheet):
+            a = base + j * (nsheet + 1) + i + 1
+            b, c, d = a + 1, a + nsheet + 2, a + nsheet + 1
+            out += [f"f {a} {b} {c}", f"f {a} {c} {d}"]
+    return "".join(f"v {x:.7f} {y:.7f} {z:.7f}\n" for x, y, z in V) + "\n".join(out) + "\n"
+
+
+def mesh_materials() -> str:
+    """The materials ``mesh_obj``'s triangles name (obj2mesh -a)."""
+    return (_mat_plastic("mesh_red", (0.7, 0.25, 0.2)) +
+            "void plastic mesh_grey\n0\n0\n5 0.5 0.5 0.5 0.03 0.05\n\n")
+
+
+def mesh_room(mesh_file: str, seed: int = 0, n: int = 10) -> str:
+    """The room shell and ceiling light of ``instance_room`` with ``n``
+    placements of the compiled mesh ``mesh_file`` on the floor: rotated
+    about z, some scaled, one mirrored; every third one with its own
+    material (which replaces the mesh's), the others with the mesh's."""
+    rng = np.random.default_rng(seed)
+    X, Y, Z = ROOM
+    out = [_mat_plastic("room_mat", (0.5, 0.5, 0.5)), _room_shell("room_mat"),
+           _mat_plastic("override", (0.3, 0.6, 0.3))]
+    for i in range(n):
+        x, y = rng.uniform((1.2, 1.2), (X - 1.2, Y - 1.2))
+        args = ["-rz", f"{rng.uniform(0, 360):.6g}"]
+        if i % 4 == 1:
+            args += ["-s", f"{rng.uniform(0.6, 1.4):.6g}"]
+        if i == 2:
+            args += ["-mx"]
+        args += ["-t", f"{x:.6g}", f"{y:.6g}", "0.002"]
+        mod = "override" if i % 3 == 0 else "void"
+        out.append(f"{mod} mesh mesh{i}\n{1 + len(args)} {mesh_file} {' '.join(args)}\n0\n0\n\n")
+    out.append("void light light_mat\n0\n0\n3 100 100 100\n\n")
+    cx, cy = X / 2, Y / 2
+    out.append(_poly("light_mat", "light", [(cx - .5, cy - .5, Z - 0.01), (cx - .5, cy + .5, Z - 0.01),
+                                            (cx + .5, cy + .5, Z - 0.01), (cx + .5, cy - .5, Z - 0.01)]))
+    return "".join(out)
+
+
 def shape_zoo(seed: int = 0, n: int = 40) -> str:
     """Room with every primitive type the intersectors handle: spheres,
     bubbles, cones, cups, cylinders, tubes, rings and polygons, gray plastic

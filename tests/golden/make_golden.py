@@ -420,6 +420,48 @@ def instances(tmp: Path) -> None:
         len(hit)))
 
 
+def meshes(tmp: Path) -> None:
+    """Compiled meshes (rt/o_mesh.c, common/mesh.c, common/readmesh.c): a
+    sphere and a bumpy sheet of triangles with two materials, compiled by
+    the reference obj2mesh, placed 10 times in the room, rotated, scaled,
+    mirrored, some with their own material.  The mesh file and the room's
+    octree (frozen, by the reference oconv; it names the mesh by its file
+    name) are kept beside the vectors.  Random interior rays: first-hit
+    surfaces and distances, deterministic -ab 0 radiance and -I
+    irradiance."""
+    (tmp / "mesh.obj").write_text(w.mesh_obj())
+    (tmp / "mesh_mat.rad").write_text(w.mesh_materials())
+    run(["obj2mesh", "-a", "mesh_mat.rad", "mesh.obj", "mesh_parts.rtm"], b"", cwd=tmp)
+    (tmp / "mesh_room.rad").write_text(w.mesh_room("mesh_parts.rtm"))
+    (tmp / "mesh_room.oct").write_bytes(run(["oconv", "-f", "mesh_room.rad"], b"", cwd=tmp))
+    rays = w.random_rays(4000, seed=12)
+    rng = np.random.default_rng(12)                # half of them aimed low, where the meshes stand
+    tgt = rng.uniform((0.5, 0.5, 0.0), (9.5, 7.5, 1.1), size=(2000, 3))
+    d = tgt - rays[:2000, :3]
+    rays[:2000, 3:] = d / np.linalg.norm(d, axis=1, keepdims=True)
+    inp = rays.astype("<f8").tobytes()
+    det = ["-dj", "0", "-ds", "0", "-dr", "0", "-dt", "0"]
+    hit = names(run(["rtrace", "-h", "-u-", "-ab", "0", "-fda", "-os", "mesh_room.oct"], inp, cwd=tmp))
+    dist = np.frombuffer(run(["rtrace", "-h", "-u-", "-ab", "0", "-fdd", "-oL", "mesh_room.oct"], inp, cwd=tmp),
+                         dtype="<f8")
+    val = np.frombuffer(run(["rtrace", "-h", "-u-", "-ab", "0", *det, "-fdd", "-ov", "mesh_room.oct"], inp,
+                            cwd=tmp), dtype="<f8").reshape(-1, 3)
+    irr = np.frombuffer(run(["rtrace", "-h", "-u-", "-I", "-ab", "0", *det, "-fdd", "-ov", "mesh_room.oct"], inp,
+                            cwd=tmp), dtype="<f8").reshape(-1, 3)
+    # a mesh with vertex normals (refused: their shading perturbation is not built)
+    (tmp / "mesh_vn.obj").write_text("v 0 0 0\nv 1 0 0\nv 0 1 0\nvn 0 0 1\nvn 0 0.1 1\nvn 0.1 0 1\n"
+                                     "usemtl mesh_red\nf 1//1 2//2 3//3\n")
+    run(["obj2mesh", "-a", "mesh_mat.rad", "mesh_vn.obj", "mesh_normals.rtm"], b"", cwd=tmp)
+    (tmp / "mesh_normals.rad").write_text("void mesh smooth\n1 mesh_normals.rtm\n0\n0\n")
+    (tmp / "mesh_normals.oct").write_bytes(run(["oconv", "-f", "mesh_normals.rad"], b"", cwd=tmp))
+    for f in ("mesh_parts.rtm", "mesh_room.oct", "mesh_normals.rtm", "mesh_normals.oct"):
+        (OUT / f).write_bytes((tmp / f).read_bytes())
+    np.savez_compressed(OUT / "meshes.npz", rays=rays, hit_name=hit, hit_dist=dist, radiance=val,
+                        irradiance=irr, cmd="rtrace -h -u- -ab 0 -os | -oL | [-I] -dj 0 -ds 0 -dr 0 -dt 0 -ov")
+    print("meshes: %d of %d rays hit mesh triangles" % (
+        sum(n == "M-Tri" or n.startswith("mesh") for n in hit), len(hit)))
+
+
 # bin groups of the 146 columns: ground, then the 8 Reinhart MF:1 altitude rows
 ROW_EDGES = [0, 1, 31, 61, 85, 109, 127, 139, 145, 146]
 
@@ -760,7 +802,7 @@ def main() -> None:
     if not (BIN / "rtrace").exists():
         sys.exit("reference programs missing: make -f oracle/build_ref.mk REF=/root/reference -j8")
     parts = {"octree": octree_digests, "c1": c1_direct, "c1p": c1_partitioned, "zoo": zoo, "glossy": glossy, "irr": surface_irradiance,
-             "ss": supersampled_irradiance, "inst": instances, "circ": circular_sources,
+             "ss": supersampled_irradiance, "inst": instances, "mesh": meshes, "circ": circular_sources,
              "trans": translucent, "bins": general_bins,
              "spot": spotlights, "mirror": mirrors, "flux": flux_matrices, "flux_sc": flux_shirchiu,
              "dct": lambda tmp: dct_small(), "dct4": lambda tmp: dct_four(), "rmtxop": lambda tmp: rmtxop_cases(), "trace_oct": lambda tmp: ref_fixture_trace(),

@@ -589,6 +589,30 @@ def test_instances(gb):
     assert (rel <= 1e-4).mean() >= 0.99, np.sort(rel)[-5:]
 
 
+def test_meshes(gb):
+    """Compiled meshes (rt/o_mesh.c): the reference obj2mesh's mesh 10 times
+    in the room, read from the reference oconv's octree; each mesh is an
+    instance of its triangles.  First hits cast in FP64: every hit name is
+    the reference's (the mesh's, or "M-Tri" for a mesh without its own
+    modifier).  Radiance and irradiance as for the instances."""
+    from pathlib import Path
+    g = golden("meshes.npz")
+    sc = gb.Scene(str(Path(__file__).resolve().parent / "golden" / "mesh_room.oct"))
+    rgb, hid, ht = rtrace_c(gb, sc, opts("rtrace", ab=0, dj=0, ds=0, dr=0, dt=0, u=0), g["rays"])
+    names = names_of(sc, hid)
+    match = names == g["hit_name"]
+    print("meshes: %d of %d hits named alike" % (match.sum(), len(match)))
+    assert match.all(), np.nonzero(~match)
+    ok = g["hit_dist"] < 1e9
+    np.testing.assert_allclose(ht[ok], g["hit_dist"][ok], rtol=1e-6, atol=1e-7)
+    rel = np.abs(rgb - g["radiance"]).max(1) / np.maximum(np.abs(g["radiance"]).max(1), 1e-9)
+    assert (rel <= 1e-4).mean() >= 0.99, np.sort(rel)[-5:]
+    o = opts("rtrace", I=1, ab=0, dj=0, ds=0, dr=0, dt=0, u=0)
+    irr, _, _ = rtrace_c(gb, sc, o, g["rays"])
+    rel = np.abs(irr - g["irradiance"]).max(1) / np.maximum(np.abs(g["irradiance"]).max(1), 1e-9)
+    assert (rel <= 1e-4).mean() >= 0.99, np.sort(rel)[-5:]
+
+
 def test_dctimestep_fp32_fp64(gb):
     g = golden("dct_small.npz")
     r64 = gb.dctimestep_array(g["dc"], g["sky"], mode="fp64")

@@ -317,6 +317,35 @@ def test_instances():
     np.testing.assert_allclose(irr, g["irradiance"], rtol=1e-6, atol=1e-9)
 
 
+def test_meshes():
+    """Compiled meshes (rt/o_mesh.c, common/mesh.c, common/readmesh.c):
+    the reference obj2mesh's mesh of a sphere and a bumpy sheet, 10 times in
+    the room, rotated, scaled, mirrored, some with their own material.  Hit
+    surfaces by name (the mesh's when it has a modifier, else the
+    reference's triangle pseudo object "M-Tri"), distances, -ab 0 radiance
+    and -I irradiance."""
+    g = golden("meshes.npz")
+    sc = po.Scene(Path(__file__).resolve().parent / "golden" / "mesh_room.oct")
+    o = po.default_opts("rtrace", ab=0, dj=0, ds=0, dr=0, dt=0, u=0)
+    rgb, hid, ht, _ = po.rtrace(sc, o, g["rays"], threads=8)
+    names = np.array([sc.object_name(i) if i >= 0 else "*" for i in hid])
+    assert (names == g["hit_name"]).all(), np.nonzero(names != g["hit_name"])
+    assert (names == "M-Tri").sum() > 100 and np.char.startswith(names, "mesh").sum() > 100
+    hit = g["hit_dist"] < 1e9
+    np.testing.assert_allclose(ht[hit], g["hit_dist"][hit], rtol=1e-6, atol=1e-9)
+    np.testing.assert_allclose(rgb, g["radiance"], rtol=1e-6, atol=1e-9)
+    o.I = 1
+    irr, _, _, _ = po.rtrace(sc, o, g["rays"], hits=False, threads=8)
+    np.testing.assert_allclose(irr, g["irradiance"], rtol=1e-6, atol=1e-9)
+
+
+def test_mesh_with_vertex_normals_refused():
+    """A mesh whose vertices carry normals (rt/o_mesh.c:198-206 perturbs the
+    shading normal with them) is refused by the scene reader."""
+    with pytest.raises(RuntimeError, match="normals are not supported"):
+        po.Scene(Path(__file__).resolve().parent / "golden" / "mesh_normals.oct")
+
+
 def test_zoo_cast_and_direct(oscenes):
     g = golden("zoo.npz")
     sc = oscenes["zoo"]
