@@ -21,7 +21,7 @@ import numpy as np
 from . import _lib
 from ._lib import GbError, GbModspec, Scene, check, last_stats, lib, parse_opts, ptr
 
-__all__ = ["rtrace", "Rcontrib", "dctimestep", "rfluxmtx", "rmtxop", "Scene", "load_scene", "read_rays", "GbError", "last_stats"]
+__all__ = ["rtrace", "Rcontrib", "dctimestep", "rfluxmtx", "rmtxop", "Rmtxop", "Scene", "load_scene", "read_rays", "GbError", "last_stats"]
 
 _SCENES: dict = {}
 
@@ -590,7 +590,7 @@ from .rflux import _rfluxmtx  # noqa: E402
 
 rfluxmtx = _wrap(_rfluxmtx)
 
-from .rmtx import _rmtxop  # noqa: E402
+from .rmtx import _rmtxop, Rmtxop  # noqa: E402
 
 rmtxop = _wrap(_rmtxop)
 

@@ -1,11 +1,16 @@
-"""rmtxop's single-matrix operations with pyradiance's signature.
+"""rmtxop with pyradiance's signatures.
 
 ``pyradiance.rmtxop(inp, outform, transpose, scale, transform, reflectance)``
 (src/pyradiance/util.py:873-910) runs util/rmtxop.c on one matrix: an
 optional component transform (``-c``, with the scale folded into it), else a
 scale (``-s``), then a transpose (``-t``), in the order of rmtxop.c:288-381
-(loadop).  These are element-wise passes over a matrix in host memory; the
-products of the daylight chain run on the GPU through ``dctimestep``.
+(loadop).  ``pyradiance.Rmtxop`` (util.py:912-965) chains several matrices,
+each with those operations, by matrix products and element-wise sums,
+products and quotients (rmtxop.c:383-520 binaryop, op_left2right,
+op_right2left).  The element-wise passes run over matrices in host memory,
+held in single precision as util/rmatrix.c holds them; the matrix products
+run on the GPU (the FP64 dctimestep kernel: double sums of single-precision
+products, rounded to single precision, as rmx_multiply computes them).
 """
 from __future__ import annotations
 
@@ -109,3 +114,107 @@ def _rmtxop(inp, outform: str = "a", transpose: bool = False, scale: float | Non
         raise GbError(-3, f"output format '{outform}' is not supported")
     m = rmtxop_array(read_rmatrix(inp), transpose, scale, transform)
     return write_rmatrix(m, outform, "rmtxop")
+
+
+def _product(a: np.ndarray, b: np.ndarray, name: str) -> np.ndarray:
+    """rmx_multiply (util/rmatrix.c:806-838) on the GPU."""
+    from . import dctimestep_array
+    if a.shape[2] != b.shape[2]:
+        raise GbError(-1, f"{name}: # components do not match")
+    if a.shape[1] != b.shape[0]:
+        raise GbError(-1, f"{name}: mismatched dimensions")
+    n = a.shape[2]
+    if n not in (1, 3):
+        raise GbError(-3, f"{name}: products of {n}-component matrices are not supported")
+    if n == 1:
+        a, b = np.repeat(a, 3, axis=2), np.repeat(b, 3, axis=2)
+    r = dctimestep_array(a, b, mode="fp64").astype(np.float64)
+    return r[..., :1] if n == 1 else r
+
+
+def _elementwise(a: np.ndarray, op: str, b: np.ndarray, name: str) -> np.ndarray:
+    """rmx_sum and rmx_elemult (util/rmatrix.c:840-925) in single precision;
+    a quotient by zero gives zero, as there."""
+    if a.shape[:2] != b.shape[:2]:
+        raise GbError(-1, f"{name}: mismatched dimensions")
+    a32, b32 = a.astype(np.float32), b.astype(np.float32)
+    if op == "+":
+        if a.shape[2] != b.shape[2]:
+            raise GbError(-1, f"{name}: matrix sum failed")
+        return (a32 + b32).astype(np.float64)
+    if b.shape[2] > 1 and b.shape[2] != a.shape[2]:
+        raise GbError(-1, f"{name}: element-wise {'division' if op == '/' else 'multiplication'} failed")
+    if op == "*":
+        return (a32 * b32).astype(np.float64)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        if b.shape[2] == 1:                        # d = 1/d in double, stored as a float
+            d = b[..., 0]
+            inv = np.where(d == 0, 0.0, 1.0 / np.where(d == 0, 1.0, d)).astype(np.float32)
+            r = a32 * inv[..., None]
+            r[d == 0] = 0
+        else:
+            r = np.where(b32 == 0, np.float32(0), a32 / np.where(b32 == 0, np.float32(1), b32))
+    return r.astype(np.float64)
+
+
+class Rmtxop:
+    """pyradiance.Rmtxop (src/pyradiance/util.py:912-965): matrices added
+    with ``add_input`` (each with its own scale, component transform and
+    transpose), joined by ``op`` to the one before: "." matrix product, "+"
+    sum, "*" and "/" element-wise product and quotient; evaluated left to
+    right, or, for a chain of products only whose rightmost matrix is
+    narrower than the leftmost is tall, right to left (rmtxop.c:501-525
+    prefer_right2left).  Calling the object returns the result in the
+    output format ("a", "f" or "d") as rmtxop writes it."""
+
+    def __init__(self, outform: str = "a", color: str | None = None):
+        if color is not None:
+            raise GbError(-3, "symbolic colour transforms (-C) are not supported")
+        if outform not in ("a", "f", "d"):
+            raise GbError(-3, f"output format '{outform}' is not supported")
+        self.outform = outform
+        self.parts = []
+        self._stdin = False
+
+    def add_input(self, input_data, op: str = ".", scale=None, transform=None, transpose: bool = False,
+                  refl_side: str | None = None, color: str | None = None):
+        if refl_side is not None:
+            raise GbError(-3, "BSDF reflectance matrices (-rf / -rb) are not supported")
+        if color is not None:
+            raise GbError(-3, "symbolic colour transforms (-C) are not supported")
+        if self.parts and op not in (".", "+", "*", "/"):
+            raise GbError(-1, f"unknown operation '{op}'")
+        if isinstance(input_data, bytes):
+            if self._stdin:
+                raise ValueError("stdin is already taken")
+            self._stdin = True
+        self.parts.append((input_data, op if self.parts else None, scale, transform, transpose))
+        return self
+
+    def _load(self, i: int) -> np.ndarray:
+        src, _, scale, transform, transpose = self.parts[i]
+        return rmtxop_array(read_rmatrix(src), transpose, scale, transform)
+
+    def result(self) -> np.ndarray:
+        """The combined matrix, (rows, cols, components) float64 holding
+        single-precision values."""
+        if not self.parts:
+            raise GbError(-1, "no matrix to operate on")
+        ops = [p[1] for p in self.parts[1:]]
+        name = lambda i: str(self.parts[i][0])[:60] if not isinstance(self.parts[i][0], bytes) else "-"  # noqa: E731
+        mats = [self._load(i) for i in range(len(self.parts))]
+        if len(mats) > 2 and all(o == "." for o in ops):
+            right, left = mats[-1], mats[0]
+            r2l = right.shape[1] == 1 or (right.shape[1] < right.shape[0] and right.shape[1] < left.shape[0])
+            if r2l:
+                res = mats[-1]
+                for i in range(len(mats) - 2, -1, -1):
+                    res = _product(mats[i], res, name(i + 1))
+                return res
+        res = mats[0]
+        for i, op in enumerate(ops, start=1):
+            res = _product(res, mats[i], name(i)) if op == "." else _elementwise(res, op, mats[i], name(i))
+        return res
+
+    def __call__(self) -> bytes:
+        return write_rmatrix(self.result(), self.outform, "rmtxop")

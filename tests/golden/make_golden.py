@@ -745,6 +745,41 @@ def rmtxop_cases() -> None:
     print("rmtxop: %d cases" % len(cases))
 
 
+def rmtxop_chains() -> None:
+    """rmtxop (util/rmtxop.c:383-525) on several matrices: products (a
+    three-matrix chain whose rightmost matrix is a column, evaluated right
+    to left), sums, element-wise products and quotients (with zeros, and by
+    a one-component matrix), each matrix with its own scale, transform or
+    transpose."""
+    rng = np.random.default_rng(14)
+    mats = {"A": rng.lognormal(-1, 1, (6, 9, 3)), "B": rng.lognormal(-1, 1, (9, 5, 3)),
+            "Bt": rng.lognormal(-1, 1, (5, 9, 3)), "C": rng.lognormal(-1, 1, (5, 1, 3)),
+            "D": rng.lognormal(-1, 1, (6, 9, 3)), "E": rng.lognormal(-1, 1, (6, 9, 1)),
+            "F": rng.lognormal(-1, 1, (9, 9, 3))}
+    mats["D"][rng.random((6, 9, 3)) < 0.2] = 0
+    mats["E"][rng.random((6, 9, 1)) < 0.2] = 0
+    chains = [["A", ".", "B"], ["A", ".", "B", ".", "C"], ["-s", "2", "A", ".", "-t", "Bt"],
+              ["A", "+", "D"], ["A", "*", "D"], ["A", "/", "D"], ["A", "*", "E"], ["A", "/", "E"],
+              ["A", ".", "F", ".", "B"], ["-c", ".3", ".6", ".1", "A", "*", "-c", ".3", ".6", ".1", "D"],
+              ["A", "+", "-s", "0.5", "D", ".", "B"]]
+    outs = {}
+    with tempfile.TemporaryDirectory() as td:
+        td = Path(td)
+        for k, m in mats.items():
+            (td / f"{k}.mtx").write_bytes(
+                f"#?RADIANCE\nNROWS={m.shape[0]}\nNCOLS={m.shape[1]}\nNCOMP={m.shape[2]}\nBigEndian=0\n"
+                "FORMAT=double\n\n".encode() + m.astype("<f8").tobytes())
+        for i, c in enumerate(chains):
+            args = [a + ".mtx" if a in mats else a for a in c]
+            out = run(["rmtxop", "-fd", *args], b"", cwd=td)
+            head, body = out.split(b"\n\n", 1)
+            dims = {ln.split("=")[0]: int(ln.split("=")[1]) for ln in head.decode().splitlines()
+                    if ln.startswith(("NROWS=", "NCOLS=", "NCOMP="))}
+            outs[f"out{i}"] = np.frombuffer(body, dtype="<f8").reshape(dims["NROWS"], dims["NCOLS"], dims["NCOMP"])
+    np.savez_compressed(OUT / "rmtxop_chains.npz", chains=np.array([" ".join(c) for c in chains]), **mats, **outs)
+    print("rmtxop chains: %d" % len(chains))
+
+
 def dct_small() -> None:
     """dctimestep on small matrices with the annual workload's value
     distributions (DC lognormal with zeros, sky spikes and night columns)."""
@@ -805,7 +840,7 @@ def main() -> None:
              "ss": supersampled_irradiance, "inst": instances, "mesh": meshes, "circ": circular_sources,
              "trans": translucent, "bins": general_bins,
              "spot": spotlights, "mirror": mirrors, "flux": flux_matrices, "flux_sc": flux_shirchiu,
-             "dct": lambda tmp: dct_small(), "dct4": lambda tmp: dct_four(), "rmtxop": lambda tmp: rmtxop_cases(), "trace_oct": lambda tmp: ref_fixture_trace(),
+             "dct": lambda tmp: dct_small(), "dct4": lambda tmp: dct_four(), "rmtxop": lambda tmp: rmtxop_cases(), "rmtxop_chains": lambda tmp: rmtxop_chains(), "trace_oct": lambda tmp: ref_fixture_trace(),
              "c2ab1": lambda tmp: c2_stats(tmp, ab=1, K=256), "c2ab3": lambda tmp: c2_stats(tmp, ab=3, K=256),
              "c2head": c2_headline, "gradfd": grad_fd, "bytes": bytes_surface,
              "edges": edge_rays}

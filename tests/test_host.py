@@ -157,6 +157,71 @@ def test_rfluxmtx_receiver_arguments(tmp_path):
     assert np.allclose(rays[:, 1], 0) and (rays[:, 0] >= 3.5).all() and (rays[:, 0] <= 6.5).all()
 
 
+def rmtxop_chain(gb, g, chain: str, outform: str = "d"):
+    """An Rmtxop built from a recorded rmtxop command line (options before
+    each matrix, operators between them), matrices as bytes or paths."""
+    import tempfile
+    w = chain.split()
+    rm = gb.Rmtxop(outform=outform)
+    kw, op, i = {}, ".", 0
+    tmp = Path(tempfile.mkdtemp())
+    while i < len(w):
+        t = w[i]
+        if t == "-s":
+            kw["scale"] = float(w[i + 1])
+            i += 2
+        elif t == "-t":
+            kw["transpose"] = True
+            i += 1
+        elif t == "-c":
+            j = i + 1
+            while j < len(w) and w[j][0] in ".0123456789":
+                j += 1
+            kw["transform"] = [float(x) for x in w[i + 1:j]]
+            i = j
+        elif t in (".", "+", "*", "/"):
+            op = t
+            i += 1
+        else:
+            m = g[t]
+            f = tmp / f"{t}.mtx"
+            f.write_bytes(f"#?RADIANCE\nNROWS={m.shape[0]}\nNCOLS={m.shape[1]}\nNCOMP={m.shape[2]}\n"
+                          "BigEndian=0\nFORMAT=double\n\n".encode() + m.astype("<f8").tobytes())
+            rm.add_input(f, op=op, **kw)
+            kw, op = {}, "."
+            i += 1
+    return rm
+
+
+def test_rmtxop_elementwise_chains():
+    """Rmtxop (util/rmtxop.c:383-525) chains of sums, element-wise products
+    and quotients (zeros in the divisor give zeros, a one-component divisor
+    is inverted first), with per-matrix scales and transforms: sums and
+    products equal to the reference program's output, quotients within two
+    single-precision ulps (the reference is built with -ffast-math, whose
+    divisions round differently from IEEE division).  Chains with matrix
+    products run on the GPU (tests/test_gpu_rmtxop.py)."""
+    import pyradiance_gb300 as gb
+    from pyradiance_gb300 import rmtx
+    g = np.load(ROOT / "tests" / "golden" / "rmtxop_chains.npz")
+    n = 0
+    for i, chain in enumerate(g["chains"]):
+        chain = str(chain)
+        if " . " in f" {chain} ":
+            continue
+        a = rmtx.read_rmatrix(rmtxop_chain(gb, g, chain)())
+        np.testing.assert_allclose(a, g[f"out{i}"], rtol=3e-7 if "/" in chain else 0, atol=0, err_msg=chain)
+        n += 1
+    assert n == 6
+    rm = gb.Rmtxop().add_input(b"x")
+    with pytest.raises(gb.GbError, match="unknown operation"):
+        rm.add_input("y.mtx", op="-")
+    with pytest.raises(ValueError, match="stdin"):
+        rm.add_input(b"y", op="+")
+    with pytest.raises(gb.GbError):
+        gb.Rmtxop(color="XYZ")
+
+
 def test_rmtxop_against_reference():
     """rmtxop's single-matrix operations (util/rmtxop.c:288-381: transform with
     the scale folded in, else scale, then transpose) equal the reference
