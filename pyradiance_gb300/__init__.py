@@ -531,16 +531,20 @@ def _dctimestep(*mtx, nstep: int | None = None, header: bool = True, xres: int |
     does, D x sky first, then T, then V, each product on the GPU's tensor
     cores (pre-scaled FP16 split, within 1e-5 of FP64) with FP32
     intermediates (the reference's matrices hold floats).  A transmission
-    matrix given as an XML BSDF (cm_loadBTDF) raises."""
+    matrix given as a Klems matrix BSDF (an .xml file) is converted as
+    cm_loadBTDF converts it (pyradiance_gb300/bsdf.py)."""
     if len(mtx) not in (2, 4):
         raise ValueError("mtx must be a list of 2 or 4 items")
     if ospec:
         raise GbError(-3, "output specification files are not supported")
     if len(mtx) == 4:
-        if isinstance(mtx[1], (str, Path)) and str(mtx[1]).lower().endswith(".xml"):
-            raise GbError(-3, "XML BSDF transmission matrices (cm_loadBTDF) are not supported; "
-                          "give the matrix as a Radiance matrix file")
-        V, T, D = (_read_matrix(m) for m in mtx[:3])
+        tx = mtx[1]
+        if isinstance(tx, (str, Path)) and not str(tx).startswith("!") and str(tx).lower().endswith(".xml"):
+            from .bsdf import load_btdf
+            T = load_btdf(tx)                        # util/dctimestep.c:250-254
+        else:
+            T = _read_matrix(tx)
+        V, D = _read_matrix(mtx[0]), _read_matrix(mtx[2])
         sky = _read_matrix(mtx[3], inform)
         for a, b, what in ((D, sky, "daylight and sky"), (T, D, "transmission and daylight"),
                            (V, T, "view and transmission")):

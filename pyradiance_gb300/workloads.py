@@ -500,6 +500,65 @@ def mesh_room(mesh_file: str, seed: int = 0, n: int = 10) -> str:
     return "".join(out)
 
 
+def klems_bsdf_xml(seed: int = 0, basis: str = "full", front: bool = True, back: bool = True,
+                   rows: bool = False, base: float = 0.002) -> str:
+    """A WINDOW 6 style XML matrix BSDF of synthetic glazing in a Klems
+    basis (defined in the file as WINDOW 6 writes it): "Visible"
+    transmission with a straight-through peak (exiting patch opposite in
+    azimuth, same ring), a smooth forward lobe, a floor ``base`` and seeded
+    noise; "Transmission Front" and/or "Transmission Back" blocks, data
+    ordered by columns (one line per exiting patch) or rows."""
+    rng = np.random.default_rng(seed)
+    rings = {"full": [(0, 5, 1), (5, 15, 8), (15, 25, 16), (25, 35, 20), (35, 45, 24), (45, 55, 24),
+                      (55, 65, 24), (65, 75, 16), (75, 90, 12)],
+             "half": [(0, 6.5, 1), (6.5, 19.5, 8), (19.5, 32.5, 12), (32.5, 45.5, 16), (45.5, 58.5, 20),
+                      (58.5, 71.5, 12), (71.5, 90, 8)]}[basis]
+    name = {"full": "LBNL/Klems Full", "half": "LBNL/Klems Half"}[basis]
+    centres = []
+    for lo, hi, nph in rings:
+        for k in range(nph):
+            centres.append((np.radians(0.5 * (lo + hi)), 2 * np.pi * k / nph, lo, hi, nph))
+    n = len(centres)
+    th = np.array([c[0] for c in centres])
+    ph = np.array([c[1] for c in centres])
+    d = np.array([[np.sin(t) * np.cos(p), np.sin(t) * np.sin(p), np.cos(t)] for t, p in zip(th, ph)])
+
+    def matrix(scale):
+        m = base + 0.3 * scale * np.maximum(0, d[:, None, 2] * d[None, :, 2]) ** 2
+        m += 0.02 * rng.random((n, n))
+        for i in range(n):                          # straight through: opposite azimuth, same ring
+            j = int(np.argmin(np.linalg.norm(d - d[i] * np.array([-1, -1, 1]), axis=1)))
+            m[j, i] += 12.0 * scale * np.cos(th[i])
+        return m                                    # m[exiting, incident]
+
+    def block(direction, m):
+        data = m.T if rows else m
+        body = "\n".join(" ".join(f"{v:.6e}" for v in row) for row in data)
+        return (f"\t\t<WavelengthDataBlock>\n\t\t\t<WavelengthDataDirection>{direction}</WavelengthDataDirection>\n"
+                f"\t\t\t<ColumnAngleBasis>{name}</ColumnAngleBasis>\n\t\t\t<RowAngleBasis>{name}</RowAngleBasis>\n"
+                f"\t\t\t<ScatteringDataType>BTDF</ScatteringDataType>\n\t\t\t<ScatteringData>\n{body}\n"
+                "\t\t\t</ScatteringData>\n\t\t</WavelengthDataBlock>\n")
+
+    blocks = ("".join(f"\t\t\t<AngleBasisBlock>\n\t\t\t\t<Theta>{0.5 * (lo + hi) if lo else 0}</Theta>\n"
+                      f"\t\t\t\t<nPhis>{nph}</nPhis>\n\t\t\t\t<ThetaBounds>\n\t\t\t\t\t<LowerTheta>{lo}</LowerTheta>\n"
+                      f"\t\t\t\t\t<UpperTheta>{hi}</UpperTheta>\n\t\t\t\t</ThetaBounds>\n\t\t\t</AngleBasisBlock>\n"
+                      for lo, hi, nph in rings))
+    out = ['<?xml version="1.0" encoding="UTF-8"?>\n',
+           '<WindowElement xmlns="http://windows.lbl.gov" xmlns:xsi="http://www.w3.org/2001/XMLSchema-instance">\n',
+           "<WindowElementType>System</WindowElementType>\n<FileType>BSDF</FileType>\n<Optical>\n<Layer>\n",
+           "\t<Material>\n\t\t<Name>synthetic glazing</Name>\n\t\t<DeviceType>Other</DeviceType>\n\t</Material>\n",
+           f"\t<DataDefinition>\n\t\t<IncidentDataStructure>{'Rows' if rows else 'Columns'}</IncidentDataStructure>\n",
+           f"\t\t<AngleBasis>\n\t\t\t<AngleBasisName>{name}</AngleBasisName>\n{blocks}\t\t</AngleBasis>\n",
+           "\t</DataDefinition>\n\t<WavelengthData>\n\t\t<LayerNumber>System</LayerNumber>\n",
+           '\t\t<Wavelength unit="Integral">Visible</Wavelength>\n']
+    if back:
+        out.append(block("Transmission Back", matrix(1.0)))
+    if front:
+        out.append(block("Transmission Front", matrix(0.8)))
+    out.append("\t</WavelengthData>\n</Layer>\n</Optical>\n</WindowElement>\n")
+    return "".join(out)
+
+
 def shape_zoo(seed: int = 0, n: int = 40) -> str:
     """Room with every primitive type the intersectors handle: spheres,
     bubbles, cones, cups, cylinders, tubes, rings and polygons, gray plastic

@@ -780,6 +780,49 @@ def rmtxop_chains() -> None:
     print("rmtxop chains: %d" % len(chains))
 
 
+BTDF_CASES = {"fb_cols": dict(seed=1, basis="full", front=True, back=True, rows=False),
+              "back_rows": dict(seed=2, basis="full", front=False, back=True, rows=True, base=0.01),
+              "half_front": dict(seed=3, basis="half", front=True, back=False, rows=False, base=0.05)}
+
+
+def btdf_matrices() -> None:
+    """Klems matrix BSDFs (util/cmbsdf.c cm_loadBTDF, common/bsdf_m.c) as
+    the reference dctimestep converts them: three synthetic XML files
+    (workloads.klems_bsdf_xml, regenerated from their arguments by the
+    tests): front and back transmission by columns, back transmission only
+    by rows (reciprocity) with a floor taken out as a Lambertian part, and
+    the Klems half basis.  Each transmission matrix is read through
+    dctimestep with identity view, daylight and sky matrices; and one
+    four-matrix product V T D sky per file."""
+    def mtx(path, m):
+        path.write_bytes(f"#?RADIANCE\nNROWS={m.shape[0]}\nNCOLS={m.shape[1]}\nNCOMP=3\nBigEndian=0\n"
+                         "FORMAT=float\n\n".encode() + np.ascontiguousarray(m, dtype="<f4").tobytes())
+    rng = np.random.default_rng(15)
+    out = {}
+    with tempfile.TemporaryDirectory() as td:
+        td = Path(td)
+        for k, kw in BTDF_CASES.items():
+            xml = td / f"{k}.xml"
+            xml.write_text(w.klems_bsdf_xml(**kw))
+            n = 145 if kw["basis"] == "full" else 77
+            eye = np.repeat(np.eye(n)[:, :, None], 3, axis=2)
+            mtx(td / "I.mtx", eye)
+            T = np.frombuffer(run(["dctimestep", "-h", "-of", td / "I.mtx", xml, td / "I.mtx", td / "I.mtx"]),
+                              dtype="<f4").reshape(n, n, 3)
+            V = rng.lognormal(-3, 1, (4, n, 3))
+            D = rng.lognormal(-4, 1, (n, 20, 3))
+            S = rng.lognormal(1, 1, (20, 5, 3))
+            for name, m in (("V", V), ("D", D), ("S", S)):
+                mtx(td / f"{name}.mtx", m)
+            R = np.frombuffer(run(["dctimestep", "-h", "-of", td / "V.mtx", xml, td / "D.mtx", td / "S.mtx"]),
+                              dtype="<f4").reshape(4, 5, 3)
+            out.update({f"{k}_T": T[..., 0].copy(), f"{k}_V": V.astype(np.float32), f"{k}_D": D.astype(np.float32),
+                        f"{k}_S": S.astype(np.float32), f"{k}_R": R})
+            print("btdf %s: T %s max %.4g, channels equal %s" % (k, T.shape, T.max(),
+                                                                 bool((T[..., 0] == T[..., 1]).all())))
+    np.savez_compressed(OUT / "btdf.npz", cases=np.array(list(BTDF_CASES)), **out)
+
+
 def dct_small() -> None:
     """dctimestep on small matrices with the annual workload's value
     distributions (DC lognormal with zeros, sky spikes and night columns)."""
@@ -840,7 +883,7 @@ def main() -> None:
              "ss": supersampled_irradiance, "inst": instances, "mesh": meshes, "circ": circular_sources,
              "trans": translucent, "bins": general_bins,
              "spot": spotlights, "mirror": mirrors, "flux": flux_matrices, "flux_sc": flux_shirchiu,
-             "dct": lambda tmp: dct_small(), "dct4": lambda tmp: dct_four(), "rmtxop": lambda tmp: rmtxop_cases(), "rmtxop_chains": lambda tmp: rmtxop_chains(), "trace_oct": lambda tmp: ref_fixture_trace(),
+             "dct": lambda tmp: dct_small(), "dct4": lambda tmp: dct_four(), "rmtxop": lambda tmp: rmtxop_cases(), "rmtxop_chains": lambda tmp: rmtxop_chains(), "btdf": lambda tmp: btdf_matrices(), "trace_oct": lambda tmp: ref_fixture_trace(),
              "c2ab1": lambda tmp: c2_stats(tmp, ab=1, K=256), "c2ab3": lambda tmp: c2_stats(tmp, ab=3, K=256),
              "c2head": c2_headline, "gradfd": grad_fd, "bytes": bytes_surface,
              "edges": edge_rays}

@@ -623,8 +623,8 @@ def test_dctimestep_fp32_fp64(gb):
 
 def test_dctimestep_four_matrix(gb, tmp_path):
     """dctimestep V T D sky (util/dctimestep.c:243-264) through the drop-in:
-    matrix files in, the reference program's output within 1e-5; an XML
-    BSDF transmission raises."""
+    matrix files in, the reference program's output within 1e-5; a
+    missing XML BSDF transmission raises."""
     g = golden("dct_four.npz")
     paths = []
     for n in "VTDS":
@@ -640,6 +640,32 @@ def test_dctimestep_four_matrix(gb, tmp_path):
         gb.dctimestep(paths[0], tmp_path / "T.xml", paths[2], paths[3])
     with pytest.raises(RuntimeError):
         gb.dctimestep(paths[0], paths[0], paths[2], paths[3])
+
+
+def test_dctimestep_xml_transmission(gb, tmp_path):
+    """dctimestep V T.xml D sky with Klems matrix BSDFs for T
+    (util/dctimestep.c:250-254 cm_loadBTDF): the three synthetic XML files
+    of tests/golden/btdf.npz, each product on the GPU: the reference
+    program's output within 1e-5."""
+    import sys
+    from pathlib import Path
+    from pyradiance_gb300 import workloads as w
+    sys.path.insert(0, str(Path(__file__).resolve().parent / "golden"))
+    from make_golden import BTDF_CASES
+    g = golden("btdf.npz")
+    for k, kw in BTDF_CASES.items():
+        (tmp_path / f"{k}.xml").write_text(w.klems_bsdf_xml(**kw))
+        paths = []
+        for n in "VDS":
+            m = g[f"{k}_{n}"]
+            hdr = (f"#?RADIANCE\nNROWS={m.shape[0]}\nNCOLS={m.shape[1]}\nNCOMP=3\nBigEndian=0\n"
+                   "FORMAT=float\n\n").encode()
+            (tmp_path / f"{k}_{n}.mtx").write_bytes(hdr + m.astype("<f4").tobytes())
+            paths.append(tmp_path / f"{k}_{n}.mtx")
+        out = gb.dctimestep(paths[0], tmp_path / f"{k}.xml", paths[1], paths[2], header=False, outform="d")
+        ref = g[f"{k}_R"]
+        r = np.frombuffer(out, dtype="<f8").reshape(ref.shape)
+        np.testing.assert_allclose(r, ref, rtol=1e-5, atol=1e-6 * np.abs(ref).max(), err_msg=k)
 
 
 def test_errors_are_reported(gb, scenes):

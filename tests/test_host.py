@@ -2,6 +2,7 @@
 every declared symbol, option defaults and parsing follow the reference,
 bin expressions compile, and the workloads are deterministic."""
 import hashlib
+import sys
 import re
 from pathlib import Path
 
@@ -247,3 +248,29 @@ def test_rmtxop_against_reference():
         np.testing.assert_allclose(back, a, rtol=1e-6)
     with pytest.raises(RuntimeError):
         gb.rmtxop(src, transform=[1, 2])
+
+
+def test_btdf_matrices_against_reference(tmp_path):
+    """Klems matrix BSDFs read as dctimestep reads a transmission matrix
+    (util/cmbsdf.c:146-181 cm_loadBTDF over common/bsdf_m.c): front and back
+    transmission by columns; back transmission only, by rows, turned
+    around by reciprocity, with a floor taken out as a Lambertian part; the
+    Klems half basis.  Equal to the reference dctimestep's matrices to
+    within 3.5e-7 (the reference's RGB conversion of the Lambertian part
+    rounds some values by a single-precision ulp or two)."""
+    from pyradiance_gb300 import bsdf, workloads as w
+    sys.path.insert(0, str(ROOT / "tests" / "golden"))
+    from make_golden import BTDF_CASES
+    g = np.load(ROOT / "tests" / "golden" / "btdf.npz")
+    for k, kw in BTDF_CASES.items():
+        xml = tmp_path / f"{k}.xml"
+        xml.write_text(w.klems_bsdf_xml(**kw))
+        T = bsdf.load_btdf(xml)
+        ref = g[f"{k}_T"]
+        assert T.shape == ref.shape + (3,), k
+        for c in range(3):
+            np.testing.assert_allclose(T[..., c], ref, rtol=3.5e-7, atol=0, err_msg=k)
+    bad = tmp_path / "tree.xml"
+    bad.write_text(w.klems_bsdf_xml(seed=1).replace("<IncidentDataStructure>Columns", "<IncidentDataStructure>TensorTree3"))
+    with pytest.raises(RuntimeError, match="unsupported BSDF"):
+        bsdf.load_btdf(bad)
