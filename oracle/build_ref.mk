@@ -46,7 +46,7 @@ LIBRAD   := $(OBJ)/libradiance.a
 LIBRL    := $(OBJ)/libraycalls.a
 
 CALS := $(RAD)/rt/rayinit.cal $(RAD)/util/reinhartb.cal $(RAD)/util/klems_full.cal $(RAD)/util/klems_half.cal \
-        $(RAD)/util/klems_quarter.cal $(RAD)/util/disk2square.cal
+        $(RAD)/util/klems_quarter.cal $(RAD)/util/disk2square.cal $(RAD)/util/cieskyscan.cal
 
 all: $(OUT)/bin/rtrace $(OUT)/bin/rcontrib $(OUT)/bin/oconv $(OUT)/bin/obj2mesh $(OUT)/bin/dctimestep $(OUT)/bin/rfluxmtx $(OUT)/bin/rmtxop
 	@mkdir -p $(OUT)/lib && cp $(CALS) $(OUT)/lib/

@@ -1061,6 +1061,30 @@ static void trace_contrib(ctx *X, const RAY *r)
                 pc += 2;
                 break;
             }
+            case GB_OP_CBIN: {
+                /* util/cieskyscan.cal: rows of 12 degrees, azimuth from behind, alternate windings */
+                const gb_binins *q = pr + pc + 1;
+                double RHS = q[0].a, rNx = q[0].b, rNy = q[0].c, rNz = q[1].op, Ux = q[1].a, Uy = q[1].b,
+                       Uz = q[1].c, DEG = PI / 180;
+                double Dx = r->rdir[0], Dy = r->rdir[1], Dz = r->rdir[2];
+                double inc_dz = -Dx * rNx - Dy * rNy - Dz * rNz;
+                double inc_rx = -RHS * (Dx * (Uy * rNz - Uz * rNy) + Dy * (Uz * rNx - Ux * rNz) + Dz * (Ux * rNy - Uy * rNx));
+                double inc_ry = Dx * Ux + Dy * Uy + Dz * Uz + inc_dz * (rNx * Ux + rNy * Uy + rNz * Uz);
+                double alt = (inc_dz - 1 > 0 ? PI / 2 : (-1 - inc_dz > 0 ? -PI / 2 : asin(inc_dz))) / DEG;
+                static const double cnaz[8] = {30, 30, 24, 24, 18, 12, 6, 1};
+                if (!(alt > 0)) st[sp++] = -1;
+                else {
+                    double a = atan2(-inc_rx, -inc_ry), azi = (-a > 0 ? a + 2 * PI : a) / DEG, acc = 0, n, inc;
+                    int row = (int)floor(alt / (90 / 7.5)), rr;
+                    if (row > 7) row = 7;
+                    for (rr = 0; rr < row; rr++) acc += cnaz[rr];
+                    n = cnaz[row];
+                    inc = 360 / n;
+                    st[sp++] = acc + (359.9999 - azi > 0 ? ((row & 1) ? n - 1 - floor(azi / inc) : floor(azi / inc)) : 0);
+                }
+                pc += 2;
+                break;
+            }
             default: return;
             }
         }

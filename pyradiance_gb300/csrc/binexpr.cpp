@@ -22,7 +22,9 @@
  *    klems_half.cal and klems_quarter.cal (kbin, khbin, kqbin with their bin
  *    counts) built in: rfluxmtx receivers name these files;
  *  - the Shirley-Chiu square bins of util/disk2square.cal (scbin, with
- *    SCdim and the frame parameters) built in.
+ *    SCdim and the frame parameters) built in;
+ *  - the CIE sky scanner bins of util/cieskyscan.cal (cbin, Ncbins, with
+ *    the frame parameters) built in.
  *
  * Calls are expanded where they are used (partial evaluation): arguments
  * that are constants are substituted and folded, so recursion on constant
@@ -50,7 +52,7 @@ using NP = std::shared_ptr<Node>;
 
 struct Node {
     enum Kind {
-        NUM, DX, DY, DZ, NEG, ADD, SUB, MUL, DIV, POW, IF, FN1, ATAN2, MAXN, MINN, SELECT, FLOOR, RBIN, KBIN, SCBIN,
+        NUM, DX, DY, DZ, NEG, ADD, SUB, MUL, DIV, POW, IF, FN1, ATAN2, MAXN, MINN, SELECT, FLOOR, RBIN, KBIN, SCBIN, CBIN,
         TEMP, LET,              /* residual only: temporary t, and let t = a[0] in a[1] */
         VAR, CALL               /* parsed only */
     } k;
@@ -80,6 +82,7 @@ struct Ctx {
     bool reinhart = false;
     int klems = 0;              /* 1, 2, 4: built-in full, half, quarter Klems bins */
     bool shirchiu = false;      /* built-in Shirley-Chiu bins (scbin) */
+    bool cie = false;           /* built-in CIE sky scanner bins (cbin) */
     std::string err;
     int temps = 0;
     NP fail(const std::string &m)
@@ -350,6 +353,21 @@ struct Eval {
             }
             return n;
         }
+        if (C.cie && !C.defs.count(name) && (name == "cbin" || name == "Ncbins")) {
+            if (name == "Ncbins")
+                return num(145);
+            static const char *cn[7] = {"RHS", "rNx", "rNy", "rNz", "Ux", "Uy", "Uz"};
+            static const double dflt[7] = {1, 0, 0, -1, 0, 1, 0};   /* +Y north, normal down */
+            NP n = mk(Node::CBIN);
+            n->a.push_back(num(0));
+            for (int i = 0; i < 7; i++) {
+                NP v = C.defs.count(cn[i]) ? var(cn[i], Env()) : num(dflt[i]);
+                if (!v) return nullptr;
+                if (!isnum(v)) return C.fail(std::string("CIE bin parameter ") + cn[i] + " must be constant");
+                n->a.push_back(v);
+            }
+            return n;
+        }
         if (C.klems && !C.defs.count(name)) {
             /* Nkbins / Nkhbins / Nkqbins, and the full basis's kbinN, kbinE,
              * kbinS, kbinW (walls, up +Z) and kbinD (skylight, up +Y) */
@@ -550,10 +568,11 @@ struct Emitter {
                 (float)(n->k == Node::SELECT ? k - 1 : k), 1 - k);
             return;
         }
-        case Node::RBIN: case Node::KBIN: case Node::SCBIN: {
+        case Node::RBIN: case Node::KBIN: case Node::SCBIN: case Node::CBIN: {
             float p[8];
             for (int i = 0; i < 8; i++) p[i] = (float)n->a[i]->v;
-            put(n->k == Node::RBIN ? GB_OP_RBIN : n->k == Node::KBIN ? GB_OP_KBIN : GB_OP_SCBIN, 0, 1);
+            put(n->k == Node::RBIN ? GB_OP_RBIN : n->k == Node::KBIN ? GB_OP_KBIN
+                : n->k == Node::SCBIN ? GB_OP_SCBIN : GB_OP_CBIN, 0, 1);
             out.push_back({p[0], p[1], p[2], p[3]});
             out.push_back({p[4], p[5], p[6], p[7]});
             return;
@@ -593,6 +612,8 @@ int gb_compile_bin(const char *binv, const char *params, const char *calfile, co
             C.reinhart = true;
         else if (!strcmp(b, "disk2square.cal"))
             C.shirchiu = true;
+        else if (!strcmp(b, "cieskyscan.cal"))
+            C.cie = true;
         else if (!strcmp(b, "klems_full.cal"))
             C.klems = 1;
         else if (!strcmp(b, "klems_half.cal"))

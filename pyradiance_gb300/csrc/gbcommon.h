@@ -339,6 +339,8 @@ enum gb_binop {
                         {basis 1/2/4, RHS, Nx, Ny} {Nz, Ux, Uy, Uz} */
     GB_OP_SCBIN,     /* Shirley-Chiu bin; params in the next 2 records:
                         {SCdim, RHS, rNx, rNy} {rNz, Ux, Uy, Uz} */
+    GB_OP_CBIN,      /* CIE sky scanner bin; params in the next 2 records:
+                        {0, RHS, rNx, rNy} {rNz, Ux, Uy, Uz} */
     GB_OP_MAX
 };
 enum gb_binfn { GB_FN_SQRT, GB_FN_SIN, GB_FN_COS, GB_FN_TAN, GB_FN_ASIN, GB_FN_ACOS, GB_FN_ATAN, GB_FN_EXP,

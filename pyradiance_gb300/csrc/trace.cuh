@@ -858,6 +858,37 @@ GB_DFN float reinhart_bin(float Dx, float Dy, float Dz, const gb_binins *p)
     return acc + azn;
 }
 
+/* CIE sky scanner bin for the incident direction -D about normal rN with up
+ * vector U (util/cieskyscan.cal): 8 rows of 12 degrees of altitude with 30,
+ * 30, 24, 24, 18, 12, 6 and 1 patches, azimuth from -(right) clockwise,
+ * patches starting at azimuth 0 and wound forward in even rows, backward in
+ * odd ones; -1 below the horizon. */
+GB_DFN float cie_bin(float Dx, float Dy, float Dz, const gb_binins *p)
+{
+    float RHS = p[0].a, rNx = p[0].b, rNy = p[0].c;
+    float rNz = p[1].op, Ux = p[1].a, Uy = p[1].b, Uz = p[1].c;
+    const float DEG = D_PI / 180.f;
+    float inc_dz = -Dx * rNx - Dy * rNy - Dz * rNz;
+    float inc_rx = -RHS * (Dx * (Uy * rNz - Uz * rNy) + Dy * (Uz * rNx - Ux * rNz) + Dz * (Ux * rNy - Uy * rNx));
+    float inc_ry = Dx * Ux + Dy * Uy + Dz * Uz + inc_dz * (rNx * Ux + rNy * Uy + rNz * Uz);
+    float r_alt = (inc_dz - 1.f > 0.f ? D_PI / 2 : (-1.f - inc_dz > 0.f ? -D_PI / 2 : asinf(inc_dz))) / DEG;
+    if (!(r_alt > 0.f))
+        return -1.f;
+    float a = atan2f(-inc_rx, -inc_ry);
+    float c_azi = (-a > 0.f ? a + 2.f * D_PI : a) / DEG;
+    const float cnaz[8] = {30.f, 30.f, 24.f, 24.f, 18.f, 12.f, 6.f, 1.f};
+    int row = (int)floorf(r_alt / (90.f / 7.5f));
+    row = min(max(row, 0), 7);
+    float acc = 0.f;
+    for (int r = 0; r < row; r++)
+        acc += cnaz[r];
+    float n = cnaz[row], inc = 360.f / n;
+    float azn = 0.f;
+    if (359.9999f - c_azi > 0.f)
+        azn = (row & 1) ? n - 1.f - floorf(c_azi / inc) : floorf(c_azi / inc);
+    return acc + azn;
+}
+
 /* Klems bin of the LBNL/Klems full, half or quarter basis for the incident
  * direction -D about normal N with up vector U (util/klems_full.cal:10-40,
  * klems_half.cal, klems_quarter.cal): the polar angle picks the ring (the
@@ -976,6 +1007,10 @@ GB_DFN float eval_bin(const gb_binins *prog, float3 d)
             break;
         case GB_OP_SCBIN:
             st[sp++] = shirchiu_bin(d.x, d.y, d.z, prog + pc + 1);
+            pc += 2;
+            break;
+        case GB_OP_CBIN:
+            st[sp++] = cie_bin(d.x, d.y, d.z, prog + pc + 1);
             pc += 2;
             break;
         case GB_OP_POW: sp--; st[sp - 1] = powf(st[sp - 1], st[sp]); break;

@@ -11,8 +11,9 @@ bin.  Here the same arguments drive the in-process GPU rcontrib
 Hemisphere bases: uniform (``h=u``), Klems full / half / quarter (``h=kf``,
 ``kh``, ``kq``; the bases of util/klems_full.cal, klems_half.cal and
 klems_quarter.cal, built into the bin compiler), Reinhart (``h=r``,
-``h=rN``) and Shirley-Chiu (``h=scN``, util/disk2square.cal's scbin, built
-in).  CIE (``h=cie``) bins, bin jitter
+``h=rN``), Shirley-Chiu (``h=scN``, util/disk2square.cal's scbin, built
+in) and, for receivers, the CIE sky scanner (``h=cie``, util/cieskyscan.cal's
+cbin, built in).  Bin jitter
 (``-bj``) and per-bin output files (``o=`` with ``%d``) raise
 ``RuntimeError``; receivers with ``o=`` write their columns to that file.
 """
@@ -253,6 +254,10 @@ def _receivers(path) -> list[dict]:
             spec["calfile"], spec["nbins"] = cal, nb
             spec["params"] = "RHS=%s1" % p.sign
             spec["binv"] = "%s(%g,%g,%g,%g,%g,%g)" % (fn, *nrm, *vup)
+        elif h == "cie":                               # util/rfluxmtx.c:523-533
+            spec["calfile"] = "cieskyscan.cal"
+            spec["params"] = "rNx=%g,rNy=%g,rNz=%g,Ux=%g,Uy=%g,Uz=%g,RHS=%s1" % (*nrm, *vup, p.sign)
+            spec["binv"], spec["nbins"] = "cbin", "Ncbins"
         else:
             raise GbError(-3, f"hemisphere sampling h={p.hemis} is not supported")
         if not h[0] in "u1":

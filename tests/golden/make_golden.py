@@ -323,6 +323,25 @@ def general_bins(tmp: Path) -> None:
                                                                                 hit.any(0).sum()))
 
 
+def cie_bins(tmp: Path) -> None:
+    """CIE sky scanner bins (util/cieskyscan.cal, cbin) with rcontrib -ab 0
+    in radiance mode: rays in random directions in a scene of the sky and
+    ground glows alone (every direction meets the sky or the ground), for
+    the default frame and one turned a quarter round (up +X)."""
+    octp = oconv(w.SKY_GLOW, tmp, "cbins")
+    rng = np.random.default_rng(19)
+    d = rng.normal(size=(4000, 3))
+    rays = np.hstack([np.zeros((4000, 3)), d / np.linalg.norm(d, axis=1, keepdims=True)])
+    res = {}
+    for key, p in (("default", []), ("upx", ["-p", "Ux=1,Uy=0,Uz=0"])):
+        out = run(["rcontrib", "-h", "-u-", "-ab", "0", "-fdd", "-f", "cieskyscan.cal", *p, "-b", "cbin", "-bn",
+                   "Ncbins", "-m", "skyglow", "-m", "groundglow", octp.name], rays.astype("<f8").tobytes(), cwd=tmp)
+        res[key] = np.frombuffer(out, dtype="<f8").reshape(len(rays), -1, 3)[..., 0].astype(np.float32)
+        print("cie_bins %s: %d bins, %d distinct bins hit" % (key, res[key].shape[1], (res[key] > 0).any(0).sum()))
+    np.savez_compressed(OUT / "cie_bins.npz", rays=rays, **res,
+                        cmd="rcontrib -h -u- -ab 0 -fdd -f cieskyscan.cal [-p Ux=1,Uy=0,Uz=0] -b cbin -bn Ncbins -m skyglow -m groundglow")
+
+
 def translucent(tmp: Path, K: int = 256) -> None:
     """The trans material (rt/normal.c, MAT_TRANS): -I irradiance on a grid
     at 0.8 m (the light seen through the diffuser: shadow rays pass its
@@ -881,7 +900,7 @@ def main() -> None:
         sys.exit("reference programs missing: make -f oracle/build_ref.mk REF=/root/reference -j8")
     parts = {"octree": octree_digests, "c1": c1_direct, "c1p": c1_partitioned, "zoo": zoo, "glossy": glossy, "irr": surface_irradiance,
              "ss": supersampled_irradiance, "inst": instances, "mesh": meshes, "circ": circular_sources,
-             "trans": translucent, "bins": general_bins,
+             "trans": translucent, "bins": general_bins, "cbins": cie_bins,
              "spot": spotlights, "mirror": mirrors, "flux": flux_matrices, "flux_sc": flux_shirchiu,
              "dct": lambda tmp: dct_small(), "dct4": lambda tmp: dct_four(), "rmtxop": lambda tmp: rmtxop_cases(), "rmtxop_chains": lambda tmp: rmtxop_chains(), "btdf": lambda tmp: btdf_matrices(), "trace_oct": lambda tmp: ref_fixture_trace(),
              "c2ab1": lambda tmp: c2_stats(tmp, ab=1, K=256), "c2ab3": lambda tmp: c2_stats(tmp, ab=3, K=256),

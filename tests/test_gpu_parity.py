@@ -390,6 +390,26 @@ def test_general_bin_expressions(gb, scenes):
     np.testing.assert_allclose(got[same], g["bins"][same], rtol=1e-5, atol=1e-9)
 
 
+def test_cie_sky_scanner_bins(gb, tmp_path):
+    """CIE sky scanner bins (util/cieskyscan.cal cbin) built into the
+    device byte code: rays in every direction through a scene of the sky
+    and ground glows land in the reference's bin (FP32 directions: a ray
+    within rounding of a bin edge may land beside it), for the default and
+    a quarter-turned frame."""
+    from pyradiance_gb300 import workloads as w
+    g = golden("cie_bins.npz")
+    (tmp_path / "sky.rad").write_text(w.SKY_GLOW)
+    sc = gb.Scene(rad_files=[tmp_path / "sky.rad"])
+    for key, params in (("default", None), ("upx", "Ux=1,Uy=0,Uz=0")):
+        mods = [dict(modifier=m, calfile="cieskyscan.cal", binv="cbin", nbins="Ncbins", **(
+            {"params": params} if params else {})) for m in ("skyglow", "groundglow")]
+        out, _ = rcontrib_c(gb, sc, opts("rcontrib", I=0, ab=0, c=1, u=0), g["rays"], mods=mods)
+        got = out[..., 0]
+        same = ((got > 0) == (g[key] > 0)).all(1)
+        assert same.mean() >= 0.999, (key, np.nonzero(~same))
+        np.testing.assert_allclose(got[same], g[key][same], rtol=1e-5, atol=1e-9, err_msg=key)
+
+
 def test_translucent(gb, tmp_path, scene_dir):
     """The trans material (rt/normal.c, MAT_TRANS): -I irradiance through
     the diffuser (shadow rays continue through its specular transmission)

@@ -141,7 +141,12 @@ def test_rfluxmtx_receiver_arguments(tmp_path):
     kf = rflux._receivers(tmp_path / "window_kf.rad")
     assert [(m["modifier"], m["calfile"], m["params"], m["nbins"], m["binv"]) for m in kf] == [
         ("windowglow", "klems_full.cal", "RHS=+1", "Nkbins", "kbin(0,1,0,0,0,1)")]
-    (tmp_path / "bad.rad").write_text("#@rfluxmtx h=cie\nvoid glow g\n0\n0\n4 1 1 1 0\n\n"
+    (tmp_path / "cie.rad").write_text("#@rfluxmtx h=cie\nvoid glow g\n0\n0\n4 1 1 1 0\n\n"
+                                      "g polygon p\n0\n0\n9 0 0 0 1 0 0 0 1 0\n")
+    cie = rflux._receivers(tmp_path / "cie.rad")        # the reference's -v: -f cieskyscan.cal -p ... -b cbin
+    assert [(m["modifier"], m["calfile"], m["params"], m["nbins"], m["binv"]) for m in cie] == [
+        ("g", "cieskyscan.cal", "rNx=0,rNy=0,rNz=1,Ux=0,Uy=1,Uz=0,RHS=+1", "Ncbins", "cbin")]
+    (tmp_path / "bad.rad").write_text("#@rfluxmtx h=xyz\nvoid glow g\n0\n0\n4 1 1 1 0\n\n"
                                       "g polygon p\n0\n0\n9 0 0 0 1 0 0 0 1 0\n")
     with pytest.raises(Exception):
         rflux._receivers(tmp_path / "bad.rad")

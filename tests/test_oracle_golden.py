@@ -11,6 +11,7 @@ import pytest
 
 from conftest import MODS_C2, golden, reference_tree, zscores
 from oracle import pyoracle as po
+from pyradiance_gb300 import workloads as w
 
 _TREE = reference_tree()
 REF_TRACE = _TREE / "tests" / "Resources" / "trace.oct" if _TREE else Path("/nonexistent")
@@ -151,6 +152,24 @@ def test_general_bin_expressions(oscenes):
     got = out[..., 0]
     np.testing.assert_array_equal(got > 0, g["bins"] > 0)
     np.testing.assert_allclose(got, g["bins"], rtol=1e-6, atol=1e-9)
+
+
+def test_cie_sky_scanner_bins(tmp_path):
+    """The CIE sky scanner bins of util/cieskyscan.cal (cbin, Ncbins) built
+    into the bin compiler: rays in every direction in a scene of the sky and
+    ground glows land in the reference's bin, for the default frame and one
+    turned a quarter round."""
+    g = golden("cie_bins.npz")
+    (tmp_path / "sky.rad").write_text(w.SKY_GLOW)
+    sc = po.Scene(tmp_path / "sky.rad")
+    o = po.default_opts("rcontrib", I=0, ab=0, c=1, u=0)
+    for key, params in (("default", None), ("upx", "Ux=1,Uy=0,Uz=0")):
+        mods = [dict(modifier=m, calfile="cieskyscan.cal", binv="cbin", nbins="Ncbins", **(
+            {"params": params} if params else {})) for m in ("skyglow", "groundglow")]
+        out, _ = po.rcontrib(sc, o, mods, g["rays"], threads=8)
+        got = out[..., 0]
+        np.testing.assert_array_equal(got > 0, g[key] > 0, err_msg=key)
+        np.testing.assert_allclose(got, g[key], rtol=1e-6, atol=1e-9, err_msg=key)
 
 
 def test_translucent(tmp_path):
