@@ -13,9 +13,10 @@ Hemisphere bases: uniform (``h=u``), Klems full / half / quarter (``h=kf``,
 klems_quarter.cal, built into the bin compiler), Reinhart (``h=r``,
 ``h=rN``), Shirley-Chiu (``h=scN``, util/disk2square.cal's scbin, built
 in) and, for receivers, the CIE sky scanner (``h=cie``, util/cieskyscan.cal's
-cbin, built in).  Bin jitter
-(``-bj``) and per-bin output files (``o=`` with ``%d``) raise
-``RuntimeError``; receivers with ``o=`` write their columns to that file.
+cbin, built in).  Bin jitter (``-bj``) is passed to the bin parameters
+as ``JTR`` as rfluxmtx passes it (none of these bases reads it).  Per-bin
+output files (``o=`` with ``%d``) raise ``RuntimeError``; receivers with
+``o=`` write their columns to that file.
 """
 from __future__ import annotations
 
@@ -192,7 +193,7 @@ def _objects(path):
     return out
 
 
-def _receivers(path) -> list[dict]:
+def _receivers(path, jitter: str | None = None) -> list[dict]:
     """Receiver modifiers as rcontrib modifier arguments (rfluxmtx.c:427-582
     finish_receiver, :1116-1151 add_recv_object)."""
     groups: list[tuple[str, _Params]] = []
@@ -228,6 +229,7 @@ def _receivers(path) -> list[dict]:
         nrm = p.normal()
         vup = p.up(nrm)
         h = p.hemis.lower()
+        jtr = ",JTR=" + jitter if jitter is not None else ""   # rfluxmtx.c:413-424 addbinjitter
         spec = dict(modifier=mod, calfile=None, params=None, nbins=None, binv=None, expr=None, output=ospec)
         if h[0] in "u1":
             if p.surfs[-1].styp != "source":
@@ -240,23 +242,23 @@ def _receivers(path) -> list[dict]:
                 raise GbError(-1, "missing size for Shirley-Chiu sampling!")
             spec["calfile"] = "disk2square.cal"
             spec["params"] = "SCdim=%d,rNx=%g,rNy=%g,rNz=%g,Ux=%g,Uy=%g,Uz=%g,RHS=%s1" % (
-                p.hsiz, *nrm, *vup, p.sign)
+                p.hsiz, *nrm, *vup, p.sign) + jtr
             spec["binv"], spec["nbins"] = "scbin", "SCdim*SCdim"
         elif h[0] in "rt":
             spec["calfile"] = "reinhartb.cal"
             spec["params"] = "MF=%d,rNx=%g,rNy=%g,rNz=%g,Ux=%g,Uy=%g,Uz=%g,RHS=%s1" % (
-                p.hsiz, *nrm, *vup, p.sign)
+                p.hsiz, *nrm, *vup, p.sign) + jtr
             spec["binv"], spec["nbins"] = "rbin", "Nrbins"
         elif h[0] == "k" and (len(h) == 1 or h[1] in "f1h2q4"):
             kind = "f" if len(h) == 1 or h[1] in "f1" else ("h" if h[1] in "h2" else "q")
             cal, fn, nb = {"f": ("klems_full.cal", "kbin", "Nkbins"), "h": ("klems_half.cal", "khbin", "Nkhbins"),
                            "q": ("klems_quarter.cal", "kqbin", "Nkqbins")}[kind]
             spec["calfile"], spec["nbins"] = cal, nb
-            spec["params"] = "RHS=%s1" % p.sign
+            spec["params"] = "RHS=%s1" % p.sign + jtr
             spec["binv"] = "%s(%g,%g,%g,%g,%g,%g)" % (fn, *nrm, *vup)
         elif h == "cie":                               # util/rfluxmtx.c:523-533
             spec["calfile"] = "cieskyscan.cal"
-            spec["params"] = "rNx=%g,rNy=%g,rNz=%g,Ux=%g,Uy=%g,Uz=%g,RHS=%s1" % (*nrm, *vup, p.sign)
+            spec["params"] = "rNx=%g,rNy=%g,rNz=%g,Ux=%g,Uy=%g,Uz=%g,RHS=%s1" % (*nrm, *vup, p.sign) + jtr
             spec["binv"], spec["nbins"] = "cbin", "Ncbins"
         else:
             raise GbError(-3, f"hemisphere sampling h={p.hemis} is not supported")
@@ -475,6 +477,7 @@ def _sender(path) -> _Params:
 def _screen(params: Sequence[str]):
     """Split rfluxmtx's own options from those passed to rcontrib, with each
     option's argument count (rfluxmtx.c:1267-1420)."""
+    jitter = None
     rc, fmt, xres, yres, sampcnt, iropt, ldopt = [], ["a", "a"], None, None, 0, None, None
     a = 0
     params = list(params)
@@ -509,8 +512,12 @@ def _screen(params: Sequence[str]):
             iropt = o
             a += 1
             continue
-        if o == "-bj":
-            raise GbError(-3, "bin jitter (-bj) is not supported")
+        if o == "-bj":                          # rfluxmtx.c:1356-1360: passed to the bin parameters
+            if a + 1 >= len(params):
+                raise GbError(-1, "missing bin jitter value")
+            jitter = params[a + 1]
+            a += 2
+            continue
         if o.startswith("-ld"):                # passed on in pass-through mode only
             ldopt = o
             a += 1
@@ -539,7 +546,7 @@ def _screen(params: Sequence[str]):
             raise GbError(-1, f"unsupported option '{o}'")
         rc.extend(params[a:a + na])
         a += na
-    return rc, fmt, xres, yres, sampcnt, iropt, ldopt
+    return rc, fmt, xres, yres, sampcnt, iropt, ldopt, jitter
 
 
 def rfluxmtx_array(receiver, surface=None, rays=None, params: Sequence[str] | None = None, octree=None,
@@ -547,8 +554,8 @@ def rfluxmtx_array(receiver, surface=None, rays=None, params: Sequence[str] | No
     """(contributions (rows, bins, 3), rcontrib arguments, modifier specs,
     output format, yres) of an rfluxmtx run."""
     from . import Rcontrib, read_rays
-    rc, fmt, xres, yres, sampcnt, iropt, ldopt = _screen(params or [])
-    specs = _receivers(receiver)
+    rc, fmt, xres, yres, sampcnt, iropt, ldopt, jitter = _screen(params or [])
+    specs = _receivers(receiver, jitter)
     # oconv -f [-i octree] scene... receiver: the receiver goes last (rfluxmtx.c:139-178)
     files = ([str(octree)] if octree is not None else []) + [str(s) for s in (scene or [])] + [str(receiver)]
     sc = Scene(rad_files=files)

@@ -150,9 +150,10 @@ def test_rfluxmtx_receiver_arguments(tmp_path):
                                       "g polygon p\n0\n0\n9 0 0 0 1 0 0 0 1 0\n")
     with pytest.raises(Exception):
         rflux._receivers(tmp_path / "bad.rad")
-    with pytest.raises(Exception):
-        rflux._screen(["-bj", ".5"])
-    rc, fmt, xres, yres, cnt, iropt, ld = rflux._screen(["-v", "-ab", "2", "-ff", "-c", "30", "-I+", "-y", "4",
+    assert rflux._screen(["-bj", ".5"])[-1] == ".5"      # bin jitter: JTR among the bin parameters
+    assert rflux._receivers(tmp_path / "cie.rad", ".5")[0]["params"].endswith(",RHS=+1,JTR=.5")
+    assert rflux._receivers(tmp_path / "window_kf.rad", ".5")[0]["params"] == "RHS=+1,JTR=.5"
+    rc, fmt, xres, yres, cnt, iropt, ld, jit = rflux._screen(["-v", "-ab", "2", "-ff", "-c", "30", "-I+", "-y", "4",
                                                          "-av", "1", "1", "1", "-ld-"])
     assert rc == ["-ab", "2", "-av", "1", "1", "1"] and fmt == ["f", "f"] and cnt == 30 and iropt == "-I+"
     assert yres == "4" and ld == "-ld-"
