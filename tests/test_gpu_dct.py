@@ -44,11 +44,13 @@ BOUNDS = {"fp16x3": (1e-5, 1e-6), "bf16x3": (3e-5, 3e-6), "fp16": (4e-3, 1e-3), 
 
 
 @pytest.mark.parametrize("mode", ["fp16x3", "bf16x3", "fp16"])
-@pytest.mark.parametrize("M,K,N", [(300, 333, 700), (2100, 700, 2100), (520, 2306, 1000)])
+@pytest.mark.parametrize("M,K,N", [(300, 333, 700), (2100, 700, 2100), (520, 2306, 1000), (131, 150, 1003)])
 def test_tensor_core_forms_vs_fp64(gb, mode, M, K, N):
-    """Sizes that are not multiples of the 128 x 256 x 64 tiles; the second
+    """Sizes that are not multiples of the 128 x 256 x 32 tiles; the second
     has more tiles than SMs and a partial row-tile group, the third the
-    Reinhart MF:4 patch count of the annual workload."""
+    Reinhart MF:4 patch count of the annual workload, the fourth an odd
+    column count (rows not 16-byte aligned: zero columns stored float by
+    float)."""
     dc, sky, ref = dc_pair(np.random.default_rng(M + K), M, K, N)
     out = gb.dctimestep_array(dc, sky, mode=mode)
     nz = ref != 0
