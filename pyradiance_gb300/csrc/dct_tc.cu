@@ -486,6 +486,22 @@ k_dct_tc(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUten
         long long cl = 0;
         bool ok = true;
         for (long long t = unit0; t < s.units && ok; t += ustride) {
+            /* the tile's rows, columns and scale exponents, loaded now so
+             * that their latency hides behind the products */
+            int c, mi, ni;
+            tile_coords<CL>(s, t, c, mi, ni);
+            mi = mi * CL + rank;
+            const int row0 = mi * TM + sub * 32, ir = row0 + lane;
+            const int my_ea = (ir < s.M && s.scaled) ? ea[(long long)c * s.M + ir] : 0;
+            const int nrows = min(32, s.M - row0);
+            const int jc0 = ni * TN + half * EPI_COLS;
+            int ncol[EPI_COLS / 32], ecol[EPI_COLS / 32];   /* per block: this lane's column, its exponent */
+#pragma unroll
+            for (int b = 0; b < EPI_COLS / 32; b++) {
+                const int jc = jc0 + b * 32 + lane;
+                ncol[b] = jc < s.Nc ? colidx[jc] : -1;
+                ecol[b] = (jc < s.Nc && s.scaled) ? eb[(long long)c * s.Nc + jc] : 0;
+            }
             float acc[EPI_COLS];
 #pragma unroll
             for (int i = 0; i < EPI_COLS; i++)
@@ -514,15 +530,8 @@ k_dct_tc(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUten
             }
             if (!ok)
                 break;
-            int c, mi, ni;
-            tile_coords<CL>(s, t, c, mi, ni);
-            mi = mi * CL + rank;
             /* this warp's 32 rows: lane r holds row r's scale exponent,
              * broadcast below */
-            const int row0 = mi * TM + sub * 32, ir = row0 + lane;
-            const int my_ea = (ir < s.M && s.scaled) ? ea[(long long)c * s.M + ir] : 0;
-            const int nrows = min(32, s.M - row0);
-            const int jc0 = ni * TN + half * EPI_COLS;
 #pragma unroll
             for (int b = 0; b < EPI_COLS / 32; b++) {
                 /* lane = row, i = column -> xs[row][i ^ row]: no bank conflicts */
@@ -530,10 +539,9 @@ k_dct_tc(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUten
                 for (int i = 0; i < 32; i++)
                     xs[lane * 32 + (i ^ lane)] = acc[b * 32 + i];
                 __syncwarp();
-                const int jc = jc0 + b * 32 + lane;       /* this lane's compact column */
-                const bool colok = jc < s.Nc;
-                const int n = colok ? colidx[jc] : 0;
-                const int ebn = (colok && s.scaled) ? eb[(long long)c * s.Nc + jc] : 0;
+                const bool colok = ncol[b] >= 0;         /* this lane's compact column exists */
+                const int n = colok ? ncol[b] : 0;
+                const int ebn = ecol[b];
                 float *out = C + ((long long)row0 * s.N + n) * 3 + c;
                 const long long rstride = 3LL * s.N;
                 for (int r = 0; r < nrows; r++, out += rstride) {
