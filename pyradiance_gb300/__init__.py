@@ -398,43 +398,63 @@ class Rcontrib:
         """rcontrib's output streams (rt/rc2.c:131-250 getostream): the
         modifiers without an output specification go to the returned bytes,
         the others to files named by their specification (%s: the
-        modifier), each stream with its own header; an existing file is an
-        error, as rcontrib does not overwrite without -fo."""
+        modifier; %d and the like: one file per bin), each stream with its
+        own header; an existing file is an error, as rcontrib does not
+        overwrite without -fo."""
         from .rflux import _nbins_each
-        streams: list[tuple[str | None, list[int]]] = []
+        nb = _nbins_each(self.mods)
+        start = np.concatenate([[0], np.cumsum(nb)]).astype(int)
+        # streams: (file name or None, [(modifier, bin or None)]); rt/rc2.c:41-97 ofname:
+        # at most one %s (the modifier) and one %d-like (the bin) in a specification
+        streams: list[tuple[str | None, list]] = []
         for i, m in enumerate(self.mods):
             spec = m.get("output")
-            if spec is not None and re.search(r"%[0-9]*d", spec):
-                raise GbError(-3, f"per-bin output files ({spec}) are not supported")
-            name = None if spec is None else (spec.replace("%s", m["modifier"]) if "%s" in spec else spec)
-            for nm, idx in streams:
-                if nm == name:
-                    idx.append(i)
-                    break
-            else:
-                streams.append((name, [i]))
+            conv = re.findall(r"%[0-9]*([a-zA-Z%])", spec) if spec is not None else []
+            conv = [c for c in conv if c != "%"]
+            if any(c not in "sdioxX" for c in conv) or conv.count("s") > 1 or \
+                    sum(c in "dioxX" for c in conv) > 1:
+                raise GbError(-1, f"bad output format '{spec}'")
+            per_bin = any(c in "dioxX" for c in conv)
+            for b in (range(int(nb[i])) if per_bin else [None]):
+                if spec is None:
+                    name = None
+                elif per_bin:
+                    name = spec % ((m["modifier"], b) if "s" in conv and conv.index("s") == 0 else
+                                   ((b, m["modifier"]) if "s" in conv else (b,)))
+                else:
+                    name = spec % (m["modifier"],) if "s" in conv else spec
+                for nm, idx in streams:
+                    if nm == name:
+                        idx.append((i, b))
+                        break
+                else:
+                    streams.append((name, [(i, b)]))
         for name, _ in streams:
             if name is not None and Path(name).exists():
                 raise GbError(-2, f"cannot open '{name}' for writing")
         arr = self.run_array()
         opts = self._opts
         fout = opts.fout.decode()
-        nb = _nbins_each(self.mods)
-        start = np.concatenate([[0], np.cumsum(nb)]).astype(int)
         result = b""
         for name, idx in streams:
-            cols = np.concatenate([arr[:, start[i]:start[i + 1]] for i in idx], axis=1)
+            cols = np.concatenate([arr[:, start[i]:start[i + 1]] if b is None else arr[:, start[i] + b:start[i] + b + 1]
+                                   for i, b in idx], axis=1)
             parts = []
+            i0, b0 = idx[0]
+            spec = self.mods[i0].get("output")
             if opts.h:
                 extra = []
-                spec = self.mods[idx[0]].get("output")
                 if name is not None and ((spec is not None and "%s" in spec) or cols.shape[1] == 1):
-                    extra.append(f"MODIFIER={self.mods[idx[0]]['modifier']}")
+                    extra.append(f"MODIFIER={self.mods[i0]['modifier']}")
+                if name is not None and b0 is not None:
+                    extra.append(f"BIN={b0}")
                 if opts.y > 0:
                     extra.append(f"NROWS={opts.y * max(opts.x, 1)}")
                 if opts.x <= 0 or cols.shape[1] > 1:
                     extra.append(f"NCOLS={cols.shape[1]}")
                 parts.append(_header("rcontrib", self.args + self.mod_args, self.octree, fout, 3, extra))
+            if cols.shape[1] == 1 and opts.x > 0 and opts.y > 0:     # rt/rc2.c:129-134 printresolu
+                parts.append(f"-Y {opts.y} +X {opts.x}\n".encode())
             if fout == "a":
                 parts.append("".join(_ascii_rows(cols.reshape(cols.shape[0], -1), end="\t\n")).encode())
             else:

@@ -14,9 +14,9 @@ klems_quarter.cal, built into the bin compiler), Reinhart (``h=r``,
 ``h=rN``), Shirley-Chiu (``h=scN``, util/disk2square.cal's scbin, built
 in) and, for receivers, the CIE sky scanner (``h=cie``, util/cieskyscan.cal's
 cbin, built in).  Bin jitter (``-bj``) is passed to the bin parameters
-as ``JTR`` as rfluxmtx passes it (none of these bases reads it).  Per-bin
-output files (``o=`` with ``%d``) raise ``RuntimeError``; receivers with
-``o=`` write their columns to that file.
+as ``JTR`` as rfluxmtx passes it (none of these bases reads it).
+Receivers with ``o=`` write their columns to that file (``%s``: the
+modifier; ``%d``: one file per bin).
 """
 from __future__ import annotations
 
@@ -219,9 +219,7 @@ def _receivers(path, jitter: str | None = None) -> list[dict]:
     specs, ospec = [], None
     for mod, p in groups:
         if p.outfn is not None:                 # rcontrib -o: this and the following modifiers
-            ospec = p.outfn
-            if "%d" in ospec or "%i" in ospec:
-                raise GbError(-3, f"per-bin output files (o={ospec}) are not supported")
+            ospec = p.outfn                     # (%s the modifier, %d one file per bin)
         if not p.hemis:
             raise GbError(-1, "missing hemisphere sampling type!")
         if not p.surfs:

@@ -688,6 +688,11 @@ def bytes_surface(tmp: Path) -> None:
         rc.add_modifier(modifier="groundglow").add_modifier(**sky, output="sky_%s.mtx")
         c2_split = rc()
         c2_file = (tmp / "sky_skyglow.mtx").read_bytes()
+        rc = rt.Rcontrib(w.rays_ascii(rays2), str(c2oct), params=rcp)
+        rc.add_modifier(modifier="groundglow").add_modifier(**sky, output="bin_%s_%03d.mtx")
+        c2_binsplit = rc()
+        bin_files = sorted(tmp.glob("bin_skyglow_*.mtx"))
+        c2_bins = b"\0".join(f.name.encode() + b"\n" + f.read_bytes() for f in bin_files)
     finally:
         os.chdir(cwd)
     g = np.load(OUT / "dct_small.npz")
@@ -699,7 +704,8 @@ def bytes_surface(tmp: Path) -> None:
     u8 = lambda b: np.frombuffer(b, dtype=np.uint8)
     np.savez_compressed(OUT / "bytes_surface.npz", c1_oct=u8(c1oct.read_bytes()), c2_oct=u8(c2oct.read_bytes()),
                         rays1=rays1, rays2=rays2, c1_a=u8(c1_a), c1_d=u8(c1_d), c1_s=u8(c1_s), c2_out=u8(c2_out),
-                        c2_split=u8(c2_split), c2_file=u8(c2_file), dct_a=u8(dct_a), dct_d=u8(dct_d),
+                        c2_split=u8(c2_split), c2_file=u8(c2_file), c2_binsplit=u8(c2_binsplit),
+                        c2_bins=u8(c2_bins), dct_a=u8(dct_a), dct_d=u8(dct_d),
                         params1=np.array(params1), rcp=np.array(rcp))
     print("bytes_surface: rtrace %d/%d/%d bytes, rcontrib %d (+ %d in a file), dctimestep %d/%d bytes" %
           (len(c1_a), len(c1_d), len(c1_s), len(c2_out), len(c2_file), len(dct_a), len(dct_d)))

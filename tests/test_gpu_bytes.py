@@ -132,6 +132,23 @@ def test_rcontrib_modifier_output_file(env, monkeypatch):
         _rc(gb, g, d, output="sky_%s.mtx")()
 
 
+def test_rcontrib_per_bin_output_files(env, monkeypatch):
+    """add_modifier(output="bin_%s_%03d.mtx") (rt/rc2.c:41-97 ofname): one
+    file per sky bin, named with the modifier and the bin, each with its
+    own header (MODIFIER=, BIN=, NCOLS=1) and its column; the returned
+    bytes keep the ground's column."""
+    gb, g, d = env
+    wd = d / "bins"
+    wd.mkdir(exist_ok=True)
+    monkeypatch.chdir(wd)
+    compare(_rc(gb, g, d, output="bin_%s_%03d.mtx")(), g["c2_binsplit"].tobytes())
+    ref = dict(part.split(b"\n", 1) for part in g["c2_bins"].tobytes().split(b"\0"))
+    ours = sorted(wd.glob("bin_skyglow_*.mtx"))
+    assert [f.name.encode() for f in ours] == sorted(ref)
+    for f in ours:
+        compare(f.read_bytes(), ref[f.name.encode()])
+
+
 def test_dctimestep_bytes(env):
     gb, g, d = env
     m = golden("dct_small.npz")
