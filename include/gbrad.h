@@ -111,6 +111,17 @@ int  gb_opts_parse(int argc, const char *const *argv, int prog, gb_opts *out, in
 int  gb_rtrace(gb_scene *scene, const gb_opts *opts, const double *org_dir, int64_t n,
                double *out_rgb, int32_t *hit_id, double *hit_t);
 
+/* First hits with their surface normals, for rtrace's -oN and -on: for
+ * each ray the object hit (-1 none), its distance (1e10 none), the
+ * surface's normal at the hit as the object defines it (hit_normal, n x 3:
+ * -oN, rt/rtrace.c:787-804) and, if hit_pnormal is not null, the shading
+ * normal (-on, :807-820: turned toward the ray where the material turns a
+ * surface hit from behind); zero where nothing is hit or a source at
+ * infinity is.  The casts are those of gb_rtrace's hit ids (FP64).
+ * Replaces: the -on/-oN columns of rt/rtrace.c:274-345. */
+int  gb_rtrace_hits(gb_scene *scene, const gb_opts *opts, const double *org_dir, int64_t n, int32_t *hit_id,
+                    double *hit_t, double *hit_normal, double *hit_pnormal);
+
 /* The values of gb_rtrace for rays already in device memory (d_org_dir:
  * n x 6 doubles; d_rgb: n x 3 doubles, overwritten), allocating no device
  * memory.  For callers that cannot allocate while they run: a service that

@@ -133,7 +133,7 @@ def _fmt_values(vals: np.ndarray, fmt: str) -> bytes:
 
 # ------------------------------------------------------------------ rtrace
 
-_CAST_ONLY = set("odLpNsmMw~")
+_CAST_ONLY = set("odLpNnsmMw~")
 
 
 def _rtrace(rays: bytes, octree, header: bool = True, inform: str = "a", outform: str = "a",
@@ -203,6 +203,14 @@ def _rtrace(rays: bytes, octree, header: bool = True, inform: str = "a", outform
         vals[good] = gv
     hit[good] = gh
     hitt[good] = gt
+    nrm_geo = nrm_shade = None
+    if any(ch in "nN" for ch in spec):           # first-hit normals (rt/rtrace.c:787-820 oputN, oputn)
+        nrm_geo, nrm_shade = np.zeros((n, 3)), np.zeros((n, 3))
+        gN, gn = np.zeros((ng, 3)), np.zeros((ng, 3))
+        gh2, gt2 = np.zeros(ng, dtype=np.int32), np.zeros(ng)
+        if ng:
+            check(lib().gb_rtrace_hits(sc.handle, opts, ptr(rr), ng, ptr(gh2), ptr(gt2), ptr(gN), ptr(gn)))
+        nrm_geo[good], nrm_shade[good] = gN, gn
     out = []
     ncomp = 0                                    # rt/rtrace.c:244-370 setrtoutput
     for ch in spec:
@@ -239,6 +247,10 @@ def _rtrace(rays: bytes, octree, header: bool = True, inform: str = "a", outform
             items.append(names)
         elif ch == "w":
             items.append(np.ones((n, 1)))
+        elif ch == "N":
+            items.append(nrm_geo)
+        elif ch == "n":
+            items.append(nrm_shade)
         else:
             raise GbError(-3, f"output option -o{ch} is not supported")
     if fout == "a":

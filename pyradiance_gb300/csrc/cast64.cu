@@ -634,7 +634,7 @@ __device__ int cast_source64(const gb_dscene &S, const double dir[3])
     return glowsrc >= 0 ? S.src[glowsrc].so : -1;
 }
 
-__global__ void k_cast64(gb_run P, int *hit_obj, float *hit_t, float *hit_pn)
+__global__ void k_cast64(gb_run P, int *hit_obj, float *hit_t, double *hit_pn)
 {
     for (long long s = blockIdx.x * (long long)blockDim.x + threadIdx.x; s < P.nsensors;
          s += (long long)gridDim.x * blockDim.x) {
@@ -668,16 +668,16 @@ __global__ void k_cast64(gb_run P, int *hit_obj, float *hit_t, float *hit_pn)
         if (hit_t)
             hit_t[s] = (float)t;
         if (hit_pn) {
-            float *o = hit_pn + 6 * s;
+            double *o = hit_pn + 6 * s;
             for (int i = 0; i < 3; i++) {
-                o[i] = (float)p[i];
-                o[3 + i] = (float)n[i];
+                o[i] = p[i];
+                o[3 + i] = n[i];
             }
         }
     }
 }
 
-int gb_launch_cast64(const gb_run *P, int *hit_obj, float *hit_t, float *hit_pn, cudaStream_t st, int sms)
+int gb_launch_cast64(const gb_run *P, int *hit_obj, float *hit_t, double *hit_pn, cudaStream_t st, int sms)
 {
     long long g = (P->nsensors + 127) / 128;
     if (g > (long long)sms * 8)

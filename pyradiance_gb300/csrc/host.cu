@@ -109,7 +109,7 @@ struct gb_scene {
     DevBuf kids, setdata, obj, geo, fvert, fv4, cone, matd, srcd, trk, instd, orec, oslot, g64, g64off;
     gb_dscene ds;
     /* work buffers */
-    DevBuf sensors, value, bins, stats, roots, rootspt, qa, qb, qcount, binprog, modinfo, hits, hitt, trkrun,
+    DevBuf sensors, value, bins, stats, roots, rootspt, qa, qb, qcount, binprog, modinfo, hits, hitt, hitpn, trkrun,
         hitrec, adja, adjb, dlde, gradd, rootdraw, rootlot, tga, tgb, ssval, sscnt, sserr, slow;
     cudaStream_t stream = nullptr;
     int sms = 0;
@@ -1279,6 +1279,7 @@ struct RunOut {
     double *hit_t;
     const double *dlde;     /* gradient runs: host n x 3 d(loss)/d(value) */
     double *grad;           /* gradient runs: host nslots x 3 */
+    double *hit_normal;     /* host n x 3 or null: the first hit's surface normal */
 };
 
 /* largest generation and queue capacity of the last run on this thread */
@@ -1364,19 +1365,28 @@ static int run(gb_scene *G, const gb_opts *o, int follow, const double *org_dir,
         if (G->hits.ensure((size_t)n * sizeof(int)) < 0 || G->hitt.ensure((size_t)n * sizeof(float)) < 0)
             return set_err(GB_ENOMEM, "device allocation failed");
         P.S.trk = nullptr;
+        if (out.hit_normal && G->hitpn.ensure((size_t)n * 6 * sizeof(double)) < 0)
+            return set_err(GB_ENOMEM, "device allocation failed");
+        double *d_pn = out.hit_normal ? (double *)G->hitpn.p : nullptr;
         int rc = launch(GB_K_CAST, P, [&](gb_run &R) {
-            return gb_launch_cast64(&R, (int *)G->hits.p, (float *)G->hitt.p, nullptr, st, G->sms); });
+            return gb_launch_cast64(&R, (int *)G->hits.p, (float *)G->hitt.p, d_pn, st, G->sms); });
         if (rc < 0)
             return rc;
         std::vector<int> h(n);
         std::vector<float> t(n);
+        std::vector<double> pn(out.hit_normal ? (size_t)n * 6 : 0);
         CK(cudaMemcpyAsync(h.data(), G->hits.p, (size_t)n * sizeof(int), cudaMemcpyDeviceToHost, st));
         CK(cudaMemcpyAsync(t.data(), G->hitt.p, (size_t)n * sizeof(float), cudaMemcpyDeviceToHost, st));
+        if (d_pn)
+            CK(cudaMemcpyAsync(pn.data(), d_pn, (size_t)n * 6 * sizeof(double), cudaMemcpyDeviceToHost, st));
         CK(cudaStreamSynchronize(st));
         for (int64_t i = 0; i < n; i++) {
             out.hit_id[i] = h[i];
             if (out.hit_t)
                 out.hit_t[i] = t[i];
+            if (out.hit_normal)
+                for (int k = 0; k < 3; k++)
+                    out.hit_normal[3 * i + k] = pn[6 * i + 3 + k];
         }
         if (!out.value && !out.bins) {
             g_stats[0] = n;
@@ -1713,6 +1723,7 @@ static int run_sliced(gb_scene *G, const gb_opts *o, int follow, const double *o
         if (out.bins) so.bins = out.bins + (size_t)(b / acc) * nbins_total * 3;
         if (out.hit_id) so.hit_id = out.hit_id + b;
         if (out.hit_t) so.hit_t = out.hit_t + b;
+        if (out.hit_normal) so.hit_normal = out.hit_normal + 3 * b;
         if (grad) {
             so.dlde = out.dlde + 3 * b;
             so.grad = gpart.data();
@@ -1740,7 +1751,7 @@ extern "C" int gb_rtrace(gb_scene *G, const gb_opts *o, const double *org_dir, i
         if (rc < 0)
             return rc;
     }
-    RunOut out = {out_rgb, nullptr, hit_id, hit_t, nullptr, nullptr};
+    RunOut out = {out_rgb, nullptr, hit_id, hit_t, nullptr, nullptr, nullptr};
     double per = 0.0;
     int rc = GB_OK;
     for (int attempt = 0; attempt < 4; attempt++) {
@@ -1750,6 +1761,37 @@ extern "C" int gb_rtrace(gb_scene *G, const gb_opts *o, const double *org_dir, i
         per = 2 * (per > 0 ? per : slots_per_sensor(G, o));   /* a larger queue, fewer sensors per slice */
     }
     return rc;
+}
+
+extern "C" int gb_rtrace_hits(gb_scene *G, const gb_opts *o, const double *org_dir, int64_t n, int32_t *hit_id,
+                              double *hit_t, double *hit_normal, double *hit_pnormal)
+{
+    if (!G || !o || (n > 0 && (!org_dir || !hit_id || !hit_normal)))
+        return set_err(GB_EINVAL, "null argument");
+    RunOut out = {nullptr, nullptr, hit_id, hit_t, nullptr, nullptr, hit_normal};
+    int rc = run_sliced(G, o, 0, org_dir, n, nullptr, nullptr, 0, nullptr, out, 0.0);
+    if (rc < 0 || !hit_pnormal)
+        return rc;
+    /* the shading normal (rt/rtrace.c:807-820 oputn): plastic, metal,
+     * trans (rt/normal.c:200-207, with back faces visible) and glass
+     * (rt/glass.c:88-89) turn a surface hit from behind toward the ray
+     * (flipsurface); the other materials leave it */
+    for (int64_t i = 0; i < n; i++) {
+        const double *N = hit_normal + 3 * i, *d = org_dir + 6 * i + 3;
+        double *pn = hit_pnormal + 3 * i;
+        double dl = sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+        double rod = dl > 0 ? -(d[0] * N[0] + d[1] * N[1] + d[2] * N[2]) / dl : 0.0;
+        bool flip = false;
+        const int32_t h = hit_id[i];
+        if (h >= 0 && h < G->H.nobjs && rod < 0.0) {
+            const int32_t m = gb_find_material(&G->H, h);
+            const int t = m >= 0 ? G->H.objs[m].otype : -1;
+            flip = t == GT_GLASS || (o->bv && (t == GT_PLASTIC || t == GT_METAL || t == GT_TRANS));
+        }
+        for (int k = 0; k < 3; k++)
+            pn[k] = flip ? -N[k] : N[k];
+    }
+    return GB_OK;
 }
 
 extern "C" int gb_rtrace_grad(gb_scene *G, const gb_opts *o, const double *org_dir, int64_t n,
@@ -1770,7 +1812,7 @@ extern "C" int gb_rtrace_grad(gb_scene *G, const gb_opts *o, const double *org_d
     memset(grad, 0, (size_t)nslots * 3 * sizeof(double));
     if (nslots == 0)
         return GB_OK;
-    RunOut out = {nullptr, nullptr, nullptr, nullptr, dl_dvalue, grad};
+    RunOut out = {nullptr, nullptr, nullptr, nullptr, dl_dvalue, grad, nullptr};
     return run_sliced(G, o, 0, org_dir, n, nullptr, nullptr, 0, nullptr, out, 0.0);
 }
 

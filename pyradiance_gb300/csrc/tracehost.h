@@ -135,7 +135,7 @@ typedef struct {
 
 int gb_launch_cast(const gb_run *P, int *hit_obj, float *hit_t, float *hit_pn, cudaStream_t st, int sms);
 /* the same first hits in FP64 (cast64.cu) */
-int gb_launch_cast64(const gb_run *P, int *hit_obj, float *hit_t, float *hit_pn, cudaStream_t st, int sms);
+int gb_launch_cast64(const gb_run *P, int *hit_obj, float *hit_t, double *hit_pn, cudaStream_t st, int sms);
 int gb_launch_root(const gb_run *P, cudaStream_t st, int sms);
 /* -I roots with root_n >= 4: the strata's draws and the lots in parallel,
  * then the sequential placement per sensor */

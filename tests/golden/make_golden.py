@@ -130,6 +130,32 @@ def zoo(tmp: Path) -> None:
                                                                    "west", "light")) for n in hit))
 
 
+def normals(tmp: Path) -> None:
+    """First-hit normals (rt/rtrace.c:787-820 oputN, oputn): the surface's
+    own normal (-oN) and the shading normal turned toward the ray by the
+    material (-on) of random rays in the shape zoo (every primitive, plastic
+    and metal), the instances room (transformed octrees) and rays through
+    the window room's glass from both sides."""
+    out = {}
+    rng = np.random.default_rng(21)
+    x0, x1, z0, z1 = w.WINDOW
+    tgt = np.column_stack([rng.uniform(x0 + .05, x1 - .05, 400), np.zeros(400), rng.uniform(z0 + .05, z1 - .05, 400)])
+    org = np.vstack([rng.uniform((1.0, 1.0, 0.5), (9.0, 5.0, 2.5), (200, 3)),
+                     rng.uniform((1.0, -6.0, 0.5), (9.0, -1.0, 2.5), (200, 3))])
+    d = tgt - org
+    cases = {"zoo": (oconv(w.shape_zoo(), tmp, "nzoo"), w.random_rays(3000, seed=4)),
+             "win": (oconv(w.window_room(ntri=0), tmp, "nwin"), np.hstack([org, d / np.linalg.norm(d, axis=1,
+                                                                                          keepdims=True)]))}
+    for key, (octp, rays) in cases.items():
+        inp = rays.astype("<f8").tobytes()
+        v = np.frombuffer(run(["rtrace", "-h", "-u-", "-ab", "0", "-fdd", "-oNn", octp], inp),
+                          dtype="<f8").reshape(-1, 6)
+        out[f"{key}_rays"], out[f"{key}_N"], out[f"{key}_n"] = rays, v[:, :3], v[:, 3:]
+        print("normals %s: %d rays, %d flipped" % (key, len(rays), (np.abs(v[:, :3] + v[:, 3:]).sum(1) < 1e-9).sum()
+                                                     - (np.abs(v[:, :3]).sum(1) == 0).sum()))
+    np.savez_compressed(OUT / "normals.npz", **out, cmd="rtrace -h -u- -ab 0 -fdd -oNn")
+
+
 def glossy(tmp: Path, n: int = 300, K: int = 1024) -> None:
     """Rough specular plastic and metal (glossy_room), radiance of view rays
     from random interior points: deterministic with -st 1 (every rough lobe
@@ -905,7 +931,7 @@ def main() -> None:
     if not (BIN / "rtrace").exists():
         sys.exit("reference programs missing: make -f oracle/build_ref.mk REF=/root/reference -j8")
     parts = {"octree": octree_digests, "c1": c1_direct, "c1p": c1_partitioned, "zoo": zoo, "glossy": glossy, "irr": surface_irradiance,
-             "ss": supersampled_irradiance, "inst": instances, "mesh": meshes, "circ": circular_sources,
+             "ss": supersampled_irradiance, "normals": normals, "inst": instances, "mesh": meshes, "circ": circular_sources,
              "trans": translucent, "bins": general_bins, "cbins": cie_bins,
              "spot": spotlights, "mirror": mirrors, "flux": flux_matrices, "flux_sc": flux_shirchiu,
              "dct": lambda tmp: dct_small(), "dct4": lambda tmp: dct_four(), "rmtxop": lambda tmp: rmtxop_cases(), "rmtxop_chains": lambda tmp: rmtxop_chains(), "btdf": lambda tmp: btdf_matrices(), "trace_oct": lambda tmp: ref_fixture_trace(),

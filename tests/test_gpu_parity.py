@@ -155,6 +155,24 @@ def test_glossy_lobe_statistics_vs_reference(gb, scenes, key, kw):
     assert np.abs(z).max() < 5 and abs(z.mean()) < 4 / np.sqrt(n)
 
 
+def test_first_hit_normals(gb, scenes, tmp_path):
+    """rtrace -oN and -on (rt/rtrace.c:787-820) through the drop-in: the
+    surface's own normal at the first hit (FP64 casts) and the shading
+    normal, turned toward the ray where plastic, metal, trans or glass meet
+    a surface from behind, for every primitive of the shape zoo and for rays
+    through the window glass from both sides: the reference's within 1e-6."""
+    from pyradiance_gb300 import workloads as w
+    g = golden("normals.npz")
+    (tmp_path / "win.rad").write_text(w.window_room(ntri=0))
+    for key, sc in (("zoo", scenes["zoo"]), ("win", gb.Scene(rad_files=[tmp_path / "win.rad"]))):
+        rays = g[f"{key}_rays"]
+        out = gb.rtrace(rays.astype("<f8").tobytes(), sc, params=["-ab", "0"], inform="d", outform="d",
+                        outspec="Nn", header=False)
+        v = np.frombuffer(out, dtype="<f8").reshape(-1, 6)
+        np.testing.assert_allclose(v[:, :3], g[f"{key}_N"], rtol=1e-6, atol=1e-6, err_msg=key)
+        np.testing.assert_allclose(v[:, 3:], g[f"{key}_n"], rtol=1e-6, atol=1e-6, err_msg=key)
+
+
 def test_zoo_all_primitives(gb, scenes):
     g = golden("zoo.npz")
     sc = scenes["zoo"]
