@@ -133,7 +133,7 @@ def _fmt_values(vals: np.ndarray, fmt: str) -> bytes:
 
 # ------------------------------------------------------------------ rtrace
 
-_CAST_ONLY = set("odLpNnsmMw~")
+_CAST_ONLY = set("odLpNnsmMwW~")
 
 
 def _rtrace(rays: bytes, octree, header: bool = True, inform: str = "a", outform: str = "a",
@@ -214,8 +214,8 @@ def _rtrace(rays: bytes, octree, header: bool = True, inform: str = "a", outform
     out = []
     ncomp = 0                                    # rt/rtrace.c:244-370 setrtoutput
     for ch in spec:
-        ncomp += {"v": 3, "o": 3, "d": 3, "p": 3, "N": 3, "n": 3, "L": 1, "l": 1, "w": 1, "s": 1, "m": 1,
-                  "M": 1}.get(ch, 0)
+        ncomp += {"v": 3, "V": 3, "W": 3, "o": 3, "d": 3, "p": 3, "N": 3, "n": 3, "L": 1, "l": 1, "w": 1,
+                  "s": 1, "m": 1, "M": 1}.get(ch, 0)
     if opts.h:
         out.append(_header("rtrace", args, octree, fout, ncomp or None))
     unit = np.where(good[:, None], r[:, 3:6] / np.where(dirlen > 0, dirlen, 1)[:, None], 0.0) if n else r[:, 3:6]
@@ -223,7 +223,7 @@ def _rtrace(rays: bytes, octree, header: bool = True, inform: str = "a", outform
     # the output columns in spec order: numeric blocks (n x k) or names (n)
     items = []
     for ch in spec:
-        if ch == "v":
+        if ch in "vV":                              # a primary ray's contribution is its value
             items.append(vals)
         elif ch == "o":
             items.append(r[:, 0:3])
@@ -247,6 +247,8 @@ def _rtrace(rays: bytes, octree, header: bool = True, inform: str = "a", outform
             items.append(names)
         elif ch == "w":
             items.append(np.ones((n, 1)))
+        elif ch == "W":                             # a primary ray's coefficient (rt/rtrace.c:847-860)
+            items.append(np.ones((n, 3)))
         elif ch == "N":
             items.append(nrm_geo)
         elif ch == "n":

@@ -153,7 +153,11 @@ def normals(tmp: Path) -> None:
         out[f"{key}_rays"], out[f"{key}_N"], out[f"{key}_n"] = rays, v[:, :3], v[:, 3:]
         print("normals %s: %d rays, %d flipped" % (key, len(rays), (np.abs(v[:, :3] + v[:, 3:]).sum(1) < 1e-9).sum()
                                                      - (np.abs(v[:, :3]).sum(1) == 0).sum()))
-    np.savez_compressed(OUT / "normals.npz", **out, cmd="rtrace -h -u- -ab 0 -fdd -oNn")
+    zoo_oct, zoo_rays = cases["zoo"]
+    vw = np.frombuffer(run(["rtrace", "-h", "-u-", "-ab", "0", "-dj", "0", "-ds", "0", "-dr", "0", "-dt", "0",
+                            "-fdd", "-oVWv", zoo_oct], zoo_rays[:500].astype("<f8").tobytes()), dtype="<f8")
+    out["zoo_VWv"] = vw.reshape(-1, 9)
+    np.savez_compressed(OUT / "normals.npz", **out, cmd="rtrace -h -u- -ab 0 -fdd -oNn | -dj 0 -ds 0 -dr 0 -dt 0 -oVWv")
 
 
 def glossy(tmp: Path, n: int = 300, K: int = 1024) -> None:

@@ -171,6 +171,16 @@ def test_first_hit_normals(gb, scenes, tmp_path):
         v = np.frombuffer(out, dtype="<f8").reshape(-1, 6)
         np.testing.assert_allclose(v[:, :3], g[f"{key}_N"], rtol=1e-6, atol=1e-6, err_msg=key)
         np.testing.assert_allclose(v[:, 3:], g[f"{key}_n"], rtol=1e-6, atol=1e-6, err_msg=key)
+    # -oV and -oW of primary rays (rt/rtrace.c:734-743, 847-860): the contribution is the value, the
+    # coefficient one, as in the reference's output
+    ref = g["zoo_VWv"]
+    assert (ref[:, :3] == ref[:, 6:]).all() and (ref[:, 3:6] == 1).all()
+    out = gb.rtrace(g["zoo_rays"][:500].astype("<f8").tobytes(), scenes["zoo"], inform="d", outform="d",
+                    outspec="VWv", header=False, params=["-ab", "0", "-dj", "0", "-ds", "0", "-dr", "0", "-dt", "0"])
+    v = np.frombuffer(out, dtype="<f8").reshape(-1, 9)
+    assert (v[:, :3] == v[:, 6:]).all() and (v[:, 3:6] == 1).all()
+    rel = np.abs(v[:, 6:] - ref[:, 6:]).max(1) / np.maximum(np.abs(ref[:, 6:]).max(1), 1e-9)
+    assert (rel <= 1e-4).mean() >= 0.99
 
 
 def test_zoo_all_primitives(gb, scenes):
