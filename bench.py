@@ -388,6 +388,78 @@ def dct_measure(dev, steps: int, rows: int | None = None):
 GRAD_ARGS = ["-I+", "-ab", "2", "-ad", "1024", "-aa", "0", "-as", "0", "-lw", "1e-4", "-u-"]
 
 
+def c1_measure(steps: int):
+    """The deterministic direct-irradiance workload (rtrace -I -ab 0 -dj 0
+    -ds 0 -dr 0 on the 100 x 100 sensor grid of the room of 200 boxes):
+    whole gb_rtrace calls through the C ABI (host rays in, host values and
+    first-hit ids out), best of `steps` after one warm-up, with CUDA events
+    not needed (the call returns when its results are on the host); and
+    the oracle port of rtrace on all host cores on the same sensors (the
+    reference program is not on the GPU host)."""
+    import torch
+    from pyradiance_gb300 import workloads as w
+    from pyradiance_gb300 import _lib
+    from oracle import pyoracle as po
+    L = _lib.lib()
+    with tempfile.TemporaryDirectory() as td:
+        rad = Path(td) / "c1.rad"
+        rad.write_text(w.daylight_room())
+        import pyradiance_gb300 as gb
+        sc = gb.Scene(rad_files=[rad])
+        rays = np.ascontiguousarray(w.sensor_grid(100, 100), dtype=np.float64)
+        n = len(rays)
+        o, _ = _lib.parse_opts(["-I+", "-ab", "0", "-dj", "0", "-ds", "0", "-dr", "0"], _lib.GB_PROG_RTRACE)
+        rgb = np.zeros((n, 3))
+        hid = np.zeros(n, dtype=np.int32)
+        ht = np.zeros(n)
+
+        def call():
+            _lib.check(L.gb_rtrace(sc.handle, o, _lib.ptr(rays), n, _lib.ptr(rgb), _lib.ptr(hid), _lib.ptr(ht)))
+        call()
+        torch.cuda.synchronize()
+        ts = []
+        for _ in range(max(3, steps)):
+            t0 = time.perf_counter()
+            call()
+            ts.append(time.perf_counter() - t0)
+        gpu_s = min(ts)
+        # the same values for rays already in HBM (gb_rtrace_device_noalloc), CUDA events on its stream
+        dev = torch.device("cuda", 0)
+        d_rays = torch.as_tensor(rays, device=dev)
+        d_rgb = torch.zeros(n, 3, dtype=torch.float64, device=dev)
+        st = torch.cuda.current_stream(dev)
+        import ctypes as C
+        dts = []
+        for _ in range(max(3, steps) + 1):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(st)
+            _lib.check(L.gb_rtrace_device_noalloc(sc.handle, o, C.c_void_p(d_rays.data_ptr()), n,
+                                                  C.c_void_p(d_rgb.data_ptr()), C.c_void_p(st.cuda_stream)))
+            e1.record(st)
+            torch.cuda.synchronize(dev)
+            dts.append(e0.elapsed_time(e1))
+        dev_ms = min(dts[1:])
+        threads = os.cpu_count() or 1
+        osc = po.Scene(rad)
+        oo = po.default_opts("rtrace", I=1, ab=0, dj=0, ds=0, dr=0, u=0)
+        t0 = time.perf_counter()
+        po.rtrace(osc, oo, rays, threads=threads)
+        cpu_s = time.perf_counter() - t0
+    return {"workload": "rtrace -I -ab 0 -dj 0 -ds 0 -dr 0: 10,000 sensors (100x100 grid, z=0.8, +z) in a 10x8x3 m "
+                        "room of 200 random boxes (1,200 quads) with a 1x1 m ceiling light; values and first-hit ids",
+            "gpu_ms_per_call": round(gpu_s * 1e3, 3), "gpu_sensors_per_s": round(n / gpu_s),
+            "timing": "whole gb_rtrace call with host buffers (host to device and back inside, values and "
+                      f"first-hit ids), best of {len(ts)}",
+            "gpu_device_ms": round(dev_ms, 3),
+            "device_timing": "values of rays already in HBM (gb_rtrace_device_noalloc), CUDA events, best of "
+                             f"{len(dts) - 1}",
+            "cpu_baseline": {"value_ms": round(cpu_s * 1e3, 1), "cores": threads, "kind": "port",
+                             "sample": "all 10,000 sensors"},
+            "speedup_vs_cpu": round(cpu_s / gpu_s, 1), "speedup_device_vs_cpu": round(cpu_s * 1e3 / dev_ms, 1),
+            "note": "a small workload (about 20,000 rays): the call's fixed costs (copies, launches, two "
+                    "synchronisations: first hits in FP64, then values) dominate it"}
+
+
 def grad_measure(steps: int):
     """Gradient of the MSE between 4,096 sensor irradiances and a target
     map (made by a seed-fixed ground-truth parameter set) with respect to 64
@@ -658,6 +730,7 @@ def gpu_arm(args):
             "clocks": ck,
         }
         if not (args.sensors or args.no_extras):
+            line["c1_rtrace"] = c1_measure(args.steps)
             line["dctimestep"] = dct_measure(dev, args.steps)
             line["gradient"] = grad_measure(args.steps)
             line["batching"] = batch_measure(min(args.steps, 3))
