@@ -23,6 +23,14 @@
  *                                 fv4 of each object in one 64-byte record,
  *                                 in the order the leaves first reach them
  *   oslot     int32[nobjs]        each object's record slot
+ *   wkids     int32[8 * nnodes]   the FP32 walk's copy of kids: full-leaf
+ *                                 codes give the leaf's place in lrec
+ *   lrec      float4[4 * ...]     per leaf set: a header record (first
+ *                                 word: member count), then its members'
+ *                                 64-byte orec records in test order (an
+ *                                 object in several leaves has a copy in
+ *                                 each), so that a leaf's objects are
+ *                                 tested without loading its member list
  *   cone      float[24 * ncones]  3x4 world->canonical transform (rings),
  *                                 axis, base point, length, slant, radii
  *   mat       float4[2 * nmats]   material kind and parameters
@@ -97,7 +105,7 @@ typedef struct {
     float bx[12], fx[12];      /* backward (world -> instance) and forward */
     float bsca, fsca;
     float cuorg[3], cusize, grid_scale, cell;
-    int   root;                /* leaf-coded root code of its octree */
+    int   root;                /* root code of its octree in the walk's copy (wkids, lrec) */
     int   obj;                 /* the instance object */
     int   hasmod;              /* the instance's modifier replaces its surfaces' own */
     int   sidbase;             /* first surface id */
@@ -114,6 +122,12 @@ typedef struct {
     int   nnodes;
     const int   *kids;
     const int   *set_data;
+    /* the FP32 walk's copy of the octree: leaf codes address lrec, where
+     * each leaf set is a header record (first word: its member count)
+     * followed by its members' 64-byte records in test order */
+    int   wroot;
+    const int   *wkids;
+    const float4 *lrec;
     /* objects */
     int   nobjs;
     const int4  *obj;

@@ -99,20 +99,22 @@ struct gb_scene {
     std::vector<int4> hobj;
     std::vector<float4> hgeo;
     std::vector<float2> hfvert;
-    std::vector<float4> hfv4, horec;
+    std::vector<float4> hfv4, horec, hlrec;
+    std::vector<int> hwkids;
     std::vector<int> hoslot;
     std::vector<float> hcone;
     std::vector<gb_dsrc> hsrc;
     std::vector<double> hg64;          /* FP64 geometry of the first-hit casts */
     std::vector<long long> hg64off;
     /* device scene */
-    DevBuf kids, setdata, obj, geo, fvert, fv4, cone, matd, srcd, trk, instd, orec, oslot, g64, g64off;
+    DevBuf kids, setdata, obj, geo, fvert, fv4, cone, matd, srcd, trk, instd, orec, oslot, g64, g64off, wkids, lrec;
     gb_dscene ds;
     /* work buffers */
     DevBuf sensors, value, bins, stats, roots, rootspt, qa, qb, qcount, binprog, modinfo, hits, hitt, hitpn, trkrun,
         hitrec, adja, adjb, dlde, gradd, rootdraw, rootlot, tga, tgb, ssval, sscnt, sserr, slow;
     cudaStream_t stream = nullptr;
     int sms = 0;
+    int wroot = 0;                 /* the walk's root code (wkids, lrec) */
     cudaEvent_t ev[2 * GB_TIMED_LAUNCHES + 2];
     int nev = 0;
     int octree_on_device = 0;          /* the octree was built by the device builder */
@@ -475,11 +477,14 @@ static int prepare_device(gb_scene *G)
         upload(G->orec, G->horec) < 0 || upload(G->oslot, G->hoslot) < 0 ||
         upload(G->obj, G->hobj) < 0 || upload(G->geo, G->hgeo) < 0 || upload(G->fvert, G->hfvert) < 0 ||
         upload(G->fv4, G->hfv4) < 0 || upload(G->cone, G->hcone) < 0 || upload(G->matd, G->mat) < 0 ||
-        upload(G->srcd, G->hsrc) < 0 || upload(G->g64, G->hg64) < 0 || upload(G->g64off, G->hg64off) < 0)
+        upload(G->srcd, G->hsrc) < 0 || upload(G->g64, G->hg64) < 0 || upload(G->g64off, G->hg64off) < 0 ||
+        upload(G->wkids, G->hwkids) < 0 || upload(G->lrec, G->hlrec) < 0)
         return set_err(GB_ENOMEM, "device upload of the scene failed");
     gb_dscene &d = G->ds;
     d.kids = (const int *)G->kids.p;
     d.set_data = (const int *)G->setdata.p;
+    d.wkids = (const int *)G->wkids.p;
+    d.lrec = (const float4 *)G->lrec.p;
     d.obj = (const int4 *)G->obj.p;
     d.geo = (const float4 *)G->geo.p;
     d.fvert = (const float2 *)G->fvert.p;
@@ -725,6 +730,46 @@ static int build_arrays(gb_scene *G)
     }
     if (orec.empty())
         orec.assign(4, make_float4(0, 0, 0, 0));
+    /* the walk's leaf records: per set a header record (its first word the
+     * member count), then the members' records in test order, so that
+     * entering a leaf needs no load of its member list; an object in
+     * several leaves has a record in each */
+    {
+        std::vector<int64_t> woff((size_t)(H.nsets > 0 ? H.nsets : 1), 0);
+        int64_t nrec = 0;
+        for (int32_t k = 0; k < H.nsets; k++) {
+            woff[k] = nrec;
+            nrec += 1 + H.set_data[H.set_off[k]];
+        }
+        if (nrec >= GB_LEAF_MAXOFF)
+            return set_err(GB_EUNSUPPORTED, "octree leaves of %lld object records exceed the %d a leaf code addresses",
+                           (long long)nrec, GB_LEAF_MAXOFF);
+        std::vector<float4> lrec(4 * (size_t)(nrec > 0 ? nrec : 1), make_float4(0, 0, 0, 0));
+        for (int32_t k = 0; k < H.nsets; k++) {
+            const int cnt = setdata[H.set_off[k]];
+            lrec[4 * (size_t)woff[k]] = make_float4(__int_as_float_host(cnt), 0.f, 0.f, 0.f);
+            for (int j = 1; j <= cnt; j++) {
+                const size_t from = 4 * (size_t)setdata[H.set_off[k] + j], to = 4 * (size_t)(woff[k] + j);
+                for (int q = 0; q < 4; q++)
+                    lrec[to + q] = orec[from + q];
+            }
+        }
+        auto wcode = [&](int code) {
+            if (code > -2)
+                return code;
+            const int32_t k = -code - 2;
+            return gb_leaf_code((int)woff[k], setdata[H.set_off[k]]);
+        };
+        std::vector<int> wkids(H.kids, H.kids + 8 * (size_t)H.nnodes);
+        if (wkids.empty()) wkids.assign(8, -1);
+        for (int &k : wkids)
+            k = wcode(k);
+        for (int k = 0; k < H.ninst; k++)
+            G->hinst[k].root = wcode(H.subs[H.inst[k].sub].root);
+        G->wroot = wcode(H.root);
+        G->hlrec.swap(lrec);
+        G->hwkids.swap(wkids);
+    }
     G->horec.swap(orec);
     G->hoslot.swap(slot_of);
     /* FP64 geometry per object for the first-hit casts (cast64.cu) */
@@ -805,6 +850,9 @@ static int build_arrays(gb_scene *G)
     d.nnodes = H.nnodes;
     d.kids = G->hkids.data();
     d.set_data = G->hsetdata.data();
+    d.wroot = G->wroot;
+    d.wkids = G->hwkids.data();
+    d.lrec = G->hlrec.data();
     d.nobjs = H.nobjs;
     d.obj = G->hobj.data();
     d.geo = G->hgeo.data();
@@ -966,7 +1014,7 @@ extern "C" void gb_scene_free(gb_scene *G)
     if (!G)
         return;
     DevBuf *bufs[] = {&G->kids, &G->setdata, &G->instd, &G->orec, &G->oslot, &G->obj, &G->geo, &G->fvert, &G->fv4,
-                      &G->cone, &G->matd, &G->g64, &G->g64off,
+                      &G->cone, &G->matd, &G->g64, &G->g64off, &G->wkids, &G->lrec,
                       &G->srcd, &G->trk, &G->sensors, &G->value, &G->bins, &G->stats, &G->roots, &G->rootspt, &G->qa,
                       &G->qb, &G->qcount, &G->binprog, &G->modinfo, &G->hits, &G->hitt, &G->trkrun, &G->hitrec,
                       &G->adja, &G->adjb, &G->dlde, &G->gradd, &G->rootdraw, &G->rootlot, &G->tga, &G->tgb,

@@ -420,10 +420,9 @@ GB_DFN void hit_record(const gb_dscene &S, int obj, int4 od, float4 pl, float4 v
  * loads issued together.  The object the ray leaves (skip) is not tested,
  * or, when curved, tested with its root at the origin excluded. */
 template <int MODE = WALK_FULL>
-GB_DFN void hit_slot(const gb_dscene &S, int sl, float3 org, float3 dir, Hit &best, float tmin, int skip,
-                     bool curved_skip)
+GB_DFN void hit_rec(const gb_dscene &S, const float4 *rec, float3 org, float3 dir, Hit &best, float tmin, int skip,
+                    bool curved_skip)
 {
-    const float4 *rec = S.orec + 4 * sl;
     const int4 od = GB_LDG(reinterpret_cast<const int4 *>(rec));
     const float4 pl = GB_LDG(rec + 1);
     const float4 va = GB_LDG(rec + 2), vb = GB_LDG(rec + 3);
@@ -432,6 +431,13 @@ GB_DFN void hit_slot(const gb_dscene &S, int sl, float3 org, float3 dir, Hit &be
         hit_record<MODE>(S, obj, od, pl, va, vb, org, dir, best, tmin, false, skip);
     else if (curved_skip)                        /* curved origin surface */
         hit_record<MODE>(S, obj, od, pl, va, vb, org, dir, best, tmin, true, skip);
+}
+
+template <int MODE = WALK_FULL>
+GB_DFN void hit_slot(const gb_dscene &S, int sl, float3 org, float3 dir, Hit &best, float tmin, int skip,
+                     bool curved_skip)
+{
+    hit_rec<MODE>(S, S.orec + 4 * sl, org, dir, best, tmin, skip, curved_skip);
 }
 
 /* the test of object obj (by index) */
@@ -468,7 +474,7 @@ struct Walk {
     bool curved_skip, leaf;
     int q[3];                     /* integer position on the 2^24 grid */
     int rl, k, cnt, span, ax;     /* restart level; leaf set cursor; cube size; exit axis */
-    int set;                      /* current leaf set: offset into set_data */
+    int set;                      /* current leaf: its header record in lrec */
     float texit;
     Hit best;
     uint32_t steps, nodes, tests;
@@ -487,7 +493,7 @@ struct TopCube {                /* (holds nothing: the scene header is read in p
     GB_DFN float size(const gb_dscene &S) const { return S.cusize; }
     GB_DFN float gscale(const gb_dscene &S) const { return S.grid_scale; }
     GB_DFN float cell(const gb_dscene &S) const { return S.cell; }
-    GB_DFN int root(const gb_dscene &S) const { return S.root; }
+    GB_DFN int root(const gb_dscene &S) const { return S.wroot; }
 };
 
 /* the scene's cube, instances deferred */
@@ -614,9 +620,9 @@ GB_DFN bool walk_iter(const gb_dscene &S, const Cube &C, Walk &W, Stack &stk)
     for (int u = 0; u < WALK_TESTS; u++) {
         if (W.k > W.cnt)
             break;
-        const int sl = GB_LDG(S.set_data + W.set + W.k);
+        const float4 *rec = S.lrec + 4 * (W.set + W.k);
         W.k++;
-        hit_slot<Cube::mode>(S, sl, W.org, W.dir, W.best, D_FTINY, W.skip, W.curved_skip);
+        hit_rec<Cube::mode>(S, rec, W.org, W.dir, W.best, D_FTINY, W.skip, W.curved_skip);
     }
     if (W.k <= W.cnt)
         return false;
@@ -653,7 +659,7 @@ GB_DFN bool walk_iter(const gb_dscene &S, const Cube &C, Walk &W, Stack &stk)
     while (node >= 0) {
         int sh = GRID_BITS - 1 - level;
         int br = ((W.q[0] >> sh) & 1) | (((W.q[1] >> sh) & 1) << 1) | (((W.q[2] >> sh) & 1) << 2);
-        node = GB_LDG(S.kids + 8 * node + br);
+        node = GB_LDG(S.wkids + 8 * node + br);
         stk[++level] = node;
         W.nodes++;
     }
@@ -680,7 +686,7 @@ GB_DFN bool walk_iter(const gb_dscene &S, const Cube &C, Walk &W, Stack &stk)
         W.set = code >> GB_LEAF_SIZEBITS;
         W.cnt = code & ((1 << GB_LEAF_SIZEBITS) - 1);
         if (W.cnt == (1 << GB_LEAF_SIZEBITS) - 1)
-            W.cnt = GB_LDG(S.set_data + W.set);
+            W.cnt = GB_LDG(reinterpret_cast<const int *>(S.lrec + 4 * W.set));
         W.tests += W.cnt;
     }
     return false;
