@@ -13,6 +13,9 @@ value   device throughput: rays / (CUDA-event time of the kernel region on the
         library's stream), inputs and outputs resident in HBM;
 e2e     the same through the C ABI with host buffers (sensor upload and
         bin download inside the timed region), wall clock per call;
+e2e_bytes  the same through the pyradiance byte surface, Rcontrib(...)():
+        rays parsed from bytes, output formatted to bytes (ASCII, and
+        double in / float out);
 L2 is flushed (256 MB write) before every timed step.  Multi-GPU runs shard
 independent sensor replicas across ranks (weak scaling, no data collective).
 """
@@ -460,6 +463,38 @@ def c1_measure(steps: int):
                     "synchronisations: first hits in FP64, then values) dominate it"}
 
 
+def bytes_measure(sc, rays, steps: int):
+    """The headline workload through the pyradiance byte surface: rays as
+    bytes in, the rcontrib output as bytes out (Rcontrib(...)() as a
+    pyradiance user calls it), ASCII both ways (the default) and double in,
+    float out (-fdf); whole calls timed on the host, best of `steps` after
+    one warm-up, rays from the library's counters."""
+    import pyradiance_gb300 as gb
+    from pyradiance_gb300 import _lib
+    res = {}
+    forms = {"ascii": (None, None, "".join(f"{a:.9g} {b:.9g} {c:.9g} {d:.9g} {e:.9g} {f:.9g}\n"
+                                           for a, b, c, d, e, f in rays).encode()),
+             "binary": ("d", "f", np.ascontiguousarray(rays, dtype="<f8").tobytes())}
+    for name, (fi, fo, inp) in forms.items():
+        rc = gb.Rcontrib(inp, sc, inform=fi, outform=fo, params=PARAMS)
+        for m in MODS:
+            rc.add_modifier(**m)
+        rc.seed = 20261203
+        out = rc()
+        ts = []
+        for _ in range(max(3, steps)):
+            t0 = time.perf_counter()
+            out = rc()
+            ts.append(time.perf_counter() - t0)
+        best = min(ts)
+        nray = _lib.last_stats()["rays"]
+        res[name] = {"mrays_s": round(nray / best / 1e6, 1), "s_per_call": round(best, 4),
+                     "in_bytes": len(inp), "out_bytes": len(out)}
+    res["note"] = ("Rcontrib(inp, scene, inform, outform, params)() with the headline modifiers: the input parsed, "
+                   "the GPU run, the output formatted, per call; best of the calls after one warm-up")
+    return res
+
+
 def grad_measure(steps: int):
     """Gradient of the MSE between 4,096 sensor irradiances and a target
     map (made by a seed-fixed ground-truth parameter set) with respect to 64
@@ -730,6 +765,7 @@ def gpu_arm(args):
             "clocks": ck,
         }
         if not (args.sensors or args.no_extras):
+            line["e2e_bytes"] = bytes_measure(sc, rays, min(args.steps, 5))
             line["c1_rtrace"] = c1_measure(args.steps)
             line["dctimestep"] = dct_measure(dev, args.steps)
             line["gradient"] = grad_measure(args.steps)
