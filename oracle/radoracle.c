@@ -310,6 +310,13 @@ static oscene *scene_open(const char *path, int is_rad, char *err, int errlen)
     }
     if (gb_scene_prepare(&O->H) < 0)
         goto bad;
+    for (i = 0; i < O->H.nobjs; i++)
+        if (O->H.objs[i].vnorm) {               /* the shading of smooth meshes is not restated here */
+            snprintf(err, errlen, "mesh vertex normals are not supported by the oracle");
+            gb_scene_clear(&O->H);
+            free(O);
+            return NULL;
+        }
     O->mat = (int *)malloc(sizeof(int) * ((size_t)O->H.nobjs + 1));
     O->inst_of = (int *)malloc(sizeof(int) * ((size_t)O->H.nobjs + 1));
     for (i = 0; i < O->H.nobjs; i++) {

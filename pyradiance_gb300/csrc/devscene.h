@@ -23,6 +23,10 @@
  *                                 fv4 of each object in one 64-byte record,
  *                                 in the order the leaves first reach them
  *   oslot     int32[nobjs]        each object's record slot
+ *   vnidx     int32[nobjs]        mesh triangles with vertex normals: the
+ *                                 index of their normals in vnrm (else -1)
+ *   vnrm      float4[3 * ...]     their three unit vertex normals, in the
+ *                                 mesh's coordinates, vertex order
  *   wkids     int32[8 * nnodes]   the FP32 walk's copy of kids: full-leaf
  *                                 codes give the leaf's place in lrec
  *   lrec      float4[4 * ...]     per leaf set: a header record (first
@@ -57,6 +61,7 @@ enum { DK_NONE = 0, DK_FACE, DK_SPHERE, DK_BUBBLE, DK_CONE, DK_CUP, DK_CYL, DK_T
 #define DF_HASMAT  0x01   /* has a material (findmaterial != NULL) */
 #define DF_TRANSP  0x02   /* material is nominally transparent */
 #define DF_AXSHIFT 2      /* bits 2-3: dominant normal axis of a face */
+#define DF_VNORM   0x10   /* a mesh triangle with vertex normals (vnidx, vnrm) */
 
 /* full-leaf code: -2 - (offset << 6 | min(size, 63)); a size field of 63
  * means "63 or more: read the count word" */
@@ -135,6 +140,8 @@ typedef struct {
     const float2 *fvert;
     const float4 *fv4;
     const float4 *orec;        /* per record slot: obj (y: the object's index), geo, fv4; 64 bytes */
+    const int   *vnidx;        /* per object: its vertex normals in vnrm (DF_VNORM objects) */
+    const float4 *vnrm;        /* three unit normals (x, y, z, 0) per smooth mesh triangle, mesh coordinates */
     const int   *oslot;        /* per object: its record slot */
     const float *cone;
     /* materials */

@@ -99,15 +99,18 @@ struct gb_scene {
     std::vector<int4> hobj;
     std::vector<float4> hgeo;
     std::vector<float2> hfvert;
-    std::vector<float4> hfv4, horec, hlrec;
-    std::vector<int> hwkids;
+    std::vector<float4> hfv4, horec, hlrec, hvnrm;
+    std::vector<int> hwkids, hvnidx;
+    bool has_vnorm = false;        /* some mesh triangle has vertex normals */
+    std::string vnorm_error;       /* a smooth mesh triangle on a material whose shading with them is not built */
     std::vector<int> hoslot;
     std::vector<float> hcone;
     std::vector<gb_dsrc> hsrc;
     std::vector<double> hg64;          /* FP64 geometry of the first-hit casts */
     std::vector<long long> hg64off;
     /* device scene */
-    DevBuf kids, setdata, obj, geo, fvert, fv4, cone, matd, srcd, trk, instd, orec, oslot, g64, g64off, wkids, lrec;
+    DevBuf kids, setdata, obj, geo, fvert, fv4, cone, matd, srcd, trk, instd, orec, oslot, g64, g64off, wkids, lrec,
+        vnidx, vnrm;
     gb_dscene ds;
     /* work buffers */
     DevBuf sensors, value, bins, stats, roots, rootspt, qa, qb, qcount, binprog, modinfo, hits, hitt, hitpn, trkrun,
@@ -478,13 +481,16 @@ static int prepare_device(gb_scene *G)
         upload(G->obj, G->hobj) < 0 || upload(G->geo, G->hgeo) < 0 || upload(G->fvert, G->hfvert) < 0 ||
         upload(G->fv4, G->hfv4) < 0 || upload(G->cone, G->hcone) < 0 || upload(G->matd, G->mat) < 0 ||
         upload(G->srcd, G->hsrc) < 0 || upload(G->g64, G->hg64) < 0 || upload(G->g64off, G->hg64off) < 0 ||
-        upload(G->wkids, G->hwkids) < 0 || upload(G->lrec, G->hlrec) < 0)
+        upload(G->wkids, G->hwkids) < 0 || upload(G->lrec, G->hlrec) < 0 || upload(G->vnidx, G->hvnidx) < 0 ||
+        upload(G->vnrm, G->hvnrm) < 0)
         return set_err(GB_ENOMEM, "device upload of the scene failed");
     gb_dscene &d = G->ds;
     d.kids = (const int *)G->kids.p;
     d.set_data = (const int *)G->setdata.p;
     d.wkids = (const int *)G->wkids.p;
     d.lrec = (const float4 *)G->lrec.p;
+    d.vnidx = (const int *)G->vnidx.p;
+    d.vnrm = (const float4 *)G->vnrm.p;
     d.obj = (const int4 *)G->obj.p;
     d.geo = (const float4 *)G->geo.p;
     d.fvert = (const float2 *)G->fvert.p;
@@ -559,6 +565,8 @@ static int build_arrays(gb_scene *G)
             kind = DK_FACE;
             nv = f->nv;
             flags |= f->ax << DF_AXSHIFT;
+            if (o->vnorm && nv == 3)
+                flags |= DF_VNORM;
             geo[i] = make_float4((float)f->norm[0], (float)f->norm[1], (float)f->norm[2], (float)f->offset);
             aux = (int)fvert.size();
             int xi = (f->ax + 1) % 3, yi = (xi + 1) % 3;
@@ -771,6 +779,42 @@ static int build_arrays(gb_scene *G)
         G->hwkids.swap(wkids);
     }
     G->horec.swap(orec);
+    /* smooth mesh triangles (rt/o_mesh.c:185-206): their vertex normals for
+     * the shading kernels; the materials whose shading uses the perturbed
+     * normal here are plastic and metal (light and glow ignore it) */
+    {
+        std::vector<int> vnidx((size_t)(H.nobjs > 0 ? H.nobjs : 1), -1);
+        std::vector<float4> vnrm;
+        G->has_vnorm = false;
+        G->vnorm_error.clear();
+        auto shaded = [&](int32_t carrier) {     /* the material slot's kind allows the perturbation */
+            const int ms = G->matslot[carrier];
+            const int k = ms >= 0 ? (int)G->mat[2 * ms].x : DM_NONE;
+            return k == DM_NONE || k == DM_PLASTIC || k == DM_METAL || k == DM_LIGHT || k == DM_GLOW;
+        };
+        for (int32_t i = 0; i < H.nobjs; i++) {
+            if (!((obj[i].x >> 8) & DF_VNORM))
+                continue;
+            G->has_vnorm = true;
+            vnidx[i] = (int)(vnrm.size() / 3);
+            for (int k = 0; k < 3; k++)
+                vnrm.push_back(make_float4((float)H.objs[i].vnorm[3 * k], (float)H.objs[i].vnorm[3 * k + 1],
+                                           (float)H.objs[i].vnorm[3 * k + 2], 0.f));
+            bool ok = shaded(i);
+            for (int k = 0; k < H.ninst && ok; k++) {
+                const gb_subscene &sc = H.subs[H.inst[k].sub];
+                if (i >= sc.firstobj && i < sc.firstobj + sc.nobjs && H.objs[H.inst[k].obj].omod >= 0)
+                    ok = shaded(H.inst[k].obj);
+            }
+            if (!ok && G->vnorm_error.empty())
+                G->vnorm_error = "mesh triangles with vertex normals are supported on plastic, metal, light and glow "
+                                 "materials only";
+        }
+        if (vnrm.empty())
+            vnrm.assign(3, make_float4(0, 0, 0, 0));
+        G->hvnidx.swap(vnidx);
+        G->hvnrm.swap(vnrm);
+    }
     G->hoslot.swap(slot_of);
     /* FP64 geometry per object for the first-hit casts (cast64.cu) */
     {
@@ -792,6 +836,8 @@ static int build_arrays(gb_scene *G)
                 g64.push_back((double)f->ax);
                 g64.push_back((double)f->nv);
                 for (int j = 0; j < 3 * f->nv; j++) g64.push_back(o->farg[j]);
+                if ((obj[i].x >> 8) & DF_VNORM)          /* then its three vertex normals */
+                    for (int j = 0; j < 9; j++) g64.push_back(o->vnorm[j]);
             } else if (kind == DK_SPHERE || kind == DK_BUBBLE) {
                 for (int j = 0; j < 4; j++) g64.push_back(o->farg[j]);
             } else if (kind == DK_CONE || kind == DK_CUP || kind == DK_CYL || kind == DK_TUBE || kind == DK_RING) {
@@ -853,6 +899,8 @@ static int build_arrays(gb_scene *G)
     d.wroot = G->wroot;
     d.wkids = G->hwkids.data();
     d.lrec = G->hlrec.data();
+    d.vnidx = G->hvnidx.data();
+    d.vnrm = G->hvnrm.data();
     d.nobjs = H.nobjs;
     d.obj = G->hobj.data();
     d.geo = G->hgeo.data();
@@ -1014,7 +1062,7 @@ extern "C" void gb_scene_free(gb_scene *G)
     if (!G)
         return;
     DevBuf *bufs[] = {&G->kids, &G->setdata, &G->instd, &G->orec, &G->oslot, &G->obj, &G->geo, &G->fvert, &G->fv4,
-                      &G->cone, &G->matd, &G->g64, &G->g64off, &G->wkids, &G->lrec,
+                      &G->cone, &G->matd, &G->g64, &G->g64off, &G->wkids, &G->lrec, &G->vnidx, &G->vnrm,
                       &G->srcd, &G->trk, &G->sensors, &G->value, &G->bins, &G->stats, &G->roots, &G->rootspt, &G->qa,
                       &G->qb, &G->qcount, &G->binprog, &G->modinfo, &G->hits, &G->hitt, &G->trkrun, &G->hitrec,
                       &G->adja, &G->adjb, &G->dlde, &G->gradd, &G->rootdraw, &G->rootlot, &G->tga, &G->tgb,
@@ -1215,6 +1263,16 @@ static int check_shading(gb_scene *G, const gb_opts *o)
     }
     if (!G->src_error.empty())
         return set_err(GB_EUNSUPPORTED, "%s", G->src_error.c_str());
+    if (!G->vnorm_error.empty())
+        return set_err(GB_EUNSUPPORTED, "%s", G->vnorm_error.c_str());
+    /* the ambient value of a smooth surface in rtrace carries a texture
+     * factor made from the whole hemisphere's sample values and distances
+     * (rt/ambient.c:269-296, doambient's rotational gradient); the wavefront
+     * queues each sample as an independent child ray, so it is not formed.
+     * rcontrib's contributions (ray coefficients) do not carry it. */
+    if (G->has_vnorm && o->prog == GB_PROG_RTRACE && o->ab >= (o->I ? 2 : 1))
+        return set_err(GB_EUNSUPPORTED, "rtrace -ab %d on meshes with vertex normals is not implemented (the ambient "
+                       "texture gradient); rcontrib, or rtrace -ab %d, is", o->ab, o->I ? 1 : 0);
     if (o->ab > 0 && o->aa > GB_FTINY)
         return set_err(GB_EUNSUPPORTED, "the ambient cache (-aa %g) is not implemented; use -aa 0", o->aa);
     if (o->as > 0 && o->ab > 0 && o->aa > GB_FTINY)
@@ -1328,6 +1386,7 @@ struct RunOut {
     const double *dlde;     /* gradient runs: host n x 3 d(loss)/d(value) */
     double *grad;           /* gradient runs: host nslots x 3 */
     double *hit_normal;     /* host n x 3 or null: the first hit's surface normal */
+    double *hit_vnormal;    /* host n x 3 or null: a smooth mesh hit's interpolated vertex normal (else 0) */
 };
 
 /* largest generation and queue capacity of the last run on this thread */
@@ -1413,7 +1472,7 @@ static int run(gb_scene *G, const gb_opts *o, int follow, const double *org_dir,
         if (G->hits.ensure((size_t)n * sizeof(int)) < 0 || G->hitt.ensure((size_t)n * sizeof(float)) < 0)
             return set_err(GB_ENOMEM, "device allocation failed");
         P.S.trk = nullptr;
-        if (out.hit_normal && G->hitpn.ensure((size_t)n * 6 * sizeof(double)) < 0)
+        if (out.hit_normal && G->hitpn.ensure((size_t)n * 9 * sizeof(double)) < 0)
             return set_err(GB_ENOMEM, "device allocation failed");
         double *d_pn = out.hit_normal ? (double *)G->hitpn.p : nullptr;
         int rc = launch(GB_K_CAST, P, [&](gb_run &R) {
@@ -1422,11 +1481,11 @@ static int run(gb_scene *G, const gb_opts *o, int follow, const double *org_dir,
             return rc;
         std::vector<int> h(n);
         std::vector<float> t(n);
-        std::vector<double> pn(out.hit_normal ? (size_t)n * 6 : 0);
+        std::vector<double> pn(out.hit_normal ? (size_t)n * 9 : 0);
         CK(cudaMemcpyAsync(h.data(), G->hits.p, (size_t)n * sizeof(int), cudaMemcpyDeviceToHost, st));
         CK(cudaMemcpyAsync(t.data(), G->hitt.p, (size_t)n * sizeof(float), cudaMemcpyDeviceToHost, st));
         if (d_pn)
-            CK(cudaMemcpyAsync(pn.data(), d_pn, (size_t)n * 6 * sizeof(double), cudaMemcpyDeviceToHost, st));
+            CK(cudaMemcpyAsync(pn.data(), d_pn, (size_t)n * 9 * sizeof(double), cudaMemcpyDeviceToHost, st));
         CK(cudaStreamSynchronize(st));
         for (int64_t i = 0; i < n; i++) {
             out.hit_id[i] = h[i];
@@ -1434,7 +1493,10 @@ static int run(gb_scene *G, const gb_opts *o, int follow, const double *org_dir,
                 out.hit_t[i] = t[i];
             if (out.hit_normal)
                 for (int k = 0; k < 3; k++)
-                    out.hit_normal[3 * i + k] = pn[6 * i + 3 + k];
+                    out.hit_normal[3 * i + k] = pn[9 * i + 3 + k];
+            if (out.hit_vnormal)
+                for (int k = 0; k < 3; k++)
+                    out.hit_vnormal[3 * i + k] = pn[9 * i + 6 + k];
         }
         if (!out.value && !out.bins) {
             g_stats[0] = n;
@@ -1816,19 +1878,24 @@ extern "C" int gb_rtrace_hits(gb_scene *G, const gb_opts *o, const double *org_d
 {
     if (!G || !o || (n > 0 && (!org_dir || !hit_id || !hit_normal)))
         return set_err(GB_EINVAL, "null argument");
-    RunOut out = {nullptr, nullptr, hit_id, hit_t, nullptr, nullptr, hit_normal};
+    std::vector<double> vn(hit_pnormal && G->has_vnorm ? (size_t)n * 3 : 0);
+    RunOut out = {nullptr, nullptr, hit_id, hit_t, nullptr, nullptr, hit_normal, vn.empty() ? nullptr : vn.data()};
     int rc = run_sliced(G, o, 0, org_dir, n, nullptr, nullptr, 0, nullptr, out, 0.0);
     if (rc < 0 || !hit_pnormal)
         return rc;
     /* the shading normal (rt/rtrace.c:807-820 oputn): plastic, metal,
      * trans (rt/normal.c:200-207, with back faces visible) and glass
      * (rt/glass.c:88-89) turn a surface hit from behind toward the ray
-     * (flipsurface); the other materials leave it */
+     * (flipsurface); the other materials leave it.  A smooth mesh hit's
+     * normal is perturbed toward its interpolated vertex normal
+     * (rt/o_mesh.c:198-206), the result oriented as the surface is toward
+     * the ray (rt/raytrace.c:446-478 raynormal) */
     for (int64_t i = 0; i < n; i++) {
-        const double *N = hit_normal + 3 * i, *d = org_dir + 6 * i + 3;
+        const double *N = hit_normal + 3 * i, *d0 = org_dir + 6 * i + 3;
         double *pn = hit_pnormal + 3 * i;
-        double dl = sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
-        double rod = dl > 0 ? -(d[0] * N[0] + d[1] * N[1] + d[2] * N[2]) / dl : 0.0;
+        double dl = sqrt(d0[0] * d0[0] + d0[1] * d0[1] + d0[2] * d0[2]);
+        const double d[3] = {dl > 0 ? d0[0] / dl : 0.0, dl > 0 ? d0[1] / dl : 0.0, dl > 0 ? d0[2] / dl : 0.0};
+        double rod = -(d[0] * N[0] + d[1] * N[1] + d[2] * N[2]);
         bool flip = false;
         const int32_t h = hit_id[i];
         if (h >= 0 && h < G->H.nobjs && rod < 0.0) {
@@ -1836,8 +1903,24 @@ extern "C" int gb_rtrace_hits(gb_scene *G, const gb_opts *o, const double *org_d
             const int t = m >= 0 ? G->H.objs[m].otype : -1;
             flip = t == GT_GLASS || (o->bv && (t == GT_PLASTIC || t == GT_METAL || t == GT_TRANS));
         }
-        for (int k = 0; k < 3; k++)
-            pn[k] = flip ? -N[k] : N[k];
+        const double *V = vn.empty() ? nullptr : vn.data() + 3 * i;
+        double pert2 = 0.0;
+        if (V)
+            for (int k = 0; k < 3; k++)
+                pert2 += (V[k] - N[k]) * (V[k] - N[k]);
+        if (V && (V[0] != 0.0 || V[1] != 0.0 || V[2] != 0.0) && pert2 > GB_FTINY * GB_FTINY) {
+            double nm[3], r2 = flip ? -rod : rod;
+            for (int k = 0; k < 3; k++)
+                nm[k] = flip ? -V[k] : V[k];                 /* ron + pert, after any flip */
+            double nd = -(nm[0] * d[0] + nm[1] * d[1] + nm[2] * d[2]);
+            if ((nd > 0.0) != (r2 > 0.0))
+                for (int k = 0; k < 3; k++)
+                    nm[k] += 2.0 * nd * d[k];
+            for (int k = 0; k < 3; k++)
+                pn[k] = nm[k];
+        } else
+            for (int k = 0; k < 3; k++)
+                pn[k] = flip ? -N[k] : N[k];
     }
     return GB_OK;
 }

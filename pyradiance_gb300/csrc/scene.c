@@ -110,6 +110,7 @@ void gb_scene_clear(gb_scene_host *S)
             free(o->sarg[k]);
         free(o->sarg);
         free(o->farg);
+        free(o->vnorm);
     }
     free(S->objs);
     free(S->kids);
@@ -1150,6 +1151,7 @@ static int merge_subscene(gb_scene_host *S, gb_scene_host *T, const char *name)
  * triangles joining one or two vertices of other patches. */
 typedef struct {
     uint32_t (*xyz)[3];
+    int32_t *norm;               /* encoded vertex normals (0: none), or NULL */
     int nverts, ntris, nj1, nj2;
     unsigned char (*tri)[3];
     int16_t *trimat, solemat;
@@ -1164,6 +1166,7 @@ static void mpatch_free(mpatch *pp, int n)
     int i;
     for (i = 0; i < n; i++) {
         free(pp[i].xyz);
+        free(pp[i].norm);
         free(pp[i].tri);
         free(pp[i].trimat);
         free(pp[i].j1v);
@@ -1180,8 +1183,6 @@ static int read_patch(rdr *R, mpatch *pp, const char *path)
     long flags = r_int(R, 1, &ok), n;
     if (!ok || !(flags & 1) || (flags & ~7L))
         return fail("(%s): bad patch flags", path);
-    if (flags & 2)
-        return fail("(%s): mesh vertex normals are not supported", path);
     pp->nverts = (int)r_int(R, 2, &ok);
     if (!ok || pp->nverts <= 0 || pp->nverts > 256)
         return fail("(%s): bad number of patch vertices", path);
@@ -1191,6 +1192,13 @@ static int read_patch(rdr *R, mpatch *pp, const char *path)
     for (i = 0; i < pp->nverts; i++)
         for (j = 0; j < 3; j++)
             pp->xyz[i][j] = (uint32_t)r_int(R, 4, &ok);
+    if (flags & 2) {                             /* vertex normals, 32-bit direction codes */
+        pp->norm = (int32_t *)malloc((size_t)pp->nverts * sizeof(int32_t));
+        if (!pp->norm)
+            return fail("out of memory");
+        for (i = 0; i < pp->nverts; i++)
+            pp->norm[i] = (int32_t)r_int(R, 4, &ok);
+    }
     if (flags & 4)                               /* (u,v): read past, unused */
         for (i = 0; i < 2 * pp->nverts; i++)
             r_int(R, 4, &ok);
@@ -1241,6 +1249,54 @@ static int read_patch(rdr *R, mpatch *pp, const char *path)
         pp->j2mat[i] = (int16_t)r_int(R, 2, &ok);
     }
     return ok ? 0 : fail("(%s): truncated mesh file", path);
+}
+
+/* A 32-bit direction code (common/dircode.c decodedir, the format
+ * obj2mesh writes vertex normals in): bits 0-2 the signs of x, y and z;
+ * two magnitudes of 13 bits at bits 5 and 18 in units of
+ * 1 / ((2^13 - 1/2) sqrt 2); bit 3 set: the first is x, else y; bit 4 set:
+ * the second is z, else the component the first is not (x or y); the
+ * third component completes the unit length.  Code 0 is no normal. */
+static void decode_dir(int32_t dc, double v[3])
+{
+    const double unit = 1. / 11584.5;
+    double a, b, c;
+    int first, second, third;
+    if (!dc) {
+        v[0] = v[1] = v[2] = 0.;
+        return;
+    }
+    a = (dc >> 5 & 0x1fff) * unit;
+    b = (dc >> 18 & 0x1fff) * unit;
+    c = sqrt(1. - a * a - b * b);
+    first = (dc & 010) ? 0 : 1;
+    if (dc & 020) {
+        second = 2;
+        third = 1 - first;
+    } else {
+        second = 1 - first;
+        third = 2;
+    }
+    v[first] = a;
+    v[second] = b;
+    v[third] = c;
+    if (dc & 01)
+        v[0] = -v[0];
+    if (dc & 02)
+        v[1] = -v[1];
+    if (dc & 04)
+        v[2] = -v[2];
+}
+
+/* vertex id -> its decoded normal; 0 when the vertex has none
+ * (common/mesh.c:263-267) */
+static int mesh_normal(const mpatch *pp, int npatches, int32_t vid, double *n)
+{
+    int pn = vid >> 8, k = vid & 0xff;
+    if (vid < 0 || pn >= npatches || k >= pp[pn].nverts || !pp[pn].norm || !pp[pn].norm[k])
+        return 0;
+    decode_dir(pp[pn].norm[k], n);
+    return 1;
 }
 
 /* vertex id (patch << 8 | index) -> position (common/mesh.c:236-279
@@ -1387,6 +1443,18 @@ static int read_mesh(gb_scene_host *T, const char *path, const char *mesh_name)
                 goto done;
             }
             memcpy(o->farg, xyz, sizeof xyz);
+            {                                    /* normals where all three vertices have one */
+                double nv[9];
+                if (mesh_normal(pp, np, v[0], nv) && mesh_normal(pp, np, v[1], nv + 3) &&
+                    mesh_normal(pp, np, v[2], nv + 6)) {
+                    o->vnorm = (double *)malloc(sizeof nv);
+                    if (!o->vnorm) {
+                        fail("out of memory");
+                        goto done;
+                    }
+                    memcpy(o->vnorm, nv, sizeof nv);
+                }
+            }
             map[i * 1024 + t] = ntri++;
         }
     }

@@ -54,6 +54,9 @@ typedef struct {
     char   **sarg;
     int      nfargs;
     double  *farg;
+    double  *vnorm;              /* mesh triangles with vertex normals: the three
+                                    unit normals in the mesh's coordinates, in the
+                                    order of the vertices in farg; else NULL */
 } gb_object;
 
 /* face record: common/face.h + common/face.c:35-112 */

@@ -535,6 +535,7 @@ __device__ __noinline__ void spawn_hemi_big(const gb_run &P, const Ray &parent, 
 
 struct Surf {                 /* rt/normal.c NORMDAT */
     float3 mcolor, scolor, pnorm;
+    float3 ron;                   /* the surface normal, oriented toward the ray; pnorm: the shading normal */
     float rdiff, rspec, alpha2, pdot;
     float trans, tspec, tdiff;    /* trans material; 0 for plastic and metal */
     bool pure, refl, rblt, flat, tran, tblt;
@@ -976,14 +977,15 @@ __device__ void direct(const gb_run &P, const Ray &r, float3 hp, const Surf &s, 
 }
 
 /* Shade a hit on plastic or metal: returns false if unsupported */
-__device__ __forceinline__ void setup_surf(const gb_run &P, int mk, float4 m0, float4 m1, float3 n, float rod,
-                                           bool flat, Surf &s)
+__device__ __forceinline__ void setup_surf(const gb_run &P, int mk, float4 m0, float4 m1, float3 n, float3 pn,
+                                           float pd, bool flat, Surf &s)
 {
     s.mcolor = f3(m0.y, m0.z, m0.w);
     s.alpha2 = m1.y * m1.y;
     s.pure = s.alpha2 <= D_FTINY;
-    s.pnorm = n;
-    s.pdot = rod < .001f ? .001f : rod;
+    s.ron = n;
+    s.pnorm = pn;
+    s.pdot = pd < .001f ? .001f : pd;
     s.flat = flat;
     s.rspec = m1.x;
     float fest = 0.f;
@@ -1034,7 +1036,7 @@ __device__ __forceinline__ float spec_trial(const gb_run &P, const Ray &r, const
     const float3 h = su.pnorm + (u * cosp + v * sinp) * d;
     const float s = -2.f * dot3(h, r.dir) / (1.f + d * d);
     sdir = normalize3(r.dir + h * s);
-    return dot3(sdir, su.pnorm);
+    return dot3(sdir, su.ron);                  /* rejection against the surface normal */
 }
 
 /* rt/normal.c:441-495, the transmitted part of gaussamp: samples about
@@ -1076,7 +1078,7 @@ __device__ __forceinline__ void gaussamp_trans(const gb_run &P, const Ray &r, co
             rv1 = 1.f - P.specjitter * rv1;
         const float d = rv1 <= D_FTINY ? 1.f : sqrtf(su.alpha2 * -logf(rv1));
         const float3 sd = r.dir + (u * cosp + v * sinp) * d;
-        if (dot3(sd, su.pnorm) >= -D_FTINY)
+        if (dot3(sd, su.ron) >= -D_FTINY)
             continue;
         c.dir = normalize3(sd);
         if (taken)
@@ -1190,6 +1192,70 @@ __device__ __noinline__ void ambient_back(const gb_run &P, const Ray &r, float3 
     Ray rb = r;
     rb.path = gb_child(r.path, GB_C_BACK);
     ambient_side<G>(P, rb, aval, nrm, true, hp, obj, ms);
+}
+
+/* The shading normal of a hit on a smooth mesh triangle (rt/o_mesh.c:
+ * 185-206, rt/raytrace.c:446-478 raynormal): its vertex normals
+ * interpolated at the hit by barycentric weights (in the triangle's
+ * dominant-axis projection, in the mesh's coordinates), carried to the
+ * scene by the instance's forward transform and normalised, turned with
+ * the surface if it was flipped toward the ray, and reflected about the
+ * ray's plane if it then faces away from the ray.  sid: the hit's surface
+ * id; n0: its unflipped normal; rod > 0 after any flip.  false (pn, pd
+ * untouched) when the triangle has no vertex normals or they do not
+ * perturb its normal. */
+__device__ __noinline__ bool mesh_pnorm(const gb_dscene &S, int sid, float3 hp, float3 dir, float3 n0, bool flipped,
+                                        float rod, float3 &pn, float &pd)
+{
+    if (S.ninst == 0)
+        return false;
+    int lo = 0, hi = S.ninst - 1;                 /* the last instance with sidbase <= sid */
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (S.inst[mid].sidbase <= sid)
+            lo = mid;
+        else
+            hi = mid - 1;
+    }
+    const gb_dinst &I = S.inst[lo];
+    const int o = I.firstobj + (sid - I.sidbase);
+    const int fl = S.obj[o].x >> 8;
+    if (!(fl & DF_VNORM))
+        return false;
+    const float *b = I.bx;
+    const float3 p = f3(hp.x * b[0] + hp.y * b[3] + hp.z * b[6] + b[9], hp.x * b[1] + hp.y * b[4] + hp.z * b[7] + b[10],
+                        hp.x * b[2] + hp.y * b[5] + hp.z * b[8] + b[11]);
+    const int ax = (fl >> DF_AXSHIFT) & 3;
+    const int xi = ax + 1 >= 3 ? ax - 2 : ax + 1, yi = xi + 1 >= 3 ? xi - 2 : xi + 1;
+    const float4 va = S.fv4[2 * o], vb = S.fv4[2 * o + 1];     /* projected v0, v1 | v2 */
+    const float e1x = va.z - va.x, e1y = va.w - va.y, e2x = vb.x - va.x, e2y = vb.y - va.y;
+    const float den = e1x * e2y - e1y * e2x;
+    if (den == 0.f)
+        return false;
+    const float qx = comp(p, xi) - va.x, qy = comp(p, yi) - va.y;
+    const float w1 = (qx * e2y - qy * e2x) / den, w2 = (e1x * qy - e1y * qx) / den, w0 = 1.f - w1 - w2;
+    const float4 *vn = S.vnrm + 3 * S.vnidx[o];
+    const float3 m = f3(w0 * vn[0].x + w1 * vn[1].x + w2 * vn[2].x, w0 * vn[0].y + w1 * vn[1].y + w2 * vn[2].y,
+                        w0 * vn[0].z + w1 * vn[1].z + w2 * vn[2].z);
+    const float *f = I.fx;
+    float3 w = f3(m.x * f[0] + m.y * f[3] + m.z * f[6], m.x * f[1] + m.y * f[4] + m.z * f[7],
+                  m.x * f[2] + m.y * f[5] + m.z * f[8]);
+    const float l = sqrtf(dot3(w, w));
+    if (l == 0.f)
+        return false;
+    w = w * (1.f / l);
+    const float3 pert = w - n0;
+    if (dot3(pert, pert) <= D_FTINY * D_FTINY)
+        return false;
+    float3 nm = flipped ? -w : w;                  /* ron + pert after any flip: unit */
+    float nd = -dot3(nm, dir);
+    if ((nd > 0.f) != (rod > 0.f)) {
+        nm = nm + dir * (2.f * nd);
+        nd = -nd;
+    }
+    pn = nm;
+    pd = nd;
+    return true;
 }
 
 /* Shade ray r given its trace result (h.obj < 0: the ray left the scene)
@@ -1317,8 +1383,11 @@ __device__ void shade_ray(const gb_run &P, const Ray &r, const Hit &h, Counters 
     }
     /* plastic / metal */
     int okd = S.obj[ro].x & 0xff;
+    float3 pn = n;
+    float pd = rod;
+    const bool tex = h.obj >= S.nobjs && mesh_pnorm(S, h.obj, hp, r.dir, h.n, h.rod < 0.f, rod, pn, pd);
     Surf su;
-    setup_surf(P, mk, m0, m1, n, rod, okd == DK_FACE || okd == DK_RING, su);
+    setup_surf(P, mk, m0, m1, n, pn, pd, (okd == DK_FACE || okd == DK_RING) && !tex, su);
     if (su.tran && su.pure) {                    /* the transmitted ray (rt/normal.c:280-301) */
         Ray c;
         if (ray_origin(P, r, GB_TRANS, su.mcolor * su.tspec, true, GB_C_TRANS, c, nullptr)) {
@@ -1335,6 +1404,8 @@ __device__ void shade_ray(const gb_run &P, const Ray &r, const Hit &h, Counters 
         if (ray_origin(P, r, GB_REFLECTED, su.scolor, true, GB_C_REFL, c, nullptr)) {
             c.org = hp;
             c.dir = normalize3(r.dir + su.pnorm * (2.f * su.pdot));
+            if (tex && dot3(c.dir, n) <= D_FTINY)          /* would enter the surface */
+                c.dir = normalize3(r.dir + n * (2.f * rod));
             c.origin = h.obj;
             if (G)                               /* specular color: not a parameter */
                 c.adj = r.adj;
@@ -1347,7 +1418,12 @@ __device__ void shade_ray(const gb_run &P, const Ray &r, const Hit &h, Counters 
         float3 aval = su.mcolor * su.rdiff;
         if (su.rblt)
             aval = aval + su.scolor;
-        ambient_side<G>(P, r, aval, n, false, hp, h.obj, ms);
+        /* the hemisphere about the surface normal, on the side the
+         * shading normal faces (rt/ambient.c:269-279) */
+        if (tex && dot3(pn, n) < 0.f)
+            ambient_side<G>(P, r, aval, -n, true, hp, h.obj, ms);
+        else
+            ambient_side<G>(P, r, aval, n, false, hp, h.obj, ms);
     }
     if (su.tdiff > D_FTINY)                      /* ambient from the other side (trans) */
         ambient_back<G>(P, r, su.mcolor * (su.tblt ? su.trans : su.tdiff), -n, hp, h.obj, ms);

@@ -424,7 +424,7 @@ def instance_room(sub_octree: str, seed: int = 0, n: int = 12) -> str:
         if i == 2:
             args += ["-mx"]
         args += ["-t", f"{x:.6g}", f"{y:.6g}", "0.002"]
-        mod = "override" if i % 3 == 0 else "void"
+        mod = "override" if i % 3 == 0 else "override_metal" if metal and i % 3 == 1 else "void"
         out.append(f"{mod} instance inst{i}\n{1 + len(args)} {sub_octree} {' '.join(args)}\n0\n0\n\n")
     out.append("void light light_mat\n0\n0\n3 100 100 100\n\n")
     cx, cy = X / 2, Y / 2
@@ -433,18 +433,21 @@ def instance_room(sub_octree: str, seed: int = 0, n: int = 12) -> str:
     return "".join(out)
 
 
-def mesh_obj(nu: int = 24, nv: int = 12, nsheet: int = 16, seed: int = 0) -> str:
+def mesh_obj(nu: int = 24, nv: int = 12, nsheet: int = 16, seed: int = 0, normals: bool = False) -> str:
     """A Wavefront OBJ for obj2mesh, in its own coordinates around the
     origin: a UV sphere of radius 0.45 centred 0.45 above the origin
     (material ``mesh_red``) and a bumpy square sheet of side 1.2 at height
-    0.9 .. 1.0 (``mesh_grey``), triangles only, no vertex normals."""
+    0.9 .. 1.0 (``mesh_grey``), triangles only; with ``normals``, every
+    vertex carries a normal (the sphere's radial direction, the sheet's
+    height-field normal by central differences) and the faces name them."""
     rng = np.random.default_rng(seed)
-    V, out = [], []
+    V, N, out = [], [], []
     for j in range(nv + 1):
         th = np.pi * j / nv
         for i in range(nu):
             ph = 2 * np.pi * i / nu
             V.append((0.45 * np.sin(th) * np.cos(ph), 0.45 * np.sin(th) * np.sin(ph), 0.45 + 0.45 * np.cos(th)))
+            N.append((np.sin(th) * np.cos(ph), np.sin(th) * np.sin(ph), np.cos(th)))
     out.append("usemtl mesh_red")
     for j in range(nv):
         for i in range(nu):
@@ -456,16 +459,24 @@ def mesh_obj(nu: int = 24, nv: int = 12, nsheet: int = 16, seed: int = 0) -> str
                 out.append(f"f {a} {d} {c}")
     base = len(V)
     h = rng.uniform(0.9, 1.0, size=(nsheet + 1, nsheet + 1))
+    gy, gx = np.gradient(h, 1.2 / nsheet)
     for j in range(nsheet + 1):
         for i in range(nsheet + 1):
             V.append((-0.6 + 1.2 * i / nsheet, -0.6 + 1.2 * j / nsheet, h[j, i]))
+            n = np.array([-gx[j, i], -gy[j, i], 1.0])
+            N.append(tuple(n / np.linalg.norm(n)))
     out.append("usemtl mesh_grey")
     for j in range(nsheet):
         for i in range(nsheet):
             a = base + j * (nsheet + 1) + i + 1
             b, c, d = a + 1, a + nsheet + 2, a + nsheet + 1
             out += [f"f {a} {b} {c}", f"f {a} {c} {d}"]
-    return "".join(f"v {x:.7f} {y:.7f} {z:.7f}\n" for x, y, z in V) + "\n".join(out) + "\n"
+    text = "".join(f"v {x:.7f} {y:.7f} {z:.7f}\n" for x, y, z in V)
+    if normals:
+        text += "".join(f"vn {x:.7f} {y:.7f} {z:.7f}\n" for x, y, z in N)
+        out = [" ".join([t[0]] + [f"{k}//{k}" for k in t[1:]]) if t[0] == "f" else " ".join(t)
+               for t in (ln.split() for ln in out)]
+    return text + "\n".join(out) + "\n"
 
 
 def mesh_materials() -> str:
@@ -474,15 +485,18 @@ def mesh_materials() -> str:
             "void plastic mesh_grey\n0\n0\n5 0.5 0.5 0.5 0.03 0.05\n\n")
 
 
-def mesh_room(mesh_file: str, seed: int = 0, n: int = 10) -> str:
+def mesh_room(mesh_file: str, seed: int = 0, n: int = 10, metal: bool = False) -> str:
     """The room shell and ceiling light of ``instance_room`` with ``n``
     placements of the compiled mesh ``mesh_file`` on the floor: rotated
     about z, some scaled, one mirrored; every third one with its own
-    material (which replaces the mesh's), the others with the mesh's."""
+    material (which replaces the mesh's), the others with the mesh's; with
+    ``metal``, the second of every three with a rough metal of its own."""
     rng = np.random.default_rng(seed)
     X, Y, Z = ROOM
     out = [_mat_plastic("room_mat", (0.5, 0.5, 0.5)), _room_shell("room_mat"),
            _mat_plastic("override", (0.3, 0.6, 0.3))]
+    if metal:
+        out.append("void metal override_metal\n0\n0\n5 0.7 0.6 0.4 0.6 0.08\n\n")
     for i in range(n):
         x, y = rng.uniform((1.2, 1.2), (X - 1.2, Y - 1.2))
         args = ["-rz", f"{rng.uniform(0, 360):.6g}"]
@@ -491,7 +505,7 @@ def mesh_room(mesh_file: str, seed: int = 0, n: int = 10) -> str:
         if i == 2:
             args += ["-mx"]
         args += ["-t", f"{x:.6g}", f"{y:.6g}", "0.002"]
-        mod = "override" if i % 3 == 0 else "void"
+        mod = "override" if i % 3 == 0 else "override_metal" if metal and i % 3 == 1 else "void"
         out.append(f"{mod} mesh mesh{i}\n{1 + len(args)} {mesh_file} {' '.join(args)}\n0\n0\n\n")
     out.append("void light light_mat\n0\n0\n3 100 100 100\n\n")
     cx, cy = X / 2, Y / 2

@@ -37,7 +37,7 @@ def run(args, inp: bytes | None = None, cwd=None) -> bytes:
     return p.stdout
 
 
-def run_independent(args, rays: np.ndarray, shards: int | None = None) -> bytes:
+def run_independent(args, rays: np.ndarray, shards: int | None = None, cwd=None) -> bytes:
     """A -u+ (time-seeded) rcontrib or rtrace run over many rays in parallel
     with independent random streams: `shards` separate single-process runs
     over contiguous parts of the rays, started more than a second apart.
@@ -60,7 +60,7 @@ def run_independent(args, rays: np.ndarray, shards: int | None = None) -> bytes:
             with open(fin, "rb") as fi, open(Path(td) / f"out{i}", "wb") as fo, \
                     open(Path(td) / f"err{i}", "wb") as fe:
                 procs.append(subprocess.Popen([str(BIN / args[0]), *map(str, args[1:])], stdin=fi, stdout=fo,
-                                              stderr=fe, env=env))
+                                              stderr=fe, env=env, cwd=cwd))
         outs = []
         for i, p in enumerate(procs):
             if p.wait() != 0:
@@ -511,6 +511,54 @@ def meshes(tmp: Path) -> None:
         sum(n == "M-Tri" or n.startswith("mesh") for n in hit), len(hit)))
 
 
+def smooth_meshes(tmp: Path, nstat: int = 24, K: int = 256) -> None:
+    """Meshes with vertex normals (rt/o_mesh.c:185-206): the sphere and
+    sheet of `meshes` with a normal at every vertex, compiled by the
+    reference obj2mesh and placed 10 times in the room (one mirrored, some
+    scaled, some with a plastic or a rough metal of their own).  Random
+    interior rays, half aimed at the meshes: first-hit names and distances,
+    the surface normal and the shading normal (-oNn), and deterministic
+    -ab 0 -st 1 radiance (direct light through the shading normal, the
+    rough lobes' direct Gaussian term only, none sampled); and, for
+    `nstat` rays that meet a mesh, rcontrib -ab 1 contributions of the
+    ceiling light as means and standard errors over K replicas (-u+,
+    independent processes)."""
+    (tmp / "mesh_vn.obj").write_text(w.mesh_obj(normals=True))
+    (tmp / "mesh_mat.rad").write_text(w.mesh_materials())
+    run(["obj2mesh", "-a", "mesh_mat.rad", "mesh_vn.obj", "mesh_smooth.rtm"], b"", cwd=tmp)
+    (tmp / "mesh_smooth_room.rad").write_text(w.mesh_room("mesh_smooth.rtm", metal=True))
+    (tmp / "mesh_smooth_room.oct").write_bytes(run(["oconv", "-f", "mesh_smooth_room.rad"], b"", cwd=tmp))
+    rays = w.random_rays(3000, seed=13)
+    rng = np.random.default_rng(13)
+    tgt = rng.uniform((0.5, 0.5, 0.0), (9.5, 7.5, 1.1), size=(2000, 3))
+    d = tgt - rays[:2000, :3]
+    rays[:2000, 3:] = d / np.linalg.norm(d, axis=1, keepdims=True)
+    inp = rays.astype("<f8").tobytes()
+    octn = "mesh_smooth_room.oct"
+    det = ["-dj", "0", "-ds", "0", "-dr", "0", "-dt", "0"]
+    hit = names(run(["rtrace", "-h", "-u-", "-ab", "0", "-fda", "-os", octn], inp, cwd=tmp))
+    dist = np.frombuffer(run(["rtrace", "-h", "-u-", "-ab", "0", "-fdd", "-oL", octn], inp, cwd=tmp), dtype="<f8")
+    nn = np.frombuffer(run(["rtrace", "-h", "-u-", "-ab", "0", "-fdd", "-oNn", octn], inp, cwd=tmp),
+                       dtype="<f8").reshape(-1, 6)
+    val = np.frombuffer(run(["rtrace", "-h", "-u-", "-ab", "0", *det, "-st", "1", "-fdd", "-ov", octn], inp,
+                            cwd=tmp), dtype="<f8").reshape(-1, 3)
+    smooth = np.abs(nn[:, :3] - nn[:, 3:]).max(1) > 1e-6
+    onmesh = np.array([n == "M-Tri" or n.startswith("mesh") for n in hit])
+    pick = np.nonzero(onmesh[:2000] & (dist[:2000] < 1e9))[0][:: max(1, int(onmesh[:2000].sum()) // nstat)][:nstat]
+    srays = rays[pick]
+    out = run_independent(["rcontrib", "-h", "-u+", "-ab", "1", "-ad", "256", "-lw", "1e-4", "-fdd", "-m", "light_mat",
+                           octn], np.repeat(srays, K, axis=0), cwd=tmp)
+    a = np.frombuffer(out, dtype="<f8").reshape(len(srays), K, 3)
+    for f in ("mesh_smooth.rtm", "mesh_smooth_room.oct"):
+        (OUT / f).write_bytes((tmp / f).read_bytes())
+    np.savez_compressed(OUT / "smooth_meshes.npz", rays=rays, hit_name=hit, hit_dist=dist, N=nn[:, :3], n=nn[:, 3:],
+                        radiance=val, stat_rays=srays, K=K, mean=a.mean(1), se=a.std(1, ddof=1) / np.sqrt(K),
+                        cmd="rtrace -h -u- -ab 0 -os | -oL | -oNn | -dj 0 -ds 0 -dr 0 -dt 0 -st 1 -ov; "
+                            "rcontrib -h -u+ -ab 1 -ad 256 -lw 1e-4 -m light_mat (independent -n 1 processes)")
+    print("smooth meshes: %d of %d rays hit mesh triangles, %d with a perturbed normal; %d stat rays" % (
+        onmesh.sum(), len(hit), smooth.sum(), len(srays)))
+
+
 # bin groups of the 146 columns: ground, then the 8 Reinhart MF:1 altitude rows
 ROW_EDGES = [0, 1, 31, 61, 85, 109, 127, 139, 145, 146]
 
@@ -935,7 +983,7 @@ def main() -> None:
     if not (BIN / "rtrace").exists():
         sys.exit("reference programs missing: make -f oracle/build_ref.mk REF=/root/reference -j8")
     parts = {"octree": octree_digests, "c1": c1_direct, "c1p": c1_partitioned, "zoo": zoo, "glossy": glossy, "irr": surface_irradiance,
-             "ss": supersampled_irradiance, "normals": normals, "inst": instances, "mesh": meshes, "circ": circular_sources,
+             "ss": supersampled_irradiance, "normals": normals, "inst": instances, "mesh": meshes, "meshvn": smooth_meshes, "circ": circular_sources,
              "trans": translucent, "bins": general_bins, "cbins": cie_bins,
              "spot": spotlights, "mirror": mirrors, "flux": flux_matrices, "flux_sc": flux_shirchiu,
              "dct": lambda tmp: dct_small(), "dct4": lambda tmp: dct_four(), "rmtxop": lambda tmp: rmtxop_cases(), "rmtxop_chains": lambda tmp: rmtxop_chains(), "btdf": lambda tmp: btdf_matrices(), "trace_oct": lambda tmp: ref_fixture_trace(),

@@ -661,6 +661,52 @@ def test_meshes(gb):
     assert (rel <= 1e-4).mean() >= 0.99, np.sort(rel)[-5:]
 
 
+def test_smooth_meshes(gb):
+    """Meshes with vertex normals (rt/o_mesh.c:185-206; the reference
+    obj2mesh's mesh, placed 10 times, one mirrored, some scaled, some with
+    a plastic or rough metal of their own).  First hits cast in FP64: names
+    and distances; the surface normal and the shading normal (-oNn, the
+    vertex normals interpolated at the hit and oriented as the reference's
+    raynormal does) within 1e-6 of the reference's.  -ab 0 -st 1 radiance
+    (direct light through the shading normal, the rough lobes' direct
+    Gaussian term) within 1e-4 on 99% of the rays, mesh hits among them.
+    rcontrib -ab 1 contributions of the ceiling light on rays that meet a
+    mesh (hemisphere about the surface normal, rough specular about the
+    shading normal, samples rejected below the surface): every ray's mean
+    over K replicas within 4 combined standard errors of the reference's.
+    rtrace with ambient bounces on these surfaces is refused (their ambient
+    texture factor is not formed)."""
+    from pathlib import Path
+    from pyradiance_gb300 import _lib
+    g = golden("smooth_meshes.npz")
+    sc = gb.Scene(str(Path(__file__).resolve().parent / "golden" / "mesh_smooth_room.oct"))
+    rgb, hid, ht = rtrace_c(gb, sc, opts("rtrace", ab=0, dj=0, ds=0, dr=0, dt=0, st=1.0, u=0), g["rays"])
+    names = names_of(sc, hid)
+    assert (names == g["hit_name"]).all(), np.nonzero(names != g["hit_name"])
+    ok = g["hit_dist"] < 1e9
+    np.testing.assert_allclose(ht[ok], g["hit_dist"][ok], rtol=1e-6, atol=1e-7)
+    out = gb.rtrace(g["rays"].astype("<f8").tobytes(), sc, params=["-ab", "0"], inform="d", outform="d",
+                    outspec="Nn", header=False)
+    v = np.frombuffer(out, dtype="<f8").reshape(-1, 6)
+    np.testing.assert_allclose(v[:, :3], g["N"], rtol=1e-6, atol=1e-6)
+    np.testing.assert_allclose(v[:, 3:], g["n"], rtol=1e-6, atol=1e-6)
+    mesh = np.array([n == "M-Tri" or n.startswith("mesh") for n in g["hit_name"]])
+    assert mesh.sum() > 300 and (np.abs(g["N"] - g["n"]).max(1)[mesh] > 1e-3).mean() > 0.9
+    rel = np.abs(rgb - g["radiance"]).max(1) / np.maximum(np.abs(g["radiance"]).max(1), 1e-9)
+    assert (rel <= 1e-4).mean() >= 0.99, np.sort(rel)[-5:]
+    assert (rel[mesh] <= 1e-4).mean() >= 0.98, np.sort(rel[mesh])[-5:]
+    K = int(g["K"])
+    o = opts("rcontrib", ab=1, ad=256, lw=1e-4, u=0, seed=777)
+    st, _ = rcontrib_c(gb, sc, o, np.repeat(g["stat_rays"], K, axis=0), mods=[dict(modifier="light_mat")])
+    st = st.reshape(len(g["stat_rays"]), K, 3)
+    mean, se = st.mean(1), st.std(1, ddof=1) / np.sqrt(K)
+    z = np.abs(mean - g["mean"]) / np.sqrt(se ** 2 + g["se"] ** 2 + 1e-30)
+    print("smooth meshes rcontrib: max z %.2f, mean z %.2f" % (z.max(), z.mean()))
+    assert z.max() < 4.0 and z.mean() < 1.2, z
+    with pytest.raises(_lib.GbError, match="vertex normals"):
+        rtrace_c(gb, sc, opts("rtrace", ab=1, u=0), g["rays"][:8])
+
+
 def test_dctimestep_fp32_fp64(gb):
     g = golden("dct_small.npz")
     r64 = gb.dctimestep_array(g["dc"], g["sky"], mode="fp64")

@@ -358,10 +358,12 @@ def test_meshes():
     np.testing.assert_allclose(irr, g["irradiance"], rtol=1e-6, atol=1e-9)
 
 
-def test_mesh_with_vertex_normals_refused():
+def test_mesh_with_vertex_normals_refused_by_the_oracle():
     """A mesh whose vertices carry normals (rt/o_mesh.c:198-206 perturbs the
-    shading normal with them) is refused by the scene reader."""
-    with pytest.raises(RuntimeError, match="normals are not supported"):
+    shading normal with them) is read by the scene reader, but the oracle
+    does not restate that shading and refuses the scene; the GPU path is
+    checked against the reference's own output for it."""
+    with pytest.raises(RuntimeError, match="normals are not supported by the oracle"):
         po.Scene(Path(__file__).resolve().parent / "golden" / "mesh_normals.oct")
 
 
