@@ -140,6 +140,7 @@ typedef struct {
     const float2 *fvert;
     const float4 *fv4;
     const float4 *orec;        /* per record slot: obj (y: the object's index), geo, fv4; 64 bytes */
+    int   has_vnorm;           /* some mesh triangle has vertex normals */
     const int   *vnidx;        /* per object: its vertex normals in vnrm (DF_VNORM objects) */
     const float4 *vnrm;        /* three unit normals (x, y, z, 0) per smooth mesh triangle, mesh coordinates */
     const int   *oslot;        /* per object: its record slot */

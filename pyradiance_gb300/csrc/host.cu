@@ -899,6 +899,7 @@ static int build_arrays(gb_scene *G)
     d.wroot = G->wroot;
     d.wkids = G->hwkids.data();
     d.lrec = G->hlrec.data();
+    d.has_vnorm = G->has_vnorm;
     d.vnidx = G->hvnidx.data();
     d.vnrm = G->hvnrm.data();
     d.nobjs = H.nobjs;
@@ -1930,6 +1931,9 @@ extern "C" int gb_rtrace_grad(gb_scene *G, const gb_opts *o, const double *org_d
 {
     if (!G || !o || (n > 0 && (!org_dir || !dl_dvalue)) || !grad)
         return set_err(GB_EINVAL, "null argument");
+    if (G->has_vnorm)
+        return set_err(GB_EUNSUPPORTED, "gradients in scenes with mesh triangles with vertex normals are not "
+                       "implemented");
     if (nslots != (int64_t)G->matobj.size())
         return set_err(GB_EINVAL, "the gradient has %lld material slots, the scene %lld", (long long)nslots,
                        (long long)G->matobj.size());

@@ -534,8 +534,7 @@ __device__ __noinline__ void spawn_hemi_big(const gb_run &P, const Ray &parent, 
 /* ------------------------------------------------------------- shading */
 
 struct Surf {                 /* rt/normal.c NORMDAT */
-    float3 mcolor, scolor, pnorm;
-    float3 ron;                   /* the surface normal, oriented toward the ray; pnorm: the shading normal */
+    float3 mcolor, scolor, pnorm;       /* pnorm: the shading normal */
     float rdiff, rspec, alpha2, pdot;
     float trans, tspec, tdiff;    /* trans material; 0 for plastic and metal */
     bool pure, refl, rblt, flat, tran, tblt;
@@ -983,7 +982,6 @@ __device__ __forceinline__ void setup_surf(const gb_run &P, int mk, float4 m0, f
     s.mcolor = f3(m0.y, m0.z, m0.w);
     s.alpha2 = m1.y * m1.y;
     s.pure = s.alpha2 <= D_FTINY;
-    s.ron = n;
     s.pnorm = pn;
     s.pdot = pd < .001f ? .001f : pd;
     s.flat = flat;
@@ -1022,8 +1020,8 @@ __device__ __forceinline__ void setup_surf(const gb_run &P, int mk, float4 m0, f
  * drawn about the normal with a Gaussian slope of variance alpha2, the
  * incident direction mirrored about it.  Returns the cosine of the sample
  * with the surface normal (the caller rejects samples at or below FTINY). */
-__device__ __forceinline__ float spec_trial(const gb_run &P, const Ray &r, const Surf &su, float3 u, float3 v, int t,
-                                            float3 &sdir)
+__device__ __forceinline__ float spec_trial(const gb_run &P, const Ray &r, const Surf &su, float3 ron, float3 u,
+                                            float3 v, int t, float3 &sdir)
 {
     const gb_u4 q = gb_draw(r.path, r.sensor, GB_G_SPEC + (uint32_t)(t >> 1), P.k0, P.k1);
     const int w = (t & 1) * 2;
@@ -1036,7 +1034,7 @@ __device__ __forceinline__ float spec_trial(const gb_run &P, const Ray &r, const
     const float3 h = su.pnorm + (u * cosp + v * sinp) * d;
     const float s = -2.f * dot3(h, r.dir) / (1.f + d * d);
     sdir = normalize3(r.dir + h * s);
-    return dot3(sdir, su.ron);                  /* rejection against the surface normal */
+    return dot3(sdir, ron);                     /* rejection against the surface normal */
 }
 
 /* rt/normal.c:441-495, the transmitted part of gaussamp: samples about
@@ -1044,8 +1042,8 @@ __device__ __forceinline__ float spec_trial(const gb_run &P, const Ray &r, const
  * without the W-G-M-D weighting; trials from GB_G_TSPEC, sample k is child
  * GB_C_TSPEC(k), all sharing the first one's Russian roulette. */
 template <bool G>
-__device__ __forceinline__ void gaussamp_trans(const gb_run &P, const Ray &r, const Surf &su, float3 u, float3 v,
-                                               float3 hp, int obj)
+__device__ __forceinline__ void gaussamp_trans(const gb_run &P, const Ray &r, const Surf &su, float3 ron,
+                                               float3 u, float3 v, float3 hp, int obj)
 {
     Ray c;
     if (!ray_origin(P, r, GB_TSPECULAR, su.mcolor * su.tspec, true, GB_C_TSPEC(0), c, nullptr))
@@ -1078,7 +1076,7 @@ __device__ __forceinline__ void gaussamp_trans(const gb_run &P, const Ray &r, co
             rv1 = 1.f - P.specjitter * rv1;
         const float d = rv1 <= D_FTINY ? 1.f : sqrtf(su.alpha2 * -logf(rv1));
         const float3 sd = r.dir + (u * cosp + v * sinp) * d;
-        if (dot3(sd, su.ron) >= -D_FTINY)
+        if (dot3(sd, ron) >= -D_FTINY)
             continue;
         c.dir = normalize3(sd);
         if (taken)
@@ -1096,14 +1094,15 @@ __device__ __forceinline__ void gaussamp_trans(const gb_run &P, const Ray &r, co
  * the children are queued.  Children share one Russian-roulette decision,
  * as the reference's samples share one rayorigin. */
 template <bool G>
-__device__ __noinline__ void gaussamp(const gb_run &P, const Ray &r, const Surf &su, float rod, float3 hp, int obj)
+__device__ __noinline__ void gaussamp(const gb_run &P, const Ray &r, const Surf &su, float3 ron, float rod, float3 hp,
+                                    int obj)
 {
     const gb_u4 uf = gb_draw(r.path, r.sensor, GB_G_SPECF, P.k0, P.k1);
     const float3 u = perpendicular(su.pnorm, make_float4(gb_u01(uf.v[0]), gb_u01(uf.v[1]), gb_u01(uf.v[2]), 0.f),
                                    uf.v[3]);
     const float3 v = cross3(su.pnorm, u);
     if (su.tran && !su.tblt)
-        gaussamp_trans<G>(P, r, su, u, v, hp, obj);
+        gaussamp_trans<G>(P, r, su, ron, u, v, hp, obj);
     if (!su.refl || su.rblt)
         return;
     Ray c;
@@ -1127,7 +1126,7 @@ __device__ __noinline__ void gaussamp(const gb_run &P, const Ray &r, const Surf 
         int taken = 0, t = 0;
         for (; taken < nst && t < maxiter; t++) {
             float3 sd;
-            if (spec_trial(P, r, su, u, v, t, sd) > D_FTINY)
+            if (spec_trial(P, r, su, ron, u, v, t, sd) > D_FTINY)
                 taken++;
         }
         post = (float)nst / (float)t;
@@ -1140,7 +1139,7 @@ __device__ __noinline__ void gaussamp(const gb_run &P, const Ray &r, const Surf 
     int taken = 0;
     for (int t = 0; taken < nst && t < maxiter; t++) {
         float3 sd;
-        const float cs = spec_trial(P, r, su, u, v, t, sd);
+        const float cs = spec_trial(P, r, su, ron, u, v, t, sd);
         if (cs <= D_FTINY)
             continue;
         c.dir = sd;
@@ -1261,7 +1260,7 @@ __device__ __noinline__ bool mesh_pnorm(const gb_dscene &S, int sid, float3 hp, 
 /* Shade ray r given its trace result (h.obj < 0: the ray left the scene)
  * and push every child ray to the next generation's queue
  * (rt/raytrace.c:163-256 raytrace / rayshade, the material routines). */
-template <bool G>
+template <bool G, bool VN = false>
 __device__ void shade_ray(const gb_run &P, const Ray &r, const Hit &h, Counters &cnt)
 {
     const gb_dscene &S = P.S;
@@ -1385,7 +1384,7 @@ __device__ void shade_ray(const gb_run &P, const Ray &r, const Hit &h, Counters 
     int okd = S.obj[ro].x & 0xff;
     float3 pn = n;
     float pd = rod;
-    const bool tex = h.obj >= S.nobjs && mesh_pnorm(S, h.obj, hp, r.dir, h.n, h.rod < 0.f, rod, pn, pd);
+    const bool tex = VN && h.obj >= S.nobjs && mesh_pnorm(S, h.obj, hp, r.dir, h.n, h.rod < 0.f, rod, pn, pd);
     Surf su;
     setup_surf(P, mk, m0, m1, n, pn, pd, (okd == DK_FACE || okd == DK_RING) && !tex, su);
     if (su.tran && su.pure) {                    /* the transmitted ray (rt/normal.c:280-301) */
@@ -1420,7 +1419,7 @@ __device__ void shade_ray(const gb_run &P, const Ray &r, const Hit &h, Counters 
             aval = aval + su.scolor;
         /* the hemisphere about the surface normal, on the side the
          * shading normal faces (rt/ambient.c:269-279) */
-        if (tex && dot3(pn, n) < 0.f)
+        if (tex && dot3(su.pnorm, n) < 0.f)
             ambient_side<G>(P, r, aval, -n, true, hp, h.obj, ms);
         else
             ambient_side<G>(P, r, aval, n, false, hp, h.obj, ms);
@@ -1433,7 +1432,7 @@ __device__ void shade_ray(const gb_run &P, const Ray &r, const Hit &h, Counters 
      * diffuse terms; every draw is keyed by the path, so the order is free,
      * and last keeps the fewest values live across the call) */
     if (!su.pure && ((su.refl && !su.rblt) || (su.tran && !su.tblt)))
-        gaussamp<G>(P, r, su, rod, hp, h.obj);
+        gaussamp<G>(P, r, su, n, rod, hp, h.obj);
 }
 
 /* Persistent work loop: each warp takes work items 32 at a time with one
@@ -1957,7 +1956,7 @@ __global__ void __launch_bounds__(128) k_trace_inst(gb_run P)
 
 /* One generation, second half: shade every traced ray and queue its
  * children for the next generation. */
-template <bool G>
+template <bool G, bool VN = false>
 __global__ void __launch_bounds__(256, 4) k_shade(gb_run P)
 {
     if (G)
@@ -1973,7 +1972,7 @@ __global__ void __launch_bounds__(256, 4) k_shade(gb_run P)
         if (P.tag_in)
             r.tag = P.tag_in[g];
         const Hit h = load_hit(P.hits + g);
-        shade_ray<G>(P, r, h, cnt);
+        shade_ray<G, VN>(P, r, h, cnt);
     });
     flush_counters(P, cnt);
     if (G)
@@ -2182,10 +2181,18 @@ int gb_launch_trace(const gb_run *P, cudaStream_t st, int sms)
 
 int gb_launch_shade(const gb_run *P, cudaStream_t st, int sms)
 {
-    static int grid = 0;
-    if (!grid)
-        grid = resident_grid(k_shade<false>, 256, sms);
-    k_shade<false><<<grid, 256, 0, st>>>(*P);
+    /* scenes with smooth mesh triangles: the kernel that perturbs their
+     * shading normals; the others carry none of it */
+    static int grid = 0, grid_vn = 0;
+    if (P->S.has_vnorm) {
+        if (!grid_vn)
+            grid_vn = resident_grid(k_shade<false, true>, 256, sms);
+        k_shade<false, true><<<grid_vn, 256, 0, st>>>(*P);
+    } else {
+        if (!grid)
+            grid = resident_grid(k_shade<false>, 256, sms);
+        k_shade<false><<<grid, 256, 0, st>>>(*P);
+    }
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
