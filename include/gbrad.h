@@ -248,6 +248,16 @@ int  gb_last_profile(int kernel, double *ms, int64_t *launches, int64_t *counter
  * in the reference. */
 int  gb_probe_l2(int64_t table_bytes, int chase, double *gbps);
 
+/* ASCII output rows: each row of the nrows x ncols values in C's %e form
+ * (six digits after the point, as rt/rtrace.c puta and rt/rc2.c print
+ * them), separated by sep, the row ended by end, written to out (cap
+ * bytes); *len receives the text's length (GB_EOVERFLOW when above cap,
+ * nothing written).  Formatted by several host threads, equal to a
+ * sequential loop's text.  No counterpart in the reference (its programs
+ * print with printf). */
+int  gb_format_rows(const double *vals, int64_t nrows, int64_t ncols, const char *sep, const char *end, char *out,
+                    int64_t cap, int64_t *len);
+
 const char *gb_last_error(void);
 const char *gb_version(void);
 

@@ -12,6 +12,7 @@ from __future__ import annotations
 
 import os
 import re
+import ctypes as C
 import time
 from pathlib import Path
 from typing import Sequence
@@ -121,9 +122,25 @@ def _ascii_rows(vals: np.ndarray, sep: str = "\t", end: str = "\t\n") -> list[st
     return [row % tuple(r) for r in vals.tolist()]
 
 
+def _ascii_block(vals: np.ndarray, sep: str = "\t", end: str = "\t\n") -> bytes:
+    """The text of _ascii_rows, formatted by the library's host threads
+    (gb_format_rows)."""
+    vals = np.ascontiguousarray(vals, dtype=np.float64)
+    if vals.ndim == 1:
+        vals = vals[:, None]
+    nrows, ncols = vals.shape
+    if nrows == 0:
+        return b""
+    cap = nrows * (ncols * (16 + len(sep)) + len(end)) + 1
+    buf = C.create_string_buffer(cap)
+    n = C.c_int64(0)
+    check(lib().gb_format_rows(vals.ctypes.data, nrows, ncols, sep.encode(), end.encode(), buf, cap, C.byref(n)))
+    return buf.raw[:n.value]
+
+
 def _fmt_values(vals: np.ndarray, fmt: str) -> bytes:
     if fmt == "a":
-        return "".join(_ascii_rows(vals)).encode()
+        return _ascii_block(vals)
     if fmt == "f":
         return np.ascontiguousarray(vals, dtype=np.float32).tobytes()
     if fmt == "d":
@@ -470,7 +487,7 @@ class Rcontrib:
             if cols.shape[1] == 1 and opts.x > 0 and opts.y > 0:     # rt/rc2.c:129-134 printresolu
                 parts.append(f"-Y {opts.y} +X {opts.x}\n".encode())
             if fout == "a":
-                parts.append("".join(_ascii_rows(cols.reshape(cols.shape[0], -1), end="\t\n")).encode())
+                parts.append(_ascii_block(cols.reshape(cols.shape[0], -1), end="\t\n"))
             else:
                 parts.append(_fmt_values(cols.reshape(-1, 3), fout))
             data = b"".join(parts)

@@ -57,6 +57,8 @@ _SIGS = {
     "gb_scene_load_rad": (C.c_int, [C.POINTER(C.c_char_p), C.c_int, C.c_int, C.c_int, C.POINTER(C.c_void_p)]),
     "gb_scene_free": (None, [C.c_void_p]),
     "gb_probe_l2": (C.c_int, [C.c_int64, C.c_int, C.POINTER(C.c_double)]),
+    "gb_format_rows": (C.c_int, [C.c_void_p, C.c_int64, C.c_int64, C.c_char_p, C.c_char_p, C.c_void_p, C.c_int64,
+                                 C.POINTER(C.c_int64)]),
     "gb_scene_octree_info": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64),
                                        C.POINTER(C.c_uint64), C.POINTER(C.c_int)]),
     "gb_scene_nobjects": (C.c_int64, [C.c_void_p]),

@@ -28,7 +28,7 @@ CU_SOURCES = ["trace.cu", "host.cu", "dct.cu", "dct_tc.cu", "octbuild_gpu.cu", "
 # host builder's, and the FP64 first-hit casts as the reference's (no
 # contracted multiply-adds)
 CU_FLAGS = {"octbuild_gpu.cu": ["-fmad=false"], "cast64.cu": ["-fmad=false"]}
-CXX_SOURCES = ["binexpr.cpp"]
+CXX_SOURCES = ["binexpr.cpp", "textio.cpp"]
 C_SOURCES = ["scene.c", "octbuild.c"]
 
 
@@ -79,7 +79,7 @@ def build(verbose: bool = False, force: bool = False) -> Path:
     with cf.ThreadPoolExecutor(max_workers=min(8, max(1, len(jobs)))) as ex:
         list(ex.map(_run, jobs))
     if force or jobs or not LIB.exists():
-        _run([nvcc, *ARCH, "-shared", "-o", str(LIB), *map(str, objs), "-lcudart", "-lm"])
+        _run([nvcc, *ARCH, "-shared", "-o", str(LIB), *map(str, objs), "-lcudart", "-lm", "-lpthread"])
     return LIB
 
 

@@ -280,3 +280,24 @@ def test_btdf_matrices_against_reference(tmp_path):
     bad.write_text(w.klems_bsdf_xml(seed=1).replace("<IncidentDataStructure>Columns", "<IncidentDataStructure>TensorTree3"))
     with pytest.raises(RuntimeError, match="unsupported BSDF"):
         bsdf.load_btdf(bad)
+
+
+def test_ascii_rows_formatted_by_the_library():
+    """gb_format_rows (the byte surface's ASCII output, host threads) gives
+    the text of a sequential %e loop, for ragged shapes, zeros of both
+    signs, subnormals, infinities and huge values; an output buffer that is
+    too small is reported, not overrun."""
+    import ctypes as C
+    from pyradiance_gb300 import _ascii_block, _ascii_rows, _lib
+    rng = np.random.default_rng(3)
+    for shape in ((1, 1), (7, 3), (513, 146 * 3), (2, 0)):
+        v = rng.lognormal(-3, 6, shape) * rng.choice([-1.0, 1.0, 0.0], shape)
+        if v.size >= 5:
+            v.flat[:5] = [-0.0, 5e-324, 1e300, np.inf, -np.inf]
+        for sep, end in (("\t", "\t\n"), (" ", "\n")):
+            assert _ascii_block(v, sep, end) == "".join(_ascii_rows(v, sep, end)).encode()
+    v = np.ones((4, 3))
+    buf = C.create_string_buffer(8)
+    n = C.c_int64(0)
+    rc = _lib.lib().gb_format_rows(v.ctypes.data, 4, 3, b"\t", b"\n", buf, 8, C.byref(n))
+    assert rc == -6 and n.value == len("".join(_ascii_rows(v, "\t", "\n")))
