@@ -46,7 +46,7 @@ WORKLOAD = ("rcontrib daylight coefficients: 4096 sensors (64x64 grid, z=0.8, +z
             "triangles; glow sky + ground, Reinhart MF:1 + ground = 146 bins")
 # algorithmic bytes per unit of traversal work: one child code per node descent,
 # set offset + count per cube visit, object record + vertices per test
-# the config of both arms' lines (the driver compares them)
+# the config of both arms' lines (the two must name the same workload)
 CONFIG = {"workload": None, "sensors_per_gpu": 4096,
           "l2": "GPU arm: L2 flushed (256 MB write) before each step; CPU arm: no cache control"}
 B_NODE, B_STEP, B_TEST = 4, 8, 60
