@@ -20,7 +20,10 @@ the Klems bases or bases the file defines:
   angle of the incident patch (bsdf_m.c:185-207 io_getohm), in single
   precision as the reference holds it; grey values give equal RGB.
 
-Spectral (CIE-X/Y/Z) data, tensor-tree BSDFs and BRDFs are refused.
+A file without transmission data gives the zero matrix of the full Klems
+basis, as the reference's Lambertian fallback does.  Spectral (CIE-X/Y/Z)
+data, tensor-tree BSDFs and BRDFs are refused (the reference's
+cm_loadBTDF refuses tensor trees too).
 """
 from __future__ import annotations
 
@@ -193,7 +196,10 @@ def load_btdf(path) -> np.ndarray:
             else:
                 tf = (m, ib, ob)
     if tf is None and tb is None:
-        raise GbError(-3, f"BSDF '{path}' has no grey matrix transmission")
+        # no transmission matrix: its Lambertian part alone in the full Klems
+        # basis (cm_bsdf_Lamb, util/cmbsdf.c:122-143), zero with no data to take
+        # one from
+        return np.zeros((145, 145, 3), dtype=np.float32)
     recip = tb is None
     m, ib, ob = tf if recip else tb
     diff = np.float32(_subtract_min(m))

@@ -885,7 +885,8 @@ def rmtxop_chains() -> None:
 
 BTDF_CASES = {"fb_cols": dict(seed=1, basis="full", front=True, back=True, rows=False),
               "back_rows": dict(seed=2, basis="full", front=False, back=True, rows=True, base=0.01),
-              "half_front": dict(seed=3, basis="half", front=True, back=False, rows=False, base=0.05)}
+              "half_front": dict(seed=3, basis="half", front=True, back=False, rows=False, base=0.05),
+              "no_trans": dict(seed=4, basis="full", front=False, back=False, rows=False)}
 
 
 def btdf_matrices() -> None:
@@ -894,7 +895,8 @@ def btdf_matrices() -> None:
     (workloads.klems_bsdf_xml, regenerated from their arguments by the
     tests): front and back transmission by columns, back transmission only
     by rows (reciprocity) with a floor taken out as a Lambertian part, and
-    the Klems half basis.  Each transmission matrix is read through
+    the Klems half basis, and a file without transmission data (the
+    reference's Lambertian fallback: zeros).  Each transmission matrix is read through
     dctimestep with identity view, daylight and sky matrices; and one
     four-matrix product V T D sky per file."""
     def mtx(path, m):

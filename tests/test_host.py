@@ -261,7 +261,9 @@ def test_btdf_matrices_against_reference(tmp_path):
     (util/cmbsdf.c:146-181 cm_loadBTDF over common/bsdf_m.c): front and back
     transmission by columns; back transmission only, by rows, turned
     around by reciprocity, with a floor taken out as a Lambertian part; the
-    Klems half basis.  Equal to the reference dctimestep's matrices to
+    Klems half basis; no transmission data (the reference's Lambertian
+    fallback, util/cmbsdf.c:122-143: zeros).  Equal to the reference
+    dctimestep's matrices to
     within 3.5e-7 (the reference's RGB conversion of the Lambertian part
     rounds some values by a single-precision ulp or two)."""
     from pyradiance_gb300 import bsdf, workloads as w
