@@ -738,7 +738,7 @@ def test_dctimestep_four_matrix(gb, tmp_path):
 
 def test_dctimestep_xml_transmission(gb, tmp_path):
     """dctimestep V T.xml D sky with Klems matrix BSDFs for T
-    (util/dctimestep.c:250-254 cm_loadBTDF): the three synthetic XML files
+    (util/dctimestep.c:250-254 cm_loadBTDF): the synthetic XML files
     of tests/golden/btdf.npz, each product on the GPU: the reference
     program's output within 1e-5."""
     import sys
