@@ -792,6 +792,16 @@ static int build_arrays(gb_scene *G)
             const int k = ms >= 0 ? (int)G->mat[2 * ms].x : DM_NONE;
             return k == DM_NONE || k == DM_PLASTIC || k == DM_METAL || k == DM_LIGHT || k == DM_GLOW;
         };
+        /* per octree an instance of which replaces its surfaces' materials
+         * by one that is not shaded through vertex normals */
+        std::vector<char> bad_sub((size_t)(H.nsubs > 0 ? H.nsubs : 1), 0);
+        for (int k = 0; k < H.ninst; k++)
+            if (H.objs[H.inst[k].obj].omod >= 0 && !shaded(H.inst[k].obj))
+                bad_sub[H.inst[k].sub] = 1;
+        std::vector<int> sub_of((size_t)(H.nobjs > 0 ? H.nobjs : 1), -1);
+        for (int k = 0; k < H.nsubs; k++)
+            for (int32_t i = H.subs[k].firstobj; i < H.subs[k].firstobj + H.subs[k].nobjs; i++)
+                sub_of[i] = k;
         for (int32_t i = 0; i < H.nobjs; i++) {
             if (!((obj[i].x >> 8) & DF_VNORM))
                 continue;
@@ -800,12 +810,7 @@ static int build_arrays(gb_scene *G)
             for (int k = 0; k < 3; k++)
                 vnrm.push_back(make_float4((float)H.objs[i].vnorm[3 * k], (float)H.objs[i].vnorm[3 * k + 1],
                                            (float)H.objs[i].vnorm[3 * k + 2], 0.f));
-            bool ok = shaded(i);
-            for (int k = 0; k < H.ninst && ok; k++) {
-                const gb_subscene &sc = H.subs[H.inst[k].sub];
-                if (i >= sc.firstobj && i < sc.firstobj + sc.nobjs && H.objs[H.inst[k].obj].omod >= 0)
-                    ok = shaded(H.inst[k].obj);
-            }
+            const bool ok = shaded(i) && !(sub_of[i] >= 0 && bad_sub[sub_of[i]]);
             if (!ok && G->vnorm_error.empty())
                 G->vnorm_error = "mesh triangles with vertex normals are supported on plastic, metal, light and glow "
                                  "materials only";

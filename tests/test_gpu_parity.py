@@ -675,7 +675,7 @@ def test_smooth_meshes(gb):
     shading normal, samples rejected below the surface): every ray's mean
     over K replicas within 4 combined standard errors of the reference's.
     rtrace with ambient bounces on these surfaces is refused (their ambient
-    texture factor is not formed)."""
+    texture factor is not formed), and so is a glass over them."""
     from pathlib import Path
     from pyradiance_gb300 import _lib
     g = golden("smooth_meshes.npz")
@@ -705,6 +705,9 @@ def test_smooth_meshes(gb):
     assert z.max() < 4.0 and z.mean() < 1.2, z
     with pytest.raises(_lib.GbError, match="vertex normals"):
         rtrace_c(gb, sc, opts("rtrace", ab=1, u=0), g["rays"][:8])
+    glassy = gb.Scene(str(Path(__file__).resolve().parent / "golden" / "mesh_smooth_glass.oct"))
+    with pytest.raises(_lib.GbError, match="vertex normals"):
+        rtrace_c(gb, glassy, opts("rtrace", ab=0, u=0), g["rays"][:8])
 
 
 def test_dctimestep_fp32_fp64(gb):
