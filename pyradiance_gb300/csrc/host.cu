@@ -9,6 +9,7 @@
 #include <cstring>
 #include <ctime>
 #include <atomic>
+#include <functional>
 #include <string>
 #include <thread>
 #include <vector>
@@ -118,6 +119,8 @@ struct gb_scene {
     cudaStream_t stream = nullptr;
     int sms = 0;
     int wroot = 0;                 /* the walk's root code (wkids, lrec) */
+    void *pin = nullptr;           /* pinned host staging of the first-hit outputs */
+    size_t pin_n = 0;
     cudaEvent_t ev[2 * GB_TIMED_LAUNCHES + 2];
     int nev = 0;
     int octree_on_device = 0;          /* the octree was built by the device builder */
@@ -1072,9 +1075,11 @@ extern "C" void gb_scene_free(gb_scene *G)
                       &G->srcd, &G->trk, &G->sensors, &G->value, &G->bins, &G->stats, &G->roots, &G->rootspt, &G->qa,
                       &G->qb, &G->qcount, &G->binprog, &G->modinfo, &G->hits, &G->hitt, &G->trkrun, &G->hitrec,
                       &G->adja, &G->adjb, &G->dlde, &G->gradd, &G->rootdraw, &G->rootlot, &G->tga, &G->tgb,
-                      &G->ssval, &G->sscnt, &G->sserr, &G->slow};
+                      &G->ssval, &G->sscnt, &G->sserr, &G->slow, &G->hitpn};
     for (DevBuf *b : bufs)
         b->release();
+    if (G->pin)
+        cudaFreeHost(G->pin);
     if (G->stream)
         cudaStreamDestroy(G->stream);
     gb_scene_clear(&G->H);
@@ -1474,6 +1479,7 @@ static int run(gb_scene *G, const gb_opts *o, int follow, const double *org_dir,
     P.walk_blocks_per_sm = G->tuned_blocks;
 
     /* cast-only outputs */
+    std::function<void()> unpack_hits;
     if (out.hit_id) {
         if (G->hits.ensure((size_t)n * sizeof(int)) < 0 || G->hitt.ensure((size_t)n * sizeof(float)) < 0)
             return set_err(GB_ENOMEM, "device allocation failed");
@@ -1485,26 +1491,45 @@ static int run(gb_scene *G, const gb_opts *o, int follow, const double *org_dir,
             return gb_launch_cast64(&R, (int *)G->hits.p, (float *)G->hitt.p, d_pn, st, G->sms); });
         if (rc < 0)
             return rc;
-        std::vector<int> h(n);
-        std::vector<float> t(n);
-        std::vector<double> pn(out.hit_normal ? (size_t)n * 9 : 0);
-        CK(cudaMemcpyAsync(h.data(), G->hits.p, (size_t)n * sizeof(int), cudaMemcpyDeviceToHost, st));
-        CK(cudaMemcpyAsync(t.data(), G->hitt.p, (size_t)n * sizeof(float), cudaMemcpyDeviceToHost, st));
-        if (d_pn)
-            CK(cudaMemcpyAsync(pn.data(), d_pn, (size_t)n * 9 * sizeof(double), cudaMemcpyDeviceToHost, st));
-        CK(cudaStreamSynchronize(st));
-        for (int64_t i = 0; i < n; i++) {
-            out.hit_id[i] = h[i];
-            if (out.hit_t)
-                out.hit_t[i] = t[i];
-            if (out.hit_normal)
-                for (int k = 0; k < 3; k++)
-                    out.hit_normal[3 * i + k] = pn[9 * i + 3 + k];
-            if (out.hit_vnormal)
-                for (int k = 0; k < 3; k++)
-                    out.hit_vnormal[3 * i + k] = pn[9 * i + 6 + k];
+        /* the first hits come back through pinned staging, unpacked after
+         * the values' final synchronisation when values follow, so that the
+         * host does not wait for the casts before it queues the values */
+        const size_t hb = (size_t)n * (sizeof(int) + sizeof(float)) + (d_pn ? (size_t)n * 9 * sizeof(double) : 0);
+        if (G->pin_n < hb) {
+            if (G->pin)
+                cudaFreeHost(G->pin);
+            G->pin = nullptr;
+            G->pin_n = 0;
+            if (cudaHostAlloc(&G->pin, hb, cudaHostAllocDefault) != cudaSuccess) {
+                cudaGetLastError();
+                G->pin = nullptr;
+                return set_err(GB_ENOMEM, "cannot allocate %zu bytes of pinned host memory", hb);
+            }
+            G->pin_n = hb;
         }
+        double *pn = (double *)G->pin;
+        int *h = (int *)(pn + (d_pn ? (size_t)n * 9 : 0));
+        float *t = (float *)(h + n);
+        CK(cudaMemcpyAsync(h, G->hits.p, (size_t)n * sizeof(int), cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpyAsync(t, G->hitt.p, (size_t)n * sizeof(float), cudaMemcpyDeviceToHost, st));
+        if (d_pn)
+            CK(cudaMemcpyAsync(pn, d_pn, (size_t)n * 9 * sizeof(double), cudaMemcpyDeviceToHost, st));
+        unpack_hits = [&out, n, h, t, pn]() {
+            for (int64_t i = 0; i < n; i++) {
+                out.hit_id[i] = h[i];
+                if (out.hit_t)
+                    out.hit_t[i] = t[i];
+                if (out.hit_normal)
+                    for (int k = 0; k < 3; k++)
+                        out.hit_normal[3 * i + k] = pn[9 * i + 3 + k];
+                if (out.hit_vnormal)
+                    for (int k = 0; k < 3; k++)
+                        out.hit_vnormal[3 * i + k] = pn[9 * i + 6 + k];
+            }
+        };
         if (!out.value && !out.bins) {
+            CK(cudaStreamSynchronize(st));
+            unpack_hits();
             g_stats[0] = n;
             return GB_OK;
         }
@@ -1772,6 +1797,8 @@ static int run(gb_scene *G, const gb_opts *o, int follow, const double *org_dir,
     if (grad)
         CK(cudaMemcpyAsync(out.grad, G->gradd.p, (size_t)nslots * 3 * sizeof(double), cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
+    if (unpack_hits)
+        unpack_hits();
     unsigned long long overflow = 0;
     for (int k = 0; k < GB_K_N; k++) {
         g_stats[0] += (int64_t)stats[k][GB_ST_RAYS];
