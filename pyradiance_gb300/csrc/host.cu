@@ -121,6 +121,8 @@ struct gb_scene {
     int wroot = 0;                 /* the walk's root code (wkids, lrec) */
     void *pin = nullptr;           /* pinned host staging of the first-hit outputs */
     size_t pin_n = 0;
+    void *pinb = nullptr;          /* pinned host staging of the bins */
+    size_t pinb_n = 0;
     cudaEvent_t ev[2 * GB_TIMED_LAUNCHES + 2];
     int nev = 0;
     int octree_on_device = 0;          /* the octree was built by the device builder */
@@ -1080,6 +1082,8 @@ extern "C" void gb_scene_free(gb_scene *G)
         b->release();
     if (G->pin)
         cudaFreeHost(G->pin);
+    if (G->pinb)
+        cudaFreeHost(G->pinb);
     if (G->stream)
         cudaStreamDestroy(G->stream);
     gb_scene_clear(&G->H);
@@ -1791,12 +1795,32 @@ static int run(gb_scene *G, const gb_opts *o, int follow, const double *org_dir,
     CK(cudaMemcpyAsync(stats, G->stats.p, sizeof stats, cudaMemcpyDeviceToHost, st));
     if (out.value)
         CK(cudaMemcpyAsync(out.value, G->value.p, (size_t)n * 3 * sizeof(double), cudaMemcpyDeviceToHost, st));
-    if (out.bins && nrec > 0)
-        CK(cudaMemcpyAsync(out.bins, G->bins.p, (size_t)nrec * nbins_total * 3 * sizeof(double),
-                           cudaMemcpyDeviceToHost, st));
+    /* the bins come back through pinned staging (a copy from pageable
+     * memory is staged by the driver at a fraction of the link's rate),
+     * then into the caller's buffer */
+    const size_t binbytes = out.bins && nrec > 0 ? (size_t)nrec * nbins_total * 3 * sizeof(double) : 0;
+    bool bins_staged = false;
+    if (binbytes) {
+        if (G->pinb_n < binbytes) {
+            if (G->pinb)
+                cudaFreeHost(G->pinb);
+            G->pinb = nullptr;
+            G->pinb_n = 0;
+            if (cudaHostAlloc(&G->pinb, binbytes, cudaHostAllocDefault) == cudaSuccess)
+                G->pinb_n = binbytes;
+            else {
+                cudaGetLastError();
+                G->pinb = nullptr;
+            }
+        }
+        bins_staged = G->pinb != nullptr;
+        CK(cudaMemcpyAsync(bins_staged ? G->pinb : (void *)out.bins, G->bins.p, binbytes, cudaMemcpyDeviceToHost, st));
+    }
     if (grad)
         CK(cudaMemcpyAsync(out.grad, G->gradd.p, (size_t)nslots * 3 * sizeof(double), cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
+    if (bins_staged)
+        memcpy(out.bins, G->pinb, binbytes);
     if (unpack_hits)
         unpack_hits();
     unsigned long long overflow = 0;
