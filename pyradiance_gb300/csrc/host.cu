@@ -8,6 +8,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <ctime>
+#include <algorithm>
 #include <atomic>
 #include <functional>
 #include <string>
@@ -1819,8 +1820,21 @@ static int run(gb_scene *G, const gb_opts *o, int follow, const double *org_dir,
     if (grad)
         CK(cudaMemcpyAsync(out.grad, G->gradd.p, (size_t)nslots * 3 * sizeof(double), cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
-    if (bins_staged)
-        memcpy(out.bins, G->pinb, binbytes);
+    if (bins_staged) {                        /* large copies split over host threads */
+        const int nt = binbytes >= ((size_t)8 << 20) ? 8 : 1;
+        std::vector<std::thread> th;
+        const size_t per = (binbytes / nt + 63) & ~(size_t)63;
+        for (int k = 1; k < nt; k++) {
+            const size_t a0 = per * k;
+            if (a0 < binbytes)
+                th.emplace_back([&, a0]() {
+                    memcpy((char *)out.bins + a0, (const char *)G->pinb + a0, std::min(per, binbytes - a0));
+                });
+        }
+        memcpy(out.bins, G->pinb, std::min(per, binbytes));
+        for (auto &x : th)
+            x.join();
+    }
     if (unpack_hits)
         unpack_hits();
     unsigned long long overflow = 0;
