@@ -116,11 +116,14 @@ int  gb_rtrace(gb_scene *scene, const gb_opts *opts, const double *org_dir, int6
  * surface's normal at the hit as the object defines it (hit_normal, n x 3:
  * -oN, rt/rtrace.c:787-804) and, if hit_pnormal is not null, the shading
  * normal (-on, :807-820: turned toward the ray where the material turns a
- * surface hit from behind); zero where nothing is hit or a source at
- * infinity is.  The casts are those of gb_rtrace's hit ids (FP64).
- * Replaces: the -on/-oN columns of rt/rtrace.c:274-345. */
+ * surface hit from behind; a mesh triangle's interpolated vertex normal,
+ * rt/o_mesh.c:198-206) and, if hit_uv is not null, the local (u,v)
+ * coordinates (n x 2: -oc, :766-772: a mesh triangle's vertex (u,v)
+ * interpolated at the hit, else 0); zero where nothing is hit or a source
+ * at infinity is.  The casts are those of gb_rtrace's hit ids (FP64).
+ * Replaces: the -on/-oN/-oc columns of rt/rtrace.c:274-345. */
 int  gb_rtrace_hits(gb_scene *scene, const gb_opts *opts, const double *org_dir, int64_t n, int32_t *hit_id,
-                    double *hit_t, double *hit_normal, double *hit_pnormal);
+                    double *hit_t, double *hit_normal, double *hit_pnormal, double *hit_uv);
 
 /* The values of gb_rtrace for rays already in device memory (d_org_dir:
  * n x 6 doubles; d_rgb: n x 3 doubles, overwritten), allocating no device

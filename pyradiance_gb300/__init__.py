@@ -150,7 +150,7 @@ def _fmt_values(vals: np.ndarray, fmt: str) -> bytes:
 
 # ------------------------------------------------------------------ rtrace
 
-_CAST_ONLY = set("odLpNnsmMwW~")
+_CAST_ONLY = set("odLpNnsmMwWc~")
 
 
 def _rtrace(rays: bytes, octree, header: bool = True, inform: str = "a", outform: str = "a",
@@ -220,19 +220,20 @@ def _rtrace(rays: bytes, octree, header: bool = True, inform: str = "a", outform
         vals[good] = gv
     hit[good] = gh
     hitt[good] = gt
-    nrm_geo = nrm_shade = None
-    if any(ch in "nN" for ch in spec):           # first-hit normals (rt/rtrace.c:787-820 oputN, oputn)
-        nrm_geo, nrm_shade = np.zeros((n, 3)), np.zeros((n, 3))
-        gN, gn = np.zeros((ng, 3)), np.zeros((ng, 3))
+    nrm_geo = nrm_shade = uvs = None
+    if any(ch in "nNc" for ch in spec):          # first-hit normals and (u,v) (rt/rtrace.c:766-820)
+        nrm_geo, nrm_shade, uvs = np.zeros((n, 3)), np.zeros((n, 3)), np.zeros((n, 2))
+        gN, gn, guv = np.zeros((ng, 3)), np.zeros((ng, 3)), np.zeros((ng, 2))
         gh2, gt2 = np.zeros(ng, dtype=np.int32), np.zeros(ng)
         if ng:
-            check(lib().gb_rtrace_hits(sc.handle, opts, ptr(rr), ng, ptr(gh2), ptr(gt2), ptr(gN), ptr(gn)))
-        nrm_geo[good], nrm_shade[good] = gN, gn
+            check(lib().gb_rtrace_hits(sc.handle, opts, ptr(rr), ng, ptr(gh2), ptr(gt2), ptr(gN), ptr(gn),
+                                       ptr(guv)))
+        nrm_geo[good], nrm_shade[good], uvs[good] = gN, gn, guv
     out = []
     ncomp = 0                                    # rt/rtrace.c:244-370 setrtoutput
     for ch in spec:
         ncomp += {"v": 3, "V": 3, "W": 3, "o": 3, "d": 3, "p": 3, "N": 3, "n": 3, "L": 1, "l": 1, "w": 1,
-                  "s": 1, "m": 1, "M": 1}.get(ch, 0)
+                  "s": 1, "m": 1, "M": 1, "c": 2}.get(ch, 0)
     if opts.h:
         out.append(_header("rtrace", args, octree, fout, ncomp or None))
     unit = np.where(good[:, None], r[:, 3:6] / np.where(dirlen > 0, dirlen, 1)[:, None], 0.0) if n else r[:, 3:6]
@@ -270,6 +271,8 @@ def _rtrace(rays: bytes, octree, header: bool = True, inform: str = "a", outform
             items.append(nrm_geo)
         elif ch == "n":
             items.append(nrm_shade)
+        elif ch == "c":
+            items.append(uvs)
         else:
             raise GbError(-3, f"output option -o{ch} is not supported")
     if fout == "a":

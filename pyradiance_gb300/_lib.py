@@ -70,7 +70,7 @@ _SIGS = {
     "gb_rtrace": (C.c_int, [C.c_void_p, C.POINTER(GbOpts), C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p,
                             C.c_void_p]),
     "gb_rtrace_hits": (C.c_int, [C.c_void_p, C.POINTER(GbOpts), C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p,
-                                 C.c_void_p, C.c_void_p]),
+                                 C.c_void_p, C.c_void_p, C.c_void_p]),
     "gb_rtrace_device_noalloc": (C.c_int, [C.c_void_p, C.POINTER(GbOpts), C.c_void_p, C.c_int64, C.c_void_p,
                                             C.c_void_p]),
     "gb_rtrace_grad": (C.c_int, [C.c_void_p, C.POINTER(GbOpts), C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p,

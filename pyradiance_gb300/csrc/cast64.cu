@@ -44,6 +44,7 @@ struct Ray64 {
     int ro;              /* its object, -1 none */
     double rop[3], ron[3], rod;
     double vn[3];        /* a smooth mesh hit: its interpolated vertex normal, unit, in the scene; else 0 */
+    double uv[2];        /* a mesh hit with vertex (u,v): them interpolated; else 0 */
 };
 
 __device__ __forceinline__ double dot64(const double *a, const double *b)
@@ -144,7 +145,7 @@ __device__ int o_face64(const gb_dscene &S, int o, Ray64 &r)
     if (!inface64(p, (int)g[6], (int)g[5], g + 7))
         return 0;
     r.ro = o;
-    r.vn[0] = r.vn[1] = r.vn[2] = 0.0;
+    r.vn[0] = r.vn[1] = r.vn[2] = r.uv[0] = r.uv[1] = 0.0;
     r.rot = t;
     for (int i = 0; i < 3; i++) {
         r.rop[i] = p[i];
@@ -204,7 +205,7 @@ __device__ int o_sphere64(const gb_dscene &S, int o, bool bubble, Ray64 &r)
     if (rayreject64(S, o, r, t, (double)(1 - 2 * ((i > 0) ^ bubble))))
         return 0;
     r.ro = o;
-    r.vn[0] = r.vn[1] = r.vn[2] = 0.0;
+    r.vn[0] = r.vn[1] = r.vn[2] = r.uv[0] = r.uv[1] = 0.0;
     r.rot = t;
     const double rad = ap[3] * (1 - 2 * (int)bubble);
     for (i = 0; i < 3; i++) {
@@ -256,7 +257,7 @@ __device__ int o_cone64(const gb_dscene &S, int o, int kind, Ray64 &r)
         if (a > r1 * r1 || a < r0 * r0)
             return 0;
         r.ro = o;
-        r.vn[0] = r.vn[1] = r.vn[2] = 0.0;
+        r.vn[0] = r.vn[1] = r.vn[2] = r.uv[0] = r.uv[1] = 0.0;
         r.rot = root[0];
         for (i = 0; i < 3; i++) {
             r.rop[i] = r.org[i] + r.dir[i] * r.rot;
@@ -291,7 +292,7 @@ __device__ int o_cone64(const gb_dscene &S, int o, int kind, Ray64 &r)
         if (rayreject64(S, o, r, root[rn], (double)(1 - 2 * ((rn > 0) ^ (kind == DK_CUP || kind == DK_TUBE)))))
             break;
         r.ro = o;
-        r.vn[0] = r.vn[1] = r.vn[2] = 0.0;
+        r.vn[0] = r.vn[1] = r.vn[2] = r.uv[0] = r.uv[1] = 0.0;
         r.rot = root[rn];
         for (i = 0; i < 3; i++)
             r.rop[i] = p[i];
@@ -368,17 +369,19 @@ struct Checked {
 template <bool INST>
 __device__ bool walk64(const gb_dscene &S, Ray64 &r, const double cuorg[3], double cusize, int root);
 
-/* rt/o_mesh.c:185-206: the vertex normals of smooth mesh triangle o
- * (after its face record) interpolated at the hit point p (mesh
- * coordinates) by its barycentric weights (common/tmesh.c get_baryc: in the
- * plane of the triangle's largest projection), carried to the scene by the
- * forward transform fx (its rotation and scale rows) and normalised; vn is
- * left 0 for a degenerate triangle or a zero normal */
-__device__ void mesh_vnormal64(const gb_dscene &S, int o, const double p[3], const double *fx, double vn[3])
+/* rt/o_mesh.c:185-221: the attributes of mesh triangle o at the hit point
+ * p (mesh coordinates), interpolated by its barycentric weights (common/
+ * tmesh.c get_baryc: in the plane of the triangle's largest projection):
+ * the vertex normals (after its face record) carried to the scene by the
+ * forward transform fx (its rotation and scale rows) and normalised, into
+ * vn; the vertex (u,v) (after the normals), untransformed, into uv.  A
+ * degenerate triangle or a zero normal leaves them 0. */
+__device__ void mesh_attrs64(const gb_dscene &S, int o, int fl, const double p[3], const double *fx, double vn[3],
+                             double uv[2])
 {
     const double *g = rec64(S, o);
     const int nv = (int)g[6];
-    const double *v = g + 7, *nn = g + 7 + 3 * nv;
+    const double *v = g + 7, *x = g + 7 + 3 * nv;
     double e1[3], e2[3], cr[3];
     for (int i = 0; i < 3; i++) {
         e1[i] = v[i] - v[3 + i];
@@ -399,16 +402,21 @@ __device__ void mesh_vnormal64(const gb_dscene &S, int o, const double p[3], con
     const double w1 = (px * (y2 - y0) - (x2 - x0) * py) / den;
     const double w2 = ((x1 - x0) * py - px * (y1 - y0)) / den;
     const double w0 = 1.0 - w1 - w2;
-    double m[3], w[3];
-    for (int i = 0; i < 3; i++)
-        m[i] = w0 * nn[i] + w1 * nn[3 + i] + w2 * nn[6 + i];
-    for (int j = 0; j < 3; j++)
-        w[j] = m[0] * fx[0 * 4 + j] + m[1] * fx[1 * 4 + j] + m[2] * fx[2 * 4 + j];
-    const double l = sqrt(dot64(w, w));
-    if (l == 0.0)
-        return;
-    for (int j = 0; j < 3; j++)
-        vn[j] = w[j] / l;
+    if (fl & DF_VNORM) {
+        double m[3], w[3];
+        for (int i = 0; i < 3; i++)
+            m[i] = w0 * x[i] + w1 * x[3 + i] + w2 * x[6 + i];
+        for (int j = 0; j < 3; j++)
+            w[j] = m[0] * fx[0 * 4 + j] + m[1] * fx[1 * 4 + j] + m[2] * fx[2 * 4 + j];
+        const double l = sqrt(dot64(w, w));
+        if (l != 0.0)
+            for (int j = 0; j < 3; j++)
+                vn[j] = w[j] / l;
+        x += 9;
+    }
+    if (fl & DF_VUV)
+        for (int i = 0; i < 2; i++)
+            uv[i] = w0 * x[i] + w1 * x[2 + i] + w2 * x[4 + i];
 }
 
 /* rt/o_instance.c:15-71; record: backward transform (16), scale, forward
@@ -439,9 +447,9 @@ __device__ int o_instance64(const gb_dscene &S, int o, Ray64 &r)
         return 0;
     r.ro = g[39] != 0.0 ? o : rc.ro;
     r.rot = rc.rot * fsca;
-    r.vn[0] = r.vn[1] = r.vn[2] = 0.0;
-    if (rc.ro >= 0 && ((S.obj[rc.ro].x >> 8) & DF_VNORM))
-        mesh_vnormal64(S, rc.ro, rc.rop, fx, r.vn);
+    r.vn[0] = r.vn[1] = r.vn[2] = r.uv[0] = r.uv[1] = 0.0;
+    if (rc.ro >= 0 && ((S.obj[rc.ro].x >> 8) & (DF_VNORM | DF_VUV)))
+        mesh_attrs64(S, rc.ro, S.obj[rc.ro].x >> 8, rc.rop, fx, r.vn, r.uv);
     for (j = 0; j < 3; j++) {
         r.rop[j] = rc.rop[0] * fx[0 * 4 + j] + rc.rop[1] * fx[1 * 4 + j] + rc.rop[2] * fx[2 * 4 + j];
         r.ron[j] = rc.ron[0] * fx[0 * 4 + j] + rc.ron[1] * fx[1 * 4 + j] + rc.ron[2] * fx[2 * 4 + j];
@@ -699,7 +707,7 @@ __global__ void k_cast64(gb_run P, int *hit_obj, float *hit_t, double *hit_pn)
         r.ro = -1;
         r.rot = FHUGE64;
         r.rod = 1.0;
-        r.vn[0] = r.vn[1] = r.vn[2] = 0.0;
+        r.vn[0] = r.vn[1] = r.vn[2] = r.uv[0] = r.uv[1] = 0.0;
         int obj = -1;
         double t = FHUGE64;
         double p[3] = {0, 0, 0}, n[3] = {0, 0, 0};
@@ -720,12 +728,14 @@ __global__ void k_cast64(gb_run P, int *hit_obj, float *hit_t, double *hit_pn)
         if (hit_t)
             hit_t[s] = (float)t;
         if (hit_pn) {
-            double *o = hit_pn + 9 * s;
+            double *o = hit_pn + 11 * s;
             for (int i = 0; i < 3; i++) {
                 o[i] = p[i];
                 o[3 + i] = n[i];
                 o[6 + i] = obj >= 0 ? r.vn[i] : 0.0;
             }
+            o[9] = obj >= 0 ? r.uv[0] : 0.0;
+            o[10] = obj >= 0 ? r.uv[1] : 0.0;
         }
     }
 }

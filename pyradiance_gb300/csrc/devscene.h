@@ -62,6 +62,7 @@ enum { DK_NONE = 0, DK_FACE, DK_SPHERE, DK_BUBBLE, DK_CONE, DK_CUP, DK_CYL, DK_T
 #define DF_TRANSP  0x02   /* material is nominally transparent */
 #define DF_AXSHIFT 2      /* bits 2-3: dominant normal axis of a face */
 #define DF_VNORM   0x10   /* a mesh triangle with vertex normals (vnidx, vnrm) */
+#define DF_VUV     0x20   /* a mesh triangle with (u,v) at its vertices (after its FP64 record) */
 
 /* full-leaf code: -2 - (offset << 6 | min(size, 63)); a size field of 63
  * means "63 or more: read the count word" */

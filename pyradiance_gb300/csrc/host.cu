@@ -573,6 +573,8 @@ static int build_arrays(gb_scene *G)
             flags |= f->ax << DF_AXSHIFT;
             if (o->vnorm && nv == 3)
                 flags |= DF_VNORM;
+            if (o->vuv && nv == 3)
+                flags |= DF_VUV;
             geo[i] = make_float4((float)f->norm[0], (float)f->norm[1], (float)f->norm[2], (float)f->offset);
             aux = (int)fvert.size();
             int xi = (f->ax + 1) % 3, yi = (xi + 1) % 3;
@@ -849,6 +851,8 @@ static int build_arrays(gb_scene *G)
                 for (int j = 0; j < 3 * f->nv; j++) g64.push_back(o->farg[j]);
                 if ((obj[i].x >> 8) & DF_VNORM)          /* then its three vertex normals */
                     for (int j = 0; j < 9; j++) g64.push_back(o->vnorm[j]);
+                if ((obj[i].x >> 8) & DF_VUV)            /* and their (u,v) */
+                    for (int j = 0; j < 6; j++) g64.push_back(o->vuv[j]);
             } else if (kind == DK_SPHERE || kind == DK_BUBBLE) {
                 for (int j = 0; j < 4; j++) g64.push_back(o->farg[j]);
             } else if (kind == DK_CONE || kind == DK_CUP || kind == DK_CYL || kind == DK_TUBE || kind == DK_RING) {
@@ -1403,6 +1407,7 @@ struct RunOut {
     double *grad;           /* gradient runs: host nslots x 3 */
     double *hit_normal;     /* host n x 3 or null: the first hit's surface normal */
     double *hit_vnormal;    /* host n x 3 or null: a smooth mesh hit's interpolated vertex normal (else 0) */
+    double *hit_uv;         /* host n x 2 or null: a mesh hit's interpolated vertex (u,v) (else 0) */
 };
 
 /* largest generation and queue capacity of the last run on this thread */
@@ -1489,7 +1494,7 @@ static int run(gb_scene *G, const gb_opts *o, int follow, const double *org_dir,
         if (G->hits.ensure((size_t)n * sizeof(int)) < 0 || G->hitt.ensure((size_t)n * sizeof(float)) < 0)
             return set_err(GB_ENOMEM, "device allocation failed");
         P.S.trk = nullptr;
-        if (out.hit_normal && G->hitpn.ensure((size_t)n * 9 * sizeof(double)) < 0)
+        if (out.hit_normal && G->hitpn.ensure((size_t)n * 11 * sizeof(double)) < 0)
             return set_err(GB_ENOMEM, "device allocation failed");
         double *d_pn = out.hit_normal ? (double *)G->hitpn.p : nullptr;
         int rc = launch(GB_K_CAST, P, [&](gb_run &R) {
@@ -1499,7 +1504,7 @@ static int run(gb_scene *G, const gb_opts *o, int follow, const double *org_dir,
         /* the first hits come back through pinned staging, unpacked after
          * the values' final synchronisation when values follow, so that the
          * host does not wait for the casts before it queues the values */
-        const size_t hb = (size_t)n * (sizeof(int) + sizeof(float)) + (d_pn ? (size_t)n * 9 * sizeof(double) : 0);
+        const size_t hb = (size_t)n * (sizeof(int) + sizeof(float)) + (d_pn ? (size_t)n * 11 * sizeof(double) : 0);
         if (G->pin_n < hb) {
             if (G->pin)
                 cudaFreeHost(G->pin);
@@ -1513,12 +1518,12 @@ static int run(gb_scene *G, const gb_opts *o, int follow, const double *org_dir,
             G->pin_n = hb;
         }
         double *pn = (double *)G->pin;
-        int *h = (int *)(pn + (d_pn ? (size_t)n * 9 : 0));
+        int *h = (int *)(pn + (d_pn ? (size_t)n * 11 : 0));
         float *t = (float *)(h + n);
         CK(cudaMemcpyAsync(h, G->hits.p, (size_t)n * sizeof(int), cudaMemcpyDeviceToHost, st));
         CK(cudaMemcpyAsync(t, G->hitt.p, (size_t)n * sizeof(float), cudaMemcpyDeviceToHost, st));
         if (d_pn)
-            CK(cudaMemcpyAsync(pn, d_pn, (size_t)n * 9 * sizeof(double), cudaMemcpyDeviceToHost, st));
+            CK(cudaMemcpyAsync(pn, d_pn, (size_t)n * 11 * sizeof(double), cudaMemcpyDeviceToHost, st));
         unpack_hits = [&out, n, h, t, pn]() {
             for (int64_t i = 0; i < n; i++) {
                 out.hit_id[i] = h[i];
@@ -1526,10 +1531,13 @@ static int run(gb_scene *G, const gb_opts *o, int follow, const double *org_dir,
                     out.hit_t[i] = t[i];
                 if (out.hit_normal)
                     for (int k = 0; k < 3; k++)
-                        out.hit_normal[3 * i + k] = pn[9 * i + 3 + k];
+                        out.hit_normal[3 * i + k] = pn[11 * i + 3 + k];
                 if (out.hit_vnormal)
                     for (int k = 0; k < 3; k++)
-                        out.hit_vnormal[3 * i + k] = pn[9 * i + 6 + k];
+                        out.hit_vnormal[3 * i + k] = pn[11 * i + 6 + k];
+                if (out.hit_uv)
+                    for (int k = 0; k < 2; k++)
+                        out.hit_uv[2 * i + k] = pn[11 * i + 9 + k];
             }
         };
         if (!out.value && !out.bins) {
@@ -1945,12 +1953,13 @@ extern "C" int gb_rtrace(gb_scene *G, const gb_opts *o, const double *org_dir, i
 }
 
 extern "C" int gb_rtrace_hits(gb_scene *G, const gb_opts *o, const double *org_dir, int64_t n, int32_t *hit_id,
-                              double *hit_t, double *hit_normal, double *hit_pnormal)
+                              double *hit_t, double *hit_normal, double *hit_pnormal, double *hit_uv)
 {
     if (!G || !o || (n > 0 && (!org_dir || !hit_id || !hit_normal)))
         return set_err(GB_EINVAL, "null argument");
     std::vector<double> vn(hit_pnormal && G->has_vnorm ? (size_t)n * 3 : 0);
-    RunOut out = {nullptr, nullptr, hit_id, hit_t, nullptr, nullptr, hit_normal, vn.empty() ? nullptr : vn.data()};
+    RunOut out = {nullptr, nullptr, hit_id, hit_t, nullptr, nullptr, hit_normal, vn.empty() ? nullptr : vn.data(),
+                  hit_uv};
     int rc = run_sliced(G, o, 0, org_dir, n, nullptr, nullptr, 0, nullptr, out, 0.0);
     if (rc < 0 || !hit_pnormal)
         return rc;

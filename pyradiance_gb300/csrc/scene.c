@@ -111,6 +111,7 @@ void gb_scene_clear(gb_scene_host *S)
         free(o->sarg);
         free(o->farg);
         free(o->vnorm);
+        free(o->vuv);
     }
     free(S->objs);
     free(S->kids);
@@ -1152,6 +1153,7 @@ static int merge_subscene(gb_scene_host *S, gb_scene_host *T, const char *name)
 typedef struct {
     uint32_t (*xyz)[3];
     int32_t *norm;               /* encoded vertex normals (0: none), or NULL */
+    uint32_t (*uv)[2];           /* encoded vertex (u,v) (first 0: none), or NULL */
     int nverts, ntris, nj1, nj2;
     unsigned char (*tri)[3];
     int16_t *trimat, solemat;
@@ -1167,6 +1169,7 @@ static void mpatch_free(mpatch *pp, int n)
     for (i = 0; i < n; i++) {
         free(pp[i].xyz);
         free(pp[i].norm);
+        free(pp[i].uv);
         free(pp[i].tri);
         free(pp[i].trimat);
         free(pp[i].j1v);
@@ -1199,9 +1202,14 @@ static int read_patch(rdr *R, mpatch *pp, const char *path)
         for (i = 0; i < pp->nverts; i++)
             pp->norm[i] = (int32_t)r_int(R, 4, &ok);
     }
-    if (flags & 4)                               /* (u,v): read past, unused */
-        for (i = 0; i < 2 * pp->nverts; i++)
-            r_int(R, 4, &ok);
+    if (flags & 4) {                             /* vertex (u,v), 32-bit codes in the mesh's limits */
+        pp->uv = (uint32_t(*)[2])malloc((size_t)pp->nverts * sizeof *pp->uv);
+        if (!pp->uv)
+            return fail("out of memory");
+        for (i = 0; i < pp->nverts; i++)
+            for (j = 0; j < 2; j++)
+                pp->uv[i][j] = (uint32_t)r_int(R, 4, &ok);
+    }
     pp->ntris = (int)r_int(R, 2, &ok);
     if (!ok || pp->ntris < 0 || pp->ntris > 512)
         return fail("(%s): bad number of local triangles", path);
@@ -1299,6 +1307,18 @@ static int mesh_normal(const mpatch *pp, int npatches, int32_t vid, double *n)
     return 1;
 }
 
+/* vertex id -> its (u,v); 0 when the vertex has none (common/mesh.c:
+ * 268-275: the codes' cells' centres within the mesh's (u,v) limits) */
+static int mesh_uv(const mpatch *pp, int npatches, const double lim[2][2], int32_t vid, double *uv)
+{
+    int pn = vid >> 8, k = vid & 0xff, i;
+    if (vid < 0 || pn >= npatches || k >= pp[pn].nverts || !pp[pn].uv || !pp[pn].uv[k][0])
+        return 0;
+    for (i = 0; i < 2; i++)
+        uv[i] = lim[0][i] + (lim[1][i] - lim[0][i]) * (pp[pn].uv[k][i] + .5) * (1. / 4294967296.);
+    return 1;
+}
+
 /* vertex id (patch << 8 | index) -> position (common/mesh.c:236-279
  * getmeshvert: the 32-bit cube coordinates at their cells' centres) */
 static int mesh_vertex(const mpatch *pp, int npatches, const double org[3], double size, int32_t vid, double *v)
@@ -1329,6 +1349,7 @@ static int read_mesh(gb_scene_host *T, const char *path, const char *mesh_name)
     int ok = 1, objsize, i, k, np = 0;
     mpatch *pp = NULL;
     int32_t *map = NULL, nmats, ntri = 0, t;
+    double uvlim[2][2] = {{0, 0}, {0, 0}};
     char line[256];
     int rc = -1;
     if (!buf)
@@ -1363,8 +1384,10 @@ static int read_mesh(gb_scene_host *T, const char *path, const char *mesh_name)
     for (i = 0; i < 3; i++)
         T->cuorg[i] = atof(r_str(&R, &ok));
     T->cusize = atof(r_str(&R, &ok));
-    for (i = 0; i < 4; i++)                      /* (u,v) limits */
-        r_flt(&R, &ok);
+    for (i = 0; i < 2; i++) {                    /* (u,v) limits: u min, u max, v min, v max */
+        uvlim[0][i] = r_flt(&R, &ok);
+        uvlim[1][i] = r_flt(&R, &ok);
+    }
     T->root = read_tree(T, &R, objsize, 0, &ok, 0);
     if (!ok) {
         fail("(%s): truncated or damaged mesh octree", path);
@@ -1453,6 +1476,18 @@ static int read_mesh(gb_scene_host *T, const char *path, const char *mesh_name)
                         goto done;
                     }
                     memcpy(o->vnorm, nv, sizeof nv);
+                }
+            }
+            {                                    /* (u,v) where all three vertices have them */
+                double uv[6];
+                if (mesh_uv(pp, np, uvlim, v[0], uv) && mesh_uv(pp, np, uvlim, v[1], uv + 2) &&
+                    mesh_uv(pp, np, uvlim, v[2], uv + 4)) {
+                    o->vuv = (double *)malloc(sizeof uv);
+                    if (!o->vuv) {
+                        fail("out of memory");
+                        goto done;
+                    }
+                    memcpy(o->vuv, uv, sizeof uv);
                 }
             }
             map[i * 1024 + t] = ntri++;

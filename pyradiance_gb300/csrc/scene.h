@@ -57,6 +57,8 @@ typedef struct {
     double  *vnorm;              /* mesh triangles with vertex normals: the three
                                     unit normals in the mesh's coordinates, in the
                                     order of the vertices in farg; else NULL */
+    double  *vuv;                /* mesh triangles with (u,v) at every vertex: the
+                                    three (u,v) pairs, vertex order; else NULL */
 } gb_object;
 
 /* face record: common/face.h + common/face.c:35-112 */

@@ -433,21 +433,25 @@ def instance_room(sub_octree: str, seed: int = 0, n: int = 12) -> str:
     return "".join(out)
 
 
-def mesh_obj(nu: int = 24, nv: int = 12, nsheet: int = 16, seed: int = 0, normals: bool = False) -> str:
+def mesh_obj(nu: int = 24, nv: int = 12, nsheet: int = 16, seed: int = 0, normals: bool = False,
+             uv: bool = False) -> str:
     """A Wavefront OBJ for obj2mesh, in its own coordinates around the
     origin: a UV sphere of radius 0.45 centred 0.45 above the origin
     (material ``mesh_red``) and a bumpy square sheet of side 1.2 at height
     0.9 .. 1.0 (``mesh_grey``), triangles only; with ``normals``, every
     vertex carries a normal (the sphere's radial direction, the sheet's
-    height-field normal by central differences) and the faces name them."""
+    height-field normal by central differences) and the faces name them;
+    with ``uv``, every vertex carries texture coordinates as well (the
+    sphere's longitude and latitude fractions, the sheet's position)."""
     rng = np.random.default_rng(seed)
-    V, N, out = [], [], []
+    V, N, T, out = [], [], [], []
     for j in range(nv + 1):
         th = np.pi * j / nv
         for i in range(nu):
             ph = 2 * np.pi * i / nu
             V.append((0.45 * np.sin(th) * np.cos(ph), 0.45 * np.sin(th) * np.sin(ph), 0.45 + 0.45 * np.cos(th)))
             N.append((np.sin(th) * np.cos(ph), np.sin(th) * np.sin(ph), np.cos(th)))
+            T.append((i / nu, j / nv))
     out.append("usemtl mesh_red")
     for j in range(nv):
         for i in range(nu):
@@ -465,6 +469,7 @@ def mesh_obj(nu: int = 24, nv: int = 12, nsheet: int = 16, seed: int = 0, normal
             V.append((-0.6 + 1.2 * i / nsheet, -0.6 + 1.2 * j / nsheet, h[j, i]))
             n = np.array([-gx[j, i], -gy[j, i], 1.0])
             N.append(tuple(n / np.linalg.norm(n)))
+            T.append((i / nsheet, j / nsheet))
     out.append("usemtl mesh_grey")
     for j in range(nsheet):
         for i in range(nsheet):
@@ -474,7 +479,11 @@ def mesh_obj(nu: int = 24, nv: int = 12, nsheet: int = 16, seed: int = 0, normal
     text = "".join(f"v {x:.7f} {y:.7f} {z:.7f}\n" for x, y, z in V)
     if normals:
         text += "".join(f"vn {x:.7f} {y:.7f} {z:.7f}\n" for x, y, z in N)
-        out = [" ".join([t[0]] + [f"{k}//{k}" for k in t[1:]]) if t[0] == "f" else " ".join(t)
+    if uv:
+        text += "".join(f"vt {u:.7f} {v:.7f}\n" for u, v in T)
+    if normals or uv:
+        form = "{k}/{k}/{k}" if normals and uv else "{k}//{k}" if normals else "{k}/{k}"
+        out = [" ".join([t[0]] + [form.format(k=k) for k in t[1:]]) if t[0] == "f" else " ".join(t)
                for t in (ln.split() for ln in out)]
     return text + "\n".join(out) + "\n"
 

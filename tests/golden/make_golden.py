@@ -549,16 +549,25 @@ def smooth_meshes(tmp: Path, nstat: int = 24, K: int = 256) -> None:
     out = run_independent(["rcontrib", "-h", "-u+", "-ab", "1", "-ad", "256", "-lw", "1e-4", "-fdd", "-m", "light_mat",
                            octn], np.repeat(srays, K, axis=0), cwd=tmp)
     a = np.frombuffer(out, dtype="<f8").reshape(len(srays), K, 3)
+    # the mesh with texture coordinates too: -oc (rt/rtrace.c:766-772) and -on of every ray
+    (tmp / "mesh_uv.obj").write_text(w.mesh_obj(normals=True, uv=True))
+    run(["obj2mesh", "-a", "mesh_mat.rad", "mesh_uv.obj", "mesh_uv.rtm"], b"", cwd=tmp)
+    (tmp / "mesh_uv_room.rad").write_text(w.mesh_room("mesh_uv.rtm", seed=1))
+    (tmp / "mesh_uv_room.oct").write_bytes(run(["oconv", "-f", "mesh_uv_room.rad"], b"", cwd=tmp))
+    cn = np.frombuffer(run(["rtrace", "-h", "-u-", "-ab", "0", "-fdd", "-ocn", "mesh_uv_room.oct"], inp, cwd=tmp),
+                       dtype="<f8").reshape(-1, 5)
     # the same mesh under a glass of its own (refused: glass is not shaded through vertex normals here)
     (tmp / "mesh_smooth_glass.rad").write_text("void glass smooth_glass\n0\n0\n3 0.9 0.9 0.9\n\n"
                                                "smooth_glass mesh glassy\n1 mesh_smooth.rtm\n0\n0\n")
     (tmp / "mesh_smooth_glass.oct").write_bytes(run(["oconv", "-f", "mesh_smooth_glass.rad"], b"", cwd=tmp))
-    for f in ("mesh_smooth.rtm", "mesh_smooth_room.oct", "mesh_smooth_glass.oct"):
+    for f in ("mesh_smooth.rtm", "mesh_smooth_room.oct", "mesh_smooth_glass.oct", "mesh_uv.rtm", "mesh_uv_room.oct"):
         (OUT / f).write_bytes((tmp / f).read_bytes())
     np.savez_compressed(OUT / "smooth_meshes.npz", rays=rays, hit_name=hit, hit_dist=dist, N=nn[:, :3], n=nn[:, 3:],
                         radiance=val, stat_rays=srays, K=K, mean=a.mean(1), se=a.std(1, ddof=1) / np.sqrt(K),
+                        uv_c=cn[:, :2], uv_n=cn[:, 2:],
                         cmd="rtrace -h -u- -ab 0 -os | -oL | -oNn | -dj 0 -ds 0 -dr 0 -dt 0 -st 1 -ov; "
-                            "rcontrib -h -u+ -ab 1 -ad 256 -lw 1e-4 -m light_mat (independent -n 1 processes)")
+                            "rcontrib -h -u+ -ab 1 -ad 256 -lw 1e-4 -m light_mat (independent -n 1 processes); "
+                            "mesh_uv_room: rtrace -h -u- -ab 0 -ocn")
     print("smooth meshes: %d of %d rays hit mesh triangles, %d with a perturbed normal; %d stat rays" % (
         onmesh.sum(), len(hit), smooth.sum(), len(srays)))
 

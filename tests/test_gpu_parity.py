@@ -675,7 +675,8 @@ def test_smooth_meshes(gb):
     shading normal, samples rejected below the surface): every ray's mean
     over K replicas within 4 combined standard errors of the reference's.
     rtrace with ambient bounces on these surfaces is refused (their ambient
-    texture factor is not formed), and so is a glass over them."""
+    texture factor is not formed), and so is a glass over them.  With
+    texture coordinates, -oc within 1e-6 of the reference's."""
     from pathlib import Path
     from pyradiance_gb300 import _lib
     g = golden("smooth_meshes.npz")
@@ -705,6 +706,14 @@ def test_smooth_meshes(gb):
     assert z.max() < 4.0 and z.mean() < 1.2, z
     with pytest.raises(_lib.GbError, match="vertex normals"):
         rtrace_c(gb, sc, opts("rtrace", ab=1, u=0), g["rays"][:8])
+    # texture coordinates too (rt/rtrace.c:766-772 -oc): the vertex (u,v) interpolated at the hit, FP64 casts
+    uvsc = gb.Scene(str(Path(__file__).resolve().parent / "golden" / "mesh_uv_room.oct"))
+    out = gb.rtrace(g["rays"].astype("<f8").tobytes(), uvsc, params=["-ab", "0"], inform="d", outform="d",
+                    outspec="cn", header=False)
+    v = np.frombuffer(out, dtype="<f8").reshape(-1, 5)
+    assert (np.abs(g["uv_c"]).sum(1) > 0).sum() > 300
+    np.testing.assert_allclose(v[:, :2], g["uv_c"], rtol=1e-6, atol=1e-6)
+    np.testing.assert_allclose(v[:, 2:], g["uv_n"], rtol=1e-6, atol=1e-6)
     glassy = gb.Scene(str(Path(__file__).resolve().parent / "golden" / "mesh_smooth_glass.oct"))
     with pytest.raises(_lib.GbError, match="vertex normals"):
         rtrace_c(gb, glassy, opts("rtrace", ab=0, u=0), g["rays"][:8])
